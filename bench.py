@@ -1,0 +1,401 @@
+#!/usr/bin/env python
+"""Benchmark of the Hess-diagram hot path on one GB300 (replicas on N GPUs).
+
+Workload (the production-size configuration): 1,200 templates (40 log-ages 6.6-10.1 x
+30 [M/H] -2.5..0.3) built on the GPU by partial_cmd_smooth (V vs B-V, covariant kernel)
+on a 200 x 300 Hess grid, stored FP32; one observed diagram holding 1e6 stars.
+
+A step is one fg! evaluation (composite!, loglikelihood, ∇loglikelihood!) of one
+coefficient vector against the 60,000 x 1,200 template matrix.  The matrix (288 MB)
+is larger than L2 (129 MB), so no flush is needed between steps.
+
+  value : evals/s with inputs resident in HBM (sfh_fg_dev), CUDA events on the context stream
+  e2e   : evals/s through the host-array C ABI (sfh_fg): coefficients and data copied in,
+          composite, gradient and -logL copied out, every step
+  templates_per_s : the 1,200-template GPU build (partial_cmd_smooth), CUDA events
+
+`--impl reference` times the FP64 CPU restatement of the reference's fg! (the oracle)
+on all host cores, same metric and configuration.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "starformationhistories.jl_gb300")
+for _p in (PKG, os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "logL+grad evals/s (fg!, one coefficient vector, 1200 templates x 60000 bins)"
+UNIT = "evals/s"
+WORKLOAD = "config2: 1200 templates, 200x300 Hess grid, 1e6 stars"
+NBINS, NT = 60000, 1200
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:  # noqa: BLE001
+        return 6800.0, "fallback"
+
+
+def _profile_traffic(kernel: str):
+    """dram bytes per launch of `kernel` from the committed ncu summary, else None."""
+    path = os.path.join(ROOT, "profiles", "fg_kernels_config2.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith(f"dram_bytes_per_launch {kernel}:"):
+                    return float(line.split(":", 1)[1].strip().split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (200 ms period)."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        self.f.close()
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+                for k, nm in enumerate(names):
+                    if r[5 + k].strip().lower().startswith("active"):
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(world, x: float) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_fg_baseline(M64, r, data, budget_s=10.0, threads=None):
+    """The oracle's fg! (FP64, OpenMP over bins/templates) on a bounded number of evals."""
+    import numpy as np
+    import oracle as O
+    threads = threads or os.cpu_count() or 1
+    O.set_threads(threads)
+    O.fg(r, M64, data)  # warm
+    t0 = time.perf_counter()
+    O.fg(r, M64, data)
+    one = time.perf_counter() - t0
+    n = max(2, min(500, int(budget_s / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    for _ in range(n):
+        O.fg(r, M64, data)
+    dt = time.perf_counter() - t0
+    del np
+    return n / dt, threads, n, dt
+
+
+def cpu_template_baseline(w, budget_s=8.0):
+    """The oracle's partial_cmd_smooth (FP64, one thread) on a sample of templates."""
+    import oracle as O
+    from sfhgpu import synthetic as S
+    m_ini, mags, offs, lens = S.isochrone_batch(w)
+    nx, ny = w.grid
+    oimf = O.kroupa2001()
+    E = [O.ErrModel(e.a, e.b, e.c, e.d, e.cap) for e in S.error_models()]
+    Cm = [O.ComplModel(c.A, c.m50, c.rho) for c in S.completeness_models()]
+    ex = (w.xedges[0], (w.xedges[-1] - w.xedges[0]) / nx, nx)
+    ey = (w.yedges[0], (w.yedges[-1] - w.yedges[0]) / ny, ny)
+    # sample templates spread over the grid of ages/metallicities
+    order = list(range(0, w.ntempl, max(1, w.ntempl // 16)))
+    done, t0 = 0, time.perf_counter()
+    for t in order:
+        sl = slice(offs[t], offs[t] + lens[t])
+        O.partial_cmd_smooth(m_ini[sl], mags[:, sl], E, Cm, 1, (0, 1), oimf, w.dmod, 1.0,
+                             O.imf_mean(oimf), ex, ey)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return done / dt, done, dt
+
+
+def run_reference(args):
+    """`--impl reference`: the FP64 CPU restatement (oracle) of fg! on all host cores."""
+    import numpy as np
+    world, rank, _ = _dist()
+    if rank != 0:
+        return
+    rng = np.random.default_rng(20261203)
+    # fg! time does not depend on template values (dense FP64 gemv + gemvᵀ): a seeded
+    # matrix of the workload's shape stands in for the 1,200 GPU-built templates.
+    M64 = np.asfortranarray(rng.random((NBINS, NT)) * 1e-4)
+    r = np.exp(rng.standard_normal(NT))
+    r *= 1e6 / (M64 @ r).sum()
+    data = rng.poisson(M64 @ r).astype(np.float64)
+    import oracle as O
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    for _ in range(max(1, args.warmup)):
+        O.fg(r, M64, data)
+    steps = max(1, args.steps)
+    t0 = time.perf_counter()
+    one = None
+    done = 0
+    for i in range(steps):
+        O.fg(r, M64, data)
+        done += 1
+        if i == 0:
+            one = time.perf_counter() - t0
+        if time.perf_counter() - t0 > args.reference_budget_s:
+            break
+    dt = time.perf_counter() - t0
+    v = done / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": done, "warmup": args.warmup, "ms_per_step": 1e3 * dt / done,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "nbins": NBINS, "ntempl": NT},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{done} fg! evals (bounded to ~{args.reference_budget_s:.0f} s;"
+                                   f" first eval {1e3 * (one or 0):.1f} ms)"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import sfhgpu
+    from sfhgpu import synthetic as S
+
+    world, rank, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    ctx = sfhgpu.Context(local)
+    L = sfhgpu.load()
+    tstream = ctx.torch_stream()
+    w = S.config2()
+    nx, ny = w.grid
+
+    # ---- template build (partial_cmd_smooth on the GPU), templates/s
+    m_ini, mags, offs, lens = S.isochrone_batch(w)
+    d_m = torch.tensor(m_ini, device=dev)
+    d_mags = torch.tensor(mags, device=dev)
+    torch.cuda.synchronize()
+    d_T = torch.empty((w.ntempl, nx * ny), dtype=torch.float32, device=dev)
+
+    def build():
+        sfhgpu.partial_cmd_smooth_batch(d_m, d_mags, offs, lens, 1, (0, 1), S.error_models(),
+                                        S.completeness_models(), S.imf(), w.dmod, 1.0,
+                                        (w.xedges, w.yedges), out=d_T, ctx=ctx)
+
+    build()  # warm-up (also allocates scratch)
+    nbuild = 3
+    with torch.cuda.stream(tstream):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(tstream)
+        for _ in range(nbuild):
+            build()
+        e1.record(tstream)
+    e1.synchronize()
+    build_ms = e0.elapsed_time(e1) / nbuild
+    templates_per_s = w.ntempl / (build_ms / 1e3)
+
+    # ---- template matrix handle (FP32 storage) and observed data
+    H = sfhgpu.Models.from_device(d_T.data_ptr(), NBINS, NT, storage="f32", ctx=ctx)
+    M32 = d_T.cpu().numpy()          # (nt, nbins) row-major == (nbins, nt) column-major
+    M64 = np.asfortranarray(M32.T.astype(np.float64))
+    r, data = S.observed(M64, w.n_stars, seed=w.seed)
+    d_r = torch.tensor(r, device=dev)
+    d_n = torch.tensor(data, device=dev)
+    d_c = torch.empty(NBINS, dtype=torch.float64, device=dev)
+    d_G = torch.empty(NT, dtype=torch.float64, device=dev)
+    d_L = torch.empty(1, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    eps = float(np.finfo(np.float64).eps)
+
+    def step():
+        rc = L.sfh_fg_dev(ctx.handle, H.handle, d_r.data_ptr(), d_n.data_ptr(), d_c.data_ptr(),
+                          d_G.data_ptr(), d_L.data_ptr(), eps)
+        if rc:
+            sfhgpu._lib.check(rc, ctx.handle, "sfh_fg_dev")
+
+    for _ in range(args.warmup):
+        step()
+    ctx.synchronize()
+    clocks = Clocks(local)
+    _barrier(world)
+    torch.cuda.synchronize()
+    launches0 = ctx.launches
+    clocks.start()
+    time.sleep(0.25)  # let the sampler take its first reading under load
+    with torch.cuda.stream(tstream):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(tstream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(tstream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    _barrier(world)
+    launches = ctx.launches - launches0
+    ms = ev0.elapsed_time(ev1)
+    ms = _max_over_ranks(world, ms)
+    value = world * args.steps / (ms / 1e3)
+    neglogl = float(d_L.item())
+
+    # ---- per-kernel times (CUDA events) for the roofline of the dominant kernel
+    kms = (C.c_double * 4)()
+    sfhgpu._lib.check(L.sfh_fg_kernel_times(ctx.handle, H.handle, d_r.data_ptr(), d_n.data_ptr(),
+                                            d_c.data_ptr(), d_G.data_ptr(), d_L.data_ptr(), eps,
+                                            50, kms), ctx.handle, "sfh_fg_kernel_times")
+    names = ["k_gemv_n_f32", "k_finalize", "k_gemv_t_f32", "k_reduce_g"]
+    alg = [NBINS * NT * 4 + NT * 8 + NBINS * 8,      # M, r, m
+           NBINS * 8 * 3,                            # m, n, w
+           NBINS * NT * 4 + NBINS * 8 + NT * 8,      # M, w, G
+           NT * 8]
+    k = max(range(4), key=lambda i: kms[i])
+    peak, peak_kind = _peaks()
+    achieved = alg[k] / (kms[k] * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": names[k], "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "traffic": _profile_traffic(names[k]),
+                "peak_source": peak_kind,
+                "kernel_ms": {n: kms[i] for i, n in enumerate(names)},
+                "fg_total_gbs": (alg[0] + alg[2]) / (ms / args.steps * 1e-3) / 1e9}
+
+    # ---- end to end through the host-array C ABI (sfh_fg)
+    comp = np.empty(NBINS)
+    G = np.empty(NT)
+    h_r = r.copy()
+    h_n = data.copy()
+    for _ in range(3):
+        sfhgpu.fg_(True, G, h_r, H, h_n, comp)
+    ne2e = max(10, min(args.steps, 300))
+    _barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(ne2e):
+        sfhgpu.fg_(True, G, h_r, H, h_n, comp)
+    e2e_s = _max_over_ranks(world, time.perf_counter() - t0)
+    e2e = {"value": world * ne2e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": (NT + NBINS) * 8,
+           "d2h_bytes_per_step": (NBINS + NT + 1) * 8, "steps": ne2e}
+
+    # ---- CPU baseline (rank 0, N = 1 only): the oracle on the same inputs
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, thr, n, dt = cpu_fg_baseline(M64, r, data, budget_s=args.cpu_budget_s)
+        tps, nt_done, tdt = cpu_template_baseline(w, budget_s=args.cpu_budget_s)
+        cpu = {"value": v, "unit": UNIT, "cores": thr, "kind": "port",
+               "sample": f"{n} fg! evals in {dt:.1f} s (FP64 oracle, OpenMP {thr} threads)",
+               "templates_per_s": tps,
+               "templates_sample": f"{nt_done} partial_cmd_smooth templates in {tdt:.1f} s "
+                                   f"(FP64 oracle, 1 thread)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (compensated) + f64 logL",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "nbins": NBINS, "ntempl": NT, "storage": "f32",
+                       "l2": "inputs larger than L2 (288 MB template matrix)",
+                       "parallelism": f"replicas x{world}"},
+            "templates_per_s": templates_per_s, "template_build_ms": build_ms,
+            "negLogL": neglogl, "gpu_launches": launches, "roofline": roofline,
+            "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    H.free()
+    ctx.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--cpu-budget-s", type=float, default=10.0)
+    ap.add_argument("--reference-budget-s", type=float, default=60.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,408 @@
+// core.cu -- contexts, template-matrix handles, scratch, and the host-array
+// entry points of the C ABI (include/sfhgpu.h).
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "sfh_internal.cuh"
+
+// ------------------------------------------------------------------ errors
+int sfh_set_error(sfh_ctx *ctx, int code, const std::string &msg) {
+    if (ctx) ctx->last_error = msg;
+    return code;
+}
+
+int sfh_cuda_error(sfh_ctx *ctx, cudaError_t e, const char *what) {
+    std::string msg = std::string(what) + ": " + cudaGetErrorName(e) + " (" +
+                      cudaGetErrorString(e) + ")";
+    return sfh_set_error(ctx, e == cudaErrorMemoryAllocation ? SFH_ERR_NOMEM : SFH_ERR_CUDA, msg);
+}
+
+extern "C" int sfh_abi_version(void) { return SFH_ABI_VERSION; }
+
+extern "C" const char *sfh_status_string(int status) {
+    switch (status) {
+        case SFH_OK: return "ok";
+        case SFH_ERR_ARG: return "invalid argument";
+        case SFH_ERR_SHAPE: return "shape mismatch";
+        case SFH_ERR_CUDA: return "CUDA error";
+        case SFH_ERR_TIMEOUT: return "device wait timed out";
+        case SFH_ERR_NOMEM: return "device out of memory";
+        case SFH_ERR_UNSUPPORTED: return "unsupported device or configuration";
+        case SFH_ERR_NUMERIC: return "non-finite input";
+        default: return "unknown status";
+    }
+}
+
+// ------------------------------------------------------------------ context
+extern "C" int sfh_ctx_create(int device, sfh_ctx **out) {
+    if (!out) return SFH_ERR_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) return SFH_ERR_CUDA;
+    if (device < 0 || device >= ndev) return SFH_ERR_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return SFH_ERR_CUDA;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return SFH_ERR_CUDA;
+    // The library is compiled for sm_103a only (GB300).
+    if (!(prop.major == 10 && prop.minor == 3)) return SFH_ERR_UNSUPPORTED;
+    sfh_ctx *ctx = new sfh_ctx();
+    ctx->device = device;
+    ctx->sm_count = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&ctx->d_counters, sizeof(unsigned int) * SFH_CNT_SLOTS) != cudaSuccess ||
+        cudaMemset(ctx->d_counters, 0, sizeof(unsigned int) * SFH_CNT_SLOTS) != cudaSuccess) {
+        if (ctx->stream) cudaStreamDestroy(ctx->stream);
+        if (ctx->d_counters) cudaFree(ctx->d_counters);
+        delete ctx;
+        return SFH_ERR_CUDA;
+    }
+    *out = ctx;
+    return SFH_OK;
+}
+
+extern "C" int sfh_ctx_destroy(sfh_ctx *ctx) {
+    if (!ctx) return SFH_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->stage) cudaFree(ctx->stage);
+    if (ctx->d_counters) cudaFree(ctx->d_counters);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return SFH_OK;
+}
+
+extern "C" const char *sfh_ctx_last_error(const sfh_ctx *ctx) {
+    return ctx ? ctx->last_error.c_str() : "null context";
+}
+
+extern "C" int sfh_ctx_synchronize(sfh_ctx *ctx) {
+    if (!ctx) return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return SFH_OK;
+}
+
+extern "C" int sfh_ctx_stream(sfh_ctx *ctx, void **stream_out) {
+    if (!ctx || !stream_out) return SFH_ERR_ARG;
+    *stream_out = (void *)ctx->stream;
+    return SFH_OK;
+}
+
+extern "C" int sfh_ctx_launch_count(const sfh_ctx *ctx, int64_t *count_out) {
+    if (!ctx || !count_out) return SFH_ERR_ARG;
+    *count_out = ctx->launches;
+    return SFH_OK;
+}
+
+static int reserve(sfh_ctx *ctx, void **buf, size_t *cur, size_t bytes) {
+    if (bytes <= *cur) return SFH_OK;
+    // Growth is rare: drain the stream so the old buffer is no longer in use.
+    SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    if (*buf) cudaFree(*buf);
+    *buf = nullptr;
+    *cur = 0;
+    size_t want = bytes + bytes / 4;
+    SFH_CK(ctx, cudaMalloc(buf, want));
+    *cur = want;
+    return SFH_OK;
+}
+
+int sfh_scratch_reserve(sfh_ctx *ctx, size_t bytes) {
+    return reserve(ctx, &ctx->scratch, &ctx->scratch_bytes, bytes);
+}
+int sfh_stage_reserve(sfh_ctx *ctx, size_t bytes) {
+    return reserve(ctx, &ctx->stage, &ctx->stage_bytes, bytes);
+}
+
+// ------------------------------------------------------------------ models
+static void free_models(sfh_models *m) {
+    if (!m) return;
+    cudaSetDevice(m->device);
+    if (m->d_col) cudaFree(m->d_col);
+    if (m->d_f32 && m->d_f32 != m->d_col) cudaFree(m->d_f32);
+    if (m->col_hi) cudaFree(m->col_hi);
+    if (m->col_lo) cudaFree(m->col_lo);
+    if (m->row_hi) cudaFree(m->row_hi);
+    if (m->row_lo) cudaFree(m->row_lo);
+    delete m;
+}
+
+extern "C" int sfh_models_free(sfh_models *m) {
+    if (!m) return SFH_ERR_ARG;
+    free_models(m);
+    return SFH_OK;
+}
+
+extern "C" int sfh_models_info(const sfh_models *m, int64_t *nbins, int64_t *nt, int *storage) {
+    if (!m) return SFH_ERR_ARG;
+    if (nbins) *nbins = m->nbins;
+    if (nt) *nt = m->nt;
+    if (storage) *storage = m->storage;
+    return SFH_OK;
+}
+
+// Finishes a handle whose FP32 column-major copy is in m->d_f32.
+static int finish_models(sfh_ctx *ctx, sfh_models *m) {
+    if (m->storage == SFH_F32) {
+        m->d_col = m->d_f32;
+    } else if (m->storage == SFH_BF16X2) {
+        int rc = sfh_build_bf16_planes(ctx, m, m->d_f32);
+        if (rc != SFH_OK) return rc;
+    }
+    return SFH_OK;
+}
+
+extern "C" int sfh_models_upload(sfh_ctx *ctx, const void *host, int src_dtype, int64_t nbins,
+                                 int64_t nt, int storage, sfh_models **out) {
+    if (!ctx || !host || !out || nbins <= 0 || nt <= 0) return SFH_ERR_ARG;
+    if (src_dtype != SFH_F64 && src_dtype != SFH_F32) return SFH_ERR_ARG;
+    if (storage != SFH_F64 && storage != SFH_F32 && storage != SFH_BF16X2) return SFH_ERR_ARG;
+    *out = nullptr;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    sfh_models *m = new sfh_models();
+    m->device = ctx->device;
+    m->nbins = nbins;
+    m->nt = nt;
+    m->storage = storage;
+    const size_t n = (size_t)nbins * (size_t)nt;
+    cudaError_t e;
+    if (storage == SFH_F64) {
+        e = cudaMalloc(&m->d_col, n * sizeof(double));
+        if (e != cudaSuccess) { free_models(m); return sfh_cuda_error(ctx, e, "cudaMalloc models"); }
+        if (src_dtype == SFH_F64) {
+            e = cudaMemcpy(m->d_col, host, n * sizeof(double), cudaMemcpyHostToDevice);
+        } else {
+            std::vector<double> tmp(n);
+            const float *src = (const float *)host;
+            for (size_t i = 0; i < n; ++i) tmp[i] = src[i];
+            e = cudaMemcpy(m->d_col, tmp.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+        }
+        if (e != cudaSuccess) { free_models(m); return sfh_cuda_error(ctx, e, "upload models"); }
+        *out = m;
+        return SFH_OK;
+    }
+    e = cudaMalloc(&m->d_f32, n * sizeof(float));
+    if (e != cudaSuccess) { free_models(m); return sfh_cuda_error(ctx, e, "cudaMalloc models"); }
+    if (src_dtype == SFH_F32) {
+        e = cudaMemcpy(m->d_f32, host, n * sizeof(float), cudaMemcpyHostToDevice);
+    } else {
+        // Round-to-nearest FP64 -> FP32 on the host, chunked to bound the temporary.
+        const double *src = (const double *)host;
+        const size_t chunk = (size_t)1 << 24;
+        std::vector<float> tmp(n < chunk ? n : chunk);
+        e = cudaSuccess;
+        for (size_t off = 0; off < n && e == cudaSuccess; off += chunk) {
+            const size_t cnt = (n - off) < chunk ? (n - off) : chunk;
+            for (size_t i = 0; i < cnt; ++i) tmp[i] = (float)src[off + i];
+            e = cudaMemcpy(m->d_f32 + off, tmp.data(), cnt * sizeof(float), cudaMemcpyHostToDevice);
+        }
+    }
+    if (e != cudaSuccess) { free_models(m); return sfh_cuda_error(ctx, e, "upload models"); }
+    int rc = finish_models(ctx, m);
+    if (rc != SFH_OK) { free_models(m); return rc; }
+    *out = m;
+    return SFH_OK;
+}
+
+extern "C" int sfh_models_from_device(sfh_ctx *ctx, const float *dev, int64_t nbins, int64_t nt,
+                                      int storage, sfh_models **out) {
+    if (!ctx || !dev || !out || nbins <= 0 || nt <= 0) return SFH_ERR_ARG;
+    if (storage != SFH_F32 && storage != SFH_BF16X2) return SFH_ERR_ARG;
+    *out = nullptr;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    sfh_models *m = new sfh_models();
+    m->device = ctx->device;
+    m->nbins = nbins;
+    m->nt = nt;
+    m->storage = storage;
+    const size_t n = (size_t)nbins * (size_t)nt;
+    cudaError_t e = cudaMalloc(&m->d_f32, n * sizeof(float));
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(m->d_f32, dev, n * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream);
+    if (e != cudaSuccess) { free_models(m); return sfh_cuda_error(ctx, e, "copy models"); }
+    int rc = finish_models(ctx, m);
+    if (rc == SFH_OK) {
+        e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) rc = sfh_cuda_error(ctx, e, "models_from_device sync");
+    }
+    if (rc != SFH_OK) { free_models(m); return rc; }
+    *out = m;
+    return SFH_OK;
+}
+
+// ------------------------------------------------------------------ host-array entry points
+namespace {
+
+// Copies a host array of `dtype` elements into device doubles.
+int h2d_as_double(sfh_ctx *ctx, double *dst, const void *src, int dtype, int64_t n,
+                  std::vector<double> &tmp) {
+    if (n == 0) return SFH_OK;
+    const void *p = src;
+    if (dtype == SFH_F32) {
+        tmp.resize((size_t)n);
+        const float *s = (const float *)src;
+        for (int64_t i = 0; i < n; ++i) tmp[(size_t)i] = s[i];
+        p = tmp.data();
+    }
+    SFH_CK(ctx, cudaMemcpyAsync(dst, p, (size_t)n * sizeof(double), cudaMemcpyHostToDevice,
+                                ctx->stream));
+    // The temporary must outlive the copy: pageable copies are staged by the driver
+    // before cudaMemcpyAsync returns, so reusing `tmp` afterwards is safe.
+    return SFH_OK;
+}
+
+int d2h_from_double(sfh_ctx *ctx, void *dst, const double *src, int dtype, int64_t n) {
+    if (n == 0) return SFH_OK;
+    if (dtype == SFH_F64) {
+        SFH_CK(ctx, cudaMemcpyAsync(dst, src, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+        SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+        return SFH_OK;
+    }
+    std::vector<double> tmp((size_t)n);
+    SFH_CK(ctx, cudaMemcpyAsync(tmp.data(), src, (size_t)n * sizeof(double),
+                                cudaMemcpyDeviceToHost, ctx->stream));
+    SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    float *d = (float *)dst;
+    for (int64_t i = 0; i < n; ++i) d[i] = (float)tmp[(size_t)i];
+    return SFH_OK;
+}
+
+double eps_of(int dtype) { return dtype == SFH_F32 ? 1.1920928955078125e-7 : 2.220446049250313e-16; }
+
+bool dtype_ok(int dtype) { return dtype == SFH_F64 || dtype == SFH_F32; }
+
+}  // namespace
+
+extern "C" int sfh_composite(sfh_ctx *ctx, const sfh_models *m, int dtype, const void *coeffs,
+                             void *composite_out) {
+    if (!ctx || !m || !coeffs || !composite_out || !dtype_ok(dtype)) return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    const int64_t nb = m->nbins, nt = m->nt;
+    int rc = sfh_stage_reserve(ctx, sfh_align256(nt * 8) + sfh_align256(nb * 8));
+    if (rc) return rc;
+    double *d_r = (double *)ctx->stage;
+    double *d_c = (double *)((char *)ctx->stage + sfh_align256(nt * 8));
+    std::vector<double> tmp;
+    if ((rc = h2d_as_double(ctx, d_r, coeffs, dtype, nt, tmp))) return rc;
+    FgArgs a{};
+    a.coeffs = d_r;
+    a.composite = d_c;
+    a.eps = eps_of(dtype);
+    a.mode = FG_MODE_COMPOSITE;
+    if ((rc = sfh_launch_fg(ctx, m, a))) return rc;
+    return d2h_from_double(ctx, composite_out, d_c, dtype, nb);
+}
+
+extern "C" int sfh_loglikelihood(sfh_ctx *ctx, int dtype, const void *composite, const void *data,
+                                 int64_t nbins, double *out) {
+    if (!ctx || !composite || !data || !out || nbins < 0 || !dtype_ok(dtype)) return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    int rc = sfh_stage_reserve(ctx, 2 * sfh_align256(nbins * 8) + 256);
+    if (rc) return rc;
+    double *d_c = (double *)ctx->stage;
+    double *d_n = (double *)((char *)ctx->stage + sfh_align256(nbins * 8));
+    double *d_o = (double *)((char *)ctx->stage + 2 * sfh_align256(nbins * 8));
+    std::vector<double> t1, t2;
+    if ((rc = h2d_as_double(ctx, d_c, composite, dtype, nbins, t1))) return rc;
+    if ((rc = h2d_as_double(ctx, d_n, data, dtype, nbins, t2))) return rc;
+    if ((rc = sfh_launch_loglikelihood(ctx, d_c, d_n, nbins, eps_of(dtype), d_o))) return rc;
+    double v = 0;
+    SFH_CK(ctx, cudaMemcpyAsync(&v, d_o, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    // The reference returns T-typed results; round to Float32 for dtype F32.
+    *out = dtype == SFH_F32 ? (double)(float)v : v;
+    return SFH_OK;
+}
+
+extern "C" int sfh_grad_loglikelihood(sfh_ctx *ctx, const sfh_models *m, int dtype,
+                                      void *composite_inout, const void *data, void *G) {
+    if (!ctx || !m || !composite_inout || !data || !G || !dtype_ok(dtype)) return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    const int64_t nb = m->nbins, nt = m->nt;
+    int rc = sfh_stage_reserve(ctx, 2 * sfh_align256(nb * 8) + sfh_align256(nt * 8));
+    if (rc) return rc;
+    double *d_c = (double *)ctx->stage;
+    double *d_n = (double *)((char *)ctx->stage + sfh_align256(nb * 8));
+    double *d_G = (double *)((char *)ctx->stage + 2 * sfh_align256(nb * 8));
+    std::vector<double> t1, t2;
+    if ((rc = h2d_as_double(ctx, d_c, composite_inout, dtype, nb, t1))) return rc;
+    if ((rc = h2d_as_double(ctx, d_n, data, dtype, nb, t2))) return rc;
+    FgArgs a{};
+    a.data = d_n;
+    a.composite = d_c;
+    a.G = d_G;
+    a.eps = eps_of(dtype);
+    a.gsign = -1.0;
+    a.mode = FG_MODE_GRAD_GIVEN;
+    if ((rc = sfh_launch_fg(ctx, m, a))) return rc;
+    if ((rc = d2h_from_double(ctx, composite_inout, d_c, dtype, nb))) return rc;
+    return d2h_from_double(ctx, G, d_G, dtype, nt);
+}
+
+extern "C" int sfh_fg(sfh_ctx *ctx, const sfh_models *m, int dtype, const void *coeffs,
+                      const void *data, void *composite, void *G, double *negLogL) {
+    if (!ctx || !m || !coeffs || !data || !dtype_ok(dtype)) return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    const int64_t nb = m->nbins, nt = m->nt;
+    const size_t o_r = 0, o_n = sfh_align256(nt * 8), o_c = o_n + sfh_align256(nb * 8),
+                 o_g = o_c + sfh_align256(nb * 8), o_l = o_g + sfh_align256(nt * 8);
+    int rc = sfh_stage_reserve(ctx, o_l + 256);
+    if (rc) return rc;
+    char *base = (char *)ctx->stage;
+    std::vector<double> t1, t2;
+    if ((rc = h2d_as_double(ctx, (double *)(base + o_r), coeffs, dtype, nt, t1))) return rc;
+    if ((rc = h2d_as_double(ctx, (double *)(base + o_n), data, dtype, nb, t2))) return rc;
+    FgArgs a{};
+    a.coeffs = (const double *)(base + o_r);
+    a.data = (const double *)(base + o_n);
+    a.composite = (double *)(base + o_c);
+    a.G = G ? (double *)(base + o_g) : nullptr;
+    a.negLogL = negLogL ? (double *)(base + o_l) : nullptr;
+    a.eps = eps_of(dtype);
+    a.gsign = 1.0;
+    a.mode = FG_MODE_FG;
+    if ((rc = sfh_launch_fg(ctx, m, a))) return rc;
+    if (negLogL) {
+        double v = 0;
+        SFH_CK(ctx, cudaMemcpyAsync(&v, base + o_l, sizeof(double), cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+        SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+        *negLogL = dtype == SFH_F32 ? (double)(float)v : v;
+    }
+    if (G && (rc = d2h_from_double(ctx, G, (const double *)(base + o_g), dtype, nt))) return rc;
+    if (composite && (rc = d2h_from_double(ctx, composite, (const double *)(base + o_c), dtype, nb)))
+        return rc;
+    SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return SFH_OK;
+}
+
+extern "C" int sfh_fg_dev(sfh_ctx *ctx, const sfh_models *m, const double *d_coeffs,
+                          const double *d_data, double *d_composite, double *d_G,
+                          double *d_negLogL, double eps) {
+    if (!ctx || !m || !d_coeffs || !d_data || !d_composite) return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    FgArgs a{};
+    a.coeffs = d_coeffs;
+    a.data = d_data;
+    a.composite = d_composite;
+    a.G = d_G;
+    a.negLogL = d_negLogL;
+    a.eps = eps;
+    a.gsign = 1.0;
+    a.mode = FG_MODE_FG;
+    return sfh_launch_fg(ctx, m, a);
+}
+
+extern "C" int sfh_fg_batched_dev(sfh_ctx *ctx, const sfh_models *m, const double *d_R, int64_t B,
+                                  const double *d_data, double *d_negLogL, float *d_G, double eps) {
+    if (!ctx || !m || !d_R || !d_data || B <= 0) return SFH_ERR_ARG;
+    if (m->storage != SFH_BF16X2)
+        return sfh_set_error(ctx, SFH_ERR_ARG, "sfh_fg_batched_dev needs SFH_BF16X2 storage");
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    return sfh_launch_fg_batched(ctx, m, d_R, B, d_data, d_negLogL, d_G, eps);
+}

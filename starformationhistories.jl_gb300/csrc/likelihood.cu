@@ -1,0 +1,526 @@
+// likelihood.cu -- single-vector Poisson objective on sm_103a.
+//
+// Replaces, for one coefficient vector r:
+//   composite!(composite, coeffs, models)        src/fitting/fitting_base.jl:55-65
+//   loglikelihood(composite, data)               src/fitting/fitting_base.jl:84-96
+//   ∇loglikelihood!(G, composite, models, data)  src/fitting/fitting_base.jl:265-285
+//   fg!(F, G, coeffs, models, data, composite)   src/fitting/solvers.jl:20-38
+//
+// Both matrix passes are HBM-bound streams over the (nbins, nt) column-major
+// template matrix M.  Four kernels:
+//   k_gemv_n  : m_i partials over template splits (grid = row blocks x splits)
+//   k_finalize: sums the partials, FP64 Poisson terms with a deterministic
+//               block/last-block reduction, w_i = 1 - n_i/max(m_i, eps)
+//   k_gemv_t  : G_j partials over row chunks, w staged in shared memory
+//   k_reduce_g: fixed-order sum of the G partials
+// FP32 storage multiplies by r = r_hi + r_lo (two FP32 products) and accumulates
+// short FP32 chunks into a compensated FP32 pair, so the composite carries
+// ~1e-8 relative error against FP64 arithmetic on the same stored templates.
+// k_gemv_t walks template columns in the reverse of k_gemv_n's launch order so
+// the tail of M that k_gemv_n streamed last is still resident in L2.
+#include <cuda_runtime.h>
+#include <float.h>
+
+#include "sfh_internal.cuh"
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float x) {
+    const float s = __fadd_rn(hi, x);
+    const float bp = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(x, bp));
+    hi = s;
+    lo = __fadd_rn(lo, err);
+}
+
+// ---------------------------------------------------------------- k_gemv_n (FP32 storage)
+template <bool VEC>
+__global__ void __launch_bounds__(kThreads)
+k_gemv_n_f32(const float *__restrict__ M, int64_t nbins, int64_t nt,
+             const double *__restrict__ r, int kchunk, double *__restrict__ part) {
+    extern __shared__ float s_r[];
+    float *rhi = s_r, *rlo = s_r + kchunk;
+    const int split = blockIdx.y;
+    const int64_t j0 = (int64_t)split * kchunk;
+    const int kn = (int)min((int64_t)kchunk, nt - j0);
+    for (int t = threadIdx.x; t < kn; t += blockDim.x) {
+        const double v = r[j0 + t];
+        const float h = __double2float_rn(v);
+        rhi[t] = h;
+        rlo[t] = __double2float_rn(v - (double)h);
+    }
+    __syncthreads();
+    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4;
+    if (i >= nbins) return;
+    float ah[4] = {0.f, 0.f, 0.f, 0.f}, al[4] = {0.f, 0.f, 0.f, 0.f};
+    const float *colp = M + j0 * nbins + i;
+    int k = 0;
+    if (VEC) {
+        for (; k + 8 <= kn; k += 8) {
+            float4 v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                v[u] = __ldg(reinterpret_cast<const float4 *>(colp + (int64_t)(k + u) * nbins));
+            float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const float h = rhi[k + u], l = rlo[k + u];
+                s0 = fmaf(v[u].x, h, fmaf(v[u].x, l, s0));
+                s1 = fmaf(v[u].y, h, fmaf(v[u].y, l, s1));
+                s2 = fmaf(v[u].z, h, fmaf(v[u].z, l, s2));
+                s3 = fmaf(v[u].w, h, fmaf(v[u].w, l, s3));
+            }
+            two_sum_acc(ah[0], al[0], s0);
+            two_sum_acc(ah[1], al[1], s1);
+            two_sum_acc(ah[2], al[2], s2);
+            two_sum_acc(ah[3], al[3], s3);
+        }
+        for (; k < kn; ++k) {
+            const float4 v = __ldg(reinterpret_cast<const float4 *>(colp + (int64_t)k * nbins));
+            const float h = rhi[k], l = rlo[k];
+            two_sum_acc(ah[0], al[0], fmaf(v.x, h, v.x * l));
+            two_sum_acc(ah[1], al[1], fmaf(v.y, h, v.y * l));
+            two_sum_acc(ah[2], al[2], fmaf(v.z, h, v.z * l));
+            two_sum_acc(ah[3], al[3], fmaf(v.w, h, v.w * l));
+        }
+        double *dst = part + (int64_t)split * nbins + i;
+        dst[0] = (double)ah[0] + (double)al[0];
+        dst[1] = (double)ah[1] + (double)al[1];
+        dst[2] = (double)ah[2] + (double)al[2];
+        dst[3] = (double)ah[3] + (double)al[3];
+    } else {
+        const int nr = (int)min((int64_t)4, nbins - i);
+        for (; k + 8 <= kn; k += 8) {
+            float s[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const float h = rhi[k + u], l = rlo[k + u];
+                const float *c = colp + (int64_t)(k + u) * nbins;
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (q < nr) {
+                        const float x = __ldg(c + q);
+                        s[q] = fmaf(x, h, fmaf(x, l, s[q]));
+                    }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) two_sum_acc(ah[q], al[q], s[q]);
+        }
+        for (; k < kn; ++k) {
+            const float h = rhi[k], l = rlo[k];
+            const float *c = colp + (int64_t)k * nbins;
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (q < nr) {
+                    const float x = __ldg(c + q);
+                    two_sum_acc(ah[q], al[q], fmaf(x, h, x * l));
+                }
+        }
+        double *dst = part + (int64_t)split * nbins + i;
+        for (int q = 0; q < nr; ++q) dst[q] = (double)ah[q] + (double)al[q];
+    }
+}
+
+// ---------------------------------------------------------------- k_gemv_n (FP64 storage)
+__global__ void __launch_bounds__(kThreads)
+k_gemv_n_f64(const double *__restrict__ M, int64_t nbins, int64_t nt,
+             const double *__restrict__ r, int kchunk, double *__restrict__ part) {
+    const int split = blockIdx.y;
+    const int64_t j0 = (int64_t)split * kchunk;
+    const int kn = (int)min((int64_t)kchunk, nt - j0);
+    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 2;
+    if (i >= nbins) return;
+    const bool two = (i + 1 < nbins);
+    const bool vec = two && ((nbins & 1) == 0);
+    double a0 = 0.0, a1 = 0.0;
+    const double *colp = M + j0 * nbins + i;
+    for (int k = 0; k < kn; ++k) {
+        const double rk = __ldg(r + j0 + k);
+        const double *c = colp + (int64_t)k * nbins;
+        if (vec) {
+            const double2 v = __ldg(reinterpret_cast<const double2 *>(c));
+            a0 = fma(v.x, rk, a0);
+            a1 = fma(v.y, rk, a1);
+        } else {
+            a0 = fma(__ldg(c), rk, a0);
+            if (two) a1 = fma(__ldg(c + 1), rk, a1);
+        }
+    }
+    double *dst = part + (int64_t)split * nbins + i;
+    dst[0] = a0;
+    if (two) dst[1] = a1;
+}
+
+// ---------------------------------------------------------------- k_finalize
+struct FinArgs {
+    const double *part;   // ksplit x nbins partials, or NULL (composite is the input)
+    int ksplit;
+    int64_t nbins;
+    const double *data;
+    double eps;
+    double *composite;    // in (when part == NULL) / out
+    float2 *w32;          // w as FP32 hi/lo (FP32 storage) or NULL
+    double *w64;          // w as FP64 (FP64 storage) or NULL
+    int want_logl;
+    int want_w;           // compute w and overwrite composite with it
+    int write_m;          // write m into composite (when !want_w)
+    double *logl_part;    // gridDim.x
+    unsigned int *counter;
+    double *negLogL;      // receives -logL (or +logL when logl_sign = -1)
+    double logl_sign;
+};
+
+__global__ void __launch_bounds__(kThreads) k_finalize(FinArgs a) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double term = 0.0;
+    if (i < a.nbins) {
+        double m;
+        if (a.part) {
+            m = 0.0;
+            for (int s = 0; s < a.ksplit; ++s) m += a.part[(int64_t)s * a.nbins + i];
+        } else {
+            m = a.composite[i];
+        }
+        const double ci = m > a.eps ? m : a.eps;
+        if (a.want_logl || a.want_w) {
+            const double ni = a.data[i];
+            if (a.want_logl) term = (ni > 0.0) ? (ni - ci - ni * log(ni / ci)) : -ci;
+            if (a.want_w) {
+                const double w = 1.0 - ni / ci;
+                a.composite[i] = w;
+                if (a.w32) {
+                    const float h = __double2float_rn(w);
+                    a.w32[i] = make_float2(h, __double2float_rn(w - (double)h));
+                }
+                if (a.w64) a.w64[i] = w;
+            } else if (a.write_m) {
+                a.composite[i] = m;
+            }
+        } else if (a.write_m) {
+            a.composite[i] = m;
+        }
+    }
+    if (!a.want_logl) return;
+    // Deterministic reduction: fixed tree within the block, fixed-order sum of
+    // block partials by the last block to finish.
+    __shared__ double s_red[kThreads / 32];
+    __shared__ bool s_last;
+    double v = term;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int w = 0; w < kThreads / 32; ++w) b += s_red[w];
+        a.logl_part[blockIdx.x] = b;
+        __threadfence();
+        const unsigned int ticket = atomicAdd(a.counter, 1u);
+        s_last = (ticket == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    double acc = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+        acc += ((volatile double *)a.logl_part)[b];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tot = 0.0;
+        for (int w = 0; w < kThreads / 32; ++w) tot += s_red[w];
+        // loglikelihood returns -typemax(T) = -Inf when the sum is exactly zero
+        // (fitting_base.jl:95).
+        const double logl = (tot != 0.0) ? tot : -INFINITY;
+        if (a.negLogL) *a.negLogL = a.logl_sign * -logl;
+        *a.counter = 0u;  // re-arm for the next launch on this stream
+    }
+}
+
+// ---------------------------------------------------------------- k_gemv_t (FP32 storage)
+template <bool VEC>
+__global__ void __launch_bounds__(kThreads)
+k_gemv_t_f32(const float *__restrict__ M, int64_t nbins, int64_t nt, const float2 *__restrict__ w,
+             int R, int CB, int ncolgroups, double *__restrict__ partG) {
+    extern __shared__ float s_w[];
+    float *swh = s_w, *swl = s_w + R;
+    const int rc = blockIdx.y;
+    const int64_t i0 = (int64_t)rc * R;
+    const int rn = (int)min((int64_t)R, nbins - i0);
+    for (int t = threadIdx.x; t < R; t += blockDim.x) {
+        float2 v = make_float2(0.f, 0.f);
+        if (t < rn) v = w[i0 + t];
+        swh[t] = v.x;
+        swl[t] = v.y;
+    }
+    __syncthreads();
+    const int g = ncolgroups - 1 - (int)blockIdx.x;  // reverse of k_gemv_n's order
+    const int64_t jb = (int64_t)g * CB;
+    const int64_t je = min(nt, jb + CB);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int64_t j = je - 1 - warp; j >= jb; j -= kThreads / 32) {
+        const float *col = M + j * nbins + i0;
+        float ah = 0.f, al = 0.f;
+        if (VEC) {
+            int ii = lane * 4;
+            for (; ii + 384 < rn; ii += 512) {
+                float4 m[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    m[u] = __ldg(reinterpret_cast<const float4 *>(col + ii + 128 * u));
+                float s = 0.f;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const float4 h = *reinterpret_cast<const float4 *>(swh + ii + 128 * u);
+                    const float4 l = *reinterpret_cast<const float4 *>(swl + ii + 128 * u);
+                    s = fmaf(m[u].x, h.x, fmaf(m[u].x, l.x, s));
+                    s = fmaf(m[u].y, h.y, fmaf(m[u].y, l.y, s));
+                    s = fmaf(m[u].z, h.z, fmaf(m[u].z, l.z, s));
+                    s = fmaf(m[u].w, h.w, fmaf(m[u].w, l.w, s));
+                }
+                two_sum_acc(ah, al, s);
+            }
+            for (; ii < rn; ii += 128) {
+                const float4 mv = __ldg(reinterpret_cast<const float4 *>(col + ii));
+                const float4 h = *reinterpret_cast<const float4 *>(swh + ii);
+                const float4 l = *reinterpret_cast<const float4 *>(swl + ii);
+                float s = 0.f;
+                s = fmaf(mv.x, h.x, fmaf(mv.x, l.x, s));
+                s = fmaf(mv.y, h.y, fmaf(mv.y, l.y, s));
+                s = fmaf(mv.z, h.z, fmaf(mv.z, l.z, s));
+                s = fmaf(mv.w, h.w, fmaf(mv.w, l.w, s));
+                two_sum_acc(ah, al, s);
+            }
+        } else {
+            for (int ii = lane; ii < rn; ii += 32) {
+                const float x = __ldg(col + ii);
+                two_sum_acc(ah, al, fmaf(x, swh[ii], x * swl[ii]));
+            }
+        }
+        double v = (double)ah + (double)al;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) partG[(int64_t)rc * nt + j] = v;
+    }
+}
+
+// ---------------------------------------------------------------- k_gemv_t (FP64 storage)
+__global__ void __launch_bounds__(kThreads)
+k_gemv_t_f64(const double *__restrict__ M, int64_t nbins, int64_t nt, const double *__restrict__ w,
+             int R, int CB, int ncolgroups, double *__restrict__ partG) {
+    extern __shared__ double s_wd[];
+    const int rc = blockIdx.y;
+    const int64_t i0 = (int64_t)rc * R;
+    const int rn = (int)min((int64_t)R, nbins - i0);
+    for (int t = threadIdx.x; t < R; t += blockDim.x) s_wd[t] = (t < rn) ? w[i0 + t] : 0.0;
+    __syncthreads();
+    const int g = ncolgroups - 1 - (int)blockIdx.x;
+    const int64_t jb = (int64_t)g * CB;
+    const int64_t je = min(nt, jb + CB);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int64_t j = je - 1 - warp; j >= jb; j -= kThreads / 32) {
+        const double *col = M + j * nbins + i0;
+        double acc = 0.0;
+        for (int ii = lane; ii < rn; ii += 32) acc = fma(__ldg(col + ii), s_wd[ii], acc);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (lane == 0) partG[(int64_t)rc * nt + j] = acc;
+    }
+}
+
+__global__ void k_reduce_g(const double *__restrict__ partG, int nchunks, int64_t nt, double sign,
+                           double *__restrict__ G) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nt) return;
+    double acc = 0.0;
+    for (int c = 0; c < nchunks; ++c) acc += partG[(int64_t)c * nt + j];
+    G[j] = sign * acc;
+}
+
+struct Plan {
+    int ksplit, kchunk, nrowblk;
+    int R, CB, ncolgroups, nchunks;
+    size_t off_part, off_w, off_partG, off_logl, total;
+};
+
+Plan make_plan(const sfh_ctx *ctx, int64_t nbins, int64_t nt, bool f64) {
+    Plan p{};
+    const int rows_per_block = f64 ? 2 * kThreads : 4 * kThreads;
+    p.nrowblk = (int)((nbins + rows_per_block - 1) / rows_per_block);
+    const int target = ctx->sm_count * 6;
+    int ks = (target + p.nrowblk - 1) / p.nrowblk;
+    if (ks < 1) ks = 1;
+    if (ks > 64) ks = 64;
+    if (ks > nt) ks = (int)nt;
+    p.kchunk = (int)((nt + ks - 1) / ks);
+    p.ksplit = (int)((nt + p.kchunk - 1) / p.kchunk);
+    p.R = f64 ? 2048 : 4096;
+    p.nchunks = (int)((nbins + p.R - 1) / p.R);
+    int groups = (target + p.nchunks - 1) / p.nchunks;
+    if (groups < 1) groups = 1;
+    int cb = (int)((nt + groups - 1) / groups);
+    cb = ((cb + 7) / 8) * 8;
+    p.CB = cb;
+    p.ncolgroups = (int)((nt + cb - 1) / cb);
+    const int nfin = (int)((nbins + kThreads - 1) / kThreads);
+    p.off_part = 0;
+    p.off_w = sfh_align256((size_t)p.ksplit * nbins * sizeof(double));
+    p.off_partG = p.off_w + sfh_align256((size_t)nbins * (f64 ? sizeof(double) : sizeof(float2)));
+    p.off_logl = p.off_partG + sfh_align256((size_t)p.nchunks * nt * sizeof(double));
+    p.total = p.off_logl + sfh_align256((size_t)nfin * sizeof(double));
+    return p;
+}
+
+}  // namespace
+
+int sfh_launch_fg(sfh_ctx *ctx, const sfh_models *m, const FgArgs &a, cudaEvent_t *ev) {
+    const bool f64 = (m->storage == SFH_F64);
+    const void *Mptr = f64 ? m->d_col : (const void *)m->d_f32;
+    if (!Mptr) return sfh_set_error(ctx, SFH_ERR_ARG, "models handle has no matrix");
+    const int64_t nbins = m->nbins, nt = m->nt;
+    const Plan p = make_plan(ctx, nbins, nt, f64);
+    int rc = sfh_scratch_reserve(ctx, p.total);
+    if (rc) return rc;
+    char *s = (char *)ctx->scratch;
+    double *part = (double *)(s + p.off_part);
+    double *partG = (double *)(s + p.off_partG);
+    double *logl_part = (double *)(s + p.off_logl);
+    float2 *w32 = f64 ? nullptr : (float2 *)(s + p.off_w);
+    double *w64 = f64 ? (double *)(s + p.off_w) : nullptr;
+    cudaStream_t st = ctx->stream;
+
+    const bool from_coeffs = (a.mode == FG_MODE_FG || a.mode == FG_MODE_COMPOSITE);
+    const bool want_g = (a.mode == FG_MODE_GRAD_GIVEN) || (a.mode == FG_MODE_FG && a.G);
+    const bool want_l = (a.mode == FG_MODE_FG && a.negLogL);
+
+    if (ev) SFH_CK(ctx, cudaEventRecord(ev[0], st));
+    if (from_coeffs) {
+        dim3 grid(p.nrowblk, p.ksplit);
+        if (f64) {
+            k_gemv_n_f64<<<grid, kThreads, 0, st>>>((const double *)Mptr, nbins, nt, a.coeffs,
+                                                     p.kchunk, part);
+        } else {
+            const size_t sm = 2 * (size_t)p.kchunk * sizeof(float);
+            if (nbins % 4 == 0)
+                k_gemv_n_f32<true><<<grid, kThreads, sm, st>>>((const float *)Mptr, nbins, nt,
+                                                               a.coeffs, p.kchunk, part);
+            else
+                k_gemv_n_f32<false><<<grid, kThreads, sm, st>>>((const float *)Mptr, nbins, nt,
+                                                                a.coeffs, p.kchunk, part);
+        }
+        SFH_LAUNCHED(ctx);
+    }
+    FinArgs fa{};
+    fa.part = from_coeffs ? part : nullptr;
+    fa.ksplit = p.ksplit;
+    fa.nbins = nbins;
+    fa.data = a.data;
+    fa.eps = a.eps;
+    fa.composite = a.composite;
+    fa.w32 = want_g ? w32 : nullptr;
+    fa.w64 = want_g ? w64 : nullptr;
+    fa.want_logl = want_l ? 1 : 0;
+    fa.want_w = want_g ? 1 : 0;
+    fa.write_m = from_coeffs ? 1 : 0;
+    fa.logl_part = logl_part;
+    fa.counter = ctx->d_counters + SFH_CNT_LOGL;
+    fa.negLogL = a.negLogL;
+    fa.logl_sign = 1.0;
+    if (ev) SFH_CK(ctx, cudaEventRecord(ev[1], st));
+    const int nfin = (int)((nbins + kThreads - 1) / kThreads);
+    k_finalize<<<nfin, kThreads, 0, st>>>(fa);
+    SFH_LAUNCHED(ctx);
+    if (ev) SFH_CK(ctx, cudaEventRecord(ev[2], st));
+    if (!want_g) return SFH_OK;
+    dim3 gridt(p.ncolgroups, p.nchunks);
+    if (f64) {
+        k_gemv_t_f64<<<gridt, kThreads, (size_t)p.R * sizeof(double), st>>>(
+            (const double *)Mptr, nbins, nt, w64, p.R, p.CB, p.ncolgroups, partG);
+    } else {
+        const size_t sm = 2 * (size_t)p.R * sizeof(float);
+        if (nbins % 4 == 0)
+            k_gemv_t_f32<true><<<gridt, kThreads, sm, st>>>((const float *)Mptr, nbins, nt, w32,
+                                                            p.R, p.CB, p.ncolgroups, partG);
+        else
+            k_gemv_t_f32<false><<<gridt, kThreads, sm, st>>>((const float *)Mptr, nbins, nt, w32,
+                                                             p.R, p.CB, p.ncolgroups, partG);
+    }
+    SFH_LAUNCHED(ctx);
+    if (ev) SFH_CK(ctx, cudaEventRecord(ev[3], st));
+    k_reduce_g<<<(int)((nt + kThreads - 1) / kThreads), kThreads, 0, st>>>(partG, p.nchunks, nt,
+                                                                            a.gsign, a.G);
+    SFH_LAUNCHED(ctx);
+    if (ev) SFH_CK(ctx, cudaEventRecord(ev[4], st));
+    return SFH_OK;
+}
+
+// Average per-kernel device time of `iters` fg! evaluations (telemetry for the
+// roofline report): ms_out[0..3] = k_gemv_n, k_finalize, k_gemv_t, k_reduce_g.
+extern "C" int sfh_fg_kernel_times(sfh_ctx *ctx, const sfh_models *m, const double *d_coeffs,
+                                   const double *d_data, double *d_composite, double *d_G,
+                                   double *d_negLogL, double eps, int iters, double *ms_out) {
+    if (!ctx || !m || !d_coeffs || !d_data || !d_composite || !d_G || !ms_out || iters < 1)
+        return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    cudaEvent_t ev[5];
+    for (int k = 0; k < 5; ++k) SFH_CK(ctx, cudaEventCreate(&ev[k]));
+    double acc[4] = {0, 0, 0, 0};
+    FgArgs a{};
+    a.coeffs = d_coeffs;
+    a.data = d_data;
+    a.composite = d_composite;
+    a.G = d_G;
+    a.negLogL = d_negLogL;
+    a.eps = eps;
+    a.gsign = 1.0;
+    a.mode = FG_MODE_FG;
+    int rc = SFH_OK;
+    for (int it = 0; it < iters && rc == SFH_OK; ++it) {
+        rc = sfh_launch_fg(ctx, m, a, ev);
+        if (rc != SFH_OK) break;
+        cudaError_t e = cudaEventSynchronize(ev[4]);
+        if (e != cudaSuccess) { rc = sfh_cuda_error(ctx, e, "event sync"); break; }
+        for (int k = 0; k < 4; ++k) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+            acc[k] += ms;
+        }
+    }
+    for (int k = 0; k < 5; ++k) cudaEventDestroy(ev[k]);
+    for (int k = 0; k < 4; ++k) ms_out[k] = acc[k] / iters;
+    return rc;
+}
+
+int sfh_launch_loglikelihood(sfh_ctx *ctx, const double *composite, const double *data,
+                             int64_t nbins, double eps, double *d_out) {
+    const int nfin = (int)((nbins + kThreads - 1) / kThreads);
+    int rc = sfh_scratch_reserve(ctx, sfh_align256((size_t)(nfin > 0 ? nfin : 1) * sizeof(double)));
+    if (rc) return rc;
+    if (nbins == 0) {
+        const double v = -INFINITY;  // empty sum is exactly zero -> -typemax
+        SFH_CK(ctx, cudaMemcpyAsync(d_out, &v, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+        return SFH_OK;
+    }
+    FinArgs fa{};
+    fa.part = nullptr;
+    fa.nbins = nbins;
+    fa.data = data;
+    fa.eps = eps;
+    fa.composite = const_cast<double *>(composite);
+    fa.want_logl = 1;
+    fa.want_w = 0;
+    fa.write_m = 0;
+    fa.logl_part = (double *)ctx->scratch;
+    fa.counter = ctx->d_counters + SFH_CNT_LOGL;
+    fa.negLogL = d_out;
+    fa.logl_sign = -1.0;  // store +logL
+    k_finalize<<<nfin, kThreads, 0, ctx->stream>>>(fa);
+    SFH_LAUNCHED(ctx);
+    return SFH_OK;
+}

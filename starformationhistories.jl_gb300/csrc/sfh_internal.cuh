@@ -1,0 +1,101 @@
+// sfh_internal.cuh -- shared declarations of the sm_103a Hess-diagram library.
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include <mutex>
+#include <string>
+
+#include "../../include/sfhgpu.h"
+
+struct sfh_ctx {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    // Growable device scratch arena (one per context; single stream => no races).
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+    // Device staging used by the host-array entry points.
+    void *stage = nullptr;
+    size_t stage_bytes = 0;
+    // Zero-initialised counters for last-block reductions (reset by the last block).
+    unsigned int *d_counters = nullptr;
+    int64_t launches = 0;
+};
+
+struct sfh_models {
+    int device = 0;
+    int64_t nbins = 0, nt = 0;
+    int storage = SFH_F32;
+    // F64/F32: (nbins, nt) column-major.  BF16X2: unused.
+    void *d_col = nullptr;
+    // BF16X2 planes for the batched tensor-core path:
+    //  col_hi/col_lo: (nbins_pad, nt_pad) column-major (K = bins contiguous) for G = Mᵀ W
+    //  row_hi/row_lo: (nbins_pad, nt_pad) row-major    (K = templates contiguous) for C = M R
+    __nv_bfloat16 *col_hi = nullptr, *col_lo = nullptr, *row_hi = nullptr, *row_lo = nullptr;
+    // FP32 copy kept with BF16X2 storage so single-vector calls still work.
+    float *d_f32 = nullptr;
+    int64_t nbins_pad = 0, nt_pad = 0;
+};
+
+// Counter slots in sfh_ctx::d_counters.
+enum { SFH_CNT_LOGL = 0, SFH_CNT_BATCH = 1, SFH_CNT_SLOTS = 64 };
+
+// ------------------------------------------------------------------ error helpers
+int sfh_set_error(sfh_ctx *ctx, int code, const std::string &msg);
+int sfh_cuda_error(sfh_ctx *ctx, cudaError_t e, const char *what);
+
+#define SFH_CK(ctx, call)                                                     \
+    do {                                                                      \
+        cudaError_t _e = (call);                                              \
+        if (_e != cudaSuccess) return sfh_cuda_error((ctx), _e, #call);       \
+    } while (0)
+
+#define SFH_LAUNCHED(ctx)                                                     \
+    do {                                                                      \
+        (ctx)->launches++;                                                    \
+        cudaError_t _e = cudaGetLastError();                                  \
+        if (_e != cudaSuccess) return sfh_cuda_error((ctx), _e, "kernel launch"); \
+    } while (0)
+
+// Ensures ctx->scratch holds at least `bytes` (256-byte aligned sub-allocations).
+int sfh_scratch_reserve(sfh_ctx *ctx, size_t bytes);
+int sfh_stage_reserve(sfh_ctx *ctx, size_t bytes);
+
+static inline size_t sfh_align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// ------------------------------------------------------------------ internal launchers
+// Single-vector objective on device arrays (likelihood.cu).
+struct FgArgs {
+    const double *coeffs;   // nt (may be NULL when only loglikelihood/grad of a given composite)
+    const double *data;     // nbins
+    double *composite;      // nbins (in/out per mode)
+    double *G;              // nt or NULL
+    double *negLogL;        // device scalar or NULL
+    double eps;
+    double gsign;           // +1: gradient of -logL (fg!), -1: ∇loglikelihood!
+    int mode;               // see FG_MODE_*
+};
+enum {
+    FG_MODE_FG = 0,          // composite from coeffs, then logL/G as requested
+    FG_MODE_COMPOSITE = 1,   // composite only
+    FG_MODE_GRAD_GIVEN = 2   // ∇loglikelihood! from a given composite
+};
+int sfh_launch_fg(sfh_ctx *ctx, const sfh_models *m, const FgArgs &a, cudaEvent_t *ev = nullptr);
+int sfh_launch_loglikelihood(sfh_ctx *ctx, const double *composite, const double *data,
+                             int64_t nbins, double eps, double *d_out);
+
+// Batched objective (batched.cu).
+int sfh_launch_fg_batched(sfh_ctx *ctx, const sfh_models *m, const double *d_R, int64_t B,
+                          const double *d_data, double *d_negLogL, float *d_G, double eps);
+// Builds the BF16 hi/lo planes from an FP32 column-major matrix (batched.cu).
+int sfh_build_bf16_planes(sfh_ctx *ctx, sfh_models *m, const float *d_f32);
+
+// Templates (templates.cu).
+int sfh_launch_stamps(sfh_ctx *ctx, const double *d_x, const double *d_y, const double *d_sx,
+                      const double *d_sy, const double *d_w, const int64_t *d_start,
+                      const int32_t *d_count, const int32_t *d_cov, int64_t ntempl,
+                      double xf, double xs, int64_t nx, double yf, double ys, int64_t ny,
+                      float *d_out);

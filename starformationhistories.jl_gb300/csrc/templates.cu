@@ -1,0 +1,619 @@
+// templates.cu -- template (Hess diagram) construction on sm_103a.
+//
+// k_stamps replaces bin_cmd_smooth (src/StarFormationHistories.jl:574-621) and
+// the two addstar! methods (:345-408) with their kernels
+// GaussianPSFAsymmetric / gaussian_int_general (:191-265) and
+// GaussianPSFCovariant / gaussian_psf_covariant (:272-340).  One CTA owns a
+// band of TY Hess rows of one template in shared memory (FP32); its warps pull
+// stars from a shared counter, skip stars whose window misses the band, and
+// scatter the bin-integrated Gaussian into the band with shared-memory atomics.
+// The band is flushed to HBM with coalesced stores.  Window sizes, ties-to-even
+// centroid rounding and the "both clipped lengths > 1" skip follow the
+// reference exactly.  erf differences are formed from erfc of |t| so that bins
+// in the tails keep relative accuracy in FP32.
+//
+// k_iso_stars replaces the single-star part of partial_cmd_smooth (:829-888):
+// mini_spacing resampling (:110-148, block-wide prefix scan over segments),
+// interpolate_mini (:77-81), exp_photerr / Martin2016 callables
+// (src/utilities.jl:205,218), calculate_weights (:765-776), bias and midpoints
+// (:417-436), emitting one star record per midpoint.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <vector>
+
+#include "sfh_internal.cuh"
+
+namespace {
+
+constexpr int kStampThreads = 256;
+constexpr int kWarps = kStampThreads / 32;
+constexpr size_t kBandBudget = 96 * 1024;
+
+struct Grid2 {
+    double xf, xs, yf, ys;
+    int nx, ny;
+};
+
+// Signed erfc table entry: |value| = erfc(|t|), sign bit = sign of t.
+__device__ __forceinline__ float erfc_signed(float t) { return copysignf(erfcf(fabsf(t)), t); }
+
+// erf(tb) - erf(ta) for ta <= tb from signed erfc entries, without cancellation
+// when both edges sit in the same tail.
+__device__ __forceinline__ float erf_diff(float ea, float eb) {
+    const float a = fabsf(ea), b = fabsf(eb);
+    if (!signbit(ea)) return a - b;  // 0 <= ta <= tb
+    if (signbit(eb)) return b - a;   // ta <= tb < 0
+    return (2.0f - a) - b;           // ta < 0 <= tb
+}
+
+// Gauss-Legendre 3-point nodes/weights, src/StarFormationHistories.jl:303-304.
+__constant__ float c_glx[3] = {-0.7745966692414834f, 0.0f, 0.7745966692414834f};
+__constant__ float c_glw[3] = {0.5555555555555556f, 0.8888888888888888f, 0.5555555555555556f};
+
+__device__ __forceinline__ int64_t clamp_cut(double v) { return (int64_t)fmin(v, 4.0e9); }
+
+// ---------------------------------------------------------------- asymmetric star
+__device__ void star_asym(float *band, float *bx_buf, float *by_buf, const Grid2 &g, int ty0,
+                          int tyn, double x, double y, double sx, double sy, double A, int lane) {
+    const double x0 = (x - g.xf) / g.xs + 1.0;  // histogram_pix, :502
+    const double y0 = (y - g.yf) / g.ys + 1.0;
+    const double ssx = sx / g.xs, ssy = sy / g.ys;
+    if (!(ssx >= 0.0 && ssy >= 0.0) || !(fabs(x0) < 4.0e15 && fabs(y0) < 4.0e15)) return;
+    // size(GaussianPSFAsymmetric) = (ceil(Int, 10σx), ceil(Int, 10σy)), :247
+    const int64_t cx = clamp_cut(ceil(ssx * 10.0)), cy = clamp_cut(ceil(ssy * 10.0));
+    const int64_t xc = __double2ll_rn(x0), yc = __double2ll_rn(y0);  // round(Int, ·): ties to even
+    const int64_t xoff = max((int64_t)1, cx / 2), yoff = max((int64_t)1, cy / 2);
+    const int64_t xlo = max((int64_t)1, xc - xoff), xhi = min((int64_t)g.nx, xc + xoff);
+    const int64_t ylo = max((int64_t)1, yc - yoff), yhi = min((int64_t)g.ny, yc + yoff);
+    if (!(xhi - xlo + 1 > 1 && yhi - ylo + 1 > 1)) return;  // :359
+    const int64_t jlo = max(ylo, (int64_t)ty0 + 1), jhi = min(yhi, (int64_t)(ty0 + tyn));
+    if (jlo > jhi) return;
+    const int lx = (int)(xhi - xlo + 1), ly = (int)(jhi - jlo + 1);
+    // Bin i spans pixel coordinates [i, i+1]: evaluate at i + 1/2 with half width 1/2.
+    const float invx = (float)(0.7071067811865476 / ssx);
+    const float invy = (float)(0.7071067811865476 / ssy);
+    const float dx0 = (float)((double)xlo - x0);
+    const float dy0 = (float)((double)jlo - y0);
+    for (int m = lane; m < lx; m += 32) {
+        const float ta = (dx0 + (float)m) * invx, tb = (dx0 + (float)(m + 1)) * invx;
+        bx_buf[m] = erf_diff(erfc_signed(ta), erfc_signed(tb));
+    }
+    const float a4 = (float)(A * 0.25);
+    for (int m = lane; m < ly; m += 32) {
+        const float ta = (dy0 + (float)m) * invy, tb = (dy0 + (float)(m + 1)) * invy;
+        by_buf[m] = a4 * erf_diff(erfc_signed(ta), erfc_signed(tb));
+    }
+    __syncwarp();
+    const int total = lx * ly;
+    const float inv_lx = 1.0f / (float)lx;
+    float *base = band + (int64_t)(jlo - 1 - ty0) * g.nx + (xlo - 1);
+    for (int p = lane; p < total; p += 32) {
+        const int jj = (int)(((float)p + 0.5f) * inv_lx);
+        const int ii = p - jj * lx;
+        atomicAdd(base + (int64_t)jj * g.nx + ii, bx_buf[ii] * by_buf[jj]);
+    }
+    __syncwarp();
+}
+
+// ---------------------------------------------------------------- covariant star
+__device__ void star_cov(float *band, const Grid2 &g, int ty0, int tyn, double x, double y,
+                         double sx, double sy, double A, float cov, int lane) {
+    if (!(sx >= 0.0 && sy >= 0.0)) return;
+    const double xpix = (x - g.xf) / g.xs + 1.0, ypix = (y - g.yf) / g.ys + 1.0;
+    if (!(fabs(xpix) < 4.0e15 && fabs(ypix) < 4.0e15)) return;
+    const int64_t xp = __double2ll_rn(xpix), yp = __double2ll_rn(ypix);
+    // size(GaussianPSFCovariant) = (15σx, 10σy), :293; half widths, :383-384
+    const int64_t xoff = max((int64_t)1, (int64_t)__double2ll_rn(fmin(15.0 * sx / g.xs / 2.0, 4.0e9)));
+    const int64_t yoff = max((int64_t)1, (int64_t)__double2ll_rn(fmin(10.0 * sy / g.ys / 2.0, 4.0e9)));
+    const int64_t xlo = max((int64_t)1, xp - xoff), xhi = min((int64_t)g.nx, xp + xoff);
+    const int64_t ylo = max((int64_t)1, yp - yoff), yhi = min((int64_t)g.ny, yp + yoff);
+    const int64_t lx = xhi - xlo + 1, lyw = yhi - ylo + 1;
+    if (!(lx > 1 && lyw > 1)) return;  // :401
+    const int64_t jlo = max(ylo, (int64_t)ty0 + 1), jhi = min(yhi, (int64_t)(ty0 + tyn));
+    if (jlo > jhi) return;
+    // Bin centres: range(histogram_data(first + 1/2), histogram_data(last + 1/2); length), :390-393
+    const double xr0 = ((double)xlo - 0.5) * g.xs + g.xf, xr1 = ((double)xhi - 0.5) * g.xs + g.xf;
+    const double yr0 = ((double)ylo - 0.5) * g.ys + g.yf, yr1 = ((double)yhi - 0.5) * g.ys + g.yf;
+    const double xrs = (xr1 - xr0) / (double)(lx - 1), yrs = (yr1 - yr0) / (double)(lyw - 1);
+    const double hx = xrs / 2.0, hy = yrs / 2.0;
+    const double inv_sx = 0.7071067811865476 / sx;  // 1 / (√2 σx)
+    // t of the lower x edge of bin e, before the covariance shift: (xr_e - hx - x0)/(√2σx)
+    const float bx = (float)((xr0 - hx - x) * inv_sx);
+    const float sxr = (float)(xrs * inv_sx);
+    const float dyb = (float)(yr0 - y);   // row-0 centre minus y0
+    const float yrsf = (float)yrs, hyf = (float)hy;
+    const float inv_sy = (float)(1.0 / sy);
+    const float invsxf = (float)inv_sx;
+    // prefac = A / 2 / sqrt(2π) / σy (:320) times the scaled GL weights w_k * hy (:325)
+    const float pref = (float)(A / 2.0 / 2.5066282746310002 / sy * hy);
+    const int E = (int)lx + 1;  // edges per row
+    const int W = E <= 32 ? E : 32;
+    const int rows_per = 32 / W;
+    const int nb = W - 1;  // bins per segment pass
+    const int seg = lane / W, pos = lane - (lane / W) * W;
+    const int nrows = (int)(jhi - jlo + 1);
+    const int row_off = (int)(jlo - ylo);  // first band row's index inside the full window
+    float *band_row0 = band + (int64_t)(jlo - 1 - ty0) * g.nx + (xlo - 1);
+    for (int rb = 0; rb < nrows; rb += rows_per) {
+        const int row = rb + seg;
+        const bool vrow = (seg < rows_per) && (row < nrows);
+        float ck[3] = {0.f, 0.f, 0.f}, sk[3] = {0.f, 0.f, 0.f};
+        if (vrow) {
+            const float dyc = dyb + (float)(row_off + row) * yrsf;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float dy = dyc + c_glx[k] * hyf;
+                const float z = dy * inv_sy;
+                ck[k] = pref * c_glw[k] * __expf(-0.5f * z * z);
+                sk[k] = cov * dy * invsxf;
+            }
+        }
+        for (int e0 = 0; e0 < (int)lx; e0 += nb) {
+            const int e = e0 + pos;
+            const bool ve = vrow && (e <= (int)lx);
+            float ev[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) ev[k] = ve ? erfc_signed(bx + (float)e * sxr + sk[k]) : 0.f;
+            float nx_[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) nx_[k] = __shfl_down_sync(0xffffffffu, ev[k], 1);
+            if (ve && pos < W - 1 && e < (int)lx) {
+                float v = 0.f;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) v = fmaf(ck[k], erf_diff(ev[k], nx_[k]), v);
+                atomicAdd(band_row0 + (int64_t)row * g.nx + e, v);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- k_stamps
+__global__ void __launch_bounds__(kStampThreads)
+k_stamps(const double *__restrict__ xs, const double *__restrict__ ys,
+         const double *__restrict__ sxs, const double *__restrict__ sys,
+         const double *__restrict__ ws, const int64_t *__restrict__ start,
+         const int32_t *__restrict__ count, const int32_t *__restrict__ covs, Grid2 g, int TY,
+         float *__restrict__ out) {
+    extern __shared__ float smem[];
+    const int t = blockIdx.y;
+    const int ty0 = blockIdx.x * TY;
+    const int tyn = min(TY, g.ny - ty0);
+    float *band = smem;
+    const int bandn = tyn * g.nx;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float *wb = smem + (size_t)TY * g.nx + (size_t)warp * (g.nx + TY);
+    __shared__ int s_next;
+    for (int k = threadIdx.x; k < bandn; k += blockDim.x) band[k] = 0.f;
+    if (threadIdx.x == 0) s_next = 0;
+    __syncthreads();
+    const int64_t s0 = start[t];
+    const int n = count[t];
+    const int cov = covs[t];
+    for (;;) {
+        int q = 0;
+        if (lane == 0) q = atomicAdd(&s_next, 1);
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (q >= n) break;
+        const int64_t s = s0 + q;
+        if (cov == 0)
+            star_asym(band, wb, wb + g.nx, g, ty0, tyn, xs[s], ys[s], sxs[s], sys[s], ws[s], lane);
+        else
+            star_cov(band, g, ty0, tyn, xs[s], ys[s], sxs[s], sys[s], ws[s], (float)cov, lane);
+    }
+    __syncthreads();
+    float *dst = out + (int64_t)t * ((int64_t)g.nx * g.ny) + (int64_t)ty0 * g.nx;
+    for (int k = threadIdx.x; k < bandn; k += blockDim.x) dst[k] = band[k];
+}
+
+__global__ void k_offsets_to_counts(const int64_t *__restrict__ off, int64_t n,
+                                    int32_t *__restrict__ cnt) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) cnt[t] = (int32_t)(off[t + 1] - off[t]);
+}
+
+// ---------------------------------------------------------------- k_iso_stars (partial_cmd_smooth)
+constexpr int kIsoThreads = 256;
+constexpr int kIsoMaxPts = 4096;  // isochrone points per template held in shared memory
+
+struct IsoParams {
+    int nf, y_index, c1, c2, covariant;
+    double dmag;
+    // exp_photerr per filter: σ = min(exp2(b (m - c) log2 a) + d, cap)
+    double eb_log2a[8], ec[8], ed[8], ecap[8];
+    // Martin2016 per filter
+    double cA[8], cm50[8], crho_inv[8];
+    double bias[8];
+    // IMF: segment k covers [lo_k, hi_k) with density scale_k m^-alpha_k / norm
+    int nseg;
+    double imf_lo[4], imf_hi[4], imf_scale[4], imf_alpha[4];
+    double imf_inv_norm, inv_mean_mass;
+    int64_t total;  // stride between filters in the mags array
+};
+
+struct IsoPoint {
+    double mass, xcol, ymag, cerr, yerr, compl_;
+};
+
+__device__ __forceinline__ double imf_pdf(const IsoParams &P, double m) {
+    if (!(m >= P.imf_lo[0] && m <= P.imf_hi[P.nseg - 1])) return 0.0;
+    int k = 0;
+    while (k < P.nseg - 1 && m >= P.imf_hi[k]) ++k;
+    return P.imf_scale[k] * P.imf_inv_norm *
+           (double)exp2f((float)(-P.imf_alpha[k] * log2(m)));
+}
+
+__device__ __forceinline__ double err_eval(const IsoParams &P, int f, double m) {
+    const double s = (double)exp2f((float)(P.eb_log2a[f] * (m - P.ec[f]))) + P.ed[f];
+    return s < P.ecap[f] ? s : P.ecap[f];
+}
+
+__device__ __forceinline__ double compl_eval(const IsoParams &P, int f, double m) {
+    return P.cA[f] / (1.0 + (double)__expf((float)((m - P.cm50[f]) * P.crho_inv[f])));
+}
+
+// Resampled point q of the isochrone (mini_spacing + interpolate_mini + callables).
+__device__ IsoPoint iso_point(const IsoParams &P, const double *m, const double *mags, int n,
+                              const int *pos, const int *cnt, double dmod, int q) {
+    int k = 0;
+    double mass, frac;
+    if (q == 0) {
+        mass = m[0];
+        frac = 0.0;
+    } else {
+        // largest k in [0, n-2] with pos[k] <= q
+        int lo = 0, hi = n - 2;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (pos[mid] <= q) lo = mid; else hi = mid - 1;
+        }
+        k = lo;
+        const int j = q - pos[k] + 1;
+        const int c = cnt[k];
+        if (c == 1) {
+            mass = m[k + 1];
+            frac = 1.0;
+        } else {
+            mass = m[k] + (m[k + 1] - m[k]) / (double)c * (double)j;
+            frac = (mass - m[k]) / (m[k + 1] - m[k]);
+        }
+    }
+    const int kk = (q == 0) ? 0 : k;
+    double mag[8];
+    int fl[3] = {P.c1, P.c2, P.y_index};
+#pragma unroll
+    for (int u = 0; u < 3; ++u) {
+        const int f = fl[u];
+        const double *v = mags + (int64_t)f * P.total;
+        const double a = v[kk];
+        const double b = (kk + 1 < n) ? v[kk + 1] : a;
+        mag[u] = ((q == 0) ? a : a * (1.0 - frac) + b * frac) + dmod;
+    }
+    IsoPoint p;
+    p.mass = mass;
+    const double e1 = err_eval(P, P.c1, mag[0]), e2 = err_eval(P, P.c2, mag[1]);
+    const double ey = err_eval(P, P.y_index, mag[2]);
+    double comp = compl_eval(P, P.c1, mag[0]) * compl_eval(P, P.c2, mag[1]);
+    if (P.covariant) {
+        p.cerr = (P.y_index == P.c1) ? e2 : e1;  // error of the non-y filter, :862
+    } else {
+        p.cerr = sqrt(e1 * e1 + e2 * e2);        // :871-872
+        comp *= compl_eval(P, P.y_index, mag[2]);
+    }
+    p.yerr = ey;
+    p.compl_ = comp;
+    p.xcol = (mag[0] + P.bias[P.c1]) - (mag[1] + P.bias[P.c2]);
+    p.ymag = mag[2] + P.bias[P.y_index];
+    return p;
+}
+
+// Segment insertion counts (:128-137) and their exclusive scan, in shared memory.
+// Returns N = 1 + sum(cnt) (number of resampled points); sets *bad when masses
+// are not strictly increasing.
+__device__ int iso_scan(const IsoParams &P, const double *m, const double *mg, int n, int *s_cnt,
+                        int *s_pos, int *s_warp, int *bad) {
+    const int nseg = n - 1;
+    for (int k = threadIdx.x; k < nseg; k += blockDim.x) {
+        const double *vc1 = mg + (int64_t)P.c1 * P.total, *vc2 = mg + (int64_t)P.c2 * P.total;
+        const double *vy = mg + (int64_t)P.y_index * P.total;
+        const double dc = (vc1[k + 1] - vc2[k + 1]) - (vc1[k] - vc2[k]);
+        const double dy = vy[k + 1] - vy[k];
+        const double d = hypot(dc, dy);
+        int c = 1;
+        if (d > P.dmag) {
+            const double r = ceil(d / P.dmag);
+            c = r < 1.0e7 ? (int)r : 10000000;
+        }
+        if (!(m[k + 1] > m[k])) atomicExch(bad, 2);
+        s_cnt[k] = c;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int carry = 1;
+    for (int base = 0; base < nseg; base += blockDim.x) {
+        const int k = base + threadIdx.x;
+        const int v = (k < nseg) ? s_cnt[k] : 0;
+        int incl = v;
+#pragma unroll
+        for (int o2 = 1; o2 < 32; o2 <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o2);
+            if (lane >= o2) incl += y;
+        }
+        if (lane == 31) s_warp[warp] = incl;
+        __syncthreads();
+        int wpre = 0, tot = 0;
+        for (int w = 0; w < kIsoThreads / 32; ++w) {
+            if (w < warp) wpre += s_warp[w];
+            tot += s_warp[w];
+        }
+        if (k < nseg) s_pos[k] = carry + wpre + incl - v;
+        carry += tot;
+        __syncthreads();
+    }
+    return carry;
+}
+
+__global__ void __launch_bounds__(kIsoThreads)
+k_iso_count(const double *__restrict__ m_ini, const double *__restrict__ mags,
+            const int64_t *__restrict__ iso_off, const int32_t *__restrict__ iso_len, IsoParams P,
+            int64_t *__restrict__ nstars_out, int *__restrict__ err_flag) {
+    __shared__ int s_cnt[kIsoMaxPts];
+    __shared__ int s_pos[kIsoMaxPts];
+    __shared__ int s_warp[kIsoThreads / 32];
+    const int t = blockIdx.x;
+    const int n = iso_len[t];
+    const int npts = iso_scan(P, m_ini + iso_off[t], mags + iso_off[t], n, s_cnt, s_pos, s_warp,
+                              err_flag);
+    if (threadIdx.x == 0) nstars_out[t] = npts - 1;
+}
+
+__global__ void __launch_bounds__(kIsoThreads)
+k_iso_stars(const double *__restrict__ m_ini, const double *__restrict__ mags,
+            const int64_t *__restrict__ iso_off, const int32_t *__restrict__ iso_len,
+            const double *__restrict__ dmods, const double *__restrict__ norms, IsoParams P,
+            const int64_t *__restrict__ star_off, double *__restrict__ sx_,
+            double *__restrict__ sy_, double *__restrict__ ssx, double *__restrict__ ssy,
+            double *__restrict__ sw, int32_t *__restrict__ count, int *__restrict__ err_flag) {
+    __shared__ int s_cnt[kIsoMaxPts];
+    __shared__ int s_pos[kIsoMaxPts];
+    __shared__ int s_warp[kIsoThreads / 32];
+    const int t = blockIdx.x;
+    const int n = iso_len[t];
+    const double *m = m_ini + iso_off[t];
+    const double *mg = mags + iso_off[t];
+    const int npts = iso_scan(P, m, mg, n, s_cnt, s_pos, s_warp, err_flag);
+    const int nstars = npts - 1;
+    if (nstars != (int)(star_off[t + 1] - star_off[t])) {  // counts come from k_iso_count
+        if (threadIdx.x == 0) { count[t] = 0; atomicExch(err_flag, 1); }
+        return;
+    }
+    if (threadIdx.x == 0) count[t] = nstars;
+    const double dmod = dmods[t];
+    const double wscale = norms[t] * P.inv_mean_mass;
+    const int64_t so = star_off[t];
+    // One thread per star: endpoints q and q+1, midpoints and weight, :765-776, :884-888.
+    for (int q = threadIdx.x; q < nstars; q += blockDim.x) {
+        const IsoPoint a = iso_point(P, m, mg, n, s_pos, s_cnt, dmod, q);
+        const IsoPoint b = iso_point(P, m, mg, n, s_pos, s_cnt, dmod, q + 1);
+        const double w = (b.mass - a.mass) * (imf_pdf(P, a.mass) + imf_pdf(P, b.mass)) / 2.0 *
+                         a.compl_ * wscale;
+        sx_[so + q] = a.xcol + (b.xcol - a.xcol) / 2.0;
+        sy_[so + q] = a.ymag + (b.ymag - a.ymag) / 2.0;
+        ssx[so + q] = a.cerr + (b.cerr - a.cerr) / 2.0;
+        ssy[so + q] = a.yerr + (b.yerr - a.yerr) / 2.0;
+        sw[so + q] = w;
+    }
+}
+
+int band_rows(int64_t nx, int64_t ny) {
+    const size_t row_bytes = (size_t)nx * sizeof(float);
+    int64_t tymax = (int64_t)(kBandBudget / row_bytes);
+    if (tymax < 1) tymax = 1;
+    const int64_t ntiles = (ny + tymax - 1) / tymax;
+    return (int)((ny + ntiles - 1) / ntiles);
+}
+
+}  // namespace
+
+int sfh_launch_stamps(sfh_ctx *ctx, const double *d_x, const double *d_y, const double *d_sx,
+                      const double *d_sy, const double *d_w, const int64_t *d_start,
+                      const int32_t *d_count, const int32_t *d_cov, int64_t ntempl, double xf,
+                      double xs, int64_t nx, double yf, double ys, int64_t ny, float *d_out) {
+    if (nx < 1 || ny < 1 || nx > (1 << 20) || ny > (1 << 20) || ntempl < 1 || ntempl > 65535)
+        return sfh_set_error(ctx, SFH_ERR_ARG, "stamp grid or template count out of range");
+    if ((size_t)nx * sizeof(float) > kBandBudget)
+        return sfh_set_error(ctx, SFH_ERR_UNSUPPORTED, "nx too large for one shared-memory row");
+    Grid2 g{xf, xs, yf, ys, (int)nx, (int)ny};
+    const int TY = band_rows(nx, ny);
+    const int ntiles = (int)((ny + TY - 1) / TY);
+    const size_t smem = ((size_t)TY * nx + (size_t)kWarps * (nx + TY)) * sizeof(float);
+    static thread_local bool attr_set = false;
+    if (!attr_set) {
+        SFH_CK(ctx, cudaFuncSetAttribute(k_stamps, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         200 * 1024));
+        attr_set = true;
+    }
+    dim3 grid(ntiles, (unsigned)ntempl);
+    k_stamps<<<grid, kStampThreads, smem, ctx->stream>>>(d_x, d_y, d_sx, d_sy, d_w, d_start,
+                                                         d_count, d_cov, g, TY, d_out);
+    SFH_LAUNCHED(ctx);
+    return SFH_OK;
+}
+
+extern "C" int sfh_bin_cmd_smooth_batch_dev(sfh_ctx *ctx, const double *d_x, const double *d_y,
+                                            const double *d_sx, const double *d_sy,
+                                            const double *d_w, const int64_t *d_offsets,
+                                            const int32_t *h_cov, int64_t ntempl, double xf,
+                                            double xs, int64_t nx, double yf, double ys,
+                                            int64_t ny, float *d_models) {
+    if (!ctx || !d_x || !d_y || !d_sx || !d_sy || !d_w || !d_offsets || !h_cov || !d_models ||
+        ntempl < 1)
+        return SFH_ERR_ARG;
+    for (int64_t t = 0; t < ntempl; ++t)
+        if (h_cov[t] < -1 || h_cov[t] > 1) return sfh_set_error(ctx, SFH_ERR_ARG, "cov_mult must be -1, 0 or 1");
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    const size_t o_cnt = 0, o_cov = sfh_align256(ntempl * 4);
+    int rc = sfh_scratch_reserve(ctx, o_cov + sfh_align256(ntempl * 4));
+    if (rc) return rc;
+    int32_t *d_cnt = (int32_t *)((char *)ctx->scratch + o_cnt);
+    int32_t *d_cov = (int32_t *)((char *)ctx->scratch + o_cov);
+    SFH_CK(ctx, cudaMemcpyAsync(d_cov, h_cov, ntempl * 4, cudaMemcpyHostToDevice, ctx->stream));
+    k_offsets_to_counts<<<(int)((ntempl + 255) / 256), 256, 0, ctx->stream>>>(d_offsets, ntempl,
+                                                                                d_cnt);
+    SFH_LAUNCHED(ctx);
+    return sfh_launch_stamps(ctx, d_x, d_y, d_sx, d_sy, d_w, d_offsets, d_cnt, d_cov, ntempl, xf,
+                             xs, nx, yf, ys, ny, d_models);
+}
+
+extern "C" int sfh_bin_cmd_smooth(sfh_ctx *ctx, const double *x, const double *y,
+                                  const double *sx, const double *sy, const double *w,
+                                  int64_t npts, int cov_mult, double xf, double xs, int64_t nx,
+                                  double yf, double ys, int64_t ny, double *hist_out) {
+    if (!ctx || !hist_out || npts < 0 || nx < 1 || ny < 1) return SFH_ERR_ARG;
+    if (npts > 0 && (!x || !y || !sx || !sy || !w)) return SFH_ERR_ARG;
+    if (cov_mult < -1 || cov_mult > 1)  // @argcheck cov_mult in (-1, 0, 1), :578
+        return sfh_set_error(ctx, SFH_ERR_ARG, "cov_mult must be -1, 0 or 1");
+    for (int64_t i = 0; i < npts; ++i)
+        if (sx[i] < 0.0 || sy[i] < 0.0)
+            return sfh_set_error(ctx, SFH_ERR_ARG, "photometric errors must be non-negative");
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    const int64_t nbins = nx * ny;
+    const size_t a5 = sfh_align256((size_t)(npts > 0 ? npts : 1) * 8);
+    const size_t o_out = 5 * a5, o_meta = o_out + sfh_align256(nbins * 4);
+    int rc = sfh_stage_reserve(ctx, o_meta + 256);
+    if (rc) return rc;
+    char *b = (char *)ctx->stage;
+    const double *src[5] = {x, y, sx, sy, w};
+    for (int k = 0; k < 5 && npts > 0; ++k)
+        SFH_CK(ctx, cudaMemcpyAsync(b + k * a5, src[k], npts * 8, cudaMemcpyHostToDevice, ctx->stream));
+    struct { int64_t start; int32_t count; int32_t cov; } meta{0, (int32_t)npts, cov_mult};
+    SFH_CK(ctx, cudaMemcpyAsync(b + o_meta, &meta, sizeof(meta), cudaMemcpyHostToDevice, ctx->stream));
+    float *d_out = (float *)(b + o_out);
+    rc = sfh_launch_stamps(ctx, (const double *)b, (const double *)(b + a5),
+                           (const double *)(b + 2 * a5), (const double *)(b + 3 * a5),
+                           (const double *)(b + 4 * a5), (const int64_t *)(b + o_meta),
+                           (const int32_t *)(b + o_meta + 8), (const int32_t *)(b + o_meta + 12),
+                           1, xf, xs, nx, yf, ys, ny, d_out);
+    if (rc) return rc;
+    std::vector<float> tmp((size_t)nbins);
+    SFH_CK(ctx, cudaMemcpyAsync(tmp.data(), d_out, nbins * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int64_t i = 0; i < nbins; ++i) hist_out[i] = tmp[(size_t)i];
+    return SFH_OK;
+}
+
+extern "C" int sfh_partial_cmd_smooth_batch_dev(
+    sfh_ctx *ctx, const double *d_m_ini, const double *d_mags, int64_t total,
+    const int64_t *h_iso_off, const int32_t *h_iso_len, int64_t ntempl, int nf, int y_index,
+    int c1, int c2, const sfh_err_model *err, const sfh_compl_model *compl_, const double *bias,
+    const sfh_imf *imf, double mean_mass, const double *h_dmod, const double *h_norm, double xf,
+    double xs, int64_t nx, double yf, double ys, int64_t ny, float *d_models) {
+    if (!ctx || !d_m_ini || !d_mags || !h_iso_off || !h_iso_len || !err || !compl_ || !imf ||
+        !h_dmod || !h_norm || !d_models || ntempl < 1 || ntempl > 65535)
+        return SFH_ERR_ARG;
+    if (nf < 2 || nf > 8 || y_index < 0 || y_index >= nf || c1 < 0 || c1 >= nf || c2 < 0 ||
+        c2 >= nf || c1 == c2)
+        return sfh_set_error(ctx, SFH_ERR_ARG, "invalid filter indices");
+    if (imf->nseg < 1 || imf->nseg > 4 || !(imf->mmin > 0) || !(imf->mmax > imf->mmin) ||
+        !(mean_mass > 0))
+        return sfh_set_error(ctx, SFH_ERR_ARG, "invalid IMF");
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    IsoParams P{};
+    P.nf = nf;
+    P.y_index = y_index;
+    P.c1 = c1;
+    P.c2 = c2;
+    P.covariant = (y_index == c1 || y_index == c2) ? 1 : 0;
+    P.dmag = std::fmin(std::fabs(xs), std::fabs(ys));  // :851
+    P.total = total;
+    for (int f = 0; f < nf; ++f) {
+        if (!(err[f].a > 0) || !(compl_[f].rho != 0))
+            return sfh_set_error(ctx, SFH_ERR_ARG, "invalid error or completeness model");
+        P.eb_log2a[f] = err[f].b * std::log2(err[f].a);
+        P.ec[f] = err[f].c;
+        P.ed[f] = err[f].d;
+        P.ecap[f] = err[f].cap;
+        P.cA[f] = compl_[f].A;
+        P.cm50[f] = compl_[f].m50;
+        P.crho_inv[f] = 1.0 / compl_[f].rho;
+        P.bias[f] = bias ? bias[f] : 0.0;
+    }
+    // IMF segments: continuity at the breaks, normalised on [mmin, mmax].
+    P.nseg = imf->nseg;
+    double s = 1.0, norm = 0.0;
+    for (int k = 0; k < imf->nseg; ++k) {
+        const double lo = (k == 0) ? imf->mmin : imf->breaks[k - 1];
+        const double hi = (k == imf->nseg - 1) ? imf->mmax : imf->breaks[k];
+        if (k > 0) s *= std::pow(lo, imf->alpha[k] - imf->alpha[k - 1]);
+        P.imf_lo[k] = lo;
+        P.imf_hi[k] = hi;
+        P.imf_scale[k] = s;
+        P.imf_alpha[k] = imf->alpha[k];
+        const double p = 1.0 - imf->alpha[k];
+        norm += s * (std::fabs(p) < 1e-14 ? std::log(hi / lo) : (std::pow(hi, p) - std::pow(lo, p)) / p);
+    }
+    P.imf_inv_norm = 1.0 / norm;
+    P.inv_mean_mass = 1.0 / mean_mass;
+    for (int64_t t = 0; t < ntempl; ++t) {
+        const int32_t n = h_iso_len[t];
+        if (n < 2 || n > kIsoMaxPts)
+            return sfh_set_error(ctx, SFH_ERR_ARG, "isochrone length must be in [2, 4096]");
+        if (h_iso_off[t] < 0 || h_iso_off[t] + n > total)
+            return sfh_set_error(ctx, SFH_ERR_ARG, "isochrone offsets out of range");
+    }
+    cudaStream_t st = ctx->stream;
+    // Pass 1: resampled star count per template (one read-back), exact offsets.
+    const size_t o_off = 0, o_len = sfh_align256(ntempl * 8), o_dm = o_len + sfh_align256(ntempl * 4);
+    const size_t o_nm = o_dm + sfh_align256(ntempl * 8), o_err = o_nm + sfh_align256(ntempl * 8);
+    const size_t o_cnt64 = o_err + 256, o_soff = o_cnt64 + sfh_align256(ntempl * 8);
+    const size_t o_cnt = o_soff + sfh_align256((ntempl + 1) * 8), o_cov = o_cnt + sfh_align256(ntempl * 4);
+    const size_t o_stars = o_cov + sfh_align256(ntempl * 4);
+    int rc = sfh_scratch_reserve(ctx, o_stars);
+    if (rc) return rc;
+    char *b = (char *)ctx->scratch;
+    SFH_CK(ctx, cudaMemcpyAsync(b + o_off, h_iso_off, ntempl * 8, cudaMemcpyHostToDevice, st));
+    SFH_CK(ctx, cudaMemcpyAsync(b + o_len, h_iso_len, ntempl * 4, cudaMemcpyHostToDevice, st));
+    SFH_CK(ctx, cudaMemsetAsync(b + o_err, 0, 4, st));
+    k_iso_count<<<(unsigned)ntempl, kIsoThreads, 0, st>>>(
+        d_m_ini, d_mags, (const int64_t *)(b + o_off), (const int32_t *)(b + o_len), P,
+        (int64_t *)(b + o_cnt64), (int *)(b + o_err));
+    SFH_LAUNCHED(ctx);
+    std::vector<int64_t> nst((size_t)ntempl);
+    int flag = 0;
+    SFH_CK(ctx, cudaMemcpyAsync(nst.data(), b + o_cnt64, ntempl * 8, cudaMemcpyDeviceToHost, st));
+    SFH_CK(ctx, cudaMemcpyAsync(&flag, b + o_err, 4, cudaMemcpyDeviceToHost, st));
+    SFH_CK(ctx, cudaStreamSynchronize(st));
+    if (flag == 2) return sfh_set_error(ctx, SFH_ERR_ARG, "isochrone masses must be strictly increasing");
+    std::vector<int64_t> soff((size_t)ntempl + 1, 0);
+    for (int64_t t = 0; t < ntempl; ++t) soff[(size_t)t + 1] = soff[(size_t)t] + nst[(size_t)t];
+    const int64_t nstar_total = soff[(size_t)ntempl] > 0 ? soff[(size_t)ntempl] : 1;
+    // Pass 2: star records, then the stamps.
+    const size_t a8 = sfh_align256((size_t)nstar_total * 8);
+    rc = sfh_scratch_reserve(ctx, o_stars + 5 * a8);
+    if (rc) return rc;
+    b = (char *)ctx->scratch;  // may have moved
+    std::vector<int32_t> cov((size_t)ntempl, P.covariant ? (y_index == c1 ? -1 : 1) : 0);
+    SFH_CK(ctx, cudaMemcpyAsync(b + o_off, h_iso_off, ntempl * 8, cudaMemcpyHostToDevice, st));
+    SFH_CK(ctx, cudaMemcpyAsync(b + o_len, h_iso_len, ntempl * 4, cudaMemcpyHostToDevice, st));
+    SFH_CK(ctx, cudaMemcpyAsync(b + o_dm, h_dmod, ntempl * 8, cudaMemcpyHostToDevice, st));
+    SFH_CK(ctx, cudaMemcpyAsync(b + o_nm, h_norm, ntempl * 8, cudaMemcpyHostToDevice, st));
+    SFH_CK(ctx, cudaMemcpyAsync(b + o_soff, soff.data(), (ntempl + 1) * 8, cudaMemcpyHostToDevice, st));
+    SFH_CK(ctx, cudaMemcpyAsync(b + o_cov, cov.data(), ntempl * 4, cudaMemcpyHostToDevice, st));
+    SFH_CK(ctx, cudaMemsetAsync(b + o_err, 0, 4, st));
+    double *sxp = (double *)(b + o_stars), *syp = (double *)(b + o_stars + a8);
+    double *ssxp = (double *)(b + o_stars + 2 * a8), *ssyp = (double *)(b + o_stars + 3 * a8);
+    double *swp = (double *)(b + o_stars + 4 * a8);
+    k_iso_stars<<<(unsigned)ntempl, kIsoThreads, 0, st>>>(
+        d_m_ini, d_mags, (const int64_t *)(b + o_off), (const int32_t *)(b + o_len),
+        (const double *)(b + o_dm), (const double *)(b + o_nm), P, (const int64_t *)(b + o_soff),
+        sxp, syp, ssxp, ssyp, swp, (int32_t *)(b + o_cnt), (int *)(b + o_err));
+    SFH_LAUNCHED(ctx);
+    rc = sfh_launch_stamps(ctx, sxp, syp, ssxp, ssyp, swp, (const int64_t *)(b + o_soff),
+                           (const int32_t *)(b + o_cnt), (const int32_t *)(b + o_cov), ntempl, xf,
+                           xs, nx, yf, ys, ny, d_models);
+    if (rc) return rc;
+    SFH_CK(ctx, cudaMemcpyAsync(&flag, b + o_err, 4, cudaMemcpyDeviceToHost, st));
+    SFH_CK(ctx, cudaStreamSynchronize(st));
+    if (flag) return sfh_set_error(ctx, SFH_ERR_CUDA, "resampled star count changed between passes");
+    return SFH_OK;
+}

@@ -1,0 +1,26 @@
+"""sfhgpu: GB300 (sm_103a) Hess-diagram hot path of StarFormationHistories.jl.
+
+Python mirror of the reference's Julia API over the C ABI in include/sfhgpu.h.
+All compute runs in libsfhgpu.so; there is no CPU fallback.
+"""
+from ._lib import (SFH_BF16X2, SFH_F32, SFH_F64, EXPORTED, LIB_PATH, SFHArgumentError, SFHError,
+                   load)
+from .core import Context, Models, as_models, default_context
+from .fitting import (composite_, construct_x0, fg_, fit_templates, fit_templates_fast,
+                      fit_templates_lbfgsb, grad_loglikelihood, grad_loglikelihood_, loglikelihood,
+                      renormalize_x0, stack_models)
+from .templates import (BrokenPowerLawIMF, Histogram, Kroupa2001, Martin2016_complete,
+                        bin_cmd_smooth, calculate_edges, calculate_weights, compl_model, err_model,
+                        exp_photerr, histogram_data, histogram_pix, interpolate_mini, midpoints,
+                        mini_spacing, partial_cmd_smooth, partial_cmd_smooth_batch)
+
+__all__ = [
+    "SFH_BF16X2", "SFH_F32", "SFH_F64", "EXPORTED", "LIB_PATH", "SFHArgumentError", "SFHError",
+    "load", "Context", "Models", "as_models", "default_context", "composite_", "construct_x0",
+    "fg_", "fit_templates", "fit_templates_fast", "fit_templates_lbfgsb", "grad_loglikelihood",
+    "grad_loglikelihood_", "loglikelihood", "renormalize_x0", "stack_models", "BrokenPowerLawIMF",
+    "Histogram", "Kroupa2001", "Martin2016_complete", "bin_cmd_smooth", "calculate_edges",
+    "calculate_weights", "compl_model", "err_model", "exp_photerr", "histogram_data",
+    "histogram_pix", "interpolate_mini", "midpoints", "mini_spacing", "partial_cmd_smooth",
+    "partial_cmd_smooth_batch",
+]

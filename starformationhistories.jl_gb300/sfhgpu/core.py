@@ -1,0 +1,139 @@
+"""Contexts and template-matrix handles (sfh_ctx / sfh_models of include/sfhgpu.h)."""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+
+import numpy as np
+
+from . import _lib
+from ._lib import SFH_BF16X2, SFH_F32, SFH_F64, check, load, ptr
+
+_STORAGE = {"f64": SFH_F64, "f32": SFH_F32, "bf16x2": SFH_BF16X2,
+            SFH_F64: SFH_F64, SFH_F32: SFH_F32, SFH_BF16X2: SFH_BF16X2}
+
+
+class Context:
+    """One CUDA stream plus scratch on one device (sfh_ctx_create).  Use one per thread."""
+
+    def __init__(self, device: int = 0):
+        L = load()
+        h = C.c_void_p()
+        check(L.sfh_ctx_create(int(device), C.byref(h)), None, "sfh_ctx_create")
+        self._h = h
+        self.device = int(device)
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise RuntimeError("context destroyed")
+        return self._h
+
+    def synchronize(self):
+        check(load().sfh_ctx_synchronize(self.handle), self.handle, "synchronize")
+
+    @property
+    def stream(self) -> int:
+        s = C.c_void_p()
+        check(load().sfh_ctx_stream(self.handle, C.byref(s)), self.handle)
+        return int(s.value or 0)
+
+    @property
+    def launches(self) -> int:
+        n = C.c_int64()
+        check(load().sfh_ctx_launch_count(self.handle, C.byref(n)), self.handle)
+        return int(n.value)
+
+    def torch_stream(self):
+        import torch
+        return torch.cuda.ExternalStream(self.stream, device=torch.device("cuda", self.device))
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            load().sfh_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001 - interpreter shutdown
+            pass
+
+
+_tls = threading.local()
+
+
+def default_context() -> Context:
+    ctx = getattr(_tls, "ctx", None)
+    if ctx is None:
+        ctx = Context(0)
+        _tls.ctx = ctx
+    return ctx
+
+
+class Models:
+    """Device-resident template matrix in the flattened layout (nbins, ntemplates),
+    one template per column (stack_models, src/fitting/utilities.jl:12-13)."""
+
+    def __init__(self, M=None, storage="f32", ctx: Context | None = None, _handle=None,
+                 _shape=None):
+        self.ctx = ctx or default_context()
+        L = load()
+        self.storage = _STORAGE[storage]
+        if _handle is not None:
+            self._h = _handle
+            self.nbins, self.nt = _shape
+            return
+        A = np.asarray(M)
+        if A.ndim != 2:
+            raise ValueError("models must be a (nbins, ntemplates) matrix")
+        src = SFH_F32 if A.dtype == np.float32 else SFH_F64
+        A = np.asfortranarray(A, dtype=np.float32 if src == SFH_F32 else np.float64)
+        self.nbins, self.nt = A.shape
+        h = C.c_void_p()
+        check(L.sfh_models_upload(self.ctx.handle, A.ctypes.data, src, self.nbins, self.nt,
+                                  self.storage, C.byref(h)), self.ctx.handle, "sfh_models_upload")
+        self._h = h
+
+    @classmethod
+    def from_device(cls, dev_ptr: int, nbins: int, nt: int, storage="f32",
+                    ctx: Context | None = None):
+        """Wrap device FP32 (nbins, nt) column-major templates (copied)."""
+        ctx = ctx or default_context()
+        h = C.c_void_p()
+        st = _STORAGE[storage]
+        check(load().sfh_models_from_device(ctx.handle, int(dev_ptr), int(nbins), int(nt), st,
+                                            C.byref(h)), ctx.handle, "sfh_models_from_device")
+        return cls(ctx=ctx, storage=st, _handle=h, _shape=(int(nbins), int(nt)))
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def shape(self):
+        return (self.nbins, self.nt)
+
+    def free(self):
+        if getattr(self, "_h", None) is not None:
+            load().sfh_models_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:  # noqa: BLE001
+            pass
+
+
+def as_models(models, dtype=np.float64) -> Models:
+    """Accept a Models handle or a host (nbins, nt) matrix (uploaded with storage
+    matching its element type)."""
+    if isinstance(models, Models):
+        return models
+    A = np.asarray(models)
+    storage = "f32" if A.dtype == np.float32 else "f64"
+    return Models(A, storage=storage)
+
+
+__all__ = ["Context", "Models", "default_context", "as_models", "ptr", "_lib"]

@@ -1,0 +1,276 @@
+"""Reference-named objective and fit drivers over the GPU C ABI.
+
+Mirrors src/fitting/fitting_base.jl, src/fitting/solvers.jl and
+src/fitting/utilities.jl of StarFormationHistories.jl v1.3.1.  Julia's `!`
+suffix becomes a trailing underscore (`composite_` is `composite!`,
+`fg_` is `fg!`).  Element type T follows the arrays passed (float32 or
+float64), including eps(T) in the clamps.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from collections import namedtuple
+
+import numpy as np
+
+from ._lib import SFH_F32, SFH_F64, check, load
+from .core import Models, as_models, default_context
+
+_dp = None
+
+
+def _T(*arrays):
+    """promote_type of the floating arrays' element types (integers promote to the float)."""
+    ts = [np.asarray(a).dtype for a in arrays if a is not None]
+    fl = [t for t in ts if np.issubdtype(t, np.floating)]
+    if not fl:
+        return np.dtype(np.float64)
+    return np.result_type(*fl)
+
+
+def _code(T):
+    return SFH_F32 if np.dtype(T) == np.float32 else SFH_F64
+
+
+def _arr(a, T):
+    return np.ascontiguousarray(np.asarray(a).reshape(-1, order="F"), dtype=T)
+
+
+def _argcheck(cond, msg):
+    if not cond:
+        raise ValueError(msg)  # the reference throws ArgumentError from @argcheck
+
+
+def stack_models(models):
+    """stack_models(models), src/fitting/utilities.jl:12-13: one column per template,
+    each the column-major `vec` of its Hess matrix."""
+    return np.asfortranarray(np.stack([np.asarray(m).reshape(-1, order="F") for m in models],
+                                      axis=1))
+
+
+def composite_(composite, coeffs, models):
+    """composite!(composite, coeffs, models) flat form, fitting_base.jl:55-65."""
+    M = as_models(models)
+    _argcheck(np.size(composite) == M.nbins, "axes(composite,1) == axes(models,1)")
+    _argcheck(np.size(coeffs) == M.nt, "axes(coeffs,1) == axes(models,2)")
+    T = np.asarray(composite).dtype
+    code = _code(T)
+    r = _arr(coeffs, T)
+    out = np.empty(M.nbins, dtype=T)
+    ctx = M.ctx
+    check(load().sfh_composite(ctx.handle, M.handle, code, r.ctypes.data, out.ctypes.data),
+          ctx.handle, "composite!")
+    composite[...] = out.reshape(np.shape(composite), order="F")
+    return None
+
+
+def loglikelihood(*args):
+    """loglikelihood(composite, data), fitting_base.jl:84-96, or
+    loglikelihood(coeffs, models, data), fitting_base.jl:107-125."""
+    if len(args) == 3:
+        coeffs, models, data = args
+        M = as_models(models)
+        T = _T(coeffs, data) if M.storage != SFH_F32 else np.result_type(_T(coeffs, data),
+                                                                            np.float32)
+        c = np.empty(M.nbins, dtype=T)
+        composite_(c, coeffs, M)
+        return loglikelihood(c, data)
+    composite, data = args
+    _argcheck(np.shape(composite) == np.shape(data), "axes(composite) == axes(data)")
+    T = _T(composite, data)
+    c, n = _arr(composite, T), _arr(data, T)
+    out = C.c_double()
+    ctx = default_context()
+    check(load().sfh_loglikelihood(ctx.handle, _code(T), c.ctypes.data, n.ctypes.data, c.size,
+                                   C.byref(out)), ctx.handle, "loglikelihood")
+    return T.type(out.value)
+
+
+def grad_loglikelihood_(G, composite, models, data):
+    """∇loglikelihood!(G, composite, models, data) flat form, fitting_base.jl:265-285.
+    Overwrites composite with 1 - data/max(composite, eps)."""
+    M = as_models(models)
+    _argcheck(np.size(G) == M.nt, "axes(G,1) == axes(models,2)")
+    _argcheck(np.size(composite) == M.nbins == np.size(data),
+              "axes(models,1) == axes(data,1) == axes(composite,1)")
+    T = np.asarray(composite).dtype
+    c, n = _arr(composite, T), _arr(data, T)
+    g = np.empty(M.nt, dtype=T)
+    ctx = M.ctx
+    check(load().sfh_grad_loglikelihood(ctx.handle, M.handle, _code(T), c.ctypes.data,
+                                        n.ctypes.data, g.ctypes.data), ctx.handle,
+          "∇loglikelihood!")
+    composite[...] = c.reshape(np.shape(composite), order="F")
+    G[...] = g.astype(np.asarray(G).dtype)
+    return G
+
+
+def grad_loglikelihood(*args):
+    """∇loglikelihood forms, fitting_base.jl:144-211: (model, composite, data) for one
+    template, (models, composite, data), or (coeffs, models, data)."""
+    a0, a1, a2 = args
+    if isinstance(a1, Models) or (np.ndim(a1) == 2 and np.ndim(a0) == 1
+                                  and np.shape(a1)[1] == np.size(a0)):
+        coeffs, models, data = a0, a1, a2
+        M = as_models(models)
+        T = _T(coeffs, data)
+        c = np.empty(M.nbins, dtype=T)
+        composite_(c, coeffs, M)
+        G = np.empty(M.nt, dtype=T)
+        grad_loglikelihood_(G, c, M, data)
+        return G
+    if np.ndim(a0) == 2 and np.ndim(a1) == 1 and np.shape(a0)[0] == np.size(a1):
+        models, composite, data = a0, a1, a2
+        M = as_models(models)
+        T = _T(composite, data)
+        c = _arr(composite, T).copy()
+        G = np.empty(M.nt, dtype=T)
+        grad_loglikelihood_(G, c, M, data)
+        return G
+    model, composite, data = a0, a1, a2
+    _argcheck(np.shape(model) == np.shape(composite) == np.shape(data),
+              "axes(model) == axes(composite) == axes(data)")
+    T = _T(model, composite, data)
+    M = Models(_arr(model, T).reshape(-1, 1), storage="f32" if T == np.float32 else "f64")
+    c = _arr(composite, T).copy()
+    G = np.empty(1, dtype=T)
+    grad_loglikelihood_(G, c, M, _arr(data, T))
+    return T.type(G[0])
+
+
+def fg_(F, G, coeffs, models, data, composite):
+    """fg!(F, G, coeffs, models, data, composite), src/fitting/solvers.jl:20-38.
+    Returns -logL when F is not None; fills G with -∇logL when G is not None."""
+    M = as_models(models)
+    _argcheck(np.size(coeffs) == M.nt, "axes(coeffs,1) == axes(models,2)")
+    _argcheck(M.nbins == np.size(data) == np.size(composite),
+              "axes(models,1) == axes(data,1) == axes(composite,1)")
+    T = _T(coeffs, data, composite)
+    r, n = _arr(coeffs, T), _arr(data, T)
+    c = np.empty(M.nbins, dtype=T)
+    g = np.empty(M.nt, dtype=T) if G is not None else None
+    out = C.c_double()
+    ctx = M.ctx
+    check(load().sfh_fg(ctx.handle, M.handle, _code(T), r.ctypes.data, n.ctypes.data,
+                        c.ctypes.data, g.ctypes.data if g is not None else None,
+                        C.byref(out) if F is not None else None), ctx.handle, "fg!")
+    composite[...] = c.reshape(np.shape(composite), order="F")
+    if G is not None:
+        G[...] = g
+    if F is not None:
+        return T.type(out.value)
+    return None
+
+
+# ---------------------------------------------------------------- initial guesses
+
+def construct_x0(logAge, T_max, normalize_value=1.0):
+    """construct_x0, src/fitting/utilities.jl:31-47."""
+    logAge = np.asarray(logAge)
+    _argcheck(np.log10(T_max) + 9 > logAge.max(), "log10(T_max) + 9 > maximum(logAge)")
+    min_la = logAge.min()
+    max_la = np.log10(T_max) + 9
+    uniq = np.concatenate([np.sort(np.unique(logAge)), [max_la]])
+    sfr = normalize_value / (10.0 ** max_la - 10.0 ** min_la)
+    num = np.array([np.count_nonzero(logAge == la) for la in uniq])
+    dt = np.array([10.0 ** uniq[i + 1] - 10.0 ** uniq[i] for i in range(len(uniq) - 1)])
+    out = np.empty_like(logAge, dtype=logAge.dtype if np.issubdtype(logAge.dtype, np.floating)
+                        else np.float64)
+    for i, la in enumerate(logAge):
+        idx = int(np.nonzero(uniq == la)[0][0])
+        out[i] = sfr * dt[idx] / num[idx]
+    return out
+
+
+def renormalize_x0(data, models, x0, full_coeffs=None):
+    """renormalize_x0, src/fitting/utilities.jl:104-115: x0 scaled by Σn / Σm."""
+    M = as_models(models)
+    full = x0 if full_coeffs is None else full_coeffs
+    T = _T(data, full)
+    c = np.empty(M.nbins, dtype=T)
+    composite_(c, full, M)
+    s = c.sum()
+    if s == 0:
+        return np.array(x0, copy=True)
+    return np.asarray(x0) * (np.sum(data) / s)
+
+
+# ---------------------------------------------------------------- fit drivers
+
+def fit_templates_lbfgsb(models, data, x0=None, factr=1e-12, pgtol=1e-5, maxiter=15000):
+    """fit_templates_lbfgsb, src/fitting/solvers.jl:70-90: box-constrained L-BFGS-B on
+    fg! (LBFGSB.jl wraps the same Fortran L-BFGS-B that scipy ships).
+    Returns (-logL, coeffs)."""
+    from scipy.optimize import fmin_l_bfgs_b
+    M = as_models(models)
+    data = np.asarray(data, dtype=np.float64).reshape(-1, order="F")
+    x0 = np.ones(M.nt) if x0 is None else np.asarray(x0, dtype=np.float64)
+    x0 = renormalize_x0(data, M, x0)
+    comp = np.empty(M.nbins)
+    G = np.empty(M.nt)
+
+    def f(x):
+        v = fg_(True, G, x, M, data, comp)
+        return float(v), G.copy()
+
+    x, fval, _info = fmin_l_bfgs_b(f, x0, bounds=[(0.0, None)] * M.nt, factr=factr,
+                                   pgtol=pgtol, maxiter=maxiter, m=10)
+    return fval, x
+
+
+def fit_templates_fast(models, data, x0=None, g_abstol=1e-8, maxiter=10000):
+    """fit_templates_fast, src/fitting/solvers.jl:238-275: BFGS in sqrt space
+    (coeffs = θ²).  Returns (coeffs, result)."""
+    from scipy.optimize import minimize
+    M = as_models(models)
+    data = np.asarray(data, dtype=np.float64).reshape(-1, order="F")
+    x0 = np.ones(M.nt) if x0 is None else np.asarray(x0, dtype=np.float64)
+    x0 = np.sqrt(renormalize_x0(data, M, x0))
+    comp = np.empty(M.nbins)
+    G = np.empty(M.nt)
+
+    def f(s):
+        v = fg_(True, G, s * s, M, data, comp)
+        return float(v), G * 2.0 * s
+
+    res = minimize(f, x0, jac=True, method="BFGS",
+                   options={"gtol": g_abstol, "maxiter": maxiter})
+    return res.x ** 2, res
+
+
+LogTransformFTResult = namedtuple("LogTransformFTResult", ["mu", "sigma", "invH", "result"])
+FitTemplatesResult = namedtuple("FitTemplatesResult", ["map", "mle"])
+
+
+def fit_templates(models, data, x0=None, gtol=1e-8, maxiter=10000):
+    """fit_templates, src/fitting/solvers.jl:172-221: MAP (log transform with the
+    Jacobian term -Σθ) then MLE from the MAP point, both by BFGS; μ, σ from the
+    BFGS inverse Hessian in log space."""
+    from scipy.optimize import minimize
+    M = as_models(models)
+    data = np.asarray(data, dtype=np.float64).reshape(-1, order="F")
+    x0 = np.ones(M.nt) if x0 is None else np.asarray(x0, dtype=np.float64)
+    x0 = np.log(renormalize_x0(data, M, x0))
+    comp = np.empty(M.nbins)
+    G = np.empty(M.nt)
+
+    def fg_map(logx):
+        x = np.exp(logx)
+        v = fg_(True, G, x, M, data, comp) - logx.sum()
+        return float(v), G * x - 1.0
+
+    def fg_mle(logx):
+        x = np.exp(logx)
+        v = fg_(True, G, x, M, data, comp)
+        return float(v), G * x
+
+    opts = {"gtol": gtol, "maxiter": maxiter}
+    r_map = minimize(fg_map, x0, jac=True, method="BFGS", options=opts)
+    r_mle = minimize(fg_mle, r_map.x, jac=True, method="BFGS", options=opts)
+
+    def pack(r):
+        mu = np.exp(r.x)
+        invH = np.asarray(r.hess_inv)
+        return LogTransformFTResult(mu, np.sqrt(np.abs(np.diag(invH))) * mu, invH, r)
+
+    return FitTemplatesResult(pack(r_map), pack(r_mle))

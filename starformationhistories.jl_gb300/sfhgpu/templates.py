@@ -1,0 +1,309 @@
+"""Template (Hess diagram) construction over the GPU C ABI.
+
+Mirrors src/StarFormationHistories.jl of StarFormationHistories.jl v1.3.1:
+isochrone preprocessing (mini_spacing :110-148, interpolate_mini :77-92,
+calculate_weights :765-776, midpoints :417-436, calculate_edges :451-476) runs on
+the host with arbitrary Python callables exactly like the reference's Julia
+callables; the stamp loop of bin_cmd_smooth (:574-621) runs on the GPU.
+`partial_cmd_smooth_batch` runs the whole of partial_cmd_smooth on the GPU for
+closed-form error/completeness/IMF models (many templates per call).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from collections import namedtuple
+
+import numpy as np
+
+from ._lib import ComplModel, ErrModel, IMFParams, check, load
+from .core import default_context
+
+Histogram = namedtuple("Histogram", ["edges", "weights"])
+
+
+# ---------------------------------------------------------------- callables (src/utilities.jl)
+
+def Martin2016_complete(m, A, m50, rho):
+    """Martin2016_complete, src/utilities.jl:205."""
+    return A / (1.0 + np.exp((np.asarray(m) - m50) / rho))
+
+
+def exp_photerr(m, a, b, c, d):
+    """exp_photerr, src/utilities.jl:218."""
+    return a ** (b * (np.asarray(m) - c)) + d
+
+
+class BrokenPowerLawIMF:
+    """Continuous broken power-law IMF normalised on [mmin, mmax]; Kroupa2001 stand-in
+    (InitialMassFunctions.jl is a test dependency of the reference, not vendored)."""
+
+    def __init__(self, mmin, mmax, breaks, alphas):
+        self.mmin, self.mmax = float(mmin), float(mmax)
+        self.breaks = list(breaks)
+        self.alphas = list(alphas)
+        lo = [self.mmin] + self.breaks
+        hi = self.breaks + [self.mmax]
+        self.seg = []
+        s = 1.0
+        for k, a in enumerate(self.alphas):
+            if k > 0:
+                s *= lo[k] ** (a - self.alphas[k - 1])
+            self.seg.append((lo[k], hi[k], s, a))
+
+        def integ(p):
+            tot = 0.0
+            for lo_, hi_, s_, a_ in self.seg:
+                q = -a_ + p + 1.0
+                tot += s_ * (np.log(hi_ / lo_) if abs(q) < 1e-14 else (hi_ ** q - lo_ ** q) / q)
+            return tot
+
+        self._norm = integ(0)
+        self._mean = integ(1) / self._norm
+
+    def pdf(self, m):
+        m = np.asarray(m, dtype=np.float64)
+        out = np.zeros_like(m)
+        for k, (lo, hi, s, a) in enumerate(self.seg):
+            last = (k == len(self.seg) - 1)
+            sel = (m >= lo) & ((m <= hi) if last else (m < hi))
+            out[sel] = s * m[sel] ** (-a) / self._norm
+        return out
+
+    __call__ = pdf
+
+    def mean(self):
+        return self._mean
+
+    def params(self) -> IMFParams:
+        p = IMFParams()
+        p.nseg = len(self.alphas)
+        p.mmin, p.mmax = self.mmin, self.mmax
+        for i, b in enumerate(self.breaks):
+            p.breaks[i] = b
+        for i, a in enumerate(self.alphas):
+            p.alpha[i] = a
+        return p
+
+
+def Kroupa2001(mmin=0.08, mmax=100.0):
+    """Kroupa (2001) IMF on [mmin, mmax] for mmin >= 0.08: slopes 1.3 below 0.5 Msun, 2.3 above."""
+    return BrokenPowerLawIMF(mmin, mmax, [0.5], [1.3, 2.3])
+
+
+# ---------------------------------------------------------------- isochrone utilities
+
+def mini_spacing(m_ini, colors, mags, dmag, ret_spacing=False):
+    """mini_spacing, src/StarFormationHistories.jl:110-148."""
+    m_ini, colors, mags = (np.asarray(a, dtype=np.float64) for a in (m_ini, colors, mags))
+    if not (m_ini.shape == colors.shape == mags.shape):
+        raise ValueError("axes(m_ini) == axes(mags) == axes(colors)")
+    first = m_ini[0]
+    idx = np.argsort(m_ini, kind="stable")
+    m, mg, co = m_ini[idx], mags[idx], colors[idx]
+    d = np.hypot(np.diff(co), np.diff(mg))
+    out = [np.array([first])]
+    for i in range(len(m) - 1):
+        if d[i] > dmag:
+            n = int(np.ceil(d[i] / dmag))
+            step = (m[i + 1] - m[i]) / n
+            out.append(m[i] + step * np.arange(1, n + 1, dtype=np.float64))
+        else:
+            out.append(np.array([m[i + 1]]))
+    allv = np.concatenate(out)
+    _, first_idx = np.unique(allv, return_index=True)
+    new = allv[np.sort(first_idx)]
+    return (new, np.diff(new)) if ret_spacing else new
+
+
+def _dedup_knots(k):
+    k = k.copy()
+    last = k[0]
+    for i in range(1, len(k)):
+        if k[i] == last:
+            k[i] = np.nextafter(k[i - 1], np.inf)
+        else:
+            last = k[i]
+    return k
+
+
+def interpolate_mini(m_ini, mags, new_mini):
+    """interpolate_mini, src/StarFormationHistories.jl:77-81 (sort_ingested,
+    src/simulate.jl:54-63, then linear interpolation on the knots)."""
+    m_ini = np.asarray(m_ini, dtype=np.float64)
+    mags = np.asarray(mags, dtype=np.float64)
+    idx = np.argsort(m_ini, kind="stable")
+    k = _dedup_knots(m_ini[idx])
+    v = mags[idx]
+    x = np.asarray(new_mini, dtype=np.float64)
+    j = np.clip(np.searchsorted(k, x, side="right") - 1, 0, len(k) - 2)
+    t = (x - k[j]) / (k[j + 1] - k[j])
+    out = v[j] * (1.0 - t) + v[j + 1] * t
+    out = np.where(x <= k[0], v[0], out)
+    return np.where(x >= k[-1], v[-1], out)
+
+
+def midpoints(v):
+    """midpoints(v), src/StarFormationHistories.jl:417-436 (element form)."""
+    v = np.asarray(v, dtype=np.float64)
+    return v[:-1] + np.diff(v) / 2.0
+
+
+def calculate_weights(mini, completeness, imf, normalize_value, mean_mass, spacing=None):
+    """calculate_weights, src/StarFormationHistories.jl:765-776."""
+    mini = np.asarray(mini, dtype=np.float64)
+    sp = np.diff(mini) if spacing is None else np.asarray(spacing)
+    p = np.asarray(imf(mini), dtype=np.float64)
+    w = sp * (p[:-1] + p[1:]) / 2.0
+    return w * np.asarray(completeness)[:-1] * normalize_value / mean_mass
+
+
+def histogram_pix(d, edges):
+    """histogram_pix(d, edges::AbstractRange), src/StarFormationHistories.jl:502."""
+    f, s, _ = _range(edges)
+    return (np.asarray(d) - f) / s + 1.0
+
+
+def histogram_data(x, edges):
+    """histogram_data(x, edges::AbstractRange), src/StarFormationHistories.jl:518."""
+    f, s, _ = _range(edges)
+    return (np.asarray(x) - 1.0) * s + f
+
+
+def _range(e):
+    """(first, step, number of bins) of an evenly spaced edge vector."""
+    e = np.asarray(e, dtype=np.float64)
+    if e.ndim != 1 or e.size < 2:
+        raise ValueError("edges must be evenly spaced vectors of length >= 2")
+    step = (e[-1] - e[0]) / (e.size - 1)
+    if not np.allclose(np.diff(e), step, rtol=1e-9, atol=0.0):
+        raise ValueError("edges must be AbstractRange-like (evenly spaced)")
+    return float(e[0]), float(step), int(e.size - 1)
+
+
+def calculate_edges(edges=None, xlim=None, ylim=None, nbins=None, xwidth=None, ywidth=None):
+    """calculate_edges, src/StarFormationHistories.jl:451-476."""
+    if edges is not None:
+        return (np.asarray(edges[0], dtype=np.float64), np.asarray(edges[1], dtype=np.float64))
+    xlim, ylim = sorted(xlim), sorted(ylim)
+    if nbins is None:
+        if xwidth is None or ywidth is None:
+            raise ValueError("If edges and nbins are not provided, xwidth and ywidth must be.")
+        nbins = (int(round((xlim[1] - xlim[0]) / xwidth)), int(round((ylim[1] - ylim[0]) / ywidth)))
+    return (np.linspace(xlim[0], xlim[1], nbins[0]), np.linspace(ylim[0], ylim[1], nbins[1]))
+
+
+# ---------------------------------------------------------------- GPU template builders
+
+def bin_cmd_smooth(colors, mags, color_err, mag_err, cov_mult=0, weights=None, edges=None,
+                   xlim=None, ylim=None, nbins=None, xwidth=None, ywidth=None, ctx=None):
+    """bin_cmd_smooth, src/StarFormationHistories.jl:574-621, stamps on the GPU.
+    Returns Histogram(edges, weights) with weights (nx, ny) float64."""
+    if cov_mult not in (-1, 0, 1):
+        raise ValueError("cov_mult in (-1, 0, 1)")
+    x, y, sx, sy = (np.ascontiguousarray(a, dtype=np.float64) for a in
+                    (colors, mags, color_err, mag_err))
+    w = np.ones_like(x) if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+    if not (x.shape == y.shape == sx.shape == sy.shape == w.shape):
+        raise ValueError("axes(colors) == axes(mags) == axes(color_err) == axes(mag_err) == axes(weights)")
+    if xlim is None and edges is None:
+        xlim, ylim = (x.min(), x.max()), (y.min(), y.max())
+    e = calculate_edges(edges, xlim, ylim, nbins, xwidth, ywidth)
+    (xf, xs, nx), (yf, ys, ny) = _range(e[0]), _range(e[1])
+    ctx = ctx or default_context()
+    out = np.empty(nx * ny)
+    check(load().sfh_bin_cmd_smooth(ctx.handle, x.ctypes.data, y.ctypes.data, sx.ctypes.data,
+                                    sy.ctypes.data, w.ctypes.data, x.size, int(cov_mult), xf, xs,
+                                    nx, yf, ys, ny, out.ctypes.data), ctx.handle, "bin_cmd_smooth")
+    return Histogram(e, out.reshape(ny, nx).T)
+
+
+def partial_cmd_smooth(m_ini, mags, mag_err_funcs, y_index, color_indices, imf,
+                       completeness_funcs=None, bias_funcs=None, dmod=0.0, normalize_value=1.0,
+                       mean_mass=None, edges=None, xlim=None, ylim=None, nbins=None, xwidth=None,
+                       ywidth=None, ctx=None):
+    """partial_cmd_smooth (single stars), src/StarFormationHistories.jl:829-888.
+    y_index / color_indices are 0-based.  Callables act on numpy arrays."""
+    if len(color_indices) != 2:
+        raise ValueError("length(color_indices) == 2")
+    nf = len(mags)
+    completeness_funcs = completeness_funcs or [lambda m: np.ones_like(m)] * nf
+    bias_funcs = bias_funcs or [lambda m: np.zeros_like(m)] * nf
+    if not (nf == len(mag_err_funcs) == len(completeness_funcs) == len(bias_funcs)):
+        raise ValueError("length(mags) == length(mag_err_funcs) == length(completeness_funcs) == length(bias_funcs)")
+    if mean_mass is None:
+        mean_mass = imf.mean()
+    e = calculate_edges(edges, xlim, ylim, nbins, xwidth, ywidth)
+    (xf, xs, nx), (yf, ys, ny) = _range(e[0]), _range(e[1])
+    c1, c2 = color_indices
+    mags = [np.asarray(m, dtype=np.float64) for m in mags]
+    colors = mags[c1] - mags[c2]
+    dmag = min(abs(xs), abs(ys))
+    new_mini, spacing = mini_spacing(m_ini, colors, mags[y_index], dmag, True)
+    iso = [interpolate_mini(m_ini, m, new_mini) + dmod for m in mags]
+    err = [np.asarray(mag_err_funcs[i](iso[i]), dtype=np.float64) for i in range(nf)]
+    if y_index in (c1, c2):
+        xc = c1 if c2 == y_index else c2
+        color_err = err[xc]
+        compl = completeness_funcs[c1](iso[c1]) * completeness_funcs[c2](iso[c2])
+        cov_mult = -1 if y_index == c1 else 1
+    else:
+        color_err = np.sqrt(err[c1] ** 2 + err[c2] ** 2)
+        compl = (completeness_funcs[c1](iso[c1]) * completeness_funcs[c2](iso[c2]) *
+                 completeness_funcs[y_index](iso[y_index]))
+        cov_mult = 0
+    w = calculate_weights(new_mini, compl, imf, normalize_value, mean_mass, spacing)
+    biased = [iso[i] + bias_funcs[i](iso[i]) for i in range(nf)]
+    col = biased[c1] - biased[c2]
+    return bin_cmd_smooth(midpoints(col), midpoints(biased[y_index]), midpoints(color_err),
+                          midpoints(err[y_index]), cov_mult, weights=w, edges=e, ctx=ctx)
+
+
+def err_model(a, b, c, d, cap=np.inf) -> ErrModel:
+    """Closed-form exp_photerr(m, a, b, c, d) capped at cap."""
+    return ErrModel(a, b, c, d, cap)
+
+
+def compl_model(A, m50, rho) -> ComplModel:
+    """Closed-form Martin2016_complete(m, A, m50, rho)."""
+    return ComplModel(A, m50, rho)
+
+
+def partial_cmd_smooth_batch(m_ini, mags, iso_off, iso_len, y_index, color_indices, err_models,
+                             compl_models, imf, dmod, normalize_value, edges, mean_mass=None,
+                             bias=None, out=None, ctx=None):
+    """Many partial_cmd_smooth calls in one device call (sfh_partial_cmd_smooth_batch_dev).
+
+    m_ini, mags: torch CUDA float64 tensors; mags is (nf, total) with the isochrones of
+    all templates concatenated; iso_off / iso_len (numpy int64 / int32) locate template
+    t.  dmod and normalize_value are scalars or per-template arrays.  Returns (or fills)
+    a CUDA float32 tensor of shape (ntempl, nx*ny): template t's column-major Hess
+    diagram is row t (i.e. the (nbins, ntempl) column-major template matrix)."""
+    import torch
+    ctx = ctx or default_context()
+    nf, total = mags.shape
+    iso_off = np.ascontiguousarray(iso_off, dtype=np.int64)
+    iso_len = np.ascontiguousarray(iso_len, dtype=np.int32)
+    nt = iso_off.size
+    dm = np.ascontiguousarray(np.broadcast_to(np.asarray(dmod, dtype=np.float64), (nt,)))
+    nm = np.ascontiguousarray(np.broadcast_to(np.asarray(normalize_value, dtype=np.float64), (nt,)))
+    (xf, xs, nx), (yf, ys, ny) = _range(edges[0]), _range(edges[1])
+    if out is None:
+        out = torch.empty((nt, nx * ny), dtype=torch.float32, device=m_ini.device)
+    E = (ErrModel * nf)(*err_models)
+    Cm = (ComplModel * nf)(*compl_models)
+    b = None
+    if bias is not None:
+        barr = np.ascontiguousarray(bias, dtype=np.float64)
+        b = barr.ctypes.data
+    ip = imf.params()
+    mm = imf.mean() if mean_mass is None else float(mean_mass)
+    m_ini = m_ini.contiguous()
+    mags = mags.contiguous()
+    # Inputs were produced on torch's stream; the library runs on the context stream.
+    torch.cuda.current_stream(m_ini.device).synchronize()
+    check(load().sfh_partial_cmd_smooth_batch_dev(
+        ctx.handle, m_ini.data_ptr(), mags.data_ptr(), int(total), iso_off.ctypes.data,
+        iso_len.ctypes.data, nt, nf, int(y_index), int(color_indices[0]), int(color_indices[1]),
+        E, Cm, b, C.byref(ip), mm, dm.ctypes.data, nm.ctypes.data, xf, xs, nx, yf, ys, ny,
+        out.data_ptr()), ctx.handle, "partial_cmd_smooth_batch")
+    return out
