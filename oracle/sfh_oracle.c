@@ -539,7 +539,7 @@ static void cum_mass(const double *x, const int64_t *s_idxs, int64_t n, double *
 int sfho_mzr_calculate_coeffs(double alpha, double MH0, double logMstar0, double sigma,
                               const double *mstars, int64_t nages, const double *logAge,
                               const double *MH, int64_t nt, double *coeffs) {
-    double *uniq = (double *)malloc(sizeof(double) * (size_t)nt);
+    double *uniq = (double *)calloc((size_t)nt, sizeof(double));
     int64_t *jidx = (int64_t *)malloc(sizeof(int64_t) * (size_t)nt);
     const int64_t nu = unique_ages(logAge, nt, uniq, jidx);
     if (nu != nages) { free(uniq); free(jidx); return -1; }

@@ -28,7 +28,7 @@ namespace {
 
 constexpr int kStampThreads = 256;
 constexpr int kWarps = kStampThreads / 32;
-constexpr size_t kBandBudget = 96 * 1024;
+constexpr size_t kBandBudget = 110 * 1024;
 
 struct Grid2 {
     double xf, xs, yf, ys;
@@ -50,6 +50,29 @@ __device__ __forceinline__ float erf_diff(float ea, float eb) {
 // Gauss-Legendre 3-point nodes/weights, src/StarFormationHistories.jl:303-304.
 __constant__ float c_glx[3] = {-0.7745966692414834f, 0.0f, 0.7745966692414834f};
 __constant__ float c_glw[3] = {0.5555555555555556f, 0.8888888888888888f, 0.5555555555555556f};
+
+// exp(-z^2) with the rounding error of z*z folded back in (z*z = p + e exactly).
+__device__ __forceinline__ float exp_negsq(float z) {
+    const float p = z * z;
+    const float e = fmaf(z, z, -p);
+    return expf(-p) * (1.0f - e);
+}
+
+// erf(ta + h) - erf(ta) = (2/√π) ∫ exp(-t²) dt over one bin, by 3-point Gauss-Legendre.
+// Relative error < 3e-7 whenever h * max(1, |t|) <= 0.3 (checked against 50-digit erfc).
+__device__ __forceinline__ float gl3_bin(float ta, float h) {
+    const float hh = 0.5f * h, tm = ta + hh, d = 0.7745966692414834f * hh;
+    return 1.1283791670955126f * hh *
+           (0.5555555555555556f * (exp_negsq(tm - d) + exp_negsq(tm + d)) +
+            0.8888888888888888f * exp_negsq(tm));
+}
+
+// Integral of the unit Gaussian kernel over one bin, erf(ta + h) - erf(ta): quadrature
+// for bins narrow against the local scale (no cancellation), erfc differences otherwise.
+__device__ __forceinline__ float gauss_bin(float ta, float h) {
+    if (h * fmaxf(1.0f, fabsf(ta + 0.5f * h)) <= 0.3f) return gl3_bin(ta, h);
+    return erf_diff(erfc_signed(ta), erfc_signed(ta + h));
+}
 
 __device__ __forceinline__ int64_t clamp_cut(double v) { return (int64_t)fmin(v, 4.0e9); }
 
@@ -75,15 +98,9 @@ __device__ void star_asym(float *band, float *bx_buf, float *by_buf, const Grid2
     const float invy = (float)(0.7071067811865476 / ssy);
     const float dx0 = (float)((double)xlo - x0);
     const float dy0 = (float)((double)jlo - y0);
-    for (int m = lane; m < lx; m += 32) {
-        const float ta = (dx0 + (float)m) * invx, tb = (dx0 + (float)(m + 1)) * invx;
-        bx_buf[m] = erf_diff(erfc_signed(ta), erfc_signed(tb));
-    }
+    for (int m = lane; m < lx; m += 32) bx_buf[m] = gauss_bin((dx0 + (float)m) * invx, invx);
     const float a4 = (float)(A * 0.25);
-    for (int m = lane; m < ly; m += 32) {
-        const float ta = (dy0 + (float)m) * invy, tb = (dy0 + (float)(m + 1)) * invy;
-        by_buf[m] = a4 * erf_diff(erfc_signed(ta), erfc_signed(tb));
-    }
+    for (int m = lane; m < ly; m += 32) by_buf[m] = a4 * gauss_bin((dy0 + (float)m) * invy, invy);
     __syncwarp();
     const int total = lx * ly;
     const float inv_lx = 1.0f / (float)lx;
@@ -97,8 +114,8 @@ __device__ void star_asym(float *band, float *bx_buf, float *by_buf, const Grid2
 }
 
 // ---------------------------------------------------------------- covariant star
-__device__ void star_cov(float *band, const Grid2 &g, int ty0, int tyn, double x, double y,
-                         double sx, double sy, double A, float cov, int lane) {
+__device__ void star_cov(float *band, float *rowbuf, const Grid2 &g, int ty0, int tyn, double x,
+                         double y, double sx, double sy, double A, float cov, int lane) {
     if (!(sx >= 0.0 && sy >= 0.0)) return;
     const double xpix = (x - g.xf) / g.xs + 1.0, ypix = (y - g.yf) / g.ys + 1.0;
     if (!(fabs(xpix) < 4.0e15 && fabs(ypix) < 4.0e15)) return;
@@ -127,14 +144,43 @@ __device__ void star_cov(float *band, const Grid2 &g, int ty0, int tyn, double x
     const float invsxf = (float)inv_sx;
     // prefac = A / 2 / sqrt(2π) / σy (:320) times the scaled GL weights w_k * hy (:325)
     const float pref = (float)(A / 2.0 / 2.5066282746310002 / sy * hy);
+    const int nrows = (int)(jhi - jlo + 1);
+    const int row_off = (int)(jlo - ylo);  // first band row's index inside the full window
+    float *band_row0 = band + (int64_t)(jlo - 1 - ty0) * g.nx + (xlo - 1);
+    if (sxr <= 0.05f) {
+        // Narrow bins in t: per-row GL weights c_k and shifts s_k in shared memory, then
+        // every (row, bin) integrates its three sheared x-intervals by quadrature.
+        for (int row = lane; row < nrows; row += 32) {
+            const float dyc = dyb + (float)(row_off + row) * yrsf;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float dy = dyc + c_glx[k] * hyf;
+                rowbuf[6 * row + k] = pref * c_glw[k] * exp_negsq(0.7071067811865476f * dy * inv_sy);
+                rowbuf[6 * row + 3 + k] = cov * dy * invsxf;
+            }
+        }
+        __syncwarp();
+        const int total = nrows * (int)lx;
+        const float inv_lx = 1.0f / (float)lx;
+        for (int p = lane; p < total; p += 32) {
+            const int row = (int)(((float)p + 0.5f) * inv_lx);
+            const int e = p - row * (int)lx;
+            const float tb0 = bx + (float)e * sxr;
+            float v = 0.f;
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                v = fmaf(rowbuf[6 * row + k], gl3_bin(tb0 + rowbuf[6 * row + 3 + k], sxr), v);
+            atomicAdd(band_row0 + (int64_t)row * g.nx + e, v);
+        }
+        __syncwarp();
+        return;
+    }
+    // Wide bins: erfc at the shared bin edges, neighbours exchanged by shuffles.
     const int E = (int)lx + 1;  // edges per row
     const int W = E <= 32 ? E : 32;
     const int rows_per = 32 / W;
     const int nb = W - 1;  // bins per segment pass
     const int seg = lane / W, pos = lane - (lane / W) * W;
-    const int nrows = (int)(jhi - jlo + 1);
-    const int row_off = (int)(jlo - ylo);  // first band row's index inside the full window
-    float *band_row0 = band + (int64_t)(jlo - 1 - ty0) * g.nx + (xlo - 1);
     for (int rb = 0; rb < nrows; rb += rows_per) {
         const int row = rb + seg;
         const bool vrow = (seg < rows_per) && (row < nrows);
@@ -144,8 +190,7 @@ __device__ void star_cov(float *band, const Grid2 &g, int ty0, int tyn, double x
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 const float dy = dyc + c_glx[k] * hyf;
-                const float z = dy * inv_sy;
-                ck[k] = pref * c_glw[k] * __expf(-0.5f * z * z);
+                ck[k] = pref * c_glw[k] * exp_negsq(0.7071067811865476f * dy * inv_sy);
                 sk[k] = cov * dy * invsxf;
             }
         }
@@ -182,7 +227,7 @@ k_stamps(const double *__restrict__ xs, const double *__restrict__ ys,
     float *band = smem;
     const int bandn = tyn * g.nx;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float *wb = smem + (size_t)TY * g.nx + (size_t)warp * (g.nx + TY);
+    float *wb = smem + (size_t)TY * g.nx + (size_t)warp * (g.nx + 6 * TY);
     __shared__ int s_next;
     for (int k = threadIdx.x; k < bandn; k += blockDim.x) band[k] = 0.f;
     if (threadIdx.x == 0) s_next = 0;
@@ -199,7 +244,7 @@ k_stamps(const double *__restrict__ xs, const double *__restrict__ ys,
         if (cov == 0)
             star_asym(band, wb, wb + g.nx, g, ty0, tyn, xs[s], ys[s], sxs[s], sys[s], ws[s], lane);
         else
-            star_cov(band, g, ty0, tyn, xs[s], ys[s], sxs[s], sys[s], ws[s], (float)cov, lane);
+            star_cov(band, wb, g, ty0, tyn, xs[s], ys[s], sxs[s], sys[s], ws[s], (float)cov, lane);
     }
     __syncthreads();
     float *dst = out + (int64_t)t * ((int64_t)g.nx * g.ny) + (int64_t)ty0 * g.nx;
@@ -405,10 +450,18 @@ k_iso_stars(const double *__restrict__ m_ini, const double *__restrict__ mags,
     }
 }
 
+// Shared memory of one k_stamps CTA: the FP32 band (TY x nx) plus per-warp buffers
+// (nx + 6 TY floats: the x/y factor tables of the separable kernel, or the per-row
+// Gauss-Legendre weights and shifts of the covariant kernel).
+size_t stamp_smem(int64_t nx, int64_t TY) {
+    return ((size_t)TY * nx + (size_t)kWarps * (nx + 6 * TY)) * sizeof(float);
+}
+
+// Band height: as many rows as fit in ~110 KB (two CTAs per SM), balanced over tiles.
 int band_rows(int64_t nx, int64_t ny) {
-    const size_t row_bytes = (size_t)nx * sizeof(float);
-    int64_t tymax = (int64_t)(kBandBudget / row_bytes);
-    if (tymax < 1) tymax = 1;
+    int64_t tymax = 0;
+    while (tymax < ny && stamp_smem(nx, tymax + 1) <= kBandBudget) ++tymax;
+    if (tymax < 1) return 0;
     const int64_t ntiles = (ny + tymax - 1) / tymax;
     return (int)((ny + ntiles - 1) / ntiles);
 }
@@ -421,12 +474,12 @@ int sfh_launch_stamps(sfh_ctx *ctx, const double *d_x, const double *d_y, const 
                       double xs, int64_t nx, double yf, double ys, int64_t ny, float *d_out) {
     if (nx < 1 || ny < 1 || nx > (1 << 20) || ny > (1 << 20) || ntempl < 1 || ntempl > 65535)
         return sfh_set_error(ctx, SFH_ERR_ARG, "stamp grid or template count out of range");
-    if ((size_t)nx * sizeof(float) > kBandBudget)
-        return sfh_set_error(ctx, SFH_ERR_UNSUPPORTED, "nx too large for one shared-memory row");
-    Grid2 g{xf, xs, yf, ys, (int)nx, (int)ny};
     const int TY = band_rows(nx, ny);
+    if (TY < 1)
+        return sfh_set_error(ctx, SFH_ERR_UNSUPPORTED, "Hess grid too wide for a shared-memory band");
+    Grid2 g{xf, xs, yf, ys, (int)nx, (int)ny};
     const int ntiles = (int)((ny + TY - 1) / TY);
-    const size_t smem = ((size_t)TY * nx + (size_t)kWarps * (nx + TY)) * sizeof(float);
+    const size_t smem = stamp_smem(nx, TY);
     static thread_local bool attr_set = false;
     if (!attr_set) {
         SFH_CK(ctx, cudaFuncSetAttribute(k_stamps, cudaFuncAttributeMaxDynamicSharedMemorySize,

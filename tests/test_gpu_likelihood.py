@@ -56,7 +56,11 @@ def test_reference_kats(sfh, kats, T, ri):
 
 
 def test_zero_sum_is_minus_inf(sfh):
-    assert sfh.loglikelihood(np.zeros(5), np.zeros(5)) == -np.inf
+    # Every term n - c - n log(n/c) is exactly 0 when n == c == 1, so the sum is 0 and the
+    # reference returns -typemax(T) = -Inf (fitting_base.jl:95).  Zero composites are
+    # clamped to eps and do not sum to zero.
+    assert sfh.loglikelihood(np.ones(5), np.ones(5)) == -np.inf
+    assert sfh.loglikelihood(np.zeros(5), np.zeros(5)) == pytest.approx(-5 * np.finfo(float).eps)
 
 
 def _problem(nbins, nt, seed, n_stars=1e4, zero_frac=0.2):

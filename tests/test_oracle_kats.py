@@ -47,7 +47,7 @@ def test_loglikelihood(O, kats, T, ri):
 
 def test_loglikelihood_zero_sum_is_minus_inf(O):
     # loglikelihood returns -typemax(T) when the sum is exactly zero, fitting_base.jl:95
-    assert O.loglikelihood(np.zeros(4), np.zeros(4), 0.0) == -np.inf
+    assert O.loglikelihood(np.ones(4), np.ones(4)) == -np.inf
 
 
 def test_gradients(O):
