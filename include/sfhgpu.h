@@ -118,6 +118,21 @@ int sfh_fg_kernel_times(sfh_ctx *ctx, const sfh_models *models, const double *d_
                         const double *d_data, double *d_composite, double *d_G,
                         double *d_negLogL, double eps, int iters, double *ms_out);
 
+/* fg! for callers that cannot allocate device memory (no counterpart in the
+   reference): graph-capture regions that must not allocate, plugins inside a host
+   application that owns the device memory budget, allocation-free real-time loops.
+   Same result as sfh_fg_dev on FP32 templates, but all scratch lives in one fixed
+   11 MiB device array inside the library, so the call allocates nothing: the caller
+   passes the (nbins, ntempl) column-major FP32 templates, every input and output,
+   and the stream.  Limits: nbins <= 131072 and ntempl <= 4096 (SFH_ERR_SHAPE beyond).
+   The first call on each device looks up the array's device address; make that
+   first call before any stream capture.  All calls share the one array, so calls
+   that overlap on the GPU (different streams, or different host threads) race:
+   serialise them on one stream.  d_G and d_negLogL may be NULL as in sfh_fg_dev. */
+int sfh_fg_dev_noalloc(void *stream, const float *d_models, int64_t nbins, int64_t ntempl,
+                       const double *d_coeffs, const double *d_data, double *d_composite,
+                       double *d_G, double *d_negLogL, double eps);
+
 /* B coefficient vectors in one call (HMC chains, line-search probes):
    d_R[b*ntempl + j] -> d_negLogL[b] (may be NULL: gradient-only substeps skip the
    logarithms) and d_G[b*ntempl + j] = -∂logL/∂r (may be NULL).  Needs models

@@ -524,3 +524,126 @@ int sfh_launch_loglikelihood(sfh_ctx *ctx, const double *composite, const double
     SFH_LAUNCHED(ctx);
     return SFH_OK;
 }
+
+// ---------------------------------------------------------------- allocation-free fg!
+// Some callers cannot call cudaMalloc at all: code running inside a CUDA-graph
+// capture that must not allocate, plugins living inside a host application that
+// owns the device memory budget (and forbids side allocations), or real-time loops
+// where an allocation could stall.  sfh_fg_dev_noalloc serves them: it runs the same
+// four kernels as sfh_fg_dev, but its scratch is this fixed, file-scope device array,
+// so the call itself allocates nothing.  The array is 11 MiB and is held by every GPU
+// that loads the library until the process exits.
+namespace {
+constexpr int64_t kNoAllocMaxBins = 131072;  // e.g. a 362 x 362 Hess grid
+constexpr int64_t kNoAllocMaxTempl = 4096;
+constexpr int kNoAllocMaxSplit = 8;
+constexpr size_t kNoAllocBytes = 11u << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[64] = {nullptr};
+}  // namespace
+
+extern "C" int sfh_fg_dev_noalloc(void *stream, const float *d_models, int64_t nbins,
+                                  int64_t ntempl, const double *d_coeffs, const double *d_data,
+                                  double *d_composite, double *d_G, double *d_negLogL,
+                                  double eps) {
+    if (!d_models || !d_coeffs || !d_data || !d_composite || nbins < 1 || ntempl < 1)
+        return SFH_ERR_ARG;
+    if (nbins > kNoAllocMaxBins || ntempl > kNoAllocMaxTempl)
+        return SFH_ERR_SHAPE;  // beyond the fixed scratch: use sfh_fg_dev instead
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return SFH_ERR_CUDA;
+    void *base = nullptr;
+    {
+        // First call on this device: resolve the device address of the array (the
+        // host-side symbol is only a stand-in).  Make that first call outside any
+        // stream capture.
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            if (cudaGetSymbolAddress(&g_noalloc_ptr[dev], g_noalloc_scratch) != cudaSuccess) {
+                g_noalloc_ptr[dev] = nullptr;
+                return SFH_ERR_CUDA;
+            }
+        }
+        base = g_noalloc_ptr[dev];
+    }
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return SFH_ERR_CUDA;
+    cudaStream_t st = (cudaStream_t)stream;
+    // Launch plan as in make_plan, with the template split capped so the partials fit.
+    const int rows_per_block = 4 * kThreads;
+    const int nrowblk = (int)((nbins + rows_per_block - 1) / rows_per_block);
+    const int target = sms * 6;
+    int ks = (target + nrowblk - 1) / nrowblk;
+    ks = ks < 1 ? 1 : (ks > kNoAllocMaxSplit ? kNoAllocMaxSplit : ks);
+    if (ks > ntempl) ks = (int)ntempl;
+    const int kchunk = (int)((ntempl + ks - 1) / ks);
+    const int ksplit = (int)((ntempl + kchunk - 1) / kchunk);
+    const int R = 4096;
+    const int nchunks = (int)((nbins + R - 1) / R);
+    int groups = (target + nchunks - 1) / nchunks;
+    if (groups < 1) groups = 1;
+    int cb = (int)((ntempl + groups - 1) / groups);
+    cb = ((cb + 7) / 8) * 8;
+    const int ncolgroups = (int)((ntempl + cb - 1) / cb);
+    const int nfin = (int)((nbins + kThreads - 1) / kThreads);
+    const size_t off_part = 0;
+    const size_t off_w = sfh_align256((size_t)ksplit * nbins * sizeof(double));
+    const size_t off_partG = off_w + sfh_align256((size_t)nbins * sizeof(float2));
+    const size_t off_logl = off_partG + sfh_align256((size_t)nchunks * ntempl * sizeof(double));
+    const size_t off_cnt = off_logl + sfh_align256((size_t)nfin * sizeof(double));
+    if (off_cnt + 256 > kNoAllocBytes) return SFH_ERR_SHAPE;
+    char *s = (char *)base;
+    double *part = (double *)(s + off_part);
+    float2 *w32 = (float2 *)(s + off_w);
+    double *partG = (double *)(s + off_partG);
+    double *logl_part = (double *)(s + off_logl);
+    unsigned int *counter = (unsigned int *)(s + off_cnt);
+    // The array keeps the previous call's contents: the reduction counter must start at 0.
+    if (cudaMemsetAsync(counter, 0, sizeof(unsigned int), st) != cudaSuccess) return SFH_ERR_CUDA;
+
+    dim3 grid(nrowblk, ksplit);
+    const size_t sm_n = 2 * (size_t)kchunk * sizeof(float);
+    if (nbins % 4 == 0)
+        k_gemv_n_f32<true><<<grid, kThreads, sm_n, st>>>(d_models, nbins, ntempl, d_coeffs, kchunk,
+                                                         part);
+    else
+        k_gemv_n_f32<false><<<grid, kThreads, sm_n, st>>>(d_models, nbins, ntempl, d_coeffs,
+                                                          kchunk, part);
+    if (cudaGetLastError() != cudaSuccess) return SFH_ERR_CUDA;
+    const bool want_g = d_G != nullptr;
+    FinArgs fa{};
+    fa.part = part;
+    fa.ksplit = ksplit;
+    fa.nbins = nbins;
+    fa.data = d_data;
+    fa.eps = eps;
+    fa.composite = d_composite;
+    fa.w32 = want_g ? w32 : nullptr;
+    fa.w64 = nullptr;
+    fa.want_logl = d_negLogL ? 1 : 0;
+    fa.want_w = want_g ? 1 : 0;
+    fa.write_m = 1;
+    fa.logl_part = logl_part;
+    fa.counter = counter;
+    fa.negLogL = d_negLogL;
+    fa.logl_sign = 1.0;
+    k_finalize<<<nfin, kThreads, 0, st>>>(fa);
+    if (cudaGetLastError() != cudaSuccess) return SFH_ERR_CUDA;
+    if (!want_g) return SFH_OK;
+    dim3 gridt(ncolgroups, nchunks);
+    const size_t sm_t = 2 * (size_t)R * sizeof(float);
+    if (nbins % 4 == 0)
+        k_gemv_t_f32<true><<<gridt, kThreads, sm_t, st>>>(d_models, nbins, ntempl, w32, R, cb,
+                                                          ncolgroups, partG);
+    else
+        k_gemv_t_f32<false><<<gridt, kThreads, sm_t, st>>>(d_models, nbins, ntempl, w32, R, cb,
+                                                           ncolgroups, partG);
+    if (cudaGetLastError() != cudaSuccess) return SFH_ERR_CUDA;
+    k_reduce_g<<<(int)((ntempl + kThreads - 1) / kThreads), kThreads, 0, st>>>(partG, nchunks,
+                                                                                ntempl, 1.0, d_G);
+    if (cudaGetLastError() != cudaSuccess) return SFH_ERR_CUDA;
+    return SFH_OK;
+}
