@@ -242,7 +242,13 @@ def run_ours(args):
     L = sfhgpu.load()
     tstream = ctx.torch_stream()
     w = S.config2()
+    if args.ntempl != NT:
+        # profiling case: the first ntempl templates of the production grid
+        nages = max(1, args.ntempl // w.MHs.size)
+        w.logAges = w.logAges[:nages]
+        w.name = f"config2 grid, {w.ntempl} templates (profiling case)"
     nx, ny = w.grid
+    NTW = w.ntempl
 
     # ---- template build (partial_cmd_smooth on the GPU), templates/s
     m_ini, mags, offs, lens = S.isochrone_batch(w)
@@ -269,14 +275,14 @@ def run_ours(args):
     templates_per_s = w.ntempl / (build_ms / 1e3)
 
     # ---- template matrix handle (FP32 storage) and observed data
-    H = sfhgpu.Models.from_device(d_T.data_ptr(), NBINS, NT, storage="f32", ctx=ctx)
+    H = sfhgpu.Models.from_device(d_T.data_ptr(), NBINS, NTW, storage="f32", ctx=ctx)
     M32 = d_T.cpu().numpy()          # (nt, nbins) row-major == (nbins, nt) column-major
     M64 = np.asfortranarray(M32.T.astype(np.float64))
     r, data = S.observed(M64, w.n_stars, seed=w.seed)
     d_r = torch.tensor(r, device=dev)
     d_n = torch.tensor(data, device=dev)
     d_c = torch.empty(NBINS, dtype=torch.float64, device=dev)
-    d_G = torch.empty(NT, dtype=torch.float64, device=dev)
+    d_G = torch.empty(NTW, dtype=torch.float64, device=dev)
     d_L = torch.empty(1, dtype=torch.float64, device=dev)
     torch.cuda.synchronize()
     eps = float(np.finfo(np.float64).eps)
@@ -317,11 +323,13 @@ def run_ours(args):
     sfhgpu._lib.check(L.sfh_fg_kernel_times(ctx.handle, H.handle, d_r.data_ptr(), d_n.data_ptr(),
                                             d_c.data_ptr(), d_G.data_ptr(), d_L.data_ptr(), eps,
                                             50, kms), ctx.handle, "sfh_fg_kernel_times")
-    names = ["k_gemv_n_f32", "k_finalize", "k_gemv_t_f32", "k_reduce_g"]
-    alg = [NBINS * NT * 4 + NT * 8 + NBINS * 8,      # M, r, m
+    # FP32 storage runs two fused kernels: [0] pass 1 (m, logL, w), [2] pass 2 (G);
+    # slots [1] and [3] stay empty.
+    names = ["k_fg_pass1_f32", "(fused into pass 1)", "k_fg_pass2_f32", "(fused into pass 2)"]
+    alg = [NBINS * NTW * 4 + NTW * 8 + NBINS * 8,    # M, r, m
            NBINS * 8 * 3,                            # m, n, w
-           NBINS * NT * 4 + NBINS * 8 + NT * 8,      # M, w, G
-           NT * 8]
+           NBINS * NTW * 4 + NBINS * 8 + NTW * 8,    # M, w, G
+           NTW * 8]
     k = max(range(4), key=lambda i: kms[i])
     peak, peak_kind = _peaks()
     achieved = alg[k] / (kms[k] * 1e-3) / 1e9
@@ -333,7 +341,7 @@ def run_ours(args):
 
     # ---- end to end through the host-array C ABI (sfh_fg)
     comp = np.empty(NBINS)
-    G = np.empty(NT)
+    G = np.empty(NTW)
     h_r = r.copy()
     h_n = data.copy()
     for _ in range(3):
@@ -344,8 +352,8 @@ def run_ours(args):
     for _ in range(ne2e):
         sfhgpu.fg_(True, G, h_r, H, h_n, comp)
     e2e_s = _max_over_ranks(world, time.perf_counter() - t0)
-    e2e = {"value": world * ne2e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": (NT + NBINS) * 8,
-           "d2h_bytes_per_step": (NBINS + NT + 1) * 8, "steps": ne2e}
+    e2e = {"value": world * ne2e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": (NTW + NBINS) * 8,
+           "d2h_bytes_per_step": (NBINS + NTW + 1) * 8, "steps": ne2e}
 
     # ---- CPU baseline (rank 0, N = 1 only): the oracle on the same inputs
     cpu = None
@@ -364,7 +372,8 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (compensated) + f64 logL",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "nbins": NBINS, "ntempl": NT, "storage": "f32",
+            "config": {"workload": WORKLOAD if NTW == NT else w.name, "nbins": NBINS,
+                       "ntempl": NTW, "storage": "f32",
                        "l2": "inputs larger than L2 (288 MB template matrix)",
                        "parallelism": f"replicas x{world}"},
             "templates_per_s": templates_per_s, "template_build_ms": build_ms,
@@ -386,6 +395,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--ntempl", type=int, default=NT,
+                    help="templates (multiple of 30); fewer than 1200 only for profiling")
     ap.add_argument("--cpu-budget-s", type=float, default=10.0)
     ap.add_argument("--reference-budget-s", type=float, default=60.0)
     args = ap.parse_args()

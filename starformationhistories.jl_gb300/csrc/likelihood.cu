@@ -35,6 +35,49 @@ __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float x) {
     lo = __fadd_rn(lo, err);
 }
 
+// 16-byte streaming load issued in program order with its neighbours (volatile keeps a
+// batch of these in flight together instead of interleaving them with the FMAs).
+__device__ __forceinline__ float4 ld_stream4(const float *p) {
+    float4 v;
+    asm volatile("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "l"(p));
+    return v;
+}
+
+// Poisson term of an occupied bin, n - c - n log(n/c) (fitting_base.jl:93), in the form
+//   n (log1p(d) - d),  d = (c - n)/n,  z = (c - n)/(c + n),
+//   log1p(d) - d = -d z + 2 z^3 (1/3 + z^2/5 + z^4/7 + ...)   (log1p(d) = 2 atanh z)
+// so the term is  L + C  with  L = -(c - n)^2/(c + n)  formed in FP64 from a
+// double-float quotient (a handful of FP64 operations) and the small remainder
+// C = 2 n z^3 S(z^2) in FP32.  Bins far from their model (|d| > 1/2) take one FP64
+// log instead.  FP64 throughput on this part is a small fraction of FP32, so the
+// series path keeps FP64 work per bin to five operations.
+__device__ __forceinline__ double poisson_term_occupied(double c, double n) {
+    const double diff = c - n;
+    const float df = (float)diff, nf = (float)n;
+    const float d = __fdiv_rn(df, nf);
+    if (fabsf(d) <= 0.5f) {
+        const double sum = c + n;
+        const float sf = (float)sum;
+        const float q0 = __fdiv_rn(df, sf);
+        const double r = fma(-(double)q0, sum, diff);
+        const float q1 = __fdiv_rn((float)r, sf);
+        const double L = -diff * ((double)q0 + (double)q1);
+        const float z = q0 + q1, z2 = z * z;
+        float S = 1.0f / 17.0f;
+        S = fmaf(S, z2, 1.0f / 15.0f);
+        S = fmaf(S, z2, 1.0f / 13.0f);
+        S = fmaf(S, z2, 1.0f / 11.0f);
+        S = fmaf(S, z2, 1.0f / 9.0f);
+        S = fmaf(S, z2, 1.0f / 7.0f);
+        S = fmaf(S, z2, 1.0f / 5.0f);
+        S = fmaf(S, z2, 1.0f / 3.0f);
+        return L + (double)(2.0f * nf * z * z2 * S);
+    }
+    return n * log(c / n) - diff;
+}
+
 // ---------------------------------------------------------------- k_gemv_n (FP32 storage)
 template <bool VEC>
 __global__ void __launch_bounds__(kThreads)
@@ -342,29 +385,348 @@ __global__ void k_reduce_g(const double *__restrict__ partG, int nchunks, int64_
     G[j] = sign * acc;
 }
 
+
+// ---------------------------------------------------------------- fused pass 1 (FP32 storage)
+// m partials over template splits (register double-buffered loads).  The last split
+// block to finish a row tile sums its rows' partials in split order, forms the FP64
+// Poisson terms and w, and the last row tile sums the per-tile logL partials in tile
+// order, so every result is deterministic.
+struct Pass1Args {
+    const float *M;
+    int64_t nbins, nt;
+    const double *r;
+    int kchunk;
+    float2 *part;  // (hi, lo) partial sums, ksplit x nbins
+    const double *data;
+    double eps;
+    double *composite;
+    float2 *w32;
+    int want_logl, want_w;
+    double *tile_logl;
+    unsigned int *tile_cnt;
+    unsigned int *all_cnt;
+    double *negLogL;
+};
+
+__device__ __forceinline__ void block_sum_to(double v, double *s_red, double *out_tid0) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += s_red[w];
+        *out_tid0 = b;
+    }
+}
+
+template <bool VEC>
+__global__ void __launch_bounds__(kThreads) k_fg_pass1_f32(Pass1Args a) {
+    extern __shared__ float s_r[];
+    float *rhi = s_r, *rlo = s_r + a.kchunk;
+    __shared__ double s_red[kThreads / 32];
+    __shared__ bool s_last;
+    // Grid: x = template split (fastest), y = row tile, so row tiles complete one after
+    // another and their finalisation overlaps the streaming of later tiles.
+    const int split = blockIdx.x, tile = blockIdx.y;
+    const int nsplit = gridDim.x, ntile = gridDim.y;
+    const int64_t j0 = (int64_t)split * a.kchunk;
+    const int kn = (int)min((int64_t)a.kchunk, a.nt - j0);
+    for (int t = threadIdx.x; t < kn; t += blockDim.x) {
+        const double v = a.r[j0 + t];
+        const float h = __double2float_rn(v);
+        rhi[t] = h;
+        rlo[t] = __double2float_rn(v - (double)h);
+    }
+    __syncthreads();
+    const int64_t nbins = a.nbins;
+    const int64_t i = ((int64_t)tile * blockDim.x + threadIdx.x) * 4;
+    if (i < nbins) {
+        float ah[4] = {0.f, 0.f, 0.f, 0.f}, al[4] = {0.f, 0.f, 0.f, 0.f};
+        const float *colp = a.M + j0 * nbins + i;
+        int k = 0;
+        if (VEC) {
+            for (; k + 8 <= kn; k += 8) {
+                float4 v[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) v[u] = ld_stream4(colp + (int64_t)(k + u) * nbins);
+                float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const float h = rhi[k + u], l = rlo[k + u];
+                    s0 = fmaf(v[u].x, h, fmaf(v[u].x, l, s0));
+                    s1 = fmaf(v[u].y, h, fmaf(v[u].y, l, s1));
+                    s2 = fmaf(v[u].z, h, fmaf(v[u].z, l, s2));
+                    s3 = fmaf(v[u].w, h, fmaf(v[u].w, l, s3));
+                }
+                two_sum_acc(ah[0], al[0], s0);
+                two_sum_acc(ah[1], al[1], s1);
+                two_sum_acc(ah[2], al[2], s2);
+                two_sum_acc(ah[3], al[3], s3);
+            }
+            for (; k < kn; ++k) {
+                const float4 x = __ldg(reinterpret_cast<const float4 *>(colp + (int64_t)k * nbins));
+                const float h = rhi[k], l = rlo[k];
+                two_sum_acc(ah[0], al[0], fmaf(x.x, h, x.x * l));
+                two_sum_acc(ah[1], al[1], fmaf(x.y, h, x.y * l));
+                two_sum_acc(ah[2], al[2], fmaf(x.z, h, x.z * l));
+                two_sum_acc(ah[3], al[3], fmaf(x.w, h, x.w * l));
+            }
+            float2 *dst = a.part + (int64_t)split * nbins + i;
+            *reinterpret_cast<float4 *>(dst) = make_float4(ah[0], al[0], ah[1], al[1]);
+            *reinterpret_cast<float4 *>(dst + 2) = make_float4(ah[2], al[2], ah[3], al[3]);
+        } else {
+            const int nr = (int)min((int64_t)4, nbins - i);
+            for (; k < kn; ++k) {
+                const float h = rhi[k], l = rlo[k];
+                const float *c = colp + (int64_t)k * nbins;
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (q < nr) {
+                        const float x = __ldg(c + q);
+                        two_sum_acc(ah[q], al[q], fmaf(x, h, x * l));
+                    }
+            }
+            float2 *dst = a.part + (int64_t)split * nbins + i;
+            for (int q = 0; q < nr; ++q) dst[q] = make_float2(ah[q], al[q]);
+        }
+    }
+    // ---- the last split block of this row tile finalises the tile's rows
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned int tk = atomicAdd(&a.tile_cnt[tile], 1u);
+        s_last = (tk == nsplit - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const int ks = nsplit;
+    const int64_t rbase = (int64_t)tile * blockDim.x * 4;
+    double term = 0.0;
+    for (int q = 0; q < 4; ++q) {
+        const int64_t ii = rbase + (int64_t)q * blockDim.x + threadIdx.x;
+        if (ii >= nbins) continue;
+        float mh = 0.f, ml = 0.f;
+        int sp = 0;
+        for (; sp + 16 <= ks; sp += 16) {
+            float2 v[16];
+#pragma unroll
+            for (int u = 0; u < 16; ++u) v[u] = __ldcg(a.part + (int64_t)(sp + u) * nbins + ii);
+#pragma unroll
+            for (int u = 0; u < 16; ++u) {
+                two_sum_acc(mh, ml, v[u].x);
+                ml += v[u].y;
+            }
+        }
+        for (; sp < ks; ++sp) {
+            const float2 v = __ldcg(a.part + (int64_t)sp * nbins + ii);
+            two_sum_acc(mh, ml, v.x);
+            ml += v.y;
+        }
+        const double m = (double)mh + (double)ml;
+        if (!a.want_logl && !a.want_w) {  // composite only: data may be NULL
+            a.composite[ii] = m;
+            continue;
+        }
+        const double ci = m > a.eps ? m : a.eps;
+        const double ni = a.data[ii];
+        if (a.want_logl) term += (ni > 0.0) ? poisson_term_occupied(ci, ni) : -ci;
+        if (a.want_w) {
+            const float w = __fdiv_rn((float)(ci - ni), (float)ci);  // 1 - n/c
+            a.composite[ii] = (double)w;
+            a.w32[ii] = make_float2(w, 0.f);
+        } else {
+            a.composite[ii] = m;
+        }
+    }
+    double tile_sum = 0.0;
+    block_sum_to(term, s_red, &tile_sum);
+    if (threadIdx.x == 0) {
+        a.tile_cnt[tile] = 0u;  // re-arm for the next launch on this stream
+        s_last = false;
+        if (a.want_logl) {
+            a.tile_logl[tile] = tile_sum;
+            __threadfence();
+            const unsigned int tk = atomicAdd(a.all_cnt, 1u);
+            s_last = (tk == ntile - 1);
+        }
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    double acc = 0.0;
+    for (int b = threadIdx.x; b < ntile; b += blockDim.x) acc += __ldcg(a.tile_logl + b);
+    double tot = 0.0;
+    block_sum_to(acc, s_red, &tot);
+    if (threadIdx.x == 0) {
+        // loglikelihood returns -typemax(T) = -Inf when the sum is exactly zero (fitting_base.jl:95)
+        const double logl = (tot != 0.0) ? tot : -INFINITY;
+        if (a.negLogL) *a.negLogL = -logl;
+        *a.all_cnt = 0u;
+    }
+}
+
+// ---------------------------------------------------------------- fused pass 2 (FP32 storage)
+// G partials over row chunks (w staged in shared memory); the last row-chunk block of a
+// column group sums that group's partials in chunk order.
+struct Pass2Args {
+    const float *M;
+    int64_t nbins, nt;
+    const float2 *w;
+    int R, CB, ncolgroups;
+    double *partG;
+    unsigned int *grp_cnt;
+    double gsign;
+    double *G;
+};
+
+template <bool VEC>
+__global__ void __launch_bounds__(kThreads) k_fg_pass2_f32(Pass2Args a) {
+    extern __shared__ float s_w[];
+    __shared__ bool s_last;
+    const int R = a.R;
+    // Last row chunk first: pass 1 streamed the last row tiles most recently.
+    const int rc = (int)gridDim.y - 1 - (int)blockIdx.y;
+    const int64_t nbins = a.nbins, nt = a.nt;
+    const int64_t i0 = (int64_t)rc * R;
+    const int rn = (int)min((int64_t)R, nbins - i0);
+    for (int t = threadIdx.x; t < R; t += blockDim.x) s_w[t] = (t < rn) ? a.w[i0 + t].x : 0.f;
+    __syncthreads();
+    const int g = a.ncolgroups - 1 - (int)blockIdx.x;
+    const int64_t jb = (int64_t)g * a.CB;
+    const int64_t je = min(nt, jb + a.CB);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int64_t j = je - 1 - warp; j >= jb; j -= kThreads / 32) {
+        const float *col = a.M + j * nbins + i0;
+        float ah = 0.f, al = 0.f;
+        if (VEC) {
+            int ii = lane * 4;
+            for (; ii + 896 < rn; ii += 1024) {
+                float4 m[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) m[u] = ld_stream4(col + ii + 128 * u);
+                float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const float4 h = *reinterpret_cast<const float4 *>(s_w + ii + 128 * u);
+                    float &sx = (u & 1) ? s1 : s0;
+                    sx = fmaf(m[u].x, h.x, sx);
+                    sx = fmaf(m[u].y, h.y, sx);
+                    sx = fmaf(m[u].z, h.z, sx);
+                    sx = fmaf(m[u].w, h.w, sx);
+                }
+                two_sum_acc(ah, al, s0);
+                two_sum_acc(ah, al, s1);
+            }
+            for (; ii < rn; ii += 128) {
+                const float4 mv = ld_stream4(col + ii);
+                const float4 h = *reinterpret_cast<const float4 *>(s_w + ii);
+                float sx = mv.x * h.x;
+                sx = fmaf(mv.y, h.y, sx);
+                sx = fmaf(mv.z, h.z, sx);
+                sx = fmaf(mv.w, h.w, sx);
+                two_sum_acc(ah, al, sx);
+            }
+        } else {
+            for (int ii = lane; ii < rn; ii += 32) two_sum_acc(ah, al, __ldg(col + ii) * s_w[ii]);
+        }
+        double v = (double)ah + (double)al;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) a.partG[(int64_t)rc * nt + j] = v;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned int tk = atomicAdd(&a.grp_cnt[g], 1u);
+        s_last = (tk == gridDim.y - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const int nch = (int)gridDim.y;
+    for (int64_t j = jb + threadIdx.x; j < je; j += blockDim.x) {
+        double acc = 0.0;
+        int c = 0;
+        for (; c + 8 <= nch; c += 8) {
+            double v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = __ldcg(a.partG + (int64_t)(c + u) * nt + j);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) acc += v[u];
+        }
+        for (; c < nch; ++c) acc += __ldcg(a.partG + (int64_t)c * nt + j);
+        a.G[j] = a.gsign * acc;
+    }
+    if (threadIdx.x == 0) a.grp_cnt[g] = 0u;
+}
+
 struct Plan {
     int ksplit, kchunk, nrowblk;
     int R, CB, ncolgroups, nchunks;
     size_t off_part, off_w, off_partG, off_logl, total;
 };
 
-Plan make_plan(const sfh_ctx *ctx, int64_t nbins, int64_t nt, bool f64) {
+// Row chunk of the fused pass 2 (w staged in shared memory as FP32).
+constexpr int kFusedR = 2048;
+
+// Resident blocks per SM of the fused kernels (queried once per process).
+struct FusedOcc {
+    int p1 = 0, p2 = 0;
+};
+FusedOcc fused_occupancy(bool vec) {
+    static FusedOcc cache[2];
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lk(mu);
+    FusedOcc &c = cache[vec ? 1 : 0];
+    if (c.p1 == 0) {
+        int a = 0, b = 0;
+        if (vec) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_fg_pass1_f32<true>, kThreads, 8192);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fg_pass2_f32<true>, kThreads,
+                                                          kFusedR * sizeof(float));
+        } else {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_fg_pass1_f32<false>, kThreads, 8192);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fg_pass2_f32<false>, kThreads,
+                                                          kFusedR * sizeof(float));
+        }
+        c.p1 = a > 0 ? a : 1;
+        c.p2 = b > 0 ? b : 1;
+    }
+    return c;
+}
+
+Plan make_plan(const sfh_ctx *ctx, int64_t nbins, int64_t nt, bool f64, bool fused = false) {
     Plan p{};
     const int rows_per_block = f64 ? 2 * kThreads : 4 * kThreads;
     p.nrowblk = (int)((nbins + rows_per_block - 1) / rows_per_block);
     const int target = ctx->sm_count * 6;
     int ks = (target + p.nrowblk - 1) / p.nrowblk;
+    p.R = f64 ? 2048 : 4096;
+    p.nchunks = (int)((nbins + p.R - 1) / p.R);
+    int groups = (target + p.nchunks - 1) / p.nchunks;
+    if (fused) {
+        // Pass 1: two whole waves of resident blocks.  Pass 2: 2,048-row chunks, column
+        // groups of a multiple of 8 (every warp busy) sized to about one wave.
+        const FusedOcc occ = fused_occupancy(nbins % 4 == 0);
+        const int slots1 = occ.p1 * ctx->sm_count, slots2 = occ.p2 * ctx->sm_count;
+        ks = (2 * slots1 + p.nrowblk / 2) / p.nrowblk;
+        p.R = kFusedR;
+        p.nchunks = (int)((nbins + p.R - 1) / p.R);
+        const double per_block = (double)nt * p.nchunks / (double)slots2;
+        const int cb8 = 8 * (int)ceil(per_block / 8.0);
+        groups = (int)((nt + cb8 - 1) / cb8);
+    }
     if (ks < 1) ks = 1;
     if (ks > 64) ks = 64;
     if (ks > nt) ks = (int)nt;
     p.kchunk = (int)((nt + ks - 1) / ks);
     p.ksplit = (int)((nt + p.kchunk - 1) / p.kchunk);
-    p.R = f64 ? 2048 : 4096;
-    p.nchunks = (int)((nbins + p.R - 1) / p.R);
-    int groups = (target + p.nchunks - 1) / p.nchunks;
     if (groups < 1) groups = 1;
     int cb = (int)((nt + groups - 1) / groups);
-    cb = ((cb + 7) / 8) * 8;
+    if (!fused) cb = ((cb + 7) / 8) * 8;
     p.CB = cb;
     p.ncolgroups = (int)((nt + cb - 1) / cb);
     const int nfin = (int)((nbins + kThreads - 1) / kThreads);
@@ -383,7 +745,8 @@ int sfh_launch_fg(sfh_ctx *ctx, const sfh_models *m, const FgArgs &a, cudaEvent_
     const void *Mptr = f64 ? m->d_col : (const void *)m->d_f32;
     if (!Mptr) return sfh_set_error(ctx, SFH_ERR_ARG, "models handle has no matrix");
     const int64_t nbins = m->nbins, nt = m->nt;
-    const Plan p = make_plan(ctx, nbins, nt, f64);
+    const bool fused_path = !f64 && (a.mode == FG_MODE_FG || a.mode == FG_MODE_COMPOSITE);
+    const Plan p = make_plan(ctx, nbins, nt, f64, fused_path);
     int rc = sfh_scratch_reserve(ctx, p.total);
     if (rc) return rc;
     char *s = (char *)ctx->scratch;
@@ -397,6 +760,61 @@ int sfh_launch_fg(sfh_ctx *ctx, const sfh_models *m, const FgArgs &a, cudaEvent_
     const bool from_coeffs = (a.mode == FG_MODE_FG || a.mode == FG_MODE_COMPOSITE);
     const bool want_g = (a.mode == FG_MODE_GRAD_GIVEN) || (a.mode == FG_MODE_FG && a.G);
     const bool want_l = (a.mode == FG_MODE_FG && a.negLogL);
+
+    // FP32 storage from coefficients: two fused kernels (pass 1: m, logL, w; pass 2: G).
+    if (!f64 && from_coeffs && p.nrowblk <= 32768 && p.ncolgroups <= 16384) {
+        if (ev) SFH_CK(ctx, cudaEventRecord(ev[0], st));
+        Pass1Args p1{};
+        p1.M = (const float *)Mptr;
+        p1.nbins = nbins;
+        p1.nt = nt;
+        p1.r = a.coeffs;
+        p1.kchunk = p.kchunk;
+        p1.part = reinterpret_cast<float2 *>(part);
+        p1.data = a.data;
+        p1.eps = a.eps;
+        p1.composite = a.composite;
+        p1.w32 = w32;
+        p1.want_logl = want_l ? 1 : 0;
+        p1.want_w = want_g ? 1 : 0;
+        p1.tile_logl = logl_part;
+        p1.tile_cnt = ctx->d_counters + SFH_CNT_ROWTILE;
+        p1.all_cnt = ctx->d_counters + SFH_CNT_FG_LOGL;
+        p1.negLogL = a.negLogL;
+        dim3 grid(p.ksplit, p.nrowblk);
+        const size_t sm = 2 * (size_t)p.kchunk * sizeof(float);
+        if (nbins % 4 == 0)
+            k_fg_pass1_f32<true><<<grid, kThreads, sm, st>>>(p1);
+        else
+            k_fg_pass1_f32<false><<<grid, kThreads, sm, st>>>(p1);
+        SFH_LAUNCHED(ctx);
+        if (ev) SFH_CK(ctx, cudaEventRecord(ev[1], st));
+        if (ev) SFH_CK(ctx, cudaEventRecord(ev[2], st));
+        if (want_g) {
+            Pass2Args p2{};
+            p2.M = (const float *)Mptr;
+            p2.nbins = nbins;
+            p2.nt = nt;
+            p2.w = w32;
+            p2.R = p.R;
+            p2.CB = p.CB;
+            p2.ncolgroups = p.ncolgroups;
+            p2.partG = partG;
+            p2.grp_cnt = ctx->d_counters + SFH_CNT_COLGROUP;
+            p2.gsign = a.gsign;
+            p2.G = a.G;
+            dim3 gridt(p.ncolgroups, p.nchunks);
+            const size_t smt = (size_t)p.R * sizeof(float);
+            if (nbins % 4 == 0)
+                k_fg_pass2_f32<true><<<gridt, kThreads, smt, st>>>(p2);
+            else
+                k_fg_pass2_f32<false><<<gridt, kThreads, smt, st>>>(p2);
+            SFH_LAUNCHED(ctx);
+        }
+        if (ev) SFH_CK(ctx, cudaEventRecord(ev[3], st));
+        if (ev) SFH_CK(ctx, cudaEventRecord(ev[4], st));
+        return SFH_OK;
+    }
 
     if (ev) SFH_CK(ctx, cudaEventRecord(ev[0], st));
     if (from_coeffs) {

@@ -40,8 +40,16 @@ struct sfh_models {
     int64_t nbins_pad = 0, nt_pad = 0;
 };
 
-// Counter slots in sfh_ctx::d_counters.
-enum { SFH_CNT_LOGL = 0, SFH_CNT_BATCH = 1, SFH_CNT_SLOTS = 64 };
+// Counter slots in sfh_ctx::d_counters (zeroed at context creation; every kernel that
+// takes a ticket from a slot resets it before it exits).
+enum {
+    SFH_CNT_LOGL = 0,          // k_finalize last-block reduction
+    SFH_CNT_BATCH = 1,
+    SFH_CNT_FG_LOGL = 2,       // fused pass 1: last row tile
+    SFH_CNT_ROWTILE = 256,     // fused pass 1: one per row tile (<= 32768)
+    SFH_CNT_COLGROUP = 256 + 32768,  // fused pass 2: one per column group (<= 16384)
+    SFH_CNT_SLOTS = 65536
+};
 
 // ------------------------------------------------------------------ error helpers
 int sfh_set_error(sfh_ctx *ctx, int code, const std::string &msg);
