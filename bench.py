@@ -135,6 +135,72 @@ def _max_over_ranks(world, x: float) -> float:
     return float(t.item())
 
 
+def _bf16_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["bf16_tflops"]), "measured"
+    except Exception:  # noqa: BLE001
+        return 1900.0, "fallback"
+
+
+def run_batched(ctx, d_T, nbins, nt, r, data, M64, steps, warmup, B=4096, check=2):
+    """Many coefficient vectors per call on the tensor cores (sfh_fg_batched_dev)."""
+    import numpy as np
+    import torch
+
+    import oracle as O
+    import sfhgpu
+    L = sfhgpu.load()
+    dev = torch.device("cuda", ctx.device)
+    Hb = sfhgpu.Models.from_device(d_T.data_ptr(), nbins, nt, storage="bf16x2", ctx=ctx)
+    rng = np.random.default_rng(7)
+    R = r[None, :] * np.exp(0.3 * rng.standard_normal((B, nt)))  # chain states near r
+    d_R = torch.tensor(R, device=dev)
+    d_n = torch.tensor(data, device=dev)
+    d_L = torch.empty(B, dtype=torch.float64, device=dev)
+    d_G = torch.empty((B, nt), dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+    args = (ctx.handle, Hb.handle, d_R.data_ptr(), B, d_n.data_ptr(), d_L.data_ptr(),
+            d_G.data_ptr(), float(np.finfo(np.float64).eps))
+    for _ in range(warmup):
+        sfhgpu._lib.check(L.sfh_fg_batched_dev(*args), ctx.handle, "sfh_fg_batched_dev")
+    ts = ctx.torch_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ts)
+    for _ in range(steps):
+        sfhgpu._lib.check(L.sfh_fg_batched_dev(*args), ctx.handle, "sfh_fg_batched_dev")
+    e1.record(ts)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    negL = d_L.cpu().numpy()
+    # accuracy against the FP64 oracle on a few vectors (stored hi+lo values, and FP32 templates)
+    Mt = torch.tensor(M64)
+    hi = Mt.float().to(torch.bfloat16).double()
+    Ms = np.asfortranarray((hi + (Mt - hi).float().to(torch.bfloat16).double()).numpy())
+    Rt = torch.tensor(R[:check])
+    rh = Rt.float().to(torch.bfloat16).double()
+    Rs = (rh + (Rt - rh).float().to(torch.bfloat16).double()).numpy()
+    O.set_threads(os.cpu_count() or 1)
+    ref_s, _ = O.fg_batched(Rs, Ms, data, nthreads=os.cpu_count() or 1, want_g=False)
+    ref_f, _ = O.fg_batched(R[:check], M64, data, nthreads=os.cpu_count() or 1, want_g=False)
+    nst = float(data.sum())
+    flops = 4.0 * nbins * nt * B  # two GEMMs, algorithmic (the hi/lo split triples tensor work)
+    peak, kind = _bf16_peak()
+    Hb.free()
+    return {
+        "workload": f"{B} coefficient vectors x {nt} templates x {nbins} bins (one call)",
+        "evals_per_s": B / (ms / 1e3), "ms_per_batch": ms, "B": B, "steps": steps,
+        "tensor_roofline": {"bound": "tensor", "achieved": flops / (ms / 1e3) / 1e12,
+                            "achieved_with_hilo": 3 * flops / (ms / 1e3) / 1e12, "peak": peak,
+                            "unit": "TFLOP/s", "frac": 3 * flops / (ms / 1e3) / 1e12 / peak,
+                            "peak_source": kind},
+        "dlogL_per_1e4_stars_vs_stored": float(np.max(np.abs(negL[:check] - ref_s)) / (nst / 1e4)),
+        "dlogL_per_1e4_stars_vs_fp32_templates": float(
+            np.max(np.abs(negL[:check] - ref_f)) / (nst / 1e4)),
+    }
+
+
 def cpu_fg_baseline(M64, r, data, budget_s=10.0, threads=None):
     """The oracle's fg! (FP64, OpenMP over bins/templates) on a bounded number of evals."""
     import numpy as np
@@ -355,6 +421,12 @@ def run_ours(args):
     e2e = {"value": world * ne2e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": (NTW + NBINS) * 8,
            "d2h_bytes_per_step": (NBINS + NTW + 1) * 8, "steps": ne2e}
 
+    # ---- batched form (tensor cores): 4,096 vectors per call on the same templates
+    batched = None
+    if not args.no_batched:
+        batched = run_batched(ctx, d_T, NBINS, NTW, r, data, M64, steps=5, warmup=2)
+        batched["speedup_vs_plain"] = batched["evals_per_s"] / value
+
     # ---- CPU baseline (rank 0, N = 1 only): the oracle on the same inputs
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -378,6 +450,7 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}"},
             "templates_per_s": templates_per_s, "template_build_ms": build_ms,
             "negLogL": neglogl, "gpu_launches": launches, "roofline": roofline,
+            "batched": batched,
             "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
         }
         print(json.dumps(line), flush=True)
@@ -395,6 +468,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched tensor-core leg")
     ap.add_argument("--ntempl", type=int, default=NT,
                     help="templates (multiple of 30); fewer than 1200 only for profiling")
     ap.add_argument("--cpu-budget-s", type=float, default=10.0)

@@ -74,6 +74,38 @@ int sfh_stage_reserve(sfh_ctx *ctx, size_t bytes);
 
 static inline size_t sfh_align256(size_t b) { return (b + 255) & ~size_t(255); }
 
+// ------------------------------------------------------------------ shared device math
+// Compensated FP32 accumulation: (hi, lo) += x.
+__device__ __forceinline__ void sfh_two_sum_acc(float &hi, float &lo, float x) {
+    const float s = __fadd_rn(hi, x);
+    const float bp = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(x, bp));
+    hi = s;
+    lo = __fadd_rn(lo, err);
+}
+
+// log1p(d) - d for d = c/n - 1 > -1, in FP32 without cancellation (relative error
+// < 6e-7 for eps <= c <= 1e30, checked against 40-digit arithmetic).  With
+// z = d / (2 + d):  log1p(d) = 2 atanh(z)  and  d - 2z = d z, hence
+// log1p(d) - d = -d z + 2 z^3 (1/3 + z^2/5 + z^4/7 + ...).
+__device__ __forceinline__ float sfh_log1p_minus_id(float d, float c, float n) {
+    if (fabsf(d) <= 0.5f) {
+        const float z = __fdiv_rn(d, 2.0f + d);
+        const float z2 = z * z;
+        float S = 1.0f / 17.0f;
+        S = fmaf(S, z2, 1.0f / 15.0f);
+        S = fmaf(S, z2, 1.0f / 13.0f);
+        S = fmaf(S, z2, 1.0f / 11.0f);
+        S = fmaf(S, z2, 1.0f / 9.0f);
+        S = fmaf(S, z2, 1.0f / 7.0f);
+        S = fmaf(S, z2, 1.0f / 5.0f);
+        S = fmaf(S, z2, 1.0f / 3.0f);
+        return fmaf(2.0f * z * z2, S, -d * z);
+    }
+    if (d < 0.0f) return logf(__fdiv_rn(c, n)) - d;  // c/n < 1/2: log of the ratio itself
+    return log1pf(d) - d;
+}
+
 // ------------------------------------------------------------------ internal launchers
 // Single-vector objective on device arrays (likelihood.cu).
 struct FgArgs {

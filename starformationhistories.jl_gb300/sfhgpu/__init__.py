@@ -6,7 +6,7 @@ All compute runs in libsfhgpu.so; there is no CPU fallback.
 from ._lib import (SFH_BF16X2, SFH_F32, SFH_F64, EXPORTED, LIB_PATH, SFHArgumentError, SFHError,
                    load)
 from .core import Context, Models, as_models, default_context
-from .fitting import (composite_, construct_x0, fg_, fit_templates, fit_templates_fast,
+from .fitting import (composite_, construct_x0, fg_, fg_batched, fit_templates, fit_templates_fast,
                       fit_templates_lbfgsb, grad_loglikelihood, grad_loglikelihood_, loglikelihood,
                       renormalize_x0, stack_models)
 from .templates import (BrokenPowerLawIMF, Histogram, Kroupa2001, Martin2016_complete,
@@ -17,7 +17,7 @@ from .templates import (BrokenPowerLawIMF, Histogram, Kroupa2001, Martin2016_com
 __all__ = [
     "SFH_BF16X2", "SFH_F32", "SFH_F64", "EXPORTED", "LIB_PATH", "SFHArgumentError", "SFHError",
     "load", "Context", "Models", "as_models", "default_context", "composite_", "construct_x0",
-    "fg_", "fit_templates", "fit_templates_fast", "fit_templates_lbfgsb", "grad_loglikelihood",
+    "fg_", "fg_batched", "fit_templates", "fit_templates_fast", "fit_templates_lbfgsb", "grad_loglikelihood",
     "grad_loglikelihood_", "loglikelihood", "renormalize_x0", "stack_models", "BrokenPowerLawIMF",
     "Histogram", "Kroupa2001", "Martin2016_complete", "bin_cmd_smooth", "calculate_edges",
     "calculate_weights", "compl_model", "err_model", "exp_photerr", "histogram_data",

@@ -274,3 +274,30 @@ def fit_templates(models, data, x0=None, gtol=1e-8, maxiter=10000):
         return LogTransformFTResult(mu, np.sqrt(np.abs(np.diag(invH))) * mu, invH, r)
 
     return FitTemplatesResult(pack(r_map), pack(r_mle))
+
+
+def fg_batched(models, R, data, want_logl=True, want_grad=True, eps=None):
+    """B fg! evaluations in one call on the tensor cores (sfh_fg_batched_dev).
+
+    models: a Models handle stored as "bf16x2"; R: (B, nt) coefficient vectors (torch CUDA
+    float64 tensor or numpy); data: (nbins,) observed counts.  Returns (negLogL, G): -logL
+    per vector (float64, or None) and -∇logL per vector (B x nt float32, or None), as
+    torch CUDA tensors.  Accuracy: FP32 accumulation of BF16 hi/lo products (see the
+    library header); use fg_ for FP64-level single evaluations."""
+    import torch
+    M = models if isinstance(models, Models) else Models(np.asarray(models), storage="bf16x2")
+    dev = torch.device("cuda", M.ctx.device)
+    Rt = torch.as_tensor(R, dtype=torch.float64, device=dev).contiguous()
+    nt_t = torch.as_tensor(data, dtype=torch.float64, device=dev).reshape(-1).contiguous()
+    B, nt = Rt.shape
+    _argcheck(nt == M.nt, "size(R, 2) == size(models, 2)")
+    _argcheck(nt_t.numel() == M.nbins, "length(data) == size(models, 1)")
+    negL = torch.empty(B, dtype=torch.float64, device=dev) if want_logl else None
+    G = torch.empty((B, nt), dtype=torch.float32, device=dev) if want_grad else None
+    torch.cuda.current_stream(dev).synchronize()
+    e = float(np.finfo(np.float64).eps) if eps is None else float(eps)
+    check(load().sfh_fg_batched_dev(M.ctx.handle, M.handle, Rt.data_ptr(), B, nt_t.data_ptr(),
+                                    negL.data_ptr() if want_logl else None,
+                                    G.data_ptr() if want_grad else None, e),
+          M.ctx.handle, "fg_batched")
+    return negL, G
