@@ -13,7 +13,8 @@
 // Kernel structure (k_tc_gemm, one CTA per SM, 192 threads):
 //   warp 0     TMA producer: 2-stage ring of {A_hi, A_lo, B_hi, B_lo} tiles (128B swizzle)
 //   warp 1     allocates 512 TMEM columns; lane 0 issues tcgen05.mma (M=128, N=256, K=16)
-//   warps 2-5  epilogue: tcgen05.ld of the finished accumulator (double-buffered in TMEM)
+//   warps 2-9  epilogue: tcgen05.ld of the finished accumulator (double-buffered in TMEM);
+//              two warps per TMEM lane quarter, each taking half of the 256 columns
 // Every mbarrier wait is bounded: on timeout the kernel records an error, stops the
 // other roles through a shared flag, drains what it issued and frees its TMEM.
 //
@@ -42,7 +43,8 @@ constexpr int A_BYTES = BM * BK * 2;               // 16 KB per plane
 constexpr int B_BYTES = BN * BK * 2;               // 32 KB per plane
 constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // 96 KB
 constexpr int TMEM_COLS = 512;                     // two 128 x 256 FP32 accumulators
-constexpr int kGemmThreads = 192;
+constexpr int kGemmThreads = 320;  // producer, MMA, 8 epilogue warps
+constexpr int kEpiThreads = 256;
 constexpr size_t kGemmSmem = 1024 + (size_t)STAGES * STAGE_BYTES + 256;
 constexpr long long kWaitBudget = 4000000000LL;   // ~2 s of SM clock per wait
 
@@ -62,7 +64,7 @@ struct GemmParams {
     __nv_bfloat16 *W_hi, *W_lo;
     int64_t w_ld;  // = nbins_pad
     int want_w, want_logl;
-    float2 *logl_part;  // [n_tiles][B_pad]
+    float2 *logl_part;  // [n_tiles * 2][B_pad] (two column halves per tile)
     // epilogue 1
     float *Gpart;  // [ksplit][B_pad][nt]
     int64_t nt;
@@ -222,7 +224,7 @@ k_tc_gemm(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUten
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&tfull[b], 1);
-            mbar_init(&tempty[b], 128);
+            mbar_init(&tempty[b], kEpiThreads);
         }
         mbar_init(drain, 1);
         *s_abort = 0;
@@ -329,9 +331,10 @@ k_tc_gemm(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUten
             }
         }
     } else {
-        // ---------------- epilogue (warps 2-5)
-        const int q = warp & 3;          // TMEM lane quarter this warp may access
-        const int row = 32 * q + lane;   // accumulator row = coefficient vector in tile
+        // ---------------- epilogue (warps 2-9)
+        const int q = warp & 3;                 // TMEM lane quarter this warp may access
+        const int half = (warp - 2) >> 2;       // which 128 of the 256 columns
+        const int row = 32 * q + lane;          // accumulator row = coefficient vector in tile
         int lt = 0;
         for (int u = blockIdx.x; u < total; u += gridDim.x, ++lt) {
             int m, n, ks;
@@ -341,12 +344,14 @@ k_tc_gemm(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUten
             if (!mbar_wait(&tfull[buf], tph, s_abort, P.err, 4)) break;
             tc_fence_after();
             const int b = m * BM + row;
-            const uint32_t tbase = tmem_base + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * BN);
+            const uint32_t tbase = tmem_base + ((uint32_t)(32 * q) << 16) +
+                                   (uint32_t)(buf * BN + half * (BN / 2));
             if (P.epi == 0) {
-                const int64_t i0 = (int64_t)n * BN;
-                float th = 0.f, tl = 0.f;
+                const int64_t i0 = (int64_t)n * BN + half * (BN / 2);
+                // four independent compensated sums keep the dependency chains short
+                float th[4] = {0.f, 0.f, 0.f, 0.f}, tl[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll 1
-                for (int c = 0; c < BN / 32; ++c) {
+                for (int c = 0; c < BN / 64; ++c) {
                     float v[32];
                     tmem_ld32(tbase + (uint32_t)(c * 32), v);
                     const int64_t ic = i0 + c * 32;
@@ -364,7 +369,7 @@ k_tc_gemm(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUten
                                 const float t = (ni > 0.f)
                                                     ? ni * sfh_log1p_minus_id(__fdividef(df, ni), ci, ni)
                                                     : -ci;
-                                sfh_two_sum_acc(th, tl, t);
+                                sfh_two_sum_acc(th[e & 3], tl[e & 3], t);
                             }
                         }
                     }
@@ -389,13 +394,20 @@ k_tc_gemm(const __grid_constant__ CUtensorMap tAh, const __grid_constant__ CUten
                         }
                     }
                 }
-                if (P.want_logl && b < P.B_pad)
-                    P.logl_part[(int64_t)n * P.B_pad + b] = make_float2(th, tl);
+                if (P.want_logl && b < P.B_pad) {
+                    float h = 0.f, l = 0.f;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        sfh_two_sum_acc(h, l, th[k]);
+                        l += tl[k];
+                    }
+                    P.logl_part[((int64_t)n * 2 + half) * P.B_pad + b] = make_float2(h, l);
+                }
             } else {
-                const int64_t j0 = (int64_t)n * BN;
+                const int64_t j0 = (int64_t)n * BN + half * (BN / 2);
                 float *dst = P.Gpart + ((int64_t)ks * P.B_pad + b) * P.nt;
 #pragma unroll 1
-                for (int c = 0; c < BN / 32; ++c) {
+                for (int c = 0; c < BN / 64; ++c) {
                     float v[32];
                     tmem_ld32(tbase + (uint32_t)(c * 32), v);
                     if (b < P.B) {
@@ -604,7 +616,7 @@ int sfh_launch_fg_batched(sfh_ctx *ctx, const sfh_models *m, const double *d_R, 
     const size_t o_rl = o_rh + sz_r;
     const size_t sz_w = sfh_align256((size_t)B_pad * nbp * 2);
     const size_t o_wh = o_rl + sz_r, o_wl = o_wh + sz_w;
-    const size_t o_lp = o_wl + sz_w, sz_lp = sfh_align256((size_t)n_tiles1 * B_pad * sizeof(float2));
+    const size_t o_lp = o_wl + sz_w, sz_lp = sfh_align256((size_t)n_tiles1 * 2 * B_pad * sizeof(float2));
     const size_t o_gp = o_lp + sz_lp, sz_gp = sfh_align256((size_t)ks2 * B_pad * nt * sizeof(float));
     const size_t o_data = o_gp + sz_gp, sz_data = sfh_align256((size_t)nbins * sizeof(float));
     const size_t o_err = o_data + sz_data;
@@ -653,8 +665,8 @@ int sfh_launch_fg_batched(sfh_ctx *ctx, const sfh_models *m, const double *d_R, 
     P1.err = err;
     if ((rc = launch_gemm(ctx, mRh, mRl, mMh, mMl, P1))) return rc;
     if (want_l) {
-        k_logl_reduce<<<(unsigned)((B + 255) / 256), 256, 0, st>>>(lp, n_tiles1, (int)B, (int)B_pad,
-                                                                   d_negLogL);
+        k_logl_reduce<<<(unsigned)((B + 255) / 256), 256, 0, st>>>(lp, 2 * n_tiles1, (int)B,
+                                                                   (int)B_pad, d_negLogL);
         SFH_LAUNCHED(ctx);
     }
     if (want_g) {

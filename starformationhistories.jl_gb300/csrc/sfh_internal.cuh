@@ -90,7 +90,7 @@ __device__ __forceinline__ void sfh_two_sum_acc(float &hi, float &lo, float x) {
 // log1p(d) - d = -d z + 2 z^3 (1/3 + z^2/5 + z^4/7 + ...).
 __device__ __forceinline__ float sfh_log1p_minus_id(float d, float c, float n) {
     if (fabsf(d) <= 0.5f) {
-        const float z = __fdiv_rn(d, 2.0f + d);
+        const float z = __fdividef(d, 2.0f + d);
         const float z2 = z * z;
         float S = 1.0f / 17.0f;
         S = fmaf(S, z2, 1.0f / 15.0f);
@@ -102,7 +102,7 @@ __device__ __forceinline__ float sfh_log1p_minus_id(float d, float c, float n) {
         S = fmaf(S, z2, 1.0f / 3.0f);
         return fmaf(2.0f * z * z2, S, -d * z);
     }
-    if (d < 0.0f) return logf(__fdiv_rn(c, n)) - d;  // c/n < 1/2: log of the ratio itself
+    if (d < 0.0f) return logf(__fdividef(c, n)) - d;  // c/n < 1/2: log of the ratio itself
     return log1pf(d) - d;
 }
 
