@@ -141,6 +141,55 @@ int sfh_fg_dev_noalloc(void *stream, const float *d_models, int64_t nbins, int64
 int sfh_fg_batched_dev(sfh_ctx *ctx, const sfh_models *models, const double *d_R, int64_t B,
                        const double *d_data, double *d_negLogL, float *d_G, double eps);
 
+/* ---------------------------------------------------------------- batched HMC */
+enum sfh_hmc_model {
+    SFH_HMC_DIRECT = 0, /* θ = log coeffs: hmc_sample's log density, hmc_sample.jl:24-37 */
+    SFH_HMC_MZR = 1     /* PowerLawMZR + GaussianDispersion: sample_sfh's log density,
+                           generic_fitting.jl:90-199 with mzr.jl:50-215 */
+};
+typedef struct {
+    int32_t nchains;        /* chains advanced together (one batched gradient per step) */
+    int32_t model;          /* enum sfh_hmc_model */
+    int64_t ntraj;          /* trajectories kept after warmup */
+    int64_t nwarmup;        /* warmup trajectories: step-size (dual averaging) and mass adaptation */
+    int32_t nleap;          /* leapfrog steps per trajectory */
+    int32_t thin;           /* keep every thin-th draw when draws are requested */
+    double step0;           /* initial leapfrog step */
+    double target_accept;   /* dual-averaging target acceptance (e.g. 0.8) */
+    uint64_t seed;          /* Philox key */
+    /* SFH_HMC_MZR only: ages and metallicities of the templates */
+    int32_t nages;
+    const int32_t *h_age_index; /* per template: its age, 0..nages-1 */
+    const double *h_logAge;     /* per age (any order) */
+    const double *h_MH;         /* per template [M/H] */
+    double logMstar0;           /* PowerLawMZR logMstar0 (fixed), mzr.jl:263-272 */
+    int32_t alpha_free, beta_free, sigma_free;
+    double alpha, beta, sigma;  /* values of parameters held fixed */
+} sfh_hmc_config;
+
+/* Batched HMC over all chains at once, every leapfrog step one sfh_fg_batched_dev-style
+   evaluation on the tensor cores; replaces the per-chain DynamicHMC loop of hmc_sample
+   (hmc_sample.jl:105-141) and sample_sfh (generic_fitting.jl:458-527).  Fixed-length
+   trajectories, per-chain dual-averaging step size and a pooled diagonal mass during
+   warmup, Metropolis accept.  Device arrays: d_theta0 (nchains x D) starting points in
+   the transformed space (D = ntempl for SFH_HMC_DIRECT; nages + free parameters, order
+   [log R_j..., log α, β, log σ], for SFH_HMC_MZR).  Outputs (each may be NULL):
+   d_mean / d_var (nchains x D) posterior mean and variance of the natural parameters
+   (exp of the log-transformed ones), d_accept (nchains) mean acceptance, d_step
+   (nchains) final step, d_draws (nchains x ceil(ntraj/thin) x D) FP32 natural draws.
+   Models must be stored as SFH_BF16X2.  The call returns after the run completes. */
+int sfh_hmc_sample_dev(sfh_ctx *ctx, const sfh_models *models, const double *d_data,
+                       const sfh_hmc_config *cfg, const double *d_theta0, double *d_mean,
+                       double *d_var, double *d_accept, double *d_step, float *d_draws);
+
+/* Log density and its gradient for B parameter vectors of the same model as
+   sfh_hmc_sample_dev (logdensity_and_gradient of hmc_sample.jl:24-37 and
+   generic_fitting.jl:90-199 with Jacobian terms), batched on the tensor cores:
+   d_theta (B x D, B = cfg->nchains) -> d_logd (B), d_grad (B x D). */
+int sfh_logdensity_batched_dev(sfh_ctx *ctx, const sfh_models *models, const double *d_data,
+                               const sfh_hmc_config *cfg, const double *d_theta, double *d_logd,
+                               double *d_grad);
+
 /* ---------------------------------------------------------------- template construction */
 /* bin_cmd_smooth(colors, mags, color_err, mag_err, cov_mult; weights, edges),
    StarFormationHistories.jl:574-621 (kernels :191-340, addstar! :345-408).

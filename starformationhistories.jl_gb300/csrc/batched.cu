@@ -586,17 +586,18 @@ int sfh_build_bf16_planes(sfh_ctx *ctx, sfh_models *m, const float *d_f32) {
     return SFH_OK;
 }
 
-int sfh_launch_fg_batched(sfh_ctx *ctx, const sfh_models *m, const double *d_R, int64_t B,
-                          const double *d_data, double *d_negLogL, float *d_G, double eps) {
+int sfh_batched_prepare(sfh_ctx *ctx, const sfh_models *m, int64_t B, const double *d_data,
+                        void *scratch, size_t scratch_bytes, SfhBatchedPlan *pl) {
     if (!m->row_hi || !m->col_hi)
         return sfh_set_error(ctx, SFH_ERR_ARG, "models have no BF16 hi/lo planes");
-    if (B > (1 << 24)) return sfh_set_error(ctx, SFH_ERR_ARG, "too many coefficient vectors");
+    if (B < 1 || B > (1 << 24)) return sfh_set_error(ctx, SFH_ERR_ARG, "bad number of coefficient vectors");
     const int64_t nbins = m->nbins, nt = m->nt, nbp = m->nbins_pad, ntp = m->nt_pad;
-    const int64_t B_pad = ((B + BM - 1) / BM) * BM;
-    const int m_tiles = (int)(B_pad / BM);
-    const int n_tiles1 = (int)((nbins + BN - 1) / BN);
-    const int n_tiles2 = (int)((nt + BN - 1) / BN);
-    const bool want_g = d_G != nullptr, want_l = d_negLogL != nullptr;
+    SfhBatchedPlan P{};
+    P.B = B;
+    P.B_pad = ((B + BM - 1) / BM) * BM;
+    P.m_tiles = (int)(P.B_pad / BM);
+    P.n_tiles1 = (int)((nbins + BN - 1) / BN);
+    P.n_tiles2 = (int)((nt + BN - 1) / BN);
     // G = W M split over K so that every SM gets work: pick the split that minimises
     // (rounds of work units) x (k-blocks per unit).
     const int kb2 = (int)(nbp / BK);
@@ -604,96 +605,132 @@ int sfh_launch_fg_batched(sfh_ctx *ctx, const sfh_models *m, const double *d_R, 
     double best = 1e300;
     for (int ks = 1; ks <= 32 && ks <= kb2; ++ks) {
         const int per = (kb2 + ks - 1) / ks;
-        const int units = ks * m_tiles * n_tiles2;
+        const int units = ks * P.m_tiles * P.n_tiles2;
         const int rounds = (units + ctx->sm_count - 1) / ctx->sm_count;
         const double cost = (double)rounds * per * (1.0 + 0.01 * ks);
         if (cost < best) { best = cost; ks2 = ks; }
     }
-    const int per2 = (kb2 + ks2 - 1) / ks2;
-    ks2 = (kb2 + per2 - 1) / per2;  // no empty splits
-    // scratch
+    P.per2 = (kb2 + ks2 - 1) / ks2;
+    P.ks2 = (kb2 + P.per2 - 1) / P.per2;  // no empty splits
+    P.kb2 = kb2;
+    const int64_t B_pad = P.B_pad;
     const size_t o_rh = 0, sz_r = sfh_align256((size_t)B_pad * ntp * 2);
     const size_t o_rl = o_rh + sz_r;
     const size_t sz_w = sfh_align256((size_t)B_pad * nbp * 2);
     const size_t o_wh = o_rl + sz_r, o_wl = o_wh + sz_w;
-    const size_t o_lp = o_wl + sz_w, sz_lp = sfh_align256((size_t)n_tiles1 * 2 * B_pad * sizeof(float2));
-    const size_t o_gp = o_lp + sz_lp, sz_gp = sfh_align256((size_t)ks2 * B_pad * nt * sizeof(float));
+    const size_t o_lp = o_wl + sz_w, sz_lp = sfh_align256((size_t)P.n_tiles1 * 2 * B_pad * sizeof(float2));
+    const size_t o_gp = o_lp + sz_lp, sz_gp = sfh_align256((size_t)P.ks2 * B_pad * nt * sizeof(float));
     const size_t o_data = o_gp + sz_gp, sz_data = sfh_align256((size_t)nbins * sizeof(float));
     const size_t o_err = o_data + sz_data;
-    int rc = sfh_scratch_reserve(ctx, o_err + 256);
-    if (rc) return rc;
-    char *s = (char *)ctx->scratch;
-    __nv_bfloat16 *Rh = (__nv_bfloat16 *)(s + o_rh), *Rl = (__nv_bfloat16 *)(s + o_rl);
-    __nv_bfloat16 *Wh = (__nv_bfloat16 *)(s + o_wh), *Wl = (__nv_bfloat16 *)(s + o_wl);
-    float2 *lp = (float2 *)(s + o_lp);
-    float *gp = (float *)(s + o_gp);
-    float *dataf = (float *)(s + o_data);
-    int *err = (int *)(s + o_err);
+    P.scratch_bytes = o_err + 256;
+    if (!scratch) {  // size query
+        *pl = P;
+        return SFH_OK;
+    }
+    if (scratch_bytes < P.scratch_bytes) return sfh_set_error(ctx, SFH_ERR_ARG, "batched scratch too small");
+    char *s = (char *)scratch;
+    P.Rh = (__nv_bfloat16 *)(s + o_rh);
+    P.Rl = (__nv_bfloat16 *)(s + o_rl);
+    P.Wh = (__nv_bfloat16 *)(s + o_wh);
+    P.Wl = (__nv_bfloat16 *)(s + o_wl);
+    P.lp = (float2 *)(s + o_lp);
+    P.gp = (float *)(s + o_gp);
+    P.dataf = (float *)(s + o_data);
+    P.err = (int *)(s + o_err);
     cudaStream_t st = ctx->stream;
-    SFH_CK(ctx, cudaMemsetAsync(err, 0, sizeof(int), st));
+    SFH_CK(ctx, cudaMemsetAsync(P.err, 0, sizeof(int), st));
+    // data as FP32 (counts are exact below 2^24)
+    k_f64_to_f32<<<(unsigned)((nbins + 255) / 256), 256, 0, st>>>(d_data, P.dataf, nbins);
+    SFH_LAUNCHED(ctx);
+    CUtensorMap *mp = P.maps;
+    int rc;
+    if ((rc = make_map(ctx, &mp[0], P.Rh, B_pad, ntp, ntp, BM))) return rc;
+    if ((rc = make_map(ctx, &mp[1], P.Rl, B_pad, ntp, ntp, BM))) return rc;
+    if ((rc = make_map(ctx, &mp[2], m->row_hi, nbins, ntp, ntp, BN))) return rc;
+    if ((rc = make_map(ctx, &mp[3], m->row_lo, nbins, ntp, ntp, BN))) return rc;
+    if ((rc = make_map(ctx, &mp[4], P.Wh, B_pad, nbp, nbp, BM))) return rc;
+    if ((rc = make_map(ctx, &mp[5], P.Wl, B_pad, nbp, nbp, BM))) return rc;
+    if ((rc = make_map(ctx, &mp[6], m->col_hi, nt, nbp, nbp, BN))) return rc;
+    if ((rc = make_map(ctx, &mp[7], m->col_lo, nt, nbp, nbp, BN))) return rc;
+    *pl = P;
+    return SFH_OK;
+}
+
+int sfh_batched_launch(sfh_ctx *ctx, const sfh_models *m, const SfhBatchedPlan &pl,
+                       const double *d_R, double *d_negLogL, float *d_G, double eps) {
+    const int64_t nbins = m->nbins, nt = m->nt, nbp = m->nbins_pad, ntp = m->nt_pad;
+    const int64_t B = pl.B, B_pad = pl.B_pad;
+    const bool want_g = d_G != nullptr, want_l = d_negLogL != nullptr;
+    cudaStream_t st = ctx->stream;
     {
         const int64_t n = B_pad * ntp;
-        k_split_coeffs<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_R, B, nt, B_pad, ntp, Rh, Rl);
+        k_split_coeffs<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_R, B, nt, B_pad, ntp, pl.Rh,
+                                                                    pl.Rl);
         SFH_LAUNCHED(ctx);
     }
-    // data as FP32 (counts are exact below 2^24)
-    k_f64_to_f32<<<(unsigned)((nbins + 255) / 256), 256, 0, st>>>(d_data, dataf, nbins);
-    SFH_LAUNCHED(ctx);
-    CUtensorMap mRh, mRl, mMh, mMl, mWh, mWl, mCh, mCl;
-    if ((rc = make_map(ctx, &mRh, Rh, B_pad, ntp, ntp, BM))) return rc;
-    if ((rc = make_map(ctx, &mRl, Rl, B_pad, ntp, ntp, BM))) return rc;
-    if ((rc = make_map(ctx, &mMh, m->row_hi, nbins, ntp, ntp, BN))) return rc;
-    if ((rc = make_map(ctx, &mMl, m->row_lo, nbins, ntp, ntp, BN))) return rc;
+    int rc;
     GemmParams P1{};
-    P1.m_tiles = m_tiles;
-    P1.n_tiles = n_tiles1;
+    P1.m_tiles = pl.m_tiles;
+    P1.n_tiles = pl.n_tiles1;
     P1.ksplit = 1;
     P1.kb_total = (int)(ntp / BK);
     P1.kb_per_split = P1.kb_total;
     P1.epi = 0;
-    P1.data = dataf;
+    P1.data = pl.dataf;
     P1.nbins = nbins;
     P1.B = (int)B;
     P1.B_pad = (int)B_pad;
     P1.eps = (float)fmax(eps, 1.1754943508222875e-38);
-    P1.W_hi = Wh;
-    P1.W_lo = Wl;
+    P1.W_hi = pl.Wh;
+    P1.W_lo = pl.Wl;
     P1.w_ld = nbp;
     P1.want_w = want_g ? 1 : 0;
     P1.want_logl = want_l ? 1 : 0;
-    P1.logl_part = lp;
-    P1.err = err;
-    if ((rc = launch_gemm(ctx, mRh, mRl, mMh, mMl, P1))) return rc;
+    P1.logl_part = pl.lp;
+    P1.err = pl.err;
+    if ((rc = launch_gemm(ctx, pl.maps[0], pl.maps[1], pl.maps[2], pl.maps[3], P1))) return rc;
     if (want_l) {
-        k_logl_reduce<<<(unsigned)((B + 255) / 256), 256, 0, st>>>(lp, 2 * n_tiles1, (int)B,
+        k_logl_reduce<<<(unsigned)((B + 255) / 256), 256, 0, st>>>(pl.lp, 2 * pl.n_tiles1, (int)B,
                                                                    (int)B_pad, d_negLogL);
         SFH_LAUNCHED(ctx);
     }
     if (want_g) {
-        if ((rc = make_map(ctx, &mWh, Wh, B_pad, nbp, nbp, BM))) return rc;
-        if ((rc = make_map(ctx, &mWl, Wl, B_pad, nbp, nbp, BM))) return rc;
-        if ((rc = make_map(ctx, &mCh, m->col_hi, nt, nbp, nbp, BN))) return rc;
-        if ((rc = make_map(ctx, &mCl, m->col_lo, nt, nbp, nbp, BN))) return rc;
         GemmParams P2{};
-        P2.m_tiles = m_tiles;
-        P2.n_tiles = n_tiles2;
-        P2.ksplit = ks2;
-        P2.kb_total = kb2;
-        P2.kb_per_split = per2;
+        P2.m_tiles = pl.m_tiles;
+        P2.n_tiles = pl.n_tiles2;
+        P2.ksplit = pl.ks2;
+        P2.kb_total = pl.kb2;
+        P2.kb_per_split = pl.per2;
         P2.epi = 1;
         P2.B = (int)B;
         P2.B_pad = (int)B_pad;
-        P2.Gpart = gp;
+        P2.Gpart = pl.gp;
         P2.nt = nt;
-        P2.err = err;
-        if ((rc = launch_gemm(ctx, mWh, mWl, mCh, mCl, P2))) return rc;
+        P2.err = pl.err;
+        if ((rc = launch_gemm(ctx, pl.maps[4], pl.maps[5], pl.maps[6], pl.maps[7], P2))) return rc;
         const int64_t n = B * nt;
-        k_g_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(gp, ks2, B, B_pad, nt, d_G);
+        k_g_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(pl.gp, pl.ks2, B, B_pad, nt, d_G);
         SFH_LAUNCHED(ctx);
     }
+    (void)nbp;
+    return SFH_OK;
+}
+
+int sfh_batched_check(sfh_ctx *ctx, const SfhBatchedPlan &pl) {
     int herr = 0;
-    SFH_CK(ctx, cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
-    SFH_CK(ctx, cudaStreamSynchronize(st));
+    SFH_CK(ctx, cudaMemcpyAsync(&herr, pl.err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
     if (herr) return sfh_set_error(ctx, SFH_ERR_TIMEOUT, "tensor-core pipeline wait timed out");
     return SFH_OK;
+}
+
+int sfh_launch_fg_batched(sfh_ctx *ctx, const sfh_models *m, const double *d_R, int64_t B,
+                          const double *d_data, double *d_negLogL, float *d_G, double eps) {
+    SfhBatchedPlan pl{};
+    int rc = sfh_batched_prepare(ctx, m, B, d_data, nullptr, 0, &pl);
+    if (rc) return rc;
+    if ((rc = sfh_scratch_reserve(ctx, pl.scratch_bytes))) return rc;
+    if ((rc = sfh_batched_prepare(ctx, m, B, d_data, ctx->scratch, ctx->scratch_bytes, &pl))) return rc;
+    if ((rc = sfh_batched_launch(ctx, m, pl, d_R, d_negLogL, d_G, eps))) return rc;
+    return sfh_batched_check(ctx, pl);
 }

@@ -1,0 +1,695 @@
+// hmc.cu -- many HMC chains at once on the batched tensor-core objective.
+//
+// Replaces the per-chain DynamicHMC loop of hmc_sample (src/fitting/hmc_sample.jl:105-141,
+// log density :24-37) and of sample_sfh with a PowerLawMZR + GaussianDispersion model
+// (src/fitting/hierarchical/generic_fitting.jl:90-199, mzr.jl:50-215): all chains advance
+// together, every leapfrog step evaluates all gradients with one batched call.
+//
+//   direct model (hmc_sample):  θ = log r, log p(θ) = logL(exp θ) + Σ θ,
+//                               ∇ = -G ⊙ r + 1 with G = -∂logL/∂r (hmc_sample.jl:34-36)
+//   MZR model (sample_sfh):     θ = (log R_j, log α | β, log σ) for the free parameters,
+//                               r = calculate_coeffs(...) (mzr.jl:50-79), chain rule as
+//                               mzr.jl:131-209, Jacobian terms as generic_fitting.jl:143-157
+//
+// Sampler: fixed-length HMC (nleap leapfrog steps per trajectory), Metropolis accept,
+// per-chain dual-averaging step size during warmup (Hoffman & Gelman 2014, Alg. 5),
+// diagonal inverse mass set once at half of warmup from the variance of θ pooled over
+// all chains, Welford posterior mean/variance of the natural parameters after warmup.
+// Random numbers: Philox4x32-10 (Salmon et al., SC'11) keyed by the seed, counter =
+// (element, chain, trajectory, stream).  One trajectory is captured in a CUDA graph and
+// replayed; the trajectory counter lives on the device.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "sfh_internal.cuh"
+
+namespace {
+
+constexpr int kT = 256;
+
+struct u4 {
+    uint32_t x, y, z, w;
+};
+
+// Philox4x32 with 10 rounds (multipliers 0xD2511F53 / 0xCD9E8D57, Weyl key increments
+// 0x9E3779B9 / 0xBB67AE85), as published by Salmon, Moraes, Dror and Shaw (2011).
+__device__ __forceinline__ u4 philox(u4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = u4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+
+__device__ __forceinline__ double u01(uint32_t a, uint32_t b) {  // (0, 1], 53 bits
+    const uint64_t v = ((uint64_t)a << 21) ^ (uint64_t)b;
+    return ((double)(v & ((1ull << 53) - 1)) + 1.0) * (1.0 / 9007199254740992.0);
+}
+
+__device__ __forceinline__ double normal(uint64_t seed, uint32_t e, uint32_t b, uint32_t t,
+                                         uint32_t stream) {
+    const u4 r = philox(u4{e, b, t, stream}, (uint32_t)seed, (uint32_t)(seed >> 32));
+    const double u1 = u01(r.x, r.y), u2 = u01(r.z, r.w);
+    return sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+}
+
+__device__ __forceinline__ double block_sum(double v, double *s_red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double tot = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += s_red[w];
+    __syncthreads();
+    return tot;
+}
+
+// Per-chain sampler state.
+struct ChainState {
+    double *theta, *p, *g, *theta0, *g0;  // B x D
+    double *logd, *logd0, *kin0;          // B
+    double *eps;                          // B step sizes
+    double *da;                           // B x 4 dual averaging: mu, Hbar, log_eps_bar, m
+    double *acc_sum;                      // B: sum of acceptance probabilities (sampling)
+    double *mean, *m2;                    // B x D Welford of the natural parameters
+    double *minv;                         // D inverse mass (diagonal)
+    int64_t *t;                           // trajectory counter (device)
+    float *draws;                         // optional B x ndraws x D
+};
+
+struct HmcConst {
+    int B, D;
+    int64_t nwarm, nsamp;
+    int nleap;
+    double target;
+    uint64_t seed;
+    int thin;
+    int64_t ndraws;
+    int model;   // 0 direct, 1 MZR
+    int nages;
+    int alpha_free, beta_free, sigma_free;
+    double alpha, beta, sigma, logM0;
+};
+
+// ---------------------------------------------------------------- trajectory kernels
+__global__ void k_refresh(ChainState s, HmcConst c) {
+    __shared__ double s_red[kT / 32];
+    const int b = blockIdx.x;
+    const int64_t t = *s.t;
+    double kin = 0.0;
+    for (int d = threadIdx.x; d < c.D; d += blockDim.x) {
+        const int64_t k = (int64_t)b * c.D + d;
+        const double mi = s.minv[d];
+        const double pk = normal(c.seed, (uint32_t)d, (uint32_t)b, (uint32_t)t, 1u) / sqrt(mi);
+        s.p[k] = pk;
+        s.theta0[k] = s.theta[k];
+        s.g0[k] = s.g[k];
+        kin += 0.5 * pk * pk * mi;
+    }
+    kin = block_sum(kin, s_red);
+    if (threadIdx.x == 0) {
+        s.kin0[b] = kin;
+        s.logd0[b] = s.logd[b];
+    }
+}
+
+// p += frac * eps * g; then (drift) θ += eps * minv * p
+__global__ void k_kick_drift(ChainState s, HmcConst c, double frac, int drift) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= (int64_t)c.B * c.D) return;
+    const int b = (int)(k / c.D), d = (int)(k - (int64_t)b * c.D);
+    const double e = s.eps[b];
+    double pk = s.p[k] + frac * e * s.g[k];
+    s.p[k] = pk;
+    if (drift) s.theta[k] += e * s.minv[d] * pk;
+}
+
+// Dual averaging (Hoffman & Gelman 2014): gamma 0.05, t0 10, kappa 0.75.
+__device__ void dual_average(double *da, double *eps, double alpha, double target) {
+    const double m = da[3] + 1.0;
+    da[3] = m;
+    da[1] = (1.0 - 1.0 / (m + 10.0)) * da[1] + (target - alpha) / (m + 10.0);
+    const double log_eps = da[0] - sqrt(m) / 0.05 * da[1];
+    const double eta = pow(m, -0.75);
+    da[2] = eta * log_eps + (1.0 - eta) * da[2];
+    *eps = exp(fmin(fmax(log_eps, -30.0), 5.0));
+}
+
+__device__ double nat_param(const HmcConst &c, const double *th, int d) {
+    if (c.model == 0) return exp(th[d]);
+    if (d < c.nages) return exp(th[d]);
+    int q = c.nages;
+    if (c.alpha_free) { if (d == q) return exp(th[d]); ++q; }
+    if (c.beta_free) { if (d == q) return th[d]; ++q; }
+    return exp(th[d]);  // sigma
+}
+
+__global__ void k_accept(ChainState s, HmcConst c) {
+    __shared__ double s_red[kT / 32];
+    __shared__ int s_acc;
+    const int b = blockIdx.x;
+    const int64_t t = *s.t;
+    double kin = 0.0;
+    for (int d = threadIdx.x; d < c.D; d += blockDim.x) {
+        const double pk = s.p[(int64_t)b * c.D + d];
+        kin += 0.5 * pk * pk * s.minv[d];
+    }
+    kin = block_sum(kin, s_red);
+    if (threadIdx.x == 0) {
+        const double H0 = -s.logd0[b] + s.kin0[b];
+        const double H1 = -s.logd[b] + kin;
+        const double dH = H0 - H1;
+        // A divergent trajectory (non-finite energy) is rejected; fmin would drop a NaN.
+        const double a = (dH == dH && dH > -1e300) ? exp(fmin(0.0, dH)) : 0.0;
+        const u4 r = philox(u4{0xFFFFFFFFu, (uint32_t)b, (uint32_t)t, 2u}, (uint32_t)c.seed,
+                            (uint32_t)(c.seed >> 32));
+        const int acc = u01(r.x, r.y) < a;
+        s_acc = acc;
+        if (!acc) s.logd[b] = s.logd0[b];
+        if (t < c.nwarm) {
+            dual_average(s.da + 4 * b, s.eps + b, a, c.target);
+            if (t == c.nwarm - 1) s.eps[b] = exp(s.da[4 * b + 2]);
+        } else {
+            s.acc_sum[b] += a;
+        }
+    }
+    __syncthreads();
+    const int acc = s_acc;
+    const int64_t ts = t - c.nwarm;  // sampling index
+    for (int d = threadIdx.x; d < c.D; d += blockDim.x) {
+        const int64_t k = (int64_t)b * c.D + d;
+        if (!acc) {
+            s.theta[k] = s.theta0[k];
+            s.g[k] = s.g0[k];
+        }
+        if (ts >= 0) {
+            const double x = nat_param(c, s.theta + (int64_t)b * c.D, d);
+            const double n1 = (double)(ts + 1);
+            const double delta = x - s.mean[k];
+            s.mean[k] += delta / n1;
+            s.m2[k] += delta * (x - s.mean[k]);
+            if (s.draws && c.thin > 0 && ts % c.thin == 0 && ts / c.thin < c.ndraws)
+                s.draws[((int64_t)b * c.ndraws + ts / c.thin) * c.D + d] = (float)x;
+        }
+    }
+}
+
+// At half of warmup: inverse mass = variance of θ pooled over chains; restart dual
+// averaging around the current step sizes.
+__global__ void k_adapt_mass(ChainState s, HmcConst c) {
+    const int64_t t = *s.t;
+    if (c.nwarm < 20 || t != c.nwarm / 2) return;
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d < c.D) {
+        double m = 0.0, q = 0.0;
+        for (int b = 0; b < c.B; ++b) {
+            const double x = s.theta[(int64_t)b * c.D + d];
+            const double dl = x - m;
+            m += dl / (b + 1);
+            q += dl * (x - m);
+        }
+        const double var = c.B > 1 ? q / (c.B - 1) : 1.0;
+        // regularised towards 1e-3 as in common practice for few samples
+        s.minv[d] = (c.B / (c.B + 5.0)) * var + 1e-3 * (5.0 / (c.B + 5.0));
+    }
+    if (d < c.B) {
+        double *da = s.da + 4 * d;
+        da[0] = log(10.0 * s.eps[d]);
+        da[1] = 0.0;
+        da[2] = 0.0;
+        da[3] = 0.0;
+    }
+}
+
+__global__ void k_next_traj(ChainState s) { *s.t += 1; }
+
+// ---------------------------------------------------------------- model maps
+__global__ void k_direct_map(const double *__restrict__ theta, int64_t n, double *__restrict__ r) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) r[k] = exp(theta[k]);
+}
+
+// log p = -negLogL + Σ θ;  ∇ = -G ⊙ r + 1   (hmc_sample.jl:34-36)
+__global__ void k_direct_grad(const double *__restrict__ theta, const double *__restrict__ r,
+                              const float *__restrict__ G, const double *__restrict__ negL, int D,
+                              double *__restrict__ g, double *__restrict__ logd, int want_logd) {
+    __shared__ double s_red[kT / 32];
+    const int b = blockIdx.x;
+    double st = 0.0;
+    for (int d = threadIdx.x; d < D; d += blockDim.x) {
+        const int64_t k = (int64_t)b * D + d;
+        g[k] = -(double)G[k] * r[k] + 1.0;
+        st += theta[k];
+    }
+    if (want_logd) {
+        st = block_sum(st, s_red);
+        if (threadIdx.x == 0) logd[b] = -negL[b] + st;
+    }
+}
+
+struct MzrDev {
+    int nt, nages;
+    const int *jidx;         // template -> age
+    const double *MH;        // template [M/H]
+    const int *age_off;      // CSR: templates of age j
+    const int *age_tmpl;
+    const int *sorted;       // ages by decreasing logAge (sortperm(unique_logAge; rev=true))
+    double *aux;             // B x (4 nages): cum, mu, Asum, (spare)
+    double *A;               // B x nt Gaussian weights A_jk
+};
+
+// calculate_coeffs (mzr.jl:50-79) per chain: one block per chain.
+__global__ void k_mzr_map(const double *__restrict__ theta, HmcConst c, MzrDev z,
+                          double *__restrict__ r) {
+    const int b = blockIdx.x;
+    const double *th = theta + (int64_t)b * c.D;
+    double *cum = z.aux + (int64_t)b * 4 * z.nages, *mu = cum + z.nages, *Asum = mu + z.nages;
+    double alpha = c.alpha, beta = c.beta, sigma = c.sigma;
+    int q = z.nages;
+    if (c.alpha_free) alpha = exp(th[q++]);
+    if (c.beta_free) beta = th[q++];
+    if (c.sigma_free) sigma = exp(th[q++]);
+    if (threadIdx.x == 0) {
+        double acc = 0.0;  // cumsum in decreasing-age order
+        for (int p = 0; p < z.nages; ++p) {
+            const int j = z.sorted[p];
+            acc += exp(th[j]);
+            cum[j] = acc;
+        }
+        for (int j = 0; j < z.nages; ++j) mu[j] = beta + alpha * (log10(cum[j]) - c.logM0);
+    }
+    __syncthreads();
+    double *A = z.A + (int64_t)b * z.nt;
+    for (int k = threadIdx.x; k < z.nt; k += blockDim.x) {
+        const double dd = (z.MH[k] - mu[z.jidx[k]]) / sigma;
+        A[k] = exp(-dd * dd / 2.0);  // dispersion_models.jl:92
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < z.nages; j += blockDim.x) {
+        double s = 0.0;
+        for (int q2 = z.age_off[j]; q2 < z.age_off[j + 1]; ++q2) s += A[z.age_tmpl[q2]];
+        Asum[j] = s;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < z.nt; k += blockDim.x) {
+        const int j = z.jidx[k];
+        r[(int64_t)b * z.nt + k] = A[k] * exp(th[j]) / Asum[j];
+    }
+}
+
+// Chain rule of mzr.jl:131-209 (gradient of -logL w.r.t. R_j, α, β, σ) followed by the
+// transforms and Jacobian terms of generic_fitting.jl:143-171; writes ∇ log p and log p.
+__global__ void k_mzr_grad(const double *__restrict__ theta, const double *__restrict__ r,
+                           const float *__restrict__ Gfg, const double *__restrict__ negL,
+                           HmcConst c, MzrDev z, double *__restrict__ g, double *__restrict__ logd,
+                           int want_logd) {
+    extern __shared__ double sm[];
+    const int b = blockIdx.x;
+    const int na = z.nages;
+    double *Gv = sm;                 // na + 3: gradient of -logL w.r.t. (R, α, β, σ)
+    double *ksR = Gv + na + 3;       // per age: Σ dA/dR
+    double *ksMu = ksR + na;         // Σ dA/dμ
+    double *ksS = ksMu + na;         // Σ dA/dσ
+    double *ksDr = ksS + na;         // Σ drjk/dRj
+    double *t1 = ksDr + na;          // Σ fullG (r/R + ...)
+    double *ps = t1 + na;            // psum per age
+    double *ss = ps + na;            // ssum per age
+    const double *th = theta + (int64_t)b * c.D;
+    const double *cum = z.aux + (int64_t)b * 4 * na, *mu = cum + na, *Asum = mu + na;
+    const double *A = z.A + (int64_t)b * z.nt;
+    const float *G = Gfg + (int64_t)b * z.nt;
+    double alpha = c.alpha, sigma = c.sigma;
+    {
+        int q = na;
+        if (c.alpha_free) alpha = exp(th[q++]);
+        if (c.beta_free) ++q;
+        if (c.sigma_free) sigma = exp(th[q++]);
+    }
+    const double ln10 = 2.302585092994046;
+    // per-age sums in fixed template order (deterministic)
+    for (int j = threadIdx.x; j < na; j += blockDim.x) {
+        const double Rj = exp(th[j]);
+        const double dmu_dR = alpha / cum[j] / ln10;
+        double sR = 0.0, sM = 0.0, sS = 0.0;
+        for (int q2 = z.age_off[j]; q2 < z.age_off[j + 1]; ++q2) {
+            const int k = z.age_tmpl[q2];
+            const double d = z.MH[k] - mu[j];
+            const double dAmu = A[k] * d / (sigma * sigma);
+            sR += dAmu * dmu_dR;
+            sM += dAmu;
+            sS += A[k] * d * d / (sigma * sigma * sigma);
+        }
+        ksR[j] = sR;
+        ksMu[j] = sM;
+        ksS[j] = sS;
+        double dr = 0.0, tt = 0.0, psum = 0.0, ssum = 0.0;
+        const double Av = Asum[j];
+        for (int q2 = z.age_off[j]; q2 < z.age_off[j + 1]; ++q2) {
+            const int k = z.age_tmpl[q2];
+            const double fullG = -(double)G[k];  // ∂logL/∂r_k
+            const double d = z.MH[k] - mu[j];
+            const double dAmu = A[k] * d / (sigma * sigma);
+            const double dAR = dAmu * dmu_dR;
+            const double dAs = A[k] * d * d / (sigma * sigma * sigma);
+            dr += fullG * (Rj / Av * (dAR - A[k] * sR / Av));
+            tt += fullG * (r[(int64_t)b * z.nt + k] / Rj + (dAR - sR * A[k] / Av) * Rj / Av);
+            psum -= fullG * Rj / Av * (dAmu - A[k] / Av * sM);
+            ssum += fullG * Rj / Av * (dAs - A[k] / Av * sS);
+        }
+        ksDr[j] = dr;
+        t1[j] = tt;
+        ps[j] = psum;
+        ss[j] = ssum;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < na + 3; ++q) Gv[q] = 0.0;
+        double acc = 0.0;  // reverse cumulative sum over the decreasing-age order
+        for (int p = na - 1; p >= 1; --p) {
+            acc += ksDr[z.sorted[p]];
+            Gv[z.sorted[p - 1]] -= acc;
+        }
+        for (int j = 0; j < na; ++j) {
+            Gv[j] -= t1[j];
+            Gv[na] += ps[j] * (log10(cum[j]) - c.logM0);  // ∂μ/∂α
+            Gv[na + 1] += ps[j];                          // ∂μ/∂β = 1
+            Gv[na + 2] -= ss[j];
+        }
+        // ∇ log p over the free variables; log p = logL + Σ log(positive x)
+        double* gb = g + (int64_t)b * c.D;
+        double jac = 0.0;
+        for (int j = 0; j < na; ++j) {
+            const double Rj = exp(th[j]);
+            gb[j] = -Gv[j] * Rj + 1.0;
+            jac += th[j];
+        }
+        int q = na;
+        if (c.alpha_free) { gb[q] = -Gv[na] * alpha + 1.0; jac += th[q]; ++q; }
+        if (c.beta_free) { gb[q] = -Gv[na + 1]; ++q; }
+        if (c.sigma_free) { gb[q] = -Gv[na + 2] * sigma + 1.0; jac += th[q]; ++q; }
+        if (want_logd) logd[b] = -negL[b] + jac;
+    }
+}
+
+struct HmcRun {
+    HmcConst c;
+    ChainState s;
+    MzrDev z;
+    SfhBatchedPlan plan;
+    double *d_r = nullptr, *d_negL = nullptr;
+    float *d_G = nullptr;
+    double eps_abs;
+};
+
+int launch_eval(sfh_ctx *ctx, const sfh_models *m, HmcRun &h, bool want_logd) {
+    cudaStream_t st = ctx->stream;
+    const int64_t n = (int64_t)h.c.B * m->nt;
+    if (h.c.model == 0) {
+        k_direct_map<<<(unsigned)((n + kT - 1) / kT), kT, 0, st>>>(h.s.theta, n, h.d_r);
+    } else {
+        k_mzr_map<<<h.c.B, kT, 0, st>>>(h.s.theta, h.c, h.z, h.d_r);
+    }
+    SFH_LAUNCHED(ctx);
+    int rc = sfh_batched_launch(ctx, m, h.plan, h.d_r, want_logd ? h.d_negL : nullptr, h.d_G,
+                                h.eps_abs);
+    if (rc) return rc;
+    if (h.c.model == 0) {
+        k_direct_grad<<<h.c.B, kT, 0, st>>>(h.s.theta, h.d_r, h.d_G, h.d_negL, h.c.D, h.s.g,
+                                            h.s.logd, want_logd ? 1 : 0);
+    } else {
+        const size_t sm = (size_t)(h.z.nages * 8 + 3) * sizeof(double);
+        k_mzr_grad<<<h.c.B, 64, sm, st>>>(h.s.theta, h.d_r, h.d_G, h.d_negL, h.c, h.z, h.s.g,
+                                          h.s.logd, want_logd ? 1 : 0);
+    }
+    SFH_LAUNCHED(ctx);
+    return SFH_OK;
+}
+
+int launch_trajectory(sfh_ctx *ctx, const sfh_models *m, HmcRun &h) {
+    cudaStream_t st = ctx->stream;
+    const int64_t n = (int64_t)h.c.B * h.c.D;
+    const unsigned gb = (unsigned)((n + kT - 1) / kT);
+    k_refresh<<<h.c.B, kT, 0, st>>>(h.s, h.c);
+    SFH_LAUNCHED(ctx);
+    for (int l = 0; l < h.c.nleap; ++l) {
+        k_kick_drift<<<gb, kT, 0, st>>>(h.s, h.c, l == 0 ? 0.5 : 1.0, 1);
+        SFH_LAUNCHED(ctx);
+        int rc = launch_eval(ctx, m, h, l == h.c.nleap - 1);
+        if (rc) return rc;
+    }
+    k_kick_drift<<<gb, kT, 0, st>>>(h.s, h.c, 0.5, 0);
+    SFH_LAUNCHED(ctx);
+    k_accept<<<h.c.B, kT, 0, st>>>(h.s, h.c);
+    SFH_LAUNCHED(ctx);
+    k_adapt_mass<<<(unsigned)((std::max(h.c.D, h.c.B) + kT - 1) / kT), kT, 0, st>>>(h.s, h.c);
+    SFH_LAUNCHED(ctx);
+    k_next_traj<<<1, 1, 0, st>>>(h.s);
+    SFH_LAUNCHED(ctx);
+    return SFH_OK;
+}
+
+__global__ void k_init_state(ChainState s, HmcConst c, double step0) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < (int64_t)c.B * c.D) {
+        s.mean[k] = 0.0;
+        s.m2[k] = 0.0;
+    }
+    if (k < c.D) s.minv[k] = 1.0;
+    if (k < c.B) {
+        s.eps[k] = step0;
+        s.acc_sum[k] = 0.0;
+        s.da[4 * k + 0] = log(10.0 * step0);
+        s.da[4 * k + 1] = 0.0;
+        s.da[4 * k + 2] = 0.0;
+        s.da[4 * k + 3] = 0.0;
+    }
+    if (k == 0) *s.t = 0;
+}
+
+__global__ void k_finish(ChainState s, HmcConst c, double *mean, double *var, double *acc,
+                         double *eps) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < (int64_t)c.B * c.D) {
+        if (mean) mean[k] = s.mean[k];
+        if (var) var[k] = c.nsamp > 1 ? s.m2[k] / (double)(c.nsamp - 1) : 0.0;
+    }
+    if (k < c.B) {
+        if (acc) acc[k] = c.nsamp > 0 ? s.acc_sum[k] / (double)c.nsamp : 0.0;
+        if (eps) eps[k] = s.eps[k];
+    }
+}
+
+
+// Validates the configuration, allocates the run's device buffers (recorded in `owned`)
+// and prepares the batched objective for nchains vectors.
+int setup_run(sfh_ctx *ctx, const sfh_models *m, const double *d_data, const sfh_hmc_config *cfg,
+              float *d_draws, HmcRun &h, std::vector<void *> &owned) {
+    if (!ctx || !m || !d_data || !cfg) return SFH_ERR_ARG;
+    if (m->storage != SFH_BF16X2)
+        return sfh_set_error(ctx, SFH_ERR_ARG, "HMC needs models stored as SFH_BF16X2");
+    if (cfg->nchains < 1 || cfg->nleap < 1 || cfg->ntraj < 0 || cfg->nwarmup < 0 ||
+        !(cfg->step0 > 0) || !(cfg->target_accept > 0 && cfg->target_accept < 1))
+        return sfh_set_error(ctx, SFH_ERR_ARG, "invalid HMC configuration");
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    HmcConst &c = h.c;
+    c.B = cfg->nchains;
+    c.model = cfg->model;
+    c.nwarm = cfg->nwarmup;
+    c.nsamp = cfg->ntraj;
+    c.nleap = cfg->nleap;
+    c.target = cfg->target_accept;
+    c.seed = cfg->seed;
+    c.thin = cfg->thin > 0 ? cfg->thin : 1;
+    c.ndraws = d_draws ? (cfg->ntraj + c.thin - 1) / c.thin : 0;
+    h.eps_abs = 2.220446049250313e-16;
+    const int nt = (int)m->nt;
+    std::vector<int> jidx, age_off, age_tmpl, sorted;
+    if (c.model == SFH_HMC_DIRECT) {
+        c.D = nt;
+    } else if (c.model == SFH_HMC_MZR) {
+        if (cfg->nages < 1 || !cfg->h_age_index || !cfg->h_logAge || !cfg->h_MH ||
+            !(cfg->alpha >= 0) || !(cfg->sigma > 0))
+            return sfh_set_error(ctx, SFH_ERR_ARG, "invalid MZR description");
+        c.nages = cfg->nages;
+        c.alpha_free = cfg->alpha_free ? 1 : 0;
+        c.beta_free = cfg->beta_free ? 1 : 0;
+        c.sigma_free = cfg->sigma_free ? 1 : 0;
+        c.alpha = cfg->alpha;
+        c.beta = cfg->beta;
+        c.sigma = cfg->sigma;
+        c.logM0 = cfg->logMstar0;
+        c.D = c.nages + c.alpha_free + c.beta_free + c.sigma_free;
+        jidx.assign(cfg->h_age_index, cfg->h_age_index + nt);
+        age_off.assign(c.nages + 1, 0);
+        for (int k = 0; k < nt; ++k) {
+            if (jidx[k] < 0 || jidx[k] >= c.nages)
+                return sfh_set_error(ctx, SFH_ERR_ARG, "age index out of range");
+            age_off[jidx[k] + 1]++;
+        }
+        for (int j = 0; j < c.nages; ++j) age_off[j + 1] += age_off[j];
+        age_tmpl.assign(nt, 0);
+        std::vector<int> fill(age_off.begin(), age_off.end() - 1);
+        for (int k = 0; k < nt; ++k) age_tmpl[fill[jidx[k]]++] = k;
+        sorted.resize(c.nages);
+        for (int j = 0; j < c.nages; ++j) sorted[j] = j;
+        std::stable_sort(sorted.begin(), sorted.end(),
+                         [&](int a, int b) { return cfg->h_logAge[a] > cfg->h_logAge[b]; });
+    } else {
+        return sfh_set_error(ctx, SFH_ERR_ARG, "unknown HMC model");
+    }
+    const int64_t BD = (int64_t)c.B * c.D;
+    // ---- device buffers for the run (freed by the caller)
+    auto alloc = [&](size_t bytes) -> void * {
+        void *p = nullptr;
+        if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) return nullptr;
+        owned.push_back(p);
+        return p;
+    };
+    ChainState &s = h.s;
+    s.theta = (double *)alloc(BD * 8);
+    s.p = (double *)alloc(BD * 8);
+    s.g = (double *)alloc(BD * 8);
+    s.theta0 = (double *)alloc(BD * 8);
+    s.g0 = (double *)alloc(BD * 8);
+    s.mean = (double *)alloc(BD * 8);
+    s.m2 = (double *)alloc(BD * 8);
+    s.logd = (double *)alloc(c.B * 8);
+    s.logd0 = (double *)alloc(c.B * 8);
+    s.kin0 = (double *)alloc(c.B * 8);
+    s.eps = (double *)alloc(c.B * 8);
+    s.da = (double *)alloc(c.B * 4 * 8);
+    s.acc_sum = (double *)alloc(c.B * 8);
+    s.minv = (double *)alloc(c.D * 8);
+    s.t = (int64_t *)alloc(8);
+    s.draws = d_draws;
+    h.d_r = (double *)alloc((size_t)c.B * nt * 8);
+    h.d_negL = (double *)alloc(c.B * 8);
+    h.d_G = (float *)alloc((size_t)c.B * nt * 4);
+    if (c.model == SFH_HMC_MZR) {
+        int *dj = (int *)alloc(nt * 4), *dao = (int *)alloc((c.nages + 1) * 4);
+        int *dat = (int *)alloc(nt * 4), *dso = (int *)alloc(c.nages * 4);
+        double *dmh = (double *)alloc(nt * 8);
+        h.z.aux = (double *)alloc((size_t)c.B * 4 * c.nages * 8);
+        h.z.A = (double *)alloc((size_t)c.B * nt * 8);
+        for (void *p : owned)
+            if (!p) return sfh_set_error(ctx, SFH_ERR_NOMEM, "HMC buffers");
+        cudaMemcpy(dj, jidx.data(), nt * 4, cudaMemcpyHostToDevice);
+        cudaMemcpy(dao, age_off.data(), (c.nages + 1) * 4, cudaMemcpyHostToDevice);
+        cudaMemcpy(dat, age_tmpl.data(), nt * 4, cudaMemcpyHostToDevice);
+        cudaMemcpy(dso, sorted.data(), c.nages * 4, cudaMemcpyHostToDevice);
+        cudaMemcpy(dmh, cfg->h_MH, nt * 8, cudaMemcpyHostToDevice);
+        h.z.nt = nt;
+        h.z.nages = c.nages;
+        h.z.jidx = dj;
+        h.z.age_off = dao;
+        h.z.age_tmpl = dat;
+        h.z.sorted = dso;
+        h.z.MH = dmh;
+    }
+    for (void *p : owned)
+        if (!p) return sfh_set_error(ctx, SFH_ERR_NOMEM, "HMC buffers");
+    int rc;
+    if ((rc = sfh_batched_prepare(ctx, m, c.B, d_data, nullptr, 0, &h.plan))) return rc;
+    if ((rc = sfh_scratch_reserve(ctx, h.plan.scratch_bytes))) return rc;
+    return sfh_batched_prepare(ctx, m, c.B, d_data, ctx->scratch, ctx->scratch_bytes, &h.plan);
+}
+
+void free_run(sfh_ctx *ctx, std::vector<void *> &owned) {
+    cudaStreamSynchronize(ctx->stream);
+    for (void *p : owned) cudaFree(p);
+    owned.clear();
+}
+
+}  // namespace
+
+extern "C" int sfh_logdensity_batched_dev(sfh_ctx *ctx, const sfh_models *m, const double *d_data,
+                                          const sfh_hmc_config *cfg, const double *d_theta,
+                                          double *d_logd, double *d_grad) {
+    if (!ctx || !m || !d_data || !cfg || !d_theta || !d_logd || !d_grad) return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    HmcRun h{};
+    std::vector<void *> owned;
+    int rc = setup_run(ctx, m, d_data, cfg, nullptr, h, owned);
+    if (!rc) {
+        const int64_t BD = (int64_t)h.c.B * h.c.D;
+        // evaluate into the run's state arrays, then copy out
+        cudaMemcpyAsync(h.s.theta, d_theta, BD * 8, cudaMemcpyDeviceToDevice, ctx->stream);
+        rc = launch_eval(ctx, m, h, true);
+        if (!rc) rc = sfh_batched_check(ctx, h.plan);
+        if (!rc) {
+            cudaMemcpyAsync(d_logd, h.s.logd, (size_t)h.c.B * 8, cudaMemcpyDeviceToDevice, ctx->stream);
+            cudaMemcpyAsync(d_grad, h.s.g, BD * 8, cudaMemcpyDeviceToDevice, ctx->stream);
+        }
+    }
+    free_run(ctx, owned);
+    return rc;
+}
+
+extern "C" int sfh_hmc_sample_dev(sfh_ctx *ctx, const sfh_models *m, const double *d_data,
+                                  const sfh_hmc_config *cfg, const double *d_theta0,
+                                  double *d_mean, double *d_var, double *d_accept,
+                                  double *d_step, float *d_draws) {
+    if (!ctx || !m || !d_data || !cfg || !d_theta0) return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    HmcRun h{};
+    std::vector<void *> owned;
+    auto cleanup = [&]() { free_run(ctx, owned); };
+    int rc = setup_run(ctx, m, d_data, cfg, d_draws, h, owned);
+    if (rc) { cleanup(); return rc; }
+    HmcConst &c = h.c;
+    ChainState &s = h.s;
+    const int64_t BD = (int64_t)c.B * c.D;
+    cudaStream_t st = ctx->stream;
+    SFH_CK(ctx, cudaMemcpyAsync(s.theta, d_theta0, BD * 8, cudaMemcpyDeviceToDevice, st));
+    k_init_state<<<(unsigned)((std::max(BD, (int64_t)std::max(c.B, c.D)) + kT - 1) / kT), kT, 0, st>>>(
+        s, c, cfg->step0);
+    SFH_LAUNCHED(ctx);
+    // gradient and log density at the starting points (eager: also warms every kernel)
+    if ((rc = launch_eval(ctx, m, h, true))) { cleanup(); return rc; }
+    if ((rc = sfh_batched_check(ctx, h.plan))) { cleanup(); return rc; }
+    // capture one trajectory and replay it
+    const int64_t ntot = c.nwarm + c.nsamp;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool use_graph = ntot > 1;
+    if (use_graph) {
+        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) use_graph = false;
+    }
+    if (use_graph) {
+        rc = launch_trajectory(ctx, m, h);
+        cudaError_t e = cudaStreamEndCapture(st, &graph);
+        if (rc || e != cudaSuccess || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            cudaGetLastError();
+            use_graph = false;
+            exec = nullptr;
+        }
+    }
+    for (int64_t t = 0; t < ntot; ++t) {
+        if (use_graph) {
+            if (cudaGraphLaunch(exec, st) != cudaSuccess) { rc = sfh_cuda_error(ctx, cudaGetLastError(), "graph launch"); break; }
+            ctx->launches += 7 * c.nleap + 6;
+        } else if ((rc = launch_trajectory(ctx, m, h))) {
+            break;
+        }
+        if ((t & 63) == 63 && (rc = sfh_batched_check(ctx, h.plan))) break;
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (!rc) rc = sfh_batched_check(ctx, h.plan);
+    if (!rc) {
+        k_finish<<<(unsigned)((std::max(BD, (int64_t)c.B) + kT - 1) / kT), kT, 0, st>>>(
+            s, c, d_mean, d_var, d_accept, d_step);
+        cudaGetLastError();
+    }
+    cleanup();
+    return rc;
+}

@@ -127,7 +127,25 @@ int sfh_launch_fg(sfh_ctx *ctx, const sfh_models *m, const FgArgs &a, cudaEvent_
 int sfh_launch_loglikelihood(sfh_ctx *ctx, const double *composite, const double *data,
                              int64_t nbins, double eps, double *d_out);
 
-// Batched objective (batched.cu).
+// Batched objective (batched.cu).  prepare() sizes/lays out scratch (scratch == NULL
+// is a size query), converts the data and encodes the tensor maps; launch() only
+// enqueues kernels (capturable in a CUDA graph); check() reads the timeout flag.
+#include <cuda.h>
+struct SfhBatchedPlan {
+    int64_t B = 0, B_pad = 0;
+    int m_tiles = 0, n_tiles1 = 0, n_tiles2 = 0, ks2 = 1, per2 = 0, kb2 = 0;
+    size_t scratch_bytes = 0;
+    __nv_bfloat16 *Rh = nullptr, *Rl = nullptr, *Wh = nullptr, *Wl = nullptr;
+    float2 *lp = nullptr;
+    float *gp = nullptr, *dataf = nullptr;
+    int *err = nullptr;
+    CUtensorMap maps[8];
+};
+int sfh_batched_prepare(sfh_ctx *ctx, const sfh_models *m, int64_t B, const double *d_data,
+                        void *scratch, size_t scratch_bytes, SfhBatchedPlan *pl);
+int sfh_batched_launch(sfh_ctx *ctx, const sfh_models *m, const SfhBatchedPlan &pl,
+                       const double *d_R, double *d_negLogL, float *d_G, double eps);
+int sfh_batched_check(sfh_ctx *ctx, const SfhBatchedPlan &pl);
 int sfh_launch_fg_batched(sfh_ctx *ctx, const sfh_models *m, const double *d_R, int64_t B,
                           const double *d_data, double *d_negLogL, float *d_G, double eps);
 // Builds the BF16 hi/lo planes from an FP32 column-major matrix (batched.cu).

@@ -9,6 +9,8 @@ from .core import Context, Models, as_models, default_context
 from .fitting import (composite_, construct_x0, fg_, fg_batched, fit_templates, fit_templates_fast,
                       fit_templates_lbfgsb, grad_loglikelihood, grad_loglikelihood_, loglikelihood,
                       renormalize_x0, stack_models)
+from .sampling import (GaussianDispersion, PowerLawMZR, calculate_coeffs, hmc_sample,
+                       logdensity_batched, sample_sfh)
 from .templates import (BrokenPowerLawIMF, Histogram, Kroupa2001, Martin2016_complete,
                         bin_cmd_smooth, calculate_edges, calculate_weights, compl_model, err_model,
                         exp_photerr, histogram_data, histogram_pix, interpolate_mini, midpoints,
@@ -22,5 +24,6 @@ __all__ = [
     "Histogram", "Kroupa2001", "Martin2016_complete", "bin_cmd_smooth", "calculate_edges",
     "calculate_weights", "compl_model", "err_model", "exp_photerr", "histogram_data",
     "histogram_pix", "interpolate_mini", "midpoints", "mini_spacing", "partial_cmd_smooth",
-    "partial_cmd_smooth_batch",
+    "partial_cmd_smooth_batch", "GaussianDispersion", "PowerLawMZR", "calculate_coeffs",
+    "hmc_sample", "logdensity_batched", "sample_sfh",
 ]

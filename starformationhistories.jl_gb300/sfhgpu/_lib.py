@@ -24,7 +24,8 @@ EXPORTED = [
     "sfh_ctx_last_error", "sfh_ctx_synchronize", "sfh_ctx_stream", "sfh_ctx_launch_count",
     "sfh_models_upload", "sfh_models_from_device", "sfh_models_free", "sfh_models_info",
     "sfh_composite", "sfh_loglikelihood", "sfh_grad_loglikelihood", "sfh_fg", "sfh_fg_dev",
-    "sfh_fg_batched_dev", "sfh_fg_kernel_times", "sfh_fg_dev_noalloc", "sfh_bin_cmd_smooth", "sfh_bin_cmd_smooth_batch_dev",
+    "sfh_fg_batched_dev", "sfh_fg_kernel_times", "sfh_fg_dev_noalloc", "sfh_hmc_sample_dev",
+    "sfh_logdensity_batched_dev", "sfh_bin_cmd_smooth", "sfh_bin_cmd_smooth_batch_dev",
     "sfh_partial_cmd_smooth_batch_dev",
 ]
 

@@ -1,0 +1,197 @@
+"""Batched HMC and hierarchical (MZR) log densities over the GPU C ABI.
+
+Mirrors hmc_sample (src/fitting/hmc_sample.jl:105-141) and the PowerLawMZR /
+GaussianDispersion sampling of sample_sfh (src/fitting/hierarchical/generic_fitting.jl:
+458-527) with all chains advanced together on the tensor cores
+(sfh_hmc_sample_dev), plus the batched logdensity_and_gradient
+(sfh_logdensity_batched_dev).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from ._lib import check, load
+from .core import Models
+
+SFH_HMC_DIRECT, SFH_HMC_MZR = 0, 1
+
+
+class HMCConfig(C.Structure):
+    _fields_ = [("nchains", C.c_int32), ("model", C.c_int32), ("ntraj", C.c_int64),
+                ("nwarmup", C.c_int64), ("nleap", C.c_int32), ("thin", C.c_int32),
+                ("step0", C.c_double), ("target_accept", C.c_double), ("seed", C.c_uint64),
+                ("nages", C.c_int32), ("h_age_index", C.POINTER(C.c_int32)),
+                ("h_logAge", C.POINTER(C.c_double)), ("h_MH", C.POINTER(C.c_double)),
+                ("logMstar0", C.c_double), ("alpha_free", C.c_int32), ("beta_free", C.c_int32),
+                ("sigma_free", C.c_int32), ("alpha", C.c_double), ("beta", C.c_double),
+                ("sigma", C.c_double)]
+
+
+def _bind():
+    L = load()
+    if not getattr(L, "_sfh_hmc_bound", False):
+        vp, i64 = C.c_void_p, C.c_int64
+        L.sfh_hmc_sample_dev.argtypes = [vp, vp, vp, C.POINTER(HMCConfig), vp, vp, vp, vp, vp, vp]
+        L.sfh_hmc_sample_dev.restype = C.c_int
+        L.sfh_logdensity_batched_dev.argtypes = [vp, vp, vp, C.POINTER(HMCConfig), vp, vp, vp]
+        L.sfh_logdensity_batched_dev.restype = C.c_int
+        L._sfh_hmc_bound = True
+        del i64
+    return L
+
+
+@dataclass
+class PowerLawMZR:
+    """PowerLawMZR(α, MH0, logMstar0, free), src/fitting/hierarchical/mzr.jl:263-284."""
+    alpha: float
+    MH0: float
+    logMstar0: float = 6.0
+    free: tuple = (True, True)
+
+    def __call__(self, Mstar):
+        return self.MH0 + self.alpha * (np.log10(Mstar) - self.logMstar0)
+
+
+@dataclass
+class GaussianDispersion:
+    """GaussianDispersion(σ, free), src/fitting/hierarchical/dispersion_models.jl:80-110."""
+    sigma: float
+    free: tuple = (True,)
+
+    def __call__(self, x, mu):
+        return np.exp(-((np.asarray(x) - mu) / self.sigma) ** 2 / 2)
+
+
+def calculate_coeffs(mzr: PowerLawMZR, disp: GaussianDispersion, mstars, logAge, MH):
+    """calculate_coeffs (mzr.jl:50-79) on the host (a handful of values per age)."""
+    logAge, MH = np.asarray(logAge, float), np.asarray(MH, float)
+    uniq = list(dict.fromkeys(logAge.tolist()))
+    mstars = np.asarray(mstars, float)
+    if len(mstars) != len(uniq):
+        raise ValueError("Length of `mstars` must be the same as `unique(logAge)`.")
+    order = np.argsort(-np.asarray(uniq), kind="stable")
+    cum = np.empty(len(uniq))
+    cum[order] = np.cumsum(mstars[order])
+    out = np.empty_like(logAge)
+    for i, la in enumerate(uniq):
+        idx = np.nonzero(logAge == la)[0]
+        w = disp(MH[idx], mzr(cum[i]))
+        out[idx] = w * mstars[i] / w.sum()
+    return out
+
+
+def _config(nchains, model, nsteps=0, nwarmup=0, nleap=10, thin=1, step0=0.01, target=0.8,
+            seed=0x5F3759DF, mzr=None, disp=None, logAge=None, MH=None):
+    cfg = HMCConfig()
+    cfg.nchains, cfg.model = int(nchains), int(model)
+    cfg.ntraj, cfg.nwarmup, cfg.nleap, cfg.thin = int(nsteps), int(nwarmup), int(nleap), int(thin)
+    cfg.step0, cfg.target_accept, cfg.seed = float(step0), float(target), int(seed)
+    keep = []
+    if model == SFH_HMC_MZR:
+        logAge = np.asarray(logAge, float)
+        uniq = list(dict.fromkeys(logAge.tolist()))
+        age_index = np.ascontiguousarray([uniq.index(a) for a in logAge], dtype=np.int32)
+        ua = np.ascontiguousarray(uniq, dtype=np.float64)
+        mh = np.ascontiguousarray(MH, dtype=np.float64)
+        keep += [age_index, ua, mh]
+        cfg.nages = len(uniq)
+        cfg.h_age_index = age_index.ctypes.data_as(C.POINTER(C.c_int32))
+        cfg.h_logAge = ua.ctypes.data_as(C.POINTER(C.c_double))
+        cfg.h_MH = mh.ctypes.data_as(C.POINTER(C.c_double))
+        cfg.logMstar0 = float(mzr.logMstar0)
+        cfg.alpha_free, cfg.beta_free = int(bool(mzr.free[0])), int(bool(mzr.free[1]))
+        cfg.sigma_free = int(bool(disp.free[0]))
+        cfg.alpha, cfg.beta, cfg.sigma = float(mzr.alpha), float(mzr.MH0), float(disp.sigma)
+    return cfg, keep
+
+
+def mzr_theta(mstars, mzr: PowerLawMZR, disp: GaussianDispersion):
+    """Transformed variables [log R_j..., log α, β, log σ] (free ones only), the order
+    used by logdensity_and_gradient (generic_fitting.jl:117-136)."""
+    th = list(np.log(np.asarray(mstars, float)))
+    if mzr.free[0]:
+        th.append(np.log(mzr.alpha))
+    if mzr.free[1]:
+        th.append(mzr.MH0)
+    if disp.free[0]:
+        th.append(np.log(disp.sigma))
+    return np.asarray(th)
+
+
+def logdensity_batched(models: Models, data, theta, model=SFH_HMC_DIRECT, mzr=None, disp=None,
+                       logAge=None, MH=None):
+    """log p and ∇ log p for B parameter vectors (rows of theta) in one batched call."""
+    import torch
+    L = _bind()
+    dev = torch.device("cuda", models.ctx.device)
+    th = torch.as_tensor(np.asarray(theta, float), device=dev).contiguous()
+    n = torch.as_tensor(np.asarray(data, float).reshape(-1), device=dev).contiguous()
+    B = th.shape[0]
+    cfg, keep = _config(B, model, mzr=mzr, disp=disp, logAge=logAge, MH=MH)
+    logd = torch.empty(B, dtype=torch.float64, device=dev)
+    grad = torch.empty_like(th)
+    torch.cuda.synchronize(dev)
+    check(L.sfh_logdensity_batched_dev(models.ctx.handle, models.handle, n.data_ptr(),
+                                       C.byref(cfg), th.data_ptr(), logd.data_ptr(),
+                                       grad.data_ptr()), models.ctx.handle, "logdensity_batched")
+    del keep
+    return logd.cpu().numpy(), grad.cpu().numpy()
+
+
+def _run_hmc(models, data, theta0, cfg, keep, keep_draws):
+    import torch
+    L = _bind()
+    dev = torch.device("cuda", models.ctx.device)
+    th0 = torch.as_tensor(np.asarray(theta0, float), device=dev).contiguous()
+    n = torch.as_tensor(np.asarray(data, float).reshape(-1), device=dev).contiguous()
+    B, D = th0.shape
+    mean = torch.empty((B, D), dtype=torch.float64, device=dev)
+    var = torch.empty_like(mean)
+    acc = torch.empty(B, dtype=torch.float64, device=dev)
+    step = torch.empty(B, dtype=torch.float64, device=dev)
+    ndraw = (cfg.ntraj + cfg.thin - 1) // cfg.thin
+    draws = torch.empty((B, ndraw, D), dtype=torch.float32, device=dev) if keep_draws else None
+    torch.cuda.synchronize(dev)
+    check(L.sfh_hmc_sample_dev(models.ctx.handle, models.handle, n.data_ptr(), C.byref(cfg),
+                               th0.data_ptr(), mean.data_ptr(), var.data_ptr(), acc.data_ptr(),
+                               step.data_ptr(), draws.data_ptr() if keep_draws else None),
+          models.ctx.handle, "hmc")
+    del keep
+    out = {"mean": mean.cpu().numpy(), "var": var.cpu().numpy(), "accept": acc.cpu().numpy(),
+           "step": step.cpu().numpy()}
+    if keep_draws:
+        out["draws"] = draws.cpu().numpy()
+    return out
+
+
+def hmc_sample(models: Models, data, nsteps, nchains=1, nwarmup=200, nleap=10, step0=0.01,
+               target_accept=0.8, seed=20261203, theta0=None, keep_draws=False, thin=1):
+    """hmc_sample(models, data, nsteps, nchains), hmc_sample.jl:105-141: posterior of the
+    log coefficients, all chains in lock step.  Returns a dict with per-chain posterior
+    mean / variance of the coefficients (natural scale), acceptance and step size, and
+    optionally the draws (nchains x ceil(nsteps/thin) x ntemplates)."""
+    if theta0 is None:
+        from .fitting import renormalize_x0
+        x0 = renormalize_x0(np.asarray(data, float).reshape(-1), models, np.ones(models.nt))
+        rng = np.random.default_rng(seed)
+        theta0 = np.log(x0)[None, :] + 0.1 * rng.standard_normal((nchains, models.nt))
+    cfg, keep = _config(nchains, SFH_HMC_DIRECT, nsteps, nwarmup, nleap, thin, step0,
+                        target_accept, seed)
+    return _run_hmc(models, data, theta0, cfg, keep, keep_draws)
+
+
+def sample_sfh(models: Models, data, logAge, MH, mzr: PowerLawMZR, disp: GaussianDispersion,
+               mstars0, nsteps, nchains=1, nwarmup=200, nleap=10, step0=0.01,
+               target_accept=0.8, seed=20261203, keep_draws=False, thin=1, jitter=0.05):
+    """Posterior sampling of (R_j, α, MH0, σ) under a PowerLawMZR + GaussianDispersion model
+    (sample_sfh, generic_fitting.jl:458-527), all chains in lock step.  Means are reported
+    on the natural scale in the order [R_j..., α, MH0, σ] (free parameters only)."""
+    th = mzr_theta(mstars0, mzr, disp)
+    rng = np.random.default_rng(seed)
+    theta0 = th[None, :] + jitter * rng.standard_normal((nchains, th.size))
+    cfg, keep = _config(nchains, SFH_HMC_MZR, nsteps, nwarmup, nleap, thin, step0,
+                        target_accept, seed, mzr=mzr, disp=disp, logAge=logAge, MH=MH)
+    return _run_hmc(models, data, theta0, cfg, keep, keep_draws)

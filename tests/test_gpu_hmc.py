@@ -1,0 +1,121 @@
+"""Batched HMC and the hierarchical (MZR) log density on the GPU.
+
+* The MZR log density and gradient (calculate_coeffs + chain rule of mzr.jl:84-215 and
+  the transforms / Jacobian terms of generic_fitting.jl:90-199) against the FP64 oracle
+  on the same stored templates.
+* hmc_sample's posterior against the Laplace approximation around the maximum
+  likelihood point (observed Fisher information), which the posterior approaches for
+  large counts; acceptance in range.
+* sample_sfh (PowerLawMZR + GaussianDispersion) recovers the generating parameters.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _bf16_hilo(x):
+    import torch
+    t = torch.tensor(np.asarray(x, dtype=np.float32))
+    hi = t.to(torch.bfloat16).to(torch.float32)
+    lo = (t - hi).to(torch.bfloat16).to(torch.float32)
+    return (hi.double() + lo.double()).numpy()
+
+
+def _mzr_problem(seed=11, nages=5, nmh=6, nbins=3000, scale=1.0):
+    from sfhgpu.sampling import GaussianDispersion, PowerLawMZR, calculate_coeffs
+    rng = np.random.default_rng(seed)
+    la = np.repeat(np.linspace(10.0, 8.0, nages), nmh)
+    mh = np.tile(np.linspace(-2.5, 0.0, nmh), nages)
+    M = (rng.random((nbins, nages * nmh)) / 1e2).astype(np.float32)
+    R = (rng.random(nages) * 1e4 + 1e3) * scale
+    mzr, disp = PowerLawMZR(0.5, -1.0, 6.0), GaussianDispersion(0.2)
+    coeffs = calculate_coeffs(mzr, disp, R, la, mh)
+    data = rng.poisson(M.astype(np.float64) @ coeffs).astype(np.float64)
+    return la, mh, np.asfortranarray(M), R, mzr, disp, data
+
+
+def test_mzr_logdensity_matches_oracle(sfh, O):
+    from sfhgpu.sampling import GaussianDispersion, PowerLawMZR, SFH_HMC_MZR, mzr_theta
+    la, mh, M32, R, mzr, disp, data = _mzr_problem()
+    H = sfh.Models(M32, storage="bf16x2")
+    Ms = np.asfortranarray(_bf16_hilo(M32))
+    rng = np.random.default_rng(5)
+    thetas, nats = [], []
+    for _ in range(6):
+        Rb = R * np.exp(0.2 * rng.standard_normal(R.size))
+        a = 0.5 * np.exp(0.2 * rng.standard_normal())
+        b = -1.0 + 0.1 * rng.standard_normal()
+        s = 0.2 * np.exp(0.2 * rng.standard_normal())
+        thetas.append(mzr_theta(Rb, PowerLawMZR(a, b, 6.0), GaussianDispersion(s)))
+        nats.append(np.concatenate([Rb, [a, b, s]]))
+    theta = np.stack(thetas)
+    logd, grad = sfh.logdensity_batched(H, data, theta, SFH_HMC_MZR, mzr, disp, la, mh)
+    nst = data.sum()
+    for k, v in enumerate(nats):
+        nlogL, Gv = O.mzr_fg(v, 6.0, Ms, data, la, mh)
+        na = R.size
+        ref_logd = -nlogL + np.sum(np.log(v[:na])) + np.log(v[na]) + np.log(v[na + 2])
+        ref_g = np.concatenate([-Gv[:na] * v[:na] + 1.0, [-Gv[na] * v[na] + 1.0, -Gv[na + 1],
+                                                          -Gv[na + 2] * v[na + 2] + 1.0]])
+        assert abs(logd[k] - ref_logd) <= 1e-2 * max(1.0, nst / 1e4), (logd[k], ref_logd)
+        scale = np.abs(ref_g).max()
+        np.testing.assert_allclose(grad[k], ref_g, rtol=2e-3, atol=2e-3 * scale)
+
+
+def test_direct_logdensity_matches_oracle(sfh, O):
+    from sfhgpu.sampling import SFH_HMC_DIRECT
+    rng = np.random.default_rng(2)
+    M32 = np.asfortranarray((rng.random((5000, 12)) * (rng.random((5000, 12)) > 0.3))
+                            .astype(np.float32))
+    x = rng.random(12) * 50 + 10
+    data = rng.poisson(M32.astype(np.float64) @ x).astype(np.float64)
+    H = sfh.Models(M32, storage="bf16x2")
+    Ms = np.asfortranarray(_bf16_hilo(M32))
+    theta = np.log(x)[None, :] + 0.1 * rng.standard_normal((5, 12))
+    logd, grad = sfh.logdensity_batched(H, data, theta, SFH_HMC_DIRECT)
+    for k in range(5):
+        xs = np.exp(theta[k])
+        v, G, _ = O.fg(xs, Ms, data)
+        # hmc_sample.jl:34-36: logL + Σθ and -G x + 1
+        assert abs(logd[k] - (-v + theta[k].sum())) <= 1e-2 * max(1.0, data.sum() / 1e4)
+        ref = -G * xs + 1.0
+        np.testing.assert_allclose(grad[k], ref, rtol=2e-3, atol=2e-3 * np.abs(ref).max())
+
+
+def test_hmc_direct_matches_laplace_posterior(sfh):
+    rng = np.random.default_rng(21)
+    nbins, nt = 4000, 4
+    M32 = np.asfortranarray((rng.random((nbins, nt)) ** 3).astype(np.float32))
+    x_true = np.array([2000.0, 1000.0, 3000.0, 500.0]) / 100
+    data = rng.poisson(M32.astype(np.float64) @ x_true).astype(np.float64)
+    Ms = np.asfortranarray(_bf16_hilo(M32))
+    _, mle = sfh.fit_templates_lbfgsb(sfh.Models(Ms, storage="f64"), data, x0=x_true,
+                                      factr=10.0, pgtol=1e-10)
+    m = Ms @ mle
+    Hobs = (Ms * (data / m ** 2)[:, None]).T @ Ms  # observed information at the MLE
+    sd_lap = np.sqrt(np.diag(np.linalg.inv(Hobs)))
+    H = sfh.Models(M32, storage="bf16x2")
+    out = sfh.hmc_sample(H, data, nsteps=400, nchains=64, nwarmup=300, nleap=10, seed=3)
+    pm = out["mean"].mean(axis=0)
+    pv = out["var"].mean(axis=0) + out["mean"].var(axis=0)
+    assert 0.5 < out["accept"].mean() < 0.995, out["accept"].mean()
+    assert np.all(np.abs(pm - mle) < 0.25 * sd_lap + 3 * np.sqrt(pv / (64 * 100))), (pm, mle, sd_lap)
+    ratio = np.sqrt(pv) / sd_lap
+    assert np.all((ratio > 0.8) & (ratio < 1.25)), ratio
+
+
+def test_hmc_mzr_recovers_parameters(sfh):
+    la, mh, M32, R, mzr, disp, data = _mzr_problem(seed=8, nbins=6000, scale=5.0)
+    H = sfh.Models(M32, storage="bf16x2")
+    from sfhgpu.sampling import GaussianDispersion, PowerLawMZR
+    out = sfh.sample_sfh(H, data, la, mh, PowerLawMZR(0.4, -0.8, 6.0), GaussianDispersion(0.3),
+                         R * 1.1, nsteps=300, nchains=32, nwarmup=300, nleap=10, seed=9)
+    na = R.size
+    pm = out["mean"].mean(axis=0)
+    psd = np.sqrt(out["var"].mean(axis=0) + out["mean"].var(axis=0))
+    truth = np.concatenate([R, [0.5, -1.0, 0.2]])
+    assert 0.4 < out["accept"].mean() < 0.995, out["accept"].mean()
+    z = np.abs(pm - truth) / psd
+    assert np.all(z[na:] < 4.0), (pm[na:], psd[na:])
+    assert np.median(z[:na]) < 3.0, z[:na]
