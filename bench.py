@@ -113,26 +113,18 @@ class Clocks:
 
 
 def _dist():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    from sfhgpu.replicas import dist_env
+    return dist_env()
 
 
 def _barrier(world):
-    if world > 1:
-        import torch.distributed as dist
-        dist.barrier()
+    from sfhgpu.replicas import barrier
+    barrier(world)
 
 
 def _max_over_ranks(world, x: float) -> float:
-    if world == 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from sfhgpu.replicas import max_over_ranks
+    return max_over_ranks(world, x)
 
 
 def _bf16_peak():
@@ -198,6 +190,145 @@ def run_batched(ctx, d_T, nbins, nt, r, data, M64, steps, warmup, B=4096, check=
         "dlogL_per_1e4_stars_vs_stored": float(np.max(np.abs(negL[:check] - ref_s)) / (nst / 1e4)),
         "dlogL_per_1e4_stars_vs_fp32_templates": float(
             np.max(np.abs(negL[:check] - ref_f)) / (nst / 1e4)),
+    }
+
+
+def run_hmc(ctx, d_T, w, nchains=1024, nwarmup=40, ntraj=40, nleap=10, seed=20261205):
+    """End-to-end hierarchical HMC (PowerLawMZR slope 0.5, GaussianDispersion 0.2) on the
+    1,200-template grid: all chains advance together, one batched tensor-core evaluation
+    per leapfrog substep, trajectories replayed from a captured CUDA graph."""
+    import numpy as np
+    import torch
+
+    import sfhgpu
+    from sfhgpu.sampling import GaussianDispersion, PowerLawMZR, calculate_coeffs
+    nbins, nt = w.nbins, w.ntempl
+    la, mh = w.template_params
+    Hb = sfhgpu.Models.from_device(d_T.data_ptr(), nbins, nt, storage="bf16x2", ctx=ctx)
+    rng = np.random.default_rng(seed)
+    mzr, disp = PowerLawMZR(0.5, -1.0, 6.0), GaussianDispersion(0.2)
+    R = np.exp(0.5 * rng.standard_normal(w.logAges.size))
+    M = d_T.double()
+    c = calculate_coeffs(mzr, disp, R, la, mh)
+    R = R * (1e6 / float((M.T @ torch.as_tensor(c, device=M.device)).sum()))
+    c = calculate_coeffs(mzr, disp, R, la, mh)
+    data = rng.poisson((M.T @ torch.as_tensor(c, device=M.device)).cpu().numpy()).astype(float)
+    del M
+    torch.cuda.synchronize()
+    l0 = ctx.launches
+    t0 = time.perf_counter()
+    out = sfhgpu.sample_sfh(Hb, data, la, mh, PowerLawMZR(0.45, -0.9, 6.0),
+                            GaussianDispersion(0.25), R * 1.1, nsteps=ntraj, nchains=nchains,
+                            nwarmup=nwarmup, nleap=nleap, step0=1e-3, seed=seed)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    launches = ctx.launches - l0
+    Hb.free()
+    substeps = nchains * (nwarmup + ntraj) * nleap
+    na = w.logAges.size
+    pm = out["mean"].mean(0)
+    return {
+        "workload": f"{nchains} chains x {nwarmup}+{ntraj} trajectories x {nleap} leapfrog "
+                    f"steps, PowerLawMZR + GaussianDispersion over {nt} templates x {nbins} bins",
+        "chain_gradient_evals_per_s": substeps / dt, "seconds": dt,
+        "trajectories_per_s": nchains * (nwarmup + ntraj) / dt, "gpu_launches": launches,
+        "accept_mean": float(np.mean(out["accept"])),
+        "posterior_mean_alpha_MH0_sigma": [float(x) for x in pm[na:na + 3]],
+        "truth_alpha_MH0_sigma": [0.5, -1.0, 0.2],
+        "posterior_mean_abs_err": [float(abs(a - b)) for a, b in zip(pm[na:na + 3],
+                                                                      [0.5, -1.0, 0.2])],
+        "note": "wall clock of sample_sfh (setup, graph capture, warmup and sampling); "
+                "one batched gradient per leapfrog step (the start gradient is carried over)",
+    }
+
+
+def run_ragged(ctx, steps=50, warmup=5, check=2):
+    """256 independent galaxies with uneven Hess grids (50-300 bins per axis) and
+    isochrone lengths (100-2,000 points): one ragged template build, then fg! over all
+    galaxies per call (sfh_fg_ragged_dev)."""
+    import numpy as np
+    import torch
+
+    import oracle as O
+    import sfhgpu
+    from sfhgpu import synthetic as S
+    dev = torch.device("cuda", ctx.device)
+    gals = S.ragged()
+    m, mags, offs, lens, dm, edges = S.ragged_isochrones(gals)
+    d_m, d_mags = torch.as_tensor(m, device=dev), torch.as_tensor(mags, device=dev)
+    args = (d_m, d_mags, offs, lens, 1, (0, 1), S.error_models(), S.completeness_models(),
+            S.imf(), dm, 1.0, edges)
+    out, toff = sfhgpu.partial_cmd_smooth_ragged(*args, ctx=ctx)  # warm-up, sizes the output
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sfhgpu.partial_cmd_smooth_ragged(*args, out=out, ctx=ctx)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    nt = np.array([g.ntempl for g in gals])
+    nb = np.array([g.nbins for g in gals])
+    gal = sfhgpu.Galaxies(out, nb, nt, ctx=ctx)
+    # per-galaxy coefficients exp(N(0,1)) scaled to 1e4 stars, Poisson data
+    rng = np.random.default_rng(11)
+    r = np.exp(rng.standard_normal(int(nt.sum())))
+    _, _, comp = sfhgpu.fg_ragged(gal, r, np.zeros(int(nb.sum())), want_logl=False,
+                                  want_grad=False)
+    comp = comp.cpu().numpy()
+    for g in range(len(gals)):
+        b0, b1 = gal.bin_offsets[g], gal.bin_offsets[g + 1]
+        t0_, t1_ = gal.templ_offsets[g], gal.templ_offsets[g + 1]
+        r[t0_:t1_] *= 1e4 / max(comp[b0:b1].sum(), 1e-300)
+    _, _, comp = sfhgpu.fg_ragged(gal, r, np.zeros(int(nb.sum())), want_logl=False,
+                                  want_grad=False)
+    data = rng.poisson(np.maximum(comp.cpu().numpy(), 0)).astype(float)
+    d_r = torch.tensor(r, device=dev)
+    d_n = torch.tensor(data, device=dev)
+    d_c = torch.empty_like(d_n)
+    d_G = torch.empty_like(d_r)
+    d_L = torch.empty(len(gals), dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    L = sfhgpu.load()
+    eps = float(np.finfo(np.float64).eps)
+    call = (ctx.handle, gal.handle, d_r.data_ptr(), d_n.data_ptr(), d_c.data_ptr(),
+            d_G.data_ptr(), d_L.data_ptr(), eps)
+    for _ in range(warmup):
+        sfhgpu._lib.check(L.sfh_fg_ragged_dev(*call), ctx.handle, "fg_ragged")
+    ts = ctx.torch_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ts)
+    for _ in range(steps):
+        sfhgpu._lib.check(L.sfh_fg_ragged_dev(*call), ctx.handle, "fg_ragged")
+    e1.record(ts)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    negL, G = d_L.cpu().numpy(), d_G.cpu().numpy()
+    M = out.cpu().numpy()
+    err_l, err_g = 0.0, 0.0
+    for g in np.argsort(-nb)[:check]:  # the largest galaxies
+        mo = int(sum(nb[:g] * nt[:g]))
+        Mg = M[mo:mo + nb[g] * nt[g]].reshape(nt[g], nb[g]).T.astype(np.float64)
+        b0, b1 = gal.bin_offsets[g], gal.bin_offsets[g + 1]
+        t0_, t1_ = gal.templ_offsets[g], gal.templ_offsets[g + 1]
+        v, Gr, w = O.fg(r[t0_:t1_], np.asfortranarray(Mg), data[b0:b1])
+        err_l = max(err_l, abs(negL[g] - v) / max(1.0, data[b0:b1].sum() / 1e4))
+        err_g = max(err_g, float(np.max(np.abs(G[t0_:t1_] - Gr) /
+                                        (np.abs(Mg).T @ np.abs(w) + 1e-300))))
+    # galaxies with <= 32 templates take the fused pass (M read once); larger ones read
+    # M twice (composite pass, then the gradient pass)
+    reads = np.where(nt <= 32, 1, 2)
+    alg_bytes = (4 * float((reads * nb * nt).sum()) + 16 * float(nb.sum())
+                 + 16 * float(nt.sum()))
+    peak, kind = _peaks()
+    gal.free()
+    return {
+        "workload": f"{len(gals)} galaxies, grids 50-300 bins per axis ({int(nb.sum())} bins), "
+                    f"isochrones 100-2000 points, {int(nt.sum())} templates",
+        "templates_per_s": float(nt.sum()) / build_s, "template_build_s": build_s,
+        "fg_calls_per_s": 1e3 / ms, "galaxy_evals_per_s": len(gals) * 1e3 / ms,
+        "ms_per_call": ms,
+        "roofline": {"bound": "hbm", "achieved": alg_bytes / (ms * 1e-3) / 1e9, "peak": peak,
+                     "unit": "GB/s", "frac": alg_bytes / (ms * 1e-3) / 1e9 / peak,
+                     "peak_source": kind, "algorithmic_bytes_per_call": alg_bytes},
+        "dlogL_per_1e4_stars_vs_oracle": err_l, "grad_err_rel_scale_vs_oracle": err_g,
     }
 
 
@@ -427,6 +558,17 @@ def run_ours(args):
         batched = run_batched(ctx, d_T, NBINS, NTW, r, data, M64, steps=5, warmup=2)
         batched["speedup_vs_plain"] = batched["evals_per_s"] / value
 
+    # ---- ragged galaxies: 256 uneven Hess grids, templates + fg! in one call each
+    ragged = None
+    if not args.no_ragged:
+        ragged = run_ragged(ctx)
+
+    # ---- end-to-end hierarchical HMC (1,024 chains, MZR) on the same templates
+    hmc = None
+    if not args.no_hmc:
+        hmc = run_hmc(ctx, d_T, w)
+        hmc["speedup_vs_plain_evals"] = hmc["chain_gradient_evals_per_s"] / value
+
     # ---- CPU baseline (rank 0, N = 1 only): the oracle on the same inputs
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -450,7 +592,7 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}"},
             "templates_per_s": templates_per_s, "template_build_ms": build_ms,
             "negLogL": neglogl, "gpu_launches": launches, "roofline": roofline,
-            "batched": batched,
+            "batched": batched, "hmc": hmc, "ragged": ragged,
             "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
         }
         print(json.dumps(line), flush=True)
@@ -469,6 +611,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched tensor-core leg")
+    ap.add_argument("--no-hmc", action="store_true", help="skip the batched HMC leg")
+    ap.add_argument("--no-ragged", action="store_true", help="skip the ragged-galaxies leg")
     ap.add_argument("--ntempl", type=int, default=NT,
                     help="templates (multiple of 30); fewer than 1200 only for profiling")
     ap.add_argument("--cpu-budget-s", type=float, default=10.0)

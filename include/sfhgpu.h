@@ -247,6 +247,103 @@ int sfh_partial_cmd_smooth_batch_dev(sfh_ctx *ctx, const double *d_m_ini, const 
                                      int64_t nx, double y_first, double y_step, int64_t ny,
                                      float *d_models);
 
+/* One template's Hess grid in a ragged batch: colour edges x_first + k x_step (k = 0..nx),
+   magnitude edges y_first + k y_step (k = 0..ny); its (nx*ny) column-major histogram is
+   written at d_models + out_offset. */
+typedef struct {
+    double x_first, x_step;
+    int64_t nx;
+    double y_first, y_step;
+    int64_t ny;
+    int64_t out_offset;
+} sfh_hess_grid;
+
+/* Ragged batch of partial_cmd_smooth calls (many galaxies with uneven Hess grids and
+   isochrone lengths, StarFormationHistories.jl:829-888 per template): as
+   sfh_partial_cmd_smooth_batch_dev, but template t is binned on h_grids[t] with its own
+   mini_spacing step min(|x_step|, |y_step|) (:851).  d_models holds models_len floats;
+   every template's histogram must lie inside it.  One launch per pass for the whole batch. */
+int sfh_partial_cmd_smooth_ragged_dev(sfh_ctx *ctx, const double *d_m_ini, const double *d_mags,
+                                      int64_t total_points, const int64_t *h_iso_off,
+                                      const int32_t *h_iso_len, int64_t ntempl, int nf,
+                                      int y_index, int c1, int c2, const sfh_err_model *err,
+                                      const sfh_compl_model *compl_, const double *bias,
+                                      const sfh_imf *imf, double mean_mass, const double *h_dmod,
+                                      const double *h_norm, const sfh_hess_grid *h_grids,
+                                      int64_t models_len, float *d_models);
+
+/* ---------------------------------------------------------------- ragged galaxies (fg!) */
+/* One galaxy of a ragged batch: its (nbins x ntempl) column-major FP32 templates start at
+   d_models + model_offset; its data / composite bins at bin_offset and its coefficients /
+   gradient at templ_offset of the packed arrays. */
+typedef struct {
+    int64_t model_offset;
+    int64_t nbins, ntempl;
+    int64_t bin_offset;
+    int64_t templ_offset;
+} sfh_galaxy;
+typedef struct sfh_galaxies sfh_galaxies;
+
+/* Builds the work lists of a ragged batch once (descriptors are copied; d_models is
+   referenced, not copied, and must outlive the handle).  models_len: floats in d_models. */
+int sfh_galaxies_create(sfh_ctx *ctx, const float *d_models, int64_t models_len,
+                        const sfh_galaxy *h_galaxies, int64_t ngal, sfh_galaxies **out);
+int sfh_galaxies_free(sfh_galaxies *galaxies);
+int sfh_galaxies_info(const sfh_galaxies *galaxies, int64_t *ngal, int64_t *total_bins,
+                      int64_t *total_templ);
+/* fg! (solvers.jl:20-38) for every galaxy of the batch at once, device arrays packed by
+   the descriptors: d_coeffs / d_G by templ_offset, d_data / d_composite by bin_offset,
+   d_negLogL one value per galaxy.  d_G and d_negLogL may be NULL (the reference's
+   `nothing` branches); d_composite receives what fg! leaves there (1 - n/c when G is
+   requested, the model otherwise).  Enqueued on the context stream, no synchronisation. */
+int sfh_fg_ragged_dev(sfh_ctx *ctx, const sfh_galaxies *galaxies, const double *d_coeffs,
+                      const double *d_data, double *d_composite, double *d_G,
+                      double *d_negLogL, double eps);
+
+/* ---------------------------------------------------------------- learned template emulator */
+/* No reference counterpart (new component).  An MLP in -> h1 -> h2 -> out (GELU after the
+   hidden layers, FP32 master weights, BF16-rounded matmul operands with FP32
+   accumulation) maps standardised (log age, [M/H], distance modulus) to scaled
+   coefficients on a PCA basis of variance-stabilised templates; templates are rebuilt
+   from the coefficients, and the exact partial_cmd_smooth template judges them by Poisson
+   deviance per star and replaces any that fail.  All arrays are device FP32 and
+   row-major.  Parameter block: W1 (h1 x in), b1, W2 (h2 x h1), b2, W3 (out x h2), b3. */
+int sfh_mlp_param_count(int in, int h1, int h2, int out, int64_t *n);
+/* d_Y (B x out) = MLP(d_X (B x in)). */
+int sfh_mlp_forward(sfh_ctx *ctx, int in, int h1, int h2, int out, const float *d_params,
+                    const float *d_X, int B, float *d_Y);
+/* Mean-squared-error loss mean((Y - T)^2) over B x out and its gradient d_grad (same layout
+   as the parameters); d_loss (one float) may be NULL. */
+int sfh_mlp_loss_grad(sfh_ctx *ctx, int in, int h1, int h2, int out, const float *d_params,
+                      const float *d_X, const float *d_T, int B, float *d_grad, float *d_loss);
+/* nsteps Adam steps (beta 0.9 / 0.999, eps 1e-8, bias-corrected from step0 + 1) on
+   minibatches of `batch` rows drawn with replacement (Philox keyed by seed and the step)
+   from d_X (nsamples x in) / d_T (nsamples x out).  d_adam_m / d_adam_v hold the moment
+   estimates (parameter layout, zero before the first call).  d_loss_trace (nsteps floats,
+   may be NULL) receives each step's minibatch loss before its update. */
+int sfh_mlp_train(sfh_ctx *ctx, int in, int h1, int h2, int out, float *d_params,
+                  float *d_adam_m, float *d_adam_v, int64_t step0, const float *d_X,
+                  const float *d_T, int64_t nsamples, int batch, int64_t nsteps, float lr,
+                  uint64_t seed, float *d_loss_trace);
+/* d_C (M x N) = alpha op(A) op(B) (+ d_C when accum), FP32 accumulation, ta / tb select
+   row-major A (M x K) / (K x M) and B (K x N) / (N x K); bf16 != 0 rounds the operands to
+   BF16 first.  Used for the PCA basis (randomized range finder) and projections. */
+int sfh_gemm_f32(sfh_ctx *ctx, const float *d_A, const float *d_B, float *d_C, int64_t M,
+                 int64_t N, int64_t K, int ta, int tb, int accum, float alpha, int bf16);
+/* In place on d_Y (rows templates x cols bins): transform (mode 1: sqrt; mode 0: none),
+   column mean into d_mean (cols), then centre the rows on it. */
+int sfh_emu_prepare(sfh_ctx *ctx, float *d_Y, int64_t rows, int64_t cols, int mode,
+                    float *d_mean);
+/* Templates from coefficients: d_out (B x nbins) = inverse transform of
+   (d_offset + d_coef (B x K) d_basis (K x nbins)), clamped at 0 (mode 1 squares). */
+int sfh_emu_reconstruct(sfh_ctx *ctx, const float *d_coef, const float *d_basis,
+                        const float *d_offset, int K, int64_t nbins, int64_t B, int mode,
+                        float *d_out);
+/* Judge: d_dev[t] = 2 sum_i (e - x + x log(x / e)) / sum_i x for exact x = d_exact[t, :],
+   emulated e = d_emul[t, :] (floored at 1e-30), in FP64; B x nbins row-major inputs. */
+int sfh_poisson_deviance(sfh_ctx *ctx, const float *d_exact, const float *d_emul,
+                         int64_t nbins, int B, double *d_dev);
+
 #ifdef __cplusplus
 }
 #endif

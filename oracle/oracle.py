@@ -110,6 +110,13 @@ def lib():
             L.sfho_mzr_fg.argtypes = [_dp, _i64, C.c_double, C.c_int, C.c_int, C.c_int, _dp, _dp,
                                       _i64, _i64, _dp, _dp, C.c_double, C.c_void_p]
             L.sfho_mzr_fg.restype = C.c_double
+            L.sfho_mlp_param_count.argtypes = [C.c_int] * 4
+            L.sfho_mlp_param_count.restype = _i64
+            L.sfho_mlp_forward.argtypes = [C.c_int] * 4 + [_dp, _dp, _i64, C.c_int, _dp]
+            L.sfho_mlp_loss_grad.argtypes = [C.c_int] * 4 + [_dp, _dp, _dp, _i64, C.c_int, _dp]
+            L.sfho_mlp_loss_grad.restype = C.c_double
+            L.sfho_poisson_deviance.argtypes = [_dp, _dp, _i64]
+            L.sfho_poisson_deviance.restype = C.c_double
             L.sfho_set_threads.argtypes = [C.c_int]
             L.sfho_get_max_threads.restype = C.c_int
             _lib = L
@@ -342,3 +349,33 @@ def mzr_fg(variables, logMstar0, M, n, logAge, MH, free=(True, True, True), want
                           int(free[2]), M.ravel(order="F"), _f64(n), nb, nt, _f64(logAge),
                           _f64(MH), eps, G.ctypes.data if want_g else None)
     return v, G
+
+
+# ---------------- learned template emulator (no reference counterpart) ----------------
+
+def mlp_param_count(shape):
+    return int(lib().sfho_mlp_param_count(*shape))
+
+
+def mlp_forward(shape, params, X, bf16=True):
+    """FP64 MLP forward (GELU hidden layers); bf16 rounds every matmul operand."""
+    X = _f64(X)
+    B = X.shape[0]
+    Y = np.empty((B, shape[3]))
+    lib().sfho_mlp_forward(*shape, _f64(params), X.ravel(), B, int(bf16), Y.ravel())
+    return Y
+
+
+def mlp_loss_grad(shape, params, X, T, bf16=True):
+    """(MSE loss, gradient w.r.t. the flat parameter block) in FP64."""
+    X, T = _f64(X), _f64(T)
+    g = np.empty(mlp_param_count(shape))
+    loss = lib().sfho_mlp_loss_grad(*shape, _f64(params), X.ravel(), T.ravel(), X.shape[0],
+                                    int(bf16), g)
+    return loss, g
+
+
+def poisson_deviance(exact, emul):
+    """Poisson deviance per star of emul against exact."""
+    e, t = _f64(emul).ravel(), _f64(exact).ravel()
+    return lib().sfho_poisson_deviance(t, e, t.size)

@@ -649,3 +649,130 @@ double sfho_mzr_fg(const double *variables, int64_t nages, double logMstar0, int
     free(c);
     return -logL;
 }
+
+/* ======================= learned template emulator (no reference counterpart) ====== */
+/* A plain FP64 restatement of the device MLP: the forward pass, the backward pass of
+   the mean-squared-error loss, and the Poisson deviance used as the judge. */
+
+static double bf16_round(double x) {
+    float f = (float)x;
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    if ((u & 0x7F800000u) != 0x7F800000u) {
+        u += 0x7FFFu + ((u >> 16) & 1u);
+        u &= 0xFFFF0000u;
+    }
+    memcpy(&f, &u, 4);
+    return (double)f;
+}
+
+static double gelu64(double z) { return 0.5 * z * (1.0 + erf(z / sqrt(2.0))); }
+static double gelu64_grad(double z) {
+    return 0.5 * (1.0 + erf(z / sqrt(2.0))) + z * exp(-0.5 * z * z) / sqrt(2.0 * M_PI);
+}
+
+int64_t sfho_mlp_param_count(int in, int h1, int h2, int out) {
+    return (int64_t)h1 * in + h1 + (int64_t)h2 * h1 + h2 + (int64_t)out * h2 + out;
+}
+
+/* out (B x n) = rnd(A) (B x k) * rnd(W)^T (n x k) + b */
+static void dense(const double *A, const double *W, const double *b, int64_t B, int k, int n,
+                  int bf16, double *out) {
+    for (int64_t r = 0; r < B; ++r)
+        for (int j = 0; j < n; ++j) {
+            double s = 0.0;
+            for (int i = 0; i < k; ++i) {
+                double a = A[r * k + i], w = W[(int64_t)j * k + i];
+                if (bf16) { a = bf16_round(a); w = bf16_round(w); }
+                s += a * w;
+            }
+            out[r * n + j] = s + b[j];
+        }
+}
+
+void sfho_mlp_forward(int in, int h1, int h2, int out, const double *P, const double *X,
+                      int64_t B, int bf16, double *Y) {
+    const double *W1 = P, *b1 = W1 + (int64_t)h1 * in, *W2 = b1 + h1, *b2 = W2 + (int64_t)h2 * h1,
+                 *W3 = b2 + h2, *b3 = W3 + (int64_t)out * h2;
+    double *A1 = calloc((size_t)(B * h1), sizeof(double)), *A2 = calloc((size_t)(B * h2), sizeof(double));
+    dense(X, W1, b1, B, in, h1, bf16, A1);
+    for (int64_t k = 0; k < B * h1; ++k) A1[k] = gelu64(A1[k]);
+    dense(A1, W2, b2, B, h1, h2, bf16, A2);
+    for (int64_t k = 0; k < B * h2; ++k) A2[k] = gelu64(A2[k]);
+    dense(A2, W3, b3, B, h2, out, bf16, Y);
+    free(A1);
+    free(A2);
+}
+
+/* dW (n x k) = rnd(dZ)^T (n x B) rnd(A) (B x k); db = column sums of dZ;
+   dA (B x k) = rnd(dZ) (B x n) rnd(W) (n x k) when dA != NULL */
+static void dense_back(const double *dZ, const double *A, const double *W, int64_t B, int k, int n,
+                       int bf16, double *dW, double *db, double *dA) {
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < k; ++i) {
+            double s = 0.0;
+            for (int64_t r = 0; r < B; ++r) {
+                double g = dZ[r * n + j], a = A[r * k + i];
+                if (bf16) { g = bf16_round(g); a = bf16_round(a); }
+                s += g * a;
+            }
+            dW[(int64_t)j * k + i] = s;
+        }
+    for (int j = 0; j < n; ++j) {
+        double s = 0.0;
+        for (int64_t r = 0; r < B; ++r) s += dZ[r * n + j];
+        db[j] = s;
+    }
+    if (dA)
+        for (int64_t r = 0; r < B; ++r)
+            for (int i = 0; i < k; ++i) {
+                double s = 0.0;
+                for (int j = 0; j < n; ++j) {
+                    double g = dZ[r * n + j], w = W[(int64_t)j * k + i];
+                    if (bf16) { g = bf16_round(g); w = bf16_round(w); }
+                    s += g * w;
+                }
+                dA[r * k + i] = s;
+            }
+}
+
+double sfho_mlp_loss_grad(int in, int h1, int h2, int out, const double *P, const double *X,
+                          const double *T, int64_t B, int bf16, double *grad) {
+    const double *W1 = P, *b1 = W1 + (int64_t)h1 * in, *W2 = b1 + h1, *b2 = W2 + (int64_t)h2 * h1,
+                 *W3 = b2 + h2, *b3 = W3 + (int64_t)out * h2;
+    double *gW1 = grad, *gb1 = gW1 + (int64_t)h1 * in, *gW2 = gb1 + h1,
+           *gb2 = gW2 + (int64_t)h2 * h1, *gW3 = gb2 + h2, *gb3 = gW3 + (int64_t)out * h2;
+    double *Z1 = malloc(sizeof(double) * B * h1), *A1 = malloc(sizeof(double) * B * h1);
+    double *Z2 = malloc(sizeof(double) * B * h2), *A2 = calloc((size_t)(B * h2), sizeof(double));
+    double *Y = malloc(sizeof(double) * B * out), *dA2 = malloc(sizeof(double) * B * h2);
+    double *dA1 = malloc(sizeof(double) * B * h1);
+    dense(X, W1, b1, B, in, h1, bf16, Z1);
+    for (int64_t k = 0; k < B * h1; ++k) A1[k] = gelu64(Z1[k]);
+    dense(A1, W2, b2, B, h1, h2, bf16, Z2);
+    for (int64_t k = 0; k < B * h2; ++k) A2[k] = gelu64(Z2[k]);
+    dense(A2, W3, b3, B, h2, out, bf16, Y);
+    const double scale = 1.0 / ((double)B * out);
+    double loss = 0.0;
+    for (int64_t k = 0; k < B * out; ++k) {
+        const double d = Y[k] - T[k];
+        loss += d * d * scale;
+        Y[k] = 2.0 * d * scale; /* dY */
+    }
+    dense_back(Y, A2, W3, B, h2, out, bf16, gW3, gb3, dA2);
+    for (int64_t k = 0; k < B * h2; ++k) dA2[k] *= gelu64_grad(Z2[k]);
+    dense_back(dA2, A1, W2, B, h1, h2, bf16, gW2, gb2, dA1);
+    for (int64_t k = 0; k < B * h1; ++k) dA1[k] *= gelu64_grad(Z1[k]);
+    dense_back(dA1, X, W1, B, in, h1, bf16, gW1, gb1, NULL);
+    free(Z1); free(A1); free(Z2); free(A2); free(Y); free(dA2); free(dA1);
+    return loss;
+}
+
+double sfho_poisson_deviance(const double *exact, const double *emul, int64_t n) {
+    double d = 0.0, tot = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+        const double t = exact[i], e = emul[i] > 1e-30 ? emul[i] : 1e-30;
+        d += e - t + (t > 0.0 ? t * log(t / e) : 0.0);
+        tot += t;
+    }
+    return tot > 0.0 ? 2.0 * d / tot : 0.0;
+}

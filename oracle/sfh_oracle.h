@@ -128,6 +128,21 @@ double sfho_mzr_fg(const double *variables, int64_t nages, double logMstar0,
                    const double *n, int64_t nbins, int64_t nt, const double *logAge,
                    const double *MH, double eps, double *G);
 
+/* ---------------- learned template emulator (no reference counterpart) ---------------- */
+/* MLP in -> h1 -> h2 -> out with GELU (erf form) after the two hidden layers.
+   Parameter block (row-major): W1 (h1 x in), b1 (h1), W2 (h2 x h1), b2 (h2),
+   W3 (out x h2), b3 (out).  Z1 = X W1^T + b1, A1 = gelu(Z1), ..., Y = A2 W3^T + b3.
+   bf16 != 0 rounds every matmul operand to BF16 (round to nearest even, through
+   FP32) before the FP64 products, as the device kernels do. */
+int64_t sfho_mlp_param_count(int in, int h1, int h2, int out);
+void sfho_mlp_forward(int in, int h1, int h2, int out, const double *params, const double *X,
+                      int64_t B, int bf16, double *Y);
+/* MSE loss mean((Y - T)^2) over B x out and its gradient w.r.t. params. */
+double sfho_mlp_loss_grad(int in, int h1, int h2, int out, const double *params,
+                          const double *X, const double *T, int64_t B, int bf16, double *grad);
+/* Poisson deviance per star 2 sum(e - t + t log(t/e)) / sum(t), e floored at 1e-30. */
+double sfho_poisson_deviance(const double *exact, const double *emul, int64_t n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,485 @@
+// emulator.cu -- learned template emulator: MLP on a PCA basis of templates.
+//
+// No counterpart in the reference (new component): (log age, [M/H], distance modulus)
+// -> MLP 3 -> 256 -> 256 -> 64 (GELU) -> standardised PCA coefficients -> template
+// = mean + Σ_k c_k v_k.  The exact partial_cmd_smooth template is the judge (Poisson
+// deviance per star) and the fallback.
+//
+// Kernels: tiled GEMMs with BF16-rounded operands and FP32 accumulation (the MLP's
+// "BF16 matmuls" over FP32 master weights), bias + GELU, GELU backward, MSE loss
+// gradient, Adam; reconstruction of templates from coefficients; the judge.  The
+// training loop runs on the device: each step draws its minibatch indices with Philox.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <vector>
+
+#include "sfh_internal.cuh"
+
+namespace {
+
+constexpr int GBM = 64, GBN = 64, GBK = 16, GTHREADS = 256;
+
+__device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+
+// C[M x N] = alpha op(A) op(B) (+ C when accum).  op(A) is M x K: A stored (M x K) row-major
+// (ta = 0) or (K x M) row-major (ta = 1); op(B) is K x N: B stored (K x N) (tb = 0) or
+// (N x K) (tb = 1).  FP32 accumulation; ROUND rounds every operand to BF16 first (the
+// MLP's BF16 matmuls over FP32 master weights).  64 x 64 tiles, 16 x 16 threads with
+// 4 x 4 outputs each; loads run along each operand's contiguous dimension.
+template <bool ROUND>
+__global__ void __launch_bounds__(GTHREADS)
+k_gemm(const float *__restrict__ A, const float *__restrict__ B, float *__restrict__ C, int M, int N,
+       int K, int ta, int tb, int accum, float alpha) {
+    __shared__ float sA[GBK][GBM + 4];
+    __shared__ float sB[GBK][GBN + 4];
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int row0 = blockIdx.y * GBM, col0 = blockIdx.x * GBN;
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+    for (int k0 = 0; k0 < K; k0 += GBK) {
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+            const int l = tid + GTHREADS * p;
+            int kl, ml;
+            float v = 0.f;
+            if (!ta) { kl = l & 15; ml = l >> 4; } else { ml = l & 63; kl = l >> 6; }
+            const int m = row0 + ml, k = k0 + kl;
+            if (m < M && k < K) v = ta ? A[(int64_t)k * M + m] : A[(int64_t)m * K + k];
+            sA[kl][ml] = ROUND ? bf16r(v) : v;
+            int nl;
+            v = 0.f;
+            if (!tb) { nl = l & 63; kl = l >> 6; } else { kl = l & 15; nl = l >> 4; }
+            const int n = col0 + nl, kk = k0 + kl;
+            if (n < N && kk < K) v = tb ? B[(int64_t)n * K + kk] : B[(int64_t)kk * N + n];
+            sB[kl][nl] = ROUND ? bf16r(v) : v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < GBK; ++k) {
+            float a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) a[i] = sA[k][ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) b[j] = sB[k][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int m = row0 + ty + 16 * i;
+        if (m >= M) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int n = col0 + tx + 16 * j;
+            if (n < N) {
+                float *c = C + (int64_t)m * N + n;
+                *c = accum ? fmaf(alpha, acc[i][j], *c) : alpha * acc[i][j];
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ float gelu(float z) {
+    return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f));
+}
+__device__ __forceinline__ float gelu_grad(float z) {
+    return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) +
+           z * 0.3989422804014327f * expf(-0.5f * z * z);
+}
+
+// Z += b (per column); A = GELU(Z) when act.
+__global__ void k_bias_act(float *__restrict__ Z, float *__restrict__ A, const float *__restrict__ b,
+                           int64_t M, int N, int act) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= M * N) return;
+    const float z = Z[k] + b[k % N];
+    Z[k] = z;
+    if (act) A[k] = gelu(z);
+}
+
+// dZ = dA * GELU'(Z)
+__global__ void k_gelu_back(float *__restrict__ dA, const float *__restrict__ Z, int64_t n) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) dA[k] *= gelu_grad(Z[k]);
+}
+
+// column sums of X (M x N): db = Σ_rows
+__global__ void k_colsum(const float *__restrict__ X, int64_t M, int64_t N, float *__restrict__ out,
+                         float scale) {
+    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    float h = 0.f, l = 0.f;
+    for (int64_t m = 0; m < M; ++m) sfh_two_sum_acc(h, l, X[m * N + n]);
+    out[n] = (h + l) * scale;
+}
+
+// MSE: dY = 2 (Y - T) / (M N); per-block partial loss
+__global__ void k_mse(const float *__restrict__ Y, const float *__restrict__ T, int64_t n,
+                      float scale, float *__restrict__ dY, float *__restrict__ loss_part) {
+    __shared__ float s[256];
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    float l = 0.f;
+    if (k < n) {
+        const float d = Y[k] - T[k];
+        dY[k] = 2.0f * d * scale;
+        l = d * d * scale;
+    }
+    s[threadIdx.x] = l;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) loss_part[blockIdx.x] = s[0];
+}
+
+__global__ void k_sum(const float *__restrict__ x, int n, float *__restrict__ out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        float h = 0.f, l = 0.f;
+        for (int i = 0; i < n; ++i) sfh_two_sum_acc(h, l, x[i]);
+        *out = h + l;
+    }
+}
+
+// Adam (Kingma & Ba 2015), bias-corrected, on FP32 master weights.
+__global__ void k_adam(float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m,
+                       float *__restrict__ v, int64_t n, float lr, float b1, float b2, float eps,
+                       float c1, float c2) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float gk = g[k];
+    const float mk = b1 * m[k] + (1.0f - b1) * gk;
+    const float vk = b2 * v[k] + (1.0f - b2) * gk * gk;
+    m[k] = mk;
+    v[k] = vk;
+    w[k] -= lr * (mk / c1) / (sqrtf(vk / c2) + eps);
+}
+
+struct u4 {
+    uint32_t x, y, z, w;
+};
+__device__ __forceinline__ u4 philox(u4 c, uint32_t k0, uint32_t k1) {  // Salmon et al. 2011
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = u4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// Minibatch gather: row i of the batch = sample floor(u * N) for a Philox uniform u.
+__global__ void k_gather(const float *__restrict__ X, const float *__restrict__ T, int64_t N,
+                         int din, int dout, int B, uint64_t seed, int64_t step,
+                         float *__restrict__ Xb, float *__restrict__ Tb) {
+    const int i = blockIdx.x;
+    const u4 r = philox(u4{(uint32_t)i, (uint32_t)step, (uint32_t)(step >> 32), 7u}, (uint32_t)seed,
+                        (uint32_t)(seed >> 32));
+    const int64_t s = (int64_t)(((uint64_t)r.x * (uint64_t)N) >> 32);
+    for (int j = threadIdx.x; j < din; j += blockDim.x) Xb[(int64_t)i * din + j] = X[s * din + j];
+    for (int j = threadIdx.x; j < dout; j += blockDim.x) Tb[(int64_t)i * dout + j] = T[s * dout + j];
+}
+
+// Variance-stabilising transform of templates, in place: y = sqrt(t) (mode 1) or y = t.
+__global__ void k_transform(float *__restrict__ Y, int64_t n, int mode) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n && mode == 1) Y[k] = sqrtf(fmaxf(Y[k], 0.f));
+}
+
+// Y[r, :] -= mean (row-major rows x cols)
+__global__ void k_center(float *__restrict__ Y, int64_t rows, int64_t cols,
+                         const float *__restrict__ mean) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < rows * cols) Y[k] -= mean[k % cols];
+}
+
+// out = inverse transform of (offset + out): max(0, .)^2 for mode 1, max(0, .) for mode 0.
+__global__ void k_finish(float *__restrict__ out, int64_t rows, int64_t cols,
+                         const float *__restrict__ offset, int mode) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= rows * cols) return;
+    const float y = fmaxf(out[k] + offset[k % cols], 0.f);
+    out[k] = mode == 1 ? y * y : y;
+}
+
+// Judge: Poisson deviance per star of emulated e against exact t,
+// 2 Σ_i [e_i - t_i + t_i log(t_i / e_i)] / Σ_i t_i  (e clamped to a tiny floor).
+__global__ void k_deviance(const float *__restrict__ exact, const float *__restrict__ emul,
+                           int64_t nbins, double *__restrict__ dev) {
+    __shared__ double s1[256], s2[256];
+    const int t = blockIdx.x;
+    double d = 0.0, tot = 0.0;
+    for (int64_t i = threadIdx.x; i < nbins; i += blockDim.x) {
+        const double tv = exact[(int64_t)t * nbins + i];
+        const double ev = fmax((double)emul[(int64_t)t * nbins + i], 1e-30);
+        d += ev - tv + (tv > 0.0 ? tv * log(tv / ev) : 0.0);
+        tot += tv;
+    }
+    s1[threadIdx.x] = d;
+    s2[threadIdx.x] = tot;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            s1[threadIdx.x] += s1[threadIdx.x + o];
+            s2[threadIdx.x] += s2[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) dev[t] = s2[0] > 0.0 ? 2.0 * s1[0] / s2[0] : 0.0;
+}
+
+// Parameter block layout (floats): W1 (H1 x IN), b1, W2 (H2 x H1), b2, W3 (OUT x H2), b3.
+struct MlpShape {
+    int in, h1, h2, out;
+    int64_t oW1, ob1, oW2, ob2, oW3, ob3, n;
+};
+MlpShape mlp_shape(int in, int h1, int h2, int out) {
+    MlpShape s{in, h1, h2, out, 0, 0, 0, 0, 0, 0, 0};
+    s.oW1 = 0;
+    s.ob1 = s.oW1 + (int64_t)h1 * in;
+    s.oW2 = s.ob1 + h1;
+    s.ob2 = s.oW2 + (int64_t)h2 * h1;
+    s.oW3 = s.ob2 + h2;
+    s.ob3 = s.oW3 + (int64_t)out * h2;
+    s.n = s.ob3 + out;
+    return s;
+}
+
+struct Acts {  // activations of one batch
+    float *Z1, *A1, *Z2, *A2, *Y;
+};
+
+int gemm(sfh_ctx *ctx, const float *A, const float *B, float *C, int M, int N, int K, int ta,
+         int tb, int accum, bool round = true, float alpha = 1.0f) {
+    if (M < 1 || N < 1 || K < 1) return SFH_OK;
+    dim3 grid((N + GBN - 1) / GBN, (M + GBM - 1) / GBM);
+    if (grid.y > 65535) return sfh_set_error(ctx, SFH_ERR_SHAPE, "GEMM too many row tiles");
+    if (round)
+        k_gemm<true><<<grid, GTHREADS, 0, ctx->stream>>>(A, B, C, M, N, K, ta, tb, accum, alpha);
+    else
+        k_gemm<false><<<grid, GTHREADS, 0, ctx->stream>>>(A, B, C, M, N, K, ta, tb, accum, alpha);
+    SFH_LAUNCHED(ctx);
+    return SFH_OK;
+}
+
+int forward(sfh_ctx *ctx, const MlpShape &S, const float *P, const float *X, int B, Acts &a) {
+    int rc;
+    const int T = 256;
+    // Z1 = X W1ᵀ + b1, A1 = GELU(Z1)
+    if ((rc = gemm(ctx, X, P + S.oW1, a.Z1, B, S.h1, S.in, 0, 1, 0))) return rc;
+    k_bias_act<<<(unsigned)(((int64_t)B * S.h1 + T - 1) / T), T, 0, ctx->stream>>>(a.Z1, a.A1, P + S.ob1, B, S.h1, 1);
+    SFH_LAUNCHED(ctx);
+    if ((rc = gemm(ctx, a.A1, P + S.oW2, a.Z2, B, S.h2, S.h1, 0, 1, 0))) return rc;
+    k_bias_act<<<(unsigned)(((int64_t)B * S.h2 + T - 1) / T), T, 0, ctx->stream>>>(a.Z2, a.A2, P + S.ob2, B, S.h2, 1);
+    SFH_LAUNCHED(ctx);
+    if ((rc = gemm(ctx, a.A2, P + S.oW3, a.Y, B, S.out, S.h2, 0, 1, 0))) return rc;
+    k_bias_act<<<(unsigned)(((int64_t)B * S.out + T - 1) / T), T, 0, ctx->stream>>>(a.Y, nullptr, P + S.ob3, B, S.out, 0);
+    SFH_LAUNCHED(ctx);
+    return SFH_OK;
+}
+
+// Gradient of the MSE loss w.r.t. all parameters into Gr; dY is consumed (overwritten).
+int backward(sfh_ctx *ctx, const MlpShape &S, const float *P, const float *X, int B, Acts &a,
+             float *dY, float *dA2, float *dA1, float *Gr) {
+    int rc;
+    const int T = 256;
+    // layer 3
+    if ((rc = gemm(ctx, dY, a.A2, Gr + S.oW3, S.out, S.h2, B, 1, 0, 0))) return rc;  // dYᵀ A2
+    k_colsum<<<(S.out + T - 1) / T, T, 0, ctx->stream>>>(dY, B, S.out, Gr + S.ob3, 1.0f);
+    SFH_LAUNCHED(ctx);
+    if ((rc = gemm(ctx, dY, P + S.oW3, dA2, B, S.h2, S.out, 0, 0, 0))) return rc;  // dY W3
+    k_gelu_back<<<(unsigned)(((int64_t)B * S.h2 + T - 1) / T), T, 0, ctx->stream>>>(dA2, a.Z2, (int64_t)B * S.h2);
+    SFH_LAUNCHED(ctx);
+    // layer 2
+    if ((rc = gemm(ctx, dA2, a.A1, Gr + S.oW2, S.h2, S.h1, B, 1, 0, 0))) return rc;
+    k_colsum<<<(S.h2 + T - 1) / T, T, 0, ctx->stream>>>(dA2, B, S.h2, Gr + S.ob2, 1.0f);
+    SFH_LAUNCHED(ctx);
+    if ((rc = gemm(ctx, dA2, P + S.oW2, dA1, B, S.h1, S.h2, 0, 0, 0))) return rc;
+    k_gelu_back<<<(unsigned)(((int64_t)B * S.h1 + T - 1) / T), T, 0, ctx->stream>>>(dA1, a.Z1, (int64_t)B * S.h1);
+    SFH_LAUNCHED(ctx);
+    // layer 1
+    if ((rc = gemm(ctx, dA1, X, Gr + S.oW1, S.h1, S.in, B, 1, 0, 0))) return rc;
+    k_colsum<<<(S.h1 + T - 1) / T, T, 0, ctx->stream>>>(dA1, B, S.h1, Gr + S.ob1, 1.0f);
+    SFH_LAUNCHED(ctx);
+    return SFH_OK;
+}
+
+struct Work {
+    Acts a{};
+    float *dY = nullptr, *dA2 = nullptr, *dA1 = nullptr, *lp = nullptr;
+    float *Xb = nullptr, *Tb = nullptr, *Gr = nullptr;  // training only
+};
+
+// Carves the MLP buffers out of the context scratch: no allocation once the scratch
+// is large enough, so repeated inference and training calls cost only their kernels.
+int make_work(sfh_ctx *ctx, Work &w, const MlpShape &S, int B, bool train) {
+    const size_t b = (size_t)B;
+    struct Item {
+        float **p;
+        size_t n;
+    } items[] = {{&w.a.Z1, b * S.h1}, {&w.a.A1, b * S.h1}, {&w.a.Z2, b * S.h2},
+                 {&w.a.A2, b * S.h2}, {&w.a.Y, b * S.out}, {&w.dY, b * S.out},
+                 {&w.dA2, b * S.h2}, {&w.dA1, b * S.h1}, {&w.lp, (b * S.out + 255) / 256 + 1},
+                 {&w.Xb, train ? b * S.in : 0}, {&w.Tb, train ? b * S.out : 0},
+                 {&w.Gr, train ? (size_t)S.n : 0}};
+    size_t total = 0;
+    for (const Item &it : items) total += sfh_align256((it.n ? it.n : 1) * sizeof(float));
+    int rc = sfh_scratch_reserve(ctx, total);
+    if (rc) return rc;
+    char *base = (char *)ctx->scratch;
+    size_t off = 0;
+    for (const Item &it : items) {
+        *it.p = it.n ? (float *)(base + off) : nullptr;
+        off += sfh_align256((it.n ? it.n : 1) * sizeof(float));
+    }
+    return SFH_OK;
+}
+
+int loss_grad(sfh_ctx *ctx, const MlpShape &S, const float *P, const float *X, const float *Tg,
+              int B, Work &w, float *Gr, float *d_loss) {
+    int rc = forward(ctx, S, P, X, B, w.a);
+    if (rc) return rc;
+    const int64_t n = (int64_t)B * S.out;
+    const int nb = (int)((n + 255) / 256);
+    k_mse<<<nb, 256, 0, ctx->stream>>>(w.a.Y, Tg, n, 1.0f / (float)n, w.dY, w.lp);
+    SFH_LAUNCHED(ctx);
+    if (d_loss) {
+        k_sum<<<1, 32, 0, ctx->stream>>>(w.lp, nb, d_loss);
+        SFH_LAUNCHED(ctx);
+    }
+    return backward(ctx, S, P, X, B, w.a, w.dY, w.dA2, w.dA1, Gr);
+}
+
+}  // namespace
+
+extern "C" int sfh_mlp_param_count(int in, int h1, int h2, int out, int64_t *n) {
+    if (!n || in < 1 || h1 < 1 || h2 < 1 || out < 1) return SFH_ERR_ARG;
+    *n = mlp_shape(in, h1, h2, out).n;
+    return SFH_OK;
+}
+
+extern "C" int sfh_mlp_forward(sfh_ctx *ctx, int in, int h1, int h2, int out, const float *d_params,
+                               const float *d_X, int B, float *d_Y) {
+    if (!ctx || !d_params || !d_X || !d_Y || B < 1 || in < 1 || h1 < 1 || h2 < 1 || out < 1)
+        return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    const MlpShape S = mlp_shape(in, h1, h2, out);
+    Work w;
+    int rc = make_work(ctx, w, S, B, false);
+    if (rc) return rc;
+    rc = forward(ctx, S, d_params, d_X, B, w.a);
+    if (rc) return rc;
+    SFH_CK(ctx, cudaMemcpyAsync(d_Y, w.a.Y, (size_t)B * out * sizeof(float), cudaMemcpyDeviceToDevice,
+                                ctx->stream));
+    SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return SFH_OK;
+}
+
+extern "C" int sfh_mlp_loss_grad(sfh_ctx *ctx, int in, int h1, int h2, int out,
+                                 const float *d_params, const float *d_X, const float *d_T, int B,
+                                 float *d_grad, float *d_loss) {
+    if (!ctx || !d_params || !d_X || !d_T || !d_grad || B < 1 || in < 1 || h1 < 1 || h2 < 1 ||
+        out < 1)
+        return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    const MlpShape S = mlp_shape(in, h1, h2, out);
+    Work w;
+    int rc = make_work(ctx, w, S, B, false);
+    if (rc) return rc;
+    rc = loss_grad(ctx, S, d_params, d_X, d_T, B, w, d_grad, d_loss);
+    if (rc) return rc;
+    SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return SFH_OK;
+}
+
+extern "C" int sfh_mlp_train(sfh_ctx *ctx, int in, int h1, int h2, int out, float *d_params,
+                             float *d_adam_m, float *d_adam_v, int64_t step0, const float *d_X,
+                             const float *d_T, int64_t nsamples, int batch, int64_t nsteps,
+                             float lr, uint64_t seed, float *d_loss_trace) {
+    if (!ctx || !d_params || !d_adam_m || !d_adam_v || !d_X || !d_T || nsamples < 1 || batch < 1 ||
+        nsteps < 0 || !(lr > 0) || in < 1 || h1 < 1 || h2 < 1 || out < 1)
+        return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    const MlpShape S = mlp_shape(in, h1, h2, out);
+    Work w;
+    int rc0 = make_work(ctx, w, S, batch, true);
+    if (rc0) return rc0;
+    float *Xb = w.Xb, *Tb = w.Tb, *Gr = w.Gr;
+    cudaStream_t st = ctx->stream;
+    const float b1 = 0.9f, b2 = 0.999f;
+    for (int64_t it = 0; it < nsteps; ++it) {
+        const int64_t step = step0 + it + 1;
+        k_gather<<<batch, 64, 0, st>>>(d_X, d_T, nsamples, in, out, batch, seed, step, Xb, Tb);
+        SFH_LAUNCHED(ctx);
+        int rc = loss_grad(ctx, S, d_params, Xb, Tb, batch, w, Gr,
+                           d_loss_trace ? d_loss_trace + it : nullptr);
+        if (rc) return rc;
+        const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
+        k_adam<<<(unsigned)((S.n + 255) / 256), 256, 0, st>>>(d_params, Gr, d_adam_m, d_adam_v, S.n,
+                                                             lr, b1, b2, 1e-8f, c1, c2);
+        SFH_LAUNCHED(ctx);
+    }
+    SFH_CK(ctx, cudaStreamSynchronize(st));
+    return SFH_OK;
+}
+
+extern "C" int sfh_gemm_f32(sfh_ctx *ctx, const float *d_A, const float *d_B, float *d_C, int64_t M,
+                            int64_t N, int64_t K, int ta, int tb, int accum, float alpha, int bf16) {
+    if (!ctx || !d_A || !d_B || !d_C || M < 1 || N < 1 || K < 1 || M > INT32_MAX ||
+        N > INT32_MAX || K > INT32_MAX)
+        return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    return gemm(ctx, d_A, d_B, d_C, (int)M, (int)N, (int)K, ta, tb, accum, bf16 != 0, alpha);
+}
+
+extern "C" int sfh_emu_prepare(sfh_ctx *ctx, float *d_Y, int64_t rows, int64_t cols, int mode,
+                               float *d_mean) {
+    if (!ctx || !d_Y || !d_mean || rows < 1 || cols < 1 || (mode != 0 && mode != 1))
+        return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    const int64_t n = rows * cols;
+    const unsigned nb = (unsigned)((n + 255) / 256);
+    k_transform<<<nb, 256, 0, ctx->stream>>>(d_Y, n, mode);
+    SFH_LAUNCHED(ctx);
+    k_colsum<<<(unsigned)((cols + 255) / 256), 256, 0, ctx->stream>>>(d_Y, rows, cols, d_mean,
+                                                                     1.0f / (float)rows);
+    SFH_LAUNCHED(ctx);
+    k_center<<<nb, 256, 0, ctx->stream>>>(d_Y, rows, cols, d_mean);
+    SFH_LAUNCHED(ctx);
+    return SFH_OK;
+}
+
+extern "C" int sfh_emu_reconstruct(sfh_ctx *ctx, const float *d_coef, const float *d_basis,
+                                   const float *d_offset, int K, int64_t nbins, int64_t B,
+                                   int mode, float *d_out) {
+    if (!ctx || !d_coef || !d_basis || !d_offset || !d_out || K < 1 || nbins < 1 || B < 1 ||
+        nbins > INT32_MAX || B > INT32_MAX || (mode != 0 && mode != 1))
+        return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    int rc = gemm(ctx, d_coef, d_basis, d_out, (int)B, (int)nbins, K, 0, 0, 0, false);
+    if (rc) return rc;
+    k_finish<<<(unsigned)((B * nbins + 255) / 256), 256, 0, ctx->stream>>>(d_out, B, nbins, d_offset,
+                                                                           mode);
+    SFH_LAUNCHED(ctx);
+    return SFH_OK;
+}
+
+extern "C" int sfh_poisson_deviance(sfh_ctx *ctx, const float *d_exact, const float *d_emul,
+                                    int64_t nbins, int B, double *d_dev) {
+    if (!ctx || !d_exact || !d_emul || !d_dev || nbins < 1 || B < 1) return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    k_deviance<<<B, 256, 0, ctx->stream>>>(d_exact, d_emul, nbins, d_dev);
+    SFH_LAUNCHED(ctx);
+    return SFH_OK;
+}

@@ -45,39 +45,6 @@ __device__ __forceinline__ float4 ld_stream4(const float *p) {
     return v;
 }
 
-// Poisson term of an occupied bin, n - c - n log(n/c) (fitting_base.jl:93), in the form
-//   n (log1p(d) - d),  d = (c - n)/n,  z = (c - n)/(c + n),
-//   log1p(d) - d = -d z + 2 z^3 (1/3 + z^2/5 + z^4/7 + ...)   (log1p(d) = 2 atanh z)
-// so the term is  L + C  with  L = -(c - n)^2/(c + n)  formed in FP64 from a
-// double-float quotient (a handful of FP64 operations) and the small remainder
-// C = 2 n z^3 S(z^2) in FP32.  Bins far from their model (|d| > 1/2) take one FP64
-// log instead.  FP64 throughput on this part is a small fraction of FP32, so the
-// series path keeps FP64 work per bin to five operations.
-__device__ __forceinline__ double poisson_term_occupied(double c, double n) {
-    const double diff = c - n;
-    const float df = (float)diff, nf = (float)n;
-    const float d = __fdiv_rn(df, nf);
-    if (fabsf(d) <= 0.5f) {
-        const double sum = c + n;
-        const float sf = (float)sum;
-        const float q0 = __fdiv_rn(df, sf);
-        const double r = fma(-(double)q0, sum, diff);
-        const float q1 = __fdiv_rn((float)r, sf);
-        const double L = -diff * ((double)q0 + (double)q1);
-        const float z = q0 + q1, z2 = z * z;
-        float S = 1.0f / 17.0f;
-        S = fmaf(S, z2, 1.0f / 15.0f);
-        S = fmaf(S, z2, 1.0f / 13.0f);
-        S = fmaf(S, z2, 1.0f / 11.0f);
-        S = fmaf(S, z2, 1.0f / 9.0f);
-        S = fmaf(S, z2, 1.0f / 7.0f);
-        S = fmaf(S, z2, 1.0f / 5.0f);
-        S = fmaf(S, z2, 1.0f / 3.0f);
-        return L + (double)(2.0f * nf * z * z2 * S);
-    }
-    return n * log(c / n) - diff;
-}
-
 // ---------------------------------------------------------------- k_gemv_n (FP32 storage)
 template <bool VEC>
 __global__ void __launch_bounds__(kThreads)
@@ -532,7 +499,7 @@ __global__ void __launch_bounds__(kThreads) k_fg_pass1_f32(Pass1Args a) {
         }
         const double ci = m > a.eps ? m : a.eps;
         const double ni = a.data[ii];
-        if (a.want_logl) term += (ni > 0.0) ? poisson_term_occupied(ci, ni) : -ci;
+        if (a.want_logl) term += (ni > 0.0) ? sfh_poisson_term_occupied(ci, ni) : -ci;
         if (a.want_w) {
             const float w = __fdiv_rn((float)(ci - ni), (float)ci);  // 1 - n/c
             a.composite[ii] = (double)w;

@@ -19,6 +19,7 @@
 // (:417-436), emitting one star record per midpoint.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -251,6 +252,52 @@ k_stamps(const double *__restrict__ xs, const double *__restrict__ ys,
     for (int k = threadIdx.x; k < bandn; k += blockDim.x) dst[k] = band[k];
 }
 
+// One band of one template per CTA from a flattened tile list: templates with their own
+// Hess grids (ragged galaxies).  Same star loop and band flush as k_stamps.
+struct StampTile {
+    int32_t t, ty0, ty;  // template, first row, band height of this template
+};
+
+__global__ void __launch_bounds__(kStampThreads)
+k_stamps_ragged(const double *__restrict__ xs, const double *__restrict__ ys,
+                const double *__restrict__ sxs, const double *__restrict__ sys,
+                const double *__restrict__ ws, const int64_t *__restrict__ start,
+                const int32_t *__restrict__ count, const int32_t *__restrict__ covs,
+                const StampTile *__restrict__ tiles, const Grid2 *__restrict__ grids,
+                const int64_t *__restrict__ out_off, float *__restrict__ out) {
+    extern __shared__ float smem[];
+    const StampTile tile = tiles[blockIdx.x];
+    const int t = tile.t;
+    const Grid2 g = grids[t];
+    const int TY = tile.ty, ty0 = tile.ty0;
+    const int tyn = min(TY, g.ny - ty0);
+    float *band = smem;
+    const int bandn = tyn * g.nx;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float *wb = smem + (size_t)TY * g.nx + (size_t)warp * (g.nx + 6 * TY);
+    __shared__ int s_next;
+    for (int k = threadIdx.x; k < bandn; k += blockDim.x) band[k] = 0.f;
+    if (threadIdx.x == 0) s_next = 0;
+    __syncthreads();
+    const int64_t s0 = start[t];
+    const int n = count[t];
+    const int cov = covs[t];
+    for (;;) {
+        int q = 0;
+        if (lane == 0) q = atomicAdd(&s_next, 1);
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (q >= n) break;
+        const int64_t s = s0 + q;
+        if (cov == 0)
+            star_asym(band, wb, wb + g.nx, g, ty0, tyn, xs[s], ys[s], sxs[s], sys[s], ws[s], lane);
+        else
+            star_cov(band, wb, g, ty0, tyn, xs[s], ys[s], sxs[s], sys[s], ws[s], (float)cov, lane);
+    }
+    __syncthreads();
+    float *dst = out + out_off[t] + (int64_t)ty0 * g.nx;
+    for (int k = threadIdx.x; k < bandn; k += blockDim.x) dst[k] = band[k];
+}
+
 __global__ void k_offsets_to_counts(const int64_t *__restrict__ off, int64_t n,
                                     int32_t *__restrict__ cnt) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -355,8 +402,8 @@ __device__ IsoPoint iso_point(const IsoParams &P, const double *m, const double 
 // Segment insertion counts (:128-137) and their exclusive scan, in shared memory.
 // Returns N = 1 + sum(cnt) (number of resampled points); sets *bad when masses
 // are not strictly increasing.
-__device__ int iso_scan(const IsoParams &P, const double *m, const double *mg, int n, int *s_cnt,
-                        int *s_pos, int *s_warp, int *bad) {
+__device__ int iso_scan(const IsoParams &P, double dmag, const double *m, const double *mg, int n,
+                        int *s_cnt, int *s_pos, int *s_warp, int *bad) {
     const int nseg = n - 1;
     for (int k = threadIdx.x; k < nseg; k += blockDim.x) {
         const double *vc1 = mg + (int64_t)P.c1 * P.total, *vc2 = mg + (int64_t)P.c2 * P.total;
@@ -365,8 +412,8 @@ __device__ int iso_scan(const IsoParams &P, const double *m, const double *mg, i
         const double dy = vy[k + 1] - vy[k];
         const double d = hypot(dc, dy);
         int c = 1;
-        if (d > P.dmag) {
-            const double r = ceil(d / P.dmag);
+        if (d > dmag) {
+            const double r = ceil(d / dmag);
             c = r < 1.0e7 ? (int)r : 10000000;
         }
         if (!(m[k + 1] > m[k])) atomicExch(bad, 2);
@@ -401,14 +448,16 @@ __device__ int iso_scan(const IsoParams &P, const double *m, const double *mg, i
 __global__ void __launch_bounds__(kIsoThreads)
 k_iso_count(const double *__restrict__ m_ini, const double *__restrict__ mags,
             const int64_t *__restrict__ iso_off, const int32_t *__restrict__ iso_len, IsoParams P,
-            int64_t *__restrict__ nstars_out, int *__restrict__ err_flag) {
+            const double *__restrict__ dmag_t, int64_t *__restrict__ nstars_out,
+            int *__restrict__ err_flag) {
     __shared__ int s_cnt[kIsoMaxPts];
     __shared__ int s_pos[kIsoMaxPts];
     __shared__ int s_warp[kIsoThreads / 32];
     const int t = blockIdx.x;
     const int n = iso_len[t];
-    const int npts = iso_scan(P, m_ini + iso_off[t], mags + iso_off[t], n, s_cnt, s_pos, s_warp,
-                              err_flag);
+    const double dmag = dmag_t ? dmag_t[t] : P.dmag;
+    const int npts = iso_scan(P, dmag, m_ini + iso_off[t], mags + iso_off[t], n, s_cnt, s_pos,
+                              s_warp, err_flag);
     if (threadIdx.x == 0) nstars_out[t] = npts - 1;
 }
 
@@ -416,7 +465,8 @@ __global__ void __launch_bounds__(kIsoThreads)
 k_iso_stars(const double *__restrict__ m_ini, const double *__restrict__ mags,
             const int64_t *__restrict__ iso_off, const int32_t *__restrict__ iso_len,
             const double *__restrict__ dmods, const double *__restrict__ norms, IsoParams P,
-            const int64_t *__restrict__ star_off, double *__restrict__ sx_,
+            const double *__restrict__ dmag_t, const int64_t *__restrict__ star_off,
+            double *__restrict__ sx_,
             double *__restrict__ sy_, double *__restrict__ ssx, double *__restrict__ ssy,
             double *__restrict__ sw, int32_t *__restrict__ count, int *__restrict__ err_flag) {
     __shared__ int s_cnt[kIsoMaxPts];
@@ -426,7 +476,8 @@ k_iso_stars(const double *__restrict__ m_ini, const double *__restrict__ mags,
     const int n = iso_len[t];
     const double *m = m_ini + iso_off[t];
     const double *mg = mags + iso_off[t];
-    const int npts = iso_scan(P, m, mg, n, s_cnt, s_pos, s_warp, err_flag);
+    const int npts = iso_scan(P, dmag_t ? dmag_t[t] : P.dmag, m, mg, n, s_cnt, s_pos, s_warp,
+                              err_flag);
     const int nstars = npts - 1;
     if (nstars != (int)(star_off[t + 1] - star_off[t])) {  // counts come from k_iso_count
         if (threadIdx.x == 0) { count[t] = 0; atomicExch(err_flag, 1); }
@@ -555,29 +606,24 @@ extern "C" int sfh_bin_cmd_smooth(sfh_ctx *ctx, const double *x, const double *y
     return SFH_OK;
 }
 
-extern "C" int sfh_partial_cmd_smooth_batch_dev(
-    sfh_ctx *ctx, const double *d_m_ini, const double *d_mags, int64_t total,
-    const int64_t *h_iso_off, const int32_t *h_iso_len, int64_t ntempl, int nf, int y_index,
-    int c1, int c2, const sfh_err_model *err, const sfh_compl_model *compl_, const double *bias,
-    const sfh_imf *imf, double mean_mass, const double *h_dmod, const double *h_norm, double xf,
-    double xs, int64_t nx, double yf, double ys, int64_t ny, float *d_models) {
-    if (!ctx || !d_m_ini || !d_mags || !h_iso_off || !h_iso_len || !err || !compl_ || !imf ||
-        !h_dmod || !h_norm || !d_models || ntempl < 1 || ntempl > 65535)
-        return SFH_ERR_ARG;
+namespace {
+// Validates the filter indices, IMF and callables of partial_cmd_smooth and fills the
+// device-side parameter block (everything but the grid-dependent Δmag).
+int make_iso_params(sfh_ctx *ctx, int nf, int y_index, int c1, int c2, const sfh_err_model *err,
+                    const sfh_compl_model *compl_, const double *bias, const sfh_imf *imf,
+                    double mean_mass, int64_t total, IsoParams &P) {
     if (nf < 2 || nf > 8 || y_index < 0 || y_index >= nf || c1 < 0 || c1 >= nf || c2 < 0 ||
         c2 >= nf || c1 == c2)
         return sfh_set_error(ctx, SFH_ERR_ARG, "invalid filter indices");
     if (imf->nseg < 1 || imf->nseg > 4 || !(imf->mmin > 0) || !(imf->mmax > imf->mmin) ||
         !(mean_mass > 0))
         return sfh_set_error(ctx, SFH_ERR_ARG, "invalid IMF");
-    SFH_CK(ctx, cudaSetDevice(ctx->device));
-    IsoParams P{};
+    P = IsoParams{};
     P.nf = nf;
     P.y_index = y_index;
     P.c1 = c1;
     P.c2 = c2;
     P.covariant = (y_index == c1 || y_index == c2) ? 1 : 0;
-    P.dmag = std::fmin(std::fabs(xs), std::fabs(ys));  // :851
     P.total = total;
     for (int f = 0; f < nf; ++f) {
         if (!(err[f].a > 0) || !(compl_[f].rho != 0))
@@ -607,6 +653,12 @@ extern "C" int sfh_partial_cmd_smooth_batch_dev(
     }
     P.imf_inv_norm = 1.0 / norm;
     P.inv_mean_mass = 1.0 / mean_mass;
+    return SFH_OK;
+}
+
+// Isochrone lengths and offsets inside the concatenated point arrays.
+int check_isochrones(sfh_ctx *ctx, const int64_t *h_iso_off, const int32_t *h_iso_len,
+                     int64_t ntempl, int64_t total) {
     for (int64_t t = 0; t < ntempl; ++t) {
         const int32_t n = h_iso_len[t];
         if (n < 2 || n > kIsoMaxPts)
@@ -614,21 +666,49 @@ extern "C" int sfh_partial_cmd_smooth_batch_dev(
         if (h_iso_off[t] < 0 || h_iso_off[t] + n > total)
             return sfh_set_error(ctx, SFH_ERR_ARG, "isochrone offsets out of range");
     }
+    return SFH_OK;
+}
+}  // namespace
+
+namespace {
+// Host-side description of per-template Hess grids (ragged galaxies).
+struct RaggedSpec {
+    std::vector<Grid2> grids;
+    std::vector<int64_t> out_off;
+    std::vector<double> dmag;
+    std::vector<StampTile> tiles;
+    size_t smem = 0;
+};
+
+// The two device passes of partial_cmd_smooth for a batch of isochrones (resampled star
+// counts, then star records), followed by the stamps on one shared grid (rg == nullptr)
+// or on each template's own grid.
+int partial_run(sfh_ctx *ctx, const double *d_m_ini, const double *d_mags,
+                const int64_t *h_iso_off, const int32_t *h_iso_len, int64_t ntempl,
+                const IsoParams &P, int y_index, int c1, const double *h_dmod,
+                const double *h_norm, const RaggedSpec *rg, double xf, double xs, int64_t nx,
+                double yf, double ys, int64_t ny, float *d_models) {
     cudaStream_t st = ctx->stream;
     // Pass 1: resampled star count per template (one read-back), exact offsets.
     const size_t o_off = 0, o_len = sfh_align256(ntempl * 8), o_dm = o_len + sfh_align256(ntempl * 4);
     const size_t o_nm = o_dm + sfh_align256(ntempl * 8), o_err = o_nm + sfh_align256(ntempl * 8);
     const size_t o_cnt64 = o_err + 256, o_soff = o_cnt64 + sfh_align256(ntempl * 8);
     const size_t o_cnt = o_soff + sfh_align256((ntempl + 1) * 8), o_cov = o_cnt + sfh_align256(ntempl * 4);
-    const size_t o_stars = o_cov + sfh_align256(ntempl * 4);
+    const size_t o_dmag = o_cov + sfh_align256(ntempl * 4);
+    const size_t o_stars = o_dmag + sfh_align256(ntempl * 8);
+    const double *d_dmag = nullptr;  // per-template Δmag (ragged grids), set once uploaded
     int rc = sfh_scratch_reserve(ctx, o_stars);
     if (rc) return rc;
     char *b = (char *)ctx->scratch;
     SFH_CK(ctx, cudaMemcpyAsync(b + o_off, h_iso_off, ntempl * 8, cudaMemcpyHostToDevice, st));
     SFH_CK(ctx, cudaMemcpyAsync(b + o_len, h_iso_len, ntempl * 4, cudaMemcpyHostToDevice, st));
     SFH_CK(ctx, cudaMemsetAsync(b + o_err, 0, 4, st));
+    if (rg) {
+        SFH_CK(ctx, cudaMemcpyAsync(b + o_dmag, rg->dmag.data(), ntempl * 8, cudaMemcpyHostToDevice, st));
+        d_dmag = (const double *)(b + o_dmag);
+    }
     k_iso_count<<<(unsigned)ntempl, kIsoThreads, 0, st>>>(
-        d_m_ini, d_mags, (const int64_t *)(b + o_off), (const int32_t *)(b + o_len), P,
+        d_m_ini, d_mags, (const int64_t *)(b + o_off), (const int32_t *)(b + o_len), P, d_dmag,
         (int64_t *)(b + o_cnt64), (int *)(b + o_err));
     SFH_LAUNCHED(ctx);
     std::vector<int64_t> nst((size_t)ntempl);
@@ -642,7 +722,11 @@ extern "C" int sfh_partial_cmd_smooth_batch_dev(
     const int64_t nstar_total = soff[(size_t)ntempl] > 0 ? soff[(size_t)ntempl] : 1;
     // Pass 2: star records, then the stamps.
     const size_t a8 = sfh_align256((size_t)nstar_total * 8);
-    rc = sfh_scratch_reserve(ctx, o_stars + 5 * a8);
+    const size_t o_grid = o_stars + 5 * a8;
+    const size_t o_oof = o_grid + (rg ? sfh_align256(ntempl * sizeof(Grid2)) : 0);
+    const size_t o_tiles = o_oof + (rg ? sfh_align256(ntempl * 8) : 0);
+    const size_t o_end = o_tiles + (rg ? sfh_align256(rg->tiles.size() * sizeof(StampTile)) : 0);
+    rc = sfh_scratch_reserve(ctx, o_end);
     if (rc) return rc;
     b = (char *)ctx->scratch;  // may have moved
     std::vector<int32_t> cov((size_t)ntempl, P.covariant ? (y_index == c1 ? -1 : 1) : 0);
@@ -653,20 +737,107 @@ extern "C" int sfh_partial_cmd_smooth_batch_dev(
     SFH_CK(ctx, cudaMemcpyAsync(b + o_soff, soff.data(), (ntempl + 1) * 8, cudaMemcpyHostToDevice, st));
     SFH_CK(ctx, cudaMemcpyAsync(b + o_cov, cov.data(), ntempl * 4, cudaMemcpyHostToDevice, st));
     SFH_CK(ctx, cudaMemsetAsync(b + o_err, 0, 4, st));
+    if (rg) {
+        SFH_CK(ctx, cudaMemcpyAsync(b + o_dmag, rg->dmag.data(), ntempl * 8, cudaMemcpyHostToDevice, st));
+        d_dmag = (const double *)(b + o_dmag);
+        SFH_CK(ctx, cudaMemcpyAsync(b + o_grid, rg->grids.data(), ntempl * sizeof(Grid2),
+                                    cudaMemcpyHostToDevice, st));
+        SFH_CK(ctx, cudaMemcpyAsync(b + o_oof, rg->out_off.data(), ntempl * 8, cudaMemcpyHostToDevice, st));
+        SFH_CK(ctx, cudaMemcpyAsync(b + o_tiles, rg->tiles.data(), rg->tiles.size() * sizeof(StampTile),
+                                    cudaMemcpyHostToDevice, st));
+    }
     double *sxp = (double *)(b + o_stars), *syp = (double *)(b + o_stars + a8);
     double *ssxp = (double *)(b + o_stars + 2 * a8), *ssyp = (double *)(b + o_stars + 3 * a8);
     double *swp = (double *)(b + o_stars + 4 * a8);
     k_iso_stars<<<(unsigned)ntempl, kIsoThreads, 0, st>>>(
         d_m_ini, d_mags, (const int64_t *)(b + o_off), (const int32_t *)(b + o_len),
-        (const double *)(b + o_dm), (const double *)(b + o_nm), P, (const int64_t *)(b + o_soff),
-        sxp, syp, ssxp, ssyp, swp, (int32_t *)(b + o_cnt), (int *)(b + o_err));
+        (const double *)(b + o_dm), (const double *)(b + o_nm), P, d_dmag,
+        (const int64_t *)(b + o_soff), sxp, syp, ssxp, ssyp, swp, (int32_t *)(b + o_cnt),
+        (int *)(b + o_err));
     SFH_LAUNCHED(ctx);
-    rc = sfh_launch_stamps(ctx, sxp, syp, ssxp, ssyp, swp, (const int64_t *)(b + o_soff),
-                           (const int32_t *)(b + o_cnt), (const int32_t *)(b + o_cov), ntempl, xf,
-                           xs, nx, yf, ys, ny, d_models);
-    if (rc) return rc;
+    if (rg) {
+        static thread_local bool attr_set = false;
+        if (!attr_set) {
+            SFH_CK(ctx, cudaFuncSetAttribute(k_stamps_ragged,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+            attr_set = true;
+        }
+        k_stamps_ragged<<<(unsigned)rg->tiles.size(), kStampThreads, rg->smem, st>>>(
+            sxp, syp, ssxp, ssyp, swp, (const int64_t *)(b + o_soff), (const int32_t *)(b + o_cnt),
+            (const int32_t *)(b + o_cov), (const StampTile *)(b + o_tiles),
+            (const Grid2 *)(b + o_grid), (const int64_t *)(b + o_oof), d_models);
+        SFH_LAUNCHED(ctx);
+    } else {
+        rc = sfh_launch_stamps(ctx, sxp, syp, ssxp, ssyp, swp, (const int64_t *)(b + o_soff),
+                               (const int32_t *)(b + o_cnt), (const int32_t *)(b + o_cov), ntempl,
+                               xf, xs, nx, yf, ys, ny, d_models);
+        if (rc) return rc;
+    }
     SFH_CK(ctx, cudaMemcpyAsync(&flag, b + o_err, 4, cudaMemcpyDeviceToHost, st));
     SFH_CK(ctx, cudaStreamSynchronize(st));
     if (flag) return sfh_set_error(ctx, SFH_ERR_CUDA, "resampled star count changed between passes");
     return SFH_OK;
+}
+}  // namespace
+
+extern "C" int sfh_partial_cmd_smooth_batch_dev(
+    sfh_ctx *ctx, const double *d_m_ini, const double *d_mags, int64_t total,
+    const int64_t *h_iso_off, const int32_t *h_iso_len, int64_t ntempl, int nf, int y_index,
+    int c1, int c2, const sfh_err_model *err, const sfh_compl_model *compl_, const double *bias,
+    const sfh_imf *imf, double mean_mass, const double *h_dmod, const double *h_norm, double xf,
+    double xs, int64_t nx, double yf, double ys, int64_t ny, float *d_models) {
+    if (!ctx || !d_m_ini || !d_mags || !h_iso_off || !h_iso_len || !err || !compl_ || !imf ||
+        !h_dmod || !h_norm || !d_models || ntempl < 1 || ntempl > 65535)
+        return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    IsoParams P;
+    int rc0 = make_iso_params(ctx, nf, y_index, c1, c2, err, compl_, bias, imf, mean_mass, total, P);
+    if (rc0) return rc0;
+    P.dmag = std::fmin(std::fabs(xs), std::fabs(ys));  // :851
+    if ((rc0 = check_isochrones(ctx, h_iso_off, h_iso_len, ntempl, total))) return rc0;
+    return partial_run(ctx, d_m_ini, d_mags, h_iso_off, h_iso_len, ntempl, P, y_index, c1, h_dmod,
+                       h_norm, nullptr, xf, xs, nx, yf, ys, ny, d_models);
+}
+
+extern "C" int sfh_partial_cmd_smooth_ragged_dev(
+    sfh_ctx *ctx, const double *d_m_ini, const double *d_mags, int64_t total,
+    const int64_t *h_iso_off, const int32_t *h_iso_len, int64_t ntempl, int nf, int y_index,
+    int c1, int c2, const sfh_err_model *err, const sfh_compl_model *compl_, const double *bias,
+    const sfh_imf *imf, double mean_mass, const double *h_dmod, const double *h_norm,
+    const sfh_hess_grid *h_grids, int64_t models_len, float *d_models) {
+    if (!ctx || !d_m_ini || !d_mags || !h_iso_off || !h_iso_len || !err || !compl_ || !imf ||
+        !h_dmod || !h_norm || !h_grids || !d_models || ntempl < 1 || ntempl > (1 << 24) ||
+        models_len < 1)
+        return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    IsoParams P;
+    int rc0 = make_iso_params(ctx, nf, y_index, c1, c2, err, compl_, bias, imf, mean_mass, total, P);
+    if (rc0) return rc0;
+    if ((rc0 = check_isochrones(ctx, h_iso_off, h_iso_len, ntempl, total))) return rc0;
+    RaggedSpec rg;
+    rg.grids.resize((size_t)ntempl);
+    rg.out_off.resize((size_t)ntempl);
+    rg.dmag.resize((size_t)ntempl);
+    for (int64_t t = 0; t < ntempl; ++t) {
+        const sfh_hess_grid &h = h_grids[t];
+        if (h.nx < 1 || h.ny < 1 || h.nx > (1 << 20) || h.ny > (1 << 20) || !(h.x_step != 0) ||
+            !(h.y_step != 0))
+            return sfh_set_error(ctx, SFH_ERR_ARG, "Hess grid out of range");
+        if (h.out_offset < 0 || h.out_offset + h.nx * h.ny > models_len)
+            return sfh_set_error(ctx, SFH_ERR_ARG, "template output outside d_models");
+        const int TY = band_rows(h.nx, h.ny);
+        if (TY < 1)
+            return sfh_set_error(ctx, SFH_ERR_UNSUPPORTED, "Hess grid too wide for a shared-memory band");
+        rg.grids[(size_t)t] = Grid2{h.x_first, h.x_step, h.y_first, h.y_step, (int)h.nx, (int)h.ny};
+        rg.out_off[(size_t)t] = h.out_offset;
+        rg.dmag[(size_t)t] = std::fmin(std::fabs(h.x_step), std::fabs(h.y_step));  // :851
+        rg.smem = std::max(rg.smem, stamp_smem(h.nx, TY));
+        for (int64_t y0 = 0; y0 < h.ny; y0 += TY)
+            rg.tiles.push_back(StampTile{(int32_t)t, (int32_t)y0, (int32_t)TY});
+    }
+    if (rg.tiles.size() > 0x7fffffffu)
+        return sfh_set_error(ctx, SFH_ERR_UNSUPPORTED, "too many stamp tiles");
+    P.dmag = rg.dmag[0];
+    return partial_run(ctx, d_m_ini, d_mags, h_iso_off, h_iso_len, ntempl, P, y_index, c1, h_dmod,
+                       h_norm, &rg, 0.0, 0.0, 0, 0.0, 0.0, 0, d_models);
 }

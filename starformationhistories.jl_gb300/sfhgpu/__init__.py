@@ -6,15 +6,17 @@ All compute runs in libsfhgpu.so; there is no CPU fallback.
 from ._lib import (SFH_BF16X2, SFH_F32, SFH_F64, EXPORTED, LIB_PATH, SFHArgumentError, SFHError,
                    load)
 from .core import Context, Models, as_models, default_context
-from .fitting import (composite_, construct_x0, fg_, fg_batched, fit_templates, fit_templates_fast,
-                      fit_templates_lbfgsb, grad_loglikelihood, grad_loglikelihood_, loglikelihood,
-                      renormalize_x0, stack_models)
+from .emulator import SyntheticGenerator, TemplateEmulator
+from .fitting import (Galaxies, composite_, construct_x0, fg_, fg_batched, fg_ragged, fit_templates,
+                      fit_templates_fast, fit_templates_lbfgsb, grad_loglikelihood,
+                      grad_loglikelihood_, loglikelihood, renormalize_x0, stack_models)
 from .sampling import (GaussianDispersion, PowerLawMZR, calculate_coeffs, hmc_sample,
                        logdensity_batched, sample_sfh)
 from .templates import (BrokenPowerLawIMF, Histogram, Kroupa2001, Martin2016_complete,
                         bin_cmd_smooth, calculate_edges, calculate_weights, compl_model, err_model,
                         exp_photerr, histogram_data, histogram_pix, interpolate_mini, midpoints,
-                        mini_spacing, partial_cmd_smooth, partial_cmd_smooth_batch)
+                        mini_spacing, partial_cmd_smooth, partial_cmd_smooth_batch,
+                        partial_cmd_smooth_ragged)
 
 __all__ = [
     "SFH_BF16X2", "SFH_F32", "SFH_F64", "EXPORTED", "LIB_PATH", "SFHArgumentError", "SFHError",
@@ -25,5 +27,6 @@ __all__ = [
     "calculate_weights", "compl_model", "err_model", "exp_photerr", "histogram_data",
     "histogram_pix", "interpolate_mini", "midpoints", "mini_spacing", "partial_cmd_smooth",
     "partial_cmd_smooth_batch", "GaussianDispersion", "PowerLawMZR", "calculate_coeffs",
-    "hmc_sample", "logdensity_batched", "sample_sfh",
+    "hmc_sample", "logdensity_batched", "sample_sfh", "Galaxies", "fg_ragged",
+    "partial_cmd_smooth_ragged", "SyntheticGenerator", "TemplateEmulator",
 ]

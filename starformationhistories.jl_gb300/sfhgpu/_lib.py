@@ -26,7 +26,11 @@ EXPORTED = [
     "sfh_composite", "sfh_loglikelihood", "sfh_grad_loglikelihood", "sfh_fg", "sfh_fg_dev",
     "sfh_fg_batched_dev", "sfh_fg_kernel_times", "sfh_fg_dev_noalloc", "sfh_hmc_sample_dev",
     "sfh_logdensity_batched_dev", "sfh_bin_cmd_smooth", "sfh_bin_cmd_smooth_batch_dev",
-    "sfh_partial_cmd_smooth_batch_dev",
+    "sfh_partial_cmd_smooth_batch_dev", "sfh_partial_cmd_smooth_ragged_dev",
+    "sfh_galaxies_create", "sfh_galaxies_free", "sfh_galaxies_info", "sfh_fg_ragged_dev",
+    "sfh_mlp_param_count", "sfh_mlp_forward",
+    "sfh_mlp_loss_grad", "sfh_mlp_train", "sfh_gemm_f32", "sfh_emu_prepare",
+    "sfh_emu_reconstruct", "sfh_poisson_deviance",
 ]
 
 
@@ -113,6 +117,28 @@ def load(path: str | None = None):
                 [_vp, _vp, _vp, _i64, _vp, _vp, _i64, C.c_int, C.c_int, C.c_int, C.c_int,
                  C.POINTER(ErrModel), C.POINTER(ComplModel), _vp, C.POINTER(IMFParams), _d, _vp,
                  _vp, _d, _d, _i64, _d, _d, _i64, _vp], C.c_int),
+            "sfh_partial_cmd_smooth_ragged_dev": (
+                [_vp, _vp, _vp, _i64, _vp, _vp, _i64, C.c_int, C.c_int, C.c_int, C.c_int,
+                 C.POINTER(ErrModel), C.POINTER(ComplModel), _vp, C.POINTER(IMFParams), _d, _vp,
+                 _vp, _vp, _i64, _vp], C.c_int),
+            "sfh_galaxies_create": ([_vp, _vp, _i64, _vp, _i64, C.POINTER(_vp)], C.c_int),
+            "sfh_galaxies_free": ([_vp], C.c_int),
+            "sfh_galaxies_info": ([_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64)],
+                                  C.c_int),
+            "sfh_fg_ragged_dev": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _d], C.c_int),
+            "sfh_mlp_param_count": ([C.c_int] * 4 + [C.POINTER(_i64)], C.c_int),
+            "sfh_mlp_forward": ([_vp] + [C.c_int] * 4 + [_vp, _vp, C.c_int, _vp], C.c_int),
+            "sfh_mlp_loss_grad": ([_vp] + [C.c_int] * 4 + [_vp, _vp, _vp, C.c_int, _vp, _vp],
+                                  C.c_int),
+            "sfh_mlp_train": ([_vp] + [C.c_int] * 4 + [_vp, _vp, _vp, _i64, _vp, _vp, _i64,
+                                                       C.c_int, _i64, C.c_float, C.c_uint64,
+                                                       _vp], C.c_int),
+            "sfh_gemm_f32": ([_vp, _vp, _vp, _vp, _i64, _i64, _i64, C.c_int, C.c_int, C.c_int,
+                              C.c_float, C.c_int], C.c_int),
+            "sfh_emu_prepare": ([_vp, _vp, _i64, _i64, C.c_int, _vp], C.c_int),
+            "sfh_emu_reconstruct": ([_vp, _vp, _vp, _vp, C.c_int, _i64, _i64, C.c_int, _vp],
+                                    C.c_int),
+            "sfh_poisson_deviance": ([_vp, _vp, _vp, _i64, C.c_int, _vp], C.c_int),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)

@@ -301,3 +301,77 @@ def fg_batched(models, R, data, want_logl=True, want_grad=True, eps=None):
                                     G.data_ptr() if want_grad else None, e),
           M.ctx.handle, "fg_batched")
     return negL, G
+
+
+class GalaxyDesc(C.Structure):
+    """sfh_galaxy: where one galaxy's templates, bins and coefficients sit in the packed
+    arrays of a ragged batch."""
+    _fields_ = [("model_offset", C.c_int64), ("nbins", C.c_int64), ("ntempl", C.c_int64),
+                ("bin_offset", C.c_int64), ("templ_offset", C.c_int64)]
+
+
+class Galaxies:
+    """A ragged batch of independent galaxies (sfh_galaxies handle): galaxy g's
+    (nbins_g x ntempl_g) column-major FP32 templates live in one packed CUDA tensor.
+    Coefficients / gradients are packed galaxy after galaxy, as are data / composites."""
+
+    def __init__(self, models_packed, nbins, ntempl, model_offsets=None, ctx=None):
+        self.ctx = ctx or default_context()
+        nbins = np.asarray(nbins, dtype=np.int64)
+        ntempl = np.asarray(ntempl, dtype=np.int64)
+        _argcheck(nbins.shape == ntempl.shape and nbins.ndim == 1, "one nbins and ntempl per galaxy")
+        n = nbins.size
+        if model_offsets is None:
+            model_offsets = np.concatenate([[0], np.cumsum(nbins * ntempl)[:-1]])
+        self.bin_offsets = np.concatenate([[0], np.cumsum(nbins)]).astype(np.int64)
+        self.templ_offsets = np.concatenate([[0], np.cumsum(ntempl)]).astype(np.int64)
+        desc = (GalaxyDesc * n)()
+        for g in range(n):
+            desc[g] = GalaxyDesc(int(model_offsets[g]), int(nbins[g]), int(ntempl[g]),
+                                 int(self.bin_offsets[g]), int(self.templ_offsets[g]))
+        self.models = models_packed  # referenced by the handle: keep alive
+        self.nbins, self.ntempl = nbins, ntempl
+        h = C.c_void_p()
+        check(load().sfh_galaxies_create(self.ctx.handle, models_packed.data_ptr(),
+                                         int(models_packed.numel()), desc, n, C.byref(h)),
+              self.ctx.handle, "galaxies_create")
+        self.handle = h.value
+
+    @property
+    def ngal(self):
+        return self.nbins.size
+
+    def free(self):
+        if getattr(self, "handle", None):
+            load().sfh_galaxies_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:  # noqa: BLE001 - interpreter shutdown
+            pass
+
+
+def fg_ragged(galaxies: Galaxies, coeffs, data, want_logl=True, want_grad=True, eps=None):
+    """fg! (solvers.jl:20-38) for every galaxy of a ragged batch in one device call.
+    coeffs / data: packed CUDA float64 tensors (or numpy).  Returns (negLogL per galaxy or
+    None, packed G or None, packed composite) as CUDA tensors."""
+    import torch
+    ctx = galaxies.ctx
+    dev = torch.device("cuda", ctx.device)
+    r = torch.as_tensor(coeffs, dtype=torch.float64, device=dev).contiguous()
+    n = torch.as_tensor(data, dtype=torch.float64, device=dev).contiguous()
+    _argcheck(r.numel() == galaxies.templ_offsets[-1], "coefficients do not match the galaxies")
+    _argcheck(n.numel() == galaxies.bin_offsets[-1], "data do not match the galaxies")
+    comp = torch.empty_like(n)
+    G = torch.empty_like(r) if want_grad else None
+    negL = torch.empty(galaxies.ngal, dtype=torch.float64, device=dev) if want_logl else None
+    eps = float(np.finfo(np.float64).eps) if eps is None else float(eps)
+    torch.cuda.current_stream(dev).synchronize()
+    check(load().sfh_fg_ragged_dev(ctx.handle, galaxies.handle, r.data_ptr(), n.data_ptr(),
+                                   comp.data_ptr(), G.data_ptr() if G is not None else None,
+                                   negL.data_ptr() if negL is not None else None, eps),
+          ctx.handle, "fg_ragged")
+    ctx.synchronize()
+    return negL, G, comp

@@ -38,6 +38,24 @@ def isochrone(logAge: float, MH: float, n: int = 400):
     return m, np.stack([V + BV, V, V - 0.55 * BV])
 
 
+def isochrones(logAge, MH, n: int = 400):
+    """Vectorised isochrone() over B templates: (m_ini[B*n], mags[3, B*n]) with template
+    b's points at [b*n, (b+1)*n)."""
+    logAge = np.asarray(logAge, dtype=np.float64).reshape(-1, 1)
+    MH = np.asarray(MH, dtype=np.float64).reshape(-1, 1)
+    m = np.logspace(np.log10(0.1), np.log10(1.5), n)[None, :]
+    x = np.log10(m)
+    t = logAge - 6.6
+    xto = np.log10(1.45) - 0.07 * t
+    g = 0.5 * (1.0 + np.tanh((x - xto) / 0.02))
+    V = 4.8 - 7.5 * x + 0.3 * t - 6.0 * g
+    BV = 0.65 - 1.1 * x + 0.2 * MH + 0.9 * g * (1.0 - 0.3 * t / 3.5)
+    B = logAge.shape[0]
+    mags = np.stack([(V + BV).ravel(), np.broadcast_to(V, (B, n)).ravel(),
+                     (V - 0.55 * BV).ravel()])
+    return np.broadcast_to(m, (B, n)).ravel().copy(), mags
+
+
 @dataclass
 class Workload:
     name: str
@@ -158,3 +176,62 @@ def observed(models_f64: np.ndarray, n_stars: float, seed: int = SEED):
     m = models_f64 @ r
     rng = np.random.default_rng(seed + 1)
     return r, rng.poisson(m).astype(np.float64)
+
+
+@dataclass
+class Galaxy:
+    """One galaxy of the ragged workload: its own Hess grid, isochrone length, ages,
+    metallicities and distance modulus."""
+    xedges: np.ndarray
+    yedges: np.ndarray
+    n_iso: int
+    logAges: np.ndarray
+    MHs: np.ndarray
+    dmod: float
+
+    @property
+    def grid(self):
+        return (self.xedges.size - 1, self.yedges.size - 1)
+
+    @property
+    def nbins(self):
+        nx, ny = self.grid
+        return nx * ny
+
+    @property
+    def ntempl(self):
+        return self.logAges.size * self.MHs.size
+
+
+def ragged(ngal=256, nages=4, nmh=3, nxy=(50, 300), niso=(100, 2000), seed=SEED):
+    """Independent galaxies with uneven Hess grids (nx, ny uniform on nxy per axis, over
+    the same colour / magnitude window) and uneven isochrone lengths (uniform on niso);
+    ages uniform on [6.6, 10.1], [M/H] on [-2.5, 0.3], distance modulus on [24.5, 26.5]."""
+    rng = np.random.default_rng(seed + 7)
+    out = []
+    for _ in range(ngal):
+        nx, ny = (int(v) for v in rng.integers(nxy[0], nxy[1] + 1, 2))
+        xe, ye = _edges(nx, ny)
+        out.append(Galaxy(xe, ye, int(rng.integers(niso[0], niso[1] + 1)),
+                          np.sort(rng.uniform(6.6, 10.1, nages)), rng.uniform(-2.5, 0.3, nmh),
+                          float(rng.uniform(24.5, 26.5))))
+    return out
+
+
+def ragged_isochrones(galaxies):
+    """Concatenated isochrones of every template of every galaxy (galaxy-major, then
+    log age, then [M/H]): (m_ini, mags[3, total], iso_off, iso_len, dmod per template,
+    (xedges, yedges) per template)."""
+    ms, mg, lens, dm, edges = [], [], [], [], []
+    for g in galaxies:
+        la = np.repeat(g.logAges, g.MHs.size)
+        mh = np.tile(g.MHs, g.logAges.size)
+        m, mags = isochrones(la, mh, g.n_iso)
+        ms.append(m)
+        mg.append(mags)
+        lens += [g.n_iso] * la.size
+        dm += [g.dmod] * la.size
+        edges += [(g.xedges, g.yedges)] * la.size
+    lens = np.asarray(lens, dtype=np.int32)
+    offs = np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(np.int64)
+    return np.concatenate(ms), np.concatenate(mg, axis=1), offs, lens, np.asarray(dm), edges

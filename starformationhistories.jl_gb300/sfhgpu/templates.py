@@ -307,3 +307,56 @@ def partial_cmd_smooth_batch(m_ini, mags, iso_off, iso_len, y_index, color_indic
         E, Cm, b, C.byref(ip), mm, dm.ctypes.data, nm.ctypes.data, xf, xs, nx, yf, ys, ny,
         out.data_ptr()), ctx.handle, "partial_cmd_smooth_batch")
     return out
+
+
+class HessGrid(C.Structure):
+    """sfh_hess_grid: one template's Hess grid and output offset in a ragged batch."""
+    _fields_ = [("x_first", C.c_double), ("x_step", C.c_double), ("nx", C.c_int64),
+                ("y_first", C.c_double), ("y_step", C.c_double), ("ny", C.c_int64),
+                ("out_offset", C.c_int64)]
+
+
+def partial_cmd_smooth_ragged(m_ini, mags, iso_off, iso_len, y_index, color_indices, err_models,
+                              compl_models, imf, dmod, normalize_value, edges, mean_mass=None,
+                              bias=None, out=None, ctx=None):
+    """Many partial_cmd_smooth calls with their own Hess grids (ragged galaxies) in one
+    device call (sfh_partial_cmd_smooth_ragged_dev).  edges: one (xedges, yedges) pair per
+    template.  Returns (packed CUDA float32 tensor, offsets): template t's column-major
+    (nx_t, ny_t) histogram is out[offsets[t]:offsets[t+1]]."""
+    import torch
+    ctx = ctx or default_context()
+    nf, total = mags.shape
+    iso_off = np.ascontiguousarray(iso_off, dtype=np.int64)
+    iso_len = np.ascontiguousarray(iso_len, dtype=np.int32)
+    nt = iso_off.size
+    if len(edges) != nt:
+        raise ValueError("one (xedges, yedges) pair per template is required")
+    dm = np.ascontiguousarray(np.broadcast_to(np.asarray(dmod, dtype=np.float64), (nt,)))
+    nm = np.ascontiguousarray(np.broadcast_to(np.asarray(normalize_value, dtype=np.float64), (nt,)))
+    grids = (HessGrid * nt)()
+    offsets = np.zeros(nt + 1, dtype=np.int64)
+    for t, (xe, ye) in enumerate(edges):
+        (xf, xs, nx), (yf, ys, ny) = _range(xe), _range(ye)
+        grids[t] = HessGrid(xf, xs, nx, yf, ys, ny, int(offsets[t]))
+        offsets[t + 1] = offsets[t] + nx * ny
+    if out is None:
+        out = torch.empty(int(offsets[-1]), dtype=torch.float32, device=m_ini.device)
+    elif out.numel() < offsets[-1]:
+        raise ValueError("out is smaller than the packed histograms")
+    E = (ErrModel * nf)(*err_models)
+    Cm = (ComplModel * nf)(*compl_models)
+    b = None
+    if bias is not None:
+        barr = np.ascontiguousarray(bias, dtype=np.float64)
+        b = barr.ctypes.data
+    ip = imf.params()
+    mm = imf.mean() if mean_mass is None else float(mean_mass)
+    m_ini = m_ini.contiguous()
+    mags = mags.contiguous()
+    torch.cuda.current_stream(m_ini.device).synchronize()
+    check(load().sfh_partial_cmd_smooth_ragged_dev(
+        ctx.handle, m_ini.data_ptr(), mags.data_ptr(), int(total), iso_off.ctypes.data,
+        iso_len.ctypes.data, nt, nf, int(y_index), int(color_indices[0]), int(color_indices[1]),
+        E, Cm, b, C.byref(ip), mm, dm.ctypes.data, nm.ctypes.data, grids, int(out.numel()),
+        out.data_ptr()), ctx.handle, "partial_cmd_smooth_ragged")
+    return out, offsets
