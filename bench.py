@@ -332,6 +332,56 @@ def run_ragged(ctx, steps=50, warmup=5, check=2):
     }
 
 
+def run_emulator(ctx, w, n_train=65536, n_val=4096, steps=4000, cells=(8, 2, 16), nreq=1200):
+    """Learned template emulator on the production grid: per-cell PCA bases (64
+    components of sqrt templates) and per-cell MLPs 3-256-256-64 trained on templates the
+    GPU partial_cmd_smooth generates at random (log age, [M/H], distance modulus); judged
+    by Poisson deviance per star against exact templates (tolerance 1e-3)."""
+    import numpy as np
+    import torch
+
+    from sfhgpu.emulator import SyntheticGenerator, TemplateEmulator
+    gen = SyntheticGenerator(w.xedges, w.yedges, ctx=ctx)
+    em = TemplateEmulator(gen.nbins, ncomp=64, hidden=(256, 256), tol=1e-3, basis_cells=cells,
+                          ctx=ctx)
+    t0 = time.perf_counter()
+    rep = em.fit(gen, n_train=n_train, n_val=n_val, steps=steps, lr=1e-3, batch_per_cell=32)
+    fit_s = time.perf_counter() - t0
+    th = em.sample_theta(nreq, np.random.default_rng(5))
+    em.predict(th)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    exact = gen(th)
+    torch.cuda.synchronize()
+    t_exact = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    emul = em.predict(th)
+    torch.cuda.synchronize()
+    t_emul = time.perf_counter() - t0
+    dev = em.judge(exact, emul)
+    trusted = em.trusted(th)
+    t0 = time.perf_counter()
+    em.templates(th, gen)  # trust-map routing: emulated where validated, exact elsewhere
+    torch.cuda.synchronize()
+    t_routed = time.perf_counter() - t0
+    return {
+        "workload": f"{n_train} training templates on the 200x300 grid, theta = (log age "
+                    f"U[6.6,10.1], [M/H] U[-2.5,0.3], dmod U[24,30]); {int(np.prod(cells))} "
+                    f"cells {cells}, PCA 64 of sqrt templates, MLP 3-256-256-64 per cell; "
+                    f"{nreq} fresh requests",
+        "fit_seconds": fit_s, "generate_seconds": rep.generate_seconds,
+        "pca_seconds": rep.pca_seconds, "train_seconds": rep.train_seconds,
+        "final_loss": rep.final_loss, "val_deviance_quantiles": rep.val_deviance_quantiles,
+        "val_frac_within_1e-3": rep.val_frac_within_tol,
+        "requests_frac_within_1e-3": float(np.mean(dev <= 1e-3)),
+        "requests_deviance_median": float(np.median(dev)),
+        "trusted_frac": float(np.mean(trusted)),
+        "emulated_templates_per_s": nreq / t_emul, "exact_templates_per_s": nreq / t_exact,
+        "routed_templates_per_s": nreq / t_routed,
+        "routed_speedup_vs_exact": t_exact / t_routed,
+    }
+
+
 def cpu_fg_baseline(M64, r, data, budget_s=10.0, threads=None):
     """The oracle's fg! (FP64, OpenMP over bins/templates) on a bounded number of evals."""
     import numpy as np
@@ -470,6 +520,19 @@ def run_ours(args):
     e1.synchronize()
     build_ms = e0.elapsed_time(e1) / nbuild
     templates_per_s = w.ntempl / (build_ms / 1e3)
+    # work of the build in its own unit: bin updates (stamp windows clipped to the grid,
+    # counted by the host mirror on 48 templates spread over the grid, scaled to all)
+    from sfhgpu.templates import partial_cmd_smooth_stars, stamp_bin_updates
+    la, mh = w.template_params
+    pick = np.linspace(0, w.ntempl - 1, 48).astype(int)
+    upd = 0
+    for t in pick:
+        mi, mg = S.isochrone(la[t], mh[t], w.n_iso)
+        xs_, ys_, sx_, sy_, _, cov_, e_ = partial_cmd_smooth_stars(
+            mi, list(mg), S.error_funcs(), 1, (0, 1), S.imf(), S.completeness_funcs(),
+            dmod=w.dmod, edges=(w.xedges, w.yedges))
+        upd += int(stamp_bin_updates(xs_, ys_, sx_, sy_, cov_, e_).sum())
+    bin_updates = upd * w.ntempl / pick.size
 
     # ---- template matrix handle (FP32 storage) and observed data
     H = sfhgpu.Models.from_device(d_T.data_ptr(), NBINS, NTW, storage="f32", ctx=ctx)
@@ -563,6 +626,11 @@ def run_ours(args):
     if not args.no_ragged:
         ragged = run_ragged(ctx)
 
+    # ---- learned template emulator (production grid), judged against exact templates
+    emulator = None
+    if not args.no_emulator:
+        emulator = run_emulator(ctx, w)
+
     # ---- end-to-end hierarchical HMC (1,024 chains, MZR) on the same templates
     hmc = None
     if not args.no_hmc:
@@ -591,8 +659,10 @@ def run_ours(args):
                        "l2": "inputs larger than L2 (288 MB template matrix)",
                        "parallelism": f"replicas x{world}"},
             "templates_per_s": templates_per_s, "template_build_ms": build_ms,
+            "template_bin_updates_per_s": bin_updates / (build_ms / 1e3),
+            "template_bin_updates_per_build": bin_updates,
             "negLogL": neglogl, "gpu_launches": launches, "roofline": roofline,
-            "batched": batched, "hmc": hmc, "ragged": ragged,
+            "batched": batched, "hmc": hmc, "ragged": ragged, "emulator": emulator,
             "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
         }
         print(json.dumps(line), flush=True)
@@ -613,6 +683,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched tensor-core leg")
     ap.add_argument("--no-hmc", action="store_true", help="skip the batched HMC leg")
     ap.add_argument("--no-ragged", action="store_true", help="skip the ragged-galaxies leg")
+    ap.add_argument("--no-emulator", action="store_true", help="skip the emulator leg")
     ap.add_argument("--ntempl", type=int, default=NT,
                     help="templates (multiple of 30); fewer than 1200 only for profiling")
     ap.add_argument("--cpu-budget-s", type=float, default=10.0)

@@ -325,6 +325,26 @@ int sfh_mlp_train(sfh_ctx *ctx, int in, int h1, int h2, int out, float *d_params
                   float *d_adam_m, float *d_adam_v, int64_t step0, const float *d_X,
                   const float *d_T, int64_t nsamples, int batch, int64_t nsteps, float lr,
                   uint64_t seed, float *d_loss_trace);
+/* Local-basis emulator: ngroups independent MLPs (one per cell of the parameter space),
+   parameter blocks back to back (d_params is ngroups x n).  Training draws batch_per_group
+   rows per group and step from the group's samples [h_group_off[g], h_group_off[g+1]) of
+   d_X / d_T (samples sorted by group; host offsets, every group non-empty); one Adam
+   update covers all groups; d_loss_trace receives the loss averaged over groups. */
+int sfh_mlp_train_grouped(sfh_ctx *ctx, int in, int h1, int h2, int out, int64_t ngroups,
+                          float *d_params, float *d_adam_m, float *d_adam_v, int64_t step0,
+                          const float *d_X, const float *d_T, const int64_t *h_group_off,
+                          int batch_per_group, int64_t nsteps, float lr, uint64_t seed,
+                          float *d_loss_trace);
+/* d_Y (B x out): row b through the MLP of group d_group[b] (d_group may be NULL when
+   ngroups == 1).  Same BF16-operand arithmetic as training.  Enqueued, not synchronised. */
+int sfh_mlp_forward_rows(sfh_ctx *ctx, int in, int h1, int h2, int out, const float *d_params,
+                         int64_t ngroups, const float *d_X, const int32_t *d_group, int64_t B,
+                         float *d_Y);
+/* As sfh_emu_reconstruct with one basis (ngroups x K x nbins) and offset (ngroups x nbins)
+   per group; row b uses group d_group[b].  B <= 65535.  Enqueued, not synchronised. */
+int sfh_emu_reconstruct_rows(sfh_ctx *ctx, const float *d_coef, const int32_t *d_group,
+                             int64_t ngroups, const float *d_basis, const float *d_offset, int K,
+                             int64_t nbins, int64_t B, int mode, float *d_out);
 /* d_C (M x N) = alpha op(A) op(B) (+ d_C when accum), FP32 accumulation, ta / tb select
    row-major A (M x K) / (K x M) and B (K x N) / (N x K); bf16 != 0 rounds the operands to
    BF16 first.  Used for the PCA basis (randomized range finder) and projections. */

@@ -23,7 +23,7 @@ constexpr int GBM = 64, GBN = 64, GBK = 16, GTHREADS = 256;
 
 __device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
 
-// C[M x N] = alpha op(A) op(B) (+ C when accum).  op(A) is M x K: A stored (M x K) row-major
+// C[M x N] = alpha op(A) op(B) (+ C when accum), for each GEMM of a strided batch.  op(A) is M x K: A stored (M x K) row-major
 // (ta = 0) or (K x M) row-major (ta = 1); op(B) is K x N: B stored (K x N) (tb = 0) or
 // (N x K) (tb = 1).  FP32 accumulation; ROUND rounds every operand to BF16 first (the
 // MLP's BF16 matmuls over FP32 master weights).  64 x 64 tiles, 16 x 16 threads with
@@ -31,7 +31,12 @@ __device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__floa
 template <bool ROUND>
 __global__ void __launch_bounds__(GTHREADS)
 k_gemm(const float *__restrict__ A, const float *__restrict__ B, float *__restrict__ C, int M, int N,
-       int K, int ta, int tb, int accum, float alpha) {
+       int K, int ta, int tb, int accum, float alpha, int64_t strideA, int64_t strideB,
+       int64_t strideC) {
+    // blockIdx.z selects one GEMM of a strided batch (one per MLP group)
+    A += blockIdx.z * strideA;
+    B += blockIdx.z * strideB;
+    C += blockIdx.z * strideC;
     __shared__ float sA[GBK][GBM + 4];
     __shared__ float sB[GBK][GBN + 4];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
@@ -96,12 +101,13 @@ __device__ __forceinline__ float gelu_grad(float z) {
            z * 0.3989422804014327f * expf(-0.5f * z * z);
 }
 
-// Z += b (per column); A = GELU(Z) when act.
+// Z += b (per column; rows come in groups of rpg, group g's bias at b + g * pstride);
+// A = GELU(Z) when act.
 __global__ void k_bias_act(float *__restrict__ Z, float *__restrict__ A, const float *__restrict__ b,
-                           int64_t M, int N, int act) {
+                           int64_t M, int N, int act, int64_t rpg, int64_t pstride) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= M * N) return;
-    const float z = Z[k] + b[k % N];
+    const float z = Z[k] + b[(k / N / rpg) * pstride + k % N];
     Z[k] = z;
     if (act) A[k] = gelu(z);
 }
@@ -112,14 +118,15 @@ __global__ void k_gelu_back(float *__restrict__ dA, const float *__restrict__ Z,
     if (k < n) dA[k] *= gelu_grad(Z[k]);
 }
 
-// column sums of X (M x N): db = Σ_rows
-__global__ void k_colsum(const float *__restrict__ X, int64_t M, int64_t N, float *__restrict__ out,
-                         float scale) {
-    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= N) return;
+// Column sums of each group of rpg rows of X (G*rpg x N): out[g * pstride + n].
+__global__ void k_colsum(const float *__restrict__ X, int64_t rpg, int64_t N, int64_t G,
+                         float *__restrict__ out, int64_t pstride, float scale) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= G * N) return;
+    const int64_t g = t / N, n = t % N;
     float h = 0.f, l = 0.f;
-    for (int64_t m = 0; m < M; ++m) sfh_two_sum_acc(h, l, X[m * N + n]);
-    out[n] = (h + l) * scale;
+    for (int64_t m = g * rpg; m < (g + 1) * rpg; ++m) sfh_two_sum_acc(h, l, X[m * N + n]);
+    out[g * pstride + n] = (h + l) * scale;
 }
 
 // MSE: dY = 2 (Y - T) / (M N); per-block partial loss
@@ -179,16 +186,19 @@ __device__ __forceinline__ u4 philox(u4 c, uint32_t k0, uint32_t k1) {  // Salmo
     return c;
 }
 
-// Minibatch gather: row i of the batch = sample floor(u * N) for a Philox uniform u.
+// Minibatch gather: row i of group g's batch = sample off[g] + floor(u * (off[g+1] - off[g]))
+// for a Philox uniform u (off == NULL: one group over all N samples).
 __global__ void k_gather(const float *__restrict__ X, const float *__restrict__ T, int64_t N,
-                         int din, int dout, int B, uint64_t seed, int64_t step,
-                         float *__restrict__ Xb, float *__restrict__ Tb) {
-    const int i = blockIdx.x;
-    const u4 r = philox(u4{(uint32_t)i, (uint32_t)step, (uint32_t)(step >> 32), 7u}, (uint32_t)seed,
-                        (uint32_t)(seed >> 32));
-    const int64_t s = (int64_t)(((uint64_t)r.x * (uint64_t)N) >> 32);
-    for (int j = threadIdx.x; j < din; j += blockDim.x) Xb[(int64_t)i * din + j] = X[s * din + j];
-    for (int j = threadIdx.x; j < dout; j += blockDim.x) Tb[(int64_t)i * dout + j] = T[s * dout + j];
+                         const int64_t *__restrict__ off, int din, int dout, int B, uint64_t seed,
+                         int64_t step, float *__restrict__ Xb, float *__restrict__ Tb) {
+    const int i = blockIdx.x, g = blockIdx.y;
+    const u4 r = philox(u4{(uint32_t)i, (uint32_t)step, (uint32_t)(step >> 32), 7u ^ ((uint32_t)g << 8)},
+                        (uint32_t)seed, (uint32_t)(seed >> 32));
+    const int64_t lo = off ? off[g] : 0, cnt = off ? off[g + 1] - off[g] : N;
+    const int64_t s = lo + (int64_t)(((uint64_t)r.x * (uint64_t)cnt) >> 32);
+    const int64_t row = (int64_t)g * B + i;
+    for (int j = threadIdx.x; j < din; j += blockDim.x) Xb[row * din + j] = X[s * din + j];
+    for (int j = threadIdx.x; j < dout; j += blockDim.x) Tb[row * dout + j] = T[s * dout + j];
 }
 
 // Variance-stabilising transform of templates, in place: y = sqrt(t) (mode 1) or y = t.
@@ -256,101 +266,201 @@ MlpShape mlp_shape(int in, int h1, int h2, int out) {
     return s;
 }
 
-struct Acts {  // activations of one batch
+// One row per CTA, each row with its own group's parameters (inference over rows that
+// belong to different groups).  Same arithmetic as the GEMM path: BF16-rounded operands,
+// FP32 products accumulated in k order, bias added last, GELU after the hidden layers.
+__global__ void k_mlp_rows(const float *__restrict__ P, int64_t pstride, int64_t ngroups, MlpShape S,
+                           const float *__restrict__ X, const int32_t *__restrict__ group,
+                           float *__restrict__ Y) {
+    extern __shared__ float sm[];
+    float *x = sm, *a1 = sm + S.in, *a2 = a1 + S.h1;
+    const int64_t row = blockIdx.x;
+    const int64_t g = group ? (int64_t)group[row] : 0;
+    if (g < 0 || g >= ngroups) {  // invalid group: NaN row, no out-of-range read
+        for (int j = threadIdx.x; j < S.out; j += blockDim.x) Y[row * S.out + j] = __int_as_float(0x7fc00000);
+        return;
+    }
+    const float *p = P + g * pstride;
+    for (int j = threadIdx.x; j < S.in; j += blockDim.x) x[j] = bf16r(X[row * S.in + j]);
+    __syncthreads();
+    for (int j = threadIdx.x; j < S.h1; j += blockDim.x) {
+        const float *w = p + S.oW1 + (int64_t)j * S.in;
+        float acc = 0.f;
+        for (int k = 0; k < S.in; ++k) acc = fmaf(x[k], bf16r(w[k]), acc);
+        a1[j] = bf16r(gelu(acc + p[S.ob1 + j]));
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < S.h2; j += blockDim.x) {
+        const float *w = p + S.oW2 + (int64_t)j * S.h1;
+        float acc = 0.f;
+        for (int k = 0; k < S.h1; ++k) acc = fmaf(a1[k], bf16r(w[k]), acc);
+        a2[j] = bf16r(gelu(acc + p[S.ob2 + j]));
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < S.out; j += blockDim.x) {
+        const float *w = p + S.oW3 + (int64_t)j * S.h2;
+        float acc = 0.f;
+        for (int k = 0; k < S.h2; ++k) acc = fmaf(a2[k], bf16r(w[k]), acc);
+        Y[row * S.out + j] = acc + p[S.ob3 + j];
+    }
+}
+
+// Templates from coefficients with a basis per row's group:
+// out[b, i] = inverse transform of (offset[g, i] + Σ_k coef[b, k] basis[g, k, i]), g = group[b].
+__global__ void k_recon_rows(const float *__restrict__ coef, const int32_t *__restrict__ group,
+                             int64_t ngroups, const float *__restrict__ basis,
+                             const float *__restrict__ offset, int K, int64_t nbins, int mode,
+                             float *__restrict__ out) {
+    extern __shared__ float sc[];
+    const int64_t b = blockIdx.y;
+    const int64_t g = group ? group[b] : 0;
+    if (g < 0 || g >= ngroups) {  // invalid group: NaN row, no out-of-range read
+        const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+        if (i < nbins) out[b * nbins + i] = __int_as_float(0x7fc00000);
+        return;
+    }
+    for (int k = threadIdx.x; k < K; k += blockDim.x) sc[k] = coef[b * K + k];
+    __syncthreads();
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nbins) return;
+    const float *v = basis + g * K * nbins + i;
+    float acc = 0.f;
+    for (int k = 0; k < K; ++k) acc = fmaf(sc[k], v[(int64_t)k * nbins], acc);
+    const float y = fmaxf(acc + offset[g * nbins + i], 0.f);
+    out[b * nbins + i] = mode == 1 ? y * y : y;
+}
+
+struct Acts {  // activations of one batch (G groups x B rows)
     float *Z1, *A1, *Z2, *A2, *Y;
 };
 
 int gemm(sfh_ctx *ctx, const float *A, const float *B, float *C, int M, int N, int K, int ta,
-         int tb, int accum, bool round = true, float alpha = 1.0f) {
-    if (M < 1 || N < 1 || K < 1) return SFH_OK;
-    dim3 grid((N + GBN - 1) / GBN, (M + GBM - 1) / GBM);
-    if (grid.y > 65535) return sfh_set_error(ctx, SFH_ERR_SHAPE, "GEMM too many row tiles");
+         int tb, int accum, bool round = true, float alpha = 1.0f, int batch = 1,
+         int64_t sA = 0, int64_t sB = 0, int64_t sC = 0) {
+    if (M < 1 || N < 1 || K < 1 || batch < 1) return SFH_OK;
+    dim3 grid((N + GBN - 1) / GBN, (M + GBM - 1) / GBM, batch);
+    if (grid.y > 65535 || batch > 65535)
+        return sfh_set_error(ctx, SFH_ERR_SHAPE, "GEMM too many row tiles or groups");
     if (round)
-        k_gemm<true><<<grid, GTHREADS, 0, ctx->stream>>>(A, B, C, M, N, K, ta, tb, accum, alpha);
+        k_gemm<true><<<grid, GTHREADS, 0, ctx->stream>>>(A, B, C, M, N, K, ta, tb, accum, alpha, sA,
+                                                         sB, sC);
     else
-        k_gemm<false><<<grid, GTHREADS, 0, ctx->stream>>>(A, B, C, M, N, K, ta, tb, accum, alpha);
+        k_gemm<false><<<grid, GTHREADS, 0, ctx->stream>>>(A, B, C, M, N, K, ta, tb, accum, alpha, sA,
+                                                          sB, sC);
     SFH_LAUNCHED(ctx);
     return SFH_OK;
 }
 
-int forward(sfh_ctx *ctx, const MlpShape &S, const float *P, const float *X, int B, Acts &a) {
-    int rc;
-    const int T = 256;
-    // Z1 = X W1ᵀ + b1, A1 = GELU(Z1)
-    if ((rc = gemm(ctx, X, P + S.oW1, a.Z1, B, S.h1, S.in, 0, 1, 0))) return rc;
-    k_bias_act<<<(unsigned)(((int64_t)B * S.h1 + T - 1) / T), T, 0, ctx->stream>>>(a.Z1, a.A1, P + S.ob1, B, S.h1, 1);
-    SFH_LAUNCHED(ctx);
-    if ((rc = gemm(ctx, a.A1, P + S.oW2, a.Z2, B, S.h2, S.h1, 0, 1, 0))) return rc;
-    k_bias_act<<<(unsigned)(((int64_t)B * S.h2 + T - 1) / T), T, 0, ctx->stream>>>(a.Z2, a.A2, P + S.ob2, B, S.h2, 1);
-    SFH_LAUNCHED(ctx);
-    if ((rc = gemm(ctx, a.A2, P + S.oW3, a.Y, B, S.out, S.h2, 0, 1, 0))) return rc;
-    k_bias_act<<<(unsigned)(((int64_t)B * S.out + T - 1) / T), T, 0, ctx->stream>>>(a.Y, nullptr, P + S.ob3, B, S.out, 0);
+int bias_act(sfh_ctx *ctx, float *Z, float *A, const float *b, int64_t rows, int N, int act,
+             int64_t rpg, int64_t pstride) {
+    k_bias_act<<<(unsigned)((rows * N + 255) / 256), 256, 0, ctx->stream>>>(Z, A, b, rows, N, act,
+                                                                           rpg, pstride);
     SFH_LAUNCHED(ctx);
     return SFH_OK;
 }
 
-// Gradient of the MSE loss w.r.t. all parameters into Gr; dY is consumed (overwritten).
-int backward(sfh_ctx *ctx, const MlpShape &S, const float *P, const float *X, int B, Acts &a,
-             float *dY, float *dA2, float *dA1, float *Gr) {
+int colsum(sfh_ctx *ctx, const float *X, int64_t rpg, int64_t N, int64_t G, float *out,
+           int64_t pstride) {
+    k_colsum<<<(unsigned)((G * N + 255) / 256), 256, 0, ctx->stream>>>(X, rpg, N, G, out, pstride,
+                                                                       1.0f);
+    SFH_LAUNCHED(ctx);
+    return SFH_OK;
+}
+
+int gelu_back(sfh_ctx *ctx, float *dA, const float *Z, int64_t n) {
+    k_gelu_back<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(dA, Z, n);
+    SFH_LAUNCHED(ctx);
+    return SFH_OK;
+}
+
+// Forward pass of G independent MLPs (parameters P + g * S.n), B rows each; X is G*B x in.
+int forward(sfh_ctx *ctx, const MlpShape &S, const float *P, int G, const float *X, int B,
+            Acts &a) {
     int rc;
-    const int T = 256;
-    // layer 3
-    if ((rc = gemm(ctx, dY, a.A2, Gr + S.oW3, S.out, S.h2, B, 1, 0, 0))) return rc;  // dYᵀ A2
-    k_colsum<<<(S.out + T - 1) / T, T, 0, ctx->stream>>>(dY, B, S.out, Gr + S.ob3, 1.0f);
-    SFH_LAUNCHED(ctx);
-    if ((rc = gemm(ctx, dY, P + S.oW3, dA2, B, S.h2, S.out, 0, 0, 0))) return rc;  // dY W3
-    k_gelu_back<<<(unsigned)(((int64_t)B * S.h2 + T - 1) / T), T, 0, ctx->stream>>>(dA2, a.Z2, (int64_t)B * S.h2);
-    SFH_LAUNCHED(ctx);
+    const int64_t rows = (int64_t)G * B;
+    if ((rc = gemm(ctx, X, P + S.oW1, a.Z1, B, S.h1, S.in, 0, 1, 0, true, 1.f, G,
+                   (int64_t)B * S.in, S.n, (int64_t)B * S.h1)))
+        return rc;
+    if ((rc = bias_act(ctx, a.Z1, a.A1, P + S.ob1, rows, S.h1, 1, B, S.n))) return rc;
+    if ((rc = gemm(ctx, a.A1, P + S.oW2, a.Z2, B, S.h2, S.h1, 0, 1, 0, true, 1.f, G,
+                   (int64_t)B * S.h1, S.n, (int64_t)B * S.h2)))
+        return rc;
+    if ((rc = bias_act(ctx, a.Z2, a.A2, P + S.ob2, rows, S.h2, 1, B, S.n))) return rc;
+    if ((rc = gemm(ctx, a.A2, P + S.oW3, a.Y, B, S.out, S.h2, 0, 1, 0, true, 1.f, G,
+                   (int64_t)B * S.h2, S.n, (int64_t)B * S.out)))
+        return rc;
+    return bias_act(ctx, a.Y, nullptr, P + S.ob3, rows, S.out, 0, B, S.n);
+}
+
+// Gradient of the MSE loss w.r.t. all G parameter blocks into Gr (G x S.n); dY is consumed.
+int backward(sfh_ctx *ctx, const MlpShape &S, const float *P, int G, const float *X, int B,
+             Acts &a, float *dY, float *dA2, float *dA1, float *Gr) {
+    int rc;
+    const int64_t b = B;
+    // layer 3: dW3 = dYᵀ A2, db3 = Σ dY, dA2 = dY W3
+    if ((rc = gemm(ctx, dY, a.A2, Gr + S.oW3, S.out, S.h2, B, 1, 0, 0, true, 1.f, G, b * S.out,
+                   b * S.h2, S.n)))
+        return rc;
+    if ((rc = colsum(ctx, dY, B, S.out, G, Gr + S.ob3, S.n))) return rc;
+    if ((rc = gemm(ctx, dY, P + S.oW3, dA2, B, S.h2, S.out, 0, 0, 0, true, 1.f, G, b * S.out, S.n,
+                   b * S.h2)))
+        return rc;
+    if ((rc = gelu_back(ctx, dA2, a.Z2, (int64_t)G * b * S.h2))) return rc;
     // layer 2
-    if ((rc = gemm(ctx, dA2, a.A1, Gr + S.oW2, S.h2, S.h1, B, 1, 0, 0))) return rc;
-    k_colsum<<<(S.h2 + T - 1) / T, T, 0, ctx->stream>>>(dA2, B, S.h2, Gr + S.ob2, 1.0f);
-    SFH_LAUNCHED(ctx);
-    if ((rc = gemm(ctx, dA2, P + S.oW2, dA1, B, S.h1, S.h2, 0, 0, 0))) return rc;
-    k_gelu_back<<<(unsigned)(((int64_t)B * S.h1 + T - 1) / T), T, 0, ctx->stream>>>(dA1, a.Z1, (int64_t)B * S.h1);
-    SFH_LAUNCHED(ctx);
+    if ((rc = gemm(ctx, dA2, a.A1, Gr + S.oW2, S.h2, S.h1, B, 1, 0, 0, true, 1.f, G, b * S.h2,
+                   b * S.h1, S.n)))
+        return rc;
+    if ((rc = colsum(ctx, dA2, B, S.h2, G, Gr + S.ob2, S.n))) return rc;
+    if ((rc = gemm(ctx, dA2, P + S.oW2, dA1, B, S.h1, S.h2, 0, 0, 0, true, 1.f, G, b * S.h2, S.n,
+                   b * S.h1)))
+        return rc;
+    if ((rc = gelu_back(ctx, dA1, a.Z1, (int64_t)G * b * S.h1))) return rc;
     // layer 1
-    if ((rc = gemm(ctx, dA1, X, Gr + S.oW1, S.h1, S.in, B, 1, 0, 0))) return rc;
-    k_colsum<<<(S.h1 + T - 1) / T, T, 0, ctx->stream>>>(dA1, B, S.h1, Gr + S.ob1, 1.0f);
-    SFH_LAUNCHED(ctx);
-    return SFH_OK;
+    if ((rc = gemm(ctx, dA1, X, Gr + S.oW1, S.h1, S.in, B, 1, 0, 0, true, 1.f, G, b * S.h1,
+                   b * S.in, S.n)))
+        return rc;
+    return colsum(ctx, dA1, B, S.h1, G, Gr + S.ob1, S.n);
 }
 
 struct Work {
     Acts a{};
     float *dY = nullptr, *dA2 = nullptr, *dA1 = nullptr, *lp = nullptr;
     float *Xb = nullptr, *Tb = nullptr, *Gr = nullptr;  // training only
+    int64_t *off = nullptr;                              // grouped training only
 };
 
-// Carves the MLP buffers out of the context scratch: no allocation once the scratch
-// is large enough, so repeated inference and training calls cost only their kernels.
-int make_work(sfh_ctx *ctx, Work &w, const MlpShape &S, int B, bool train) {
-    const size_t b = (size_t)B;
+// Carves the MLP buffers for G groups of B rows out of the context scratch: no allocation
+// once the scratch is large enough, so repeated calls cost only their kernels.
+int make_work(sfh_ctx *ctx, Work &w, const MlpShape &S, int G, int B, bool train) {
+    const size_t b = (size_t)G * (size_t)B;
     struct Item {
-        float **p;
-        size_t n;
-    } items[] = {{&w.a.Z1, b * S.h1}, {&w.a.A1, b * S.h1}, {&w.a.Z2, b * S.h2},
-                 {&w.a.A2, b * S.h2}, {&w.a.Y, b * S.out}, {&w.dY, b * S.out},
-                 {&w.dA2, b * S.h2}, {&w.dA1, b * S.h1}, {&w.lp, (b * S.out + 255) / 256 + 1},
-                 {&w.Xb, train ? b * S.in : 0}, {&w.Tb, train ? b * S.out : 0},
-                 {&w.Gr, train ? (size_t)S.n : 0}};
+        void *p;
+        size_t bytes;
+    } items[] = {{&w.a.Z1, b * S.h1 * 4}, {&w.a.A1, b * S.h1 * 4}, {&w.a.Z2, b * S.h2 * 4},
+                 {&w.a.A2, b * S.h2 * 4}, {&w.a.Y, b * S.out * 4}, {&w.dY, b * S.out * 4},
+                 {&w.dA2, b * S.h2 * 4}, {&w.dA1, b * S.h1 * 4},
+                 {&w.lp, ((b * S.out + 255) / 256 + 1) * 4},
+                 {&w.Xb, train ? b * S.in * 4 : 0}, {&w.Tb, train ? b * S.out * 4 : 0},
+                 {&w.Gr, train ? (size_t)G * S.n * 4 : 0},
+                 {&w.off, train ? ((size_t)G + 1) * 8 : 0}};
     size_t total = 0;
-    for (const Item &it : items) total += sfh_align256((it.n ? it.n : 1) * sizeof(float));
+    for (const Item &it : items) total += sfh_align256(it.bytes ? it.bytes : 4);
     int rc = sfh_scratch_reserve(ctx, total);
     if (rc) return rc;
     char *base = (char *)ctx->scratch;
-    size_t off = 0;
+    size_t o = 0;
     for (const Item &it : items) {
-        *it.p = it.n ? (float *)(base + off) : nullptr;
-        off += sfh_align256((it.n ? it.n : 1) * sizeof(float));
+        *(void **)it.p = it.bytes ? (void *)(base + o) : nullptr;
+        o += sfh_align256(it.bytes ? it.bytes : 4);
     }
     return SFH_OK;
 }
 
-int loss_grad(sfh_ctx *ctx, const MlpShape &S, const float *P, const float *X, const float *Tg,
-              int B, Work &w, float *Gr, float *d_loss) {
-    int rc = forward(ctx, S, P, X, B, w.a);
+int loss_grad(sfh_ctx *ctx, const MlpShape &S, const float *P, int G, const float *X,
+              const float *Tg, int B, Work &w, float *Gr, float *d_loss) {
+    int rc = forward(ctx, S, P, G, X, B, w.a);
     if (rc) return rc;
-    const int64_t n = (int64_t)B * S.out;
+    const int64_t n = (int64_t)G * B * S.out;
     const int nb = (int)((n + 255) / 256);
     k_mse<<<nb, 256, 0, ctx->stream>>>(w.a.Y, Tg, n, 1.0f / (float)n, w.dY, w.lp);
     SFH_LAUNCHED(ctx);
@@ -358,47 +468,92 @@ int loss_grad(sfh_ctx *ctx, const MlpShape &S, const float *P, const float *X, c
         k_sum<<<1, 32, 0, ctx->stream>>>(w.lp, nb, d_loss);
         SFH_LAUNCHED(ctx);
     }
-    return backward(ctx, S, P, X, B, w.a, w.dY, w.dA2, w.dA1, Gr);
+    return backward(ctx, S, P, G, X, B, w.a, w.dY, w.dA2, w.dA1, Gr);
+}
+
+bool bad_shape(int in, int h1, int h2, int out) {
+    return in < 1 || h1 < 1 || h2 < 1 || out < 1 || in > 1024 || h1 > 1024 || h2 > 1024 ||
+           out > 1024;
+}
+
+// Adam steps over minibatches drawn per group; G == 1 with off == NULL draws from all rows.
+int train(sfh_ctx *ctx, const MlpShape &S, int G, float *d_params, float *d_m, float *d_v,
+          int64_t step0, const float *d_X, const float *d_T, int64_t nsamples,
+          const int64_t *h_off, int batch, int64_t nsteps, float lr, uint64_t seed,
+          float *d_loss_trace) {
+    Work w;
+    int rc = make_work(ctx, w, S, G, batch, true);
+    if (rc) return rc;
+    cudaStream_t st = ctx->stream;
+    if (h_off) SFH_CK(ctx, cudaMemcpyAsync(w.off, h_off, ((size_t)G + 1) * 8, cudaMemcpyHostToDevice, st));
+    const float b1 = 0.9f, b2 = 0.999f;
+    const int64_t np = (int64_t)G * S.n;
+    for (int64_t it = 0; it < nsteps; ++it) {
+        const int64_t step = step0 + it + 1;
+        k_gather<<<dim3((unsigned)batch, (unsigned)G), 64, 0, st>>>(
+            d_X, d_T, nsamples, h_off ? w.off : nullptr, S.in, S.out, batch, seed, step, w.Xb, w.Tb);
+        SFH_LAUNCHED(ctx);
+        rc = loss_grad(ctx, S, d_params, G, w.Xb, w.Tb, batch, w, w.Gr,
+                       d_loss_trace ? d_loss_trace + it : nullptr);
+        if (rc) return rc;
+        const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
+        k_adam<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(d_params, w.Gr, d_m, d_v, np, lr, b1, b2,
+                                                             1e-8f, c1, c2);
+        SFH_LAUNCHED(ctx);
+    }
+    SFH_CK(ctx, cudaStreamSynchronize(st));
+    return SFH_OK;
 }
 
 }  // namespace
 
 extern "C" int sfh_mlp_param_count(int in, int h1, int h2, int out, int64_t *n) {
-    if (!n || in < 1 || h1 < 1 || h2 < 1 || out < 1) return SFH_ERR_ARG;
+    if (!n || bad_shape(in, h1, h2, out)) return SFH_ERR_ARG;
     *n = mlp_shape(in, h1, h2, out).n;
     return SFH_OK;
 }
 
 extern "C" int sfh_mlp_forward(sfh_ctx *ctx, int in, int h1, int h2, int out, const float *d_params,
                                const float *d_X, int B, float *d_Y) {
-    if (!ctx || !d_params || !d_X || !d_Y || B < 1 || in < 1 || h1 < 1 || h2 < 1 || out < 1)
-        return SFH_ERR_ARG;
+    if (!ctx || !d_params || !d_X || !d_Y || B < 1 || bad_shape(in, h1, h2, out)) return SFH_ERR_ARG;
     SFH_CK(ctx, cudaSetDevice(ctx->device));
     const MlpShape S = mlp_shape(in, h1, h2, out);
     Work w;
-    int rc = make_work(ctx, w, S, B, false);
+    int rc = make_work(ctx, w, S, 1, B, false);
     if (rc) return rc;
-    rc = forward(ctx, S, d_params, d_X, B, w.a);
-    if (rc) return rc;
+    if ((rc = forward(ctx, S, d_params, 1, d_X, B, w.a))) return rc;
     SFH_CK(ctx, cudaMemcpyAsync(d_Y, w.a.Y, (size_t)B * out * sizeof(float), cudaMemcpyDeviceToDevice,
                                 ctx->stream));
     SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
     return SFH_OK;
 }
 
+extern "C" int sfh_mlp_forward_rows(sfh_ctx *ctx, int in, int h1, int h2, int out,
+                                    const float *d_params, int64_t ngroups, const float *d_X,
+                                    const int32_t *d_group, int64_t B, float *d_Y) {
+    if (!ctx || !d_params || !d_X || !d_Y || B < 1 || B > INT32_MAX || ngroups < 1 ||
+        bad_shape(in, h1, h2, out) || (ngroups > 1 && !d_group))
+        return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    const MlpShape S = mlp_shape(in, h1, h2, out);
+    const size_t smem = (size_t)(in + h1 + h2) * sizeof(float);
+    k_mlp_rows<<<(unsigned)B, 256, smem, ctx->stream>>>(d_params, S.n, ngroups, S, d_X, d_group,
+                                                        d_Y);
+    SFH_LAUNCHED(ctx);
+    return SFH_OK;
+}
+
 extern "C" int sfh_mlp_loss_grad(sfh_ctx *ctx, int in, int h1, int h2, int out,
                                  const float *d_params, const float *d_X, const float *d_T, int B,
                                  float *d_grad, float *d_loss) {
-    if (!ctx || !d_params || !d_X || !d_T || !d_grad || B < 1 || in < 1 || h1 < 1 || h2 < 1 ||
-        out < 1)
+    if (!ctx || !d_params || !d_X || !d_T || !d_grad || B < 1 || bad_shape(in, h1, h2, out))
         return SFH_ERR_ARG;
     SFH_CK(ctx, cudaSetDevice(ctx->device));
     const MlpShape S = mlp_shape(in, h1, h2, out);
     Work w;
-    int rc = make_work(ctx, w, S, B, false);
+    int rc = make_work(ctx, w, S, 1, B, false);
     if (rc) return rc;
-    rc = loss_grad(ctx, S, d_params, d_X, d_T, B, w, d_grad, d_loss);
-    if (rc) return rc;
+    if ((rc = loss_grad(ctx, S, d_params, 1, d_X, d_T, B, w, d_grad, d_loss))) return rc;
     SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
     return SFH_OK;
 }
@@ -408,30 +563,31 @@ extern "C" int sfh_mlp_train(sfh_ctx *ctx, int in, int h1, int h2, int out, floa
                              const float *d_T, int64_t nsamples, int batch, int64_t nsteps,
                              float lr, uint64_t seed, float *d_loss_trace) {
     if (!ctx || !d_params || !d_adam_m || !d_adam_v || !d_X || !d_T || nsamples < 1 || batch < 1 ||
-        nsteps < 0 || !(lr > 0) || in < 1 || h1 < 1 || h2 < 1 || out < 1)
+        batch > 65535 || nsteps < 0 || !(lr > 0) || bad_shape(in, h1, h2, out))
         return SFH_ERR_ARG;
     SFH_CK(ctx, cudaSetDevice(ctx->device));
-    const MlpShape S = mlp_shape(in, h1, h2, out);
-    Work w;
-    int rc0 = make_work(ctx, w, S, batch, true);
-    if (rc0) return rc0;
-    float *Xb = w.Xb, *Tb = w.Tb, *Gr = w.Gr;
-    cudaStream_t st = ctx->stream;
-    const float b1 = 0.9f, b2 = 0.999f;
-    for (int64_t it = 0; it < nsteps; ++it) {
-        const int64_t step = step0 + it + 1;
-        k_gather<<<batch, 64, 0, st>>>(d_X, d_T, nsamples, in, out, batch, seed, step, Xb, Tb);
-        SFH_LAUNCHED(ctx);
-        int rc = loss_grad(ctx, S, d_params, Xb, Tb, batch, w, Gr,
-                           d_loss_trace ? d_loss_trace + it : nullptr);
-        if (rc) return rc;
-        const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
-        k_adam<<<(unsigned)((S.n + 255) / 256), 256, 0, st>>>(d_params, Gr, d_adam_m, d_adam_v, S.n,
-                                                             lr, b1, b2, 1e-8f, c1, c2);
-        SFH_LAUNCHED(ctx);
-    }
-    SFH_CK(ctx, cudaStreamSynchronize(st));
-    return SFH_OK;
+    return train(ctx, mlp_shape(in, h1, h2, out), 1, d_params, d_adam_m, d_adam_v, step0, d_X, d_T,
+                 nsamples, nullptr, batch, nsteps, lr, seed, d_loss_trace);
+}
+
+extern "C" int sfh_mlp_train_grouped(sfh_ctx *ctx, int in, int h1, int h2, int out,
+                                     int64_t ngroups, float *d_params, float *d_adam_m,
+                                     float *d_adam_v, int64_t step0, const float *d_X,
+                                     const float *d_T, const int64_t *h_group_off,
+                                     int batch_per_group, int64_t nsteps, float lr,
+                                     uint64_t seed, float *d_loss_trace) {
+    if (!ctx || !d_params || !d_adam_m || !d_adam_v || !d_X || !d_T || !h_group_off ||
+        ngroups < 1 || ngroups > 65535 || batch_per_group < 1 || batch_per_group > 65535 ||
+        nsteps < 0 || !(lr > 0) || bad_shape(in, h1, h2, out))
+        return SFH_ERR_ARG;
+    if (h_group_off[0] != 0) return sfh_set_error(ctx, SFH_ERR_ARG, "group offsets must start at 0");
+    for (int64_t g = 0; g < ngroups; ++g)
+        if (h_group_off[g + 1] <= h_group_off[g])
+            return sfh_set_error(ctx, SFH_ERR_ARG, "every group needs at least one sample");
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    return train(ctx, mlp_shape(in, h1, h2, out), (int)ngroups, d_params, d_adam_m, d_adam_v,
+                 step0, d_X, d_T, h_group_off[ngroups], h_group_off, batch_per_group, nsteps, lr,
+                 seed, d_loss_trace);
 }
 
 extern "C" int sfh_gemm_f32(sfh_ctx *ctx, const float *d_A, const float *d_B, float *d_C, int64_t M,
@@ -452,7 +608,7 @@ extern "C" int sfh_emu_prepare(sfh_ctx *ctx, float *d_Y, int64_t rows, int64_t c
     const unsigned nb = (unsigned)((n + 255) / 256);
     k_transform<<<nb, 256, 0, ctx->stream>>>(d_Y, n, mode);
     SFH_LAUNCHED(ctx);
-    k_colsum<<<(unsigned)((cols + 255) / 256), 256, 0, ctx->stream>>>(d_Y, rows, cols, d_mean,
+    k_colsum<<<(unsigned)((cols + 255) / 256), 256, 0, ctx->stream>>>(d_Y, rows, cols, 1, d_mean, 0,
                                                                      1.0f / (float)rows);
     SFH_LAUNCHED(ctx);
     k_center<<<nb, 256, 0, ctx->stream>>>(d_Y, rows, cols, d_mean);
@@ -471,6 +627,21 @@ extern "C" int sfh_emu_reconstruct(sfh_ctx *ctx, const float *d_coef, const floa
     if (rc) return rc;
     k_finish<<<(unsigned)((B * nbins + 255) / 256), 256, 0, ctx->stream>>>(d_out, B, nbins, d_offset,
                                                                            mode);
+    SFH_LAUNCHED(ctx);
+    return SFH_OK;
+}
+
+extern "C" int sfh_emu_reconstruct_rows(sfh_ctx *ctx, const float *d_coef, const int32_t *d_group,
+                                        int64_t ngroups, const float *d_basis,
+                                        const float *d_offset, int K, int64_t nbins, int64_t B,
+                                        int mode, float *d_out) {
+    if (!ctx || !d_coef || !d_basis || !d_offset || !d_out || K < 1 || K > 4096 || nbins < 1 ||
+        B < 1 || B > 65535 || ngroups < 1 || (ngroups > 1 && !d_group) || (mode != 0 && mode != 1))
+        return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    dim3 grid((unsigned)((nbins + 255) / 256), (unsigned)B);
+    k_recon_rows<<<grid, 256, (size_t)K * sizeof(float), ctx->stream>>>(
+        d_coef, d_group, ngroups, d_basis, d_offset, K, nbins, mode, d_out);
     SFH_LAUNCHED(ctx);
     return SFH_OK;
 }

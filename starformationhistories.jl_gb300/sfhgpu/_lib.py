@@ -29,8 +29,9 @@ EXPORTED = [
     "sfh_partial_cmd_smooth_batch_dev", "sfh_partial_cmd_smooth_ragged_dev",
     "sfh_galaxies_create", "sfh_galaxies_free", "sfh_galaxies_info", "sfh_fg_ragged_dev",
     "sfh_mlp_param_count", "sfh_mlp_forward",
-    "sfh_mlp_loss_grad", "sfh_mlp_train", "sfh_gemm_f32", "sfh_emu_prepare",
-    "sfh_emu_reconstruct", "sfh_poisson_deviance",
+    "sfh_mlp_loss_grad", "sfh_mlp_train", "sfh_mlp_train_grouped", "sfh_mlp_forward_rows",
+    "sfh_gemm_f32", "sfh_emu_prepare", "sfh_emu_reconstruct", "sfh_emu_reconstruct_rows",
+    "sfh_poisson_deviance",
 ]
 
 
@@ -133,6 +134,13 @@ def load(path: str | None = None):
             "sfh_mlp_train": ([_vp] + [C.c_int] * 4 + [_vp, _vp, _vp, _i64, _vp, _vp, _i64,
                                                        C.c_int, _i64, C.c_float, C.c_uint64,
                                                        _vp], C.c_int),
+            "sfh_mlp_train_grouped": ([_vp] + [C.c_int] * 4 + [_i64, _vp, _vp, _vp, _i64, _vp, _vp,
+                                                                _vp, C.c_int, _i64, C.c_float,
+                                                                C.c_uint64, _vp], C.c_int),
+            "sfh_mlp_forward_rows": ([_vp] + [C.c_int] * 4 + [_vp, _i64, _vp, _vp, _i64, _vp],
+                                     C.c_int),
+            "sfh_emu_reconstruct_rows": ([_vp, _vp, _vp, _i64, _vp, _vp, C.c_int, _i64, _i64,
+                                          C.c_int, _vp], C.c_int),
             "sfh_gemm_f32": ([_vp, _vp, _vp, _vp, _i64, _i64, _i64, C.c_int, C.c_int, C.c_int,
                               C.c_float, C.c_int], C.c_int),
             "sfh_emu_prepare": ([_vp, _vp, _i64, _i64, C.c_int, _vp], C.c_int),

@@ -99,8 +99,15 @@ class TemplateEmulator:
 
     def __init__(self, nbins, ncomp=64, hidden=(256, 256),
                  bounds=((6.6, 10.1), (-2.5, 0.3), (24.0, 30.0)), mode=MODE_SQRT,
-                 tol=1e-3, cells=(12, 12, 12), ctx=None):
+                 tol=1e-3, cells=(12, 12, 12), basis_cells=None, ctx=None):
+        """basis_cells=None: one global PCA basis and one MLP.  basis_cells=(na, nm, nd):
+        one basis and one MLP per cell of that grid over theta (local form); the trust
+        map then uses the same cells."""
         self.ctx = ctx or default_context()
+        self.basis_cells = tuple(int(c) for c in basis_cells) if basis_cells else None
+        if self.basis_cells:
+            cells = self.basis_cells
+        self.ngroups = int(np.prod(self.basis_cells)) if self.basis_cells else 1
         self.nbins = int(nbins)
         self.K = int(ncomp)
         self.shape = (3, int(hidden[0]), int(hidden[1]), self.K)
@@ -133,6 +140,29 @@ class TemplateEmulator:
         lo, hi = self.bounds[:, 0], self.bounds[:, 1]
         return (2.0 * (np.asarray(theta, dtype=np.float64) - lo) / (hi - lo) - 1.0)
 
+    def group_of(self, theta):
+        """Cell index of each theta in the basis grid (0 for the global form)."""
+        theta = np.asarray(theta, dtype=np.float64).reshape(-1, 3)
+        if not self.basis_cells:
+            return np.zeros(theta.shape[0], dtype=np.int64)
+        lo, hi = self.bounds[:, 0], self.bounds[:, 1]
+        n = np.asarray(self.basis_cells)
+        idx = np.clip(((theta - lo) / (hi - lo) * n).astype(np.int64), 0, n - 1)
+        return np.ravel_multi_index(idx.T, self.basis_cells)
+
+    def local_inputs(self, theta):
+        """MLP inputs: theta standardised to [-1, 1] over the whole box (global form) or
+        over the theta's own basis cell (local form)."""
+        theta = np.asarray(theta, dtype=np.float64).reshape(-1, 3)
+        if not self.basis_cells:
+            return self.standardize(theta)
+        lo, hi = self.bounds[:, 0], self.bounds[:, 1]
+        n = np.asarray(self.basis_cells)
+        w = (hi - lo) / n
+        idx = np.clip(((theta - lo) / w).astype(np.int64), 0, n - 1)
+        c_lo = lo + idx * w
+        return 2.0 * (theta - c_lo) / w - 1.0
+
     def sample_theta(self, n, rng):
         lo, hi = self.bounds[:, 0], self.bounds[:, 1]
         return lo + (hi - lo) * rng.random((n, 3))
@@ -142,16 +172,20 @@ class TemplateEmulator:
                                   M, N, K, ta, tb, accum, float(alpha), bf16),
               self.ctx.handle, "gemm_f32")
 
-    def init_params(self, seed):
-        """Uniform(+-sqrt(6 / (fan_in + fan_out))) weights (Glorot), zero biases."""
+    def init_params(self, seed, ngroups=1):
+        """Uniform(+-sqrt(6 / (fan_in + fan_out))) weights (Glorot), zero biases; one block
+        per group, back to back."""
         rng = np.random.default_rng(seed)
         i, h1, h2, o = self.shape
-        parts = []
-        for fin, fout in ((i, h1), (h1, h2), (h2, o)):
-            a = np.sqrt(6.0 / (fin + fout))
-            parts += [rng.uniform(-a, a, fout * fin), np.zeros(fout)]
-        p = np.concatenate(parts).astype(np.float32)
-        assert p.size == self.nparams
+        blocks = []
+        for _ in range(ngroups):
+            parts = []
+            for fin, fout in ((i, h1), (h1, h2), (h2, o)):
+                a = np.sqrt(6.0 / (fin + fout))
+                parts += [rng.uniform(-a, a, fout * fin), np.zeros(fout)]
+            blocks.append(np.concatenate(parts))
+        p = np.concatenate(blocks).astype(np.float32)
+        assert p.size == self.nparams * ngroups
         return p
 
     # ------------------------------------------------------------------ PCA
@@ -195,49 +229,39 @@ class TemplateEmulator:
 
     # ------------------------------------------------------------------ training
     def fit(self, generator, n_train=100_000, n_val=4096, steps=20_000, batch=1024, lr=1e-3,
-            lr_final=1e-5, seed=20261203, segments=20, power_iters=3):
-        """Generate n_train exact templates on the device, build the PCA basis, train the
-        MLP (Adam, cosine-decayed from lr to lr_final over `steps` in `segments` calls),
-        then score n_val fresh templates with the judge to build the trust map."""
+            lr_final=1e-5, seed=20261203, segments=20, power_iters=3, batch_per_cell=32):
+        """Generate n_train exact templates on the device, build the PCA basis (global, or
+        one per basis cell), train the MLP(s) (Adam, cosine-decayed from lr to lr_final over
+        `steps` in `segments` calls; global: `batch` rows per step, local: `batch_per_cell`
+        rows per cell per step), then score n_val fresh templates with the judge to build
+        the trust map."""
         torch = _torch()
         L = load()
         rng = np.random.default_rng(seed)
         theta = self.sample_theta(n_train, rng)
+        grp = self.group_of(theta)
+        order = np.argsort(grp, kind="stable")
+        theta, grp = theta[order], grp[order]
+        off = np.searchsorted(grp, np.arange(self.ngroups + 1)).astype(np.int64)
+        if np.any(np.diff(off) < 2):
+            raise ValueError("too few training templates: every basis cell needs at least two")
         t0 = time.perf_counter()
         Y = generator(theta)
         torch.cuda.synchronize(self._dev)
         t_gen = time.perf_counter() - t0
 
         t0 = time.perf_counter()
-        mean = torch.empty(self.nbins, dtype=torch.float32, device=self._dev)
-        check(L.sfh_emu_prepare(self.ctx.handle, Y.data_ptr(), n_train, self.nbins, self.mode,
-                                mean.data_ptr()), self.ctx.handle, "emu_prepare")
-        V, sv = self._pca(Y, n_train, rng, power_iters=power_iters)
-        A = torch.empty((n_train, self.K), dtype=torch.float32, device=self._dev)
-        self._sync_torch()
-        self._gemm(Y, V, A, n_train, self.K, self.nbins, 0, 1)     # A = Y V^T
-        self._sync_ctx()
+        if self.basis_cells:
+            T = self._local_basis(Y, off)
+        else:
+            T = self._global_basis(Y, n_train, rng, power_iters)
         del Y
-        Ah = A.cpu().numpy().astype(np.float64)
-        # one common scale for all components: the MSE is then proportional to the
-        # squared error in sqrt-template space, which is what the deviance judge sees
-        cmu = Ah.mean(0)
-        s = float(np.sqrt(np.mean(Ah.var(0)))) or 1.0
-        csd = np.full(self.K, s)
-        T = torch.as_tensor(((Ah - cmu) / s).astype(np.float32), device=self._dev)
-        X = torch.as_tensor(self.standardize(theta).astype(np.float32), device=self._dev)
-        # fold the standardisation into the basis and the offset
-        Vh = V.cpu().numpy().astype(np.float64)
-        self.basis = torch.as_tensor((csd[:, None] * Vh).astype(np.float32), device=self._dev)
-        self.offset = torch.as_tensor(
-            (mean.cpu().numpy().astype(np.float64) + cmu @ Vh).astype(np.float32),
-            device=self._dev)
-        self.singular_values = sv
+        X = torch.as_tensor(self.local_inputs(theta).astype(np.float32), device=self._dev)
         torch.cuda.synchronize(self._dev)
         t_pca = time.perf_counter() - t0
 
         t0 = time.perf_counter()
-        self.params = torch.as_tensor(self.init_params(seed), device=self._dev)
+        self.params = torch.as_tensor(self.init_params(seed, self.ngroups), device=self._dev)
         m = torch.zeros_like(self.params)
         v = torch.zeros_like(self.params)
         trace = torch.empty(max(steps, 1), dtype=torch.float32, device=self._dev)
@@ -248,10 +272,18 @@ class TemplateEmulator:
             k = min(per, steps - done)
             frac = (done + 0.5 * k) / steps
             lr_k = lr_final + 0.5 * (lr - lr_final) * (1.0 + np.cos(np.pi * frac))
-            check(L.sfh_mlp_train(self.ctx.handle, *self.shape, self.params.data_ptr(),
-                                  m.data_ptr(), v.data_ptr(), done, X.data_ptr(), T.data_ptr(),
-                                  n_train, batch, k, float(lr_k), seed,
-                                  trace.data_ptr() + 4 * done), self.ctx.handle, "mlp_train")
+            tp = trace.data_ptr() + 4 * done
+            if self.basis_cells:
+                check(L.sfh_mlp_train_grouped(
+                    self.ctx.handle, *self.shape, self.ngroups, self.params.data_ptr(),
+                    m.data_ptr(), v.data_ptr(), done, X.data_ptr(), T.data_ptr(),
+                    off.ctypes.data, int(batch_per_cell), k, float(lr_k), seed, tp),
+                    self.ctx.handle, "mlp_train_grouped")
+            else:
+                check(L.sfh_mlp_train(self.ctx.handle, *self.shape, self.params.data_ptr(),
+                                      m.data_ptr(), v.data_ptr(), done, X.data_ptr(),
+                                      T.data_ptr(), n_train, batch, k, float(lr_k), seed, tp),
+                      self.ctx.handle, "mlp_train")
             done += k
         t_train = time.perf_counter() - t0
         tr = trace[:steps].cpu().numpy()
@@ -270,30 +302,122 @@ class TemplateEmulator:
             trusted_cell_fraction=float(np.mean(self.trust <= self.tol)), loss_trace=tr)
         return self.report
 
+    def _global_basis(self, Y, n, rng, power_iters):
+        """One basis for all templates (randomized range finder); returns the MLP targets
+        and sets basis / offset with the coefficient scaling folded in."""
+        torch = _torch()
+        L = load()
+        mean = torch.empty(self.nbins, dtype=torch.float32, device=self._dev)
+        check(L.sfh_emu_prepare(self.ctx.handle, Y.data_ptr(), n, self.nbins, self.mode,
+                                mean.data_ptr()), self.ctx.handle, "emu_prepare")
+        V, sv = self._pca(Y, n, rng, power_iters=power_iters)
+        A = torch.empty((n, self.K), dtype=torch.float32, device=self._dev)
+        self._sync_torch()
+        self._gemm(Y, V, A, n, self.K, self.nbins, 0, 1)     # A = Y V^T
+        self._sync_ctx()
+        Ah = A.cpu().numpy().astype(np.float64)
+        # one common scale for all components: the MSE is then proportional to the
+        # squared error in sqrt-template space, which is what the deviance judge sees
+        cmu = Ah.mean(0)
+        s = float(np.sqrt(np.mean(Ah.var(0)))) or 1.0
+        Vh = V.cpu().numpy().astype(np.float64)
+        self.basis = torch.as_tensor((s * Vh).astype(np.float32), device=self._dev)
+        self.offset = torch.as_tensor(
+            (mean.cpu().numpy().astype(np.float64) + cmu @ Vh).astype(np.float32),
+            device=self._dev)
+        self.singular_values = sv
+        return torch.as_tensor(((Ah - cmu) / s).astype(np.float32), device=self._dev)
+
+    def _local_basis(self, Y, off):
+        """One basis per cell from the cell's Gram matrix (n_c x n_c on the device, its
+        eigenproblem on the host): V_c = diag(1/sqrt(l)) U^T Y_c and training coefficients
+        U sqrt(l).  Sets basis (G x K x nbins) and offset (G x nbins)."""
+        torch = _torch()
+        L = load()
+        G, K, nb = self.ngroups, self.K, self.nbins
+        self.basis = torch.zeros((G, K, nb), dtype=torch.float32, device=self._dev)
+        self.offset = torch.empty((G, nb), dtype=torch.float32, device=self._dev)
+        T = np.zeros((int(off[-1]), K), dtype=np.float32)
+        sv = []
+        for g in range(G):
+            a, b = int(off[g]), int(off[g + 1])
+            n = b - a
+            Yg = Y[a:b]
+            mean = self.offset[g]
+            self._sync_torch()
+            check(L.sfh_emu_prepare(self.ctx.handle, Yg.data_ptr(), n, nb, self.mode,
+                                    mean.data_ptr()), self.ctx.handle, "emu_prepare")
+            Gm = torch.empty((n, n), dtype=torch.float32, device=self._dev)
+            self._gemm(Yg, Yg, Gm, n, n, nb, 0, 1)               # Y_c Y_c^T
+            self._sync_ctx()
+            ev, U = np.linalg.eigh(Gm.cpu().numpy().astype(np.float64))
+            ev, U = ev[::-1], U[:, ::-1]
+            k = int(min(K, n - 1, np.sum(ev > ev[0] * 1e-12)))
+            lam = ev[:k]
+            Us = U[:, :k] / np.sqrt(lam)[None, :]
+            Ud = torch.as_tensor(np.ascontiguousarray(Us, dtype=np.float32), device=self._dev)
+            Vg = self.basis[g, :k]
+            self._sync_torch()
+            self._gemm(Ud, Yg, Vg, k, nb, n, 1, 0)                # diag(1/sqrt l) U^T Y_c
+            A = U[:, :k] * np.sqrt(lam)[None, :]                  # = Y_c V_c^T
+            s = float(np.sqrt(np.mean(A.var(0)))) or 1.0
+            cmu = A.mean(0)
+            T[a:b, :k] = (A - cmu) / s
+            self._sync_ctx()
+            Vh = Vg.cpu().numpy().astype(np.float64)
+            mean_h = mean.cpu().numpy().astype(np.float64)
+            self.offset[g] = torch.as_tensor((mean_h + cmu @ Vh).astype(np.float32),
+                                             device=self._dev)
+            Vg.mul_(s)
+            sv.append(np.sqrt(lam))
+        self.singular_values = sv
+        torch.cuda.synchronize(self._dev)
+        return torch.as_tensor(T, device=self._dev)
+
     # ------------------------------------------------------------------ inference
     def coefficients(self, theta):
-        """Scaled PCA coefficients predicted by the MLP (device, B x K)."""
+        """Scaled PCA coefficients predicted by the MLP(s) (device, B x K)."""
         torch = _torch()
-        X = torch.as_tensor(self.standardize(theta).reshape(-1, 3).astype(np.float32),
-                            device=self._dev)
+        theta = np.asarray(theta, dtype=np.float64).reshape(-1, 3)
+        X = torch.as_tensor(self.local_inputs(theta).astype(np.float32), device=self._dev)
         B = X.shape[0]
         Yc = torch.empty((B, self.K), dtype=torch.float32, device=self._dev)
+        grp = torch.as_tensor(self.group_of(theta).astype(np.int32), device=self._dev)
         self._sync_torch()
-        check(load().sfh_mlp_forward(self.ctx.handle, *self.shape, self.params.data_ptr(),
-                                     X.data_ptr(), B, Yc.data_ptr()), self.ctx.handle,
-              "mlp_forward")
+        if self.basis_cells:
+            check(load().sfh_mlp_forward_rows(self.ctx.handle, *self.shape,
+                                              self.params.data_ptr(), self.ngroups,
+                                              X.data_ptr(), grp.data_ptr(), B, Yc.data_ptr()),
+                  self.ctx.handle, "mlp_forward_rows")
+            self._sync_ctx()
+        else:
+            check(load().sfh_mlp_forward(self.ctx.handle, *self.shape, self.params.data_ptr(),
+                                         X.data_ptr(), B, Yc.data_ptr()), self.ctx.handle,
+                  "mlp_forward")
         return Yc
 
     def predict(self, theta, out=None):
         """Emulated templates (device float32, B x nbins)."""
         torch = _torch()
+        theta = np.asarray(theta, dtype=np.float64).reshape(-1, 3)
         coef = self.coefficients(theta)
         B = coef.shape[0]
         if out is None:
             out = torch.empty((B, self.nbins), dtype=torch.float32, device=self._dev)
-        check(load().sfh_emu_reconstruct(self.ctx.handle, coef.data_ptr(), self.basis.data_ptr(),
-                                         self.offset.data_ptr(), self.K, self.nbins, B, self.mode,
-                                         out.data_ptr()), self.ctx.handle, "emu_reconstruct")
+        L = load()
+        if self.basis_cells:
+            grp = torch.as_tensor(self.group_of(theta).astype(np.int32), device=self._dev)
+            self._sync_torch()
+            for s0 in range(0, B, 65535):
+                e = min(B, s0 + 65535)
+                check(L.sfh_emu_reconstruct_rows(
+                    self.ctx.handle, coef[s0:e].data_ptr(), grp[s0:e].data_ptr(), self.ngroups,
+                    self.basis.data_ptr(), self.offset.data_ptr(), self.K, self.nbins, e - s0,
+                    self.mode, out[s0:e].data_ptr()), self.ctx.handle, "emu_reconstruct_rows")
+        else:
+            check(L.sfh_emu_reconstruct(self.ctx.handle, coef.data_ptr(), self.basis.data_ptr(),
+                                        self.offset.data_ptr(), self.K, self.nbins, B, self.mode,
+                                        out.data_ptr()), self.ctx.handle, "emu_reconstruct")
         self._sync_ctx()
         return out
 

@@ -217,12 +217,14 @@ def bin_cmd_smooth(colors, mags, color_err, mag_err, cov_mult=0, weights=None, e
     return Histogram(e, out.reshape(ny, nx).T)
 
 
-def partial_cmd_smooth(m_ini, mags, mag_err_funcs, y_index, color_indices, imf,
-                       completeness_funcs=None, bias_funcs=None, dmod=0.0, normalize_value=1.0,
-                       mean_mass=None, edges=None, xlim=None, ylim=None, nbins=None, xwidth=None,
-                       ywidth=None, ctx=None):
-    """partial_cmd_smooth (single stars), src/StarFormationHistories.jl:829-888.
-    y_index / color_indices are 0-based.  Callables act on numpy arrays."""
+def partial_cmd_smooth_stars(m_ini, mags, mag_err_funcs, y_index, color_indices, imf,
+                             completeness_funcs=None, bias_funcs=None, dmod=0.0,
+                             normalize_value=1.0, mean_mass=None, edges=None, xlim=None,
+                             ylim=None, nbins=None, xwidth=None, ywidth=None):
+    """The star list partial_cmd_smooth hands to bin_cmd_smooth
+    (src/StarFormationHistories.jl:829-888): (colors, mags, color_err, mag_err, weights,
+    cov_mult, edges) after mini_spacing, interpolation, the callables, the weights, the
+    bias and midpoints.  y_index / color_indices are 0-based; callables act on arrays."""
     if len(color_indices) != 2:
         raise ValueError("length(color_indices) == 2")
     nf = len(mags)
@@ -254,8 +256,42 @@ def partial_cmd_smooth(m_ini, mags, mag_err_funcs, y_index, color_indices, imf,
     w = calculate_weights(new_mini, compl, imf, normalize_value, mean_mass, spacing)
     biased = [iso[i] + bias_funcs[i](iso[i]) for i in range(nf)]
     col = biased[c1] - biased[c2]
-    return bin_cmd_smooth(midpoints(col), midpoints(biased[y_index]), midpoints(color_err),
-                          midpoints(err[y_index]), cov_mult, weights=w, edges=e, ctx=ctx)
+    return (midpoints(col), midpoints(biased[y_index]), midpoints(color_err),
+            midpoints(err[y_index]), w, cov_mult, e)
+
+
+def partial_cmd_smooth(m_ini, mags, mag_err_funcs, y_index, color_indices, imf,
+                       completeness_funcs=None, bias_funcs=None, dmod=0.0, normalize_value=1.0,
+                       mean_mass=None, edges=None, xlim=None, ylim=None, nbins=None, xwidth=None,
+                       ywidth=None, ctx=None):
+    """partial_cmd_smooth (single stars), src/StarFormationHistories.jl:829-888.
+    y_index / color_indices are 0-based.  Callables act on numpy arrays."""
+    x, y, sx, sy, w, cov_mult, e = partial_cmd_smooth_stars(
+        m_ini, mags, mag_err_funcs, y_index, color_indices, imf, completeness_funcs, bias_funcs,
+        dmod, normalize_value, mean_mass, edges, xlim, ylim, nbins, xwidth, ywidth)
+    return bin_cmd_smooth(x, y, sx, sy, cov_mult, weights=w, edges=e, ctx=ctx)
+
+
+def stamp_bin_updates(x, y, sx, sy, cov_mult, edges):
+    """Bins each star's stamp adds to: the window of GaussianPSFAsymmetric
+    (size (ceil 10σx, ceil 10σy) in pixels, offsets max(1, size ÷ 2),
+    StarFormationHistories.jl:247, 348-364) or GaussianPSFCovariant (half widths
+    max(1, round(15σx/Δx/2)), max(1, round(10σy/Δy/2)), :293, 366-408) around the
+    ties-to-even rounded centre, clipped to the grid; stars whose clipped window is not
+    longer than one bin on both axes add nothing.  The unit of the template build's work."""
+    (xf, xs, nx), (yf, ys, ny) = _range(edges[0]), _range(edges[1])
+    x, y, sx, sy = (np.asarray(a, dtype=np.float64) for a in (x, y, sx, sy))
+    xc = np.rint((x - xf) / xs + 1.0)
+    yc = np.rint((y - yf) / ys + 1.0)
+    if cov_mult == 0:
+        xoff = np.maximum(1, np.floor(np.ceil(10.0 * sx / xs) / 2))
+        yoff = np.maximum(1, np.floor(np.ceil(10.0 * sy / ys) / 2))
+    else:
+        xoff = np.maximum(1, np.rint(15.0 * sx / xs / 2.0))
+        yoff = np.maximum(1, np.rint(10.0 * sy / ys / 2.0))
+    lx = np.minimum(nx, xc + xoff) - np.maximum(1, xc - xoff) + 1
+    ly = np.minimum(ny, yc + yoff) - np.maximum(1, yc - yoff) + 1
+    return np.where((lx > 1) & (ly > 1), lx * ly, 0).astype(np.int64)
 
 
 def err_model(a, b, c, d, cap=np.inf) -> ErrModel:

@@ -112,8 +112,10 @@ def test_adam_steps_match_numpy(torch, L, ctx, O):
     p = P.astype(np.float64)
     m = np.zeros_like(p)
     v = np.zeros_like(p)
+    g1 = None
     for step in range(1, 4):
         _, g = O.mlp_loss_grad(SHAPE, p.astype(np.float32), X, T, bf16=True)
+        g1 = g if g1 is None else g1
         m = b1 * m + (1 - b1) * g
         v = b2 * v + (1 - b2) * g * g
         p = p - lr * (m / (1 - b1 ** step)) / (np.sqrt(v / (1 - b2 ** step)) + eps)
@@ -124,8 +126,11 @@ def test_adam_steps_match_numpy(torch, L, ctx, O):
     assert L.sfh_mlp_train(ctx.handle, *SHAPE, dP.data_ptr(), dm.data_ptr(), dv.data_ptr(), 0,
                            dX.data_ptr(), dT.data_ptr(), 1, 16, 3, lr, 99, trace.data_ptr()) == 0
     got = dP.cpu().numpy()
-    # Adam normalises each coordinate, so steps are ~lr regardless of |g|
-    assert np.abs(got - p).max() <= 0.05 * lr
+    # Adam normalises each coordinate, so steps are ~lr regardless of |g|; where a
+    # gradient component is ~0 its FP32 sign is noise and the step may go either way
+    live = np.abs(g1) > 1e-4 * np.abs(g1).max()
+    assert np.abs(got - p)[live].max() <= 0.05 * lr
+    assert np.abs(got - p).max() <= 6.5 * lr
     assert np.all(np.diff(trace.cpu().numpy()) < 0)
 
 
@@ -268,3 +273,141 @@ def test_routing_falls_back_to_exact_templates(trained, torch):
     nb = np.nonzero(~used2)[0]
     if nb.size:
         assert same(out2[nb], exact[nb])
+
+
+# ---------------------------------------------------------------- grouped (local-basis) form
+
+def test_mlp_forward_rows_matches_oracle(torch, L, ctx, O):
+    rng = np.random.default_rng(21)
+    G, B = 3, 40
+    n = O.mlp_param_count(SHAPE)
+    P = (rng.standard_normal((G, n)) * 0.3).astype(np.float32)
+    X = rng.uniform(-1, 1, (B, 3)).astype(np.float32)
+    grp = rng.integers(0, G, B).astype(np.int32)
+    Y = torch.empty((B, SHAPE[3]), dtype=torch.float32, device="cuda:0")
+    dP, dX, dg = _dev(torch, P), _dev(torch, X), _dev(torch, grp, np.int32)
+    torch.cuda.synchronize()
+    assert L.sfh_mlp_forward_rows(ctx.handle, *SHAPE, dP.data_ptr(), G, dX.data_ptr(),
+                                  dg.data_ptr(), B, Y.data_ptr()) == 0
+    _sync(L, ctx)
+    got = Y.cpu().numpy()
+    ref = np.stack([O.mlp_forward(SHAPE, P[grp[b]], X[b:b + 1], bf16=True)[0] for b in range(B)])
+    assert np.abs(got - ref).max() <= 2e-3 * np.abs(ref).max()
+    assert np.median(np.abs(got - ref)) <= 1e-5 * np.abs(ref).max()
+    # one group: the row kernel and the GEMM path agree
+    Y1 = torch.empty((B, SHAPE[3]), dtype=torch.float32, device="cuda:0")
+    assert L.sfh_mlp_forward_rows(ctx.handle, *SHAPE, dP.data_ptr(), 1, dX.data_ptr(), None, B,
+                                  Y1.data_ptr()) == 0
+    Y2 = torch.empty_like(Y1)
+    assert L.sfh_mlp_forward(ctx.handle, *SHAPE, dP.data_ptr(), dX.data_ptr(), B,
+                             Y2.data_ptr()) == 0
+    _sync(L, ctx)
+    assert torch.allclose(Y1, Y2, rtol=1e-5, atol=1e-6)
+
+
+def test_grouped_adam_matches_numpy(torch, L, ctx, O):
+    """Two groups with one sample each: every minibatch row of a group is its sample, so
+    each group's update is the oracle gradient + Adam (the loss is averaged over groups,
+    which Adam's per-coordinate normalisation ignores)."""
+    rng = np.random.default_rng(22)
+    G = 2
+    n = O.mlp_param_count(SHAPE)
+    P = (rng.standard_normal((G, n)) * 0.3).astype(np.float32)
+    X = rng.uniform(-1, 1, (G, 3)).astype(np.float32)
+    T = rng.standard_normal((G, SHAPE[3])).astype(np.float32)
+    lr = 3e-3
+    ref, live = [], []
+    for g in range(G):
+        p = P[g].astype(np.float64)
+        m = np.zeros_like(p)
+        v = np.zeros_like(p)
+        for step in range(1, 4):
+            _, gr = O.mlp_loss_grad(SHAPE, p.astype(np.float32), X[g:g + 1], T[g:g + 1], True)
+            if step == 1:
+                live.append(np.abs(gr) > 1e-4 * np.abs(gr).max())
+            m = 0.9 * m + 0.1 * gr
+            v = 0.999 * v + 0.001 * gr * gr
+            p = p - lr * (m / (1 - 0.9 ** step)) / (np.sqrt(v / (1 - 0.999 ** step)) + 1e-8)
+        ref.append(p)
+    dP, dX, dT = _dev(torch, P), _dev(torch, X), _dev(torch, T)
+    dm, dv = torch.zeros_like(dP), torch.zeros_like(dP)
+    off = np.array([0, 1, 2], dtype=np.int64)
+    torch.cuda.synchronize()
+    assert L.sfh_mlp_train_grouped(ctx.handle, *SHAPE, G, dP.data_ptr(), dm.data_ptr(),
+                                   dv.data_ptr(), 0, dX.data_ptr(), dT.data_ptr(), off.ctypes.data,
+                                   8, 3, lr, 5, None) == 0
+    got = dP.cpu().numpy()
+    for g in range(G):
+        # near-zero gradient components: FP32 sign noise, see test_adam_steps_match_numpy
+        assert np.abs(got[g] - ref[g])[live[g]].max() <= 0.05 * lr
+        assert np.abs(got[g] - ref[g]).max() <= 6.5 * lr
+    # every group must own at least one sample
+    bad = np.array([0, 1, 1], dtype=np.int64)
+    assert L.sfh_mlp_train_grouped(ctx.handle, *SHAPE, G, dP.data_ptr(), dm.data_ptr(),
+                                   dv.data_ptr(), 0, dX.data_ptr(), dT.data_ptr(), bad.ctypes.data,
+                                   8, 1, lr, 5, None) != 0
+
+
+def test_reconstruct_rows_matches_numpy(torch, L, ctx):
+    rng = np.random.default_rng(23)
+    G, K, nb, B = 4, 5, 777, 33
+    coef = rng.standard_normal((B, K)).astype(np.float32)
+    basis = (rng.standard_normal((G, K, nb)) * 0.1).astype(np.float32)
+    off = (rng.standard_normal((G, nb)) * 0.3).astype(np.float32)
+    grp = rng.integers(0, G, B).astype(np.int32)
+    out = torch.empty((B, nb), dtype=torch.float32, device="cuda:0")
+    d = [_dev(torch, a) for a in (coef, basis, off)]
+    dg = _dev(torch, grp, np.int32)
+    torch.cuda.synchronize()
+    for mode in (0, 1):
+        assert L.sfh_emu_reconstruct_rows(ctx.handle, d[0].data_ptr(), dg.data_ptr(), G,
+                                          d[1].data_ptr(), d[2].data_ptr(), K, nb, B, mode,
+                                          out.data_ptr()) == 0
+        _sync(L, ctx)
+        y = np.maximum(off[grp] + np.einsum("bk,bki->bi", coef.astype(np.float64), basis[grp]), 0)
+        ref = y * y if mode == 1 else y
+        assert np.allclose(out.cpu().numpy(), ref, rtol=2e-5, atol=1e-6)
+
+
+@pytest.fixture(scope="module")
+def trained_local(torch, sfh, ctx):
+    from sfhgpu import emulator as E
+    xe, ye = np.linspace(-0.6, 2.4, 41), np.linspace(19.0, 30.0, 51)
+    gen = E.SyntheticGenerator(xe, ye, n_iso=200)
+    em = E.TemplateEmulator(gen.nbins, ncomp=64, hidden=(256, 256), tol=1e-2,
+                            basis_cells=(2, 2, 4), ctx=ctx)
+    rep = em.fit(gen, n_train=8192, n_val=2048, steps=3000, lr=1e-3, seed=3, batch_per_cell=64)
+    return em, gen, rep
+
+
+def test_local_bases_beat_the_global_basis(trained, trained_local, torch):
+    """Per-cell bases and networks follow features that move with theta better than one
+    global basis: lower median deviance per star on the same held-out templates."""
+    em_g, gen, _ = trained
+    em_l, _, rep = trained_local
+    assert np.all(np.isfinite(rep.loss_trace))
+    rng = np.random.default_rng(99)
+    th = em_g.sample_theta(1024, rng)
+    exact = gen(th)
+    d_g = em_g.judge(exact, em_g.predict(th))
+    d_l = em_l.judge(exact, em_l.predict(th))
+    assert np.median(d_l) < 0.5 * np.median(d_g)
+    # and the local networks beat the local mean templates (no network)
+    grp = torch.as_tensor(em_l.group_of(th), device=exact.device)
+    y = em_l.offset[grp].clamp_min(0)
+    d_mean = em_l.judge(exact, (y * y).contiguous())
+    assert np.median(d_l) < 0.2 * np.median(d_mean)
+
+
+def test_local_routing_falls_back_to_exact_templates(trained_local, torch):
+    em, gen, _ = trained_local
+    rng = np.random.default_rng(18)
+    th = em.sample_theta(200, rng)
+    out, used = em.templates(th, gen, audit=True)
+    exact = gen(th)
+    d = em.judge(exact, em.predict(th))
+    assert np.array_equal(used, d <= em.tol)
+    bad = np.nonzero(~used)[0]
+    if bad.size:
+        assert bool(((out[bad] - exact[bad]).abs()
+                     <= 1e-6 * exact[bad].abs() + 1e-7 * exact[bad].abs().amax()).all())
