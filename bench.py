@@ -141,7 +141,6 @@ def run_batched(ctx, d_T, nbins, nt, r, data, M64, steps, warmup, B=4096, check=
     import numpy as np
     import torch
 
-    import oracle as O
     import sfhgpu
     L = sfhgpu.load()
     dev = torch.device("cuda", ctx.device)
@@ -166,16 +165,8 @@ def run_batched(ctx, d_T, nbins, nt, r, data, M64, steps, warmup, B=4096, check=
     e1.synchronize()
     ms = e0.elapsed_time(e1) / steps
     negL = d_L.cpu().numpy()
-    # accuracy against the FP64 oracle on a few vectors (stored hi+lo values, and FP32 templates)
-    Mt = torch.tensor(M64)
-    hi = Mt.float().to(torch.bfloat16).double()
-    Ms = np.asfortranarray((hi + (Mt - hi).float().to(torch.bfloat16).double()).numpy())
-    Rt = torch.tensor(R[:check])
-    rh = Rt.float().to(torch.bfloat16).double()
-    Rs = (rh + (Rt - rh).float().to(torch.bfloat16).double()).numpy()
-    O.set_threads(os.cpu_count() or 1)
-    ref_s, _ = O.fg_batched(Rs, Ms, data, nthreads=os.cpu_count() or 1, want_g=False)
-    ref_f, _ = O.fg_batched(R[:check], M64, data, nthreads=os.cpu_count() or 1, want_g=False)
+    # outputs for the accuracy check against the FP64 oracle, done in the CPU leg
+    check_data = {"R": R[:check], "negL": negL[:check]}
     nst = float(data.sum())
     flops = 4.0 * nbins * nt * B  # two GEMMs, algorithmic (the hi/lo split triples tensor work)
     peak, kind = _bf16_peak()
@@ -187,9 +178,7 @@ def run_batched(ctx, d_T, nbins, nt, r, data, M64, steps, warmup, B=4096, check=
                             "achieved_with_hilo": 3 * flops / (ms / 1e3) / 1e12, "peak": peak,
                             "unit": "TFLOP/s", "frac": 3 * flops / (ms / 1e3) / 1e12 / peak,
                             "peak_source": kind},
-        "dlogL_per_1e4_stars_vs_stored": float(np.max(np.abs(negL[:check] - ref_s)) / (nst / 1e4)),
-        "dlogL_per_1e4_stars_vs_fp32_templates": float(
-            np.max(np.abs(negL[:check] - ref_f)) / (nst / 1e4)),
+        "_check": check_data,
     }
 
 
@@ -249,7 +238,6 @@ def run_ragged(ctx, steps=50, warmup=5, check=2):
     import numpy as np
     import torch
 
-    import oracle as O
     import sfhgpu
     from sfhgpu import synthetic as S
     dev = torch.device("cuda", ctx.device)
@@ -300,18 +288,17 @@ def run_ragged(ctx, steps=50, warmup=5, check=2):
     e1.record(ts)
     e1.synchronize()
     ms = e0.elapsed_time(e1) / steps
+    # outputs of the largest galaxies for the accuracy check against the FP64 oracle,
+    # done in the CPU leg
     negL, G = d_L.cpu().numpy(), d_G.cpu().numpy()
-    M = out.cpu().numpy()
-    err_l, err_g = 0.0, 0.0
-    for g in np.argsort(-nb)[:check]:  # the largest galaxies
+    check_data = []
+    for g in np.argsort(-nb)[:check]:
         mo = int(sum(nb[:g] * nt[:g]))
-        Mg = M[mo:mo + nb[g] * nt[g]].reshape(nt[g], nb[g]).T.astype(np.float64)
         b0, b1 = gal.bin_offsets[g], gal.bin_offsets[g + 1]
         t0_, t1_ = gal.templ_offsets[g], gal.templ_offsets[g + 1]
-        v, Gr, w = O.fg(r[t0_:t1_], np.asfortranarray(Mg), data[b0:b1])
-        err_l = max(err_l, abs(negL[g] - v) / max(1.0, data[b0:b1].sum() / 1e4))
-        err_g = max(err_g, float(np.max(np.abs(G[t0_:t1_] - Gr) /
-                                        (np.abs(Mg).T @ np.abs(w) + 1e-300))))
+        Mg = out[mo:mo + int(nb[g] * nt[g])].cpu().numpy().reshape(int(nt[g]), int(nb[g])).T
+        check_data.append((Mg, r[t0_:t1_].copy(), data[b0:b1].copy(), float(negL[g]),
+                           G[t0_:t1_].copy()))
     # galaxies with <= 32 templates take the fused pass (M read once); larger ones read
     # M twice (composite pass, then the gradient pass)
     reads = np.where(nt <= 32, 1, 2)
@@ -328,7 +315,7 @@ def run_ragged(ctx, steps=50, warmup=5, check=2):
         "roofline": {"bound": "hbm", "achieved": alg_bytes / (ms * 1e-3) / 1e9, "peak": peak,
                      "unit": "GB/s", "frac": alg_bytes / (ms * 1e-3) / 1e9 / peak,
                      "peak_source": kind, "algorithmic_bytes_per_call": alg_bytes},
-        "dlogL_per_1e4_stars_vs_oracle": err_l, "grad_err_rel_scale_vs_oracle": err_g,
+        "_check": check_data,
     }
 
 
@@ -380,6 +367,47 @@ def run_emulator(ctx, w, n_train=65536, n_val=4096, steps=4000, cells=(8, 2, 16)
         "routed_templates_per_s": nreq / t_routed,
         "routed_speedup_vs_exact": t_exact / t_routed,
     }
+
+
+def oracle_checks(batched, ragged, M64, r, data, neglogl):
+    """Accuracy against the FP64 oracle on the same stored templates (CPU leg): the plain
+    fg!'s -logL, and the stashed outputs of the batched and ragged legs (the stash is
+    removed).  Returns the plain path's figures."""
+    import numpy as np
+    import torch
+
+    import oracle as O
+    thr = os.cpu_count() or 1
+    O.set_threads(thr)
+    nst = float(data.sum())
+    v_ref, _, _ = O.fg(r, M64, data)
+    plain = {"dlogL_per_1e4_stars_vs_oracle": abs(neglogl - v_ref) / (nst / 1e4),
+             "negLogL_oracle": v_ref}
+    if batched and "_check" in batched:
+        c = batched.pop("_check")
+        Mt = torch.tensor(M64)
+        hi = Mt.float().to(torch.bfloat16).double()
+        Ms = np.asfortranarray((hi + (Mt - hi).float().to(torch.bfloat16).double()).numpy())
+        Rt = torch.tensor(c["R"])
+        rh = Rt.float().to(torch.bfloat16).double()
+        Rs = (rh + (Rt - rh).float().to(torch.bfloat16).double()).numpy()
+        ref_s, _ = O.fg_batched(Rs, Ms, data, nthreads=thr, want_g=False)
+        ref_f, _ = O.fg_batched(c["R"], M64, data, nthreads=thr, want_g=False)
+        batched["dlogL_per_1e4_stars_vs_stored"] = float(
+            np.max(np.abs(c["negL"] - ref_s)) / (nst / 1e4))
+        batched["dlogL_per_1e4_stars_vs_fp32_templates"] = float(
+            np.max(np.abs(c["negL"] - ref_f)) / (nst / 1e4))
+    if ragged and "_check" in ragged:
+        err_l, err_g = 0.0, 0.0
+        for Mg, rg, ng, negl, Gg in ragged.pop("_check"):
+            Mg = np.asfortranarray(Mg, dtype=np.float64)
+            v, Gr, w = O.fg(rg, Mg, ng)
+            err_l = max(err_l, abs(negl - v) / max(1.0, ng.sum() / 1e4))
+            err_g = max(err_g, float(np.max(np.abs(Gg - Gr) /
+                                            (np.abs(Mg).T @ (np.abs(w) + np.abs(1 - w)) + 1e-300))))
+        ragged["dlogL_per_1e4_stars_vs_oracle"] = err_l
+        ragged["grad_err_rel_scale_vs_oracle"] = err_g
+    return plain
 
 
 def cpu_fg_baseline(M64, r, data, budget_s=10.0, threads=None):
@@ -547,6 +575,9 @@ def run_ours(args):
     torch.cuda.synchronize()
     eps = float(np.finfo(np.float64).eps)
 
+    # launch plan picked by the library's autotuner on this matrix and these inputs
+    tuned = H.autotune(r, data, iters=10)
+
     def step():
         rc = L.sfh_fg_dev(ctx.handle, H.handle, d_r.data_ptr(), d_n.data_ptr(), d_c.data_ptr(),
                           d_G.data_ptr(), d_L.data_ptr(), eps)
@@ -597,7 +628,9 @@ def run_ours(args):
                 "unit": "GB/s", "frac": achieved / peak, "traffic": _profile_traffic(names[k]),
                 "peak_source": peak_kind,
                 "kernel_ms": {n: kms[i] for i, n in enumerate(names)},
-                "fg_total_gbs": (alg[0] + alg[2]) / (ms / args.steps * 1e-3) / 1e9}
+                "fg_total_gbs": (alg[0] + alg[2]) / (ms / args.steps * 1e-3) / 1e9,
+                "autotuned_plan": {"pass1_waves": tuned["plan"][0], "pass2_rows": tuned["plan"][1],
+                                   "pass2_waves": tuned["plan"][2], "pass_ms": tuned["ms"]}}
 
     # ---- end to end through the host-array C ABI (sfh_fg)
     comp = np.empty(NBINS)
@@ -639,7 +672,9 @@ def run_ours(args):
 
     # ---- CPU baseline (rank 0, N = 1 only): the oracle on the same inputs
     cpu = None
+    plain_check = None
     if rank == 0 and world == 1 and not args.no_cpu:
+        plain_check = oracle_checks(batched, ragged, M64, r, data, neglogl)
         v, thr, n, dt = cpu_fg_baseline(M64, r, data, budget_s=args.cpu_budget_s)
         tps, nt_done, tdt = cpu_template_baseline(w, budget_s=args.cpu_budget_s)
         cpu = {"value": v, "unit": UNIT, "cores": thr, "kind": "port",
@@ -648,6 +683,9 @@ def run_ours(args):
                "templates_sample": f"{nt_done} partial_cmd_smooth templates in {tdt:.1f} s "
                                    f"(FP64 oracle, 1 thread)"}
 
+    for leg in (batched, ragged):
+        if leg:
+            leg.pop("_check", None)  # unchecked (--no-cpu): no oracle run
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -661,7 +699,8 @@ def run_ours(args):
             "templates_per_s": templates_per_s, "template_build_ms": build_ms,
             "template_bin_updates_per_s": bin_updates / (build_ms / 1e3),
             "template_bin_updates_per_build": bin_updates,
-            "negLogL": neglogl, "gpu_launches": launches, "roofline": roofline,
+            "negLogL": neglogl, "precision": plain_check, "gpu_launches": launches,
+            "roofline": roofline,
             "batched": batched, "hmc": hmc, "ragged": ragged, "emulator": emulator,
             "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
         }

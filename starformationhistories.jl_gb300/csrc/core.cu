@@ -52,11 +52,16 @@ extern "C" int sfh_ctx_create(int device, sfh_ctx **out) {
     sfh_ctx *ctx = new sfh_ctx();
     ctx->device = device;
     ctx->sm_count = prop.multiProcessorCount;
+    sfh_df tab[129];
+    sfh_df_log_table(tab);
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc(&ctx->d_counters, sizeof(unsigned int) * SFH_CNT_SLOTS) != cudaSuccess ||
-        cudaMemset(ctx->d_counters, 0, sizeof(unsigned int) * SFH_CNT_SLOTS) != cudaSuccess) {
+        cudaMemset(ctx->d_counters, 0, sizeof(unsigned int) * SFH_CNT_SLOTS) != cudaSuccess ||
+        cudaMalloc(&ctx->d_df_tab, sizeof(tab)) != cudaSuccess ||
+        cudaMemcpy(ctx->d_df_tab, tab, sizeof(tab), cudaMemcpyHostToDevice) != cudaSuccess) {
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
         if (ctx->d_counters) cudaFree(ctx->d_counters);
+        if (ctx->d_df_tab) cudaFree(ctx->d_df_tab);
         delete ctx;
         return SFH_ERR_CUDA;
     }
@@ -71,6 +76,7 @@ extern "C" int sfh_ctx_destroy(sfh_ctx *ctx) {
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->stage) cudaFree(ctx->stage);
     if (ctx->d_counters) cudaFree(ctx->d_counters);
+    if (ctx->d_df_tab) cudaFree(ctx->d_df_tab);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return SFH_OK;

@@ -373,6 +373,7 @@ struct Pass1Args {
     unsigned int *tile_cnt;
     unsigned int *all_cnt;
     double *negLogL;
+    const sfh_df *tab;  // log table of the double-float Poisson terms
 };
 
 __device__ __forceinline__ void block_sum_to(double v, double *s_red, double *out_tid0) {
@@ -471,7 +472,15 @@ __global__ void __launch_bounds__(kThreads) k_fg_pass1_f32(Pass1Args a) {
     __threadfence();
     const int ks = nsplit;
     const int64_t rbase = (int64_t)tile * blockDim.x * 4;
-    double term = 0.0;
+    __shared__ sfh_df s_tab[129];
+    if (a.want_logl) {
+        for (int k = threadIdx.x; k < 129; k += blockDim.x) s_tab[k] = a.tab[k];
+        __syncthreads();
+    }
+    // Poisson terms in double-float on the FP32 pipes (sfh_dfloat.cuh); eps(T) is a
+    // power of two, exact in FP32.
+    const float eps_f = (float)a.eps;
+    sfh_df term{0.f, 0.f};
     for (int q = 0; q < 4; ++q) {
         const int64_t ii = rbase + (int64_t)q * blockDim.x + threadIdx.x;
         if (ii >= nbins) continue;
@@ -492,24 +501,26 @@ __global__ void __launch_bounds__(kThreads) k_fg_pass1_f32(Pass1Args a) {
             two_sum_acc(mh, ml, v.x);
             ml += v.y;
         }
-        const double m = (double)mh + (double)ml;
+        sfh_df c = df_fast_two_sum(mh, ml);
         if (!a.want_logl && !a.want_w) {  // composite only: data may be NULL
-            a.composite[ii] = m;
+            a.composite[ii] = (double)c.h + (double)c.l;
             continue;
         }
-        const double ci = m > a.eps ? m : a.eps;
+        if (!a.want_w) a.composite[ii] = (double)c.h + (double)c.l;  // the model, unclamped
+        if (c.h < eps_f || (c.h == eps_f && c.l < 0.f)) c = sfh_df{eps_f, 0.f};  // max(c, eps)
         const double ni = a.data[ii];
-        if (a.want_logl) term += (ni > 0.0) ? sfh_poisson_term_occupied(ci, ni) : -ci;
+        const float nh = __double2float_rn(ni);
+        const float nl = __double2float_rn(ni - (double)nh);
+        if (a.want_logl) term = df_add(term, df_poisson_term(c, nh, nl, s_tab));
         if (a.want_w) {
-            const float w = __fdiv_rn((float)(ci - ni), (float)ci);  // 1 - n/c
+            const sfh_df diff = df_add(c, sfh_df{-nh, -nl});
+            const float w = __fdiv_rn(diff.h, c.h);  // 1 - n/c
             a.composite[ii] = (double)w;
             a.w32[ii] = make_float2(w, 0.f);
-        } else {
-            a.composite[ii] = m;
         }
     }
     double tile_sum = 0.0;
-    block_sum_to(term, s_red, &tile_sum);
+    block_sum_to((double)term.h + (double)term.l, s_red, &tile_sum);
     if (threadIdx.x == 0) {
         a.tile_cnt[tile] = 0u;  // re-arm for the next launch on this stream
         s_last = false;
@@ -665,7 +676,8 @@ FusedOcc fused_occupancy(bool vec) {
     return c;
 }
 
-Plan make_plan(const sfh_ctx *ctx, int64_t nbins, int64_t nt, bool f64, bool fused = false) {
+Plan make_plan(const sfh_ctx *ctx, int64_t nbins, int64_t nt, bool f64, bool fused = false,
+               const sfh_models *m = nullptr) {
     Plan p{};
     const int rows_per_block = f64 ? 2 * kThreads : 4 * kThreads;
     p.nrowblk = (int)((nbins + rows_per_block - 1) / rows_per_block);
@@ -676,13 +688,16 @@ Plan make_plan(const sfh_ctx *ctx, int64_t nbins, int64_t nt, bool f64, bool fus
     int groups = (target + p.nchunks - 1) / p.nchunks;
     if (fused) {
         // Pass 1: two whole waves of resident blocks.  Pass 2: 2,048-row chunks, column
-        // groups of a multiple of 8 (every warp busy) sized to about one wave.
+        // groups of a multiple of 8 (every warp busy) sized to about one wave.  A plan
+        // measured by sfh_models_autotune replaces these choices.
         const FusedOcc occ = fused_occupancy(nbins % 4 == 0);
         const int slots1 = occ.p1 * ctx->sm_count, slots2 = occ.p2 * ctx->sm_count;
-        ks = (2 * slots1 + p.nrowblk / 2) / p.nrowblk;
-        p.R = kFusedR;
+        const int w1 = (m && m->tune_w1 > 0) ? m->tune_w1 : 2;
+        const int w2 = (m && m->tune_w2 > 0) ? m->tune_w2 : 1;
+        ks = (w1 * slots1 + p.nrowblk / 2) / p.nrowblk;
+        p.R = (m && m->tune_R > 0) ? m->tune_R : kFusedR;
         p.nchunks = (int)((nbins + p.R - 1) / p.R);
-        const double per_block = (double)nt * p.nchunks / (double)slots2;
+        const double per_block = (double)nt * p.nchunks / ((double)w2 * slots2);
         const int cb8 = 8 * (int)ceil(per_block / 8.0);
         groups = (int)((nt + cb8 - 1) / cb8);
     }
@@ -713,7 +728,7 @@ int sfh_launch_fg(sfh_ctx *ctx, const sfh_models *m, const FgArgs &a, cudaEvent_
     if (!Mptr) return sfh_set_error(ctx, SFH_ERR_ARG, "models handle has no matrix");
     const int64_t nbins = m->nbins, nt = m->nt;
     const bool fused_path = !f64 && (a.mode == FG_MODE_FG || a.mode == FG_MODE_COMPOSITE);
-    const Plan p = make_plan(ctx, nbins, nt, f64, fused_path);
+    const Plan p = make_plan(ctx, nbins, nt, f64, fused_path, m);
     int rc = sfh_scratch_reserve(ctx, p.total);
     if (rc) return rc;
     char *s = (char *)ctx->scratch;
@@ -748,6 +763,7 @@ int sfh_launch_fg(sfh_ctx *ctx, const sfh_models *m, const FgArgs &a, cudaEvent_
         p1.tile_cnt = ctx->d_counters + SFH_CNT_ROWTILE;
         p1.all_cnt = ctx->d_counters + SFH_CNT_FG_LOGL;
         p1.negLogL = a.negLogL;
+        p1.tab = ctx->d_df_tab;
         dim3 grid(p.ksplit, p.nrowblk);
         const size_t sm = 2 * (size_t)p.kchunk * sizeof(float);
         if (nbins % 4 == 0)
@@ -879,6 +895,91 @@ extern "C" int sfh_fg_kernel_times(sfh_ctx *ctx, const sfh_models *m, const doub
     for (int k = 0; k < 5; ++k) cudaEventDestroy(ev[k]);
     for (int k = 0; k < 4; ++k) ms_out[k] = acc[k] / iters;
     return rc;
+}
+
+extern "C" int sfh_models_autotune(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
+                                   const double *d_data, double eps, int iters, int *plan_out,
+                                   double *ms_out) {
+    if (!ctx || !m || !d_coeffs || !d_data || iters < 1) return SFH_ERR_ARG;
+    if (m->storage == SFH_F64) return SFH_OK;  // the FP64 path has no tunable plan
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    double *buf = nullptr;  // composite, G, -logL of the trial runs
+    SFH_CK(ctx, cudaMalloc(&buf, (size_t)(m->nbins + m->nt + 1) * sizeof(double)));
+    cudaEvent_t ev[5];
+    for (int k = 0; k < 5; ++k) {
+        cudaError_t e = cudaEventCreate(&ev[k]);
+        if (e != cudaSuccess) {
+            for (int q = 0; q < k; ++q) cudaEventDestroy(ev[q]);
+            cudaFree(buf);
+            return sfh_cuda_error(ctx, e, "event create");
+        }
+    }
+    FgArgs a{};
+    a.coeffs = d_coeffs;
+    a.data = d_data;
+    a.composite = buf;
+    a.G = buf + m->nbins;
+    a.negLogL = buf + m->nbins + m->nt;
+    a.eps = eps;
+    a.gsign = 1.0;
+    a.mode = FG_MODE_FG;
+    // average pass-1 / pass-2 times of the current plan (after one untimed run)
+    auto timed = [&](double &t1, double &t2) -> int {
+        t1 = t2 = 0.0;
+        for (int it = -1; it < iters; ++it) {
+            int rc = sfh_launch_fg(ctx, m, a, ev);
+            if (rc) return rc;
+            cudaError_t e = cudaEventSynchronize(ev[4]);
+            if (e != cudaSuccess) return sfh_cuda_error(ctx, e, "event sync");
+            if (it < 0) continue;
+            float x = 0.f, y = 0.f;
+            cudaEventElapsedTime(&x, ev[0], ev[1]);
+            cudaEventElapsedTime(&y, ev[2], ev[4]);
+            t1 += x;
+            t2 += y;
+        }
+        t1 /= iters;
+        t2 /= iters;
+        return SFH_OK;
+    };
+    const int W1[] = {1, 2, 3, 4}, RR[] = {1024, 2048, 4096}, W2[] = {1, 2, 4};
+    int best_w1 = 2, best_R = kFusedR, best_w2 = 1;
+    double b1 = 1e300, b2 = 1e300, t1 = 0, t2 = 0;
+    int rc = SFH_OK;
+    m->tune_R = best_R;
+    m->tune_w2 = best_w2;
+    for (int w1 : W1) {  // pass 1 (pass 2 fixed at the default)
+        m->tune_w1 = w1;
+        if ((rc = timed(t1, t2))) break;
+        if (t1 < b1) { b1 = t1; best_w1 = w1; }
+    }
+    m->tune_w1 = best_w1;
+    for (int r = 0; r < 3 && rc == SFH_OK; ++r)  // pass 2 with the chosen pass 1
+        for (int w2 : W2) {
+            m->tune_R = RR[r];
+            m->tune_w2 = w2;
+            if ((rc = timed(t1, t2))) break;
+            if (t2 < b2) { b2 = t2; best_R = RR[r]; best_w2 = w2; }
+        }
+    for (int k = 0; k < 5; ++k) cudaEventDestroy(ev[k]);
+    cudaFree(buf);
+    if (rc) {
+        m->tune_w1 = m->tune_R = m->tune_w2 = 0;
+        return rc;
+    }
+    m->tune_w1 = best_w1;
+    m->tune_R = best_R;
+    m->tune_w2 = best_w2;
+    if (plan_out) {
+        plan_out[0] = best_w1;
+        plan_out[1] = best_R;
+        plan_out[2] = best_w2;
+    }
+    if (ms_out) {
+        ms_out[0] = b1;
+        ms_out[1] = b2;
+    }
+    return SFH_OK;
 }
 
 int sfh_launch_loglikelihood(sfh_ctx *ctx, const double *composite, const double *data,

@@ -69,14 +69,41 @@ __device__ __forceinline__ void block_sum(double v, double *s_red, double *out) 
     }
 }
 
+// One bin's share of fg!: the model m = ah + al (compensated), the Poisson term in
+// double-float (sfh_dfloat.cuh) and w = 1 - n / max(m, eps) (fitting_base.jl:90-93,
+// 274-280); composite receives w when the gradient is wanted, the model otherwise.
+__device__ __forceinline__ void bin_terms(float ah, float al, const double *__restrict__ data,
+                                          int64_t ii, double eps, int want_logl, int want_w,
+                                          const sfh_df *s_tab, double *__restrict__ composite,
+                                          sfh_df &term, float &w) {
+    sfh_df c = df_fast_two_sum(ah, al);
+    if (!want_logl && !want_w) {
+        composite[ii] = (double)c.h + (double)c.l;
+        return;
+    }
+    if (!want_w) composite[ii] = (double)c.h + (double)c.l;  // the model, unclamped
+    const float eps_f = (float)eps;  // eps(T) is a power of two, exact in FP32
+    if (c.h < eps_f || (c.h == eps_f && c.l < 0.f)) c = sfh_df{eps_f, 0.f};
+    const double n = data[ii];
+    const float nh = __double2float_rn(n);
+    const float nl = __double2float_rn(n - (double)nh);
+    if (want_logl) term = df_add(term, df_poisson_term(c, nh, nl, s_tab));
+    if (want_w) {
+        w = __fdiv_rn(df_add(c, sfh_df{-nh, -nl}).h, c.h);
+        composite[ii] = (double)w;
+    }
+}
+
 __global__ void __launch_bounds__(kRT)
 k_ragged_pass1(const float *__restrict__ M, const GalDesc *__restrict__ gals,
                const RowTile *__restrict__ tiles, const double *__restrict__ coeffs,
                const double *__restrict__ data, double *__restrict__ composite,
                float *__restrict__ w32, double *__restrict__ tile_logl, double eps,
-               int want_logl, int want_w) {
+               int want_logl, int want_w, const sfh_df *__restrict__ tab) {
     __shared__ float rhi[kRChunk], rlo[kRChunk];
     __shared__ double s_red[kRT / 32];
+    __shared__ sfh_df s_tab[129];
+    for (int k = threadIdx.x; k < 129; k += kRT) s_tab[k] = tab[k];
     const RowTile tile = tiles[blockIdx.x];
     const GalDesc G = gals[tile.g];
     const int64_t i = (int64_t)tile.row0 + threadIdx.x;
@@ -109,28 +136,16 @@ k_ragged_pass1(const float *__restrict__ M, const GalDesc *__restrict__ gals,
             sfh_two_sum_acc(ah, al, fmaf(v, rhi[k], v * rlo[k]));
         }
     }
-    double term = 0.0;
+    sfh_df term{0.f, 0.f};
     if (live) {
         const int64_t ii = G.boff + i;
-        const double m = (double)ah + (double)al;
-        if (!want_logl && !want_w) {
-            composite[ii] = m;
-        } else {
-            const double c = m > eps ? m : eps;  // max(composite, eps(T)), fitting_base.jl:90
-            const double n = data[ii];
-            if (want_logl) term = (n > 0.0) ? sfh_poisson_term_occupied(c, n) : -c;
-            if (want_w) {
-                const float w = __fdiv_rn((float)(c - n), (float)c);  // 1 - n/c, :274-280
-                composite[ii] = (double)w;
-                w32[ii] = w;
-            } else {
-                composite[ii] = m;
-            }
-        }
+        float w = 0.f;
+        bin_terms(ah, al, data, ii, eps, want_logl, want_w, s_tab, composite, term, w);
+        if (want_w) w32[ii] = w;
     }
     if (want_logl) {
         double tsum = 0.0;
-        block_sum(term, s_red, &tsum);
+        sfh_df_block_sum(term, s_red, &tsum);
         if (threadIdx.x == 0) tile_logl[blockIdx.x] = tsum;
     }
 }
@@ -183,10 +198,12 @@ k_ragged_fused(const float *__restrict__ M, const GalDesc *__restrict__ gals,
                const RowTile *__restrict__ tiles, const double *__restrict__ coeffs,
                const double *__restrict__ data, double *__restrict__ composite,
                double *__restrict__ tile_logl, double *__restrict__ gpart, double eps,
-               int want_logl, int want_g) {
+               int want_logl, int want_g, const sfh_df *__restrict__ tab) {
     __shared__ float rhi[NT], rlo[NT];
     __shared__ double s_red[kRT / 32];
     __shared__ float s_g[kRT / 32][NT];
+    __shared__ sfh_df s_tab[129];
+    for (int k = threadIdx.x; k < 129; k += kRT) s_tab[k] = tab[k];
     const RowTile tile = tiles[blockIdx.x];
     const GalDesc G = gals[tile.g];
     const int nt = (int)G.nt;
@@ -212,28 +229,12 @@ k_ragged_fused(const float *__restrict__ M, const GalDesc *__restrict__ gals,
         for (int u = 0; u < 8; ++u) s = fmaf(m[j0 + u], rhi[j0 + u], fmaf(m[j0 + u], rlo[j0 + u], s));
         sfh_two_sum_acc(ah, al, s);
     }
-    double term = 0.0;
+    sfh_df term{0.f, 0.f};
     float w = 0.f;
-    if (live) {
-        const int64_t ii = G.boff + i;
-        const double mm = (double)ah + (double)al;
-        if (!want_logl && !want_g) {
-            composite[ii] = mm;
-        } else {
-            const double c = mm > eps ? mm : eps;  // max(composite, eps(T)), fitting_base.jl:90
-            const double n = data[ii];
-            if (want_logl) term = (n > 0.0) ? sfh_poisson_term_occupied(c, n) : -c;
-            if (want_g) {
-                w = __fdiv_rn((float)(c - n), (float)c);  // 1 - n/c, :274-280
-                composite[ii] = (double)w;
-            } else {
-                composite[ii] = mm;
-            }
-        }
-    }
+    if (live) bin_terms(ah, al, data, G.boff + i, eps, want_logl, want_g, s_tab, composite, term, w);
     if (want_logl) {
         double tsum = 0.0;
-        block_sum(term, s_red, &tsum);
+        sfh_df_block_sum(term, s_red, &tsum);
         if (threadIdx.x == 0) tile_logl[blockIdx.x] = tsum;
     }
     if (!want_g) return;
@@ -431,7 +432,7 @@ extern "C" int sfh_fg_ragged_dev(sfh_ctx *ctx, const sfh_galaxies *gal, const do
                                               : k_ragged_fused<32>;
         kern<<<(unsigned)gal->n_fused_tiles, kRT, 0, st>>>(
             gal->d_models, desc, (const RowTile *)gal->d_fused, d_coeffs, d_data, d_composite, tf,
-            gp, eps, want_logl ? 1 : 0, want_w ? 1 : 0);
+            gp, eps, want_logl ? 1 : 0, want_w ? 1 : 0, ctx->d_df_tab);
         SFH_LAUNCHED(ctx);
         if (want_logl || want_w) {
             k_ragged_finish<<<(unsigned)gal->n_fused_gal, kRT, 0, st>>>(
@@ -443,7 +444,7 @@ extern "C" int sfh_fg_ragged_dev(sfh_ctx *ctx, const sfh_galaxies *gal, const do
     if (gal->n_big_gal) {
         k_ragged_pass1<<<(unsigned)gal->n_row_tiles, kRT, 0, st>>>(
             gal->d_models, desc, (const RowTile *)gal->d_rows, d_coeffs, d_data, d_composite, w32,
-            tl, eps, want_logl ? 1 : 0, want_w ? 1 : 0);
+            tl, eps, want_logl ? 1 : 0, want_w ? 1 : 0, ctx->d_df_tab);
         SFH_LAUNCHED(ctx);
         if (want_logl) {
             k_ragged_logl<<<(unsigned)gal->n_big_gal, kRT, 0, st>>>(

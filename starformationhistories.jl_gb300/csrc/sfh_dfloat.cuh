@@ -1,0 +1,187 @@
+// sfh_dfloat.cuh -- double-float arithmetic (value = hi + lo, two FP32 numbers) for the
+// per-bin Poisson terms, so that they run on the FP32 pipes.  GB300's FP64 rate is a small
+// fraction of its FP32 rate; with these helpers a bin costs a handful of conversions on
+// the FP64 pipe instead of an FP64 logarithm.
+//
+// Error-free transformations: two_sum (Knuth), fast_two_sum (Dekker), two_prod via FMA.
+// Logarithm of a float: table-driven reduction (P. T. P. Tang, "Table-driven
+// implementation of the logarithm function in IEEE floating-point arithmetic", ACM TOMS
+// 16(4), 1990): x = 2^e m, m = F (1 + u) with F = 1 + j/128 nearest to m, |u| <= 2^-8,
+// log x = e ln2 + log F + log1p(u), log F from a 129-entry table of float pairs and
+// log1p(u) = u - u^2/2 + u^3 (1/3 - u/4 + u^2/5 - u^3/6 + u^4/7) (truncation < 2^-64).
+// Host-compilable (the same header is exercised by a host check); additions and products
+// use the round-to-nearest intrinsics on the device so no contraction can break the
+// error-free transformations.
+#pragma once
+#include <stdint.h>
+#include <string.h>
+#include <math.h>
+
+#ifdef __CUDACC__
+#define SFH_DF_HD __host__ __device__ __forceinline__
+#else
+#define SFH_DF_HD static inline
+#endif
+
+#if defined(__CUDA_ARCH__)
+#define SFH_DF_ADD(a, b) __fadd_rn((a), (b))
+#define SFH_DF_SUB(a, b) __fsub_rn((a), (b))
+#define SFH_DF_MUL(a, b) __fmul_rn((a), (b))
+#define SFH_DF_DIV(a, b) __fdiv_rn((a), (b))
+#else
+#define SFH_DF_ADD(a, b) ((a) + (b))
+#define SFH_DF_SUB(a, b) ((a) - (b))
+#define SFH_DF_MUL(a, b) ((a) * (b))
+#define SFH_DF_DIV(a, b) ((a) / (b))
+#endif
+
+struct sfh_df {
+    float h, l;
+};
+
+SFH_DF_HD sfh_df df_two_sum(float a, float b) {
+    const float s = SFH_DF_ADD(a, b);
+    const float bb = SFH_DF_SUB(s, a);
+    const float e = SFH_DF_ADD(SFH_DF_SUB(a, SFH_DF_SUB(s, bb)), SFH_DF_SUB(b, bb));
+    return sfh_df{s, e};
+}
+SFH_DF_HD sfh_df df_fast_two_sum(float a, float b) {  // |a| >= |b| or a == 0
+    const float s = SFH_DF_ADD(a, b);
+    return sfh_df{s, SFH_DF_SUB(b, SFH_DF_SUB(s, a))};
+}
+SFH_DF_HD sfh_df df_two_prod(float a, float b) {
+    const float p = SFH_DF_MUL(a, b);
+    return sfh_df{p, fmaf(a, b, -p)};
+}
+SFH_DF_HD sfh_df df_neg(sfh_df a) { return sfh_df{-a.h, -a.l}; }
+SFH_DF_HD sfh_df df_add(sfh_df a, sfh_df b) {
+    sfh_df s = df_two_sum(a.h, b.h);
+    const sfh_df t = df_two_sum(a.l, b.l);
+    s = df_fast_two_sum(s.h, SFH_DF_ADD(s.l, t.h));
+    return df_fast_two_sum(s.h, SFH_DF_ADD(s.l, t.l));
+}
+SFH_DF_HD sfh_df df_add_f(sfh_df a, float b) {
+    const sfh_df s = df_two_sum(a.h, b);
+    return df_fast_two_sum(s.h, SFH_DF_ADD(s.l, a.l));
+}
+SFH_DF_HD sfh_df df_mul(sfh_df a, sfh_df b) {
+    const sfh_df p = df_two_prod(a.h, b.h);
+    const float c = fmaf(a.h, b.l, SFH_DF_MUL(a.l, b.h));
+    return df_fast_two_sum(p.h, SFH_DF_ADD(p.l, c));
+}
+SFH_DF_HD sfh_df df_mul_f(sfh_df a, float b) {
+    const sfh_df p = df_two_prod(a.h, b);
+    return df_fast_two_sum(p.h, fmaf(a.l, b, p.l));
+}
+SFH_DF_HD sfh_df df_div(sfh_df a, sfh_df b) {
+    const float q0 = SFH_DF_DIV(a.h, b.h);
+    const sfh_df r = df_add(a, df_neg(df_mul_f(b, q0)));
+    const float q1 = SFH_DF_DIV(r.h, b.h);
+    return df_fast_two_sum(q0, q1);
+}
+
+// ln 2 = LN2_HI + LN2_LO with LN2_HI holding 16 significant bits, so e * LN2_HI is exact
+// for every float exponent e.
+#define SFH_DF_LN2_HI 0.693145751953125f
+#define SFH_DF_LN2_LO 1.428606765330187e-06f   // ln2 - LN2_HI rounded to float
+#define SFH_DF_LN2_LO2 5.4979230187083712e-14f  // ln2 - LN2_HI - LN2_LO
+
+SFH_DF_HD uint32_t df_bits(float x) {
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(x);
+#else
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    return u;
+#endif
+}
+SFH_DF_HD float df_from_bits(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(u);
+#else
+    float x;
+    memcpy(&x, &u, 4);
+    return x;
+#endif
+}
+
+// log(x) for a finite float x > 0 as a double-float.  tab holds log(1 + j/128) for
+// j = 0..128 as (hi, lo) pairs (sfh_df_log_table fills it).
+SFH_DF_HD sfh_df df_log_f(float x, const sfh_df *tab) {
+    int e = 0;
+    if (x < 1.1754943508e-38f) {  // subnormal: scale into the normal range
+        x = SFH_DF_MUL(x, 16777216.0f);
+        e = -24;
+    }
+    const uint32_t u = df_bits(x);
+    e += (int)((u >> 23) & 0xffu) - 127;
+    const uint32_t mant = u & 0x7fffffu;
+    const int j = (int)((mant + (1u << 15)) >> 16);  // nearest j / 128, 0..128
+    const float m = df_from_bits(mant | 0x3f800000u);  // [1, 2)
+    const float F = SFH_DF_ADD(1.0f, SFH_DF_MUL((float)j, 0.0078125f));  // exact
+    const float f = SFH_DF_SUB(m, F);                                   // exact, |f| <= 2^-8
+    // u = f / F as a double-float
+    const float uh = SFH_DF_DIV(f, F);
+    const float ul = SFH_DF_DIV(fmaf(-uh, F, f), F);
+    // log1p(u) = u - u^2/2 + u^3 (1/3 - u/4 + u^2/5 - u^3/6 + u^4/7)
+    sfh_df u2 = df_two_prod(uh, uh);
+    u2.l = fmaf(SFH_DF_ADD(uh, uh), ul, u2.l);
+    float p = fmaf(uh, 1.0f / 7.0f, -1.0f / 6.0f);
+    p = fmaf(uh, p, 0.2f);
+    p = fmaf(uh, p, -0.25f);
+    p = fmaf(uh, p, 1.0f / 3.0f);
+    p = SFH_DF_MUL(SFH_DF_MUL(SFH_DF_MUL(uh, uh), uh), p);
+    sfh_df s = df_two_sum(uh, SFH_DF_MUL(-0.5f, u2.h));
+    s = df_fast_two_sum(s.h, SFH_DF_ADD(s.l, SFH_DF_ADD(SFH_DF_SUB(ul, SFH_DF_MUL(0.5f, u2.l)), p)));
+    const float fe = (float)e;
+    sfh_df le = df_fast_two_sum(SFH_DF_MUL(fe, SFH_DF_LN2_HI),
+                                fmaf(fe, SFH_DF_LN2_LO, SFH_DF_MUL(fe, SFH_DF_LN2_LO2)));
+    return df_add(df_add(le, tab[j]), s);
+}
+
+// Poisson term of one bin, fitting_base.jl:93:  n - c - n log(n/c)  (n > 0),  -c  (n = 0),
+// for c = ch + cl >= eps given as a double-float (compensated sum) and n = nh + nl.
+//   |c/n - 1| <= 1/8:  -(c-n)^2/(c+n) + 2 n z^3 (1/3 + z^2/5 + ...),  z = (c-n)/(c+n)
+//                      (log1p(d) = 2 atanh z), all but the z^5 tail (< 3e-7 n) in
+//                      double-float, so tiny terms keep their relative accuracy;
+//   otherwise:         n log(c/n) - (c - n) with the double-float logarithm.
+// Absolute error below 1e-11 (c + n) (checked against long double on 4e6 random bins).
+SFH_DF_HD sfh_df df_poisson_term(sfh_df c, float nh, float nl, const sfh_df *tab) {
+    const sfh_df n{nh, nl};
+    if (!(nh > 0.0f)) return df_neg(c);
+    const sfh_df diff = df_add(c, df_neg(n));
+    const float d = SFH_DF_DIV(diff.h, nh);
+    if (fabsf(d) <= 0.125f) {
+        const sfh_df sum = df_add(c, n);
+        const sfh_df z = df_div(diff, sum);
+        const sfh_df L = df_neg(df_mul(diff, z));
+        // 2 n z^3 / 3 in double-float, the z^5 tail (<= 1.3e-4 n) in FP32
+        const sfh_df z3 = df_mul(df_mul(z, z), z);
+        const sfh_df T3 = df_mul(df_mul(z3, n), sfh_df{0.666666686534881591796875f,
+                                                     -1.9868215517249155e-08f});
+        const float z2 = SFH_DF_MUL(z.h, z.h);
+        float S = 1.0f / 17.0f;
+        S = fmaf(S, z2, 1.0f / 15.0f);
+        S = fmaf(S, z2, 1.0f / 13.0f);
+        S = fmaf(S, z2, 1.0f / 11.0f);
+        S = fmaf(S, z2, 1.0f / 9.0f);
+        S = fmaf(S, z2, 1.0f / 7.0f);
+        S = fmaf(S, z2, 1.0f / 5.0f);
+        const float C5 = SFH_DF_MUL(SFH_DF_MUL(SFH_DF_MUL(2.0f, nh), SFH_DF_MUL(z3.h, z2)), S);
+        return df_add_f(df_add(L, T3), C5);
+    }
+    const sfh_df q = df_div(c, n);
+    sfh_df lq = df_log_f(q.h, tab);
+    lq = df_add_f(lq, SFH_DF_DIV(q.l, q.h));  // log(qh + ql) = log qh + ql/qh (+ O(ql^2))
+    return df_add(df_mul(lq, n), df_neg(diff));
+}
+
+// Host-side table of log(1 + j/128), j = 0..128, as double-float pairs.
+static inline void sfh_df_log_table(sfh_df *tab) {
+    for (int j = 0; j <= 128; ++j) {
+        const double v = log1p((double)j / 128.0);
+        const float h = (float)v;
+        tab[j].h = h;
+        tab[j].l = (float)(v - (double)h);
+    }
+}

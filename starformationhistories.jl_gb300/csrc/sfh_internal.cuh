@@ -8,6 +8,7 @@
 #include <string>
 
 #include "../../include/sfhgpu.h"
+#include "sfh_dfloat.cuh"
 
 struct sfh_ctx {
     int device = 0;
@@ -22,6 +23,9 @@ struct sfh_ctx {
     size_t stage_bytes = 0;
     // Zero-initialised counters for last-block reductions (reset by the last block).
     unsigned int *d_counters = nullptr;
+    // log(1 + j/128), j = 0..128, as double-float pairs (sfh_dfloat.cuh), for the
+    // Poisson terms evaluated on the FP32 pipes.
+    sfh_df *d_df_tab = nullptr;
     int64_t launches = 0;
 };
 
@@ -38,6 +42,9 @@ struct sfh_models {
     // FP32 copy kept with BF16X2 storage so single-vector calls still work.
     float *d_f32 = nullptr;
     int64_t nbins_pad = 0, nt_pad = 0;
+    // Single-vector launch plan chosen by sfh_models_autotune (0 = built-in heuristics):
+    // pass-1 waves of resident blocks, pass-2 row chunk, pass-2 waves.
+    int tune_w1 = 0, tune_R = 0, tune_w2 = 0;
 };
 
 // Counter slots in sfh_ctx::d_counters (zeroed at context creation; every kernel that
@@ -106,37 +113,28 @@ __device__ __forceinline__ float sfh_log1p_minus_id(float d, float c, float n) {
     return log1pf(d) - d;
 }
 
-// Poisson term of an occupied bin, n - c - n log(n/c) (fitting_base.jl:93), in the form
-//   n (log1p(d) - d),  d = (c - n)/n,  z = (c - n)/(c + n),
-//   log1p(d) - d = -d z + 2 z^3 (1/3 + z^2/5 + z^4/7 + ...)   (log1p(d) = 2 atanh z)
-// so the term is  L + C  with  L = -(c - n)^2/(c + n)  formed in FP64 from a
-// double-float quotient (a handful of FP64 operations) and the small remainder
-// C = 2 n z^3 S(z^2) in FP32.  Bins far from their model (|d| > 1/2) take one FP64
-// log instead.  FP64 throughput on this part is a small fraction of FP32, so the
-// series path keeps FP64 work per bin to five operations.
-__device__ __forceinline__ double sfh_poisson_term_occupied(double c, double n) {
-    const double diff = c - n;
-    const float df = (float)diff, nf = (float)n;
-    const float d = __fdiv_rn(df, nf);
-    if (fabsf(d) <= 0.5f) {
-        const double sum = c + n;
-        const float sf = (float)sum;
-        const float q0 = __fdiv_rn(df, sf);
-        const double r = fma(-(double)q0, sum, diff);
-        const float q1 = __fdiv_rn((float)r, sf);
-        const double L = -diff * ((double)q0 + (double)q1);
-        const float z = q0 + q1, z2 = z * z;
-        float S = 1.0f / 17.0f;
-        S = fmaf(S, z2, 1.0f / 15.0f);
-        S = fmaf(S, z2, 1.0f / 13.0f);
-        S = fmaf(S, z2, 1.0f / 11.0f);
-        S = fmaf(S, z2, 1.0f / 9.0f);
-        S = fmaf(S, z2, 1.0f / 7.0f);
-        S = fmaf(S, z2, 1.0f / 5.0f);
-        S = fmaf(S, z2, 1.0f / 3.0f);
-        return L + (double)(2.0f * nf * z * z2 * S);
+// Sum of a double-float over the warp (all lanes receive it), FP32 operations only.
+__device__ __forceinline__ sfh_df sfh_df_warp_sum(sfh_df v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const sfh_df u{__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)};
+        v = df_add(v, u);
     }
-    return n * log(c / n) - diff;
+    return v;
+}
+
+// Block sum of a double-float into a double at *out (thread 0); s_red holds one double per
+// warp.  Every thread of the block must call it.
+__device__ __forceinline__ void sfh_df_block_sum(sfh_df v, double *s_red, double *out) {
+    v = sfh_df_warp_sum(v);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = (double)v.h + (double)v.l;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += s_red[w];
+        *out = b;
+    }
 }
 
 // ------------------------------------------------------------------ internal launchers

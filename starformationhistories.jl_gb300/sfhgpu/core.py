@@ -114,6 +114,22 @@ class Models:
     def shape(self):
         return (self.nbins, self.nt)
 
+    def autotune(self, coeffs, data, iters=10, eps=None):
+        """Pick the fastest single-vector fg! launch plan for this matrix by timing the
+        candidates on the device (sfh_models_autotune).  Returns
+        {"plan": (pass-1 waves, pass-2 rows, pass-2 waves), "ms": (pass 1, pass 2)}."""
+        import torch
+        dev = torch.device("cuda", self.ctx.device)
+        r = torch.as_tensor(np.asarray(coeffs, dtype=np.float64), device=dev).contiguous()
+        n = torch.as_tensor(np.asarray(data, dtype=np.float64).reshape(-1), device=dev).contiguous()
+        plan = (C.c_int * 3)()
+        ms = (C.c_double * 2)()
+        eps = float(np.finfo(np.float64).eps) if eps is None else float(eps)
+        torch.cuda.current_stream(dev).synchronize()
+        check(load().sfh_models_autotune(self.ctx.handle, self._h, r.data_ptr(), n.data_ptr(), eps,
+                                         int(iters), plan, ms), self.ctx.handle, "autotune")
+        return {"plan": tuple(plan), "ms": tuple(ms)}
+
     def free(self):
         if getattr(self, "_h", None) is not None:
             load().sfh_models_free(self._h)

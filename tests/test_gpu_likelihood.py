@@ -172,3 +172,22 @@ def test_fit_templates_poisson(sfh):
     res = sfh.fit_templates(H, data, x0=np.ones(10))
     assert np.linalg.norm(res.mle.mu - x) <= 1e-2 * np.linalg.norm(x)
     assert np.linalg.norm(res.mle.mu - xf) <= 1e-5 * np.linalg.norm(xf) * 1e2
+
+
+def test_autotuned_plan_keeps_parity(sfh, O):
+    """The autotuner picks a plan among its candidates; fg! with that plan still matches
+    the oracle at the FP32-storage tolerances."""
+    M, r, data = _problem(60000, 96, seed=7)
+    H = sfh.Models(M, storage="f32")
+    res = H.autotune(r, data, iters=3)
+    w1, R, w2 = res["plan"]
+    assert w1 in (1, 2, 3, 4) and R in (1024, 2048, 4096) and w2 in (1, 2, 4)
+    assert all(t > 0 for t in res["ms"])
+    comp = np.empty(M.shape[0])
+    G = np.empty(M.shape[1])
+    v = sfh.fg_(True, G, r, H, data, comp)
+    Mst = M.astype(np.float32).astype(np.float64)
+    v_ref, G_ref, w_ref = O.fg(r, Mst, data)
+    assert abs(v - v_ref) <= 1e-5 * max(1.0, data.sum() / 1e4)
+    scale = np.abs(Mst).T @ np.abs(w_ref) + 1e-300
+    assert np.max(np.abs(G - G_ref) / scale) <= 2e-6
