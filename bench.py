@@ -182,10 +182,13 @@ def run_batched(ctx, d_T, nbins, nt, r, data, M64, steps, warmup, B=4096, check=
     }
 
 
-def run_hmc(ctx, d_T, w, nchains=1024, nwarmup=40, ntraj=40, nleap=10, seed=20261205):
+def run_hmc(ctx, d_T, w, nchains=1024, nwarmup=500, ntraj=1500, nleap=10, seed=20261205,
+            d_model=None):
     """End-to-end hierarchical HMC (PowerLawMZR slope 0.5, GaussianDispersion 0.2) on the
     1,200-template grid: all chains advance together, one batched tensor-core evaluation
-    per leapfrog substep, trajectories replayed from a captured CUDA graph."""
+    per leapfrog substep, trajectories replayed from a captured CUDA graph.  The data are
+    drawn from the exact templates d_T; the sampler uses d_model when given (emulated
+    templates with exact fallback), d_T otherwise."""
     import numpy as np
     import torch
 
@@ -193,7 +196,8 @@ def run_hmc(ctx, d_T, w, nchains=1024, nwarmup=40, ntraj=40, nleap=10, seed=2026
     from sfhgpu.sampling import GaussianDispersion, PowerLawMZR, calculate_coeffs
     nbins, nt = w.nbins, w.ntempl
     la, mh = w.template_params
-    Hb = sfhgpu.Models.from_device(d_T.data_ptr(), nbins, nt, storage="bf16x2", ctx=ctx)
+    src = d_T if d_model is None else d_model
+    Hb = sfhgpu.Models.from_device(src.data_ptr(), nbins, nt, storage="bf16x2", ctx=ctx)
     rng = np.random.default_rng(seed)
     mzr, disp = PowerLawMZR(0.5, -1.0, 6.0), GaussianDispersion(0.2)
     R = np.exp(0.5 * rng.standard_normal(w.logAges.size))
@@ -226,6 +230,7 @@ def run_hmc(ctx, d_T, w, nchains=1024, nwarmup=40, ntraj=40, nleap=10, seed=2026
         "truth_alpha_MH0_sigma": [0.5, -1.0, 0.2],
         "posterior_mean_abs_err": [float(abs(a - b)) for a, b in zip(pm[na:na + 3],
                                                                       [0.5, -1.0, 0.2])],
+        "posterior_mean_R": [float(x) for x in pm[:na]],
         "note": "wall clock of sample_sfh (setup, graph capture, warmup and sampling); "
                 "one batched gradient per leapfrog step (the start gradient is carried over)",
     }
@@ -319,7 +324,7 @@ def run_ragged(ctx, steps=50, warmup=5, check=2):
     }
 
 
-def run_emulator(ctx, w, n_train=65536, n_val=4096, steps=4000, cells=(8, 2, 16), nreq=1200):
+def run_emulator(ctx, w, n_train=100_000, n_val=4096, steps=4000, cells=(8, 2, 16), nreq=1200):
     """Learned template emulator on the production grid: per-cell PCA bases (64
     components of sqrt templates) and per-cell MLPs 3-256-256-64 trained on templates the
     GPU partial_cmd_smooth generates at random (log age, [M/H], distance modulus); judged
@@ -351,6 +356,7 @@ def run_emulator(ctx, w, n_train=65536, n_val=4096, steps=4000, cells=(8, 2, 16)
     em.templates(th, gen)  # trust-map routing: emulated where validated, exact elsewhere
     torch.cuda.synchronize()
     t_routed = time.perf_counter() - t0
+    run_emulator.last = em
     return {
         "workload": f"{n_train} training templates on the 200x300 grid, theta = (log age "
                     f"U[6.6,10.1], [M/H] U[-2.5,0.3], dmod U[24,30]); {int(np.prod(cells))} "
@@ -506,6 +512,7 @@ def run_ours(args):
 
     import sfhgpu
     from sfhgpu import synthetic as S
+    from sfhgpu.emulator import SyntheticGenerator
 
     world, rank, local = _dist()
     if world > 1:
@@ -629,7 +636,7 @@ def run_ours(args):
                 "peak_source": peak_kind,
                 "kernel_ms": {n: kms[i] for i, n in enumerate(names)},
                 "fg_total_gbs": (alg[0] + alg[2]) / (ms / args.steps * 1e-3) / 1e9,
-                "autotuned_plan": {"pass1_waves": tuned["plan"][0], "pass2_rows": tuned["plan"][1],
+                "autotuned_plan": {"pass1_template_splits": tuned["plan"][0], "pass2_rows": tuned["plan"][1],
                                    "pass2_waves": tuned["plan"][2], "pass_ms": tuned["ms"]}}
 
     # ---- end to end through the host-array C ABI (sfh_fg)
@@ -669,6 +676,28 @@ def run_ours(args):
     if not args.no_hmc:
         hmc = run_hmc(ctx, d_T, w)
         hmc["speedup_vs_plain_evals"] = hmc["chain_gradient_evals_per_s"] / value
+        # the plain single-chain GPU path needs the same number of gradient evaluations to
+        # reach the same posterior-mean error (equal effective samples per draw assumed)
+        nev = 1024 * 2000 * 10
+        hmc["plain_single_chain_seconds_at_matched_error"] = nev / value
+        hmc["speedup_vs_plain_single_chain_at_matched_error"] = nev / value / hmc["seconds"]
+        em = getattr(run_emulator, "last", None)
+        if em is not None:
+            # the same fit on emulated templates (exact where the trust map says so)
+            la, mh = w.template_params
+            th = np.stack([la, mh, np.full(la.size, w.dmod)], 1)
+            d_em, used = em.templates(th, SyntheticGenerator(w.xedges, w.yedges, ctx=ctx))
+            torch.cuda.synchronize()
+            he = run_hmc(ctx, d_T, w, d_model=d_em)
+            hmc["emulated_templates"] = {
+                "emulated_fraction": float(np.mean(used)), "seconds": he["seconds"],
+                "posterior_mean_alpha_MH0_sigma": he["posterior_mean_alpha_MH0_sigma"],
+                "posterior_mean_abs_err": he["posterior_mean_abs_err"],
+                "posterior_mean_R_rel_diff_vs_exact_templates_max": float(np.max(
+                    np.abs(np.asarray(he["posterior_mean_R"]) / np.asarray(hmc["posterior_mean_R"])
+                           - 1.0))),
+            }
+            del d_em
 
     # ---- CPU baseline (rank 0, N = 1 only): the oracle on the same inputs
     cpu = None

@@ -119,12 +119,13 @@ int sfh_fg_kernel_times(sfh_ctx *ctx, const sfh_models *models, const double *d_
                         double *d_negLogL, double eps, int iters, double *ms_out);
 
 /* Autotuner (no reference counterpart): times candidate launch plans of the FP32
-   single-vector fg! on this matrix with the caller's inputs (pass-1 template splits sized
-   to 1-4 waves of resident blocks; pass-2 row chunks of 1,024 / 2,048 / 4,096 bins and
-   column groups sized to 1, 2 or 4 waves), `iters` timed runs each, and stores the
-   fastest in the handle; later fg! calls on it use that plan.  plan_out (3 ints: pass-1
-   waves, pass-2 rows, pass-2 waves) and ms_out (2 doubles: pass-1 and pass-2 ms) may be
-   NULL.  Call it before sharing the handle between contexts.  No-op for FP64 storage. */
+   single-vector fg! on this matrix with the caller's inputs (pass-1 template splits whose
+   grids fill 1/2 to 4 whole waves of resident blocks; pass-2 row chunks of 1,024 / 2,048
+   / 4,096 bins and column groups sized to 1, 2 or 4 waves), `iters` timed runs each, and
+   stores the fastest in the handle; later fg! calls on it use that plan.  plan_out
+   (3 ints: pass-1 template splits, pass-2 rows, pass-2 waves) and ms_out (2 doubles:
+   pass-1 and pass-2 ms) may be NULL.  Call it before sharing the handle between
+   contexts.  No-op for FP64 storage. */
 int sfh_models_autotune(sfh_ctx *ctx, sfh_models *models, const double *d_coeffs,
                         const double *d_data, double eps, int iters, int *plan_out,
                         double *ms_out);

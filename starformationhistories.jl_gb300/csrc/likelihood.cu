@@ -374,6 +374,7 @@ struct Pass1Args {
     unsigned int *all_cnt;
     double *negLogL;
     const sfh_df *tab;  // log table of the double-float Poisson terms
+    float eps_f;        // eps(T) (a power of two) in FP32
 };
 
 __device__ __forceinline__ void block_sum_to(double v, double *s_red, double *out_tid0) {
@@ -479,7 +480,7 @@ __global__ void __launch_bounds__(kThreads) k_fg_pass1_f32(Pass1Args a) {
     }
     // Poisson terms in double-float on the FP32 pipes (sfh_dfloat.cuh); eps(T) is a
     // power of two, exact in FP32.
-    const float eps_f = (float)a.eps;
+    const float eps_f = a.eps_f;
     sfh_df term{0.f, 0.f};
     for (int q = 0; q < 4; ++q) {
         const int64_t ii = rbase + (int64_t)q * blockDim.x + threadIdx.x;
@@ -502,25 +503,21 @@ __global__ void __launch_bounds__(kThreads) k_fg_pass1_f32(Pass1Args a) {
             ml += v.y;
         }
         sfh_df c = df_fast_two_sum(mh, ml);
-        if (!a.want_logl && !a.want_w) {  // composite only: data may be NULL
-            a.composite[ii] = (double)c.h + (double)c.l;
-            continue;
-        }
-        if (!a.want_w) a.composite[ii] = (double)c.h + (double)c.l;  // the model, unclamped
+        if (!a.want_w) a.composite[ii] = sfh_f2d(c.h) + sfh_f2d(c.l);  // the model, unclamped
+        if (!a.want_logl && !a.want_w) continue;  // composite only: data may be NULL
         if (c.h < eps_f || (c.h == eps_f && c.l < 0.f)) c = sfh_df{eps_f, 0.f};  // max(c, eps)
-        const double ni = a.data[ii];
-        const float nh = __double2float_rn(ni);
-        const float nl = __double2float_rn(ni - (double)nh);
+        float nh, nl;
+        sfh_split_double(a.data[ii], nh, nl);
         if (a.want_logl) term = df_add(term, df_poisson_term(c, nh, nl, s_tab));
         if (a.want_w) {
             const sfh_df diff = df_add(c, sfh_df{-nh, -nl});
             const float w = __fdiv_rn(diff.h, c.h);  // 1 - n/c
-            a.composite[ii] = (double)w;
+            a.composite[ii] = sfh_f2d(w);
             a.w32[ii] = make_float2(w, 0.f);
         }
     }
     double tile_sum = 0.0;
-    block_sum_to((double)term.h + (double)term.l, s_red, &tile_sum);
+    sfh_df_block_sum(term, s_red, &tile_sum);
     if (threadIdx.x == 0) {
         a.tile_cnt[tile] = 0u;  // re-arm for the next launch on this stream
         s_last = false;
@@ -610,10 +607,9 @@ __global__ void __launch_bounds__(kThreads) k_fg_pass2_f32(Pass2Args a) {
         } else {
             for (int ii = lane; ii < rn; ii += 32) two_sum_acc(ah, al, __ldg(col + ii) * s_w[ii]);
         }
-        double v = (double)ah + (double)al;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) a.partG[(int64_t)rc * nt + j] = v;
+        // warp sum in double-float on the FP32 pipes, one conversion per column
+        const sfh_df v = sfh_df_warp_sum(df_fast_two_sum(ah, al));
+        if (lane == 0) a.partG[(int64_t)rc * nt + j] = sfh_f2d(v.h) + sfh_f2d(v.l);
     }
     __threadfence();
     __syncthreads();
@@ -692,9 +688,10 @@ Plan make_plan(const sfh_ctx *ctx, int64_t nbins, int64_t nt, bool f64, bool fus
         // measured by sfh_models_autotune replaces these choices.
         const FusedOcc occ = fused_occupancy(nbins % 4 == 0);
         const int slots1 = occ.p1 * ctx->sm_count, slots2 = occ.p2 * ctx->sm_count;
-        const int w1 = (m && m->tune_w1 > 0) ? m->tune_w1 : 2;
         const int w2 = (m && m->tune_w2 > 0) ? m->tune_w2 : 1;
-        ks = (w1 * slots1 + p.nrowblk / 2) / p.nrowblk;
+        // rounded down, so the grid fills whole waves (a few leftover blocks would run
+        // as a nearly empty extra wave)
+        ks = (m && m->tune_ks > 0) ? m->tune_ks : (2 * slots1) / p.nrowblk;
         p.R = (m && m->tune_R > 0) ? m->tune_R : kFusedR;
         p.nchunks = (int)((nbins + p.R - 1) / p.R);
         const double per_block = (double)nt * p.nchunks / ((double)w2 * slots2);
@@ -764,6 +761,7 @@ int sfh_launch_fg(sfh_ctx *ctx, const sfh_models *m, const FgArgs &a, cudaEvent_
         p1.all_cnt = ctx->d_counters + SFH_CNT_FG_LOGL;
         p1.negLogL = a.negLogL;
         p1.tab = ctx->d_df_tab;
+        p1.eps_f = (float)a.eps;
         dim3 grid(p.ksplit, p.nrowblk);
         const size_t sm = 2 * (size_t)p.kchunk * sizeof(float);
         if (nbins % 4 == 0)
@@ -942,18 +940,31 @@ extern "C" int sfh_models_autotune(sfh_ctx *ctx, sfh_models *m, const double *d_
         t2 /= iters;
         return SFH_OK;
     };
-    const int W1[] = {1, 2, 3, 4}, RR[] = {1024, 2048, 4096}, W2[] = {1, 2, 4};
-    int best_w1 = 2, best_R = kFusedR, best_w2 = 1;
+    // pass-1 candidates: template splits filling 1/2 to 4 whole waves of resident blocks
+    const FusedOcc occ = fused_occupancy(m->nbins % 4 == 0);
+    const int slots1 = occ.p1 * ctx->sm_count;
+    const int nrowblk = (int)((m->nbins + 4 * kThreads - 1) / (4 * kThreads));
+    int KS[8], nks = 0;
+    for (int f2 : {1, 2, 3, 4, 6, 8}) {  // f2 / 2 waves
+        int ks = (f2 * slots1) / (2 * nrowblk);
+        ks = ks < 1 ? 1 : (ks > 64 ? 64 : ks);
+        if (ks > m->nt) ks = (int)m->nt;
+        bool dup = false;
+        for (int q = 0; q < nks; ++q) dup = dup || KS[q] == ks;
+        if (!dup) KS[nks++] = ks;
+    }
+    const int RR[] = {1024, 2048, 4096}, W2[] = {1, 2, 4};
+    int best_ks = KS[0], best_R = kFusedR, best_w2 = 1;
     double b1 = 1e300, b2 = 1e300, t1 = 0, t2 = 0;
     int rc = SFH_OK;
     m->tune_R = best_R;
     m->tune_w2 = best_w2;
-    for (int w1 : W1) {  // pass 1 (pass 2 fixed at the default)
-        m->tune_w1 = w1;
+    for (int q = 0; q < nks; ++q) {  // pass 1 (pass 2 fixed at the default)
+        m->tune_ks = KS[q];
         if ((rc = timed(t1, t2))) break;
-        if (t1 < b1) { b1 = t1; best_w1 = w1; }
+        if (t1 < b1) { b1 = t1; best_ks = KS[q]; }
     }
-    m->tune_w1 = best_w1;
+    m->tune_ks = best_ks;
     for (int r = 0; r < 3 && rc == SFH_OK; ++r)  // pass 2 with the chosen pass 1
         for (int w2 : W2) {
             m->tune_R = RR[r];
@@ -964,14 +975,14 @@ extern "C" int sfh_models_autotune(sfh_ctx *ctx, sfh_models *m, const double *d_
     for (int k = 0; k < 5; ++k) cudaEventDestroy(ev[k]);
     cudaFree(buf);
     if (rc) {
-        m->tune_w1 = m->tune_R = m->tune_w2 = 0;
+        m->tune_ks = m->tune_R = m->tune_w2 = 0;
         return rc;
     }
-    m->tune_w1 = best_w1;
+    m->tune_ks = best_ks;
     m->tune_R = best_R;
     m->tune_w2 = best_w2;
     if (plan_out) {
-        plan_out[0] = best_w1;
+        plan_out[0] = best_ks;
         plan_out[1] = best_R;
         plan_out[2] = best_w2;
     }

@@ -73,24 +73,20 @@ __device__ __forceinline__ void block_sum(double v, double *s_red, double *out) 
 // double-float (sfh_dfloat.cuh) and w = 1 - n / max(m, eps) (fitting_base.jl:90-93,
 // 274-280); composite receives w when the gradient is wanted, the model otherwise.
 __device__ __forceinline__ void bin_terms(float ah, float al, const double *__restrict__ data,
-                                          int64_t ii, double eps, int want_logl, int want_w,
+                                          int64_t ii, float eps_f, int want_logl, int want_w,
                                           const sfh_df *s_tab, double *__restrict__ composite,
                                           sfh_df &term, float &w) {
     sfh_df c = df_fast_two_sum(ah, al);
-    if (!want_logl && !want_w) {
-        composite[ii] = (double)c.h + (double)c.l;
-        return;
-    }
-    if (!want_w) composite[ii] = (double)c.h + (double)c.l;  // the model, unclamped
-    const float eps_f = (float)eps;  // eps(T) is a power of two, exact in FP32
+    if (!want_w) composite[ii] = sfh_f2d(c.h) + sfh_f2d(c.l);  // the model, unclamped
+    if (!want_logl && !want_w) return;
+    // max(composite, eps(T)); eps(T) is a power of two, exact in FP32
     if (c.h < eps_f || (c.h == eps_f && c.l < 0.f)) c = sfh_df{eps_f, 0.f};
-    const double n = data[ii];
-    const float nh = __double2float_rn(n);
-    const float nl = __double2float_rn(n - (double)nh);
+    float nh, nl;
+    sfh_split_double(data[ii], nh, nl);
     if (want_logl) term = df_add(term, df_poisson_term(c, nh, nl, s_tab));
     if (want_w) {
         w = __fdiv_rn(df_add(c, sfh_df{-nh, -nl}).h, c.h);
-        composite[ii] = (double)w;
+        composite[ii] = sfh_f2d(w);
     }
 }
 
@@ -98,7 +94,7 @@ __global__ void __launch_bounds__(kRT)
 k_ragged_pass1(const float *__restrict__ M, const GalDesc *__restrict__ gals,
                const RowTile *__restrict__ tiles, const double *__restrict__ coeffs,
                const double *__restrict__ data, double *__restrict__ composite,
-               float *__restrict__ w32, double *__restrict__ tile_logl, double eps,
+               float *__restrict__ w32, double *__restrict__ tile_logl, float eps,
                int want_logl, int want_w, const sfh_df *__restrict__ tab) {
     __shared__ float rhi[kRChunk], rlo[kRChunk];
     __shared__ double s_red[kRT / 32];
@@ -197,7 +193,7 @@ __global__ void __launch_bounds__(kRT)
 k_ragged_fused(const float *__restrict__ M, const GalDesc *__restrict__ gals,
                const RowTile *__restrict__ tiles, const double *__restrict__ coeffs,
                const double *__restrict__ data, double *__restrict__ composite,
-               double *__restrict__ tile_logl, double *__restrict__ gpart, double eps,
+               double *__restrict__ tile_logl, double *__restrict__ gpart, float eps,
                int want_logl, int want_g, const sfh_df *__restrict__ tab) {
     __shared__ float rhi[NT], rlo[NT];
     __shared__ double s_red[kRT / 32];
@@ -262,10 +258,10 @@ k_ragged_fused(const float *__restrict__ M, const GalDesc *__restrict__ gals,
     if (lane < NT) s_g[warp][lane] = v[0];
     __syncthreads();
     if (threadIdx.x < NT) {
-        double acc = 0.0;
+        sfh_df acc{0.f, 0.f};
 #pragma unroll
-        for (int wgi = 0; wgi < kRT / 32; ++wgi) acc += (double)s_g[wgi][threadIdx.x];
-        gpart[(int64_t)blockIdx.x * kFuseMax + threadIdx.x] = acc;
+        for (int wgi = 0; wgi < kRT / 32; ++wgi) acc = df_add_f(acc, s_g[wgi][threadIdx.x]);
+        gpart[(int64_t)blockIdx.x * kFuseMax + threadIdx.x] = sfh_f2d(acc.h) + sfh_f2d(acc.l);
     }
 }
 
@@ -432,7 +428,7 @@ extern "C" int sfh_fg_ragged_dev(sfh_ctx *ctx, const sfh_galaxies *gal, const do
                                               : k_ragged_fused<32>;
         kern<<<(unsigned)gal->n_fused_tiles, kRT, 0, st>>>(
             gal->d_models, desc, (const RowTile *)gal->d_fused, d_coeffs, d_data, d_composite, tf,
-            gp, eps, want_logl ? 1 : 0, want_w ? 1 : 0, ctx->d_df_tab);
+            gp, (float)eps, want_logl ? 1 : 0, want_w ? 1 : 0, ctx->d_df_tab);
         SFH_LAUNCHED(ctx);
         if (want_logl || want_w) {
             k_ragged_finish<<<(unsigned)gal->n_fused_gal, kRT, 0, st>>>(
@@ -444,7 +440,7 @@ extern "C" int sfh_fg_ragged_dev(sfh_ctx *ctx, const sfh_galaxies *gal, const do
     if (gal->n_big_gal) {
         k_ragged_pass1<<<(unsigned)gal->n_row_tiles, kRT, 0, st>>>(
             gal->d_models, desc, (const RowTile *)gal->d_rows, d_coeffs, d_data, d_composite, w32,
-            tl, eps, want_logl ? 1 : 0, want_w ? 1 : 0, ctx->d_df_tab);
+            tl, (float)eps, want_logl ? 1 : 0, want_w ? 1 : 0, ctx->d_df_tab);
         SFH_LAUNCHED(ctx);
         if (want_logl) {
             k_ragged_logl<<<(unsigned)gal->n_big_gal, kRT, 0, st>>>(

@@ -43,8 +43,8 @@ struct sfh_models {
     float *d_f32 = nullptr;
     int64_t nbins_pad = 0, nt_pad = 0;
     // Single-vector launch plan chosen by sfh_models_autotune (0 = built-in heuristics):
-    // pass-1 waves of resident blocks, pass-2 row chunk, pass-2 waves.
-    int tune_w1 = 0, tune_R = 0, tune_w2 = 0;
+    // pass-1 template splits, pass-2 row chunk, pass-2 waves.
+    int tune_ks = 0, tune_R = 0, tune_w2 = 0;
 };
 
 // Counter slots in sfh_ctx::d_counters (zeroed at context creation; every kernel that
@@ -113,6 +113,35 @@ __device__ __forceinline__ float sfh_log1p_minus_id(float d, float c, float n) {
     return log1pf(d) - d;
 }
 
+// Conversions between double and float without the FP64 pipe (GB300 retires FP64 and
+// FP64<->FP32 conversions at a small fraction of its FP32 rate).  Exact bit moves for the
+// common cases -- a double that holds a float value (counts), a normal float -- and the
+// ordinary conversion otherwise.
+__device__ __forceinline__ void sfh_split_double(double x, float &h, float &l) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned int e = (unsigned int)(b >> 52) & 0x7ffu;
+    if ((b << 1) == 0ull) {  // +-0
+        h = __uint_as_float((unsigned int)(b >> 32));
+        l = 0.f;
+    } else if ((b & 0x1fffffffull) == 0ull && e >= 897u && e <= 1150u) {  // a normal float
+        h = __uint_as_float(((unsigned int)(b >> 32) & 0x80000000u) | ((e - 896u) << 23) |
+                            (unsigned int)((b >> 29) & 0x7fffffull));
+        l = 0.f;
+    } else {
+        h = __double2float_rn(x);
+        l = __double2float_rn(x - (double)h);
+    }
+}
+__device__ __forceinline__ double sfh_f2d(float f) {
+    const unsigned int u = __float_as_uint(f);
+    const unsigned int e = (u >> 23) & 0xffu;
+    const unsigned long long s = (unsigned long long)(u & 0x80000000u) << 32;
+    if ((u << 1) == 0u) return __longlong_as_double((long long)s);  // +-0
+    if (e == 0u || e == 0xffu) return (double)f;                     // subnormal, inf, nan
+    return __longlong_as_double((long long)(s | ((unsigned long long)(e + 896u) << 52) |
+                                            ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+
 // Sum of a double-float over the warp (all lanes receive it), FP32 operations only.
 __device__ __forceinline__ sfh_df sfh_df_warp_sum(sfh_df v) {
 #pragma unroll
@@ -128,7 +157,7 @@ __device__ __forceinline__ sfh_df sfh_df_warp_sum(sfh_df v) {
 __device__ __forceinline__ void sfh_df_block_sum(sfh_df v, double *s_red, double *out) {
     v = sfh_df_warp_sum(v);
     __syncthreads();
-    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = (double)v.h + (double)v.l;
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = sfh_f2d(v.h) + sfh_f2d(v.l);
     __syncthreads();
     if (threadIdx.x == 0) {
         double b = 0.0;

@@ -117,7 +117,7 @@ class Models:
     def autotune(self, coeffs, data, iters=10, eps=None):
         """Pick the fastest single-vector fg! launch plan for this matrix by timing the
         candidates on the device (sfh_models_autotune).  Returns
-        {"plan": (pass-1 waves, pass-2 rows, pass-2 waves), "ms": (pass 1, pass 2)}."""
+        {"plan": (pass-1 template splits, pass-2 rows, pass-2 waves), "ms": (pass 1, pass 2)}."""
         import torch
         dev = torch.device("cuda", self.ctx.device)
         r = torch.as_tensor(np.asarray(coeffs, dtype=np.float64), device=dev).contiguous()

@@ -180,8 +180,8 @@ def test_autotuned_plan_keeps_parity(sfh, O):
     M, r, data = _problem(60000, 96, seed=7)
     H = sfh.Models(M, storage="f32")
     res = H.autotune(r, data, iters=3)
-    w1, R, w2 = res["plan"]
-    assert w1 in (1, 2, 3, 4) and R in (1024, 2048, 4096) and w2 in (1, 2, 4)
+    ks, R, w2 = res["plan"]
+    assert 1 <= ks <= 64 and R in (1024, 2048, 4096) and w2 in (1, 2, 4)
     assert all(t > 0 for t in res["ms"])
     comp = np.empty(M.shape[0])
     G = np.empty(M.shape[1])
