@@ -75,6 +75,14 @@ int sfh_models_upload(sfh_ctx *ctx, const void *host_models, int src_dtype, int6
 int sfh_models_from_device(sfh_ctx *ctx, const float *dev_models_f32, int64_t nbins,
                            int64_t ntempl, int storage, sfh_models **out);
 int sfh_models_free(sfh_models *models);
+/* New matrix whose column g is Σ_q w_q M[:, cols_q] over q in [h_group_off[g],
+   h_group_off[g+1]) (FP32 source storage; result stored as `storage`).  With one group per
+   unique age and the relative weights of a fixed age-metallicity relation this is the
+   expansion coeffs[idxs] = relweights[idxs] .* x[i] of fixed_amr
+   (hierarchical/fixed_amr.jl:106-113), done once so every fg! reads n_ages columns. */
+int sfh_models_combine(sfh_ctx *ctx, const sfh_models *models, int64_t ngroups,
+                       const int64_t *h_group_off, const int32_t *h_cols,
+                       const double *h_weights, int storage, sfh_models **out);
 int sfh_models_info(const sfh_models *models, int64_t *nbins, int64_t *ntempl, int *storage);
 
 /* ---------------------------------------------------------------- host-array drop-ins
@@ -156,8 +164,13 @@ int sfh_fg_batched_dev(sfh_ctx *ctx, const sfh_models *models, const double *d_R
 /* ---------------------------------------------------------------- batched HMC */
 enum sfh_hmc_model {
     SFH_HMC_DIRECT = 0, /* θ = log coeffs: hmc_sample's log density, hmc_sample.jl:24-37 */
-    SFH_HMC_MZR = 1     /* PowerLawMZR + GaussianDispersion: sample_sfh's log density,
+    SFH_HMC_MZR = 1,    /* PowerLawMZR + GaussianDispersion: sample_sfh's log density,
                            generic_fitting.jl:90-199 with mzr.jl:50-215 */
+    SFH_HMC_LINEAR_AMR = 2, /* LinearAMR + GaussianDispersion: generic_fitting.jl:90-199 with
+                               amr.jl:50-160, 205-213 (μ_j = β + α (T_max - t_j)) */
+    SFH_HMC_LOG_AMR = 3     /* LogarithmicAMR with the default MH_from_Z (utilities.jl:138-155)
+                               + GaussianDispersion: amr.jl:278-290, θ = [log R, log α, log β,
+                               log σ] (transforms (1, 1)) */
 };
 typedef struct {
     int32_t nchains;        /* chains advanced together (one batched gradient per step) */
@@ -169,7 +182,7 @@ typedef struct {
     double step0;           /* initial leapfrog step */
     double target_accept;   /* dual-averaging target acceptance (e.g. 0.8) */
     uint64_t seed;          /* Philox key */
-    /* SFH_HMC_MZR only: ages and metallicities of the templates */
+    /* SFH_HMC_MZR and the AMR models: ages and metallicities of the templates */
     int32_t nages;
     const int32_t *h_age_index; /* per template: its age, 0..nages-1 */
     const double *h_logAge;     /* per age (any order) */
@@ -177,6 +190,7 @@ typedef struct {
     double logMstar0;           /* PowerLawMZR logMstar0 (fixed), mzr.jl:263-272 */
     int32_t alpha_free, beta_free, sigma_free;
     double alpha, beta, sigma;  /* values of parameters held fixed */
+    double T_max;               /* the AMR models: earliest lookback time in Gyr */
 } sfh_hmc_config;
 
 /* Batched HMC over all chains at once, every leapfrog step one sfh_fg_batched_dev-style
@@ -189,6 +203,8 @@ typedef struct {
    d_mean / d_var (nchains x D) posterior mean and variance of the natural parameters
    (exp of the log-transformed ones), d_accept (nchains) mean acceptance, d_step
    (nchains) final step, d_draws (nchains x ceil(ntraj/thin) x D) FP32 natural draws.
+   SFH_HMC_LINEAR_AMR uses the MZR layout with [log R_j..., log α, β, log σ] (amr.jl:212
+   transforms (1, 0) for α, β).
    Models must be stored as SFH_BF16X2.  The call returns after the run completes. */
 int sfh_hmc_sample_dev(sfh_ctx *ctx, const sfh_models *models, const double *d_data,
                        const sfh_hmc_config *cfg, const double *d_theta0, double *d_mean,

@@ -117,6 +117,15 @@ def lib():
             L.sfho_mlp_loss_grad.restype = C.c_double
             L.sfho_poisson_deviance.argtypes = [_dp, _dp, _i64]
             L.sfho_poisson_deviance.restype = C.c_double
+            L.sfho_linear_amr.argtypes = [C.c_double] * 4
+            L.sfho_linear_amr.restype = C.c_double
+            L.sfho_mh_from_z.argtypes = [C.c_double]
+            L.sfho_mh_from_z.restype = C.c_double
+            L.sfho_dmh_dz.argtypes = [C.c_double]
+            L.sfho_dmh_dz.restype = C.c_double
+            L.sfho_amr_fg.argtypes = [C.c_int, _dp, _i64, C.c_double, C.c_int, C.c_int, C.c_int,
+                                      _dp, _dp, _i64, _i64, _dp, _dp, C.c_double, C.c_void_p]
+            L.sfho_amr_fg.restype = C.c_double
             L.sfho_set_threads.argtypes = [C.c_int]
             L.sfho_get_max_threads.restype = C.c_int
             _lib = L
@@ -346,6 +355,36 @@ def mzr_fg(variables, logMstar0, M, n, logAge, MH, free=(True, True, True), want
     nb, nt = M.shape
     G = np.empty(variables.size) if want_g else None
     v = lib().sfho_mzr_fg(variables, nages, float(logMstar0), int(free[0]), int(free[1]),
+                          int(free[2]), M.ravel(order="F"), _f64(n), nb, nt, _f64(logAge),
+                          _f64(MH), eps, G.ctypes.data if want_g else None)
+    return v, G
+
+
+def linear_amr(alpha, beta, T_max, logAge):
+    """LinearAMR(α, β, T_max)(logAge), amr.jl:205."""
+    return lib().sfho_linear_amr(float(alpha), float(beta), float(T_max), float(logAge))
+
+
+def mh_from_z(Z):
+    """MH_from_Z(Z) with the package defaults, src/utilities.jl:138-145."""
+    return lib().sfho_mh_from_z(float(Z))
+
+
+def dmh_dz(Z):
+    """dMH_dZ(Z), src/utilities.jl:152-155."""
+    return lib().sfho_dmh_dz(float(Z))
+
+
+def amr_fg(variables, T_max, M, n, logAge, MH, free=(True, True, True), want_g=True,
+           eps=eps_of(np.float64), kind=0):
+    """fg!(F, G, AMR, GaussianDispersion, variables, ...), amr.jl:78-160; kind 0 LinearAMR,
+    kind 1 LogarithmicAMR (MH_from_Z)."""
+    variables = _f64(variables)
+    nages = variables.size - 3
+    M = np.asfortranarray(M, dtype=np.float64)
+    nb, nt = M.shape
+    G = np.empty(variables.size) if want_g else None
+    v = lib().sfho_amr_fg(int(kind), variables, nages, float(T_max), int(free[0]), int(free[1]),
                           int(free[2]), M.ravel(order="F"), _f64(n), nb, nt, _f64(logAge),
                           _f64(MH), eps, G.ctypes.data if want_g else None)
     return v, G

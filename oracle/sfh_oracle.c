@@ -650,6 +650,92 @@ double sfho_mzr_fg(const double *variables, int64_t nages, double logMstar0, int
     return -logL;
 }
 
+/* LinearAMR(α, β, T_max)(logAge) = β + α (T_max - 10^(logAge - 9)), amr.jl:205 */
+double sfho_linear_amr(double alpha, double beta, double T_max, double logAge) {
+    return beta + alpha * (T_max - pow(10.0, logAge - 9.0));
+}
+
+/* fg!(F, G, ::AbstractAMR, ::AbstractDispersionModel, variables, ...), amr.jl:78-160, for
+   LinearAMR + GaussianDispersion: calculate_coeffs (amr.jl:50-72), composite, logL, then
+   the chain rule to (R_j, α, β, σ) -- no cross-age terms, μ_j depends on age only. */
+/* MH_from_Z(Z) and dMH_dZ(Z) with the defaults solZ = 0.01524, Y_p = 0.2485, γ = 1.78,
+   src/utilities.jl:117-155 (X = 1 - (Y_p + γ Z + Z)). */
+double sfho_mh_from_z(double Z) {
+    const double Yp = 0.2485, g = 1.78, solZ = 0.01524;
+    const double X = 1.0 - (Yp + g * Z + Z), Xsol = 1.0 - (Yp + g * solZ + solZ);
+    return X > 0 ? log10(Z / (X * solZ) * Xsol) : NAN;
+}
+double sfho_dmh_dz(double Z) {
+    const double Yp = 0.2485, g = 1.78;
+    return (Yp - 1.0) / (log(10.0) * Z * (Yp + Z + g * Z - 1.0));
+}
+
+double sfho_amr_fg(int kind, const double *variables, int64_t nages, double T_max,
+                   int alpha_free, int beta_free, int sigma_free, const double *M,
+                   const double *n, int64_t nbins, int64_t nt, const double *logAge,
+                   const double *MH, double eps, double *G) {
+    const double alpha = variables[nages], beta = variables[nages + 1], sigma = variables[nages + 2];
+    double *uniq = (double *)malloc(sizeof(double) * (size_t)nt);
+    int64_t *jidx = (int64_t *)malloc(sizeof(int64_t) * (size_t)nt);
+    const int64_t nu = unique_ages(logAge, nt, uniq, jidx);
+    if (nu != nages) {
+        free(uniq);
+        free(jidx);
+        return NAN;
+    }
+    double *mu = (double *)malloc(sizeof(double) * (size_t)nages);
+    double *Avec = (double *)calloc((size_t)nages, sizeof(double));
+    double *Ajk = (double *)malloc(sizeof(double) * (size_t)nt);
+    double *coeffs = (double *)malloc(sizeof(double) * (size_t)nt);
+    for (int64_t j = 0; j < nages; ++j)
+        mu[j] = kind == 1 ? sfho_mh_from_z(beta + alpha * (T_max - pow(10.0, uniq[j] - 9.0)))
+                          : sfho_linear_amr(alpha, beta, T_max, uniq[j]);
+    for (int64_t k = 0; k < nt; ++k) {
+        Ajk[k] = sfho_gauss_disp(sigma, MH[k], mu[jidx[k]]);
+        Avec[jidx[k]] += Ajk[k];
+    }
+    for (int64_t k = 0; k < nt; ++k) coeffs[k] = Ajk[k] * variables[jidx[k]] / Avec[jidx[k]];
+    double *c = (double *)malloc(sizeof(double) * (size_t)nbins);
+    sfho_composite(M, nbins, nt, coeffs, c);
+    const double logL = sfho_loglikelihood(c, n, nbins, eps);
+    if (G) {
+        double *fullG = (double *)malloc(sizeof(double) * (size_t)nt);
+        sfho_grad_inplace(fullG, c, M, n, nbins, nt, eps); /* ∂logL/∂r_{j,k} */
+        for (int64_t q = 0; q < nages + 3; ++q) G[q] = 0.0;
+        for (int64_t j = 0; j < nages; ++j) {
+            const double Rj = variables[j], A = Avec[j];
+            /* ∂μ/∂α, ∂μ/∂β: LinearAMR amr.jl:207-209; LogarithmicAMR amr.jl:280-288 */
+            const double dt = T_max - pow(10.0, uniq[j] - 9.0);
+            const double dz = kind == 1 ? sfho_dmh_dz(beta + alpha * dt) : 1.0;
+            const double gmu_a = dz * dt, gmu_b = dz;
+            double ks_dmu = 0.0, ks_dsig = 0.0;
+            for (int64_t k = 0; k < nt; ++k) {
+                if (jidx[k] != j) continue;
+                const double d = MH[k] - mu[j];
+                ks_dmu += Ajk[k] * d / (sigma * sigma);
+                ks_dsig += Ajk[k] * d * d / (sigma * sigma * sigma);
+            }
+            double gR = 0.0, psum = 0.0, ssum = 0.0;
+            for (int64_t k = 0; k < nt; ++k) {
+                if (jidx[k] != j) continue;
+                const double d = MH[k] - mu[j];
+                const double dAmu = Ajk[k] * d / (sigma * sigma);
+                const double dAs = Ajk[k] * d * d / (sigma * sigma * sigma);
+                gR -= fullG[k] * coeffs[k] / Rj;                              /* amr.jl:133 */
+                psum -= fullG[k] * Rj / A * (dAmu - Ajk[k] / A * ks_dmu);     /* :143-144 */
+                ssum += fullG[k] * Rj / A * (dAs - Ajk[k] / A * ks_dsig);     /* :150-156 */
+            }
+            G[j] = gR;
+            if (alpha_free) G[nages] += psum * gmu_a;
+            if (beta_free) G[nages + 1] += psum * gmu_b;
+            if (sigma_free) G[nages + 2] -= ssum;
+        }
+        free(fullG);
+    }
+    free(uniq); free(jidx); free(mu); free(Avec); free(Ajk); free(coeffs); free(c);
+    return -logL;
+}
+
 /* ======================= learned template emulator (no reference counterpart) ====== */
 /* A plain FP64 restatement of the device MLP: the forward pass, the backward pass of
    the mean-squared-error loss, and the Poisson deviance used as the judge. */

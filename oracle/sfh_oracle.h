@@ -128,6 +128,19 @@ double sfho_mzr_fg(const double *variables, int64_t nages, double logMstar0,
                    const double *n, int64_t nbins, int64_t nt, const double *logAge,
                    const double *MH, double eps, double *G);
 
+/* LinearAMR(α, β, T_max)(logAge), amr.jl:205 */
+double sfho_linear_amr(double alpha, double beta, double T_max, double logAge);
+/* MH_from_Z / dMH_dZ with the package defaults, src/utilities.jl:117-155 */
+double sfho_mh_from_z(double Z);
+double sfho_dmh_dz(double Z);
+/* fg! for an AMR + GaussianDispersion, amr.jl:78-160: kind 0 LinearAMR (amr.jl:205-213),
+   kind 1 LogarithmicAMR with MH_from_Z (amr.jl:278-290).  variables = [R_1..R_nages, α, β,
+   σ], ages in order of first appearance in logAge.  Returns -logL. */
+double sfho_amr_fg(int kind, const double *variables, int64_t nages, double T_max,
+                   int alpha_free, int beta_free, int sigma_free, const double *M,
+                   const double *n, int64_t nbins, int64_t nt, const double *logAge,
+                   const double *MH, double eps, double *G);
+
 /* ---------------- learned template emulator (no reference counterpart) ---------------- */
 /* MLP in -> h1 -> h2 -> out with GELU (erf form) after the two hidden layers.
    Parameter block (row-major): W1 (h1 x in), b1 (h1), W2 (h2 x h1), b2 (h2),

@@ -52,8 +52,9 @@ extern "C" int sfh_ctx_create(int device, sfh_ctx **out) {
     sfh_ctx *ctx = new sfh_ctx();
     ctx->device = device;
     ctx->sm_count = prop.multiProcessorCount;
-    sfh_df tab[129];
+    sfh_df tab[SFH_DF_TAB_ALL];
     sfh_df_log_table(tab);
+    sfh_df_nlogn_table(tab + SFH_DF_TAB_LOG);
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc(&ctx->d_counters, sizeof(unsigned int) * SFH_CNT_SLOTS) != cudaSuccess ||
         cudaMemset(ctx->d_counters, 0, sizeof(unsigned int) * SFH_CNT_SLOTS) != cudaSuccess ||
@@ -238,6 +239,80 @@ extern "C" int sfh_models_from_device(sfh_ctx *ctx, const float *dev, int64_t nb
     if (rc != SFH_OK) { free_models(m); return rc; }
     *out = m;
     return SFH_OK;
+}
+
+// ------------------------------------------------------------------ combined templates
+namespace {
+// out[:, g] = Σ_{q in group g} w_q M[:, col_q] for FP32 (nbins, nt) column-major M; one
+// thread per bin, compensated FP32 accumulation of the FP32 products w_q M (w split hi/lo).
+__global__ void k_combine_columns(const float *__restrict__ M, int64_t nbins,
+                                  const int64_t *__restrict__ goff, const int32_t *__restrict__ cols,
+                                  const float2 *__restrict__ w, int64_t ngroups,
+                                  float *__restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nbins) return;
+    for (int64_t g = 0; g < ngroups; ++g) {
+        float h = 0.f, l = 0.f;
+        for (int64_t q = goff[g]; q < goff[g + 1]; ++q) {
+            const float2 wq = w[q];  // weight as an FP32 hi/lo pair
+            const float m = __ldg(M + (int64_t)cols[q] * nbins + i);
+            sfh_two_sum_acc(h, l, fmaf(m, wq.x, m * wq.y));
+        }
+        out[g * nbins + i] = h + l;
+    }
+}
+}  // namespace
+
+extern "C" int sfh_models_combine(sfh_ctx *ctx, const sfh_models *models, int64_t ngroups,
+                                  const int64_t *h_group_off, const int32_t *h_cols,
+                                  const double *h_weights, int storage, sfh_models **out) {
+    if (!ctx || !models || !h_group_off || !h_cols || !h_weights || !out || ngroups < 1)
+        return SFH_ERR_ARG;
+    *out = nullptr;
+    if (!models->d_f32) return sfh_set_error(ctx, SFH_ERR_UNSUPPORTED, "needs FP32 template storage");
+    if (storage != SFH_F32 && storage != SFH_BF16X2) return SFH_ERR_ARG;
+    const int64_t nq = h_group_off[ngroups];
+    if (h_group_off[0] != 0 || nq < 1) return sfh_set_error(ctx, SFH_ERR_ARG, "bad group offsets");
+    for (int64_t g = 0; g < ngroups; ++g)
+        if (h_group_off[g + 1] < h_group_off[g]) return sfh_set_error(ctx, SFH_ERR_ARG, "bad group offsets");
+    for (int64_t q = 0; q < nq; ++q)
+        if (h_cols[q] < 0 || h_cols[q] >= models->nt)
+            return sfh_set_error(ctx, SFH_ERR_SHAPE, "template index out of range");
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    const int64_t nbins = models->nbins;
+    std::vector<float2> wf((size_t)nq);  // weights split into FP32 hi/lo on the host
+    for (int64_t q = 0; q < nq; ++q) {
+        const float wh = (float)h_weights[q];
+        wf[(size_t)q] = make_float2(wh, (float)(h_weights[q] - (double)wh));
+    }
+    void *buf = nullptr;
+    const size_t o_off = 0, o_cols = sfh_align256((size_t)(ngroups + 1) * 8);
+    const size_t o_w = o_cols + sfh_align256((size_t)nq * 4);
+    const size_t o_out = o_w + sfh_align256((size_t)nq * 8);
+    const size_t total = o_out + (size_t)ngroups * nbins * sizeof(float);
+    SFH_CK(ctx, cudaMalloc(&buf, total));
+    char *b = (char *)buf;
+    cudaError_t e = cudaMemcpyAsync(b + o_off, h_group_off, (size_t)(ngroups + 1) * 8,
+                                    cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b + o_cols, h_cols, (size_t)nq * 4, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b + o_w, wf.data(), (size_t)nq * 8, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) {
+        cudaFree(buf);
+        return sfh_cuda_error(ctx, e, "combine upload");
+    }
+    k_combine_columns<<<(unsigned)((nbins + 255) / 256), 256, 0, ctx->stream>>>(
+        models->d_f32, nbins, (const int64_t *)(b + o_off), (const int32_t *)(b + o_cols),
+        (const float2 *)(b + o_w), ngroups, (float *)(b + o_out));
+    ctx->launches++;
+    e = cudaGetLastError();
+    int rc = e == cudaSuccess ? SFH_OK : sfh_cuda_error(ctx, e, "k_combine_columns");
+    if (rc == SFH_OK) rc = sfh_models_from_device(ctx, (const float *)(b + o_out), nbins, ngroups,
+                                                  storage, out);
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(buf);
+    return rc;
 }
 
 // ------------------------------------------------------------------ host-array entry points

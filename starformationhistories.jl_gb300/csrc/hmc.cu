@@ -93,10 +93,11 @@ struct HmcConst {
     uint64_t seed;
     int thin;
     int64_t ndraws;
-    int model;   // 0 direct, 1 MZR
+    int model;   // 0 direct, 1 PowerLawMZR, 2 LinearAMR, 3 LogarithmicAMR
     int nages;
     int alpha_free, beta_free, sigma_free;
     double alpha, beta, sigma, logM0;
+    double T_max;  // LinearAMR / LogarithmicAMR: earliest lookback time (Gyr)
 };
 
 // ---------------------------------------------------------------- trajectory kernels
@@ -262,11 +263,24 @@ struct MzrDev {
     const int *age_off;      // CSR: templates of age j
     const int *age_tmpl;
     const int *sorted;       // ages by decreasing logAge (sortperm(unique_logAge; rev=true))
+    const double *tage;      // LinearAMR: lookback time of each age in Gyr, 10^(logAge - 9)
     double *aux;             // B x (4 nages): cum, mu, Asum, (spare)
     double *A;               // B x nt Gaussian weights A_jk
 };
 
-// calculate_coeffs (mzr.jl:50-79) per chain: one block per chain.
+// MH_from_Z and dMH_dZ with the package defaults (solZ 0.01524, Y_p 0.2485, γ 1.78),
+// src/utilities.jl:117-155: [M/H] of a metal mass fraction Z for LogarithmicAMR.
+__device__ __forceinline__ double mh_from_z(double Z) {
+    const double Yp = 0.2485, g = 1.78, solZ = 0.01524;
+    const double X = 1.0 - (Yp + g * Z + Z), Xsol = 1.0 - (Yp + g * solZ + solZ);
+    return X > 0.0 ? log10(Z / (X * solZ) * Xsol) : NAN;
+}
+__device__ __forceinline__ double dmh_dz(double Z) {
+    const double Yp = 0.2485, g = 1.78;
+    return (Yp - 1.0) / (2.302585092994046 * Z * (Yp + Z + g * Z - 1.0));
+}
+
+// calculate_coeffs (mzr.jl:50-79, amr.jl:50-72) per chain: one block per chain.
 __global__ void k_mzr_map(const double *__restrict__ theta, HmcConst c, MzrDev z,
                           double *__restrict__ r) {
     const int b = blockIdx.x;
@@ -275,16 +289,24 @@ __global__ void k_mzr_map(const double *__restrict__ theta, HmcConst c, MzrDev z
     double alpha = c.alpha, beta = c.beta, sigma = c.sigma;
     int q = z.nages;
     if (c.alpha_free) alpha = exp(th[q++]);
-    if (c.beta_free) beta = th[q++];
+    if (c.beta_free) beta = (c.model == 3) ? exp(th[q++]) : th[q++];  // LogarithmicAMR: β > 0
     if (c.sigma_free) sigma = exp(th[q++]);
     if (threadIdx.x == 0) {
-        double acc = 0.0;  // cumsum in decreasing-age order
-        for (int p = 0; p < z.nages; ++p) {
-            const int j = z.sorted[p];
-            acc += exp(th[j]);
-            cum[j] = acc;
+        if (c.model == 2) {
+            // LinearAMR: μ_j = β + α (T_max - t_j), amr.jl:205
+            for (int j = 0; j < z.nages; ++j) mu[j] = beta + alpha * (c.T_max - z.tage[j]);
+        } else if (c.model == 3) {
+            // LogarithmicAMR: μ_j = MH_from_Z(β + α (T_max - t_j)), amr.jl:278
+            for (int j = 0; j < z.nages; ++j) mu[j] = mh_from_z(beta + alpha * (c.T_max - z.tage[j]));
+        } else {
+            double acc = 0.0;  // cumsum in decreasing-age order
+            for (int p = 0; p < z.nages; ++p) {
+                const int j = z.sorted[p];
+                acc += exp(th[j]);
+                cum[j] = acc;
+            }
+            for (int j = 0; j < z.nages; ++j) mu[j] = beta + alpha * (log10(cum[j]) - c.logM0);
         }
-        for (int j = 0; j < z.nages; ++j) mu[j] = beta + alpha * (log10(cum[j]) - c.logM0);
     }
     __syncthreads();
     double *A = z.A + (int64_t)b * z.nt;
@@ -307,6 +329,8 @@ __global__ void k_mzr_map(const double *__restrict__ theta, HmcConst c, MzrDev z
 
 // Chain rule of mzr.jl:131-209 (gradient of -logL w.r.t. R_j, α, β, σ) followed by the
 // transforms and Jacobian terms of generic_fitting.jl:143-171; writes ∇ log p and log p.
+// For LinearAMR (amr.jl:122-157) μ_j depends on the age only: ∂μ/∂R = 0 removes the
+// cross-age terms and ∂μ/∂α = T_max - t_j.
 __global__ void k_mzr_grad(const double *__restrict__ theta, const double *__restrict__ r,
                            const float *__restrict__ Gfg, const double *__restrict__ negL,
                            HmcConst c, MzrDev z, double *__restrict__ g, double *__restrict__ logd,
@@ -326,18 +350,18 @@ __global__ void k_mzr_grad(const double *__restrict__ theta, const double *__res
     const double *cum = z.aux + (int64_t)b * 4 * na, *mu = cum + na, *Asum = mu + na;
     const double *A = z.A + (int64_t)b * z.nt;
     const float *G = Gfg + (int64_t)b * z.nt;
-    double alpha = c.alpha, sigma = c.sigma;
+    double alpha = c.alpha, beta = c.beta, sigma = c.sigma;
     {
         int q = na;
         if (c.alpha_free) alpha = exp(th[q++]);
-        if (c.beta_free) ++q;
+        if (c.beta_free) beta = (c.model == 3) ? exp(th[q++]) : th[q++];
         if (c.sigma_free) sigma = exp(th[q++]);
     }
     const double ln10 = 2.302585092994046;
     // per-age sums in fixed template order (deterministic)
     for (int j = threadIdx.x; j < na; j += blockDim.x) {
         const double Rj = exp(th[j]);
-        const double dmu_dR = alpha / cum[j] / ln10;
+        const double dmu_dR = (c.model >= 2) ? 0.0 : alpha / cum[j] / ln10;
         double sR = 0.0, sM = 0.0, sS = 0.0;
         for (int q2 = z.age_off[j]; q2 < z.age_off[j + 1]; ++q2) {
             const int k = z.age_tmpl[q2];
@@ -379,8 +403,11 @@ __global__ void k_mzr_grad(const double *__restrict__ theta, const double *__res
         }
         for (int j = 0; j < na; ++j) {
             Gv[j] -= t1[j];
-            Gv[na] += ps[j] * (log10(cum[j]) - c.logM0);  // ∂μ/∂α
-            Gv[na + 1] += ps[j];                          // ∂μ/∂β = 1
+            // ∂μ/∂α and ∂μ/∂β: mzr.jl:279-281, amr.jl:207-209, amr.jl:280-288
+            const double dt = c.T_max - z.tage[j];
+            const double dz = (c.model == 3) ? dmh_dz(beta + alpha * dt) : 1.0;
+            Gv[na] += ps[j] * ((c.model >= 2) ? dz * dt : log10(cum[j]) - c.logM0);
+            Gv[na + 1] += ps[j] * dz;
             Gv[na + 2] -= ss[j];
         }
         // ∇ log p over the free variables; log p = logL + Σ log(positive x)
@@ -393,7 +420,11 @@ __global__ void k_mzr_grad(const double *__restrict__ theta, const double *__res
         }
         int q = na;
         if (c.alpha_free) { gb[q] = -Gv[na] * alpha + 1.0; jac += th[q]; ++q; }
-        if (c.beta_free) { gb[q] = -Gv[na + 1]; ++q; }
+        if (c.beta_free) {
+            if (c.model == 3) { gb[q] = -Gv[na + 1] * beta + 1.0; jac += th[q]; }  // log β
+            else gb[q] = -Gv[na + 1];
+            ++q;
+        }
         if (c.sigma_free) { gb[q] = -Gv[na + 2] * sigma + 1.0; jac += th[q]; ++q; }
         if (want_logd) logd[b] = -negL[b] + jac;
     }
@@ -514,10 +545,16 @@ int setup_run(sfh_ctx *ctx, const sfh_models *m, const double *d_data, const sfh
     std::vector<int> jidx, age_off, age_tmpl, sorted;
     if (c.model == SFH_HMC_DIRECT) {
         c.D = nt;
-    } else if (c.model == SFH_HMC_MZR) {
+    } else if (c.model == SFH_HMC_MZR || c.model == SFH_HMC_LINEAR_AMR ||
+               c.model == SFH_HMC_LOG_AMR) {
         if (cfg->nages < 1 || !cfg->h_age_index || !cfg->h_logAge || !cfg->h_MH ||
             !(cfg->alpha >= 0) || !(cfg->sigma > 0))
-            return sfh_set_error(ctx, SFH_ERR_ARG, "invalid MZR description");
+            return sfh_set_error(ctx, SFH_ERR_ARG, "invalid metallicity model description");
+        if ((c.model == SFH_HMC_LINEAR_AMR || c.model == SFH_HMC_LOG_AMR) && !(cfg->T_max > 0))
+            return sfh_set_error(ctx, SFH_ERR_ARG, "an AMR needs T_max > 0");  // amr.jl:188
+        if (c.model == SFH_HMC_LOG_AMR && !(cfg->beta > 0))
+            return sfh_set_error(ctx, SFH_ERR_ARG, "LogarithmicAMR needs β > 0");
+        c.T_max = cfg->T_max;
         c.nages = cfg->nages;
         c.alpha_free = cfg->alpha_free ? 1 : 0;
         c.beta_free = cfg->beta_free ? 1 : 0;
@@ -573,7 +610,10 @@ int setup_run(sfh_ctx *ctx, const sfh_models *m, const double *d_data, const sfh
     h.d_r = (double *)alloc((size_t)c.B * nt * 8);
     h.d_negL = (double *)alloc(c.B * 8);
     h.d_G = (float *)alloc((size_t)c.B * nt * 4);
-    if (c.model == SFH_HMC_MZR) {
+    if (c.model == SFH_HMC_MZR || c.model == SFH_HMC_LINEAR_AMR || c.model == SFH_HMC_LOG_AMR) {
+        std::vector<double> tage(c.nages);
+        for (int j = 0; j < c.nages; ++j) tage[j] = std::pow(10.0, cfg->h_logAge[j] - 9.0);
+        double *dta = (double *)alloc(c.nages * 8);
         int *dj = (int *)alloc(nt * 4), *dao = (int *)alloc((c.nages + 1) * 4);
         int *dat = (int *)alloc(nt * 4), *dso = (int *)alloc(c.nages * 4);
         double *dmh = (double *)alloc(nt * 8);
@@ -586,6 +626,8 @@ int setup_run(sfh_ctx *ctx, const sfh_models *m, const double *d_data, const sfh
         cudaMemcpy(dat, age_tmpl.data(), nt * 4, cudaMemcpyHostToDevice);
         cudaMemcpy(dso, sorted.data(), c.nages * 4, cudaMemcpyHostToDevice);
         cudaMemcpy(dmh, cfg->h_MH, nt * 8, cudaMemcpyHostToDevice);
+        cudaMemcpy(dta, tage.data(), c.nages * 8, cudaMemcpyHostToDevice);
+        h.z.tage = dta;
         h.z.nt = nt;
         h.z.nages = c.nages;
         h.z.jidx = dj;

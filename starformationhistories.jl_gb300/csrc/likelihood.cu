@@ -473,9 +473,9 @@ __global__ void __launch_bounds__(kThreads) k_fg_pass1_f32(Pass1Args a) {
     __threadfence();
     const int ks = nsplit;
     const int64_t rbase = (int64_t)tile * blockDim.x * 4;
-    __shared__ sfh_df s_tab[129];
+    __shared__ sfh_df s_tab[SFH_DF_TAB_ALL];
     if (a.want_logl) {
-        for (int k = threadIdx.x; k < 129; k += blockDim.x) s_tab[k] = a.tab[k];
+        for (int k = threadIdx.x; k < SFH_DF_TAB_ALL; k += blockDim.x) s_tab[k] = a.tab[k];
         __syncthreads();
     }
     // Poisson terms in double-float on the FP32 pipes (sfh_dfloat.cuh); eps(T) is a
@@ -508,7 +508,8 @@ __global__ void __launch_bounds__(kThreads) k_fg_pass1_f32(Pass1Args a) {
         if (c.h < eps_f || (c.h == eps_f && c.l < 0.f)) c = sfh_df{eps_f, 0.f};  // max(c, eps)
         float nh, nl;
         sfh_split_double(a.data[ii], nh, nl);
-        if (a.want_logl) term = df_add(term, df_poisson_term(c, nh, nl, s_tab));
+        if (a.want_logl)
+            term = df_add(term, sfh_bin_term(c, nh, nl, s_tab));
         if (a.want_w) {
             const sfh_df diff = df_add(c, sfh_df{-nh, -nl});
             const float w = __fdiv_rn(diff.h, c.h);  // 1 - n/c

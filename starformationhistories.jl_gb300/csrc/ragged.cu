@@ -83,7 +83,8 @@ __device__ __forceinline__ void bin_terms(float ah, float al, const double *__re
     if (c.h < eps_f || (c.h == eps_f && c.l < 0.f)) c = sfh_df{eps_f, 0.f};
     float nh, nl;
     sfh_split_double(data[ii], nh, nl);
-    if (want_logl) term = df_add(term, df_poisson_term(c, nh, nl, s_tab));
+    if (want_logl)
+        term = df_add(term, sfh_bin_term(c, nh, nl, s_tab));
     if (want_w) {
         w = __fdiv_rn(df_add(c, sfh_df{-nh, -nl}).h, c.h);
         composite[ii] = sfh_f2d(w);
@@ -98,8 +99,8 @@ k_ragged_pass1(const float *__restrict__ M, const GalDesc *__restrict__ gals,
                int want_logl, int want_w, const sfh_df *__restrict__ tab) {
     __shared__ float rhi[kRChunk], rlo[kRChunk];
     __shared__ double s_red[kRT / 32];
-    __shared__ sfh_df s_tab[129];
-    for (int k = threadIdx.x; k < 129; k += kRT) s_tab[k] = tab[k];
+    __shared__ sfh_df s_tab[SFH_DF_TAB_ALL];
+    for (int k = threadIdx.x; k < SFH_DF_TAB_ALL; k += kRT) s_tab[k] = tab[k];
     const RowTile tile = tiles[blockIdx.x];
     const GalDesc G = gals[tile.g];
     const int64_t i = (int64_t)tile.row0 + threadIdx.x;
@@ -198,8 +199,8 @@ k_ragged_fused(const float *__restrict__ M, const GalDesc *__restrict__ gals,
     __shared__ float rhi[NT], rlo[NT];
     __shared__ double s_red[kRT / 32];
     __shared__ float s_g[kRT / 32][NT];
-    __shared__ sfh_df s_tab[129];
-    for (int k = threadIdx.x; k < 129; k += kRT) s_tab[k] = tab[k];
+    __shared__ sfh_df s_tab[SFH_DF_TAB_ALL];
+    for (int k = threadIdx.x; k < SFH_DF_TAB_ALL; k += kRT) s_tab[k] = tab[k];
     const RowTile tile = tiles[blockIdx.x];
     const GalDesc G = gals[tile.g];
     const int nt = (int)G.nt;

@@ -118,7 +118,8 @@ SFH_DF_HD sfh_df df_log_f(float x, const sfh_df *tab) {
     const uint32_t mant = u & 0x7fffffu;
     const int j = (int)((mant + (1u << 15)) >> 16);  // nearest j / 128, 0..128
     const float m = df_from_bits(mant | 0x3f800000u);  // [1, 2)
-    const float F = SFH_DF_ADD(1.0f, SFH_DF_MUL((float)j, 0.0078125f));  // exact
+    // F = 1 + j/128 built from its bits (j = 128 gives 2.0): no integer-to-float conversion
+    const float F = df_from_bits(0x3f800000u + ((uint32_t)j << 16));
     const float f = SFH_DF_SUB(m, F);                                   // exact, |f| <= 2^-8
     // u = f / F as a double-float
     const float uh = SFH_DF_DIV(f, F);
@@ -133,48 +134,50 @@ SFH_DF_HD sfh_df df_log_f(float x, const sfh_df *tab) {
     p = SFH_DF_MUL(SFH_DF_MUL(SFH_DF_MUL(uh, uh), uh), p);
     sfh_df s = df_two_sum(uh, SFH_DF_MUL(-0.5f, u2.h));
     s = df_fast_two_sum(s.h, SFH_DF_ADD(s.l, SFH_DF_ADD(SFH_DF_SUB(ul, SFH_DF_MUL(0.5f, u2.l)), p)));
-    const float fe = (float)e;
+    // (float)e exactly from bits: 1.5 * 2^23 + e (|e| < 2^22) minus 1.5 * 2^23
+    const float fe = SFH_DF_SUB(df_from_bits(0x4b400000u + (uint32_t)e), 12582912.0f);
     sfh_df le = df_fast_two_sum(SFH_DF_MUL(fe, SFH_DF_LN2_HI),
                                 fmaf(fe, SFH_DF_LN2_LO, SFH_DF_MUL(fe, SFH_DF_LN2_LO2)));
     return df_add(df_add(le, tab[j]), s);
 }
 
 // Poisson term of one bin, fitting_base.jl:93:  n - c - n log(n/c)  (n > 0),  -c  (n = 0),
-// for c = ch + cl >= eps given as a double-float (compensated sum) and n = nh + nl.
-//   |c/n - 1| <= 1/8:  -(c-n)^2/(c+n) + 2 n z^3 (1/3 + z^2/5 + ...),  z = (c-n)/(c+n)
-//                      (log1p(d) = 2 atanh z), all but the z^5 tail (< 3e-7 n) in
-//                      double-float, so tiny terms keep their relative accuracy;
-//   otherwise:         n log(c/n) - (c - n) with the double-float logarithm.
-// Absolute error below 1e-11 (c + n) (checked against long double on 4e6 random bins).
-SFH_DF_HD sfh_df df_poisson_term(sfh_df c, float nh, float nl, const sfh_df *tab) {
-    const sfh_df n{nh, nl};
-    if (!(nh > 0.0f)) return df_neg(c);
-    const sfh_df diff = df_add(c, df_neg(n));
-    const float d = SFH_DF_DIV(diff.h, nh);
-    if (fabsf(d) <= 0.125f) {
-        const sfh_df sum = df_add(c, n);
-        const sfh_df z = df_div(diff, sum);
-        const sfh_df L = df_neg(df_mul(diff, z));
-        // 2 n z^3 / 3 in double-float, the z^5 tail (<= 1.3e-4 n) in FP32
-        const sfh_df z3 = df_mul(df_mul(z, z), z);
-        const sfh_df T3 = df_mul(df_mul(z3, n), sfh_df{0.666666686534881591796875f,
-                                                     -1.9868215517249155e-08f});
-        const float z2 = SFH_DF_MUL(z.h, z.h);
-        float S = 1.0f / 17.0f;
-        S = fmaf(S, z2, 1.0f / 15.0f);
-        S = fmaf(S, z2, 1.0f / 13.0f);
-        S = fmaf(S, z2, 1.0f / 11.0f);
-        S = fmaf(S, z2, 1.0f / 9.0f);
-        S = fmaf(S, z2, 1.0f / 7.0f);
-        S = fmaf(S, z2, 1.0f / 5.0f);
-        const float C5 = SFH_DF_MUL(SFH_DF_MUL(SFH_DF_MUL(2.0f, nh), SFH_DF_MUL(z3.h, z2)), S);
-        return df_add_f(df_add(L, T3), C5);
+// for c = ch + cl >= eps given as a double-float (compensated sum) and n = nh + nl, in a
+// branch-free form (every lane of a warp takes the same path whatever its count):
+//   t = n log c - c + (n - n log n),
+// with n - n log n read from nlogn_tab for integer counts 0..255 (the usual case) and
+// computed otherwise.  Only the absolute error enters a sum of terms: below
+// 2e-12 (c + n) + 1e-13 n |log c| (checked against long double on 4e6 random bins).
+SFH_DF_HD sfh_df df_poisson_term_bf(sfh_df c, float nh, float nl, const sfh_df *tab,
+                                    const sfh_df *nlogn_tab) {
+    sfh_df lc = df_log_f(c.h, tab);
+    lc = df_add_f(lc, SFH_DF_DIV(c.l, c.h));  // log(ch + cl) = log ch + cl/ch
+    sfh_df t = df_add(df_mul(lc, sfh_df{nh, nl}), df_neg(c));
+    const bool small = (nl == 0.0f) && (nh >= 0.0f) && (nh < 256.0f) && (nh == floorf(nh));
+    if (small) {
+        t = df_add(t, nlogn_tab[(int)nh]);
+    } else {  // n - n log n for other counts
+        const sfh_df n{nh, nl};
+        sfh_df ln = df_log_f(nh, tab);
+        ln = df_add_f(ln, SFH_DF_DIV(nl, nh));
+        t = df_add(t, df_add(n, df_neg(df_mul(ln, n))));
     }
-    const sfh_df q = df_div(c, n);
-    sfh_df lq = df_log_f(q.h, tab);
-    lq = df_add_f(lq, SFH_DF_DIV(q.l, q.h));  // log(qh + ql) = log qh + ql/qh (+ O(ql^2))
-    return df_add(df_mul(lq, n), df_neg(diff));
+    return t;
 }
+
+// Host-side table of n - n log n, n = 0..255, as double-float pairs (0 for n = 0).
+static inline void sfh_df_nlogn_table(sfh_df *tab) {
+    for (int n = 0; n < 256; ++n) {
+        const double v = n > 0 ? (double)n - (double)n * log((double)n) : 0.0;
+        const float h = (float)v;
+        tab[n].h = h;
+        tab[n].l = (float)(v - (double)h);
+    }
+}
+
+// Entries of the device table: log(1 + j/128) (129), then n - n log n (256).
+#define SFH_DF_TAB_LOG 129
+#define SFH_DF_TAB_ALL (129 + 256)
 
 // Host-side table of log(1 + j/128), j = 0..128, as double-float pairs.
 static inline void sfh_df_log_table(sfh_df *tab) {

@@ -23,8 +23,8 @@ struct sfh_ctx {
     size_t stage_bytes = 0;
     // Zero-initialised counters for last-block reductions (reset by the last block).
     unsigned int *d_counters = nullptr;
-    // log(1 + j/128), j = 0..128, as double-float pairs (sfh_dfloat.cuh), for the
-    // Poisson terms evaluated on the FP32 pipes.
+    // log(1 + j/128), j = 0..128, then n - n log n, n = 0..255, as double-float pairs
+    // (sfh_dfloat.cuh), for the Poisson terms evaluated on the FP32 pipes.
     sfh_df *d_df_tab = nullptr;
     int64_t launches = 0;
 };
@@ -117,6 +117,11 @@ __device__ __forceinline__ float sfh_log1p_minus_id(float d, float c, float n) {
 // FP64<->FP32 conversions at a small fraction of its FP32 rate).  Exact bit moves for the
 // common cases -- a double that holds a float value (counts), a normal float -- and the
 // ordinary conversion otherwise.
+static __device__ __noinline__ void sfh_split_double_slow(double x, float &h, float &l) {
+    h = __double2float_rn(x);
+    l = __double2float_rn(x - (double)h);
+}
+static __device__ __noinline__ double sfh_f2d_slow(float f) { return (double)f; }
 __device__ __forceinline__ void sfh_split_double(double x, float &h, float &l) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
     const unsigned int e = (unsigned int)(b >> 52) & 0x7ffu;
@@ -127,9 +132,8 @@ __device__ __forceinline__ void sfh_split_double(double x, float &h, float &l) {
         h = __uint_as_float(((unsigned int)(b >> 32) & 0x80000000u) | ((e - 896u) << 23) |
                             (unsigned int)((b >> 29) & 0x7fffffull));
         l = 0.f;
-    } else {
-        h = __double2float_rn(x);
-        l = __double2float_rn(x - (double)h);
+    } else {  // not a float value: the ordinary conversion, kept out of line
+        sfh_split_double_slow(x, h, l);
     }
 }
 __device__ __forceinline__ double sfh_f2d(float f) {
@@ -137,9 +141,16 @@ __device__ __forceinline__ double sfh_f2d(float f) {
     const unsigned int e = (u >> 23) & 0xffu;
     const unsigned long long s = (unsigned long long)(u & 0x80000000u) << 32;
     if ((u << 1) == 0u) return __longlong_as_double((long long)s);  // +-0
-    if (e == 0u || e == 0xffu) return (double)f;                     // subnormal, inf, nan
+    if (e == 0u || e == 0xffu) return sfh_f2d_slow(f);               // subnormal, inf, nan
     return __longlong_as_double((long long)(s | ((unsigned long long)(e + 896u) << 52) |
                                             ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+
+// Poisson term of one bin for the kernels: the branch-free double-float form, skipped as a
+// whole when no active lane of the warp holds counts (empty bins give -c).
+__device__ __forceinline__ sfh_df sfh_bin_term(sfh_df c, float nh, float nl, const sfh_df *s_tab) {
+    if (!__any_sync(__activemask(), nh != 0.0f || nl != 0.0f)) return df_neg(c);
+    return df_poisson_term_bf(c, nh, nl, s_tab, s_tab + SFH_DF_TAB_LOG);
 }
 
 // Sum of a double-float over the warp (all lanes receive it), FP32 operations only.

@@ -7,11 +7,12 @@ from ._lib import (SFH_BF16X2, SFH_F32, SFH_F64, EXPORTED, LIB_PATH, SFHArgument
                    load)
 from .core import Context, Models, as_models, default_context
 from .emulator import SyntheticGenerator, TemplateEmulator
-from .fitting import (Galaxies, composite_, construct_x0, fg_, fg_batched, fg_ragged, fit_templates,
+from .fitting import (Galaxies, composite_, construct_x0, construct_x0_mdf, fg_, fg_batched,
+                      fg_ragged, fit_templates, fixed_amr, truncate_relweights,
                       fit_templates_fast, fit_templates_lbfgsb, grad_loglikelihood,
                       grad_loglikelihood_, loglikelihood, renormalize_x0, stack_models)
-from .sampling import (GaussianDispersion, PowerLawMZR, calculate_coeffs, hmc_sample,
-                       logdensity_batched, sample_sfh)
+from .sampling import (GaussianDispersion, LinearAMR, LogarithmicAMR, MH_from_Z, PowerLawMZR,
+                       calculate_coeffs, dMH_dZ, hmc_sample, logdensity_batched, sample_sfh)
 from .templates import (BrokenPowerLawIMF, Histogram, Kroupa2001, Martin2016_complete,
                         bin_cmd_smooth, calculate_edges, calculate_weights, compl_model, err_model,
                         exp_photerr, histogram_data, histogram_pix, interpolate_mini, midpoints,
@@ -28,5 +29,7 @@ __all__ = [
     "histogram_pix", "interpolate_mini", "midpoints", "mini_spacing", "partial_cmd_smooth",
     "partial_cmd_smooth_batch", "GaussianDispersion", "PowerLawMZR", "calculate_coeffs",
     "hmc_sample", "logdensity_batched", "sample_sfh", "Galaxies", "fg_ragged",
-    "partial_cmd_smooth_ragged", "SyntheticGenerator", "TemplateEmulator",
+    "partial_cmd_smooth_ragged", "SyntheticGenerator", "TemplateEmulator", "LinearAMR",
+    "construct_x0_mdf", "fixed_amr", "truncate_relweights", "LogarithmicAMR", "MH_from_Z",
+    "dMH_dZ",
 ]

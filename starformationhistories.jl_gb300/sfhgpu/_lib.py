@@ -23,6 +23,7 @@ EXPORTED = [
     "sfh_abi_version", "sfh_status_string", "sfh_ctx_create", "sfh_ctx_destroy",
     "sfh_ctx_last_error", "sfh_ctx_synchronize", "sfh_ctx_stream", "sfh_ctx_launch_count",
     "sfh_models_upload", "sfh_models_from_device", "sfh_models_free", "sfh_models_info",
+    "sfh_models_combine",
     "sfh_composite", "sfh_loglikelihood", "sfh_grad_loglikelihood", "sfh_fg", "sfh_fg_dev",
     "sfh_fg_batched_dev", "sfh_fg_kernel_times", "sfh_models_autotune", "sfh_fg_dev_noalloc", "sfh_hmc_sample_dev",
     "sfh_logdensity_batched_dev", "sfh_bin_cmd_smooth", "sfh_bin_cmd_smooth_batch_dev",
@@ -99,6 +100,8 @@ def load(path: str | None = None):
             "sfh_models_upload": ([_vp, _vp, C.c_int, _i64, _i64, C.c_int, C.POINTER(_vp)], C.c_int),
             "sfh_models_from_device": ([_vp, _vp, _i64, _i64, C.c_int, C.POINTER(_vp)], C.c_int),
             "sfh_models_free": ([_vp], C.c_int),
+            "sfh_models_combine": ([_vp, _vp, _i64, _vp, _vp, _vp, C.c_int, C.POINTER(_vp)],
+                                   C.c_int),
             "sfh_models_info": ([_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(C.c_int)],
                                 C.c_int),
             "sfh_composite": ([_vp, _vp, C.c_int, _vp, _vp], C.c_int),

@@ -114,6 +114,22 @@ class Models:
     def shape(self):
         return (self.nbins, self.nt)
 
+    def combine(self, groups, weights, storage="f32"):
+        """A new matrix whose column g is sum(weights[g][q] * self[:, groups[g][q]]): one
+        pass over this matrix on the device (sfh_models_combine)."""
+        off = np.zeros(len(groups) + 1, dtype=np.int64)
+        off[1:] = np.cumsum([len(gr) for gr in groups])
+        cols = np.ascontiguousarray(np.concatenate([np.asarray(gr) for gr in groups]),
+                                    dtype=np.int32)
+        w = np.ascontiguousarray(np.concatenate([np.asarray(x, dtype=np.float64)
+                                                 for x in weights]))
+        st = {"f32": SFH_F32, "bf16x2": SFH_BF16X2}[storage]
+        h = C.c_void_p()
+        check(load().sfh_models_combine(self.ctx.handle, self._h, len(groups), off.ctypes.data,
+                                        cols.ctypes.data, w.ctypes.data, st, C.byref(h)),
+              self.ctx.handle, "models_combine")
+        return Models(ctx=self.ctx, storage=st, _handle=h, _shape=(self.nbins, len(groups)))
+
     def autotune(self, coeffs, data, iters=10, eps=None):
         """Pick the fastest single-vector fg! launch plan for this matrix by timing the
         candidates on the device (sfh_models_autotune).  Returns

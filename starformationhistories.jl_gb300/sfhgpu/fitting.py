@@ -276,6 +276,97 @@ def fit_templates(models, data, x0=None, gtol=1e-8, maxiter=10000):
     return FitTemplatesResult(pack(r_map), pack(r_mle))
 
 
+def construct_x0_mdf(logAge, T_max, normalize_value=1.0):
+    """construct_x0_mdf(logAge, T_max), hierarchical/construct_x0_mdf.jl:58-71: stellar mass
+    per unique log age for a constant star formation rate since T_max (Gyr)."""
+    logAge = np.asarray(logAge, dtype=np.float64)
+    _argcheck(np.log10(T_max) + 9 > logAge.max(), "log10(T_max) + 9 > maximum(logAge)")
+    max_la = np.log10(T_max) + 9
+    sfr = normalize_value / (10.0 ** max_la - 10.0 ** logAge.min())
+    uniq = list(dict.fromkeys(logAge.tolist()))
+    srt = sorted(uniq) + [max_la]
+    dt = np.diff(10.0 ** np.asarray(srt))
+    return np.array([sfr * dt[srt.index(la)] for la in uniq])
+
+
+def truncate_relweights(relweightsmin, relweights, logAge):
+    """truncate_relweights, hierarchical/fixed_amr.jl:225-243: indices of the templates whose
+    relative weight is at least relweightsmin times the largest of their log age."""
+    relweights, logAge = np.asarray(relweights), np.asarray(logAge)
+    _argcheck(relweights.size == logAge.size, "length(relweights) == length(logAge)")
+    if relweightsmin == 0:
+        return np.arange(relweights.size)
+    keep = []
+    for la in dict.fromkeys(logAge.tolist()):
+        good = np.nonzero(logAge == la)[0]
+        keep.append(good[relweights[good] >= relweightsmin * relweights[good].max()])
+    return np.concatenate(keep)
+
+
+def fixed_amr(models, data, logAge, metallicities, relweights, relweightsmin=0.0, x0=None,
+              gtol=1e-8, maxiter=10000):
+    """fixed_amr, hierarchical/fixed_amr.jl:41-188: fit one stellar-mass coefficient per
+    unique log age under fixed relative weights (an externally imposed age-metallicity
+    relation).  The expansion coeffs[idxs] = relweights[idxs] * x[i] is linear, so the
+    templates of each age are combined once on the device into one column and the MAP /
+    MLE fits (log transform, BFGS) run on the reduced (nbins, n_ages) matrix.  Returns
+    (map, mle) with μ per unique age and σ = sqrt(diag(invH)) in log space
+    (fixed_amr.jl:185-186)."""
+    import warnings
+
+    from scipy.optimize import minimize
+    M = models if isinstance(models, Models) else Models(
+        np.asfortranarray(np.asarray(models, dtype=np.float32)), storage="f32")
+    data = np.asarray(data, dtype=np.float64).reshape(-1, order="F")
+    logAge = np.asarray(logAge, dtype=np.float64)
+    metallicities = np.asarray(metallicities, dtype=np.float64)
+    relweights = np.array(relweights, dtype=np.float64)
+    uniq = list(dict.fromkeys(logAge.tolist()))
+    if x0 is None:
+        x0 = construct_x0_mdf(logAge, 13.7)
+    x0 = np.asarray(x0, dtype=np.float64)
+    _argcheck(x0.size == len(uniq), "length(x0) == length(unique(logAge))")
+    _argcheck(M.nbins == data.size, "size(models, 1) == length(data)")
+    _argcheck(M.nt == logAge.size == metallicities.size == relweights.size,
+              "size(models, 2) == length(logAge) == length(metallicities) == length(relweights)")
+    _argcheck(np.all(relweights >= 0), "all relative weights must be ≥ 0")
+    _argcheck(relweightsmin >= 0, "relweightsmin >= 0")
+    keep = truncate_relweights(relweightsmin, relweights, logAge)
+    groups, weights = [], []
+    for la in uniq:
+        good = keep[logAge[keep] == la]
+        s = relweights[good].sum()
+        if not np.isclose(s, 1.0) and relweightsmin == 0:
+            warnings.warn(f"The relative weights for logAge={la} provided to fixed_amr do not "
+                          "sum to 1 and will be renormalized.", stacklevel=2)
+        groups.append(good)
+        weights.append(relweights[good] / s)
+    Mr = M.combine(groups, weights, storage="f32")
+    x0 = np.log(renormalize_x0(data, Mr, x0))
+    comp = np.empty(Mr.nbins)
+    G = np.empty(Mr.nt)
+
+    def fg_map(logx):  # fixed_amr.jl:102-125
+        x = np.exp(logx)
+        v = fg_(True, G, x, Mr, data, comp) - logx.sum()
+        return float(v), G * x - 1.0
+
+    def fg_mle(logx):  # fixed_amr.jl:127-149
+        x = np.exp(logx)
+        v = fg_(True, G, x, Mr, data, comp)
+        return float(v), G * x
+
+    opts = {"gtol": gtol, "maxiter": maxiter}
+    r_map = minimize(fg_map, x0, jac=True, method="BFGS", options=opts)
+    r_mle = minimize(fg_mle, r_map.x, jac=True, method="BFGS", options=opts)
+
+    def pack(r):
+        invH = np.asarray(r.hess_inv)
+        return LogTransformFTResult(np.exp(r.x), np.sqrt(np.abs(np.diag(invH))), invH, r)
+
+    return FitTemplatesResult(pack(r_map), pack(r_mle))
+
+
 def fg_batched(models, R, data, want_logl=True, want_grad=True, eps=None):
     """B fg! evaluations in one call on the tensor cores (sfh_fg_batched_dev).
 

@@ -16,7 +16,23 @@ import numpy as np
 from ._lib import check, load
 from .core import Models
 
-SFH_HMC_DIRECT, SFH_HMC_MZR = 0, 1
+SFH_HMC_DIRECT, SFH_HMC_MZR, SFH_HMC_LINEAR_AMR, SFH_HMC_LOG_AMR = 0, 1, 2, 3
+
+
+def MH_from_Z(Z, solZ=0.01524, Y_p=0.2485, gamma=1.78):
+    """MH_from_Z, src/utilities.jl:138-145: [M/H] = log10(Z/X) - log10(Z/X)_sun with the
+    PARSEC helium relation Y = Y_p + γ Z (NaN where X <= 0)."""
+    Z = np.asarray(Z, dtype=np.float64)
+    X = 1.0 - (Y_p + gamma * Z + Z)
+    Xs = 1.0 - (Y_p + gamma * solZ + solZ)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        return np.where(X > 0, np.log10(Z / (X * solZ) * Xs), np.nan)
+
+
+def dMH_dZ(Z, solZ=0.01524, Y_p=0.2485, gamma=1.78):
+    """dMH_dZ, src/utilities.jl:152-155."""
+    Z = np.asarray(Z, dtype=np.float64)
+    return (Y_p - 1.0) / (np.log(10.0) * Z * (Y_p + Z + gamma * Z - 1.0))
 
 
 class HMCConfig(C.Structure):
@@ -27,7 +43,7 @@ class HMCConfig(C.Structure):
                 ("h_logAge", C.POINTER(C.c_double)), ("h_MH", C.POINTER(C.c_double)),
                 ("logMstar0", C.c_double), ("alpha_free", C.c_int32), ("beta_free", C.c_int32),
                 ("sigma_free", C.c_int32), ("alpha", C.c_double), ("beta", C.c_double),
-                ("sigma", C.c_double)]
+                ("sigma", C.c_double), ("T_max", C.c_double)]
 
 
 def _bind():
@@ -56,6 +72,60 @@ class PowerLawMZR:
 
 
 @dataclass
+class LinearAMR:
+    """LinearAMR(α, β, T_max, free), src/fitting/hierarchical/amr.jl:170-213: mean [M/H]
+    μ = β + α (T_max - t) at lookback time t = 10^(logAge - 9) Gyr; α >= 0."""
+    alpha: float
+    beta: float
+    T_max: float = 13.7
+    free: tuple = (True, True)
+
+    def __post_init__(self):
+        if self.alpha < 0:
+            raise ValueError("α must be ≥ 0")
+        if self.T_max <= 0:
+            raise ValueError("T_max must be > 0")
+
+    def __call__(self, logAge):
+        return self.beta + self.alpha * (self.T_max - 10.0 ** (np.asarray(logAge) - 9.0))
+
+    @classmethod
+    def from_constraints(cls, constraint1, constraint2, T_max=13.7, free=(True, True)):
+        """LinearAMR from two ([M/H], lookback time in Gyr) constraints, amr.jl:233-248."""
+        (mh1, t1), (mh2, t2) = constraint1, constraint2
+        dt, dmh = t2 - t1, mh2 - mh1
+        if dt == 0:
+            raise ValueError("Constraints are given at identical times.")
+        if np.sign(dt) == np.sign(dmh):
+            raise ValueError("The constraints indicate metallicity decreasing towards present-day.")
+        alpha = dmh / -dt
+        beta = min(mh1, mh2) - alpha * (T_max - max(t1, t2))
+        return cls(alpha, beta, T_max, free)
+
+
+@dataclass
+class LogarithmicAMR:
+    """LogarithmicAMR(α, β, T_max, MH_from_Z, dMH_dZ, free), amr.jl:256-290: metal mass
+    fraction Z = β + α (T_max - t) at lookback time t (Gyr) and μ = MH_from_Z(Z) with the
+    package's default conversion; α, β >= 0 (transforms (1, 1))."""
+    alpha: float
+    beta: float
+    T_max: float = 13.7
+    free: tuple = (True, True)
+
+    def __post_init__(self):
+        if self.alpha < 0:
+            raise ValueError("α must be ≥ 0")
+        if self.beta < 0:
+            raise ValueError("β must be ≥ 0")
+        if self.T_max <= 0:
+            raise ValueError("T_max must be > 0")
+
+    def __call__(self, logAge):
+        return MH_from_Z(self.beta + self.alpha * (self.T_max - 10.0 ** (np.asarray(logAge) - 9.0)))
+
+
+@dataclass
 class GaussianDispersion:
     """GaussianDispersion(σ, free), src/fitting/hierarchical/dispersion_models.jl:80-110."""
     sigma: float
@@ -65,20 +135,26 @@ class GaussianDispersion:
         return np.exp(-((np.asarray(x) - mu) / self.sigma) ** 2 / 2)
 
 
-def calculate_coeffs(mzr: PowerLawMZR, disp: GaussianDispersion, mstars, logAge, MH):
-    """calculate_coeffs (mzr.jl:50-79) on the host (a handful of values per age)."""
+def calculate_coeffs(model, disp: GaussianDispersion, mstars, logAge, MH):
+    """calculate_coeffs on the host (a handful of values per age): PowerLawMZR
+    (mzr.jl:50-79, μ from the cumulative stellar mass) or LinearAMR (amr.jl:50-72,
+    μ from the age)."""
     logAge, MH = np.asarray(logAge, float), np.asarray(MH, float)
     uniq = list(dict.fromkeys(logAge.tolist()))
     mstars = np.asarray(mstars, float)
     if len(mstars) != len(uniq):
         raise ValueError("Length of `mstars` must be the same as `unique(logAge)`.")
-    order = np.argsort(-np.asarray(uniq), kind="stable")
-    cum = np.empty(len(uniq))
-    cum[order] = np.cumsum(mstars[order])
+    if isinstance(model, (LinearAMR, LogarithmicAMR)):
+        mu = [model(la) for la in uniq]
+    else:
+        order = np.argsort(-np.asarray(uniq), kind="stable")
+        cum = np.empty(len(uniq))
+        cum[order] = np.cumsum(mstars[order])
+        mu = [model(c) for c in cum]
     out = np.empty_like(logAge)
     for i, la in enumerate(uniq):
         idx = np.nonzero(logAge == la)[0]
-        w = disp(MH[idx], mzr(cum[i]))
+        w = disp(MH[idx], mu[i])
         out[idx] = w * mstars[i] / w.sum()
     return out
 
@@ -90,7 +166,7 @@ def _config(nchains, model, nsteps=0, nwarmup=0, nleap=10, thin=1, step0=0.01, t
     cfg.ntraj, cfg.nwarmup, cfg.nleap, cfg.thin = int(nsteps), int(nwarmup), int(nleap), int(thin)
     cfg.step0, cfg.target_accept, cfg.seed = float(step0), float(target), int(seed)
     keep = []
-    if model == SFH_HMC_MZR:
+    if model in (SFH_HMC_MZR, SFH_HMC_LINEAR_AMR, SFH_HMC_LOG_AMR):
         logAge = np.asarray(logAge, float)
         uniq = list(dict.fromkeys(logAge.tolist()))
         age_index = np.ascontiguousarray([uniq.index(a) for a in logAge], dtype=np.int32)
@@ -101,21 +177,28 @@ def _config(nchains, model, nsteps=0, nwarmup=0, nleap=10, thin=1, step0=0.01, t
         cfg.h_age_index = age_index.ctypes.data_as(C.POINTER(C.c_int32))
         cfg.h_logAge = ua.ctypes.data_as(C.POINTER(C.c_double))
         cfg.h_MH = mh.ctypes.data_as(C.POINTER(C.c_double))
-        cfg.logMstar0 = float(mzr.logMstar0)
+        cfg.logMstar0 = float(getattr(mzr, "logMstar0", 0.0))
+        cfg.T_max = float(getattr(mzr, "T_max", 0.0))
         cfg.alpha_free, cfg.beta_free = int(bool(mzr.free[0])), int(bool(mzr.free[1]))
         cfg.sigma_free = int(bool(disp.free[0]))
-        cfg.alpha, cfg.beta, cfg.sigma = float(mzr.alpha), float(mzr.MH0), float(disp.sigma)
+        beta = mzr.beta if isinstance(mzr, (LinearAMR, LogarithmicAMR)) else mzr.MH0
+        cfg.alpha, cfg.beta, cfg.sigma = float(mzr.alpha), float(beta), float(disp.sigma)
     return cfg, keep
 
 
-def mzr_theta(mstars, mzr: PowerLawMZR, disp: GaussianDispersion):
+def mzr_theta(mstars, mzr, disp: GaussianDispersion):
     """Transformed variables [log R_j..., log α, β, log σ] (free ones only), the order
-    used by logdensity_and_gradient (generic_fitting.jl:117-136)."""
+    used by logdensity_and_gradient (generic_fitting.jl:117-136); PowerLawMZR and
+    LinearAMR share the transforms (α > 0 log-transformed, β untransformed);
+    LogarithmicAMR log-transforms β as well (amr.jl:290)."""
     th = list(np.log(np.asarray(mstars, float)))
     if mzr.free[0]:
         th.append(np.log(mzr.alpha))
     if mzr.free[1]:
-        th.append(mzr.MH0)
+        if isinstance(mzr, LogarithmicAMR):  # β > 0: log-transformed (amr.jl:290)
+            th.append(np.log(mzr.beta))
+        else:
+            th.append(mzr.beta if isinstance(mzr, LinearAMR) else mzr.MH0)
     if disp.free[0]:
         th.append(np.log(disp.sigma))
     return np.asarray(th)
@@ -183,15 +266,18 @@ def hmc_sample(models: Models, data, nsteps, nchains=1, nwarmup=200, nleap=10, s
     return _run_hmc(models, data, theta0, cfg, keep, keep_draws)
 
 
-def sample_sfh(models: Models, data, logAge, MH, mzr: PowerLawMZR, disp: GaussianDispersion,
+def sample_sfh(models: Models, data, logAge, MH, mzr, disp: GaussianDispersion,
                mstars0, nsteps, nchains=1, nwarmup=200, nleap=10, step0=0.01,
                target_accept=0.8, seed=20261203, keep_draws=False, thin=1, jitter=0.05):
-    """Posterior sampling of (R_j, α, MH0, σ) under a PowerLawMZR + GaussianDispersion model
-    (sample_sfh, generic_fitting.jl:458-527), all chains in lock step.  Means are reported
-    on the natural scale in the order [R_j..., α, MH0, σ] (free parameters only)."""
+    """Posterior sampling of (R_j, α, β, σ) under a PowerLawMZR or LinearAMR metallicity
+    model with GaussianDispersion (sample_sfh, generic_fitting.jl:458-527), all chains in
+    lock step.  Means are reported on the natural scale in the order [R_j..., α, β, σ]
+    (free parameters only)."""
     th = mzr_theta(mstars0, mzr, disp)
     rng = np.random.default_rng(seed)
     theta0 = th[None, :] + jitter * rng.standard_normal((nchains, th.size))
-    cfg, keep = _config(nchains, SFH_HMC_MZR, nsteps, nwarmup, nleap, thin, step0,
+    kind = (SFH_HMC_LINEAR_AMR if isinstance(mzr, LinearAMR) else
+            SFH_HMC_LOG_AMR if isinstance(mzr, LogarithmicAMR) else SFH_HMC_MZR)
+    cfg, keep = _config(nchains, kind, nsteps, nwarmup, nleap, thin, step0,
                         target_accept, seed, mzr=mzr, disp=disp, logAge=logAge, MH=MH)
     return _run_hmc(models, data, theta0, cfg, keep, keep_draws)

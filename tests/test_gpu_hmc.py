@@ -119,3 +119,92 @@ def test_hmc_mzr_recovers_parameters(sfh):
     z = np.abs(pm - truth) / psd
     assert np.all(z[na:] < 4.0), (pm[na:], psd[na:])
     assert np.median(z[:na]) < 3.0, z[:na]
+
+
+def _amr_problem(seed=12, nages=5, nmh=6, nbins=3000, scale=1.0):
+    from sfhgpu.sampling import GaussianDispersion, LinearAMR, calculate_coeffs
+    rng = np.random.default_rng(seed)
+    la = np.repeat(np.linspace(10.0, 8.0, nages), nmh)
+    mh = np.tile(np.linspace(-2.5, 0.0, nmh), nages)
+    M = (rng.random((nbins, nages * nmh)) / 1e2).astype(np.float32)
+    R = (rng.random(nages) * 1e4 + 1e3) * scale
+    amr, disp = LinearAMR(0.1, -2.2, 13.7), GaussianDispersion(0.2)
+    coeffs = calculate_coeffs(amr, disp, R, la, mh)
+    data = rng.poisson(M.astype(np.float64) @ coeffs).astype(np.float64)
+    return la, mh, np.asfortranarray(M), R, amr, disp, data
+
+
+def test_amr_logdensity_matches_oracle(sfh, O):
+    from sfhgpu.sampling import SFH_HMC_LINEAR_AMR, GaussianDispersion, LinearAMR, mzr_theta
+    la, mh, M32, R, amr, disp, data = _amr_problem()
+    H = sfh.Models(M32, storage="bf16x2")
+    Ms = np.asfortranarray(_bf16_hilo(M32))
+    rng = np.random.default_rng(6)
+    thetas, nats = [], []
+    for _ in range(6):
+        Rb = R * np.exp(0.2 * rng.standard_normal(R.size))
+        a = 0.1 * np.exp(0.2 * rng.standard_normal())
+        b = -2.2 + 0.1 * rng.standard_normal()
+        s = 0.2 * np.exp(0.2 * rng.standard_normal())
+        thetas.append(mzr_theta(Rb, LinearAMR(a, b, 13.7), GaussianDispersion(s)))
+        nats.append(np.concatenate([Rb, [a, b, s]]))
+    theta = np.stack(thetas)
+    logd, grad = sfh.logdensity_batched(H, data, theta, SFH_HMC_LINEAR_AMR, amr, disp, la, mh)
+    nst = data.sum()
+    for k, v in enumerate(nats):
+        nlogL, Gv = O.amr_fg(v, 13.7, Ms, data, la, mh)
+        na = R.size
+        ref_logd = -nlogL + np.sum(np.log(v[:na])) + np.log(v[na]) + np.log(v[na + 2])
+        ref_g = np.concatenate([-Gv[:na] * v[:na] + 1.0, [-Gv[na] * v[na] + 1.0, -Gv[na + 1],
+                                                          -Gv[na + 2] * v[na + 2] + 1.0]])
+        assert abs(logd[k] - ref_logd) <= 1e-2 * max(1.0, nst / 1e4), (logd[k], ref_logd)
+        scale = np.abs(ref_g).max()
+        np.testing.assert_allclose(grad[k], ref_g, rtol=2e-3, atol=2e-3 * scale)
+
+
+def test_hmc_amr_recovers_parameters(sfh):
+    from sfhgpu.sampling import GaussianDispersion, LinearAMR
+    la, mh, M32, R, amr, disp, data = _amr_problem(seed=13, nbins=6000, scale=5.0)
+    H = sfh.Models(M32, storage="bf16x2")
+    out = sfh.sample_sfh(H, data, la, mh, LinearAMR(0.08, -2.0, 13.7), GaussianDispersion(0.3),
+                         R * 1.1, nsteps=300, nchains=32, nwarmup=300, nleap=10, seed=9)
+    na = R.size
+    pm = out["mean"].mean(axis=0)
+    psd = np.sqrt(out["var"].mean(axis=0) + out["mean"].var(axis=0))
+    truth = np.concatenate([R, [0.1, -2.2, 0.2]])
+    assert 0.4 < out["accept"].mean() < 0.995, out["accept"].mean()
+    z = np.abs(pm - truth) / psd
+    assert np.all(z[na:] < 4.0), (pm[na:], psd[na:])
+    assert np.median(z[:na]) < 3.0, z[:na]
+
+
+def test_log_amr_logdensity_matches_oracle(sfh, O):
+    from sfhgpu.sampling import (SFH_HMC_LOG_AMR, GaussianDispersion, LogarithmicAMR, MH_from_Z,
+                                 calculate_coeffs, mzr_theta)
+    rng = np.random.default_rng(14)
+    nages, nmh, nbins = 5, 6, 3000
+    la = np.repeat(np.linspace(10.0, 8.0, nages), nmh)
+    mh = np.tile(MH_from_Z(10 ** np.linspace(-4, -2, nmh)), nages)
+    M32 = np.asfortranarray((rng.random((nbins, nages * nmh)) / 1e2).astype(np.float32))
+    R = rng.random(nages) * 1e4 + 1e3
+    amr, disp = LogarithmicAMR(1e-4, 5e-5, 13.7), GaussianDispersion(0.2)
+    data = rng.poisson(M32.astype(np.float64) @ calculate_coeffs(amr, disp, R, la, mh)).astype(float)
+    H = sfh.Models(M32, storage="bf16x2")
+    Ms = np.asfortranarray(_bf16_hilo(M32))
+    thetas, nats = [], []
+    for _ in range(5):
+        Rb = R * np.exp(0.2 * rng.standard_normal(R.size))
+        a = 1e-4 * np.exp(0.2 * rng.standard_normal())
+        b = 5e-5 * np.exp(0.2 * rng.standard_normal())
+        s = 0.2 * np.exp(0.2 * rng.standard_normal())
+        thetas.append(mzr_theta(Rb, LogarithmicAMR(a, b, 13.7), GaussianDispersion(s)))
+        nats.append(np.concatenate([Rb, [a, b, s]]))
+    logd, grad = sfh.logdensity_batched(H, data, np.stack(thetas), SFH_HMC_LOG_AMR, amr, disp,
+                                        la, mh)
+    na = R.size
+    for k, v in enumerate(nats):
+        nlogL, Gv = O.amr_fg(v, 13.7, Ms, data, la, mh, kind=1)
+        ref_logd = -nlogL + np.sum(np.log(v)) 
+        ref_g = np.concatenate([-Gv[:na] * v[:na] + 1.0, -Gv[na:] * v[na:] + 1.0])
+        assert abs(logd[k] - ref_logd) <= 1e-2 * max(1.0, data.sum() / 1e4), (logd[k], ref_logd)
+        np.testing.assert_allclose(grad[k], ref_g, rtol=2e-3, atol=2e-3 * np.abs(ref_g).max())
