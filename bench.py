@@ -50,15 +50,15 @@ def _peaks():
 
 
 def _profile_traffic(kernel: str):
-    """dram bytes per launch of `kernel` from the committed ncu summary, else None."""
-    path = os.path.join(ROOT, "profiles", "fg_kernels_config2.md")
-    try:
-        with open(path) as f:
+    """dram bytes per launch of `kernel` from the committed ncu summaries, else None."""
+    pdir = os.path.join(ROOT, "profiles")
+    for name in sorted(os.listdir(pdir)) if os.path.isdir(pdir) else []:
+        if not name.endswith(".md"):
+            continue
+        with open(os.path.join(pdir, name)) as f:
             for line in f:
                 if line.startswith(f"dram_bytes_per_launch {kernel}:"):
                     return float(line.split(":", 1)[1].strip().split()[0])
-    except OSError:
-        pass
     return None
 
 
@@ -626,13 +626,24 @@ def run_ours(args):
     sfhgpu._lib.check(L.sfh_fg_kernel_times(ctx.handle, H.handle, d_r.data_ptr(), d_n.data_ptr(),
                                             d_c.data_ptr(), d_G.data_ptr(), d_L.data_ptr(), eps,
                                             50, kms), ctx.handle, "sfh_fg_kernel_times")
-    # FP32 storage runs two fused kernels: [0] pass 1 (m, logL, w), [2] pass 2 (G);
-    # slots [1] and [3] stay empty.
-    names = ["k_fg_pass1_f32", "(fused into pass 1)", "k_fg_pass2_f32", "(fused into pass 2)"]
-    alg = [NBINS * NTW * 4 + NTW * 8 + NBINS * 8,    # M, r, m
-           NBINS * 8 * 3,                            # m, n, w
-           NBINS * NTW * 4 + NBINS * 8 + NTW * 8,    # M, w, G
-           NTW * 8]
+    path = H.path
+    if path == "onepass":
+        # [0] the one-pass kernel (M once, r, n, composite out, G and -logL through
+        # per-SM partials and an in-kernel grid reduction); slots [1]-[3] stay empty.
+        nsm = torch.cuda.get_device_properties(0).multi_processor_count
+        names = ["k_fg_onepass", "(fused into the one-pass kernel)", "(fused: grid reduction)",
+                 "(none)"]
+        alg = [NBINS * NTW * 4 + NTW * 8 + NBINS * 8 * 2 + 2 * nsm * NTW * 8 + NTW * 8, 0, 0, 0]
+        alg_eval = NBINS * NTW * 4 + NTW * 8 * 2 + NBINS * 8 * 2  # M once, r, n, composite, G
+    else:
+        # FP32 storage runs two fused kernels: [0] pass 1 (m, logL, w), [2] pass 2 (G);
+        # slots [1] and [3] stay empty.
+        names = ["k_fg_pass1_f32", "(fused into pass 1)", "k_fg_pass2_f32", "(fused into pass 2)"]
+        alg = [NBINS * NTW * 4 + NTW * 8 + NBINS * 8,    # M, r, m
+               NBINS * 8 * 3,                            # m, n, w
+               NBINS * NTW * 4 + NBINS * 8 + NTW * 8,    # M, w, G
+               NTW * 8]
+        alg_eval = alg[0] + alg[2]
     k = max(range(4), key=lambda i: kms[i])
     peak, peak_kind = _peaks()
     achieved = alg[k] / (kms[k] * 1e-3) / 1e9
@@ -640,9 +651,10 @@ def run_ours(args):
                 "unit": "GB/s", "frac": achieved / peak, "traffic": _profile_traffic(names[k]),
                 "peak_source": peak_kind,
                 "kernel_ms": {n: kms[i] for i, n in enumerate(names)},
-                "fg_total_gbs": (alg[0] + alg[2]) / (ms / args.steps * 1e-3) / 1e9,
-                "autotuned_plan": {"pass1_template_splits": tuned["plan"][0], "pass2_rows": tuned["plan"][1],
-                                   "pass2_waves": tuned["plan"][2], "pass_ms": tuned["ms"]}}
+                "fg_total_gbs": alg_eval / (ms / args.steps * 1e-3) / 1e9,
+                "autotuned_plan": {"path": path, "onepass_ms": H.onepass_ms,
+                                   "pass1_template_splits": tuned["plan"][0], "pass2_rows": tuned["plan"][1],
+                                   "pass2_waves": tuned["plan"][2], "twopass_ms": tuned["ms"]}}
 
     # ---- end to end through the host-array C ABI (sfh_fg)
     comp = np.empty(NBINS)

@@ -126,14 +126,39 @@ int sfh_fg_kernel_times(sfh_ctx *ctx, const sfh_models *models, const double *d_
                         const double *d_data, double *d_composite, double *d_G,
                         double *d_negLogL, double eps, int iters, double *ms_out);
 
+/* Single-vector fg! paths for FP32 template storage (no reference counterpart; both
+   compute fg!, src/fitting/solvers.jl:20-38, to the same tolerance):
+     SFH_PATH_ONEPASS  one kernel keeps 16- or 32-bin tiles of every template in shared
+                       memory (bulk-copy ring, one persistent CTA per SM) and forms the
+                       composite, the Poisson terms, w and Mᵀ w from one read of the
+                       matrix; needs nt <= 1536, and keeps a blocked copy of the FP32
+                       templates (one more matrix of device memory, made on first use);
+     SFH_PATH_TWOPASS  pass 1 (m = M r, terms, w) then pass 2 (G = Mᵀ w): two reads;
+     SFH_PATH_AUTO     one-pass when the shape allows it (default).
+   The path applies to calls that request G; composite-only calls read the matrix once
+   either way. */
+enum sfh_fg_path { SFH_PATH_AUTO = 0, SFH_PATH_ONEPASS = 1, SFH_PATH_TWOPASS = 2 };
+/* Sets the path of later fg! calls on this handle (SFH_ERR_UNSUPPORTED when ONEPASS is
+   asked for a shape it cannot take). */
+int sfh_models_set_path(sfh_ctx *ctx, sfh_models *models, int path);
+/* One-pass variant: 16 or 32 bins per tile, and lag = 1 to form the G products one tile
+   behind the composite (overlapping the per-tile finish, two tiles resident) or 0 (one tile
+   resident, more of the ring left to the stream).  Default 16 / 1; the autotuner measures
+   all four and shapes that do not fit a variant fall back to a smaller one. */
+int sfh_models_set_onepass_tile(sfh_ctx *ctx, sfh_models *models, int bins, int lag);
+/* The path fg! calls with G take on this handle now (ONEPASS or TWOPASS), and the
+   one-pass time measured by sfh_models_autotune (0 if not measured); either may be NULL. */
+int sfh_models_path(sfh_ctx *ctx, const sfh_models *models, int *path_out, double *onepass_ms);
+
 /* Autotuner (no reference counterpart): times candidate launch plans of the FP32
    single-vector fg! on this matrix with the caller's inputs (pass-1 template splits whose
    grids fill 1/2 to 4 whole waves of resident blocks; pass-2 row chunks of 1,024 / 2,048
-   / 4,096 bins and column groups sized to 1, 2 or 4 waves), `iters` timed runs each, and
-   stores the fastest in the handle; later fg! calls on it use that plan.  plan_out
-   (3 ints: pass-1 template splits, pass-2 rows, pass-2 waves) and ms_out (2 doubles:
-   pass-1 and pass-2 ms) may be NULL.  Call it before sharing the handle between
-   contexts.  No-op for FP64 storage. */
+   / 4,096 bins and column groups sized to 1, 2 or 4 waves; the one-pass kernel when the
+   shape allows it), `iters` timed runs each, and stores the fastest in the handle; later
+   fg! calls on it use that plan.  plan_out (3 ints: pass-1 template splits, pass-2 rows,
+   pass-2 waves) and ms_out (2 doubles: pass-1 and pass-2 ms) may be NULL; the path chosen
+   and the one-pass time are read back with sfh_models_path.  Call it before sharing the
+   handle between contexts.  No-op for FP64 storage. */
 int sfh_models_autotune(sfh_ctx *ctx, sfh_models *models, const double *d_coeffs,
                         const double *d_data, double eps, int iters, int *plan_out,
                         double *ms_out);

@@ -32,6 +32,7 @@
 #include <mutex>
 
 #include "sfh_internal.cuh"
+#include "sfh_ptx.cuh"
 
 namespace {
 
@@ -46,7 +47,6 @@ constexpr int TMEM_COLS = 512;                     // two 128 x 256 FP32 accumul
 constexpr int kGemmThreads = 320;  // producer, MMA, 8 epilogue warps
 constexpr int kEpiThreads = 256;
 constexpr size_t kGemmSmem = 1024 + (size_t)STAGES * STAGE_BYTES + 256;
-constexpr long long kWaitBudget = 4000000000LL;   // ~2 s of SM clock per wait
 
 // Instruction descriptor, kind::f16: D = F32 (bits 4-5), A = B = BF16 (bits 7-9, 10-12),
 // both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28.
@@ -72,65 +72,6 @@ struct GemmParams {
 };
 
 // ------------------------------------------------------------------ PTX helpers
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-                 "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Bounded wait for the phase with the given parity.  Gives up (returns false) when
-// another role has raised the abort flag or after ~2 s, recording `code` in *err.
-__device__ __noinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag,
-                                       int *err, int code) {
-    const long long t0 = clock64();
-    for (;;) {
-        if (mbar_test(bar, parity)) return true;
-        if (*abort_flag) return false;
-        if (clock64() - t0 > kWaitBudget) {
-            *abort_flag = 1;
-            atomicExch(err, code);
-            return false;
-        }
-    }
-}
-
-__device__ __forceinline__ void fence_barrier_init() {
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
-                                            uint64_t *bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
-        "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
-        : "memory");
-}
-
 __device__ __forceinline__ void tc_fence_before() {
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 }
@@ -513,26 +454,11 @@ __global__ void k_g_reduce(const float *__restrict__ part, int ksplit, int64_t B
 }
 
 // ------------------------------------------------------------------ host side
-PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    static std::mutex mu;
-    std::lock_guard<std::mutex> lk(mu);
-    if (!fn) {
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
-                                             &q) == cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
-    }
-    return fn;
-}
-
 // 2-D BF16 tensor (rows x cols, row-major, leading dimension ld elements), box
 // (64 columns x box_rows rows), 128-byte swizzle, zero fill outside.
 int make_map(sfh_ctx *ctx, CUtensorMap *map, const void *base, int64_t rows, int64_t cols,
              int64_t ld, int box_rows) {
-    auto enc = get_encode();
+    auto enc = sfh_tensor_map_encoder();
     if (!enc) return sfh_set_error(ctx, SFH_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
     if (((uintptr_t)base & 15) || ((ld * 2) & 15))
         return sfh_set_error(ctx, SFH_ERR_ARG, "tensor base/stride not 16-byte aligned");
@@ -733,4 +659,19 @@ int sfh_launch_fg_batched(sfh_ctx *ctx, const sfh_models *m, const double *d_R, 
     if ((rc = sfh_batched_prepare(ctx, m, B, d_data, ctx->scratch, ctx->scratch_bytes, &pl))) return rc;
     if ((rc = sfh_batched_launch(ctx, m, pl, d_R, d_negLogL, d_G, eps))) return rc;
     return sfh_batched_check(ctx, pl);
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 sfh_tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lk(mu);
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
 }

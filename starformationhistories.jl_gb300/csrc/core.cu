@@ -4,6 +4,7 @@
 
 #include <cstdio>
 #include <cstring>
+#include <cmath>
 #include <vector>
 
 #include "sfh_internal.cuh"
@@ -76,6 +77,7 @@ extern "C" int sfh_ctx_destroy(sfh_ctx *ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->stage) cudaFree(ctx->stage);
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     if (ctx->d_counters) cudaFree(ctx->d_counters);
     if (ctx->d_df_tab) cudaFree(ctx->d_df_tab);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -90,7 +92,7 @@ extern "C" const char *sfh_ctx_last_error(const sfh_ctx *ctx) {
 extern "C" int sfh_ctx_synchronize(sfh_ctx *ctx) {
     if (!ctx) return SFH_ERR_ARG;
     SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
-    return SFH_OK;
+    return sfh_check_onepass(ctx);  // a timed-out one-pass fg! since the last check
 }
 
 extern "C" int sfh_ctx_stream(sfh_ctx *ctx, void **stream_out) {
@@ -124,6 +126,17 @@ int sfh_scratch_reserve(sfh_ctx *ctx, size_t bytes) {
 int sfh_stage_reserve(sfh_ctx *ctx, size_t bytes) {
     return reserve(ctx, &ctx->stage, &ctx->stage_bytes, bytes);
 }
+int sfh_host_stage_reserve(sfh_ctx *ctx, size_t bytes) {
+    if (bytes <= ctx->h_stage_bytes) return SFH_OK;
+    SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+    ctx->h_stage = nullptr;
+    ctx->h_stage_bytes = 0;
+    const size_t want = bytes + bytes / 4;
+    SFH_CK(ctx, cudaMallocHost(&ctx->h_stage, want));
+    ctx->h_stage_bytes = want;
+    return SFH_OK;
+}
 
 // ------------------------------------------------------------------ models
 static void free_models(sfh_models *m) {
@@ -135,6 +148,8 @@ static void free_models(sfh_models *m) {
     if (m->col_lo) cudaFree(m->col_lo);
     if (m->row_hi) cudaFree(m->row_hi);
     if (m->row_lo) cudaFree(m->row_lo);
+    for (float *b : m->d_blk)
+        if (b) cudaFree(b);
     delete m;
 }
 
@@ -430,14 +445,26 @@ extern "C" int sfh_fg(sfh_ctx *ctx, const sfh_models *m, int dtype, const void *
     if (!ctx || !m || !coeffs || !data || !dtype_ok(dtype)) return SFH_ERR_ARG;
     SFH_CK(ctx, cudaSetDevice(ctx->device));
     const int64_t nb = m->nbins, nt = m->nt;
+    // inputs [r | n] and outputs [composite | G | -logL] each contiguous, so one DMA each
+    // way through the pinned mirror of the staging area, and one stream sync per call
     const size_t o_r = 0, o_n = sfh_align256(nt * 8), o_c = o_n + sfh_align256(nb * 8),
-                 o_g = o_c + sfh_align256(nb * 8), o_l = o_g + sfh_align256(nt * 8);
-    int rc = sfh_stage_reserve(ctx, o_l + 256);
+                 o_g = o_c + sfh_align256(nb * 8), o_l = o_g + sfh_align256(nt * 8),
+                 o_end = o_l + 8;
+    int rc = sfh_stage_reserve(ctx, o_end + 256);
     if (rc) return rc;
-    char *base = (char *)ctx->stage;
-    std::vector<double> t1, t2;
-    if ((rc = h2d_as_double(ctx, (double *)(base + o_r), coeffs, dtype, nt, t1))) return rc;
-    if ((rc = h2d_as_double(ctx, (double *)(base + o_n), data, dtype, nb, t2))) return rc;
+    if ((rc = sfh_host_stage_reserve(ctx, o_end + 256))) return rc;
+    char *base = (char *)ctx->stage, *hb = (char *)ctx->h_stage;
+    double *hr = (double *)(hb + o_r), *hn = (double *)(hb + o_n);
+    if (dtype == SFH_F64) {
+        memcpy(hr, coeffs, (size_t)nt * 8);
+        memcpy(hn, data, (size_t)nb * 8);
+    } else {
+        const float *cf = (const float *)coeffs, *df = (const float *)data;
+        for (int64_t i = 0; i < nt; ++i) hr[i] = cf[i];
+        for (int64_t i = 0; i < nb; ++i) hn[i] = df[i];
+    }
+    SFH_CK(ctx, cudaMemcpyAsync(base, hb, o_n + (size_t)nb * 8, cudaMemcpyHostToDevice,
+                                ctx->stream));
     FgArgs a{};
     a.coeffs = (const double *)(base + o_r);
     a.data = (const double *)(base + o_n);
@@ -448,17 +475,29 @@ extern "C" int sfh_fg(sfh_ctx *ctx, const sfh_models *m, int dtype, const void *
     a.gsign = 1.0;
     a.mode = FG_MODE_FG;
     if ((rc = sfh_launch_fg(ctx, m, a))) return rc;
-    if (negLogL) {
-        double v = 0;
-        SFH_CK(ctx, cudaMemcpyAsync(&v, base + o_l, sizeof(double), cudaMemcpyDeviceToHost,
+    // the output span actually needed: from the first requested array to the last
+    const size_t lo = composite ? o_c : (G ? o_g : o_l);
+    const size_t hi = negLogL ? o_end : (G ? o_g + (size_t)nt * 8 : o_c + (size_t)nb * 8);
+    if (composite || G || negLogL)
+        SFH_CK(ctx, cudaMemcpyAsync(hb + lo, base + lo, hi - lo, cudaMemcpyDeviceToHost,
                                     ctx->stream));
-        SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    if (negLogL) {
+        double v;
+        memcpy(&v, hb + o_l, 8);
+        if (std::isnan(v) && (rc = sfh_check_onepass(ctx))) return rc;  // timed-out one-pass
         *negLogL = dtype == SFH_F32 ? (double)(float)v : v;
     }
-    if (G && (rc = d2h_from_double(ctx, G, (const double *)(base + o_g), dtype, nt))) return rc;
-    if (composite && (rc = d2h_from_double(ctx, composite, (const double *)(base + o_c), dtype, nb)))
-        return rc;
-    SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    const double *hc = (const double *)(hb + o_c), *hg = (const double *)(hb + o_g);
+    if (dtype == SFH_F64) {
+        if (G) memcpy(G, hg, (size_t)nt * 8);
+        if (composite) memcpy(composite, hc, (size_t)nb * 8);
+    } else {
+        if (G)
+            for (int64_t i = 0; i < nt; ++i) ((float *)G)[i] = (float)hg[i];
+        if (composite)
+            for (int64_t i = 0; i < nb; ++i) ((float *)composite)[i] = (float)hc[i];
+    }
     return SFH_OK;
 }
 

@@ -725,6 +725,15 @@ int sfh_launch_fg(sfh_ctx *ctx, const sfh_models *m, const FgArgs &a, cudaEvent_
     const void *Mptr = f64 ? m->d_col : (const void *)m->d_f32;
     if (!Mptr) return sfh_set_error(ctx, SFH_ERR_ARG, "models handle has no matrix");
     const int64_t nbins = m->nbins, nt = m->nt;
+    // one-pass kernel (onepass.cu) for fg! with G on FP32 storage
+    if (!f64 && a.mode == FG_MODE_FG && a.G && a.data &&
+        (m->path == SFH_PATH_ONEPASS ||
+         (m->path == SFH_PATH_AUTO && sfh_onepass_eligible(ctx, m)))) {
+        int rc = sfh_scratch_reserve(ctx, sfh_onepass_scratch(ctx, m));
+        if (rc) return rc;
+        return sfh_launch_fg_onepass(ctx, const_cast<sfh_models *>(m), a.coeffs, a.data,
+                                     a.composite, a.G, a.negLogL, a.eps, a.gsign, ctx->scratch, ev);
+    }
     const bool fused_path = !f64 && (a.mode == FG_MODE_FG || a.mode == FG_MODE_COMPOSITE);
     const Plan p = make_plan(ctx, nbins, nt, f64, fused_path, m);
     int rc = sfh_scratch_reserve(ctx, p.total);
@@ -960,6 +969,7 @@ extern "C" int sfh_models_autotune(sfh_ctx *ctx, sfh_models *m, const double *d_
     int rc = SFH_OK;
     m->tune_R = best_R;
     m->tune_w2 = best_w2;
+    m->path = SFH_PATH_TWOPASS;
     for (int q = 0; q < nks; ++q) {  // pass 1 (pass 2 fixed at the default)
         m->tune_ks = KS[q];
         if ((rc = timed(t1, t2))) break;
@@ -973,15 +983,35 @@ extern "C" int sfh_models_autotune(sfh_ctx *ctx, sfh_models *m, const double *d_
             if ((rc = timed(t1, t2))) break;
             if (t2 < b2) { b2 = t2; best_R = RR[r]; best_w2 = w2; }
         }
+    m->tune_ks = best_ks;
+    m->tune_R = best_R;
+    m->tune_w2 = best_w2;
+    m->onepass_ms = 0.0;
+    if (rc == SFH_OK && sfh_onepass_eligible(ctx, m)) {  // one-pass tile widths against the best plan
+        m->path = SFH_PATH_ONEPASS;
+        double best_op = 1e300;
+        int best_bins = 16, best_lag = 1;
+        for (int v = 0; v < 4 && rc == SFH_OK; ++v) {  // tile width x lag
+            m->onepass_bins = v < 2 ? 16 : 32;
+            m->onepass_lag = v & 1;
+            if ((rc = timed(t1, t2)) != SFH_OK) break;
+            if (t1 + t2 < best_op) { best_op = t1 + t2; best_bins = m->onepass_bins; best_lag = m->onepass_lag; }
+        }
+        m->onepass_bins = best_bins;
+        m->onepass_lag = best_lag;
+        if (rc == SFH_OK) {
+            m->onepass_ms = best_op;
+            if (best_op >= b1 + b2) m->path = SFH_PATH_TWOPASS;
+        }
+    }
     for (int k = 0; k < 5; ++k) cudaEventDestroy(ev[k]);
     cudaFree(buf);
     if (rc) {
         m->tune_ks = m->tune_R = m->tune_w2 = 0;
+        m->path = SFH_PATH_AUTO;
+        m->onepass_bins = 0;
         return rc;
     }
-    m->tune_ks = best_ks;
-    m->tune_R = best_R;
-    m->tune_w2 = best_w2;
     if (plan_out) {
         plan_out[0] = best_ks;
         plan_out[1] = best_R;
@@ -1143,5 +1173,45 @@ extern "C" int sfh_fg_dev_noalloc(void *stream, const float *d_models, int64_t n
     k_reduce_g<<<(int)((ntempl + kThreads - 1) / kThreads), kThreads, 0, st>>>(partG, nchunks,
                                                                                 ntempl, 1.0, d_G);
     if (cudaGetLastError() != cudaSuccess) return SFH_ERR_CUDA;
+    return SFH_OK;
+}
+
+extern "C" int sfh_models_set_path(sfh_ctx *ctx, sfh_models *m, int path) {
+    if (!ctx || !m || path < SFH_PATH_AUTO || path > SFH_PATH_TWOPASS) return SFH_ERR_ARG;
+    if (path == SFH_PATH_ONEPASS && !sfh_onepass_eligible(ctx, m))
+        return sfh_set_error(ctx, SFH_ERR_UNSUPPORTED,
+                             "one-pass fg! needs FP32 storage and nt <= 1536");
+    m->path = path;
+    return SFH_OK;
+}
+
+extern "C" int sfh_models_set_onepass_tile(sfh_ctx *ctx, sfh_models *m, int bins, int lag) {
+    if (!ctx || !m || (bins != 16 && bins != 32) || (lag != 0 && lag != 1)) return SFH_ERR_ARG;
+    m->onepass_bins = bins;
+    m->onepass_lag = lag;
+    return SFH_OK;
+}
+
+extern "C" int sfh_models_path(sfh_ctx *ctx, const sfh_models *m, int *path_out,
+                               double *onepass_ms) {
+    if (!ctx || !m) return SFH_ERR_ARG;
+    const bool one = m->storage != SFH_F64 &&
+                     (m->path == SFH_PATH_ONEPASS ||
+                      (m->path == SFH_PATH_AUTO && sfh_onepass_eligible(ctx, m)));
+    if (path_out) *path_out = one ? SFH_PATH_ONEPASS : SFH_PATH_TWOPASS;
+    if (onepass_ms) *onepass_ms = m->onepass_ms;
+    return SFH_OK;
+}
+
+int sfh_check_onepass(sfh_ctx *ctx) {
+    unsigned int h = 0;
+    SFH_CK(ctx, cudaMemcpyAsync(&h, ctx->d_counters + SFH_CNT_ONEPASS_ERR, sizeof(h),
+                                cudaMemcpyDeviceToHost, ctx->stream));
+    SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h) {
+        SFH_CK(ctx, cudaMemsetAsync(ctx->d_counters + SFH_CNT_ONEPASS_ERR, 0, sizeof(h), ctx->stream));
+        SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+        return sfh_set_error(ctx, SFH_ERR_TIMEOUT, "one-pass fg! pipeline wait timed out");
+    }
     return SFH_OK;
 }

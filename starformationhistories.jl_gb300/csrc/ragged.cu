@@ -12,10 +12,12 @@
 // then a per-galaxy reduction of the row-tile logL partials (fixed order, so results
 // are reproducible).  Column groups are issued largest galaxy first.
 // Galaxies with at most kFuseMax templates take one fused pass instead: each thread
-// keeps its bin's row of M in registers, forms m, the Poisson term and w, and the
-// per-template products M w are summed across the warp by a recursive-halving
-// transpose (31 shuffles for 32 templates), across the CTA in shared memory and across
-// tiles by a fixed-order per-galaxy finish.  M is then read once per evaluation.
+// walks kFuseRows bins, keeps each bin's row of M in registers, forms m, the Poisson
+// term and w, and accumulates the per-template products M w; these are summed across
+// the warp by a recursive-halving transpose (31 shuffles for 32 templates), across the
+// CTA in shared memory and across tiles by a fixed-order per-galaxy finish.  M is then
+// read once per evaluation.  Fused galaxies are launched by register class (nt <= 8,
+// <= 16, <= 32), so a batch with a few wide galaxies does not widen every tile.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -29,6 +31,7 @@ struct sfh_galaxies {
     int64_t ngal, total_bins, total_templ, n_row_tiles, n_col_tiles, max_nt;
     int64_t n_fused_tiles;  // tiles of galaxies with <= kFuseMax templates
     int64_t n_fused_gal, n_big_gal, max_fused_nt;
+    int64_t n_fused_class[3];  // fused tiles with nt <= 8, <= 16, <= 32 (in that order)
     void *d_desc;       // GalDesc[ngal]
     void *d_rows;       // RowTile[n_row_tiles] (two-pass galaxies)
     void *d_cols;       // ColTile[n_col_tiles] (two-pass galaxies)
@@ -44,6 +47,10 @@ constexpr int kRT = 256;       // threads per CTA, rows per pass-1 tile
 constexpr int kColGroup = 8;   // templates per pass-2 CTA
 constexpr int kRChunk = 2048;  // coefficients staged in shared memory at a time
 constexpr int kFuseMax = 32;   // templates per galaxy held in registers by the fused pass
+constexpr int kFuseRows = 4;   // bins per thread in the fused pass (tile = kFuseRows * kRT rows)
+
+constexpr int64_t kFuseStep = (int64_t)kRT * kFuseRows;
+__host__ __device__ inline int fused_class(int64_t nt) { return nt <= 8 ? 0 : nt <= 16 ? 1 : 2; }
 
 struct GalDesc {
     int64_t moff, nbins, nt, boff, toff, tile0, ntiles;
@@ -188,20 +195,23 @@ k_ragged_pass2(const float *__restrict__ M, const GalDesc *__restrict__ gals,
 }
 
 // One fused fg! pass for galaxies with nt <= kFuseMax: m, Poisson terms, w and the
-// tile's partial G = Mᵀ w (gpart, kFuseMax doubles per tile).
+// tile's partial G = Mᵀ w (gpart, kFuseMax doubles per tile).  Tiles tile_base + blockIdx.x
+// of the fused list; each thread takes kFuseRows bins (rows row0 + r * kRT + tid), so the
+// table load, the block reduction and the transpose are paid once per kFuseRows * kRT bins.
 template <int NT>
-__global__ void __launch_bounds__(kRT)
+__global__ void __launch_bounds__(kRT, NT <= 8 ? 4 : NT <= 16 ? 3 : 2)
 k_ragged_fused(const float *__restrict__ M, const GalDesc *__restrict__ gals,
                const RowTile *__restrict__ tiles, const double *__restrict__ coeffs,
                const double *__restrict__ data, double *__restrict__ composite,
                double *__restrict__ tile_logl, double *__restrict__ gpart, float eps,
-               int want_logl, int want_g, const sfh_df *__restrict__ tab) {
+               int want_logl, int want_g, const sfh_df *__restrict__ tab, int tile_base) {
     __shared__ float rhi[NT], rlo[NT];
     __shared__ double s_red[kRT / 32];
     __shared__ float s_g[kRT / 32][NT];
     __shared__ sfh_df s_tab[SFH_DF_TAB_ALL];
     for (int k = threadIdx.x; k < SFH_DF_TAB_ALL; k += kRT) s_tab[k] = tab[k];
-    const RowTile tile = tiles[blockIdx.x];
+    const int64_t t = (int64_t)tile_base + blockIdx.x;
+    const RowTile tile = tiles[t];
     const GalDesc G = gals[tile.g];
     const int nt = (int)G.nt;
     if (threadIdx.x < NT) {
@@ -211,36 +221,52 @@ k_ragged_fused(const float *__restrict__ M, const GalDesc *__restrict__ gals,
         rlo[threadIdx.x] = __double2float_rn(v - (double)h);
     }
     __syncthreads();
-    const int64_t i = (int64_t)tile.row0 + threadIdx.x;
-    const bool live = i < G.nbins;
-    const float *col = M + G.moff + i;
-    float m[NT];
-#pragma unroll
-    for (int j = 0; j < NT; ++j)
-        m[j] = (live && j < nt) ? __ldg(col + (int64_t)j * G.nbins) : 0.f;
-    float ah = 0.f, al = 0.f;
-#pragma unroll
-    for (int j0 = 0; j0 < NT; j0 += 8) {
-        float s = 0.f;
-#pragma unroll
-        for (int u = 0; u < 8; ++u) s = fmaf(m[j0 + u], rhi[j0 + u], fmaf(m[j0 + u], rlo[j0 + u], s));
-        sfh_two_sum_acc(ah, al, s);
-    }
     sfh_df term{0.f, 0.f};
-    float w = 0.f;
-    if (live) bin_terms(ah, al, data, G.boff + i, eps, want_logl, want_g, s_tab, composite, term, w);
+    float v[NT];
+#pragma unroll
+    for (int j = 0; j < NT; ++j) v[j] = 0.f;
+#pragma unroll 1
+    for (int r = 0; r < kFuseRows; ++r) {
+        if ((int64_t)tile.row0 + r * kRT >= G.nbins) break;  // uniform over the CTA
+        const int64_t i = (int64_t)tile.row0 + r * kRT + threadIdx.x;
+        const bool live = i < G.nbins;
+        const float *col = M + G.moff + i;
+        // templates in groups of four behind branches that are uniform over the CTA (one
+        // galaxy per tile): a galaxy with nt < NT issues no loads or products for the rest
+        float m[NT];
+#pragma unroll
+        for (int j0 = 0; j0 < NT; j0 += 4)
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                m[j0 + u] = (j0 < nt && live && j0 + u < nt)
+                                ? __ldg(col + (int64_t)(j0 + u) * G.nbins) : 0.f;
+        float ah = 0.f, al = 0.f;
+#pragma unroll
+        for (int j0 = 0; j0 < NT; j0 += 4) {
+            if (j0 >= nt) break;
+            float s = 0.f;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) s = fmaf(m[j0 + u], rhi[j0 + u], fmaf(m[j0 + u], rlo[j0 + u], s));
+            sfh_two_sum_acc(ah, al, s);
+        }
+        float w = 0.f;
+        if (live) bin_terms(ah, al, data, G.boff + i, eps, want_logl, want_g, s_tab, composite, term, w);
+#pragma unroll
+        for (int j0 = 0; j0 < NT; j0 += 4) {
+            if (j0 >= nt) break;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) v[j0 + u] = fmaf(m[j0 + u], w, v[j0 + u]);
+        }
+    }
     if (want_logl) {
         double tsum = 0.0;
         sfh_df_block_sum(term, s_red, &tsum);
-        if (threadIdx.x == 0) tile_logl[blockIdx.x] = tsum;
+        if (threadIdx.x == 0) tile_logl[t] = tsum;
     }
     if (!want_g) return;
     // warp transpose-reduce over NT templates: after the step with offset o (o < NT)
     // each lane keeps o partial column sums; lanes that differ only in bits >= log2(NT)
     // hold the same columns and are folded first.  Lane l then holds template l % NT.
-    float v[NT];
-#pragma unroll
-    for (int j = 0; j < NT; ++j) v[j] = m[j] * w;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int o = 16; o >= NT; o >>= 1)
@@ -262,7 +288,7 @@ k_ragged_fused(const float *__restrict__ M, const GalDesc *__restrict__ gals,
         sfh_df acc{0.f, 0.f};
 #pragma unroll
         for (int wgi = 0; wgi < kRT / 32; ++wgi) acc = df_add_f(acc, s_g[wgi][threadIdx.x]);
-        gpart[(int64_t)blockIdx.x * kFuseMax + threadIdx.x] = sfh_f2d(acc.h) + sfh_f2d(acc.l);
+        gpart[t * kFuseMax + threadIdx.x] = sfh_f2d(acc.h) + sfh_f2d(acc.l);
     }
 }
 
@@ -326,16 +352,33 @@ extern "C" int sfh_galaxies_create(sfh_ctx *ctx, const float *d_models, int64_t 
         d.nt = h.ntempl;
         d.boff = h.bin_offset;
         d.toff = h.templ_offset;
-        d.ntiles = (h.nbins + kRT - 1) / kRT;
         d.fused = h.ntempl <= kFuseMax ? 1 : 0;
-        std::vector<RowTile> &list = d.fused ? fused : rows;
-        d.tile0 = (int64_t)list.size();
-        for (int64_t r0 = 0; r0 < h.nbins; r0 += kRT) list.push_back(RowTile{(int32_t)g, (int32_t)r0});
-        (d.fused ? fused_ids : big_ids).push_back((int32_t)g);
-        if (d.fused) maxfnt = std::max(maxfnt, h.ntempl);
+        if (!d.fused) {
+            d.ntiles = (h.nbins + kRT - 1) / kRT;
+            d.tile0 = (int64_t)rows.size();
+            for (int64_t r0 = 0; r0 < h.nbins; r0 += kRT) rows.push_back(RowTile{(int32_t)g, (int32_t)r0});
+            big_ids.push_back((int32_t)g);
+        } else {
+            d.ntiles = (h.nbins + kFuseStep - 1) / kFuseStep;
+            fused_ids.push_back((int32_t)g);
+            maxfnt = std::max(maxfnt, h.ntempl);
+        }
         tb = std::max(tb, h.bin_offset + h.nbins);
         tt = std::max(tt, h.templ_offset + h.ntempl);
         maxnt = std::max(maxnt, h.ntempl);
+    }
+    // fused tiles grouped by register class (nt <= 8, <= 16, <= 32): one launch per class
+    int64_t ncls[3] = {0, 0, 0};
+    for (int c = 0; c < 3; ++c) {
+        const int64_t before = (int64_t)fused.size();
+        for (int32_t g : fused_ids) {
+            GalDesc &d = desc[(size_t)g];
+            if (fused_class(d.nt) != c) continue;
+            d.tile0 = (int64_t)fused.size();
+            for (int64_t r0 = 0; r0 < d.nbins; r0 += kFuseStep)
+                fused.push_back(RowTile{(int32_t)g, (int32_t)r0});
+        }
+        ncls[c] = (int64_t)fused.size() - before;
     }
     // column groups of the two-pass galaxies, largest galaxy first (shortens the tail)
     std::vector<int32_t> order(big_ids);
@@ -359,6 +402,7 @@ extern "C" int sfh_galaxies_create(sfh_ctx *ctx, const float *d_models, int64_t 
     G->n_big_gal = (int64_t)big_ids.size();
     G->max_nt = maxnt;
     G->max_fused_nt = maxfnt;
+    for (int c = 0; c < 3; ++c) G->n_fused_class[c] = ncls[c];
     G->d_models = d_models;
     void **bufs[] = {&G->d_desc, &G->d_rows, &G->d_cols, &G->d_fused, &G->d_fused_ids, &G->d_big_ids};
     const void *src[] = {desc.data(), rows.data(), cols.data(), fused.data(), fused_ids.data(),
@@ -424,13 +468,18 @@ extern "C" int sfh_fg_ragged_dev(sfh_ctx *ctx, const sfh_galaxies *gal, const do
     const GalDesc *desc = (const GalDesc *)gal->d_desc;
     cudaStream_t st = ctx->stream;
     if (gal->n_fused_gal) {
-        auto kern = gal->max_fused_nt <= 8    ? k_ragged_fused<8>
-                    : gal->max_fused_nt <= 16 ? k_ragged_fused<16>
-                                              : k_ragged_fused<32>;
-        kern<<<(unsigned)gal->n_fused_tiles, kRT, 0, st>>>(
-            gal->d_models, desc, (const RowTile *)gal->d_fused, d_coeffs, d_data, d_composite, tf,
-            gp, (float)eps, want_logl ? 1 : 0, want_w ? 1 : 0, ctx->d_df_tab);
-        SFH_LAUNCHED(ctx);
+        decltype(&k_ragged_fused<8>) kerns[3] = {k_ragged_fused<8>, k_ragged_fused<16>,
+                                                 k_ragged_fused<32>};
+        int64_t base = 0;
+        for (int c = 0; c < 3; ++c) {
+            const int64_t n = gal->n_fused_class[c];
+            if (!n) continue;
+            kerns[c]<<<(unsigned)n, kRT, 0, st>>>(
+                gal->d_models, desc, (const RowTile *)gal->d_fused, d_coeffs, d_data, d_composite,
+                tf, gp, (float)eps, want_logl ? 1 : 0, want_w ? 1 : 0, ctx->d_df_tab, (int)base);
+            SFH_LAUNCHED(ctx);
+            base += n;
+        }
         if (want_logl || want_w) {
             k_ragged_finish<<<(unsigned)gal->n_fused_gal, kRT, 0, st>>>(
                 desc, (const int32_t *)gal->d_fused_ids, tf, gp, want_logl ? d_negLogL : nullptr,

@@ -1,5 +1,6 @@
 // sfh_internal.cuh -- shared declarations of the sm_103a Hess-diagram library.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include <stdint.h>
@@ -21,6 +22,9 @@ struct sfh_ctx {
     // Device staging used by the host-array entry points.
     void *stage = nullptr;
     size_t stage_bytes = 0;
+    // Pinned host mirror of `stage` (one DMA each way per host-array call).
+    void *h_stage = nullptr;
+    size_t h_stage_bytes = 0;
     // Zero-initialised counters for last-block reductions (reset by the last block).
     unsigned int *d_counters = nullptr;
     // log(1 + j/128), j = 0..128, then n - n log n, n = 0..255, as double-float pairs
@@ -45,6 +49,16 @@ struct sfh_models {
     // Single-vector launch plan chosen by sfh_models_autotune (0 = built-in heuristics):
     // pass-1 template splits, pass-2 row chunk, pass-2 waves.
     int tune_ks = 0, tune_R = 0, tune_w2 = 0;
+    // Single-vector fg! path (SFH_PATH_*): AUTO takes the one-pass kernel when the
+    // shape fits it; sfh_models_autotune replaces AUTO by the faster measured path.
+    int path = SFH_PATH_AUTO;
+    double onepass_ms = 0.0;  // measured by sfh_models_autotune (0: not measured)
+    // One-pass tile width (16 or 32 bins; 0: 16) and, per width, the blocked copy of d_f32
+    // it streams (built on first use): for tile t and box c (64 templates) one contiguous
+    // block of [64 templates][bins] floats, blocks in (tile, box) order, zero padded.
+    int onepass_bins = 0;
+    int onepass_lag = 1;  // 1: G products one tile behind (overlap the finish), 0: in step
+    float *d_blk[2] = {nullptr, nullptr};
 };
 
 // Counter slots in sfh_ctx::d_counters (zeroed at context creation; every kernel that
@@ -53,6 +67,8 @@ enum {
     SFH_CNT_LOGL = 0,          // k_finalize last-block reduction
     SFH_CNT_BATCH = 1,
     SFH_CNT_FG_LOGL = 2,       // fused pass 1: last row tile
+    SFH_CNT_ONEPASS_ERR = 3,   // one-pass fg!: a wait timed out (cleared by the host check)
+    SFH_CNT_ONEPASS_BAR = 4,   // one-pass fg! grid barrier: arrivals (4), generation (5)
     SFH_CNT_ROWTILE = 256,     // fused pass 1: one per row tile (<= 32768)
     SFH_CNT_COLGROUP = 256 + 32768,  // fused pass 2: one per column group (<= 16384)
     SFH_CNT_SLOTS = 65536
@@ -78,6 +94,7 @@ int sfh_cuda_error(sfh_ctx *ctx, cudaError_t e, const char *what);
 // Ensures ctx->scratch holds at least `bytes` (256-byte aligned sub-allocations).
 int sfh_scratch_reserve(sfh_ctx *ctx, size_t bytes);
 int sfh_stage_reserve(sfh_ctx *ctx, size_t bytes);
+int sfh_host_stage_reserve(sfh_ctx *ctx, size_t bytes);
 
 static inline size_t sfh_align256(size_t b) { return (b + 255) & ~size_t(255); }
 
@@ -195,6 +212,15 @@ enum {
     FG_MODE_GRAD_GIVEN = 2   // ∇loglikelihood! from a given composite
 };
 int sfh_launch_fg(sfh_ctx *ctx, const sfh_models *m, const FgArgs &a, cudaEvent_t *ev = nullptr);
+// One-pass single-vector fg! (onepass.cu): FP32 storage, nt <= 1536.
+bool sfh_onepass_eligible(sfh_ctx *ctx, const sfh_models *m);
+size_t sfh_onepass_scratch(const sfh_ctx *ctx, const sfh_models *m);
+int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
+                          const double *d_data, double *d_composite, double *d_G,
+                          double *d_negLogL, double eps, double gsign, void *scratch,
+                          cudaEvent_t *ev);
+// Reads and clears the one-pass timeout slot (synchronises the stream).
+int sfh_check_onepass(sfh_ctx *ctx);
 int sfh_launch_loglikelihood(sfh_ctx *ctx, const double *composite, const double *data,
                              int64_t nbins, double eps, double *d_out);
 

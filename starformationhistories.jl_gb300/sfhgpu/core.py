@@ -130,6 +130,37 @@ class Models:
               self.ctx.handle, "models_combine")
         return Models(ctx=self.ctx, storage=st, _handle=h, _shape=(self.nbins, len(groups)))
 
+    PATHS = {"auto": 0, "onepass": 1, "twopass": 2}
+
+    def set_path(self, path):
+        """Single-vector fg! path for calls with G: "onepass" (one read of the matrix;
+        FP32 storage, nt <= 1536; keeps a blocked copy of the templates), "twopass" or
+        "auto" (sfh_models_set_path)."""
+        check(load().sfh_models_set_path(self.ctx.handle, self._h, self.PATHS[path]),
+              self.ctx.handle, "models_set_path")
+
+    def set_onepass_tile(self, bins, lag=True):
+        """One-pass variant: 16 or 32 bins per tile; lag=True forms the G products one tile
+        behind the composite (sfh_models_set_onepass_tile)."""
+        check(load().sfh_models_set_onepass_tile(self.ctx.handle, self._h, int(bins), int(bool(lag))),
+              self.ctx.handle, "models_set_onepass_tile")
+
+    @property
+    def path(self):
+        """The path fg! calls with G take on this handle now: "onepass" or "twopass"."""
+        p = C.c_int()
+        check(load().sfh_models_path(self.ctx.handle, self._h, C.byref(p), None), self.ctx.handle,
+              "models_path")
+        return {1: "onepass", 2: "twopass"}[p.value]
+
+    @property
+    def onepass_ms(self):
+        """One-pass fg! time measured by autotune (0.0 if not measured)."""
+        ms = C.c_double()
+        check(load().sfh_models_path(self.ctx.handle, self._h, None, C.byref(ms)), self.ctx.handle,
+              "models_path")
+        return ms.value
+
     def autotune(self, coeffs, data, iters=10, eps=None):
         """Pick the fastest single-vector fg! launch plan for this matrix by timing the
         candidates on the device (sfh_models_autotune).  Returns

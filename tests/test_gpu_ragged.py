@@ -93,7 +93,8 @@ def _ragged_problem(rng, shapes, n_stars=1e4, zero_frac=0.2):
 def test_fg_ragged_matches_oracle(sfh, O, torch, seed):
     rng = np.random.default_rng(seed)
     shapes = [(int(rng.integers(50, 300)) * int(rng.integers(50, 300)), int(rng.integers(1, 40)))
-              for _ in range(7)] + [(1, 3), (257, 1), (2500, 8)]
+              for _ in range(7)] + [(1, 3), (257, 1), (2500, 8), (1024, 16), (1025, 12),
+                                    (4096, 32), (1023, 17), (3073, 9)]
     Ms, rs, ns = _ragged_problem(rng, shapes)
     dev = torch.device("cuda", 0)
     packed = torch.as_tensor(np.concatenate([M.ravel(order="F") for M in Ms]), device=dev)
