@@ -141,11 +141,9 @@ enum sfh_fg_path { SFH_PATH_AUTO = 0, SFH_PATH_ONEPASS = 1, SFH_PATH_TWOPASS = 2
 /* Sets the path of later fg! calls on this handle (SFH_ERR_UNSUPPORTED when ONEPASS is
    asked for a shape it cannot take). */
 int sfh_models_set_path(sfh_ctx *ctx, sfh_models *models, int path);
-/* One-pass variant: 16 or 32 bins per tile, and lag = 1 to form the G products one tile
-   behind the composite (overlapping the per-tile finish, two tiles resident) or 0 (one tile
-   resident, more of the ring left to the stream).  Default 16 / 1; the autotuner measures
-   all four and shapes that do not fit a variant fall back to a smaller one. */
-int sfh_models_set_onepass_tile(sfh_ctx *ctx, sfh_models *models, int bins, int lag);
+/* Tile width of the one-pass kernel: 16 or 32 bins per tile (default 16; the autotuner
+   measures both; a shape whose tile does not fit the 32-bin ring takes 16). */
+int sfh_models_set_onepass_tile(sfh_ctx *ctx, sfh_models *models, int bins);
 /* The path fg! calls with G take on this handle now (ONEPASS or TWOPASS), and the
    one-pass time measured by sfh_models_autotune (0 if not measured); either may be NULL. */
 int sfh_models_path(sfh_ctx *ctx, const sfh_models *models, int *path_out, double *onepass_ms);

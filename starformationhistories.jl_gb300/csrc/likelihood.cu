@@ -990,15 +990,13 @@ extern "C" int sfh_models_autotune(sfh_ctx *ctx, sfh_models *m, const double *d_
     if (rc == SFH_OK && sfh_onepass_eligible(ctx, m)) {  // one-pass tile widths against the best plan
         m->path = SFH_PATH_ONEPASS;
         double best_op = 1e300;
-        int best_bins = 16, best_lag = 1;
-        for (int v = 0; v < 4 && rc == SFH_OK; ++v) {  // tile width x lag
-            m->onepass_bins = v < 2 ? 16 : 32;
-            m->onepass_lag = v & 1;
+        int best_bins = 16;
+        for (int bins : {16, 32}) {  // tile widths
+            m->onepass_bins = bins;
             if ((rc = timed(t1, t2)) != SFH_OK) break;
-            if (t1 + t2 < best_op) { best_op = t1 + t2; best_bins = m->onepass_bins; best_lag = m->onepass_lag; }
+            if (t1 + t2 < best_op) { best_op = t1 + t2; best_bins = bins; }
         }
         m->onepass_bins = best_bins;
-        m->onepass_lag = best_lag;
         if (rc == SFH_OK) {
             m->onepass_ms = best_op;
             if (best_op >= b1 + b2) m->path = SFH_PATH_TWOPASS;
@@ -1185,10 +1183,9 @@ extern "C" int sfh_models_set_path(sfh_ctx *ctx, sfh_models *m, int path) {
     return SFH_OK;
 }
 
-extern "C" int sfh_models_set_onepass_tile(sfh_ctx *ctx, sfh_models *m, int bins, int lag) {
-    if (!ctx || !m || (bins != 16 && bins != 32) || (lag != 0 && lag != 1)) return SFH_ERR_ARG;
+extern "C" int sfh_models_set_onepass_tile(sfh_ctx *ctx, sfh_models *m, int bins) {
+    if (!ctx || !m || (bins != 16 && bins != 32)) return SFH_ERR_ARG;
     m->onepass_bins = bins;
-    m->onepass_lag = lag;
     return SFH_OK;
 }
 

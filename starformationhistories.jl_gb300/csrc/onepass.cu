@@ -1,34 +1,35 @@
 // onepass.cu -- fg! for one coefficient vector with a single read of the template matrix
-// (FP32 storage, column-major nbins x nt).
+// (FP32 storage).
 //
 // fg! (src/fitting/solvers.jl:20-38: composite!, loglikelihood, ∇loglikelihood!,
 // fitting_base.jl:55-96, 265-285) needs every template of a bin before w = 1 - n/max(m, eps)
 // and G = Mᵀ w can be formed, so the two-kernel form reads M twice.  Here each SM keeps
-// tiles of 32 bins x all templates (nt <= kMaxTemplates) in shared memory:
+// a tile of BINS bins (16 or 32) x all templates (nt <= 1536) in shared memory:
 //
-//   one persistent CTA per SM, 16 warps; tiles of BINS = 16 (or 32) bins;
-//   warp 15 (4 lanes)  producers: boxes of BINS bins x 64 templates (bulk copies of the
-//                      blocked copy) into a ring of shared-memory slots, full / empty
-//                      mbarriers per slot; lane p issues every fourth box;
-//   box c belongs to owner warp c % 14 in both phases; lane l reads its rows (one 16-byte
-//   shared load per row and 4 bins; a warp load covers whole rows, conflict-free);
-//   phase A   as its boxes land, an owner forms m r for the lane's 4 bins (r split hi + lo,
-//             packed FP32 pairs, compensated per box) and sums the lanes that share bins;
-//   finish    warp 14 sums the 14 owner partials (double-float, fixed order), forms
-//             max(m, eps), w = 1 - n/m, the composite, and the Poisson term
-//             (double-float, sfh_dfloat.cuh) one step later;
-//   phase B   one tile behind phase A (so it overlaps the finish), an owner forms M w
-//             over the lane's 4 bins for each of its rows, accumulated over the CTA's tiles
-//             in per-lane double-float registers, and releases each box after reading it;
-//             the lanes of a row are summed once, at the end.
-// The kernel streams a blocked copy of the templates (one contiguous block per tile and
-// box, tiles in order) with 1-D bulk copies, so every CTA reads long sequential runs of
-// HBM; the copy is made once per handle and tile width (k_onepass_block).
-// The CTAs' G and logL partials are summed after a grid barrier, in a fixed order, so
-// results are reproducible.  M crosses HBM once per evaluation.  Every mbarrier wait is bounded:
-// on timeout the CTA stops at a tile boundary (all warps together, so no CTA barrier is
-// left waiting), drains its TMA loads, raises the error slot, and the reduction writes NaN
-// to G and -logL.
+//   one persistent CTA per SM, 16 warps;
+//   warp 15, 4 lanes    producers: boxes of BINS bins x 64 templates (1-D bulk copies of a
+//                       blocked copy of the matrix, one contiguous block per tile and box)
+//                       into a ring of shared-memory slots with full / empty mbarriers; lane p
+//                       issues every fourth box, so four copies are issued concurrently;
+//   warps 0-13          owners: half-box unit u (32 template rows of box u / 2) belongs to
+//                       owner u % 14 (one 16-byte shared load per lane: 4 bins of a row);
+//   warp 14             the Poisson terms.
+// Per tile, two named barriers:
+//   phase A   owners form m r for their units as the boxes land (r split hi + lo, packed
+//             FP32 pairs, compensated per unit) and sum the lanes that share bins;
+//   bar 1
+//   finish    owners 0-7: each bin's 14 owner partials summed by a group of lanes (fixed
+//             shuffle tree, double-float), max(m, eps), w = 1 - n/m, the composite;
+//   bar 2
+//   phase B   owners form M w over their units, accumulated over the CTA's tiles in
+//             per-lane double-float registers, and release each unit's box (two owners
+//             per box); warp 14 forms the tile's Poisson terms (double-float,
+//             sfh_dfloat.cuh) meanwhile.
+// After the last tile the CTAs' G and logL partials are summed after a grid barrier in a
+// fixed order, so results are reproducible.  M crosses HBM once per evaluation.  Every
+// wait is bounded: on timeout the CTA stops at a tile boundary (all warps together, so no
+// CTA barrier is left waiting), drains its copies, raises the error slot, and G and -logL
+// become NaN.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
@@ -40,26 +41,28 @@
 
 namespace {
 
-constexpr int kBoxCols = 64;                      // templates per TMA box
-constexpr int kOwners = 14;                       // warps that own boxes: box c -> warp c % 14
-constexpr int kFinishWarp = kOwners;              // forms m, w and the Poisson terms
-constexpr int kWarps = kOwners + 1;               // consumer warps
-constexpr int kThreadsOP = (kWarps + 1) * 32;     // + producer warp (16 warps: 128 registers)
+constexpr int kBoxCols = 64;                      // templates per box
+constexpr int kOwners = 14;                       // warps 0-13
+constexpr int kPoissonWarp = kOwners;             // warp 14
+constexpr int kWarps = kOwners + 1;               // consumer warps (named barriers)
+constexpr int kThreadsOP = (kWarps + 1) * 32;     // + producer warp: 16 warps, 128 registers
+constexpr int kFinishers = 8;                     // owners that also finish the bins
 constexpr int kMaxBoxes = 24;                     // boxes per tile
-constexpr int kBoxesPerWarp = (kMaxBoxes + kOwners - 1) / kOwners;  // 2
 constexpr int kMaxTemplates = kMaxBoxes * kBoxCols;  // 1536
+constexpr int kUnits = (2 * kMaxBoxes + 13) / 14;  // half-box units per owner (4)
 constexpr int kMaxSlots = 64;
 constexpr int kProducers = 4;                     // issuing lanes of the producer warp
 
-// Tile geometry for BINS bins per tile (16 or 32): a box is BINS x 64 floats; a template
-// row of a box is BINS/4 lanes of one 16-byte load, so a warp load covers 32/(BINS/4) rows.
+// Tile geometry for BINS bins per tile: a box is [64 rows][BINS] floats; a row is LPR lanes
+// of one 16-byte load, a warp load covers RPL rows, a half-box unit (32 rows) GU loads.
 template <int BINS>
 struct Geo {
     static constexpr int kBoxFloats = BINS * kBoxCols;
     static constexpr int kBoxBytes = kBoxFloats * 4;
-    static constexpr int kLanesPerRow = BINS / 4;
-    static constexpr int kRowsPerLoad = 32 / kLanesPerRow;
-    static constexpr int kRows = kBoxCols / kRowsPerLoad;  // rows of a box per lane
+    static constexpr int LPR = BINS / 4;
+    static constexpr int RPL = 32 / LPR;
+    static constexpr int GU = 32 / RPL;             // row groups of a half-box unit (32 rows)
+    static constexpr int LB = BINS == 16 ? 16 : 8;  // lanes per bin in the finish
 };
 
 struct OnePassArgs {
@@ -72,18 +75,19 @@ struct OnePassArgs {
     double *lpart;  // [gridDim.x]
     unsigned int *err;
     unsigned int *bar;  // grid barrier: arrivals, generation
-    const sfh_df *tab;  // double-float log / n log n tables (read through L1)
+    const sfh_df *tab;  // double-float log / n log n tables (copied to shared memory)
     float eps_f;
     int want_logl;
     double gsign;
     double *G, *negLogL;  // results (either may be NULL)
 };
 
-// Dynamic shared memory: ring | r (hi, lo) | s_part | s_w[2] | full | empty | flags.
+// Dynamic shared memory: ring | r (hi, lo) | s_part | s_w | s_cn | s_tab | full | empty |
+// flags.
 __host__ __device__ inline size_t op_smem_bytes(int bins, int slots, int nch) {
     return 128 + (size_t)slots * bins * kBoxCols * 4 + (size_t)nch * kBoxCols * sizeof(float2) +
-           (size_t)kOwners * bins * sizeof(sfh_df) + 2 * (size_t)bins * 4 + 2 * (size_t)slots * 8 +
-           16;
+           (size_t)kOwners * bins * sizeof(sfh_df) + (size_t)bins * 4 + (size_t)bins * 16 +
+           (size_t)SFH_DF_TAB_ALL * sizeof(sfh_df) + 2 * (size_t)slots * 8 + 16;
 }
 
 // Bounded wait with an inline fast path (the box has usually landed already).
@@ -93,29 +97,23 @@ __device__ __forceinline__ bool op_wait(uint64_t *bar, uint32_t parity, volatile
     return mbar_wait_sleep(bar, parity, abort_flag, err, code);
 }
 
-// Steps over the CTA's tiles (k = 0, 1, ...), two named barriers per step.  LAG = true:
-//   owners   phase A(k)   | bar 1 | phase B(k-1) with w(k-1)             | bar 2
-//   finish   Poisson(k-1) | bar 1 | m(k), w(k) from the owners' partials | bar 2
-// so the finish of one tile overlaps the G products of the previous one, with boxes of
-// two tiles resident (the ring needs 2 nch slots plus prefetch).  LAG = false:
-//   owners   phase A(k)   | bar 1 |                                      | bar 2 | phase B(k)
-//   finish   Poisson(k-1) | bar 1 | m(k), w(k)                           | bar 2 |
-// holds one tile (nch slots plus prefetch), leaving more of the ring to the stream.
-template <int BINS, bool LAG>
+template <int BINS>
 __global__ void __launch_bounds__(kThreadsOP, 1)
 k_fg_onepass(const OnePassArgs a) {
     using GE = Geo<BINS>;
-    constexpr int LPR = GE::kLanesPerRow, RPL = GE::kRowsPerLoad, NR = GE::kRows;
+    constexpr int LPR = GE::LPR, RPL = GE::RPL, GU = GE::GU, LB = GE::LB;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    // 128-byte aligned TMA destination; derived from the shared array by pointer arithmetic
+    // 128-byte aligned copy destination; derived from the shared array by pointer arithmetic
     // so that every access below stays a shared-memory access
     unsigned char *base = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
     const int slots = a.slots, nch = a.nch;
     float *ring = (float *)base;
     float2 *rr = (float2 *)(ring + (size_t)slots * GE::kBoxFloats);  // r split (hi, lo)
     sfh_df *s_part = (sfh_df *)(rr + nch * kBoxCols);                // [kOwners][BINS]
-    float *s_w = (float *)(s_part + kOwners * BINS);                 // [2][BINS]
-    uint64_t *full = (uint64_t *)(s_w + 2 * BINS);
+    float *s_w = (float *)(s_part + kOwners * BINS);                 // [BINS]
+    float4 *s_cn = (float4 *)(s_w + BINS);                           // [BINS] (m hi, lo, n hi, lo)
+    sfh_df *s_tab = (sfh_df *)(s_cn + BINS);                         // log / n log n tables
+    uint64_t *full = (uint64_t *)(s_tab + SFH_DF_TAB_ALL);
     uint64_t *empty = full + slots;
     volatile int *s_abort = (volatile int *)(empty + slots);
     volatile int *s_stop = s_abort + 1;
@@ -127,10 +125,12 @@ k_fg_onepass(const OnePassArgs a) {
         const float h = __double2float_rn(v);
         rr[k] = make_float2(h, __double2float_rn(v - (double)h));
     }
+    if (a.want_logl)
+        for (int k = threadIdx.x; k < SFH_DF_TAB_ALL; k += blockDim.x) s_tab[k] = a.tab[k];
     if (threadIdx.x == 0) {
         for (int s = 0; s < slots; ++s) {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], 1);  // the box's warp releases it
+            mbar_init(&empty[s], 2);  // the owners of the box's two halves release it
         }
         *s_abort = 0;
         *s_stop = 0;
@@ -139,20 +139,17 @@ k_fg_onepass(const OnePassArgs a) {
     __syncthreads();
 
     // ------------------------------------------------------------ producers
-    // kProducers lanes of the last warp; lane p issues the boxes whose sequence number
-    // q = (local tile) * nch + c has q % kProducers == p (one bulk copy occupies its issuing
-    // thread for a while, so several issuers keep more copies in flight).  slots is a
-    // multiple of kProducers: a slot is always refilled by the same lane, which waits for
-    // the release of that slot's previous box.
+    // Lane p issues the boxes whose sequence number q = (local tile) * nch + c has
+    // q % kProducers == p.  slots is a multiple of kProducers: a slot is always refilled by
+    // the same lane, which waits for the release of that slot's previous box.
     if (warp == kWarps) {
         if (lane < kProducers) {
             const int64_t nq = (int64_t)((a.ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1) * nch;
-            int64_t q = lane, last = -1;
-            bool ok = true;
-            for (; q < nq && ok; q += kProducers) {
+            int64_t last = -1;
+            for (int64_t q = lane; q < nq; q += kProducers) {
                 const int s = (int)(q % slots);
                 const uint32_t ph = (uint32_t)(q / slots) & 1u;
-                if (!op_wait(&empty[s], ph ^ 1u, s_abort, err, 1)) { ok = false; break; }
+                if (!op_wait(&empty[s], ph ^ 1u, s_abort, err, 1)) break;
                 const int64_t tl = q / nch, c = q - tl * nch;
                 const int64_t t = (int64_t)blockIdx.x + tl * gridDim.x;
                 mbar_expect_tx(&full[s], GE::kBoxBytes);
@@ -163,92 +160,58 @@ k_fg_onepass(const OnePassArgs a) {
             // every box this lane requested has landed before the CTA exits
             volatile int never = 0;
             int dummy = 0;
-            for (int64_t r = last; r >= 0 && r > last - slots; r -= kProducers)
-                mbar_wait(&full[r % slots], (uint32_t)(r / slots) & 1u, &never, &dummy, 0);
+            for (int64_t q = last; q >= 0 && q > last - slots; q -= kProducers)
+                mbar_wait(&full[q % slots], (uint32_t)(q / slots) & 1u, &never, &dummy, 0);
         }
         return;
     }
 
     // ------------------------------------------------------------ consumers
-    // Box c (templates 64c .. 64c+63) belongs to warp c % kOwners in both phases.  Lane l
-    // reads rows g + RPL k (k < NR, g = l / LPR) and bins 4 quad .. 4 quad + 3
-    // (quad = l % LPR): one 16-byte shared load per row, a warp load covering RPL whole
-    // rows (512 contiguous bytes, conflict-free).
+    // Unit u = (box c, half h) = 2c + h (rows 32h .. 32h + 31 of box c) belongs to owner
+    // u % kOwners in both phases.  Lane l reads rows 32h + g + RPL k (g = l / LPR, k < GU)
+    // and bins 4 quad .. 4 quad + 3 (quad = l % LPR): one 16-byte shared load per row, a
+    // warp load covering RPL whole rows (512 contiguous bytes, conflict-free).
     const int g = lane / LPR, quad = lane % LPR;
     const int64_t nbins = a.nbins;
     const bool want_g = a.gpart != nullptr;
-    const bool fin = warp == kFinishWarp;
-    // G of template 64c + g + RPL k over this lane's 4 bins and all of the CTA's tiles
-    float gh[kBoxesPerWarp][NR], gl[kBoxesPerWarp][NR];
+    const bool owner = warp < kOwners;
+    const int nunits = 2 * nch;
+    // finish: warp fw < kFinishers, lanes of bin fb = fw * (32 / LB) + lane / LB
+    const bool finisher = warp < kFinishers;
+    const int fb = warp * (32 / LB) + lane / LB, fl = lane % LB;
+    // G of the lane's rows of unit j over its 4 bins and all of the CTA's tiles
+    float gh[kUnits][GU], gl[kUnits][GU];
 #pragma unroll
-    for (int b = 0; b < kBoxesPerWarp; ++b)
+    for (int j = 0; j < kUnits; ++j)
 #pragma unroll
-        for (int k = 0; k < NR; ++k) gh[b][k] = gl[b][k] = 0.f;
-    // finish warp: lane = bin (lanes < BINS) + BINS * half; the Poisson term of the
-    // previous tile is kept (pending) for the window after bar 2
-    sfh_df term{0.f, 0.f}, pc{0.f, 0.f};
-    float pnh = 0.f, pnl = 0.f;
-    bool pending = false;
-    int s0 = 0, sp = 0;  // first slot of the current / previous tile
-    uint32_t ph0 = 0;    // use parity of the current tile's first slot
-    bool ok = true, have_prev = false;
-    // phase B of the tile whose first box is in slot sbase, with w at wsrc: M w over the
-    // lane's 4 bins from the resident boxes (packed FP32 pairs), compensated per template
-    // over the tiles; each box is released after its last read
-    auto phase_b = [&](int sbase, const float *wsrc) {
-        const float4 w4 = *(const float4 *)(wsrc + 4 * quad);
-        const float2 w01 = make_float2(w4.x, w4.y), w23 = make_float2(w4.z, w4.w);
-#pragma unroll
-        for (int b = 0; b < kBoxesPerWarp; ++b) {
-            const int c = warp + kOwners * b;
-            if (c >= nch) break;
-            int s = sbase + c;
-            if (s >= slots) s -= slots;
-            if (want_g) {
-                const float *bp = ring + (size_t)s * GE::kBoxFloats + g * BINS + 4 * quad;
-#pragma unroll
-                for (int k = 0; k < NR; ++k) {
-                    const float4 m = *(const float4 *)(bp + k * RPL * BINS);
-                    const float2 p = __ffma2_rn(make_float2(m.z, m.w), w23,
-                                                __fmul2_rn(make_float2(m.x, m.y), w01));
-                    sfh_two_sum_acc(gh[b][k], gl[b][k], p.x + p.y);
-                }
-            }
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&empty[s]);
-        }
-    };
-    for (int t = blockIdx.x, kk = 0;; t += gridDim.x, ++kk) {
-        const bool have_cur = t < a.ntiles;
-        if (!have_cur && (!LAG || !have_prev)) break;
-        const int64_t i = (int64_t)t * BINS + (lane % BINS);
+        for (int k = 0; k < GU; ++k) gh[j][k] = gl[j][k] = 0.f;
+    sfh_df term{0.f, 0.f};
+    int s0 = 0;        // slot of the tile's first box
+    uint32_t ph0 = 0;  // its use parity
+    bool ok = true;
+    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
+        const int64_t tb = (int64_t)t * BINS;
         double nd = 0.0;
-        if (fin) {
-            if (have_cur && lane < BINS && i < nbins) nd = a.data[i];  // loads while the boxes land
-            if (pending) {
-                term = df_add(term, sfh_bin_term(pc, pnh, pnl, a.tab));
-                pending = false;
-            }
-        } else if (have_cur) {
-            // phase A(k): m r over this warp's boxes for the lane's 4 bins (r split hi + lo,
-            // packed FP32 pairs, two chains per bin pair; compensated per box)
+        if (finisher && fl == 0 && tb + fb < nbins) nd = a.data[tb + fb];  // loads while boxes land
+        __syncwarp();  // lane-dependent code ends: reconverge the warp (here and below)
+        if (owner) {
+            // phase A: m r over the owner's units for the lane's 4 bins (r split hi + lo,
+            // packed FP32 pairs, two chains per bin pair; compensated per unit)
             float ah[4] = {0.f, 0.f, 0.f, 0.f}, al[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-            for (int b = 0; b < kBoxesPerWarp; ++b) {
-                const int c = warp + kOwners * b;
-                if (c >= nch || !ok) break;
+            for (int j = 0; j < kUnits; ++j) {
+                const int u = warp + kOwners * j;
+                if (u >= nunits || !ok) break;
+                const int c = u >> 1, h = u & 1;
                 int s = s0 + c;
                 uint32_t ph = ph0;
                 if (s >= slots) { s -= slots; ph ^= 1u; }
-                if (!op_wait(&full[s], ph, s_abort, err, 2)) {
-                    ok = false;
-                    break;
-                }
-                const float *bp = ring + (size_t)s * GE::kBoxFloats + g * BINS + 4 * quad;
-                const float2 *rp = rr + c * kBoxCols + g;
+                if (!op_wait(&full[s], ph, s_abort, err, 2)) { ok = false; break; }
+                const float *bp = ring + (size_t)s * GE::kBoxFloats + (32 * h + g) * BINS + 4 * quad;
+                const float2 *rp = rr + c * kBoxCols + 32 * h + g;
                 float2 e01 = make_float2(0.f, 0.f), e23 = e01, o01 = e01, o23 = e01;
 #pragma unroll
-                for (int k = 0; k < NR; ++k) {
+                for (int k = 0; k < GU; ++k) {
                     const float4 m = *(const float4 *)(bp + k * RPL * BINS);
                     const float2 rv = rp[RPL * k];
                     const float2 h2 = make_float2(rv.x, rv.x), l2 = make_float2(rv.y, rv.y);
@@ -266,6 +229,7 @@ k_fg_onepass(const OnePassArgs a) {
                 sfh_two_sum_acc(ah[2], al[2], e23.x + o23.x);
                 sfh_two_sum_acc(ah[3], al[3], e23.y + o23.y);
             }
+            __syncwarp();
             // sum over the lanes that hold the same bins (other rows)
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
@@ -277,24 +241,25 @@ k_fg_onepass(const OnePassArgs a) {
                 }
                 if (lane < LPR) s_part[warp * BINS + 4 * quad + k] = v;
             }
+            __syncwarp();
         }
         named_bar_sync(1, kWarps * 32);
-        if (fin) {
-            // m(k) and w(k): lane pair (bin, bin + BINS) sums the owners' partials of even /
-            // odd owners, then the two halves are added
-            if (have_cur) {
-                const int b = lane % BINS, h = lane / BINS;  // BINS == 16: h in {0, 1}
-                sfh_df cm{0.f, 0.f};
-                if (BINS == 16) {
-                    for (int w = h; w < kOwners; w += 2) cm = df_add_fast(cm, s_part[w * BINS + b]);
-                    const sfh_df u{__shfl_xor_sync(0xffffffffu, cm.h, 16),
-                                   __shfl_xor_sync(0xffffffffu, cm.l, 16)};
-                    cm = h == 0 ? df_add_fast(cm, u) : df_add_fast(u, cm);
-                } else {
-                    for (int w = 0; w < kOwners; ++w) cm = df_add_fast(cm, s_part[w * BINS + b]);
-                }
+        if (finisher) {
+            // the bin's 14 owner partials: lane fl takes owners fl, fl + LB, ...; a fixed
+            // butterfly over the LB lanes; lane fl == 0 keeps the total
+            sfh_df cm{0.f, 0.f};
+#pragma unroll
+            for (int o = 0; o < kOwners; o += LB)
+                if (o + fl < kOwners) cm = df_add_fast(cm, s_part[(o + fl) * BINS + fb]);
+#pragma unroll
+            for (int o = LB / 2; o >= 1; o >>= 1) {
+                const sfh_df u{__shfl_xor_sync(0xffffffffu, cm.h, o), __shfl_xor_sync(0xffffffffu, cm.l, o)};
+                cm = df_add_fast(cm, u);
+            }
+            const int64_t i = tb + fb;
+            if (fl == 0) {
                 float wv = 0.f;
-                if (lane < BINS && i < nbins) {
+                if (i < nbins) {
                     if (!want_g) a.composite[i] = sfh_f2d(cm.h) + sfh_f2d(cm.l);  // the model, unclamped
                     // max(composite, eps(T)); eps(T) is a power of two, exact in FP32
                     if (cm.h < a.eps_f || (cm.h == a.eps_f && cm.l < 0.f)) cm = sfh_df{a.eps_f, 0.f};
@@ -304,51 +269,73 @@ k_fg_onepass(const OnePassArgs a) {
                         wv = __fdiv_rn(df_add(cm, sfh_df{-nh, -nl}).h, cm.h);  // 1 - n/c
                         a.composite[i] = sfh_f2d(wv);
                     }
-                    if (a.want_logl) {  // the term is formed in the next window
-                        pc = cm;
-                        pnh = nh;
-                        pnl = nl;
-                        pending = true;
-                    }
+                    s_cn[fb] = make_float4(cm.h, cm.l, nh, nl);
                 }
-                if (lane < BINS) s_w[(kk & 1) * BINS + lane] = wv;
+                s_w[fb] = wv;
             }
-            if (lane == 0) *s_stop = *s_abort;
-        } else if (LAG && have_prev) {
-            phase_b(sp, s_w + ((kk - 1) & 1) * BINS);
+            if (threadIdx.x == 0) *s_stop = *s_abort;
+            __syncwarp();
         }
         named_bar_sync(1, kWarps * 32);
         if (*s_stop) break;  // the same decision in every consumer warp
-        if (!LAG && !fin && have_cur) phase_b(s0, s_w + (kk & 1) * BINS);
-        have_prev = have_cur;
-        sp = s0;
-        if (have_cur) {
-            s0 += nch;  // nch <= slots: at most one wrap
-            if (s0 >= slots) { s0 -= slots; ph0 ^= 1u; }
+        if (owner) {
+            // phase B: M w over the owner's units from the resident boxes (packed FP32 pairs),
+            // compensated per row over the tiles; each unit's box is released after its read
+            const float4 w4 = *(const float4 *)(s_w + 4 * quad);
+            const float2 w01 = make_float2(w4.x, w4.y), w23 = make_float2(w4.z, w4.w);
+#pragma unroll
+            for (int j = 0; j < kUnits; ++j) {
+                const int u = warp + kOwners * j;
+                if (u >= nunits) break;
+                const int c = u >> 1, h = u & 1;
+                int s = s0 + c;
+                if (s >= slots) s -= slots;
+                if (want_g) {
+                    const float *bp = ring + (size_t)s * GE::kBoxFloats + (32 * h + g) * BINS + 4 * quad;
+#pragma unroll
+                    for (int k = 0; k < GU; ++k) {
+                        const float4 m = *(const float4 *)(bp + k * RPL * BINS);
+                        const float2 p = __ffma2_rn(make_float2(m.z, m.w), w23,
+                                                    __fmul2_rn(make_float2(m.x, m.y), w01));
+                        sfh_two_sum_acc(gh[j][k], gl[j][k], p.x + p.y);
+                    }
+                }
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&empty[s]);
+                __syncwarp();
+            }
+        } else {
+            // warp 14: the tile's Poisson terms
+            if (a.want_logl && lane < BINS && tb + lane < nbins) {
+                const float4 cn = s_cn[lane];
+                term = df_add(term, sfh_bin_term(sfh_df{cn.x, cn.y}, cn.z, cn.w, s_tab));
+            }
+            __syncwarp();
         }
+        s0 += nch;  // nch <= slots: at most one wrap
+        if (s0 >= slots) { s0 -= slots; ph0 ^= 1u; }
     }
-    if (fin && pending) term = df_add(term, sfh_bin_term(pc, pnh, pnl, a.tab));
     // per-CTA partials of G: the lanes of a row (bin quads) summed once
-    if (want_g && !fin) {
+    if (want_g && owner) {
 #pragma unroll
-        for (int b = 0; b < kBoxesPerWarp; ++b) {
-            const int c = warp + kOwners * b;
-            if (c >= nch) break;
+        for (int j = 0; j < kUnits; ++j) {
+            const int u = warp + kOwners * j;
+            if (u >= nunits) break;
 #pragma unroll
-            for (int k = 0; k < NR; ++k) {
-                sfh_df v = df_fast_two_sum(gh[b][k], gl[b][k]);
+            for (int k = 0; k < GU; ++k) {
+                sfh_df v = df_fast_two_sum(gh[j][k], gl[j][k]);
 #pragma unroll
                 for (int o = 1; o < LPR; o <<= 1) {
-                    const sfh_df u{__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)};
-                    v = df_add(v, u);
+                    const sfh_df w{__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)};
+                    v = df_add(v, w);
                 }
-                const int64_t col = (int64_t)c * kBoxCols + g + RPL * k;
+                const int64_t col = (int64_t)(u >> 1) * kBoxCols + 32 * (u & 1) + g + RPL * k;
                 if (quad == 0 && col < a.nt)
                     a.gpart[(int64_t)blockIdx.x * a.nt + col] = sfh_f2d(v.h) + sfh_f2d(v.l);
             }
         }
     }
-    if (a.want_logl && fin) {
+    if (a.want_logl && warp == kPoissonWarp) {
         const sfh_df tot = sfh_df_warp_sum(term);
         if (lane == 0) a.lpart[blockIdx.x] = sfh_f2d(tot.h) + sfh_f2d(tot.l);
     }
@@ -430,28 +417,28 @@ int op_max_smem(sfh_ctx *ctx) {
     return cached;
 }
 
-// Ring slots for BINS-bin tiles of a matrix with nch boxes per tile, one or (lag) two tiles
-// resident (0 if it does not fit).
-int op_slots(sfh_ctx *ctx, int bins, int nch, bool lag) {
+// Ring slots for BINS-bin tiles of a matrix with nch boxes per tile: the resident tile
+// plus prefetch (0 if it does not fit).
+int op_slots(sfh_ctx *ctx, int bins, int nch) {
     const int maxs = op_max_smem(ctx);
     int slots = kMaxSlots;
     while (slots > 0 && op_smem_bytes(bins, slots, nch) > (size_t)maxs) --slots;
     slots -= slots % kProducers;  // each slot is refilled by one producer lane
-    return slots >= (lag ? 2 : 1) * nch + 2 ? slots : 0;  // resident tiles plus prefetch
+    return slots >= nch + 2 ? slots : 0;
 }
 
-template <int BINS, bool LAG>
+template <int BINS>
 int launch_onepass(sfh_ctx *ctx, const OnePassArgs &a0, int grid, cudaStream_t st) {
     static size_t attr_set = 0;
     const size_t smem = op_smem_bytes(BINS, a0.slots, a0.nch);
     if (smem > attr_set) {
-        SFH_CK(ctx, cudaFuncSetAttribute(k_fg_onepass<BINS, LAG>,
+        SFH_CK(ctx, cudaFuncSetAttribute(k_fg_onepass<BINS>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr_set = smem;
     }
     // grid <= SM count and one CTA per SM (shared memory): the CTAs are resident together,
     // as the in-kernel grid reduction needs; its barrier wait is bounded all the same
-    k_fg_onepass<BINS, LAG><<<grid, kThreadsOP, smem, st>>>(a0);
+    k_fg_onepass<BINS><<<grid, kThreadsOP, smem, st>>>(a0);
     SFH_LAUNCHED(ctx);
     return SFH_OK;
 }
@@ -462,7 +449,7 @@ bool sfh_onepass_eligible(sfh_ctx *ctx, const sfh_models *m) {
     if (!m || m->storage == SFH_F64 || !m->d_f32) return false;
     if (m->nbins > INT32_MAX - 64 || m->nt > kMaxTemplates) return false;
     const int nch = (int)((m->nt + kBoxCols - 1) / kBoxCols);
-    return op_slots(ctx, 16, nch, false) > 0;
+    return op_slots(ctx, 16, nch) > 0;
 }
 
 size_t sfh_onepass_scratch(const sfh_ctx *ctx, const sfh_models *m) {
@@ -476,13 +463,10 @@ int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
                           cudaEvent_t *ev) {
     const int64_t nbins = m->nbins, nt = m->nt;
     const int nch = (int)((nt + kBoxCols - 1) / kBoxCols);
-    // the handle's variant, else the nearest one the shape fits (16-bin, no lag always fits
-    // an eligible shape)
+    // the handle's tile width, else 16 bins (which every eligible shape fits)
     int bins = m->onepass_bins == 32 ? 32 : 16;
-    bool lag = m->onepass_lag != 0;
-    int slots = op_slots(ctx, bins, nch, lag);
-    if (!slots && lag) slots = op_slots(ctx, bins, nch, lag = false);
-    if (!slots && bins == 32) slots = op_slots(ctx, bins = 16, nch, lag);
+    int slots = op_slots(ctx, bins, nch);
+    if (!slots && bins == 32) slots = op_slots(ctx, bins = 16, nch);
     if (!slots) return sfh_set_error(ctx, SFH_ERR_UNSUPPORTED, "one-pass fg!: shape does not fit");
     const int mi = bins == 16 ? 0 : 1;
     const int ntiles = (int)((nbins + bins - 1) / bins);
@@ -516,10 +500,7 @@ int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
     a.negLogL = d_negLogL;
     cudaStream_t st = ctx->stream;
     if (ev) SFH_CK(ctx, cudaEventRecord(ev[0], st));
-    int rc = bins == 16 ? (lag ? launch_onepass<16, true>(ctx, a, grid, st)
-                               : launch_onepass<16, false>(ctx, a, grid, st))
-                        : (lag ? launch_onepass<32, true>(ctx, a, grid, st)
-                               : launch_onepass<32, false>(ctx, a, grid, st));
+    int rc = bins == 16 ? launch_onepass<16>(ctx, a, grid, st) : launch_onepass<32>(ctx, a, grid, st);
     if (rc) return rc;
     if (ev) SFH_CK(ctx, cudaEventRecord(ev[1], st));
     if (ev) SFH_CK(ctx, cudaEventRecord(ev[2], st));

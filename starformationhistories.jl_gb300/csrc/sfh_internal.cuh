@@ -57,7 +57,6 @@ struct sfh_models {
     // it streams (built on first use): for tile t and box c (64 templates) one contiguous
     // block of [64 templates][bins] floats, blocks in (tile, box) order, zero padded.
     int onepass_bins = 0;
-    int onepass_lag = 1;  // 1: G products one tile behind (overlap the finish), 0: in step
     float *d_blk[2] = {nullptr, nullptr};
 };
 

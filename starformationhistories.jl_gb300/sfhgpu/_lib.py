@@ -113,7 +113,7 @@ def load(path: str | None = None):
             "sfh_fg_batched_dev": ([_vp, _vp, _vp, _i64, _vp, _vp, _vp, _d], C.c_int),
             "sfh_models_autotune": ([_vp, _vp, _vp, _vp, _d, C.c_int, _vp, _vp], C.c_int),
             "sfh_models_set_path": ([_vp, _vp, C.c_int], C.c_int),
-            "sfh_models_set_onepass_tile": ([_vp, _vp, C.c_int, C.c_int], C.c_int),
+            "sfh_models_set_onepass_tile": ([_vp, _vp, C.c_int], C.c_int),
             "sfh_models_path": ([_vp, _vp, C.POINTER(C.c_int), C.POINTER(_d)], C.c_int),
             "sfh_fg_dev_noalloc": ([_vp, _vp, _i64, _i64, _vp, _vp, _vp, _vp, _vp, _d], C.c_int),
             "sfh_fg_kernel_times": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, C.c_int,

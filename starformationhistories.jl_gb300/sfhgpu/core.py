@@ -139,10 +139,9 @@ class Models:
         check(load().sfh_models_set_path(self.ctx.handle, self._h, self.PATHS[path]),
               self.ctx.handle, "models_set_path")
 
-    def set_onepass_tile(self, bins, lag=True):
-        """One-pass variant: 16 or 32 bins per tile; lag=True forms the G products one tile
-        behind the composite (sfh_models_set_onepass_tile)."""
-        check(load().sfh_models_set_onepass_tile(self.ctx.handle, self._h, int(bins), int(bool(lag))),
+    def set_onepass_tile(self, bins):
+        """Bins per tile of the one-pass kernel: 16 or 32 (sfh_models_set_onepass_tile)."""
+        check(load().sfh_models_set_onepass_tile(self.ctx.handle, self._h, int(bins)),
               self.ctx.handle, "models_set_onepass_tile")
 
     @property
