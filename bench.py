@@ -589,6 +589,8 @@ def run_ours(args):
 
     # launch plan picked by the library's autotuner on this matrix and these inputs
     tuned = H.autotune(r, data, iters=10)
+    if args.fg_path != "auto":
+        H.set_path(args.fg_path)
 
     def step():
         rc = L.sfh_fg_dev(ctx.handle, H.handle, d_r.data_ptr(), d_n.data_ptr(), d_c.data_ptr(),
@@ -768,6 +770,9 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched tensor-core leg")
     ap.add_argument("--no-hmc", action="store_true", help="skip the batched HMC leg")
     ap.add_argument("--no-ragged", action="store_true", help="skip the ragged-galaxies leg")
+    ap.add_argument("--fg-path", choices=("auto", "onepass", "twopass"), default="auto",
+                    help="single-vector fg! path: the autotuner's choice (auto) or a fixed one "
+                         "(for profiling runs, where profiler overhead can change the choice)")
     ap.add_argument("--no-emulator", action="store_true", help="skip the emulator leg")
     ap.add_argument("--ntempl", type=int, default=NT,
                     help="templates (multiple of 30); fewer than 1200 only for profiling")

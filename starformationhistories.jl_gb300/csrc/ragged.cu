@@ -251,6 +251,7 @@ k_ragged_fused(const float *__restrict__ M, const GalDesc *__restrict__ gals,
         }
         float w = 0.f;
         if (live) bin_terms(ah, al, data, G.boff + i, eps, want_logl, want_g, s_tab, composite, term, w);
+        __syncwarp();  // reconverge after the lane-dependent tail
 #pragma unroll
         for (int j0 = 0; j0 < NT; j0 += 4) {
             if (j0 >= nt) break;
