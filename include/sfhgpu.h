@@ -144,6 +144,11 @@ int sfh_models_set_path(sfh_ctx *ctx, sfh_models *models, int path);
 /* Tile width of the one-pass kernel: 16 or 32 bins per tile (default 16; the autotuner
    measures both; a shape whose tile does not fit the 32-bin ring takes 16). */
 int sfh_models_set_onepass_tile(sfh_ctx *ctx, sfh_models *models, int bins);
+/* CTAs per SM of the one-pass kernel: 1 (14 owner warps, the whole shared memory) or 2
+   (6 owner warps each, 16-bin tiles, half the shared memory: the two CTAs' per-tile
+   latencies overlap).  Default 1; the autotuner measures both; shapes that do not fit
+   two CTAs per SM take one. */
+int sfh_models_set_onepass_ctas(sfh_ctx *ctx, sfh_models *models, int ctas_per_sm);
 /* The path fg! calls with G take on this handle now (ONEPASS or TWOPASS), and the
    one-pass time measured by sfh_models_autotune (0 if not measured); either may be NULL. */
 int sfh_models_path(sfh_ctx *ctx, const sfh_models *models, int *path_out, double *onepass_ms);

@@ -990,13 +990,16 @@ extern "C" int sfh_models_autotune(sfh_ctx *ctx, sfh_models *m, const double *d_
     if (rc == SFH_OK && sfh_onepass_eligible(ctx, m)) {  // one-pass tile widths against the best plan
         m->path = SFH_PATH_ONEPASS;
         double best_op = 1e300;
-        int best_bins = 16;
-        for (int bins : {16, 32}) {  // tile widths
-            m->onepass_bins = bins;
+        int best_bins = 16, best_ctas = 1;
+        const int variants[3][2] = {{16, 1}, {32, 1}, {16, 2}};  // tile width, CTAs per SM
+        for (const auto &v : variants) {
+            m->onepass_bins = v[0];
+            m->onepass_ctas = v[1];
             if ((rc = timed(t1, t2)) != SFH_OK) break;
-            if (t1 + t2 < best_op) { best_op = t1 + t2; best_bins = bins; }
+            if (t1 + t2 < best_op) { best_op = t1 + t2; best_bins = v[0]; best_ctas = v[1]; }
         }
         m->onepass_bins = best_bins;
+        m->onepass_ctas = best_ctas;
         if (rc == SFH_OK) {
             m->onepass_ms = best_op;
             if (best_op >= b1 + b2) m->path = SFH_PATH_TWOPASS;
@@ -1007,7 +1010,7 @@ extern "C" int sfh_models_autotune(sfh_ctx *ctx, sfh_models *m, const double *d_
     if (rc) {
         m->tune_ks = m->tune_R = m->tune_w2 = 0;
         m->path = SFH_PATH_AUTO;
-        m->onepass_bins = 0;
+        m->onepass_bins = m->onepass_ctas = 0;
         return rc;
     }
     if (plan_out) {
@@ -1186,6 +1189,12 @@ extern "C" int sfh_models_set_path(sfh_ctx *ctx, sfh_models *m, int path) {
 extern "C" int sfh_models_set_onepass_tile(sfh_ctx *ctx, sfh_models *m, int bins) {
     if (!ctx || !m || (bins != 16 && bins != 32)) return SFH_ERR_ARG;
     m->onepass_bins = bins;
+    return SFH_OK;
+}
+
+extern "C" int sfh_models_set_onepass_ctas(sfh_ctx *ctx, sfh_models *m, int ctas_per_sm) {
+    if (!ctx || !m || (ctas_per_sm != 1 && ctas_per_sm != 2)) return SFH_ERR_ARG;
+    m->onepass_ctas = ctas_per_sm;
     return SFH_OK;
 }
 

@@ -42,27 +42,31 @@
 namespace {
 
 constexpr int kBoxCols = 64;                      // templates per box
-constexpr int kOwners = 14;                       // warps 0-13
-constexpr int kPoissonWarp = kOwners;             // warp 14
-constexpr int kWarps = kOwners + 1;               // consumer warps (named barriers)
-constexpr int kThreadsOP = (kWarps + 1) * 32;     // + producer warp: 16 warps, 128 registers
-constexpr int kFinishers = 8;                     // owners that also finish the bins
 constexpr int kMaxBoxes = 24;                     // boxes per tile
 constexpr int kMaxTemplates = kMaxBoxes * kBoxCols;  // 1536
-constexpr int kUnits = (2 * kMaxBoxes + 13) / 14;  // half-box units per owner (4)
 constexpr int kMaxSlots = 64;
 constexpr int kProducers = 4;                     // issuing lanes of the producer warp
 
-// Tile geometry for BINS bins per tile: a box is [64 rows][BINS] floats; a row is LPR lanes
-// of one 16-byte load, a warp load covers RPL rows, a half-box unit (32 rows) GU loads.
-template <int BINS>
+// Kernel shape for BINS bins per tile and OWN owner warps.  A box is [64 rows][BINS]
+// floats; a row is LPR lanes of one 16-byte load, a warp load covers RPL rows, a half-box
+// unit (32 rows) GU loads.  Warps 0 .. OWN-1 own units, warp OWN forms the Poisson terms,
+// warp OWN+1 produces; OWN = 14 runs one CTA per SM, OWN = 6 two (half the registers and
+// shared memory each, so the two CTAs' per-tile latencies overlap).
+template <int BINS, int OWN>
 struct Geo {
     static constexpr int kBoxFloats = BINS * kBoxCols;
     static constexpr int kBoxBytes = kBoxFloats * 4;
     static constexpr int LPR = BINS / 4;
     static constexpr int RPL = 32 / LPR;
-    static constexpr int GU = 32 / RPL;             // row groups of a half-box unit (32 rows)
-    static constexpr int LB = BINS == 16 ? 16 : 8;  // lanes per bin in the finish
+    static constexpr int GU = 32 / RPL;               // row groups of a half-box unit
+    static constexpr int kOwners = OWN;
+    static constexpr int kPoissonWarp = OWN;
+    static constexpr int kWarps = OWN + 1;            // consumer warps (named barriers)
+    static constexpr int kThreads = (kWarps + 1) * 32;
+    static constexpr int kFinishers = OWN >= 8 ? 8 : 4;  // owners that also finish the bins
+    static constexpr int LB = kFinishers * 32 / BINS;    // lanes per bin in the finish
+    static constexpr int kUnits = (2 * kMaxBoxes + OWN - 1) / OWN;  // units per owner
+    static constexpr int kMinBlocks = OWN >= 8 ? 1 : 2;  // CTAs per SM
 };
 
 struct OnePassArgs {
@@ -84,9 +88,9 @@ struct OnePassArgs {
 
 // Dynamic shared memory: ring | r (hi, lo) | s_part | s_w | s_cn | s_tab | full | empty |
 // flags.
-__host__ __device__ inline size_t op_smem_bytes(int bins, int slots, int nch) {
+__host__ __device__ inline size_t op_smem_bytes(int bins, int owners, int slots, int nch) {
     return 128 + (size_t)slots * bins * kBoxCols * 4 + (size_t)nch * kBoxCols * sizeof(float2) +
-           (size_t)kOwners * bins * sizeof(sfh_df) + (size_t)bins * 4 + (size_t)bins * 16 +
+           (size_t)owners * bins * sizeof(sfh_df) + (size_t)bins * 4 + (size_t)bins * 16 +
            (size_t)SFH_DF_TAB_ALL * sizeof(sfh_df) + 2 * (size_t)slots * 8 + 16;
 }
 
@@ -97,11 +101,13 @@ __device__ __forceinline__ bool op_wait(uint64_t *bar, uint32_t parity, volatile
     return mbar_wait_sleep(bar, parity, abort_flag, err, code);
 }
 
-template <int BINS>
-__global__ void __launch_bounds__(kThreadsOP, 1)
+template <int BINS, int OWN>
+__global__ void __launch_bounds__(Geo<BINS, OWN>::kThreads, Geo<BINS, OWN>::kMinBlocks)
 k_fg_onepass(const OnePassArgs a) {
-    using GE = Geo<BINS>;
+    using GE = Geo<BINS, OWN>;
     constexpr int LPR = GE::LPR, RPL = GE::RPL, GU = GE::GU, LB = GE::LB;
+    constexpr int kOwners = GE::kOwners, kWarps = GE::kWarps, kFinishers = GE::kFinishers;
+    constexpr int kUnits = GE::kUnits, kPoissonWarp = GE::kPoissonWarp;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     // 128-byte aligned copy destination; derived from the shared array by pointer arithmetic
     // so that every access below stays a shared-memory access
@@ -245,7 +251,7 @@ k_fg_onepass(const OnePassArgs a) {
         }
         named_bar_sync(1, kWarps * 32);
         if (finisher) {
-            // the bin's 14 owner partials: lane fl takes owners fl, fl + LB, ...; a fixed
+            // the bin's owner partials: lane fl takes owners fl, fl + LB, ...; a fixed
             // butterfly over the LB lanes; lane fl == 0 keeps the total
             sfh_df cm{0.f, 0.f};
 #pragma unroll
@@ -405,42 +411,67 @@ __global__ void k_onepass_block(const float *__restrict__ M, int64_t nbins, int6
     blk[idx] = (bin < nbins && col < nt) ? M[col * nbins + bin] : 0.f;
 }
 
-int op_max_smem(sfh_ctx *ctx) {
-    static int cached = -1;
-    if (cached < 0) {
-        int v = 0;
-        if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device) !=
-            cudaSuccess)
-            v = 0;
-        cached = v;
+// Shared memory a CTA may use when `per_sm` CTAs share an SM.
+int op_max_smem(sfh_ctx *ctx, int per_sm) {
+    static int optin = -1, per_smp = 0, reserved = 0;
+    if (optin < 0) {
+        int v = 0, w = 0, r = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device) != cudaSuccess) v = 0;
+        if (cudaDeviceGetAttribute(&w, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->device) != cudaSuccess) w = 0;
+        if (cudaDeviceGetAttribute(&r, cudaDevAttrReservedSharedMemoryPerBlock, ctx->device) != cudaSuccess) r = 0;
+        optin = v;
+        per_smp = w;
+        reserved = r;
     }
-    return cached;
+    if (per_sm <= 1) return optin;
+    const int share = per_smp / per_sm - reserved;
+    return share < optin ? share : optin;
 }
 
-// Ring slots for BINS-bin tiles of a matrix with nch boxes per tile: the resident tile
-// plus prefetch (0 if it does not fit).
-int op_slots(sfh_ctx *ctx, int bins, int nch) {
-    const int maxs = op_max_smem(ctx);
+// Ring slots for BINS-bin tiles of a matrix with nch boxes per tile and `owners` owner
+// warps: the resident tile plus prefetch (0 if it does not fit).
+int op_slots(sfh_ctx *ctx, int bins, int owners, int nch) {
+    const int maxs = op_max_smem(ctx, owners >= 8 ? 1 : 2);
     int slots = kMaxSlots;
-    while (slots > 0 && op_smem_bytes(bins, slots, nch) > (size_t)maxs) --slots;
+    while (slots > 0 && op_smem_bytes(bins, owners, slots, nch) > (size_t)maxs) --slots;
     slots -= slots % kProducers;  // each slot is refilled by one producer lane
     return slots >= nch + 2 ? slots : 0;
 }
 
-template <int BINS>
+template <int BINS, int OWN>
 int launch_onepass(sfh_ctx *ctx, const OnePassArgs &a0, int grid, cudaStream_t st) {
+    using GE = Geo<BINS, OWN>;
     static size_t attr_set = 0;
-    const size_t smem = op_smem_bytes(BINS, a0.slots, a0.nch);
+    const size_t smem = op_smem_bytes(BINS, OWN, a0.slots, a0.nch);
     if (smem > attr_set) {
-        SFH_CK(ctx, cudaFuncSetAttribute(k_fg_onepass<BINS>,
+        SFH_CK(ctx, cudaFuncSetAttribute(k_fg_onepass<BINS, OWN>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr_set = smem;
     }
-    // grid <= SM count and one CTA per SM (shared memory): the CTAs are resident together,
-    // as the in-kernel grid reduction needs; its barrier wait is bounded all the same
-    k_fg_onepass<BINS><<<grid, kThreadsOP, smem, st>>>(a0);
+    // grid <= SMs x kMinBlocks and that many CTAs fit an SM (checked by the caller): the
+    // CTAs are resident together, as the in-kernel grid reduction needs; its barrier wait
+    // is bounded all the same
+    k_fg_onepass<BINS, OWN><<<grid, GE::kThreads, smem, st>>>(a0);
     SFH_LAUNCHED(ctx);
     return SFH_OK;
+}
+
+// CTAs of the variant an SM holds at once with `smem` bytes (occupancy query, cached).
+template <int BINS, int OWN>
+int op_resident(size_t smem) {
+    static size_t q_smem = 0;
+    static int q_blocks = 0;
+    if (smem != q_smem) {
+        cudaFuncSetAttribute(k_fg_onepass<BINS, OWN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fg_onepass<BINS, OWN>,
+                                                          Geo<BINS, OWN>::kThreads, smem) != cudaSuccess)
+            b = 0;
+        q_smem = smem;
+        q_blocks = b;
+    }
+    return q_blocks;
 }
 
 }  // namespace
@@ -449,12 +480,12 @@ bool sfh_onepass_eligible(sfh_ctx *ctx, const sfh_models *m) {
     if (!m || m->storage == SFH_F64 || !m->d_f32) return false;
     if (m->nbins > INT32_MAX - 64 || m->nt > kMaxTemplates) return false;
     const int nch = (int)((m->nt + kBoxCols - 1) / kBoxCols);
-    return op_slots(ctx, 16, nch) > 0;
+    return op_slots(ctx, 16, 14, nch) > 0;
 }
 
-size_t sfh_onepass_scratch(const sfh_ctx *ctx, const sfh_models *m) {
-    return sfh_align256((size_t)ctx->sm_count * (size_t)m->nt * 8) +
-           sfh_align256((size_t)ctx->sm_count * 8);
+size_t sfh_onepass_scratch(const sfh_ctx *ctx, const sfh_models *m) {  // up to 2 CTAs per SM
+    return sfh_align256((size_t)2 * ctx->sm_count * (size_t)m->nt * 8) +
+           sfh_align256((size_t)2 * ctx->sm_count * 8);
 }
 
 int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
@@ -463,10 +494,19 @@ int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
                           cudaEvent_t *ev) {
     const int64_t nbins = m->nbins, nt = m->nt;
     const int nch = (int)((nt + kBoxCols - 1) / kBoxCols);
-    // the handle's tile width, else 16 bins (which every eligible shape fits)
+    // the handle's variant (tile width, CTAs per SM), else 16 bins on one CTA per SM, which
+    // every eligible shape fits
     int bins = m->onepass_bins == 32 ? 32 : 16;
-    int slots = op_slots(ctx, bins, nch);
-    if (!slots && bins == 32) slots = op_slots(ctx, bins = 16, nch);
+    int per_sm = (m->onepass_ctas == 2 && bins == 16) ? 2 : 1;
+    int slots = op_slots(ctx, bins, per_sm == 2 ? 6 : 14, nch);
+    if (slots && per_sm == 2 &&
+        op_resident<16, 6>(op_smem_bytes(16, 6, slots, nch)) < 2)  // two CTAs must fit an SM
+        slots = 0;
+    if (!slots) {
+        bins = 16;
+        per_sm = 1;
+        slots = op_slots(ctx, 16, 14, nch);
+    }
     if (!slots) return sfh_set_error(ctx, SFH_ERR_UNSUPPORTED, "one-pass fg!: shape does not fit");
     const int mi = bins == 16 ? 0 : 1;
     const int ntiles = (int)((nbins + bins - 1) / bins);
@@ -477,7 +517,8 @@ int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
             m->d_f32, nbins, nt, bins, nch, total, m->d_blk[mi]);
         SFH_LAUNCHED(ctx);
     }
-    const int grid = ntiles < ctx->sm_count ? ntiles : ctx->sm_count;
+    const int cap = ctx->sm_count * per_sm;
+    const int grid = ntiles < cap ? ntiles : cap;
     OnePassArgs a{};
     a.blk = m->d_blk[mi];
     a.nbins = nbins;
@@ -489,7 +530,7 @@ int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
     a.data = d_data;
     a.composite = d_composite;
     a.gpart = d_G ? (double *)scratch : nullptr;
-    a.lpart = (double *)((char *)scratch + sfh_align256((size_t)ctx->sm_count * (size_t)nt * 8));
+    a.lpart = (double *)((char *)scratch + sfh_align256((size_t)2 * ctx->sm_count * (size_t)nt * 8));
     a.err = ctx->d_counters + SFH_CNT_ONEPASS_ERR;
     a.bar = ctx->d_counters + SFH_CNT_ONEPASS_BAR;
     a.tab = ctx->d_df_tab;
@@ -500,7 +541,9 @@ int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
     a.negLogL = d_negLogL;
     cudaStream_t st = ctx->stream;
     if (ev) SFH_CK(ctx, cudaEventRecord(ev[0], st));
-    int rc = bins == 16 ? launch_onepass<16>(ctx, a, grid, st) : launch_onepass<32>(ctx, a, grid, st);
+    int rc = per_sm == 2 ? launch_onepass<16, 6>(ctx, a, grid, st)
+             : bins == 16 ? launch_onepass<16, 14>(ctx, a, grid, st)
+                          : launch_onepass<32, 14>(ctx, a, grid, st);
     if (rc) return rc;
     if (ev) SFH_CK(ctx, cudaEventRecord(ev[1], st));
     if (ev) SFH_CK(ctx, cudaEventRecord(ev[2], st));

@@ -57,6 +57,7 @@ struct sfh_models {
     // it streams (built on first use): for tile t and box c (64 templates) one contiguous
     // block of [64 templates][bins] floats, blocks in (tile, box) order, zero padded.
     int onepass_bins = 0;
+    int onepass_ctas = 0;  // one-pass CTAs per SM: 1 (14 owner warps) or 2 (6 each); 0: 1
     float *d_blk[2] = {nullptr, nullptr};
 };
 

@@ -144,6 +144,11 @@ class Models:
         check(load().sfh_models_set_onepass_tile(self.ctx.handle, self._h, int(bins)),
               self.ctx.handle, "models_set_onepass_tile")
 
+    def set_onepass_ctas(self, per_sm):
+        """CTAs per SM of the one-pass kernel: 1 or 2 (sfh_models_set_onepass_ctas)."""
+        check(load().sfh_models_set_onepass_ctas(self.ctx.handle, self._h, int(per_sm)),
+              self.ctx.handle, "models_set_onepass_ctas")
+
     @property
     def path(self):
         """The path fg! calls with G take on this handle now: "onepass" or "twopass"."""

@@ -36,13 +36,14 @@ SHAPES = [(4, 1), (3, 2), (32, 32), (37, 33), (1004, 64), (1005, 65), (7500, 50)
           (152 * 32 * 3 + 5, 97), (4868, 1536), (60000, 1200)]
 
 
-@pytest.mark.parametrize("bins", [16, 32])
+@pytest.mark.parametrize("bins,ctas", [(16, 1), (32, 1), (16, 2)])
 @pytest.mark.parametrize("nbins,nt", SHAPES)
-def test_onepass_matches_oracle(sfh, O, nbins, nt, bins):
+def test_onepass_matches_oracle(sfh, O, nbins, nt, bins, ctas):
     M, r, data = _problem(nbins, nt, seed=7 * nbins + nt)
     H = sfh.Models(M, storage="f32")
     H.set_path("onepass")
     H.set_onepass_tile(bins)
+    H.set_onepass_ctas(ctas)
     assert H.path == "onepass"
     comp = np.empty(nbins)
     G = np.empty(nt)
