@@ -303,6 +303,30 @@ int sfh_partial_cmd_smooth_batch_dev(sfh_ctx *ctx, const double *d_m_ini, const 
                                      int64_t nx, double y_first, double y_step, int64_t ny,
                                      float *d_models);
 
+/* binary_hess(RandomBinaryPairs, m_ini, mags, ...) for a batch of templates,
+   src/StarFormationHistories.jl:627-706 (the case y_index in color_indices, the only one the
+   reference implements; SFH_ERR_UNSUPPORTED otherwise).  Template t's isochrone points
+   (masses increasing, magnitudes with the distance modulus added; partial_cmd_smooth passes
+   every fourth resampled point, :896) are [h_off[t], h_off[t] + h_len[t]) of d_m_ini and of
+   each filter row of d_mags (row f at d_mags + f*total_points).  Every pair of interval
+   left points is a binary (fluxes added, :656), weighted by the IMF and the colour filters'
+   completeness, binned (left-closed), and the nonzero bins are smoothed as points at the
+   bin centres by the bin_cmd_smooth stamps.  h_norm[t] is normalize_value.  Output
+   (nx*ny, ntempl) column-major FP32, overwritten; edges must increase. */
+int sfh_binary_hess_batch_dev(sfh_ctx *ctx, const double *d_m_ini, const double *d_mags,
+                              int64_t total_points, const int64_t *h_off, const int32_t *h_len,
+                              int64_t ntempl, int nf, int y_index, int c1, int c2,
+                              const sfh_err_model *err, const sfh_compl_model *compl_,
+                              const double *bias, const sfh_imf *imf, double mean_mass,
+                              const double *h_norm, double x_first, double x_step, int64_t nx,
+                              double y_first, double y_step, int64_t ny, float *d_models);
+/* partial_cmd_smooth's single/binary mix (src/StarFormationHistories.jl:900-909):
+   d_out[:, t] = (1 - bmf[t]) d_single[:, t] + bmf[t] d_binary[:, t], bmf[t] the binary mass
+   fraction times trapz(new_mini, imf(new_mini)).  d_out may be d_single. */
+int sfh_mix_binary_templates_dev(sfh_ctx *ctx, const float *d_single, const float *d_binary,
+                                 const double *h_bmf, int64_t ntempl, int64_t nbins,
+                                 float *d_out);
+
 /* One template's Hess grid in a ragged batch: colour edges x_first + k x_step (k = 0..nx),
    magnitude edges y_first + k y_step (k = 0..ny); its (nx*ny) column-major histogram is
    written at d_models + out_offset. */

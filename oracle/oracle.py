@@ -100,6 +100,23 @@ def lib():
                 C.POINTER(ComplModel), C.c_void_p, C.POINTER(IMF), C.c_double, C.c_double,
                 C.c_double, C.c_double, C.c_double, _i64, C.c_double, C.c_double, _i64, _dp]
             L.sfho_partial_cmd_smooth.restype = _i64
+            L.sfho_mag2flux.argtypes = [C.c_double]
+            L.sfho_mag2flux.restype = C.c_double
+            L.sfho_flux2mag.argtypes = [C.c_double]
+            L.sfho_flux2mag.restype = C.c_double
+            L.sfho_trapz.argtypes = [_dp, _dp, _i64]
+            L.sfho_trapz.restype = C.c_double
+            L.sfho_binary_hess.argtypes = [
+                _dp, _dp, _i64, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(ErrModel),
+                C.POINTER(ComplModel), C.c_void_p, C.POINTER(IMF), C.c_double, C.c_double,
+                C.c_double, C.c_double, _i64, C.c_double, C.c_double, _i64, _dp]
+            L.sfho_binary_hess.restype = C.c_int
+            L.sfho_partial_cmd_smooth_binary.argtypes = [
+                _dp, _dp, _i64, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(ErrModel),
+                C.POINTER(ComplModel), C.c_void_p, C.POINTER(IMF), C.c_double, C.c_double,
+                C.c_double, C.c_double, C.c_double, C.c_double, _i64, C.c_double, C.c_double,
+                _i64, _dp]
+            L.sfho_partial_cmd_smooth_binary.restype = C.c_int
             L.sfho_powerlaw_mzr.argtypes = [C.c_double] * 4
             L.sfho_powerlaw_mzr.restype = C.c_double
             L.sfho_gauss_disp.argtypes = [C.c_double] * 3
@@ -329,6 +346,75 @@ def partial_cmd_smooth(m_ini, mags, err_models, compl_models, y_index, color_ind
                                       float(mean_mass), xf, xs, nx, yf, ys, ny, out)
     if k < 0:
         raise ValueError("partial_cmd_smooth: invalid arguments")
+    return out.reshape(ny, nx).T
+
+
+# ---------------- binary-star templates ----------------
+
+def mag2flux(m):
+    """mag2flux(m) with zero point 0, src/utilities.jl:57."""
+    return lib().sfho_mag2flux(float(m))
+
+
+def flux2mag(f):
+    """flux2mag(f) with zero point 0, src/utilities.jl:67."""
+    return lib().sfho_flux2mag(float(f))
+
+
+def trapz(x, y):
+    """Trapz.jl trapz(x, y)."""
+    x, y = _f64(x), _f64(y)
+    return lib().sfho_trapz(x, y, x.size)
+
+
+def binary_hess(m_ini, mags, err_models, compl_models, y_index, color_indices, imf,
+                normalize_value, mean_mass, xedges, yedges, bias=None):
+    """binary_hess(RandomBinaryPairs, ...), StarFormationHistories.jl:627-706 (magnitudes
+    already shifted by the distance modulus).  Returns (nx, ny) float64."""
+    mags = np.ascontiguousarray(mags, dtype=np.float64)
+    nf, n = mags.shape
+    E = (ErrModel * nf)(*err_models)
+    Cm = (ComplModel * nf)(*compl_models)
+    b = None
+    if bias is not None:
+        barr = _f64(bias)
+        b = barr.ctypes.data
+    xf, xs, nx = xedges
+    yf, ys, ny = yedges
+    out = np.empty(nx * ny)
+    k = lib().sfho_binary_hess(_f64(m_ini), mags.ravel(), n, nf, int(y_index),
+                               int(color_indices[0]), int(color_indices[1]), E, Cm, b,
+                               C.byref(imf), float(normalize_value), float(mean_mass), xf, xs, nx,
+                               yf, ys, ny, out)
+    if k < 0:
+        raise ValueError("binary_hess: invalid arguments" if k == -1 else
+                         "binary_hess: y_index must be one of color_indices")
+    return out.reshape(ny, nx).T
+
+
+def partial_cmd_smooth_binary(m_ini, mags, err_models, compl_models, y_index, color_indices,
+                              imf, dmod, normalize_value, mean_mass, binary_fraction, xedges,
+                              yedges, bias=None):
+    """partial_cmd_smooth with binary_model = RandomBinaryPairs(binary_fraction),
+    StarFormationHistories.jl:829-910.  Returns (nx, ny) float64."""
+    mags = np.ascontiguousarray(mags, dtype=np.float64)
+    nf, n = mags.shape
+    E = (ErrModel * nf)(*err_models)
+    Cm = (ComplModel * nf)(*compl_models)
+    b = None
+    if bias is not None:
+        barr = _f64(bias)
+        b = barr.ctypes.data
+    xf, xs, nx = xedges
+    yf, ys, ny = yedges
+    out = np.empty(nx * ny)
+    k = lib().sfho_partial_cmd_smooth_binary(_f64(m_ini), mags.ravel(), n, nf, int(y_index),
+                                             int(color_indices[0]), int(color_indices[1]), E, Cm,
+                                             b, C.byref(imf), float(dmod), float(normalize_value),
+                                             float(mean_mass), float(binary_fraction), xf, xs,
+                                             nx, yf, ys, ny, out)
+    if k < 0:
+        raise ValueError("partial_cmd_smooth_binary: invalid arguments")
     return out.reshape(ny, nx).T
 
 

@@ -493,6 +493,150 @@ int64_t sfho_partial_cmd_smooth(const double *m_ini, const double *mags, int64_t
     return M1;
 }
 
+/* ======================= binary-star templates ======================= */
+
+/* mag2flux(m, zpt = 0) = exp10(4 (zpt - m) / 10), src/utilities.jl:57 */
+double sfho_mag2flux(double m) { return pow(10.0, 4.0 * (0.0 - m) / 10.0); }
+/* flux2mag(f, zpt = 0) = zpt - 5 log10(f) / 2, src/utilities.jl:67 */
+double sfho_flux2mag(double f) { return 0.0 - 5.0 * log10(f) / 2.0; }
+
+/* Trapz.jl trapz(x, y): the trapezoidal rule Σ (x[i+1] - x[i]) (y[i] + y[i+1]) / 2. */
+double sfho_trapz(const double *x, const double *y, int64_t n) {
+    double s = 0.0;
+    for (int64_t i = 0; i + 1 < n; ++i) s += (x[i + 1] - x[i]) * (y[i] + y[i + 1]) / 2.0;
+    return s;
+}
+
+/* StatsBase fit(Histogram, ..., edges; closed=:left) on a range with step > 0: the bin k
+   (0-based) with first + k step <= v < first + (k+1) step, -1 outside. */
+static int64_t hist_bin(double v, double first, double step, int64_t n) {
+    if (!(v >= first)) return -1;
+    int64_t k = (int64_t)floor((v - first) / step);
+    if (k > 0 && v < first + (double)k * step) --k;
+    if (v >= first + (double)(k + 1) * step) ++k;
+    return (k >= 0 && k < n) ? k : -1;
+}
+
+int sfho_binary_hess(const double *m_ini, const double *mags, int64_t n, int nf, int y_index,
+                     int c1, int c2, const sfho_err_model *err, const sfho_compl_model *compl_,
+                     const double *bias, const sfho_imf *imf, double normalize_value,
+                     double mean_mass, double xfirst, double xstep, int64_t nx, double yfirst,
+                     double ystep, int64_t ny, double *out) {
+    if (nf < 2 || nf > 8 || n < 3 || !(xstep > 0) || !(ystep > 0)) return -1;
+    if (!(y_index == c1 || y_index == c2)) return -2; /* :700, not implemented there either */
+    /* :637-646 IMF values, pscale = trapz, prefactor, fluxes, mass spacing */
+    double *imfv = (double *)malloc(sizeof(double) * (size_t)n);
+    for (int64_t i = 0; i < n; ++i) imfv[i] = sfho_imf_pdf(imf, m_ini[i]);
+    const double pscale = sfho_trapz(m_ini, imfv, n);
+    const double prefac = normalize_value / mean_mass / 4.0 / pscale;
+    double *flux = (double *)malloc(sizeof(double) * (size_t)(n * nf));
+    for (int64_t k = 0; k < n * nf; ++k) flux[k] = sfho_mag2flux(mags[k]);
+    const int64_t ns = n - 1;
+    double *hist = (double *)calloc((size_t)(nx * ny), sizeof(double));
+    /* :648-664 pairs (i, j > i) of interval left points; :666-675 completeness (covariant
+       case: the two colour filters); :677-680 bias, colour, the left-closed histogram */
+    for (int64_t i = 0; i < ns; ++i) {
+        const double dMp = m_ini[i + 1] - m_ini[i], Mpint = imfv[i] + imfv[i + 1];
+        for (int64_t j = i + 1; j < ns; ++j) {
+            const double bm1 = sfho_flux2mag(flux[c1 * n + i] + flux[c1 * n + j]);
+            const double bm2 = sfho_flux2mag(flux[c2 * n + i] + flux[c2 * n + j]);
+            const double bmy = sfho_flux2mag(flux[y_index * n + i] + flux[y_index * n + j]);
+            double w = dMp * (m_ini[j + 1] - m_ini[j]) * Mpint * (imfv[j] + imfv[j + 1]) * prefac;
+            w *= compl_eval(&compl_[c1], bm1) * compl_eval(&compl_[c2], bm2);
+            const double b1 = bm1 + (bias ? bias[c1] : 0.0), b2 = bm2 + (bias ? bias[c2] : 0.0);
+            const double by = bmy + (bias ? bias[y_index] : 0.0);
+            const int64_t ix = hist_bin(b1 - b2, xfirst, xstep, nx);
+            const int64_t iy = hist_bin(by, yfirst, ystep, ny);
+            if (ix >= 0 && iy >= 0) hist[ix + nx * iy] += w;
+        }
+    }
+    /* :684-697 nonzero bins as points at the bin centres, errors at the centres */
+    int64_t ng = 0;
+    for (int64_t k = 0; k < nx * ny; ++k) ng += hist[k] != 0.0;
+    double *hx = (double *)malloc(sizeof(double) * (size_t)(ng + 1));
+    double *hy = (double *)malloc(sizeof(double) * (size_t)(ng + 1));
+    double *hsx = (double *)malloc(sizeof(double) * (size_t)(ng + 1));
+    double *hsy = (double *)malloc(sizeof(double) * (size_t)(ng + 1));
+    double *hw = (double *)malloc(sizeof(double) * (size_t)(ng + 1));
+    const int xc = (c1 != y_index) ? c1 : c2;
+    int64_t g = 0;
+    for (int64_t k = 0; k < nx * ny; ++k) {
+        if (hist[k] == 0.0) continue;
+        const int64_t ix = k % nx, iy = k / nx;
+        /* bin centres edges[k] + step / 2 with the edge correctly rounded (one fma), as the
+           device computes them: a centre is a pixel-rounding tie in bin_cmd_smooth
+           (x - first) / step + 1 = k + 1.5, so both must hold the same double */
+        const double cx = fma((double)ix, xstep, xfirst) + xstep / 2.0;
+        const double cy = fma((double)iy, ystep, yfirst) + ystep / 2.0;
+        const double xmag = (y_index == c1) ? cy - cx : cy + cx;
+        hx[g] = cx;
+        hy[g] = cy;
+        hsx[g] = err_eval(&err[xc], xmag);
+        hsy[g] = err_eval(&err[y_index], cy);
+        hw[g] = hist[k];
+        ++g;
+    }
+    /* :702-704 */
+    sfho_bin_cmd_smooth(hx, hy, hsx, hsy, hw, ng, (y_index == c1) ? -1 : 1, xfirst, xstep, nx,
+                        yfirst, ystep, ny, out);
+    free(imfv); free(flux); free(hist); free(hx); free(hy); free(hsx); free(hsy); free(hw);
+    return 0;
+}
+
+int sfho_partial_cmd_smooth_binary(const double *m_ini, const double *mags, int64_t n, int nf,
+                                   int y_index, int c1, int c2, const sfho_err_model *err,
+                                   const sfho_compl_model *compl_, const double *bias,
+                                   const sfho_imf *imf, double dmod, double normalize_value,
+                                   double mean_mass, double binary_fraction, double xfirst,
+                                   double xstep, int64_t nx, double yfirst, double ystep,
+                                   int64_t ny, double *out) {
+    /* :890-910: single stars, then for a binary fraction f > 0 the binary template of
+       every fourth resampled isochrone point, mixed by the binary mass fraction
+       2f / (1 + f) (simulate.jl:143, 190) times trapz(new_mini, imf(new_mini)) */
+    if (!(binary_fraction >= 0.0 && binary_fraction <= 1.0)) return -1;
+    if (sfho_partial_cmd_smooth(m_ini, mags, n, nf, y_index, c1, c2, err, compl_, bias, imf, dmod,
+                                normalize_value, mean_mass, xfirst, xstep, nx, yfirst, ystep, ny,
+                                out) < 0)
+        return -1;
+    if (binary_fraction == 0.0) return 0;
+    double *colors = (double *)malloc(sizeof(double) * (size_t)n);
+    for (int64_t i = 0; i < n; ++i) colors[i] = mags[c1 * n + i] - mags[c2 * n + i];
+    const double dmag = fabs(xstep) < fabs(ystep) ? fabs(xstep) : fabs(ystep);
+    int64_t cap = 1024, N;
+    double *new_mini = NULL;
+    for (;;) {
+        new_mini = (double *)realloc(new_mini, sizeof(double) * (size_t)cap);
+        N = sfho_mini_spacing(m_ini, colors, mags + (int64_t)y_index * n, n, dmag, new_mini, cap);
+        if (N >= 0) break;
+        cap = -N;
+    }
+    free(colors);
+    double *imag = (double *)malloc(sizeof(double) * (size_t)(N * nf));
+    for (int f = 0; f < nf; ++f) {
+        sfho_interpolate_mini(m_ini, mags + (int64_t)f * n, n, new_mini, N, imag + (int64_t)f * N);
+        for (int64_t i = 0; i < N; ++i) imag[f * N + i] += dmod;
+    }
+    const int64_t nd = (N + 3) / 4;  /* new_mini[begin:4:end] */
+    double *md = (double *)malloc(sizeof(double) * (size_t)nd);
+    double *magd = (double *)malloc(sizeof(double) * (size_t)(nd * nf));
+    for (int64_t i = 0; i < nd; ++i) {
+        md[i] = new_mini[4 * i];
+        for (int f = 0; f < nf; ++f) magd[f * nd + i] = imag[f * N + 4 * i];
+    }
+    double *bin = (double *)malloc(sizeof(double) * (size_t)(nx * ny));
+    int rc = sfho_binary_hess(md, magd, nd, nf, y_index, c1, c2, err, compl_, bias, imf,
+                              normalize_value, mean_mass, xfirst, xstep, nx, yfirst, ystep, ny, bin);
+    if (rc == 0) {
+        double *pv = (double *)malloc(sizeof(double) * (size_t)N);
+        for (int64_t i = 0; i < N; ++i) pv[i] = sfho_imf_pdf(imf, new_mini[i]);
+        const double bmf = 2.0 * binary_fraction / (1.0 + binary_fraction) * sfho_trapz(new_mini, pv, N);
+        for (int64_t k = 0; k < nx * ny; ++k) out[k] = out[k] * (1.0 - bmf) + bmf * bin[k];
+        free(pv);
+    }
+    free(new_mini); free(imag); free(md); free(magd); free(bin);
+    return rc;
+}
+
 /* ======================= hierarchical MZR ======================= */
 
 double sfho_powerlaw_mzr(double alpha, double MH0, double logMstar0, double Mstar) {

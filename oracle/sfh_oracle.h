@@ -111,6 +111,31 @@ int64_t sfho_partial_cmd_smooth(const double *m_ini, const double *mags, int64_t
                                 double mean_mass, double xfirst, double xstep, int64_t nx,
                                 double yfirst, double ystep, int64_t ny, double *out);
 
+/* ---------------- binary-star templates ---------------- */
+/* mag2flux / flux2mag with zero point 0, src/utilities.jl:57, 67 */
+double sfho_mag2flux(double m);
+double sfho_flux2mag(double f);
+/* Trapz.jl trapz(x, y) (trapezoidal rule), used at StarFormationHistories.jl:642, 907 */
+double sfho_trapz(const double *x, const double *y, int64_t n);
+/* binary_hess(RandomBinaryPairs, m_ini, mags, ...), src/StarFormationHistories.jl:627-706,
+   for y_index in color_indices (the only case the reference implements; -2 otherwise).
+   mags is nf*n (filter f at mags + f*n, distance modulus already added), bias constant per
+   filter, edges increasing.  out is nx*ny. */
+int sfho_binary_hess(const double *m_ini, const double *mags, int64_t n, int nf, int y_index,
+                     int c1, int c2, const sfho_err_model *err, const sfho_compl_model *compl_,
+                     const double *bias, const sfho_imf *imf, double normalize_value,
+                     double mean_mass, double xfirst, double xstep, int64_t nx, double yfirst,
+                     double ystep, int64_t ny, double *out);
+/* partial_cmd_smooth with binary_model = RandomBinaryPairs(binary_fraction),
+   src/StarFormationHistories.jl:829-910. */
+int sfho_partial_cmd_smooth_binary(const double *m_ini, const double *mags, int64_t n, int nf,
+                                   int y_index, int c1, int c2, const sfho_err_model *err,
+                                   const sfho_compl_model *compl_, const double *bias,
+                                   const sfho_imf *imf, double dmod, double normalize_value,
+                                   double mean_mass, double binary_fraction, double xfirst,
+                                   double xstep, int64_t nx, double yfirst, double ystep,
+                                   int64_t ny, double *out);
+
 /* ---------------- hierarchical MZR (src/fitting/hierarchical) ---------------- */
 /* PowerLawMZR(α, MH0, logMstar0)(Mstar), mzr.jl:275 */
 double sfho_powerlaw_mzr(double alpha, double MH0, double logMstar0, double Mstar);

@@ -841,3 +841,269 @@ extern "C" int sfh_partial_cmd_smooth_ragged_dev(
     return partial_run(ctx, d_m_ini, d_mags, h_iso_off, h_iso_len, ntempl, P, y_index, c1, h_dmod,
                        h_norm, &rg, 0.0, 0.0, 0, 0.0, 0.0, 0, d_models);
 }
+
+// ---------------------------------------------------------------- binary_hess (RandomBinaryPairs)
+// src/StarFormationHistories.jl:627-706 for a batch of templates: every pair (i, j > i) of
+// interval left points of a template's (downsampled) isochrone is a binary system whose
+// magnitudes add in flux (:656), weighted ΔMp ΔMs (imf_i + imf_i+1)(imf_j + imf_j+1) prefac
+// (:660-662) times the colour filters' completeness (:666-668), shifted by the bias
+// (:677-678) and binned in a left-closed histogram (:680, FP64 atomics); the nonzero bins
+// become points at the bin centres with errors at the centres (:684-697) and are smoothed by
+// the bin_cmd_smooth stamps (:702).  One thread per pair.
+namespace {
+
+constexpr int kPairThreads = 256;
+
+// prefac[t] = norm[t] / mean_mass / 4 / trapz(m, imf(m)) (:642-643); one block per template,
+// fixed-order block sum.
+__global__ void __launch_bounds__(kPairThreads)
+k_bin_prefac(IsoParams P, const double *__restrict__ m, const int64_t *__restrict__ off,
+             const int32_t *__restrict__ len, const double *__restrict__ norm,
+             double *__restrict__ prefac) {
+    __shared__ double s_red[kPairThreads / 32];
+    const int t = blockIdx.x, n = len[t];
+    const double *mt = m + off[t];
+    double acc = 0.0;
+    for (int i = threadIdx.x; i + 1 < n; i += blockDim.x)
+        acc += (mt[i + 1] - mt[i]) * (imf_pdf(P, mt[i]) + imf_pdf(P, mt[i + 1])) / 2.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tot = 0.0;
+        for (int w = 0; w < kPairThreads / 32; ++w) tot += s_red[w];
+        prefac[t] = norm[t] * P.inv_mean_mass / 4.0 / tot;
+    }
+}
+
+// fluxes of the two colour filters and the magnitude filter (:644), and IMF values.
+__global__ void k_bin_flux(IsoParams P, const double *__restrict__ m, const double *__restrict__ mags,
+                           int64_t total, double *__restrict__ fl, double *__restrict__ imfv) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const int fs[3] = {P.c1, P.c2, P.y_index};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) fl[q * total + i] = exp10(-0.4 * mags[(int64_t)fs[q] * total + i]);
+    imfv[i] = imf_pdf(P, m[i]);
+}
+
+// left-closed histogram bin of v (edges first + k step, step > 0), -1 outside
+__device__ __forceinline__ int hist_bin(double v, double first, double step, int n) {
+    if (!(v >= first)) return -1;
+    int k = (int)floor((v - first) / step);
+    if (k > 0 && v < first + (double)k * step) --k;
+    if (v >= first + (double)(k + 1) * step) ++k;
+    return (k >= 0 && k < n) ? k : -1;
+}
+
+// Grid: x -> j blocks, y -> i, z -> template (chunk-relative).  hist is [chunk][nx*ny].
+__global__ void __launch_bounds__(kPairThreads)
+k_bin_pairs(IsoParams P, const double *__restrict__ m, const double *__restrict__ fl,
+            const double *__restrict__ imfv, int64_t total, const int64_t *__restrict__ off,
+            const int32_t *__restrict__ len, const double *__restrict__ prefac, Grid2 g,
+            int t0, double *__restrict__ hist) {
+    const int t = t0 + blockIdx.z, n = len[t], ns = n - 1;
+    const int i = blockIdx.y, j = i + 1 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ns || j >= ns) return;
+    const int64_t o = off[t];
+    const double *mt = m + o, *iv = imfv + o;
+    const double *f1 = fl + o, *f2 = fl + total + o, *fy = fl + 2 * total + o;
+    // flux2mag(f) = -5 log10(f) / 2 (:656)
+    const double bm1 = -2.5 * log10(f1[i] + f1[j]);
+    const double bm2 = -2.5 * log10(f2[i] + f2[j]);
+    const double bmy = -2.5 * log10(fy[i] + fy[j]);
+    double w = (mt[i + 1] - mt[i]) * (mt[j + 1] - mt[j]) * (iv[i] + iv[i + 1]) * (iv[j] + iv[j + 1]) *
+               prefac[t];
+    w *= compl_eval(P, P.c1, bm1) * compl_eval(P, P.c2, bm2);
+    const double col = (bm1 + P.bias[P.c1]) - (bm2 + P.bias[P.c2]);
+    const double ym = bmy + P.bias[P.y_index];
+    const int ix = hist_bin(col, g.xf, g.xs, g.nx), iy = hist_bin(ym, g.yf, g.ys, g.ny);
+    if (ix >= 0 && iy >= 0)
+        atomicAdd(hist + (int64_t)blockIdx.z * g.nx * g.ny + ix + (int64_t)g.nx * iy, w);
+}
+
+// nonzero bins of each template (one block per template of the chunk)
+__global__ void __launch_bounds__(kPairThreads)
+k_bin_count(const double *__restrict__ hist, int64_t nbins, int32_t *__restrict__ cnt) {
+    __shared__ int s_red[kPairThreads / 32];
+    const double *h = hist + (int64_t)blockIdx.x * nbins;
+    int c = 0;
+    for (int64_t k = threadIdx.x; k < nbins; k += blockDim.x) c += h[k] != 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int tot = 0;
+        for (int w = 0; w < kPairThreads / 32; ++w) tot += s_red[w];
+        cnt[blockIdx.x] = tot;
+    }
+}
+
+// points of the nonzero bins in bin order (x fastest), at start[t]: thread q takes a
+// contiguous range of bins; a block scan of the range counts gives its first point.
+__global__ void __launch_bounds__(kPairThreads)
+k_bin_points(IsoParams P, const double *__restrict__ hist, Grid2 g, const int64_t *__restrict__ start,
+             double *__restrict__ px, double *__restrict__ py, double *__restrict__ psx,
+             double *__restrict__ psy, double *__restrict__ pw) {
+    __shared__ int s_scan[kPairThreads];
+    const int64_t nbins = (int64_t)g.nx * g.ny;
+    const double *h = hist + (int64_t)blockIdx.x * nbins;
+    const int64_t per = (nbins + kPairThreads - 1) / kPairThreads;
+    const int64_t k0 = (int64_t)threadIdx.x * per, k1 = k0 + per < nbins ? k0 + per : nbins;
+    int c = 0;
+    for (int64_t k = k0; k < k1; ++k) c += h[k] != 0.0;
+    s_scan[threadIdx.x] = c;
+    __syncthreads();
+    for (int o = 1; o < kPairThreads; o <<= 1) {  // inclusive scan (Hillis-Steele)
+        const int v = threadIdx.x >= o ? s_scan[threadIdx.x - o] : 0;
+        __syncthreads();
+        s_scan[threadIdx.x] += v;
+        __syncthreads();
+    }
+    int64_t q = start[blockIdx.x] + s_scan[threadIdx.x] - c;
+    const int xc = (P.c1 != P.y_index) ? P.c1 : P.c2;
+    for (int64_t k = k0; k < k1; ++k) {
+        if (h[k] == 0.0) continue;
+        const int ix = (int)(k % g.nx), iy = (int)(k / g.nx);
+        // edges[k] + step / 2 (:688-689) with the edge correctly rounded by one fma and no
+        // further contraction: the centre is a rounding tie of the stamp's pixel
+        // (x - first) / step + 1 = k + 1.5, so its exact double decides the stamp's pixel
+        const double cx = __dadd_rn(__fma_rn((double)ix, g.xs, g.xf), g.xs / 2.0);
+        const double cy = __dadd_rn(__fma_rn((double)iy, g.ys, g.yf), g.ys / 2.0);
+        const double xmag = (P.y_index == P.c1) ? cy - cx : cy + cx;  // :692-695
+        px[q] = cx;
+        py[q] = cy;
+        psx[q] = err_eval(P, xc, xmag);
+        psy[q] = err_eval(P, P.y_index, cy);
+        pw[q] = h[k];
+        ++q;
+    }
+}
+
+__global__ void k_mix_binary(const float *__restrict__ single, const float *__restrict__ binary,
+                             const double *__restrict__ bmf, int64_t nbins, int64_t n,
+                             float *__restrict__ out) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const double b = bmf[k / nbins];
+    out[k] = (float)((double)single[k] * (1.0 - b) + b * (double)binary[k]);
+}
+
+}  // namespace
+
+extern "C" int sfh_binary_hess_batch_dev(sfh_ctx *ctx, const double *d_m_ini, const double *d_mags,
+                                         int64_t total_points, const int64_t *h_off,
+                                         const int32_t *h_len, int64_t ntempl, int nf,
+                                         int y_index, int c1, int c2, const sfh_err_model *err,
+                                         const sfh_compl_model *compl_, const double *bias,
+                                         const sfh_imf *imf, double mean_mass,
+                                         const double *h_norm, double x_first, double x_step,
+                                         int64_t nx, double y_first, double y_step, int64_t ny,
+                                         float *d_models) {
+    if (!ctx || !d_m_ini || !d_mags || !h_off || !h_len || !err || !compl_ || !imf || !h_norm ||
+        !d_models || ntempl < 1 || ntempl > 65535 || total_points < 1 || nx < 1 || ny < 1)
+        return SFH_ERR_ARG;
+    if (!(x_step > 0) || !(y_step > 0))
+        return sfh_set_error(ctx, SFH_ERR_ARG, "binary_hess: bin edges must increase");
+    if (!(y_index == c1 || y_index == c2))  // :700
+        return sfh_set_error(ctx, SFH_ERR_UNSUPPORTED,
+                             "binary_hess for y_index not in color_indices is not implemented");
+    IsoParams P;
+    int rc = make_iso_params(ctx, nf, y_index, c1, c2, err, compl_, bias, imf, mean_mass,
+                             total_points, P);
+    if (rc) return rc;
+    int nmax = 0;
+    for (int64_t t = 0; t < ntempl; ++t) {
+        if (h_len[t] < 3 || h_len[t] > 65536 || h_off[t] < 0 || h_off[t] + h_len[t] > total_points)
+            return sfh_set_error(ctx, SFH_ERR_ARG, "binary_hess: isochrone lengths in [3, 65536]");
+        nmax = h_len[t] > nmax ? h_len[t] : nmax;
+    }
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const int64_t nbins = nx * ny;
+    // per-call buffers (template builds are not latency critical)
+    const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(ntempl, (256ll << 20) / (nbins * 8)));
+    double *fl = nullptr, *imfv = nullptr, *prefac = nullptr, *hist = nullptr, *d_norm = nullptr;
+    int64_t *d_off = nullptr, *d_start = nullptr;
+    int32_t *d_len = nullptr, *d_cnt = nullptr, *d_cov = nullptr;
+    double *pts = nullptr;
+    auto cleanup = [&]() {
+        cudaStreamSynchronize(st);
+        for (void *p : {(void *)fl, (void *)imfv, (void *)prefac, (void *)hist, (void *)d_norm,
+                        (void *)d_off, (void *)d_start, (void *)d_len, (void *)d_cnt, (void *)d_cov,
+                        (void *)pts})
+            if (p) cudaFree(p);
+    };
+    cudaError_t e = cudaSuccess;
+    if ((e = cudaMalloc(&fl, 3 * total_points * 8)) || (e = cudaMalloc(&imfv, total_points * 8)) ||
+        (e = cudaMalloc(&prefac, ntempl * 8)) || (e = cudaMalloc(&hist, chunk * nbins * 8)) ||
+        (e = cudaMalloc(&d_norm, ntempl * 8)) || (e = cudaMalloc(&d_off, ntempl * 8)) ||
+        (e = cudaMalloc(&d_start, chunk * 8)) || (e = cudaMalloc(&d_len, ntempl * 4)) ||
+        (e = cudaMalloc(&d_cnt, chunk * 4)) || (e = cudaMalloc(&d_cov, chunk * 4))) {
+        cleanup();
+        return sfh_cuda_error(ctx, e, "binary_hess buffers");
+    }
+    cudaMemcpyAsync(d_norm, h_norm, ntempl * 8, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d_off, h_off, ntempl * 8, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d_len, h_len, ntempl * 4, cudaMemcpyHostToDevice, st);
+    std::vector<int32_t> hcov((size_t)chunk, y_index == c1 ? -1 : 1);  // :698
+    cudaMemcpyAsync(d_cov, hcov.data(), chunk * 4, cudaMemcpyHostToDevice, st);
+    k_bin_flux<<<(unsigned)((total_points + 255) / 256), 256, 0, st>>>(P, d_m_ini, d_mags, total_points,
+                                                                    fl, imfv);
+    k_bin_prefac<<<(unsigned)ntempl, kPairThreads, 0, st>>>(P, d_m_ini, d_off, d_len, d_norm, prefac);
+    ctx->launches += 2;
+    Grid2 g{x_first, x_step, y_first, y_step, (int)nx, (int)ny};
+    std::vector<int32_t> hcnt((size_t)chunk);
+    std::vector<int64_t> hstart((size_t)chunk);
+    size_t pts_cap = 0;
+    for (int64_t t0 = 0; t0 < ntempl && rc == SFH_OK; t0 += chunk) {
+        const int64_t nc = std::min(chunk, ntempl - t0);
+        if ((e = cudaMemsetAsync(hist, 0, nc * nbins * 8, st))) { rc = sfh_cuda_error(ctx, e, "memset"); break; }
+        dim3 grid((unsigned)((nmax + kPairThreads - 1) / kPairThreads), (unsigned)(nmax - 1), (unsigned)nc);
+        k_bin_pairs<<<grid, kPairThreads, 0, st>>>(P, d_m_ini, fl, imfv, total_points, d_off, d_len,
+                                                    prefac, g, (int)t0, hist);
+        k_bin_count<<<(unsigned)nc, kPairThreads, 0, st>>>(hist, nbins, d_cnt);
+        ctx->launches += 2;
+        if ((e = cudaMemcpyAsync(hcnt.data(), d_cnt, nc * 4, cudaMemcpyDeviceToHost, st)) ||
+            (e = cudaStreamSynchronize(st))) { rc = sfh_cuda_error(ctx, e, "binary_hess counts"); break; }
+        int64_t tot = 0;
+        for (int64_t q = 0; q < nc; ++q) { hstart[(size_t)q] = tot; tot += hcnt[(size_t)q]; }
+        const size_t need = (size_t)std::max<int64_t>(tot, 1) * 5 * 8;
+        if (need > pts_cap) {
+            if (pts) cudaFree(pts);
+            pts = nullptr;
+            if ((e = cudaMalloc(&pts, need))) { rc = sfh_cuda_error(ctx, e, "binary_hess points"); break; }
+            pts_cap = need;
+        }
+        const int64_t np = std::max<int64_t>(tot, 1);
+        double *px = pts, *py = pts + np, *psx = pts + 2 * np, *psy = pts + 3 * np, *pw = pts + 4 * np;
+        cudaMemcpyAsync(d_start, hstart.data(), nc * 8, cudaMemcpyHostToDevice, st);
+        k_bin_points<<<(unsigned)nc, kPairThreads, 0, st>>>(P, hist, g, d_start, px, py, psx, psy, pw);
+        ctx->launches++;
+        rc = sfh_launch_stamps(ctx, px, py, psx, psy, pw, d_start, d_cnt, d_cov, nc, x_first, x_step,
+                               nx, y_first, y_step, ny, d_models + t0 * nbins);
+        if (rc == SFH_OK && (e = cudaStreamSynchronize(st))) rc = sfh_cuda_error(ctx, e, "binary_hess");
+    }
+    cleanup();
+    return rc;
+}
+
+extern "C" int sfh_mix_binary_templates_dev(sfh_ctx *ctx, const float *d_single,
+                                            const float *d_binary, const double *h_bmf,
+                                            int64_t ntempl, int64_t nbins, float *d_out) {
+    if (!ctx || !d_single || !d_binary || !h_bmf || !d_out || ntempl < 1 || nbins < 1)
+        return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    double *d_bmf = nullptr;
+    SFH_CK(ctx, cudaMalloc(&d_bmf, ntempl * 8));
+    cudaMemcpyAsync(d_bmf, h_bmf, ntempl * 8, cudaMemcpyHostToDevice, ctx->stream);
+    const int64_t n = ntempl * nbins;
+    k_mix_binary<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(d_single, d_binary, d_bmf,
+                                                                       nbins, n, d_out);
+    ctx->launches++;
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(d_bmf);
+    return e == cudaSuccess ? SFH_OK : sfh_cuda_error(ctx, e, "mix binary templates");
+}

@@ -17,7 +17,8 @@ from .templates import (BrokenPowerLawIMF, Histogram, Kroupa2001, Martin2016_com
                         bin_cmd_smooth, calculate_edges, calculate_weights, compl_model, err_model,
                         exp_photerr, histogram_data, histogram_pix, interpolate_mini, midpoints,
                         mini_spacing, partial_cmd_smooth, partial_cmd_smooth_batch,
-                        partial_cmd_smooth_ragged)
+                        partial_cmd_smooth_ragged, NoBinaries, RandomBinaryPairs, trapz,
+                        binary_points, binary_hess_batch, partial_cmd_smooth_binary_batch)
 
 __all__ = [
     "SFH_BF16X2", "SFH_F32", "SFH_F64", "EXPORTED", "LIB_PATH", "SFHArgumentError", "SFHError",
@@ -27,7 +28,8 @@ __all__ = [
     "Histogram", "Kroupa2001", "Martin2016_complete", "bin_cmd_smooth", "calculate_edges",
     "calculate_weights", "compl_model", "err_model", "exp_photerr", "histogram_data",
     "histogram_pix", "interpolate_mini", "midpoints", "mini_spacing", "partial_cmd_smooth",
-    "partial_cmd_smooth_batch", "GaussianDispersion", "PowerLawMZR", "calculate_coeffs",
+    "partial_cmd_smooth_batch", "NoBinaries", "RandomBinaryPairs", "trapz", "binary_points",
+    "binary_hess_batch", "partial_cmd_smooth_binary_batch", "GaussianDispersion", "PowerLawMZR", "calculate_coeffs",
     "hmc_sample", "logdensity_batched", "sample_sfh", "Galaxies", "fg_ragged",
     "partial_cmd_smooth_ragged", "SyntheticGenerator", "TemplateEmulator", "LinearAMR",
     "construct_x0_mdf", "fixed_amr", "truncate_relweights", "LogarithmicAMR", "MH_from_Z",

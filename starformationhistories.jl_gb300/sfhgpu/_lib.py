@@ -30,6 +30,7 @@ EXPORTED = [
     "sfh_models_path", "sfh_fg_dev_noalloc", "sfh_hmc_sample_dev",
     "sfh_logdensity_batched_dev", "sfh_bin_cmd_smooth", "sfh_bin_cmd_smooth_batch_dev",
     "sfh_partial_cmd_smooth_batch_dev", "sfh_partial_cmd_smooth_ragged_dev",
+    "sfh_binary_hess_batch_dev", "sfh_mix_binary_templates_dev",
     "sfh_galaxies_create", "sfh_galaxies_free", "sfh_galaxies_info", "sfh_fg_ragged_dev",
     "sfh_mlp_param_count", "sfh_mlp_forward",
     "sfh_mlp_loss_grad", "sfh_mlp_train", "sfh_mlp_train_grouped", "sfh_mlp_forward_rows",
@@ -128,6 +129,11 @@ def load(path: str | None = None):
                 [_vp, _vp, _vp, _i64, _vp, _vp, _i64, C.c_int, C.c_int, C.c_int, C.c_int,
                  C.POINTER(ErrModel), C.POINTER(ComplModel), _vp, C.POINTER(IMFParams), _d, _vp,
                  _vp, _d, _d, _i64, _d, _d, _i64, _vp], C.c_int),
+            "sfh_binary_hess_batch_dev": (
+                [_vp, _vp, _vp, _i64, _vp, _vp, _i64, C.c_int, C.c_int, C.c_int, C.c_int,
+                 C.POINTER(ErrModel), C.POINTER(ComplModel), _vp, C.POINTER(IMFParams), _d, _vp,
+                 _d, _d, _i64, _d, _d, _i64, _vp], C.c_int),
+            "sfh_mix_binary_templates_dev": ([_vp, _vp, _vp, _vp, _i64, _i64, _vp], C.c_int),
             "sfh_partial_cmd_smooth_ragged_dev": (
                 [_vp, _vp, _vp, _i64, _vp, _vp, _i64, C.c_int, C.c_int, C.c_int, C.c_int,
                  C.POINTER(ErrModel), C.POINTER(ComplModel), _vp, C.POINTER(IMFParams), _d, _vp,

@@ -345,6 +345,143 @@ def partial_cmd_smooth_batch(m_ini, mags, iso_off, iso_len, y_index, color_indic
     return out
 
 
+# ---------------------------------------------------------------- binary models (src/simulate.jl)
+
+class NoBinaries:
+    """NoBinaries(), src/simulate.jl:153-157: no binary systems."""
+
+    def binary_system_fraction(self):
+        return 0.0
+
+    def binary_number_fraction(self):
+        return 0.0
+
+    def binary_mass_fraction(self, imf=None):
+        return 0.0
+
+
+class RandomBinaryPairs:
+    """RandomBinaryPairs(fraction), src/simulate.jl:159-190: a fraction of stellar systems
+    are pairs of stars drawn from the single-star IMF."""
+
+    def __init__(self, fraction):
+        if not (0.0 <= fraction <= 1.0):
+            raise ValueError("0 <= fraction <= 1")
+        self.fraction = fraction
+
+    def binary_system_fraction(self):
+        return self.fraction
+
+    def binary_number_fraction(self):
+        b = self.fraction  # 2b / (1 + b), simulate.jl:143
+        return 2 * b / (1 + b)
+
+    def binary_mass_fraction(self, imf=None):
+        return self.binary_number_fraction()  # simulate.jl:190
+
+
+def trapz(x, y):
+    """Trapz.jl trapz(x, y): the trapezoidal rule."""
+    x = np.asarray(x, dtype=np.float64)
+    y = np.asarray(y, dtype=np.float64)
+    return float(np.sum(np.diff(x) * (y[1:] + y[:-1]) / 2.0))
+
+
+def binary_points(m_ini, mags, y_index, color_indices, dmod, edges, ds=4):
+    """The isochrone points partial_cmd_smooth hands to binary_hess
+    (src/StarFormationHistories.jl:848-855, 895-897): mini_spacing on the bin step,
+    interpolation of every filter plus the distance modulus, every ds-th point; and the
+    resampled masses (for the mixing fraction).  Returns (m_ds, mags_ds (nf, n_ds), new_mini)."""
+    (xf, xs, nx), (yf, ys, ny) = _range(edges[0]), _range(edges[1])
+    c1, c2 = color_indices
+    mags = [np.asarray(m, dtype=np.float64) for m in mags]
+    colors = mags[c1] - mags[c2]
+    new_mini = mini_spacing(m_ini, colors, mags[y_index], min(abs(xs), abs(ys)), False)
+    iso = np.stack([interpolate_mini(m_ini, m, new_mini) + dmod for m in mags])
+    return new_mini[::ds], np.ascontiguousarray(iso[:, ::ds]), new_mini
+
+
+def binary_hess_batch(m_ini, mags, iso_off, iso_len, y_index, color_indices, err_models,
+                      compl_models, imf, normalize_value, edges, mean_mass=None, bias=None,
+                      out=None, ctx=None):
+    """binary_hess(RandomBinaryPairs, ...) for many templates (sfh_binary_hess_batch_dev,
+    src/StarFormationHistories.jl:627-706).  m_ini, mags: torch CUDA float64 tensors of the
+    (downsampled, distance-shifted) isochrone points, mags (nf, total); iso_off / iso_len
+    locate template t.  Returns (or fills) a CUDA float32 tensor (ntempl, nx*ny)."""
+    import torch
+    ctx = ctx or default_context()
+    nf, total = mags.shape
+    iso_off = np.ascontiguousarray(iso_off, dtype=np.int64)
+    iso_len = np.ascontiguousarray(iso_len, dtype=np.int32)
+    nt = iso_off.size
+    nm = np.ascontiguousarray(np.broadcast_to(np.asarray(normalize_value, dtype=np.float64), (nt,)))
+    (xf, xs, nx), (yf, ys, ny) = _range(edges[0]), _range(edges[1])
+    if out is None:
+        out = torch.empty((nt, nx * ny), dtype=torch.float32, device=m_ini.device)
+    E = (ErrModel * nf)(*err_models)
+    Cm = (ComplModel * nf)(*compl_models)
+    b = None
+    if bias is not None:
+        barr = np.ascontiguousarray(bias, dtype=np.float64)
+        b = barr.ctypes.data
+    ip = imf.params()
+    mm = imf.mean() if mean_mass is None else float(mean_mass)
+    m_ini = m_ini.contiguous()
+    mags = mags.contiguous()
+    torch.cuda.current_stream(m_ini.device).synchronize()
+    check(load().sfh_binary_hess_batch_dev(
+        ctx.handle, m_ini.data_ptr(), mags.data_ptr(), int(total), iso_off.ctypes.data,
+        iso_len.ctypes.data, nt, nf, int(y_index), int(color_indices[0]), int(color_indices[1]),
+        E, Cm, b, C.byref(ip), mm, nm.ctypes.data, xf, xs, nx, yf, ys, ny, out.data_ptr()),
+        ctx.handle, "binary_hess_batch")
+    return out
+
+
+def partial_cmd_smooth_binary_batch(m_ini, mags, iso_off, iso_len, y_index, color_indices,
+                                    err_models, compl_models, imf, dmod, normalize_value, edges,
+                                    binary_model, mean_mass=None, bias=None, out=None, ctx=None):
+    """partial_cmd_smooth with a binary model for many templates
+    (src/StarFormationHistories.jl:829-910): the single-star batch on the GPU, then for a
+    binary fraction > 0 the binary templates of every fourth resampled isochrone point
+    (resampling on the host, pairs and smoothing on the GPU) mixed by the binary mass
+    fraction times trapz(new_mini, imf(new_mini)).  Arguments as partial_cmd_smooth_batch."""
+    import torch
+    ctx = ctx or default_context()
+    out = partial_cmd_smooth_batch(m_ini, mags, iso_off, iso_len, y_index, color_indices,
+                                   err_models, compl_models, imf, dmod, normalize_value, edges,
+                                   mean_mass=mean_mass, bias=bias, out=out, ctx=ctx)
+    frac = binary_model.binary_system_fraction()
+    if frac == 0:
+        return out
+    nf = mags.shape[0]
+    iso_off = np.asarray(iso_off, dtype=np.int64)
+    iso_len = np.asarray(iso_len, dtype=np.int32)
+    nt = iso_off.size
+    dm = np.broadcast_to(np.asarray(dmod, dtype=np.float64), (nt,))
+    hm, hg = m_ini.detach().cpu().numpy(), mags.detach().cpu().numpy()
+    md, gd, bmf = [], [], np.empty(nt)
+    bnf = binary_model.binary_mass_fraction(imf)
+    for t in range(nt):
+        o, n = int(iso_off[t]), int(iso_len[t])
+        m_ds, g_ds, new_mini = binary_points(hm[o:o + n], [hg[f, o:o + n] for f in range(nf)],
+                                             y_index, color_indices, dm[t], edges)
+        md.append(m_ds)
+        gd.append(g_ds)
+        bmf[t] = bnf * trapz(new_mini, imf.pdf(new_mini))
+    lens = np.array([m.size for m in md], dtype=np.int32)
+    offs = np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(np.int64)
+    d_m = torch.tensor(np.concatenate(md), device=m_ini.device)
+    d_g = torch.tensor(np.ascontiguousarray(np.concatenate(gd, axis=1)), device=m_ini.device)
+    binary = binary_hess_batch(d_m, d_g, offs, lens, y_index, color_indices, err_models,
+                               compl_models, imf, normalize_value, edges, mean_mass=mean_mass,
+                               bias=bias, ctx=ctx)
+    bm = np.ascontiguousarray(bmf)
+    check(load().sfh_mix_binary_templates_dev(ctx.handle, out.data_ptr(), binary.data_ptr(),
+                                              bm.ctypes.data, nt, out.shape[1], out.data_ptr()),
+          ctx.handle, "mix_binary_templates")
+    return out
+
+
 class HessGrid(C.Structure):
     """sfh_hess_grid: one template's Hess grid and output offset in a ragged batch."""
     _fields_ = [("x_first", C.c_double), ("x_step", C.c_double), ("nx", C.c_int64),
