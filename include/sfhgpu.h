@@ -247,6 +247,20 @@ int sfh_logdensity_batched_dev(sfh_ctx *ctx, const sfh_models *models, const dou
                                double *d_grad);
 
 /* ---------------------------------------------------------------- template construction */
+/* bin_cmd(colors, mags; weights, edges), StarFormationHistories.jl:544-553: the
+   hard-binned Hess diagram, StatsBase fit(Histogram, (colors, mags), Weights(weights), edges;
+   closed=:left).  Host arrays: colors, mags, weights (NULL = unit weights) of n points;
+   xedges holds nx + 1 and yedges ny + 1 finite increasing values (the ranges' elements);
+   bin (i, j) counts xedges[i] <= color < xedges[i+1] and yedges[j] <= mag < yedges[j+1].
+   hist_out is host (nx, ny) column-major doubles, overwritten.  Synchronous. */
+int sfh_bin_cmd(sfh_ctx *ctx, const double *colors, const double *mags, const double *weights,
+                int64_t n, const double *xedges, int64_t nx, const double *yedges, int64_t ny,
+                double *hist_out);
+/* sfh_bin_cmd on device buffers, ordered on the context's stream (no synchronisation). */
+int sfh_bin_cmd_dev(sfh_ctx *ctx, const double *d_colors, const double *d_mags,
+                    const double *d_weights, int64_t n, const double *d_xedges, int64_t nx,
+                    const double *d_yedges, int64_t ny, double *d_hist_out);
+
 /* bin_cmd_smooth(colors, mags, color_err, mag_err, cov_mult; weights, edges),
    StarFormationHistories.jl:574-621 (kernels :191-340, addstar! :345-408).
    Host arrays of npts doubles; edges are ranges first + k*step (k = 0..n);

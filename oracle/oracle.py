@@ -100,6 +100,10 @@ def lib():
                 C.POINTER(ComplModel), C.c_void_p, C.POINTER(IMF), C.c_double, C.c_double,
                 C.c_double, C.c_double, C.c_double, _i64, C.c_double, C.c_double, _i64, _dp]
             L.sfho_partial_cmd_smooth.restype = _i64
+            L.sfho_bin_cmd.argtypes = [_dp, _dp, C.c_void_p, _i64, _dp, _i64, _dp, _i64, _dp]
+            L.sfho_partial_cmd.argtypes = [_dp, _dp, _dp, _i64, C.POINTER(IMF), C.c_double,
+                                           C.c_double, C.c_double, _dp, _i64, _dp, _i64, _dp]
+            L.sfho_partial_cmd.restype = C.c_int
             L.sfho_mag2flux.argtypes = [C.c_double]
             L.sfho_mag2flux.restype = C.c_double
             L.sfho_flux2mag.argtypes = [C.c_double]
@@ -350,6 +354,30 @@ def partial_cmd_smooth(m_ini, mags, err_models, compl_models, y_index, color_ind
 
 
 # ---------------- binary-star templates ----------------
+
+def bin_cmd(x, y, w, xedges, yedges):
+    """bin_cmd, StarFormationHistories.jl:544-553, on explicit edge vectors.  Returns the
+    (nx, ny) float64 weights."""
+    x, y, ex, ey = _f64(x), _f64(y), _f64(xedges), _f64(yedges)
+    warr = None if w is None else _f64(w)
+    nx, ny = ex.size - 1, ey.size - 1
+    out = np.empty(nx * ny)
+    lib().sfho_bin_cmd(x, y, None if warr is None else warr.ctypes.data, x.size, ex, nx, ey, ny,
+                       out)
+    return out.reshape(ny, nx).T
+
+
+def partial_cmd(m_ini, colors, mags, imf, dmod, normalize_value, mean_mass, xedges, yedges):
+    """partial_cmd (error-free template), StarFormationHistories.jl:733-757."""
+    ex, ey = _f64(xedges), _f64(yedges)
+    nx, ny = ex.size - 1, ey.size - 1
+    out = np.empty(nx * ny)
+    m_ini, colors, mags = _f64(m_ini), _f64(colors), _f64(mags)
+    if lib().sfho_partial_cmd(m_ini, colors, mags, m_ini.size, C.byref(imf), float(dmod),
+                              float(normalize_value), float(mean_mass), ex, nx, ey, ny, out) < 0:
+        raise ValueError("partial_cmd: invalid arguments")
+    return out.reshape(ny, nx).T
+
 
 def mag2flux(m):
     """mag2flux(m) with zero point 0, src/utilities.jl:57."""

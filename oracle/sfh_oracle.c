@@ -517,6 +517,65 @@ static int64_t hist_bin(double v, double first, double step, int64_t n) {
     return (k >= 0 && k < n) ? k : -1;
 }
 
+/* searchsortedlast(e, v) - 1 over the n + 1 increasing edge values e: the 0-based bin k with
+   e[k] <= v < e[k+1], -1 outside or NaN (StatsBase's left-closed bin index on the stored
+   range elements). */
+static int64_t edge_bin(double v, const double *e, int64_t n) {
+    if (!(v >= e[0]) || !(v < e[n])) return -1;
+    int64_t lo = 0, hi = n; /* e[lo] <= v < e[hi] */
+    while (hi - lo > 1) {
+        const int64_t mid = lo + (hi - lo) / 2;
+        if (v >= e[mid]) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+/* bin_cmd(colors, mags; weights, edges), src/StarFormationHistories.jl:544-553: StatsBase
+   fit(Histogram, (x, y), Weights(w), edges; closed=:left) with xedges (nx + 1 values) and
+   yedges (ny + 1).  w NULL means unit weights.  out is nx*ny (column-major), zeroed here. */
+void sfho_bin_cmd(const double *x, const double *y, const double *w, int64_t n,
+                  const double *xedges, int64_t nx, const double *yedges, int64_t ny,
+                  double *out) {
+    memset(out, 0, sizeof(double) * (size_t)(nx * ny));
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t ix = edge_bin(x[i], xedges, nx), iy = edge_bin(y[i], yedges, ny);
+        if (ix >= 0 && iy >= 0) out[ix + nx * iy] += w ? w[i] : 1.0;
+    }
+}
+
+/* partial_cmd(m_ini, colors, mags, imf; dmod, normalize_value, mean_mass, edges),
+   src/StarFormationHistories.jl:733-757: mini_spacing with Δmag 0.01, interpolation,
+   trapezoidal IMF weights times normalize_value / mean_mass, bin_cmd of the interval left
+   points (magnitudes shifted by dmod).  out is nx*ny. */
+int sfho_partial_cmd(const double *m_ini, const double *colors, const double *mags, int64_t n,
+                     const sfho_imf *imf, double dmod, double normalize_value, double mean_mass,
+                     const double *xedges, int64_t nx, const double *yedges, int64_t ny,
+                     double *out) {
+    if (n < 2) return -1;
+    int64_t cap = 1024, N;
+    double *new_mini = NULL;
+    for (;;) {
+        new_mini = (double *)realloc(new_mini, sizeof(double) * (size_t)cap);
+        N = sfho_mini_spacing(m_ini, colors, mags, n, 0.01, new_mini, cap);
+        if (N >= 0) break;
+        cap = -N;
+    }
+    double *ic = (double *)malloc(sizeof(double) * (size_t)N);
+    double *im = (double *)malloc(sizeof(double) * (size_t)N);
+    double *w = (double *)malloc(sizeof(double) * (size_t)N);
+    sfho_interpolate_mini(m_ini, colors, n, new_mini, N, ic);
+    sfho_interpolate_mini(m_ini, mags, n, new_mini, N, im);
+    for (int64_t i = 0; i + 1 < N; ++i) {
+        w[i] = (new_mini[i + 1] - new_mini[i]) *
+               (sfho_imf_pdf(imf, new_mini[i]) + sfho_imf_pdf(imf, new_mini[i + 1])) / 2.0;
+        w[i] *= normalize_value / mean_mass;
+        im[i] += dmod;
+    }
+    sfho_bin_cmd(ic, im, w, N - 1, xedges, nx, yedges, ny, out);
+    free(new_mini); free(ic); free(im); free(w);
+    return 0;
+}
+
 int sfho_binary_hess(const double *m_ini, const double *mags, int64_t n, int nf, int y_index,
                      int c1, int c2, const sfho_err_model *err, const sfho_compl_model *compl_,
                      const double *bias, const sfho_imf *imf, double normalize_value,

@@ -111,6 +111,18 @@ int64_t sfho_partial_cmd_smooth(const double *m_ini, const double *mags, int64_t
                                 double mean_mass, double xfirst, double xstep, int64_t nx,
                                 double yfirst, double ystep, int64_t ny, double *out);
 
+/* bin_cmd, src/StarFormationHistories.jl:544-553 (StatsBase left-closed histogram on the
+   stored edge values: xedges has nx + 1 increasing values, yedges ny + 1; w NULL means unit
+   weights).  out is nx*ny. */
+void sfho_bin_cmd(const double *x, const double *y, const double *w, int64_t n,
+                  const double *xedges, int64_t nx, const double *yedges, int64_t ny,
+                  double *out);
+/* partial_cmd (error-free template), src/StarFormationHistories.jl:733-757. */
+int sfho_partial_cmd(const double *m_ini, const double *colors, const double *mags, int64_t n,
+                     const sfho_imf *imf, double dmod, double normalize_value, double mean_mass,
+                     const double *xedges, int64_t nx, const double *yedges, int64_t ny,
+                     double *out);
+
 /* ---------------- binary-star templates ---------------- */
 /* mag2flux / flux2mag with zero point 0, src/utilities.jl:57, 67 */
 double sfho_mag2flux(double m);

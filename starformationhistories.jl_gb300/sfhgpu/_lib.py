@@ -28,7 +28,7 @@ EXPORTED = [
     "sfh_fg_batched_dev", "sfh_fg_kernel_times", "sfh_models_autotune", "sfh_models_set_path", "sfh_models_set_onepass_tile",
     "sfh_models_set_onepass_ctas",
     "sfh_models_path", "sfh_fg_dev_noalloc", "sfh_hmc_sample_dev",
-    "sfh_logdensity_batched_dev", "sfh_bin_cmd_smooth", "sfh_bin_cmd_smooth_batch_dev",
+    "sfh_logdensity_batched_dev", "sfh_bin_cmd", "sfh_bin_cmd_dev", "sfh_bin_cmd_smooth", "sfh_bin_cmd_smooth_batch_dev",
     "sfh_partial_cmd_smooth_batch_dev", "sfh_partial_cmd_smooth_ragged_dev",
     "sfh_binary_hess_batch_dev", "sfh_mix_binary_templates_dev",
     "sfh_galaxies_create", "sfh_galaxies_free", "sfh_galaxies_info", "sfh_fg_ragged_dev",
@@ -121,6 +121,8 @@ def load(path: str | None = None):
             "sfh_fg_dev_noalloc": ([_vp, _vp, _i64, _i64, _vp, _vp, _vp, _vp, _vp, _d], C.c_int),
             "sfh_fg_kernel_times": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, C.c_int,
                                      C.POINTER(_d)], C.c_int),
+            "sfh_bin_cmd": ([_vp, _vp, _vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp], C.c_int),
+            "sfh_bin_cmd_dev": ([_vp, _vp, _vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp], C.c_int),
             "sfh_bin_cmd_smooth": ([_vp] + [_vp] * 5 + [_i64, C.c_int, _d, _d, _i64, _d, _d, _i64,
                                                          _vp], C.c_int),
             "sfh_bin_cmd_smooth_batch_dev": ([_vp] + [_vp] * 6 + [_vp, _i64, _d, _d, _i64, _d, _d,

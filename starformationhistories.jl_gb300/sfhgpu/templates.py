@@ -11,7 +11,9 @@ closed-form error/completeness/IMF models (many templates per call).
 from __future__ import annotations
 
 import ctypes as C
+import math
 from collections import namedtuple
+from fractions import Fraction
 
 import numpy as np
 
@@ -169,27 +171,152 @@ def histogram_data(x, edges):
     return (np.asarray(x) - 1.0) * s + f
 
 
+class Range(np.ndarray):
+    """Edge vector built like a Julia float range: the element values of
+    range(start, stop, length=n) or start:step:stop, with `step` the value Julia's
+    step(r) returns.  Slices and arithmetic give plain arrays."""
+
+    def __new__(cls, values, step):
+        obj = np.asarray(values, dtype=np.float64).view(cls)
+        obj.step = float(step)
+        return obj
+
+    def __array_finalize__(self, obj):
+        self.step = None
+
+
+_MAXINT_F32 = 16777216      # maxintfloat(Float32)
+_MAXINT_F64 = 9007199254740992
+
+
+def _rat(x):
+    """Base.rat (twiceprecision.jl): the continued-fraction convergent a/b of x with
+    Float64(a) / Float64(b) == x, or the last one with |a|, |b| <= 2^24."""
+    y = x
+    a = d = 1
+    b = c = 0
+    while abs(y) <= _MAXINT_F32:
+        f = math.trunc(y)
+        y -= f
+        a, c = f * a + c, a
+        b, d = f * b + d, b
+        if max(abs(a), abs(b)) > _MAXINT_F32:
+            return c, d
+        if float(a) / float(b) == x:
+            break
+        y = math.inf if y == 0 else 1.0 / y
+    return a, b
+
+
+def _tdiv(p, q):
+    """Julia div on integers (truncates toward zero)."""
+    r = abs(p) // abs(q)
+    return r if (p >= 0) == (q >= 0) else -r
+
+
+def julia_range(start, stop, length):
+    """The elements of Julia's range(start, stop; length) for Float64 (base/twiceprecision.jl,
+    range_start_stop_length): when start and stop are ratios of small integers the elements
+    are the correctly rounded values of the exact rational interpolation (so
+    range(17.0, 27.0, length=101) holds 17.3, not 17 + 3 * 0.1), otherwise of the exact
+    interpolation of the two doubles.  Julia evaluates these in twice precision; the two
+    agree except when an exact value lies within ~1e-32 relative of a rounding boundary."""
+    start, stop, n = float(start), float(stop), int(length)
+    if n < 2:
+        raise ValueError("an edge range needs length >= 2")
+    if not (math.isfinite(start) and math.isfinite(stop)):
+        raise ValueError("range endpoints must be finite")
+    if start == stop:
+        return Range(np.full(n, start), 0.0)
+    lo, hi = Fraction(start), Fraction(stop)
+    sn, sd = _rat(start)
+    en, ed = _rat(stop)
+    if sd != 0 and ed != 0:
+        den = math.lcm(abs(sd), abs(ed))
+        if den != 0 and abs(den * start) <= _MAXINT_F64 and abs(den * stop) <= _MAXINT_F64:
+            sn, en = round(den * start), round(den * stop)
+            if sn / den == start and en / den == stop:
+                lo, hi = Fraction(sn, den), Fraction(en, den)
+    vals = [float(lo + (hi - lo) * i / (n - 1)) for i in range(n)]
+    vals[0], vals[-1] = start, stop
+    return Range(vals, float((hi - lo) / (n - 1)))
+
+
+def julia_colon(start, step, stop):
+    """The elements of Julia's start:step:stop for Float64 (base/twiceprecision.jl, the
+    IEEEFloat colon method): exact rational arithmetic when start, step and stop are ratios
+    of small integers (so -1.0:0.1:1.5 holds 0.3 exactly), else start + k * step taken
+    literally, with the length rounded as Julia rounds it."""
+    start, step, stop = float(start), float(step), float(stop)
+    if step == 0:
+        raise ValueError("range step cannot be zero")
+    pn, pd = _rat(step)
+    if pd != 0 and pn / pd == step:
+        sn, sd = _rat(start)
+        en, ed = _rat(stop)
+        if sd != 0 and ed != 0 and sn / sd == start and en / ed == stop:
+            den = math.lcm(abs(sd), abs(pd))
+            if (den != 0 and abs(start * den) <= _MAXINT_F64 and abs(step * den) <= _MAXINT_F64
+                    and den % abs(sd) == 0 and den % abs(pd) == 0):
+                sn, pn = round(start * den), round(step * den)
+                ln = max(0, _tdiv(den * en - ed * sn + pn * ed, pn * ed))
+
+                def between(a, x, b):
+                    return a <= x <= b or b <= x <= a
+                if (between(start, start + (ln - 1) * step, stop + step / 2) and
+                        not between(start, start + ln * step, stop)):
+                    vals = [float(Fraction(sn + k * pn, den)) for k in range(ln)]
+                    return Range(vals, float(Fraction(pn, den)))
+    lf = (stop - start) / step
+    if lf < 0:
+        ln = 0
+    elif lf == 0:
+        ln = 1
+    else:
+        ln = round(lf) + 1
+        stop2 = start + (ln - 1) * step
+        ln -= int(start < stop < stop2) + int(start > stop > stop2)
+    s0, st = Fraction(start), Fraction(step)
+    return Range([float(s0 + k * st) for k in range(ln)], step)
+
+
 def _range(e):
-    """(first, step, number of bins) of an evenly spaced edge vector."""
+    """(first, step, number of bins) of an evenly spaced edge vector; `step` as Julia's
+    step(r) when e is a Range."""
+    jstep = getattr(e, "step", None)
     e = np.asarray(e, dtype=np.float64)
     if e.ndim != 1 or e.size < 2:
         raise ValueError("edges must be evenly spaced vectors of length >= 2")
     step = (e[-1] - e[0]) / (e.size - 1)
     if not np.allclose(np.diff(e), step, rtol=1e-9, atol=0.0):
         raise ValueError("edges must be AbstractRange-like (evenly spaced)")
+    if jstep is not None and jstep != 0.0:
+        step = jstep
     return float(e[0]), float(step), int(e.size - 1)
 
 
+def _edge_values(e):
+    """The element values of an increasing edge vector (hard binning compares against them)."""
+    v = np.ascontiguousarray(e, dtype=np.float64)
+    if v.ndim != 1 or v.size < 2:
+        raise ValueError("edges must be vectors of length >= 2")
+    if not (np.all(np.isfinite(v)) and np.all(np.diff(v) > 0)):
+        raise ValueError("edges must be finite and increasing")
+    return v
+
+
 def calculate_edges(edges=None, xlim=None, ylim=None, nbins=None, xwidth=None, ywidth=None):
-    """calculate_edges, src/StarFormationHistories.jl:451-476."""
+    """calculate_edges, src/StarFormationHistories.jl:451-476: `edges` as given, else
+    Julia ranges range(lim[1], lim[2], length=nbins) (julia_range) over the sorted limits."""
     if edges is not None:
-        return (np.asarray(edges[0], dtype=np.float64), np.asarray(edges[1], dtype=np.float64))
+        return tuple(e if isinstance(e, Range) else np.asarray(e, dtype=np.float64)
+                     for e in edges)
     xlim, ylim = sorted(xlim), sorted(ylim)
     if nbins is None:
         if xwidth is None or ywidth is None:
             raise ValueError("If edges and nbins are not provided, xwidth and ywidth must be.")
         nbins = (int(round((xlim[1] - xlim[0]) / xwidth)), int(round((ylim[1] - ylim[0]) / ywidth)))
-    return (np.linspace(xlim[0], xlim[1], nbins[0]), np.linspace(ylim[0], ylim[1], nbins[1]))
+    return (julia_range(xlim[0], xlim[1], nbins[0]), julia_range(ylim[0], ylim[1], nbins[1]))
 
 
 # ---------------------------------------------------------------- GPU template builders
@@ -205,8 +332,9 @@ def bin_cmd_smooth(colors, mags, color_err, mag_err, cov_mult=0, weights=None, e
     w = np.ones_like(x) if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
     if not (x.shape == y.shape == sx.shape == sy.shape == w.shape):
         raise ValueError("axes(colors) == axes(mags) == axes(color_err) == axes(mag_err) == axes(weights)")
-    if xlim is None and edges is None:
-        xlim, ylim = (x.min(), x.max()), (y.min(), y.max())
+    if edges is None:
+        xlim = (x.min(), x.max()) if xlim is None else xlim
+        ylim = (y.min(), y.max()) if ylim is None else ylim
     e = calculate_edges(edges, xlim, ylim, nbins, xwidth, ywidth)
     (xf, xs, nx), (yf, ys, ny) = _range(e[0]), _range(e[1])
     ctx = ctx or default_context()
@@ -215,6 +343,63 @@ def bin_cmd_smooth(colors, mags, color_err, mag_err, cov_mult=0, weights=None, e
                                     sy.ctypes.data, w.ctypes.data, x.size, int(cov_mult), xf, xs,
                                     nx, yf, ys, ny, out.ctypes.data), ctx.handle, "bin_cmd_smooth")
     return Histogram(e, out.reshape(ny, nx).T)
+
+
+def bin_cmd(colors, mags, weights=None, edges=None, xlim=None, ylim=None, nbins=None,
+            xwidth=None, ywidth=None, ctx=None):
+    """bin_cmd, src/StarFormationHistories.jl:544-553: the hard-binned Hess diagram
+    fit(Histogram, (colors, mags), Weights(weights), edges; closed=:left) on the GPU.  Bin
+    (i, j) holds xedges[i] <= color < xedges[i+1] and yedges[j] <= mag < yedges[j+1] against
+    the edge values themselves; points on the last edge are dropped.  xlim / ylim default to
+    the extrema of colors / mags.  Returns Histogram(edges, weights (nx, ny) float64)."""
+    x = np.ascontiguousarray(colors, dtype=np.float64)
+    y = np.ascontiguousarray(mags, dtype=np.float64)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+    if not (x.ndim == y.ndim == 1 and x.shape == y.shape and (w is None or w.shape == x.shape)):
+        raise ValueError("length(colors) == length(mags) == length(weights)")
+    if edges is None:
+        xlim = (x.min(), x.max()) if xlim is None else xlim
+        ylim = (y.min(), y.max()) if ylim is None else ylim
+    e = calculate_edges(edges, xlim, ylim, nbins, xwidth, ywidth)
+    ex, ey = _edge_values(e[0]), _edge_values(e[1])
+    nx, ny = ex.size - 1, ey.size - 1
+    ctx = ctx or default_context()
+    out = np.empty(nx * ny)
+    check(load().sfh_bin_cmd(ctx.handle, x.ctypes.data, y.ctypes.data,
+                             None if w is None else w.ctypes.data, x.size, ex.ctypes.data, nx,
+                             ey.ctypes.data, ny, out.ctypes.data), ctx.handle, "bin_cmd")
+    return Histogram(e, out.reshape(ny, nx).T)
+
+
+def partial_cmd_points(m_ini, colors, mags, imf, dmod=0.0, normalize_value=1.0,
+                       mean_mass=None):
+    """The weighted points partial_cmd bins (src/StarFormationHistories.jl:733-757): the
+    isochrone resampled by mini_spacing (Δmag 0.01), interpolated, magnitudes shifted by dmod,
+    trapezoidal IMF weights times normalize_value / mean_mass, the last point dropped."""
+    if mean_mass is None:
+        mean_mass = imf.mean()
+    new_mini, spacing = mini_spacing(m_ini, colors, mags, 0.01, True)
+    c = interpolate_mini(m_ini, colors, new_mini)
+    m = interpolate_mini(m_ini, mags, new_mini) + dmod
+    p = np.asarray(imf(new_mini), dtype=np.float64)
+    w = spacing * (p[:-1] + p[1:]) / 2.0
+    w = w * (normalize_value / mean_mass)
+    return c[:-1], m[:-1], w
+
+
+def partial_cmd(m_ini, colors, mags, imf, dmod=0.0, normalize_value=1.0, mean_mass=None,
+                edges=None, xlim=None, ylim=None, nbins=None, xwidth=None, ywidth=None, ctx=None):
+    """partial_cmd, src/StarFormationHistories.jl:733-757: the error-free Hess diagram of an
+    isochrone (no photometric smoothing), binned on the GPU.  As in the reference, xlim and
+    ylim default to the extrema of the given colors and (unshifted) mags."""
+    colors = np.asarray(colors, dtype=np.float64)
+    mags = np.asarray(mags, dtype=np.float64)
+    if edges is None:
+        xlim = (colors.min(), colors.max()) if xlim is None else xlim
+        ylim = (mags.min(), mags.max()) if ylim is None else ylim
+    x, y, w = partial_cmd_points(m_ini, colors, mags, imf, dmod, normalize_value, mean_mass)
+    return bin_cmd(x, y, weights=w, edges=edges, xlim=xlim, ylim=ylim, nbins=nbins,
+                   xwidth=xwidth, ywidth=ywidth, ctx=ctx)
 
 
 def partial_cmd_smooth_stars(m_ini, mags, mag_err_funcs, y_index, color_indices, imf,
