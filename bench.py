@@ -380,6 +380,41 @@ def run_emulator(ctx, w, n_train=100_000, n_val=4096, steps=4000, cells=(8, 2, 1
     }
 
 
+def run_fit(H, data, g_abstol=1e-3):
+    """fit_templates_fast / fit_templates on the headline templates: the device BFGS driver
+    (host arrays in, coefficients out) against scipy's BFGS looping over the host-array
+    fg! (the shape of the reference's Optim loop), both from x0 = ones, renormalised."""
+    import numpy as np
+
+    import sfhgpu
+    x0 = np.ones(H.nt)
+    sfhgpu.fit_templates_fast(H, data, x0=x0, g_abstol=g_abstol, maxiter=3)  # warm
+    t0 = time.perf_counter()
+    xd, rd = sfhgpu.fit_templates_fast(H, data, x0=x0, g_abstol=g_abstol, maxiter=3000)
+    td = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    res = sfhgpu.fit_templates(H, data, x0=x0, gtol=g_abstol, maxiter=3000)
+    tm = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    xs, rs = sfhgpu.fit_templates_fast(H, data, x0=x0, g_abstol=g_abstol, maxiter=3000,
+                                       method="scipy")
+    ts = time.perf_counter() - t0
+    big = xs > 1e-3 * xs.max()
+    return {
+        "g_abstol": g_abstol, "x0": "ones, renormalised (renormalize_x0)",
+        "device": {"seconds": td, "nfev": rd.nfev, "nit": rd.nit, "status": rd.message,
+                   "ms_per_eval": td / rd.nfev * 1e3, "f": rd.fun, "graph": rd.graph},
+        "scipy_host_loop": {"seconds": ts, "nfev": int(rs.nfev), "nit": int(rs.nit),
+                            "f": float(rs.fun), "ms_per_eval": ts / rs.nfev * 1e3},
+        "speedup_vs_scipy_host_loop": ts / td,
+        "f_device_minus_scipy": float(rd.fun - rs.fun),
+        "coeff_rel_diff_max": float(np.max(np.abs(xd[big] / xs[big] - 1.0))),
+        "fit_templates_map_mle": {"seconds": tm,
+                                  "nfev": res.map.result.nfev + res.mle.result.nfev,
+                                  "status": [res.map.result.message, res.mle.result.message]},
+    }
+
+
 def oracle_checks(batched, ragged, M64, r, data, neglogl):
     """Accuracy against the FP64 oracle on the same stored templates (CPU leg): the plain
     fg!'s -logL, and the stashed outputs of the batched and ragged legs (the stash is
@@ -674,6 +709,11 @@ def run_ours(args):
     e2e = {"value": world * ne2e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": (NTW + NBINS) * 8,
            "d2h_bytes_per_step": (NBINS + NTW + 1) * 8, "steps": ne2e}
 
+    # ---- whole fits on the same templates (device BFGS driver vs a host scipy loop)
+    fit = None
+    if not args.no_fit:
+        fit = run_fit(H, data)
+
     # ---- batched form (tensor cores): 4,096 vectors per call on the same templates
     batched = None
     if not args.no_batched:
@@ -749,7 +789,7 @@ def run_ours(args):
             "template_bin_updates_per_build": bin_updates,
             "negLogL": neglogl, "precision": plain_check, "gpu_launches": launches,
             "roofline": roofline,
-            "batched": batched, "hmc": hmc, "ragged": ragged, "emulator": emulator,
+            "batched": batched, "hmc": hmc, "ragged": ragged, "emulator": emulator, "fit": fit,
             "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
         }
         print(json.dumps(line), flush=True)
@@ -774,6 +814,7 @@ def main():
                     help="single-vector fg! path: the autotuner's choice (auto) or a fixed one "
                          "(for profiling runs, where profiler overhead can change the choice)")
     ap.add_argument("--no-emulator", action="store_true", help="skip the emulator leg")
+    ap.add_argument("--no-fit", action="store_true", help="skip the whole-fit leg")
     ap.add_argument("--ntempl", type=int, default=NT,
                     help="templates (multiple of 30); fewer than 1200 only for profiling")
     ap.add_argument("--cpu-budget-s", type=float, default=10.0)

@@ -118,6 +118,53 @@ int sfh_fg_dev(sfh_ctx *ctx, const sfh_models *models, const double *d_coeffs,
                const double *d_data, double *d_composite, double *d_G, double *d_negLogL,
                double eps);
 
+/* ---------------------------------------------------------------- device fit driver */
+/* BFGS over fg! on the device, for fit_templates (src/fitting/solvers.jl:172-221: log
+   transform, MAP with the Jacobian term -Σθ, then MLE) and fit_templates_fast (:238-275:
+   coeffs = θ²).  As Optim.BFGS there: inverse-Hessian BFGS from H0 = I, the update skipped
+   when sᵀy <= 0, first trial step min(1, |d|) / |d| (InitialStatic(1.0, scaled=true)),
+   stops on |g|∞ <= g_abstol, |Δf| <= f_reltol |f|, |Δθ|∞ <= x_abstol or max_iter
+   accepted steps.  The line search backtracks (Optim: HagerZhang), so iterates differ
+   while the optimum does not.  The loop runs on the GPU (CUDA-graph replays of
+   evaluation slots); the host reads a small state once per replay. */
+enum sfh_fit_transform { SFH_FIT_LOG_MAP = 0, SFH_FIT_LOG_MLE = 1, SFH_FIT_SQRT = 2 };
+enum sfh_fit_status {
+    SFH_FIT_CONVERGED_G = 0, /* |g|∞ <= g_abstol */
+    SFH_FIT_CONVERGED_F = 1, /* |Δf| <= f_reltol |f| */
+    SFH_FIT_CONVERGED_X = 2, /* |Δθ|∞ <= x_abstol */
+    SFH_FIT_MAXITER = 3,     /* max_iter accepted steps */
+    SFH_FIT_LINESEARCH = 4,  /* no decrease along d after 40 backtracks (noise floor) */
+    SFH_FIT_NONFINITE = 5,   /* f or g not finite at an accepted point */
+    SFH_FIT_MAXEVALS = 6     /* max_evals fg! evaluations */
+};
+typedef struct sfh_fit_options {
+    int transform;    /* sfh_fit_transform */
+    int max_iter;     /* accepted steps (Optim's iterations; its default is 1000) */
+    int max_evals;    /* fg! evaluations, 0 = 50 (max_iter + 1) */
+    int graph_slots;  /* evaluations per graph replay, 0 = 8 (at most 64) */
+    double g_abstol;  /* Optim default 1e-8 */
+    double f_reltol;  /* Optim default 0 (stops only on an unchanged f) */
+    double x_abstol;  /* Optim default 0 */
+    double eps;       /* composite floor of fg!, 0 = eps(Float64) */
+} sfh_fit_options;
+typedef struct sfh_fit_result {
+    double f;            /* objective at theta_out (fg! value, minus Σθ for LOG_MAP) */
+    double g_norm;       /* |g|∞ there */
+    int64_t iterations;  /* accepted steps */
+    int64_t evaluations; /* fg! evaluations */
+    int status;          /* sfh_fit_status */
+    int graph;           /* 1 when the slots ran as CUDA-graph replays */
+} sfh_fit_result;
+/* Device buffers: d_data (nbins), d_theta0 (nt, transformed start) -> d_theta_out (nt),
+   d_invH (nt x nt, the final BFGS inverse Hessian in θ, or NULL).  Synchronous. */
+int sfh_fit_bfgs_dev(sfh_ctx *ctx, sfh_models *models, const double *d_data,
+                     const double *d_theta0, const sfh_fit_options *opt, double *d_theta_out,
+                     double *d_invH, sfh_fit_result *res);
+/* sfh_fit_bfgs_dev on host arrays. */
+int sfh_fit_bfgs(sfh_ctx *ctx, sfh_models *models, const double *data, const double *theta0,
+                 const sfh_fit_options *opt, double *theta_out, double *invH,
+                 sfh_fit_result *res);
+
 /* Telemetry: average device time (ms) of each of the four kernels of sfh_fg_dev over
    `iters` evaluations, timed with CUDA events on the context stream:
    ms_out[0] m = M r partials, [1] Poisson terms + w, [2] Mᵀ w partials, [3] G reduction.

@@ -84,6 +84,7 @@ struct OnePassArgs {
     int want_logl;
     double gsign;
     double *G, *negLogL;  // results (either may be NULL)
+    const int *skip;      // device flag: nonzero makes every CTA return at once (may be NULL)
 };
 
 // Dynamic shared memory: ring | r (hi, lo) | s_part | s_w | s_cn | s_tab | full | empty |
@@ -105,6 +106,9 @@ template <int BINS, int OWN>
 __global__ void __launch_bounds__(Geo<BINS, OWN>::kThreads, Geo<BINS, OWN>::kMinBlocks)
 k_fg_onepass(const OnePassArgs a) {
     using GE = Geo<BINS, OWN>;
+    // a finished device-side driver turns the evaluations still queued into no-ops; every
+    // CTA reads the same flag, so none waits at the grid barrier
+    if (a.skip && *a.skip) return;
     constexpr int LPR = GE::LPR, RPL = GE::RPL, GU = GE::GU, LB = GE::LB;
     constexpr int kOwners = GE::kOwners, kWarps = GE::kWarps, kFinishers = GE::kFinishers;
     constexpr int kUnits = GE::kUnits, kPoissonWarp = GE::kPoissonWarp;
@@ -491,7 +495,7 @@ size_t sfh_onepass_scratch(const sfh_ctx *ctx, const sfh_models *m) {  // up to 
 int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
                           const double *d_data, double *d_composite, double *d_G,
                           double *d_negLogL, double eps, double gsign, void *scratch,
-                          cudaEvent_t *ev) {
+                          cudaEvent_t *ev, const int *d_skip) {
     const int64_t nbins = m->nbins, nt = m->nt;
     const int nch = (int)((nt + kBoxCols - 1) / kBoxCols);
     // the handle's variant (tile width, CTAs per SM), else 16 bins on one CTA per SM, which
@@ -539,6 +543,7 @@ int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
     a.gsign = gsign;
     a.G = d_G;
     a.negLogL = d_negLogL;
+    a.skip = d_skip;
     cudaStream_t st = ctx->stream;
     if (ev) SFH_CK(ctx, cudaEventRecord(ev[0], st));
     int rc = per_sm == 2 ? launch_onepass<16, 6>(ctx, a, grid, st)

@@ -205,6 +205,7 @@ struct FgArgs {
     double eps;
     double gsign;           // +1: gradient of -logL (fg!), -1: ∇loglikelihood!
     int mode;               // see FG_MODE_*
+    const int *skip;        // device flag that turns the one-pass kernel into a no-op (or NULL)
 };
 enum {
     FG_MODE_FG = 0,          // composite from coeffs, then logL/G as requested
@@ -218,7 +219,7 @@ size_t sfh_onepass_scratch(const sfh_ctx *ctx, const sfh_models *m);
 int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
                           const double *d_data, double *d_composite, double *d_G,
                           double *d_negLogL, double eps, double gsign, void *scratch,
-                          cudaEvent_t *ev);
+                          cudaEvent_t *ev, const int *d_skip = nullptr);
 // Reads and clears the one-pass timeout slot (synchronises the stream).
 int sfh_check_onepass(sfh_ctx *ctx);
 int sfh_launch_loglikelihood(sfh_ctx *ctx, const double *composite, const double *data,

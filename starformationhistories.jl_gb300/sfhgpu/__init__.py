@@ -10,6 +10,7 @@ from .emulator import SyntheticGenerator, TemplateEmulator
 from .fitting import (Galaxies, composite_, construct_x0, construct_x0_mdf, fg_, fg_batched,
                       fg_ragged, fit_templates, fixed_amr, truncate_relweights,
                       fit_templates_fast, fit_templates_lbfgsb, grad_loglikelihood,
+                      fit_bfgs_device, FIT_LOG_MAP, FIT_LOG_MLE, FIT_SQRT,
                       grad_loglikelihood_, loglikelihood, renormalize_x0, stack_models)
 from .sampling import (GaussianDispersion, LinearAMR, LogarithmicAMR, MH_from_Z, PowerLawMZR,
                        calculate_coeffs, dMH_dZ, hmc_sample, logdensity_batched, sample_sfh)
@@ -24,7 +25,8 @@ from .templates import (BrokenPowerLawIMF, Histogram, Kroupa2001, Martin2016_com
 __all__ = [
     "SFH_BF16X2", "SFH_F32", "SFH_F64", "EXPORTED", "LIB_PATH", "SFHArgumentError", "SFHError",
     "load", "Context", "Models", "as_models", "default_context", "composite_", "construct_x0",
-    "fg_", "fg_batched", "fit_templates", "fit_templates_fast", "fit_templates_lbfgsb", "grad_loglikelihood",
+    "fg_", "fg_batched", "fit_templates", "fit_templates_fast", "fit_templates_lbfgsb", "fit_bfgs_device", "FIT_LOG_MAP",
+    "FIT_LOG_MLE", "FIT_SQRT", "grad_loglikelihood",
     "grad_loglikelihood_", "loglikelihood", "renormalize_x0", "stack_models", "BrokenPowerLawIMF",
     "Histogram", "Kroupa2001", "Martin2016_complete", "bin_cmd", "bin_cmd_smooth", "calculate_edges",
     "partial_cmd", "partial_cmd_points", "julia_range", "julia_colon", "Range",

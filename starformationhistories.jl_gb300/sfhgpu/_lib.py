@@ -28,7 +28,7 @@ EXPORTED = [
     "sfh_fg_batched_dev", "sfh_fg_kernel_times", "sfh_models_autotune", "sfh_models_set_path", "sfh_models_set_onepass_tile",
     "sfh_models_set_onepass_ctas",
     "sfh_models_path", "sfh_fg_dev_noalloc", "sfh_hmc_sample_dev",
-    "sfh_logdensity_batched_dev", "sfh_bin_cmd", "sfh_bin_cmd_dev", "sfh_bin_cmd_smooth", "sfh_bin_cmd_smooth_batch_dev",
+    "sfh_logdensity_batched_dev", "sfh_fit_bfgs", "sfh_fit_bfgs_dev", "sfh_bin_cmd", "sfh_bin_cmd_dev", "sfh_bin_cmd_smooth", "sfh_bin_cmd_smooth_batch_dev",
     "sfh_partial_cmd_smooth_batch_dev", "sfh_partial_cmd_smooth_ragged_dev",
     "sfh_binary_hess_batch_dev", "sfh_mix_binary_templates_dev",
     "sfh_galaxies_create", "sfh_galaxies_free", "sfh_galaxies_info", "sfh_fg_ragged_dev",
@@ -43,6 +43,19 @@ class ErrModel(C.Structure):
     """exp_photerr(m, a, b, c, d) capped at ``cap`` (src/utilities.jl:218)."""
     _fields_ = [("a", C.c_double), ("b", C.c_double), ("c", C.c_double), ("d", C.c_double),
                 ("cap", C.c_double)]
+
+
+class FitOptions(C.Structure):
+    """sfh_fit_options (device BFGS driver)."""
+    _fields_ = [("transform", C.c_int), ("max_iter", C.c_int), ("max_evals", C.c_int),
+                ("graph_slots", C.c_int), ("g_abstol", C.c_double), ("f_reltol", C.c_double),
+                ("x_abstol", C.c_double), ("eps", C.c_double)]
+
+
+class FitResult(C.Structure):
+    """sfh_fit_result (device BFGS driver)."""
+    _fields_ = [("f", C.c_double), ("g_norm", C.c_double), ("iterations", C.c_int64),
+                ("evaluations", C.c_int64), ("status", C.c_int), ("graph", C.c_int)]
 
 
 class ComplModel(C.Structure):
@@ -121,6 +134,10 @@ def load(path: str | None = None):
             "sfh_fg_dev_noalloc": ([_vp, _vp, _i64, _i64, _vp, _vp, _vp, _vp, _vp, _d], C.c_int),
             "sfh_fg_kernel_times": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, C.c_int,
                                      C.POINTER(_d)], C.c_int),
+            "sfh_fit_bfgs": ([_vp, _vp, _vp, _vp, C.POINTER(FitOptions), _vp, _vp,
+                              C.POINTER(FitResult)], C.c_int),
+            "sfh_fit_bfgs_dev": ([_vp, _vp, _vp, _vp, C.POINTER(FitOptions), _vp, _vp,
+                                  C.POINTER(FitResult)], C.c_int),
             "sfh_bin_cmd": ([_vp, _vp, _vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp], C.c_int),
             "sfh_bin_cmd_dev": ([_vp, _vp, _vp, _vp, _i64, _vp, _i64, _vp, _i64, _vp], C.c_int),
             "sfh_bin_cmd_smooth": ([_vp] + [_vp] * 5 + [_i64, C.c_int, _d, _d, _i64, _d, _d, _i64,

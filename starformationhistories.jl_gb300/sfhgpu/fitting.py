@@ -13,7 +13,7 @@ from collections import namedtuple
 
 import numpy as np
 
-from ._lib import SFH_F32, SFH_F64, check, load
+from ._lib import SFH_F32, SFH_F64, FitOptions, FitResult, check, load
 from .core import Models, as_models, default_context
 
 _dp = None
@@ -218,14 +218,53 @@ def fit_templates_lbfgsb(models, data, x0=None, factr=1e-12, pgtol=1e-5, maxiter
     return fval, x
 
 
-def fit_templates_fast(models, data, x0=None, g_abstol=1e-8, maxiter=10000):
+FIT_LOG_MAP, FIT_LOG_MLE, FIT_SQRT = 0, 1, 2
+FIT_STATUS = ("converged (g)", "converged (f)", "converged (x)", "maximum iterations",
+              "line search made no progress", "non-finite objective", "maximum evaluations")
+BFGSResult = namedtuple("BFGSResult", ["x", "fun", "hess_inv", "nit", "nfev", "status",
+                                       "message", "success", "g_norm", "graph"])
+
+
+def fit_bfgs_device(models, data, theta0, transform, g_abstol=1e-8, f_reltol=0.0,
+                    x_abstol=0.0, maxiter=1000, max_evals=0, want_invH=True, graph_slots=0):
+    """BFGS over fg! run on the GPU (sfh_fit_bfgs): the minimisation Optim.BFGS performs in
+    fit_templates / fit_templates_fast (src/fitting/solvers.jl:172-275) for the transform
+    FIT_LOG_MAP (r = exp θ, Jacobian term -Σθ), FIT_LOG_MLE (r = exp θ) or FIT_SQRT
+    (r = θ²).  Returns a BFGSResult (x = θ at the minimum, hess_inv = the BFGS inverse
+    Hessian in θ when want_invH)."""
+    M = as_models(models)
+    d = np.ascontiguousarray(np.asarray(data, dtype=np.float64).reshape(-1, order="F"))
+    th = np.ascontiguousarray(theta0, dtype=np.float64)
+    _argcheck(d.size == M.nbins, "length(data) == size(models, 1)")
+    _argcheck(th.size == M.nt, "length(x0) == size(models, 2)")
+    opt = FitOptions(int(transform), int(maxiter), int(max_evals), int(graph_slots),
+                     float(g_abstol), float(f_reltol), float(x_abstol), 0.0)
+    res = FitResult()
+    out = np.empty(M.nt)
+    invH = np.empty((M.nt, M.nt)) if want_invH else None
+    ctx = M.ctx
+    check(load().sfh_fit_bfgs(ctx.handle, M.handle, d.ctypes.data, th.ctypes.data, C.byref(opt),
+                              out.ctypes.data, invH.ctypes.data if want_invH else None,
+                              C.byref(res)), ctx.handle, "fit_bfgs")
+    return BFGSResult(out, res.f, invH, int(res.iterations), int(res.evaluations),
+                      int(res.status), FIT_STATUS[res.status], res.status <= 2, res.g_norm,
+                      bool(res.graph))
+
+
+def fit_templates_fast(models, data, x0=None, g_abstol=1e-8, maxiter=1000, method="device"):
     """fit_templates_fast, src/fitting/solvers.jl:238-275: BFGS in sqrt space
-    (coeffs = θ²).  Returns (coeffs, result)."""
-    from scipy.optimize import minimize
+    (coeffs = θ²), on the GPU (method "device") or by scipy's BFGS over fg! ("scipy").
+    Returns (coeffs, result)."""
     M = as_models(models)
     data = np.asarray(data, dtype=np.float64).reshape(-1, order="F")
     x0 = np.ones(M.nt) if x0 is None else np.asarray(x0, dtype=np.float64)
     x0 = np.sqrt(renormalize_x0(data, M, x0))
+    if method == "device":
+        r = fit_bfgs_device(M, data, x0, FIT_SQRT, g_abstol=g_abstol, maxiter=maxiter,
+                            want_invH=False)
+        return r.x ** 2, r
+    _argcheck(method == "scipy", "method is 'device' or 'scipy'")
+    from scipy.optimize import minimize
     comp = np.empty(M.nbins)
     G = np.empty(M.nt)
 
@@ -242,15 +281,26 @@ LogTransformFTResult = namedtuple("LogTransformFTResult", ["mu", "sigma", "invH"
 FitTemplatesResult = namedtuple("FitTemplatesResult", ["map", "mle"])
 
 
-def fit_templates(models, data, x0=None, gtol=1e-8, maxiter=10000):
+def fit_templates(models, data, x0=None, gtol=1e-8, maxiter=1000, method="device"):
     """fit_templates, src/fitting/solvers.jl:172-221: MAP (log transform with the
-    Jacobian term -Σθ) then MLE from the MAP point, both by BFGS; μ, σ from the
-    BFGS inverse Hessian in log space."""
-    from scipy.optimize import minimize
+    Jacobian term -Σθ) then MLE from the MAP point, both by BFGS (on the GPU with method
+    "device", scipy's BFGS over fg! with "scipy"); μ, σ from the BFGS inverse Hessian in
+    log space."""
     M = as_models(models)
     data = np.asarray(data, dtype=np.float64).reshape(-1, order="F")
     x0 = np.ones(M.nt) if x0 is None else np.asarray(x0, dtype=np.float64)
     x0 = np.log(renormalize_x0(data, M, x0))
+    if method == "device":
+        r_map = fit_bfgs_device(M, data, x0, FIT_LOG_MAP, g_abstol=gtol, maxiter=maxiter)
+        r_mle = fit_bfgs_device(M, data, r_map.x, FIT_LOG_MLE, g_abstol=gtol, maxiter=maxiter)
+
+        def pack_dev(r):
+            mu = np.exp(r.x)
+            return LogTransformFTResult(mu, np.sqrt(np.abs(np.diag(r.hess_inv))) * mu,
+                                        r.hess_inv, r)
+        return FitTemplatesResult(pack_dev(r_map), pack_dev(r_mle))
+    _argcheck(method == "scipy", "method is 'device' or 'scipy'")
+    from scipy.optimize import minimize
     comp = np.empty(M.nbins)
     G = np.empty(M.nt)
 
