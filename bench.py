@@ -626,6 +626,14 @@ def run_ours(args):
     tuned = H.autotune(r, data, iters=10)
     if args.fg_path != "auto":
         H.set_path(args.fg_path)
+    if args.onepass_variant:
+        # pins the one-pass variant (profiling runs, where timings under the profiler would
+        # steer the autotuner): bins,ctas_per_sm,schedule,boxes_per_copy
+        b, c, sch, rb = args.onepass_variant.split(",")
+        H.set_onepass_tile(int(b))
+        H.set_onepass_ctas(int(c))
+        H.set_onepass_schedule(sch)
+        H.set_onepass_run(int(rb))
 
     def step():
         rc = L.sfh_fg_dev(ctx.handle, H.handle, d_r.data_ptr(), d_n.data_ptr(), d_c.data_ptr(),
@@ -690,6 +698,7 @@ def run_ours(args):
                 "kernel_ms": {n: kms[i] for i, n in enumerate(names)},
                 "fg_total_gbs": alg_eval / (ms / args.steps * 1e-3) / 1e9,
                 "autotuned_plan": {"path": path, "onepass_ms": H.onepass_ms,
+                                   "onepass_variant": list(H.onepass_variant),
                                    "pass1_template_splits": tuned["plan"][0], "pass2_rows": tuned["plan"][1],
                                    "pass2_waves": tuned["plan"][2], "twopass_ms": tuned["ms"]}}
 
@@ -815,6 +824,9 @@ def main():
                          "(for profiling runs, where profiler overhead can change the choice)")
     ap.add_argument("--no-emulator", action="store_true", help="skip the emulator leg")
     ap.add_argument("--no-fit", action="store_true", help="skip the whole-fit leg")
+    ap.add_argument("--onepass-variant", default="",
+                    help="pin the one-pass variant after autotuning: bins,ctas,schedule,boxes "
+                         "(e.g. 32,1,phased,2)")
     ap.add_argument("--ntempl", type=int, default=NT,
                     help="templates (multiple of 30); fewer than 1200 only for profiling")
     ap.add_argument("--cpu-budget-s", type=float, default=10.0)

@@ -196,6 +196,19 @@ int sfh_models_set_onepass_tile(sfh_ctx *ctx, sfh_models *models, int bins);
    latencies overlap).  Default 1; the autotuner measures both; shapes that do not fit
    two CTAs per SM take one. */
 int sfh_models_set_onepass_ctas(sfh_ctx *ctx, sfh_models *models, int ctas_per_sm);
+/* Schedule of the one-pass kernel: 0 phased (per tile: phase A, finish, phase B), 1 skewed
+   (phase B of a tile and phase A of the next in one barrier interval; 16-bin tiles, one CTA
+   per SM, shapes whose ring holds two tiles, else phased).  Default 0; the autotuner
+   measures both. */
+int sfh_models_set_onepass_schedule(sfh_ctx *ctx, sfh_models *models, int skewed);
+/* Boxes (64 templates x the tile's bins each) per bulk copy of the one-pass kernel: 1, 2 or
+   4, or 0 for the default (4 for 16-bin tiles, 2 for 32-bin); fewer where the ring does not
+   hold the runs. */
+int sfh_models_set_onepass_run(sfh_ctx *ctx, sfh_models *models, int boxes);
+/* The one-pass variant later calls launch: tile bins, CTAs per SM, skewed (0/1), boxes per
+   bulk copy (SFH_ERR_UNSUPPORTED for a handle the one-pass kernel cannot take). */
+int sfh_models_onepass_variant(sfh_ctx *ctx, const sfh_models *models, int *bins,
+                               int *ctas_per_sm, int *skewed, int *run_boxes);
 /* The path fg! calls with G take on this handle now (ONEPASS or TWOPASS), and the
    one-pass time measured by sfh_models_autotune (0 if not measured); either may be NULL. */
 int sfh_models_path(sfh_ctx *ctx, const sfh_models *models, int *path_out, double *onepass_ms);

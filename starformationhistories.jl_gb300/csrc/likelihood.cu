@@ -991,16 +991,24 @@ extern "C" int sfh_models_autotune(sfh_ctx *ctx, sfh_models *m, const double *d_
     if (rc == SFH_OK && sfh_onepass_eligible(ctx, m)) {  // one-pass tile widths against the best plan
         m->path = SFH_PATH_ONEPASS;
         double best_op = 1e300;
-        int best_bins = 16, best_ctas = 1;
-        const int variants[3][2] = {{16, 1}, {32, 1}, {16, 2}};  // tile width, CTAs per SM
+        int best_bins = 16, best_ctas = 1, best_skew = 0;
+        // tile width, CTAs per SM, skewed schedule
+        const int variants[4][3] = {{16, 1, 0}, {32, 1, 0}, {16, 2, 0}, {16, 1, 1}};
         for (const auto &v : variants) {
             m->onepass_bins = v[0];
             m->onepass_ctas = v[1];
+            m->onepass_skew = v[2];
             if ((rc = timed(t1, t2)) != SFH_OK) break;
-            if (t1 + t2 < best_op) { best_op = t1 + t2; best_bins = v[0]; best_ctas = v[1]; }
+            if (t1 + t2 < best_op) {
+                best_op = t1 + t2;
+                best_bins = v[0];
+                best_ctas = v[1];
+                best_skew = v[2];
+            }
         }
         m->onepass_bins = best_bins;
         m->onepass_ctas = best_ctas;
+        m->onepass_skew = best_skew;
         if (rc == SFH_OK) {
             m->onepass_ms = best_op;
             if (best_op >= b1 + b2) m->path = SFH_PATH_TWOPASS;
@@ -1011,7 +1019,8 @@ extern "C" int sfh_models_autotune(sfh_ctx *ctx, sfh_models *m, const double *d_
     if (rc) {
         m->tune_ks = m->tune_R = m->tune_w2 = 0;
         m->path = SFH_PATH_AUTO;
-        m->onepass_bins = m->onepass_ctas = 0;
+        m->onepass_bins = m->onepass_ctas = m->onepass_skew = 0;
+        m->onepass_lp = -1;
         return rc;
     }
     if (plan_out) {
@@ -1196,6 +1205,31 @@ extern "C" int sfh_models_set_onepass_tile(sfh_ctx *ctx, sfh_models *m, int bins
 extern "C" int sfh_models_set_onepass_ctas(sfh_ctx *ctx, sfh_models *m, int ctas_per_sm) {
     if (!ctx || !m || (ctas_per_sm != 1 && ctas_per_sm != 2)) return SFH_ERR_ARG;
     m->onepass_ctas = ctas_per_sm;
+    return SFH_OK;
+}
+
+extern "C" int sfh_models_set_onepass_schedule(sfh_ctx *ctx, sfh_models *m, int skewed) {
+    if (!ctx || !m || (skewed != 0 && skewed != 1)) return SFH_ERR_ARG;
+    m->onepass_skew = skewed;
+    return SFH_OK;
+}
+
+extern "C" int sfh_models_set_onepass_run(sfh_ctx *ctx, sfh_models *m, int boxes) {
+    if (!ctx || !m || (boxes != 0 && boxes != 1 && boxes != 2 && boxes != 4)) return SFH_ERR_ARG;
+    m->onepass_lp = boxes == 0 ? -1 : boxes == 1 ? 0 : boxes == 2 ? 1 : 2;
+    return SFH_OK;
+}
+
+extern "C" int sfh_models_onepass_variant(sfh_ctx *ctx, const sfh_models *m, int *bins,
+                                          int *ctas_per_sm, int *skewed, int *run_boxes) {
+    if (!ctx || !m || !bins || !ctas_per_sm || !skewed || !run_boxes) return SFH_ERR_ARG;
+    if (!sfh_onepass_eligible(ctx, m)) return sfh_set_error(ctx, SFH_ERR_UNSUPPORTED, "not one-pass eligible");
+    OnePassChoice c{};
+    sfh_onepass_choose(ctx, m, &c);
+    *bins = c.bins;
+    *ctas_per_sm = c.per_sm;
+    *skewed = c.skew;
+    *run_boxes = 1 << c.lp;
     return SFH_OK;
 }
 

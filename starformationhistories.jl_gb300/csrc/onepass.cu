@@ -7,10 +7,11 @@
 // a tile of BINS bins (16 or 32) x all templates (nt <= 1536) in shared memory:
 //
 //   one persistent CTA per SM, 16 warps;
-//   warp 15, 4 lanes    producers: boxes of BINS bins x 64 templates (1-D bulk copies of a
-//                       blocked copy of the matrix, one contiguous block per tile and box)
-//                       into a ring of shared-memory slots with full / empty mbarriers; lane p
-//                       issues every fourth box, so four copies are issued concurrently;
+//   warp 15, 4 lanes    producers: boxes of BINS bins x 64 templates (a blocked copy of the
+//                       matrix, the boxes of a tile contiguous), moved as runs of up to 1, 2
+//                       or 4 consecutive boxes per 1-D bulk copy into a ring of shared-memory
+//                       run-slots with full / empty mbarriers; lane p issues every fourth
+//                       run, so four copies are in issue concurrently;
 //   warps 0-13          owners: half-box unit u (32 template rows of box u / 2) belongs to
 //                       owner u % 14 (one 16-byte shared load per lane: 4 bins of a row);
 //   warp 14             the Poisson terms.
@@ -73,6 +74,7 @@ struct OnePassArgs {
     const float *blk;  // blocked copy of the templates: box (t, c) at (t * nch + c) * box floats
     int64_t nbins, nt;
     int ntiles, nch, slots;
+    int runs, lp;      // run-slots of the ring (slots = runs << lp), log2 boxes per run
     const double *r, *data;
     double *composite;
     double *gpart;  // [gridDim.x][nt]
@@ -102,7 +104,7 @@ __device__ __forceinline__ bool op_wait(uint64_t *bar, uint32_t parity, volatile
     return mbar_wait_sleep(bar, parity, abort_flag, err, code);
 }
 
-template <int BINS, int OWN>
+template <int BINS, int OWN, bool SKEW>
 __global__ void __launch_bounds__(Geo<BINS, OWN>::kThreads, Geo<BINS, OWN>::kMinBlocks)
 k_fg_onepass(const OnePassArgs a) {
     using GE = Geo<BINS, OWN>;
@@ -116,7 +118,9 @@ k_fg_onepass(const OnePassArgs a) {
     // 128-byte aligned copy destination; derived from the shared array by pointer arithmetic
     // so that every access below stays a shared-memory access
     unsigned char *base = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
-    const int slots = a.slots, nch = a.nch;
+    const int slots = a.slots, nch = a.nch, runs = a.runs, lp = a.lp, P = 1 << lp;
+    const int nr = (nch + P - 1) >> lp;             // runs (bulk copies) per tile
+    const int short_extra = 2 * ((nr << lp) - nch);  // releases the tile's last run lacks
     float *ring = (float *)base;
     float2 *rr = (float2 *)(ring + (size_t)slots * GE::kBoxFloats);  // r split (hi, lo)
     sfh_df *s_part = (sfh_df *)(rr + nch * kBoxCols);                // [kOwners][BINS]
@@ -124,54 +128,80 @@ k_fg_onepass(const OnePassArgs a) {
     float4 *s_cn = (float4 *)(s_w + BINS);                           // [BINS] (m hi, lo, n hi, lo)
     sfh_df *s_tab = (sfh_df *)(s_cn + BINS);                         // log / n log n tables
     uint64_t *full = (uint64_t *)(s_tab + SFH_DF_TAB_ALL);
-    uint64_t *empty = full + slots;
-    volatile int *s_abort = (volatile int *)(empty + slots);
+    uint64_t *empty = full + runs;
+    volatile int *s_abort = (volatile int *)(empty + runs);
     volatile int *s_stop = s_abort + 1;
     int *err = (int *)a.err;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int k = threadIdx.x; k < nch * kBoxCols; k += blockDim.x) {
-        const double v = k < a.nt ? a.r[k] : 0.0;
-        const float h = __double2float_rn(v);
-        rr[k] = make_float2(h, __double2float_rn(v - (double)h));
-    }
-    if (a.want_logl)
-        for (int k = threadIdx.x; k < SFH_DF_TAB_ALL; k += blockDim.x) s_tab[k] = a.tab[k];
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < slots; ++s) {
+    if (warp == kWarps) {  // the producer warp initialises the ring's barriers
+        for (int s = lane; s < runs; s += 32) {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], 2);  // the owners of the box's two halves release it
+            mbar_init(&empty[s], 2 * P);  // the owners of the run's box halves release it
         }
-        *s_abort = 0;
-        *s_stop = 0;
+        if (lane == 0) {
+            *s_abort = 0;
+            *s_stop = 0;
+        }
         fence_barrier_init();
     }
     __syncthreads();
+    // the first copies are issued now; the consumers stage r and the tables meanwhile and
+    // meet at a consumer-only barrier before their first tile
+    if (warp < kWarps) {
+        const int nk = nch * kBoxCols, ct = kWarps * 32;
+        for (int k0 = threadIdx.x; k0 < nk; k0 += 4 * ct) {
+            double v[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int k = k0 + q * ct;
+                v[q] = (k < nk && k < a.nt) ? a.r[k] : 0.0;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int k = k0 + q * ct;
+                const float h = __double2float_rn(v[q]);
+                if (k < nk) rr[k] = make_float2(h, __double2float_rn(v[q] - (double)h));
+            }
+        }
+        if (a.want_logl)
+            for (int k = threadIdx.x; k < SFH_DF_TAB_ALL; k += ct) s_tab[k] = a.tab[k];
+        named_bar_sync(1, kWarps * 32);
+    }
 
     // ------------------------------------------------------------ producers
-    // Lane p issues the boxes whose sequence number q = (local tile) * nch + c has
-    // q % kProducers == p.  slots is a multiple of kProducers: a slot is always refilled by
-    // the same lane, which waits for the release of that slot's previous box.
+    // A run is up to P consecutive boxes of a tile (contiguous in the blocked copy and in
+    // the ring): one bulk copy, one full and one empty barrier per run-slot.  Lane p issues
+    // the runs whose sequence number q = (local tile) * nr + k has q % kProducers == p;
+    // runs is a multiple of kProducers, so a run-slot is always refilled by the same lane,
+    // which waits for the release of that run-slot's previous run.
     if (warp == kWarps) {
         if (lane < kProducers) {
-            const int64_t nq = (int64_t)((a.ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1) * nch;
+            const int64_t nq = (int64_t)((a.ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1) * nr;
             int64_t last = -1;
+            int s = lane, k = lane;  // run-slot and run within the tile of q
+            uint32_t ph = 0;
+            int64_t tl = 0;
+            while (k >= nr) { k -= nr; ++tl; }
             for (int64_t q = lane; q < nq; q += kProducers) {
-                const int s = (int)(q % slots);
-                const uint32_t ph = (uint32_t)(q / slots) & 1u;
                 if (!op_wait(&empty[s], ph ^ 1u, s_abort, err, 1)) break;
-                const int64_t tl = q / nch, c = q - tl * nch;
                 const int64_t t = (int64_t)blockIdx.x + tl * gridDim.x;
-                mbar_expect_tx(&full[s], GE::kBoxBytes);
-                bulk_load(ring + (size_t)s * GE::kBoxFloats,
-                          a.blk + ((size_t)t * nch + c) * GE::kBoxFloats, GE::kBoxBytes, &full[s]);
+                const int c0 = k << lp, nb = min(P, nch - c0);
+                mbar_expect_tx(&full[s], (uint32_t)(nb * GE::kBoxBytes));
+                bulk_load(ring + ((size_t)s << lp) * GE::kBoxFloats,
+                          a.blk + ((size_t)t * nch + c0) * GE::kBoxFloats,
+                          (uint32_t)(nb * GE::kBoxBytes), &full[s]);
                 last = q;
+                s += kProducers;
+                if (s >= runs) { s -= runs; ph ^= 1u; }
+                k += kProducers;
+                while (k >= nr) { k -= nr; ++tl; }
             }
-            // every box this lane requested has landed before the CTA exits
+            // every run this lane requested has landed before the CTA exits
             volatile int never = 0;
             int dummy = 0;
-            for (int64_t q = last; q >= 0 && q > last - slots; q -= kProducers)
-                mbar_wait(&full[q % slots], (uint32_t)(q / slots) & 1u, &never, &dummy, 0);
+            for (int64_t q = last; q >= 0 && q > last - runs; q -= kProducers)
+                mbar_wait(&full[q % runs], (uint32_t)(q / runs) & 1u, &never, &dummy, 0);
         }
         return;
     }
@@ -199,6 +229,7 @@ k_fg_onepass(const OnePassArgs a) {
     int s0 = 0;        // slot of the tile's first box
     uint32_t ph0 = 0;  // its use parity
     bool ok = true;
+    if constexpr (!SKEW)
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
         const int64_t tb = (int64_t)t * BINS;
         double nd = 0.0;
@@ -213,10 +244,11 @@ k_fg_onepass(const OnePassArgs a) {
                 const int u = warp + kOwners * j;
                 if (u >= nunits || !ok) break;
                 const int c = u >> 1, h = u & 1;
-                int s = s0 + c;
+                int rs = s0 + (c >> lp);
                 uint32_t ph = ph0;
-                if (s >= slots) { s -= slots; ph ^= 1u; }
-                if (!op_wait(&full[s], ph, s_abort, err, 2)) { ok = false; break; }
+                if (rs >= runs) { rs -= runs; ph ^= 1u; }
+                const int s = (rs << lp) + (c & (P - 1));
+                if (!op_wait(&full[rs], ph, s_abort, err, 2)) { ok = false; break; }
                 const float *bp = ring + (size_t)s * GE::kBoxFloats + (32 * h + g) * BINS + 4 * quad;
                 const float2 *rp = rr + c * kBoxCols + 32 * h + g;
                 float2 e01 = make_float2(0.f, 0.f), e23 = e01, o01 = e01, o23 = e01;
@@ -298,8 +330,9 @@ k_fg_onepass(const OnePassArgs a) {
                 const int u = warp + kOwners * j;
                 if (u >= nunits) break;
                 const int c = u >> 1, h = u & 1;
-                int s = s0 + c;
-                if (s >= slots) s -= slots;
+                int rs = s0 + (c >> lp);
+                if (rs >= runs) rs -= runs;
+                const int s = (rs << lp) + (c & (P - 1));
                 if (want_g) {
                     const float *bp = ring + (size_t)s * GE::kBoxFloats + (32 * h + g) * BINS + 4 * quad;
 #pragma unroll
@@ -311,7 +344,10 @@ k_fg_onepass(const OnePassArgs a) {
                     }
                 }
                 __syncwarp();
-                if (lane == 0) mbar_arrive(&empty[s]);
+                if (lane == 0) {
+                    mbar_arrive(&empty[rs]);
+                    if (u == nunits - 1 && short_extra) mbar_arrive_n(&empty[rs], short_extra);
+                }
                 __syncwarp();
             }
         } else {
@@ -322,8 +358,151 @@ k_fg_onepass(const OnePassArgs a) {
             }
             __syncwarp();
         }
-        s0 += nch;  // nch <= slots: at most one wrap
-        if (s0 >= slots) { s0 -= slots; ph0 ^= 1u; }
+        s0 += nr;  // nr <= runs: at most one wrap
+        if (s0 >= runs) { s0 -= runs; ph0 ^= 1u; }
+    }
+    else {
+    // Skewed schedule (runs >= 2 nr): iteration it runs phase B of the CTA's tile it - 1
+    // and phase A of its tile it in the same barrier interval, so the two phases' latency
+    // chains overlap, then finishes tile it.  Per unit the owner reads the resident box of
+    // tile it - 1 (phase B) and releases it before waiting for tile it's box (phase A);
+    // the two tiles occupy disjoint slots.
+    const int nloc = (a.ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1;
+    int sB = 0;        // first slot of tile it - 1
+    for (int it = 0; it <= nloc; ++it) {
+        const bool doA = it < nloc, doB = it > 0;  // the same in every warp
+        const int64_t tb = ((int64_t)blockIdx.x + (int64_t)it * gridDim.x) * BINS;  // tile it
+        double nd = 0.0;
+        if (doA && finisher && fl == 0 && tb + fb < nbins) nd = a.data[tb + fb];
+        __syncwarp();
+        if (owner) {
+            float ah[4] = {0.f, 0.f, 0.f, 0.f}, al[4] = {0.f, 0.f, 0.f, 0.f};
+            float2 w01 = make_float2(0.f, 0.f), w23 = w01;
+            if (doB) {
+                const float4 w4 = *(const float4 *)(s_w + 4 * quad);
+                w01 = make_float2(w4.x, w4.y);
+                w23 = make_float2(w4.z, w4.w);
+            }
+#pragma unroll
+            for (int j = 0; j < kUnits; ++j) {
+                const int u = warp + kOwners * j;
+                if (u >= nunits) break;
+                const int c = u >> 1, h = u & 1;
+                const int rowoff = (32 * h + g) * BINS + 4 * quad;
+                if (doB) {  // phase B of tile it - 1
+                    int rs = sB + (c >> lp);
+                    if (rs >= runs) rs -= runs;
+                    const int s = (rs << lp) + (c & (P - 1));
+                    if (want_g) {
+                        const float *bp = ring + (size_t)s * GE::kBoxFloats + rowoff;
+#pragma unroll
+                        for (int k = 0; k < GU; ++k) {
+                            const float4 m = *(const float4 *)(bp + k * RPL * BINS);
+                            const float2 p = __ffma2_rn(make_float2(m.z, m.w), w23,
+                                                        __fmul2_rn(make_float2(m.x, m.y), w01));
+                            sfh_two_sum_acc(gh[j][k], gl[j][k], p.x + p.y);
+                        }
+                    }
+                    __syncwarp();
+                    if (lane == 0) {
+                        mbar_arrive(&empty[rs]);
+                        if (u == nunits - 1 && short_extra) mbar_arrive_n(&empty[rs], short_extra);
+                    }
+                    __syncwarp();
+                }
+                if (doA && ok) {  // phase A of tile it
+                    int rs = s0 + (c >> lp);
+                    uint32_t ph = ph0;
+                    if (rs >= runs) { rs -= runs; ph ^= 1u; }
+                    const int s = (rs << lp) + (c & (P - 1));
+                    if (!op_wait(&full[rs], ph, s_abort, err, 2)) {
+                        ok = false;
+                    } else {
+                        const float *bp = ring + (size_t)s * GE::kBoxFloats + rowoff;
+                        const float2 *rp = rr + c * kBoxCols + 32 * h + g;
+                        float2 e01 = make_float2(0.f, 0.f), e23 = e01, o01 = e01, o23 = e01;
+#pragma unroll
+                        for (int k = 0; k < GU; ++k) {
+                            const float4 m = *(const float4 *)(bp + k * RPL * BINS);
+                            const float2 rv = rp[RPL * k];
+                            const float2 h2 = make_float2(rv.x, rv.x), l2 = make_float2(rv.y, rv.y);
+                            const float2 m01 = make_float2(m.x, m.y), m23 = make_float2(m.z, m.w);
+                            if (k & 1) {
+                                o01 = __ffma2_rn(m01, h2, __ffma2_rn(m01, l2, o01));
+                                o23 = __ffma2_rn(m23, h2, __ffma2_rn(m23, l2, o23));
+                            } else {
+                                e01 = __ffma2_rn(m01, h2, __ffma2_rn(m01, l2, e01));
+                                e23 = __ffma2_rn(m23, h2, __ffma2_rn(m23, l2, e23));
+                            }
+                        }
+                        sfh_two_sum_acc(ah[0], al[0], e01.x + o01.x);
+                        sfh_two_sum_acc(ah[1], al[1], e01.y + o01.y);
+                        sfh_two_sum_acc(ah[2], al[2], e23.x + o23.x);
+                        sfh_two_sum_acc(ah[3], al[3], e23.y + o23.y);
+                    }
+                    __syncwarp();
+                }
+            }
+            if (doA) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    sfh_df v = df_fast_two_sum(ah[k], al[k]);
+#pragma unroll
+                    for (int o = LPR; o <= 16; o <<= 1) {
+                        const sfh_df uu{__shfl_xor_sync(0xffffffffu, v.h, o),
+                                        __shfl_xor_sync(0xffffffffu, v.l, o)};
+                        v = df_add_fast(v, uu);
+                    }
+                    if (lane < LPR) s_part[warp * BINS + 4 * quad + k] = v;
+                }
+            }
+            __syncwarp();
+        } else {
+            // warp OWN: the Poisson terms of tile it - 1 (s_cn from its finish)
+            const int64_t tbB = tb - (int64_t)gridDim.x * BINS;
+            if (doB && a.want_logl && lane < BINS && tbB + lane < nbins) {
+                const float4 cn = s_cn[lane];
+                term = df_add(term, sfh_bin_term(sfh_df{cn.x, cn.y}, cn.z, cn.w, s_tab));
+            }
+            __syncwarp();
+        }
+        if (!doA) break;
+        named_bar_sync(1, kWarps * 32);
+        if (finisher) {
+            sfh_df cm{0.f, 0.f};
+#pragma unroll
+            for (int o = 0; o < kOwners; o += LB)
+                if (o + fl < kOwners) cm = df_add_fast(cm, s_part[(o + fl) * BINS + fb]);
+#pragma unroll
+            for (int o = LB / 2; o >= 1; o >>= 1) {
+                const sfh_df uu{__shfl_xor_sync(0xffffffffu, cm.h, o), __shfl_xor_sync(0xffffffffu, cm.l, o)};
+                cm = df_add_fast(cm, uu);
+            }
+            const int64_t i = tb + fb;
+            if (fl == 0) {
+                float wv = 0.f;
+                if (i < nbins) {
+                    if (!want_g) a.composite[i] = sfh_f2d(cm.h) + sfh_f2d(cm.l);
+                    if (cm.h < a.eps_f || (cm.h == a.eps_f && cm.l < 0.f)) cm = sfh_df{a.eps_f, 0.f};
+                    float nh, nl;
+                    sfh_split_double(nd, nh, nl);
+                    if (want_g) {
+                        wv = __fdiv_rn(df_add(cm, sfh_df{-nh, -nl}).h, cm.h);
+                        a.composite[i] = sfh_f2d(wv);
+                    }
+                    s_cn[fb] = make_float4(cm.h, cm.l, nh, nl);
+                }
+                s_w[fb] = wv;
+            }
+            if (threadIdx.x == 0) *s_stop = *s_abort;
+            __syncwarp();
+        }
+        named_bar_sync(1, kWarps * 32);
+        if (*s_stop) break;
+        sB = s0;
+        s0 += nr;  // 2 nr <= runs: at most one wrap
+        if (s0 >= runs) { s0 -= runs; ph0 ^= 1u; }
+    }
     }
     // per-CTA partials of G: the lanes of a row (bin quads) summed once
     if (want_g && owner) {
@@ -384,16 +563,31 @@ k_fg_onepass(const OnePassArgs a) {
         for (int cw = warp; cw < per; cw += kWarps) {
             const int64_t j = (int64_t)blockIdx.x * per + cw;
             if (j >= a.nt) break;
+            // up to 12 CTAs' partials per lane (grid <= 2 x SMs <= 384), loads issued together
+            double v[12];
+#pragma unroll
+            for (int q = 0; q < 12; ++q) {
+                const int p = lane + 32 * q;
+                v[q] = p < (int)gridDim.x ? __ldcg(a.gpart + (int64_t)p * a.nt + j) : 0.0;
+            }
             double acc = 0.0;
-            for (int p = lane; p < (int)gridDim.x; p += 32) acc += __ldcg(a.gpart + (int64_t)p * a.nt + j);
+#pragma unroll
+            for (int q = 0; q < 12; ++q) acc += v[q];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
             if (lane == 0) a.G[j] = bad ? NAN : a.gsign * acc;
         }
     }
     if (a.negLogL && blockIdx.x == 0 && warp == 0) {
+        double v[12];
+#pragma unroll
+        for (int q = 0; q < 12; ++q) {
+            const int p = lane + 32 * q;
+            v[q] = p < (int)gridDim.x ? __ldcg(a.lpart + p) : 0.0;
+        }
         double acc = 0.0;
-        for (int p = lane; p < (int)gridDim.x; p += 32) acc += __ldcg(a.lpart + p);
+#pragma unroll
+        for (int q = 0; q < 12; ++q) acc += v[q];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
         // loglikelihood returns -typemax(T) = -Inf when the sum is exactly zero (fitting_base.jl:95)
@@ -432,30 +626,34 @@ int op_max_smem(sfh_ctx *ctx, int per_sm) {
     return share < optin ? share : optin;
 }
 
-// Ring slots for BINS-bin tiles of a matrix with nch boxes per tile and `owners` owner
+// Run-slots (of 2^lp boxes each) for BINS-bin tiles of a matrix with nch boxes per tile, with
+// tiles_resident tiles held at once, and `owners` owner
 // warps: the resident tile plus prefetch (0 if it does not fit).
-int op_slots(sfh_ctx *ctx, int bins, int owners, int nch) {
+int op_runs(sfh_ctx *ctx, int bins, int owners, int nch, int lp, int tiles_resident) {
     const int maxs = op_max_smem(ctx, owners >= 8 ? 1 : 2);
     int slots = kMaxSlots;
     while (slots > 0 && op_smem_bytes(bins, owners, slots, nch) > (size_t)maxs) --slots;
-    slots -= slots % kProducers;  // each slot is refilled by one producer lane
-    return slots >= nch + 2 ? slots : 0;
+    int runs = slots >> lp;
+    runs -= runs % kProducers;  // each run-slot is refilled by one producer lane
+    const int nr = (nch + (1 << lp) - 1) >> lp;
+    // the resident tiles' runs plus one in flight
+    return runs >= tiles_resident * nr + 1 ? runs : 0;
 }
 
-template <int BINS, int OWN>
+template <int BINS, int OWN, bool SKEW>
 int launch_onepass(sfh_ctx *ctx, const OnePassArgs &a0, int grid, cudaStream_t st) {
     using GE = Geo<BINS, OWN>;
     static size_t attr_set = 0;
     const size_t smem = op_smem_bytes(BINS, OWN, a0.slots, a0.nch);
     if (smem > attr_set) {
-        SFH_CK(ctx, cudaFuncSetAttribute(k_fg_onepass<BINS, OWN>,
+        SFH_CK(ctx, cudaFuncSetAttribute(k_fg_onepass<BINS, OWN, SKEW>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr_set = smem;
     }
     // grid <= SMs x kMinBlocks and that many CTAs fit an SM (checked by the caller): the
     // CTAs are resident together, as the in-kernel grid reduction needs; its barrier wait
     // is bounded all the same
-    k_fg_onepass<BINS, OWN><<<grid, GE::kThreads, smem, st>>>(a0);
+    k_fg_onepass<BINS, OWN, SKEW><<<grid, GE::kThreads, smem, st>>>(a0);
     SFH_LAUNCHED(ctx);
     return SFH_OK;
 }
@@ -466,10 +664,10 @@ int op_resident(size_t smem) {
     static size_t q_smem = 0;
     static int q_blocks = 0;
     if (smem != q_smem) {
-        cudaFuncSetAttribute(k_fg_onepass<BINS, OWN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(k_fg_onepass<BINS, OWN, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
         int b = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fg_onepass<BINS, OWN>,
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fg_onepass<BINS, OWN, false>,
                                                           Geo<BINS, OWN>::kThreads, smem) != cudaSuccess)
             b = 0;
         q_smem = smem;
@@ -484,7 +682,47 @@ bool sfh_onepass_eligible(sfh_ctx *ctx, const sfh_models *m) {
     if (!m || m->storage == SFH_F64 || !m->d_f32) return false;
     if (m->nbins > INT32_MAX - 64 || m->nt > kMaxTemplates) return false;
     const int nch = (int)((m->nt + kBoxCols - 1) / kBoxCols);
-    return op_slots(ctx, 16, 14, nch) > 0;
+    return op_runs(ctx, 16, 14, nch, 0, 1) > 0;
+}
+
+// The variant later launches take on this handle: the requested tile width, CTAs per SM,
+// schedule and boxes per run where they fit, else the nearest that does (fewer boxes per
+// run, the phased schedule, 16-bin tiles on one CTA per SM).  Returns false when nothing
+// fits.
+bool sfh_onepass_choose(sfh_ctx *ctx, const sfh_models *m, OnePassChoice *c) {
+    const int nch = (int)((m->nt + kBoxCols - 1) / kBoxCols);
+    int bins = m->onepass_bins == 32 ? 32 : 16;
+    int per_sm = (m->onepass_ctas == 2 && bins == 16) ? 2 : 1;
+    bool skew = m->onepass_skew == 1 && bins == 16 && per_sm == 1;
+    int runs = 0, lp = 0;
+    auto pick = [&](int b, int owners, int resident) {
+        const int pref = m->onepass_lp >= 0 ? m->onepass_lp : (b == 16 ? 2 : 1);
+        for (int l = pref; l >= 0; --l) {
+            const int r = op_runs(ctx, b, owners, nch, l, resident);
+            if (r) { runs = r; lp = l; return; }
+        }
+        runs = 0;
+    };
+    pick(bins, per_sm == 2 ? 6 : 14, skew ? 2 : 1);
+    if (runs && per_sm == 2 &&  // two CTAs must fit an SM
+        op_resident<16, 6>(op_smem_bytes(16, 6, runs << lp, nch)) < 2)
+        runs = 0;
+    if (!runs && skew) {
+        skew = false;
+        pick(bins, 14, 1);
+    }
+    if (!runs) {
+        bins = 16;
+        per_sm = 1;
+        skew = false;
+        pick(16, 14, 1);
+    }
+    c->bins = bins;
+    c->per_sm = per_sm;
+    c->skew = skew ? 1 : 0;
+    c->runs = runs;
+    c->lp = lp;
+    return runs > 0;
 }
 
 size_t sfh_onepass_scratch(const sfh_ctx *ctx, const sfh_models *m) {  // up to 2 CTAs per SM
@@ -498,20 +736,11 @@ int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
                           cudaEvent_t *ev, const int *d_skip) {
     const int64_t nbins = m->nbins, nt = m->nt;
     const int nch = (int)((nt + kBoxCols - 1) / kBoxCols);
-    // the handle's variant (tile width, CTAs per SM), else 16 bins on one CTA per SM, which
-    // every eligible shape fits
-    int bins = m->onepass_bins == 32 ? 32 : 16;
-    int per_sm = (m->onepass_ctas == 2 && bins == 16) ? 2 : 1;
-    int slots = op_slots(ctx, bins, per_sm == 2 ? 6 : 14, nch);
-    if (slots && per_sm == 2 &&
-        op_resident<16, 6>(op_smem_bytes(16, 6, slots, nch)) < 2)  // two CTAs must fit an SM
-        slots = 0;
-    if (!slots) {
-        bins = 16;
-        per_sm = 1;
-        slots = op_slots(ctx, 16, 14, nch);
-    }
-    if (!slots) return sfh_set_error(ctx, SFH_ERR_UNSUPPORTED, "one-pass fg!: shape does not fit");
+    OnePassChoice ch{};
+    if (!sfh_onepass_choose(ctx, m, &ch))
+        return sfh_set_error(ctx, SFH_ERR_UNSUPPORTED, "one-pass fg!: shape does not fit");
+    const int bins = ch.bins, per_sm = ch.per_sm;
+    const bool skew = ch.skew != 0;  // 16-bin tiles, one CTA per SM, two tiles resident
     const int mi = bins == 16 ? 0 : 1;
     const int ntiles = (int)((nbins + bins - 1) / bins);
     if (!m->d_blk[mi]) {  // the blocked copy, once per handle and tile width
@@ -521,7 +750,8 @@ int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
             m->d_f32, nbins, nt, bins, nch, total, m->d_blk[mi]);
         SFH_LAUNCHED(ctx);
     }
-    const int cap = ctx->sm_count * per_sm;
+    // the grid reduction takes at most 384 CTAs' partials per column
+    const int cap = ctx->sm_count * per_sm < 384 ? ctx->sm_count * per_sm : 384;
     const int grid = ntiles < cap ? ntiles : cap;
     OnePassArgs a{};
     a.blk = m->d_blk[mi];
@@ -529,7 +759,9 @@ int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
     a.nt = nt;
     a.ntiles = ntiles;
     a.nch = nch;
-    a.slots = slots;
+    a.slots = ch.runs << ch.lp;
+    a.runs = ch.runs;
+    a.lp = ch.lp;
     a.r = d_coeffs;
     a.data = d_data;
     a.composite = d_composite;
@@ -546,9 +778,10 @@ int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
     a.skip = d_skip;
     cudaStream_t st = ctx->stream;
     if (ev) SFH_CK(ctx, cudaEventRecord(ev[0], st));
-    int rc = per_sm == 2 ? launch_onepass<16, 6>(ctx, a, grid, st)
-             : bins == 16 ? launch_onepass<16, 14>(ctx, a, grid, st)
-                          : launch_onepass<32, 14>(ctx, a, grid, st);
+    int rc = per_sm == 2 ? launch_onepass<16, 6, false>(ctx, a, grid, st)
+             : skew       ? launch_onepass<16, 14, true>(ctx, a, grid, st)
+             : bins == 16 ? launch_onepass<16, 14, false>(ctx, a, grid, st)
+                          : launch_onepass<32, 14, false>(ctx, a, grid, st);
     if (rc) return rc;
     if (ev) SFH_CK(ctx, cudaEventRecord(ev[1], st));
     if (ev) SFH_CK(ctx, cudaEventRecord(ev[2], st));

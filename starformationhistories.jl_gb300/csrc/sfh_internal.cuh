@@ -57,7 +57,9 @@ struct sfh_models {
     // it streams (built on first use): for tile t and box c (64 templates) one contiguous
     // block of [64 templates][bins] floats, blocks in (tile, box) order, zero padded.
     int onepass_bins = 0;
-    int onepass_ctas = 0;  // one-pass CTAs per SM: 1 (14 owner warps) or 2 (6 each); 0: 1
+    int onepass_ctas = 0;
+    int onepass_skew = 0;  // 1: skewed schedule (phase B of one tile beside phase A of the next)
+    int onepass_lp = -1;   // log2 boxes per bulk copy (-1: 2 for 16-bin tiles, 1 for 32-bin)  // one-pass CTAs per SM: 1 (14 owner warps) or 2 (6 each); 0: 1
     float *d_blk[2] = {nullptr, nullptr};
 };
 
@@ -220,6 +222,10 @@ int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
                           const double *d_data, double *d_composite, double *d_G,
                           double *d_negLogL, double eps, double gsign, void *scratch,
                           cudaEvent_t *ev, const int *d_skip = nullptr);
+struct OnePassChoice {
+    int bins, per_sm, skew, runs, lp;
+};
+bool sfh_onepass_choose(sfh_ctx *ctx, const sfh_models *m, OnePassChoice *c);
 // Reads and clears the one-pass timeout slot (synchronises the stream).
 int sfh_check_onepass(sfh_ctx *ctx);
 int sfh_launch_loglikelihood(sfh_ctx *ctx, const double *composite, const double *data,

@@ -26,7 +26,7 @@ EXPORTED = [
     "sfh_models_combine",
     "sfh_composite", "sfh_loglikelihood", "sfh_grad_loglikelihood", "sfh_fg", "sfh_fg_dev",
     "sfh_fg_batched_dev", "sfh_fg_kernel_times", "sfh_models_autotune", "sfh_models_set_path", "sfh_models_set_onepass_tile",
-    "sfh_models_set_onepass_ctas",
+    "sfh_models_set_onepass_ctas", "sfh_models_set_onepass_schedule", "sfh_models_onepass_variant", "sfh_models_set_onepass_run",
     "sfh_models_path", "sfh_fg_dev_noalloc", "sfh_hmc_sample_dev",
     "sfh_logdensity_batched_dev", "sfh_fit_bfgs", "sfh_fit_bfgs_dev", "sfh_bin_cmd", "sfh_bin_cmd_dev", "sfh_bin_cmd_smooth", "sfh_bin_cmd_smooth_batch_dev",
     "sfh_partial_cmd_smooth_batch_dev", "sfh_partial_cmd_smooth_ragged_dev",
@@ -130,6 +130,10 @@ def load(path: str | None = None):
             "sfh_models_set_path": ([_vp, _vp, C.c_int], C.c_int),
             "sfh_models_set_onepass_tile": ([_vp, _vp, C.c_int], C.c_int),
             "sfh_models_set_onepass_ctas": ([_vp, _vp, C.c_int], C.c_int),
+            "sfh_models_set_onepass_schedule": ([_vp, _vp, C.c_int], C.c_int),
+            "sfh_models_onepass_variant": ([_vp, _vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                            C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
+            "sfh_models_set_onepass_run": ([_vp, _vp, C.c_int], C.c_int),
             "sfh_models_path": ([_vp, _vp, C.POINTER(C.c_int), C.POINTER(_d)], C.c_int),
             "sfh_fg_dev_noalloc": ([_vp, _vp, _i64, _i64, _vp, _vp, _vp, _vp, _vp, _d], C.c_int),
             "sfh_fg_kernel_times": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, C.c_int,

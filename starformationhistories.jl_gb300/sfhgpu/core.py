@@ -149,6 +149,29 @@ class Models:
         check(load().sfh_models_set_onepass_ctas(self.ctx.handle, self._h, int(per_sm)),
               self.ctx.handle, "models_set_onepass_ctas")
 
+    def set_onepass_schedule(self, schedule):
+        """Schedule of the one-pass kernel: "phased" or "skewed"
+        (sfh_models_set_onepass_schedule)."""
+        _s = {"phased": 0, "skewed": 1}[schedule]
+        check(load().sfh_models_set_onepass_schedule(self.ctx.handle, self._h, _s),
+              self.ctx.handle, "models_set_onepass_schedule")
+
+    def set_onepass_run(self, boxes):
+        """Boxes per bulk copy of the one-pass kernel: 1, 2, 4 or 0 for the default
+        (sfh_models_set_onepass_run)."""
+        check(load().sfh_models_set_onepass_run(self.ctx.handle, self._h, int(boxes)),
+              self.ctx.handle, "models_set_onepass_run")
+
+    @property
+    def onepass_variant(self):
+        """(bins per tile, CTAs per SM, schedule, boxes per bulk copy) of the one-pass
+        launches."""
+        b, c, k, r = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        check(load().sfh_models_onepass_variant(self.ctx.handle, self._h, C.byref(b), C.byref(c),
+                                                C.byref(k), C.byref(r)), self.ctx.handle,
+              "models_onepass_variant")
+        return b.value, c.value, ("skewed" if k.value else "phased"), r.value
+
     @property
     def path(self):
         """The path fg! calls with G take on this handle now: "onepass" or "twopass"."""

@@ -36,15 +36,25 @@ SHAPES = [(4, 1), (3, 2), (32, 32), (37, 33), (1004, 64), (1005, 65), (7500, 50)
           (152 * 32 * 3 + 5, 97), (4868, 1536), (60000, 1200)]
 
 
-@pytest.mark.parametrize("bins,ctas", [(16, 1), (32, 1), (16, 2)])
+# (tile bins, CTAs per SM, schedule, boxes per bulk copy; 0 = the default)
+VARIANTS = [(16, 1, "phased", 0), (32, 1, "phased", 0), (16, 2, "phased", 0),
+            (16, 1, "skewed", 0), (16, 1, "phased", 1), (16, 1, "phased", 2),
+            (32, 1, "phased", 1), (16, 1, "skewed", 1)]
+
+
+@pytest.mark.parametrize("bins,ctas,schedule,run", VARIANTS)
 @pytest.mark.parametrize("nbins,nt", SHAPES)
-def test_onepass_matches_oracle(sfh, O, nbins, nt, bins, ctas):
+def test_onepass_matches_oracle(sfh, O, nbins, nt, bins, ctas, schedule, run):
     M, r, data = _problem(nbins, nt, seed=7 * nbins + nt)
     H = sfh.Models(M, storage="f32")
     H.set_path("onepass")
     H.set_onepass_tile(bins)
     H.set_onepass_ctas(ctas)
+    H.set_onepass_schedule(schedule)
+    H.set_onepass_run(run)
     assert H.path == "onepass"
+    vb, vc, vs, vr = H.onepass_variant
+    assert vr in (1, 2, 4) and (run == 0 or vr <= run)
     comp = np.empty(nbins)
     G = np.empty(nt)
     v = sfh.fg_(True, G, r, H, data, comp)
@@ -78,7 +88,23 @@ def test_onepass_agrees_with_twopass_and_is_deterministic(sfh):
             assert v == out[path][0]
             assert np.array_equal(G, out[path][1]) and np.array_equal(comp, out[path][2])
         out[path] = (v, G, comp)
+    for run in (1, 2, 4):  # boxes per bulk copy: bitwise the same results
+        H.set_path("onepass")
+        H.set_onepass_run(run)
+        comp = np.empty(M.shape[0])
+        G = np.empty(M.shape[1])
+        v = sfh.fg_(True, G, r, H, data, comp)
+        assert v == out["onepass"][0] and np.array_equal(G, out["onepass"][1])
+        assert np.array_equal(comp, out["onepass"][2])
+    H.set_onepass_run(0)
+    H.set_onepass_schedule("skewed")  # the skewed schedule: bitwise the phased one's
+    comp = np.empty(M.shape[0])
+    G = np.empty(M.shape[1])
     H.set_path("onepass")
+    v = sfh.fg_(True, G, r, H, data, comp)
+    assert v == out["onepass"][0] and np.array_equal(G, out["onepass"][1])
+    assert np.array_equal(comp, out["onepass"][2])
+    H.set_onepass_schedule("phased")
     H.set_onepass_tile(32)  # the other tile width: same results to rounding
     comp = np.empty(M.shape[0])
     G = np.empty(M.shape[1])
