@@ -306,6 +306,25 @@ int sfh_logdensity_batched_dev(sfh_ctx *ctx, const sfh_models *models, const dou
                                const sfh_hmc_config *cfg, const double *d_theta, double *d_logd,
                                double *d_grad);
 
+/* ---------------------------------------------------------------- mock observation */
+/* model_cmd(mags, errfuncs, completefuncs, biasfuncs; rng, ret_idxs), src/simulate.jl:621-680:
+   star i (of n) is kept when a uniform draw is <= detect_prob[i] (the product of its per-filter
+   completeness values, evaluated by the caller as the reference evaluates its callables);
+   a kept star's magnitudes become mags + z sigma + bias with standard normal z.  mags,
+   sigma and bias (NULL = none) are n x nf row-major (star-major), nf <= 8.  out (n x nf
+   capacity) and idx (n capacity, 0-based input indices) receive the kept stars in input
+   order, *n_out their number.  Draws are Philox4x32-10 keyed by seed and counted by star
+   and filter, so they do not depend on the launch or on which other stars are kept (the
+   reference's draws come from Julia's RNG: the same distribution, not the same numbers).
+   Host arrays; synchronous. */
+int sfh_model_cmd(sfh_ctx *ctx, const double *mags, const double *sigma, const double *bias,
+                  const double *detect_prob, int64_t n, int nf, uint64_t seed, double *out,
+                  int64_t *idx, int64_t *n_out);
+/* sfh_model_cmd on device buffers (synchronises to read *n_out). */
+int sfh_model_cmd_dev(sfh_ctx *ctx, const double *d_mags, const double *d_sigma,
+                      const double *d_bias, const double *d_detect_prob, int64_t n, int nf,
+                      uint64_t seed, double *d_out, int64_t *d_idx, int64_t *n_out);
+
 /* ---------------------------------------------------------------- template construction */
 /* bin_cmd(colors, mags; weights, edges), StarFormationHistories.jl:544-553: the
    hard-binned Hess diagram, StatsBase fit(Histogram, (colors, mags), Weights(weights), edges;

@@ -20,7 +20,8 @@ from .templates import (BrokenPowerLawIMF, Histogram, Kroupa2001, Martin2016_com
                         mini_spacing, partial_cmd_smooth, partial_cmd_smooth_batch,
                         partial_cmd_smooth_ragged, NoBinaries, RandomBinaryPairs, trapz,
                         binary_points, binary_hess_batch, partial_cmd_smooth_binary_batch,
-                        bin_cmd, partial_cmd, partial_cmd_points, julia_range, julia_colon, Range)
+                        bin_cmd, partial_cmd, partial_cmd_points, julia_range, julia_colon, Range,
+                        model_cmd)
 
 __all__ = [
     "SFH_BF16X2", "SFH_F32", "SFH_F64", "EXPORTED", "LIB_PATH", "SFHArgumentError", "SFHError",
@@ -29,7 +30,7 @@ __all__ = [
     "FIT_LOG_MLE", "FIT_SQRT", "grad_loglikelihood",
     "grad_loglikelihood_", "loglikelihood", "renormalize_x0", "stack_models", "BrokenPowerLawIMF",
     "Histogram", "Kroupa2001", "Martin2016_complete", "bin_cmd", "bin_cmd_smooth", "calculate_edges",
-    "partial_cmd", "partial_cmd_points", "julia_range", "julia_colon", "Range",
+    "partial_cmd", "partial_cmd_points", "julia_range", "julia_colon", "Range", "model_cmd",
     "calculate_weights", "compl_model", "err_model", "exp_photerr", "histogram_data",
     "histogram_pix", "interpolate_mini", "midpoints", "mini_spacing", "partial_cmd_smooth",
     "partial_cmd_smooth_batch", "NoBinaries", "RandomBinaryPairs", "trapz", "binary_points",

@@ -28,7 +28,7 @@ EXPORTED = [
     "sfh_fg_batched_dev", "sfh_fg_kernel_times", "sfh_models_autotune", "sfh_models_set_path", "sfh_models_set_onepass_tile",
     "sfh_models_set_onepass_ctas", "sfh_models_set_onepass_schedule", "sfh_models_onepass_variant", "sfh_models_set_onepass_run",
     "sfh_models_path", "sfh_fg_dev_noalloc", "sfh_hmc_sample_dev",
-    "sfh_logdensity_batched_dev", "sfh_fit_bfgs", "sfh_fit_bfgs_dev", "sfh_bin_cmd", "sfh_bin_cmd_dev", "sfh_bin_cmd_smooth", "sfh_bin_cmd_smooth_batch_dev",
+    "sfh_logdensity_batched_dev", "sfh_model_cmd", "sfh_model_cmd_dev", "sfh_fit_bfgs", "sfh_fit_bfgs_dev", "sfh_bin_cmd", "sfh_bin_cmd_dev", "sfh_bin_cmd_smooth", "sfh_bin_cmd_smooth_batch_dev",
     "sfh_partial_cmd_smooth_batch_dev", "sfh_partial_cmd_smooth_ragged_dev",
     "sfh_binary_hess_batch_dev", "sfh_mix_binary_templates_dev",
     "sfh_galaxies_create", "sfh_galaxies_free", "sfh_galaxies_info", "sfh_fg_ragged_dev",
@@ -138,6 +138,10 @@ def load(path: str | None = None):
             "sfh_fg_dev_noalloc": ([_vp, _vp, _i64, _i64, _vp, _vp, _vp, _vp, _vp, _d], C.c_int),
             "sfh_fg_kernel_times": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, C.c_int,
                                      C.POINTER(_d)], C.c_int),
+            "sfh_model_cmd": ([_vp, _vp, _vp, _vp, _vp, _i64, C.c_int, C.c_uint64, _vp, _vp,
+                               C.POINTER(_i64)], C.c_int),
+            "sfh_model_cmd_dev": ([_vp, _vp, _vp, _vp, _vp, _i64, C.c_int, C.c_uint64, _vp, _vp,
+                                   C.POINTER(_i64)], C.c_int),
             "sfh_fit_bfgs": ([_vp, _vp, _vp, _vp, C.POINTER(FitOptions), _vp, _vp,
                               C.POINTER(FitResult)], C.c_int),
             "sfh_fit_bfgs_dev": ([_vp, _vp, _vp, _vp, C.POINTER(FitOptions), _vp, _vp,

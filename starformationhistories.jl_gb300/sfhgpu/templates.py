@@ -402,6 +402,49 @@ def partial_cmd(m_ini, colors, mags, imf, dmod=0.0, normalize_value=1.0, mean_ma
                    xwidth=xwidth, ywidth=ywidth, ctx=ctx)
 
 
+def model_cmd(mags, errfuncs, completefuncs, biasfuncs=None, seed=0, ret_idxs=False,
+              ctx=None):
+    """model_cmd, src/simulate.jl:621-680: mock observation of a catalogue of stellar
+    magnitudes.  mags is (nstars, nfilters) (a star's magnitudes in a row, as the
+    reference's vector of per-star vectors); errfuncs / completefuncs / biasfuncs are
+    per-filter callables on arrays, evaluated here at the input magnitudes as the reference
+    evaluates them.  A star is kept when a uniform draw is <= the product of its
+    completeness values; kept stars get Gaussian errors and the bias.  The draws (GPU,
+    Philox keyed by `seed`) follow the reference's distributions, not its RNG stream.
+    Returns the kept magnitudes (input order) and, with ret_idxs, their 0-based indices."""
+    m = np.ascontiguousarray(mags, dtype=np.float64)
+    if m.ndim != 2:
+        raise ValueError("mags must be (nstars, nfilters)")
+    n, nf = m.shape
+    if not (nf == len(errfuncs) == len(completefuncs)):
+        raise ValueError("length(first(mags)) == length(errfuncs) == length(completefuncs)")
+    if biasfuncs is not None and len(biasfuncs) != nf:
+        raise ValueError("length(biasfuncs) == length(first(mags))")
+    if nf > 8:
+        raise ValueError("at most 8 filters")
+    sigma = np.ascontiguousarray(np.stack(
+        [np.broadcast_to(np.asarray(errfuncs[j](m[:, j]), dtype=np.float64), (n,))
+         for j in range(nf)], axis=1)) if n else np.empty((0, nf))
+    compl = np.ones(n)
+    for j in range(nf):
+        compl *= np.asarray(completefuncs[j](m[:, j]), dtype=np.float64)
+    bias = None
+    if biasfuncs is not None and n:
+        bias = np.ascontiguousarray(np.stack(
+            [np.broadcast_to(np.asarray(biasfuncs[j](m[:, j]), dtype=np.float64), (n,))
+             for j in range(nf)], axis=1))
+    out = np.empty((n, nf))
+    idx = np.empty(n, dtype=np.int64)
+    nout = C.c_int64()
+    ctx = ctx or default_context()
+    check(load().sfh_model_cmd(ctx.handle, m.ctypes.data, sigma.ctypes.data,
+                               None if bias is None else bias.ctypes.data, compl.ctypes.data, n,
+                               nf, int(seed) & 0xFFFFFFFFFFFFFFFF, out.ctypes.data,
+                               idx.ctypes.data, C.byref(nout)), ctx.handle, "model_cmd")
+    k = nout.value
+    return (out[:k], idx[:k]) if ret_idxs else out[:k]
+
+
 def partial_cmd_smooth_stars(m_ini, mags, mag_err_funcs, y_index, color_indices, imf,
                              completeness_funcs=None, bias_funcs=None, dmod=0.0,
                              normalize_value=1.0, mean_mass=None, edges=None, xlim=None,
