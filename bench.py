@@ -415,6 +415,124 @@ def run_fit(H, data, g_abstol=1e-3):
     }
 
 
+def run_extras(ctx, w, cpu=True, ntempl=60, nstars=10_000_000):
+    """The rows beside the headline path, each timed on the GPU with CUDA events and, when
+    `cpu`, beside the oracle (or a numpy port) on a bounded sample:
+    binary_hess (RandomBinaryPairs) for `ntempl` templates of the production grid, bin_cmd
+    of `nstars` catalogue-precision stars on the production grid and on a 100 x 100 grid,
+    and model_cmd of `nstars` three-filter stars."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import sfhgpu
+    from sfhgpu import synthetic as S
+    L = sfhgpu.load()
+    dev = torch.device("cuda", 0)
+    out = {}
+
+    def ev_time(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(ctx.torch_stream()):
+            e0.record(ctx.torch_stream())
+            for _ in range(reps):
+                fn()
+            e1.record(ctx.torch_stream())
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps / 1e3  # seconds
+
+    # ---- binary_hess for ntempl templates (host preprocessing of the pair points once)
+    m_ini, mags, offs, lens = S.isochrone_batch(w)
+    pts = [sfhgpu.binary_points(m_ini[o:o + n], list(mags[:, o:o + n]), 1, (0, 1), w.dmod,
+                                (w.xedges, w.yedges)) for o, n in list(zip(offs, lens))[:ntempl]]
+    md = np.concatenate([p[0] for p in pts])
+    gd = np.ascontiguousarray(np.concatenate([p[1] for p in pts], axis=1))
+    ln = np.array([p[0].size for p in pts], dtype=np.int32)
+    of = np.concatenate([[0], np.cumsum(ln)[:-1]]).astype(np.int64)
+    d_m, d_g = torch.tensor(md, device=dev), torch.tensor(gd, device=dev)
+    imf = S.imf()
+    nx, ny = w.grid
+    buf = torch.empty((len(pts), nx * ny), dtype=torch.float32, device=dev)
+
+    def binary():
+        sfhgpu.binary_hess_batch(d_m, d_g, of, ln, 1, (0, 1), S.error_models(),
+                                 S.completeness_models(), imf, w.normalize_value,
+                                 (w.xedges, w.yedges), out=buf)
+    t = ev_time(binary, 3)
+    pairs = float(np.sum(ln.astype(np.float64) * (ln - 1) / 2))
+    out["binary_hess"] = {"templates": len(pts), "seconds": t, "templates_per_s": len(pts) / t,
+                          "pairs_per_s": pairs / t, "mean_points_per_template": float(ln.mean())}
+
+    # ---- bin_cmd: catalogue-precision stars (3 decimals: many on edges)
+    rng = np.random.default_rng(5)
+    x = np.round(rng.normal(0.8, 0.5, nstars), 3)
+    y = np.round(rng.uniform(float(w.yedges[0]), float(w.yedges[-1]), nstars), 3)
+    d_x, d_y = torch.tensor(x, device=dev), torch.tensor(y, device=dev)
+    for name, (ex, ey) in (("production_grid", (w.xedges, w.yedges)),
+                           ("grid_100x100", (sfhgpu.julia_range(-1.0, 3.0, 101),
+                                             sfhgpu.julia_range(float(w.yedges[0]),
+                                                                float(w.yedges[-1]), 101)))):
+        ex, ey = np.ascontiguousarray(ex, dtype=np.float64), np.ascontiguousarray(ey, dtype=np.float64)
+        d_ex, d_ey = torch.tensor(ex, device=dev), torch.tensor(ey, device=dev)
+        gx, gy = ex.size - 1, ey.size - 1
+        d_h = torch.empty(gx * gy, dtype=torch.float64, device=dev)
+
+        def bc():
+            rc = L.sfh_bin_cmd_dev(ctx.handle, d_x.data_ptr(), d_y.data_ptr(), None, nstars,
+                                   d_ex.data_ptr(), gx, d_ey.data_ptr(), gy, d_h.data_ptr())
+            if rc:
+                sfhgpu._lib.check(rc, ctx.handle, "sfh_bin_cmd_dev")
+        t = ev_time(bc, 20)
+        t0 = time.perf_counter()
+        h = sfhgpu.bin_cmd(x, y, edges=(ex, ey)).weights
+        te = time.perf_counter() - t0
+        leg = {"bins": gx * gy, "stars": nstars, "device_seconds": t,
+               "stars_per_s": nstars / t, "e2e_stars_per_s": nstars / te,
+               "achieved_gbs": nstars * 16 / t / 1e9}
+        if cpu:
+            import oracle as O
+            ns = 2_000_000
+            t0 = time.perf_counter()
+            ref = O.bin_cmd(x[:ns], y[:ns], None, ex, ey)
+            leg["cpu_baseline"] = {"stars_per_s": ns / (time.perf_counter() - t0), "cores": 1,
+                                   "kind": "port", "sample": f"{ns} stars (oracle, 1 thread)"}
+            hs = sfhgpu.bin_cmd(x[:ns], y[:ns], edges=(ex, ey)).weights
+            leg["bit_exact_vs_oracle"] = bool(np.array_equal(hs, ref))
+        out["bin_cmd_" + name] = leg
+
+    # ---- model_cmd: three filters
+    m3 = np.ascontiguousarray(rng.uniform(22.0, 30.0, (nstars, 3)))
+    sig = np.ascontiguousarray(0.01 + 0.3 * np.exp((m3 - 28.0) / 1.2))
+    prob = np.ascontiguousarray(np.prod(1.0 / (1.0 + np.exp((m3 - 28.0) / 0.3)), axis=1))
+    d_m3, d_sig, d_p = (torch.tensor(a, device=dev) for a in (m3, sig, prob))
+    d_out = torch.empty_like(d_m3)
+    d_idx = torch.empty(nstars, dtype=torch.int64, device=dev)
+    nout = C.c_int64()
+
+    def mc():
+        rc = L.sfh_model_cmd_dev(ctx.handle, d_m3.data_ptr(), d_sig.data_ptr(), None,
+                                 d_p.data_ptr(), nstars, 3, 7, d_out.data_ptr(),
+                                 d_idx.data_ptr(), C.byref(nout))
+        if rc:
+            sfhgpu._lib.check(rc, ctx.handle, "sfh_model_cmd_dev")
+    t = ev_time(mc, 10)
+    leg = {"stars": nstars, "kept": int(nout.value), "device_seconds": t,
+           "stars_per_s": nstars / t, "note": "includes the synchronisation that reads the count"}
+    if cpu:
+        ns = 2_000_000
+        g = np.random.default_rng(1)
+        t0 = time.perf_counter()
+        keep = g.random(ns) <= prob[:ns]
+        _ = m3[:ns][keep] + g.standard_normal((int(keep.sum()), 3)) * sig[:ns][keep]
+        leg["cpu_baseline"] = {"stars_per_s": ns / (time.perf_counter() - t0), "cores": 1,
+                               "kind": "port", "sample": f"{ns} stars (numpy, 1 thread)"}
+    out["model_cmd"] = leg
+    return out
+
+
 def oracle_checks(batched, ragged, M64, r, data, neglogl):
     """Accuracy against the FP64 oracle on the same stored templates (CPU leg): the plain
     fg!'s -logL, and the stashed outputs of the batched and ragged legs (the stash is
@@ -718,6 +836,11 @@ def run_ours(args):
     e2e = {"value": world * ne2e / e2e_s, "unit": UNIT, "h2d_bytes_per_step": (NTW + NBINS) * 8,
            "d2h_bytes_per_step": (NBINS + NTW + 1) * 8, "steps": ne2e}
 
+    # ---- the rows beside the headline path (binary templates, bin_cmd, model_cmd)
+    extras = None
+    if not args.no_extras and rank == 0:
+        extras = run_extras(ctx, w, cpu=not args.no_cpu)
+
     # ---- whole fits on the same templates (device BFGS driver vs a host scipy loop)
     fit = None
     if not args.no_fit:
@@ -799,6 +922,7 @@ def run_ours(args):
             "negLogL": neglogl, "precision": plain_check, "gpu_launches": launches,
             "roofline": roofline,
             "batched": batched, "hmc": hmc, "ragged": ragged, "emulator": emulator, "fit": fit,
+            "extras": extras,
             "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
         }
         print(json.dumps(line), flush=True)
@@ -824,6 +948,8 @@ def main():
                          "(for profiling runs, where profiler overhead can change the choice)")
     ap.add_argument("--no-emulator", action="store_true", help="skip the emulator leg")
     ap.add_argument("--no-fit", action="store_true", help="skip the whole-fit leg")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the binary_hess / bin_cmd / model_cmd leg")
     ap.add_argument("--onepass-variant", default="",
                     help="pin the one-pass variant after autotuning: bins,ctas,schedule,boxes "
                          "(e.g. 32,1,phased,2)")
