@@ -98,3 +98,47 @@ def test_partial_cmd_oracle_and_host_points(O, sfh):
     grid = np.linspace(m.min(), m.max(), 200001)
     integral = sfh.trapz(grid, imf(grid))
     assert w.sum() == pytest.approx(1e4 / imf.mean() * integral, rel=2e-3)
+
+
+def test_julia_ranges_edge_cases(sfh):
+    # a descending colon range and a step that does not land on stop
+    d = sfh.julia_colon(1.0, -0.25, 0.0)
+    assert list(d) == [1.0, 0.75, 0.5, 0.25, 0.0]
+    assert list(sfh.julia_colon(0.0, 0.1, 0.35)) == [0.0, 0.1, 0.2, 0.3]
+    assert len(sfh.julia_colon(1.0, 0.1, 0.0)) == 0  # empty, as in Julia
+    with pytest.raises(ValueError):
+        sfh.julia_colon(0.0, 0.0, 1.0)
+    with pytest.raises(ValueError):
+        sfh.julia_range(0.0, 1.0, 1)
+    with pytest.raises(ValueError):
+        sfh.julia_range(0.0, np.inf, 5)
+    r = sfh.julia_range(2.0, 2.0, 4)
+    assert list(r) == [2.0] * 4
+    # the Range's step (Julia's step(r)) is what the smooth binning uses
+    from sfhgpu.templates import _range
+    f, st, n = _range(sfh.julia_range(17.0, 27.0, 101))
+    assert (f, st, n) == (17.0, 0.1, 100)
+    assert _range(np.linspace(0.0, 1.0, 11))[1] == pytest.approx(0.1, rel=1e-15)
+
+
+def test_host_argument_checks(sfh):
+    e = (np.linspace(0, 1, 11), np.linspace(0, 1, 6))
+    with pytest.raises(ValueError):  # ragged inputs
+        sfh.bin_cmd(np.zeros(3), np.zeros(2), edges=e)
+    with pytest.raises(ValueError):  # weights of another length
+        sfh.bin_cmd(np.zeros(3), np.zeros(3), weights=np.ones(2), edges=e)
+    with pytest.raises(ValueError):  # edges not increasing
+        sfh.bin_cmd(np.zeros(3), np.zeros(3), edges=(np.array([0.0, 1.0, 0.5]), e[1]))
+    with pytest.raises(ValueError):  # edges not finite
+        sfh.bin_cmd(np.zeros(3), np.zeros(3), edges=(np.array([0.0, np.nan]), e[1]))
+    with pytest.raises(ValueError):  # neither edges, nbins nor widths
+        sfh.bin_cmd(np.zeros(3), np.ones(3))
+    f = [lambda m: np.zeros_like(m)] * 3
+    with pytest.raises(ValueError):  # one callable per filter
+        sfh.model_cmd(np.zeros((4, 3)), f[:2], f)
+    with pytest.raises(ValueError):
+        sfh.model_cmd(np.zeros((4, 3)), f, f, biasfuncs=f[:1])
+    with pytest.raises(ValueError):  # (nstars, nfilters)
+        sfh.model_cmd(np.zeros(4), f[:1], f[:1])
+    with pytest.raises(ValueError):  # at most 8 filters
+        sfh.model_cmd(np.zeros((2, 9)), [f[0]] * 9, [f[0]] * 9)
