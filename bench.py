@@ -327,7 +327,7 @@ def run_ragged(ctx, steps=50, warmup=5, check=2):
 def run_emulator(ctx, w, n_train=100_000, n_val=4096, steps=4000, cells=(8, 2, 16), nreq=1200):
     """Learned template emulator on the production grid: per-cell PCA bases (64
     components of sqrt templates) and per-cell MLPs 3-256-256-64 trained on templates the
-    GPU partial_cmd_smooth generates at random (log age, [M/H], distance modulus); judged
+    GPU partial_cmd_smooth generates at random (log age, [M/H], distance modulus); scored
     by Poisson deviance per star against exact templates (tolerance 1e-3)."""
     import numpy as np
     import torch
@@ -350,7 +350,7 @@ def run_emulator(ctx, w, n_train=100_000, n_val=4096, steps=4000, cells=(8, 2, 1
     emul = em.predict(th)
     torch.cuda.synchronize()
     t_emul = time.perf_counter() - t0
-    dev = em.judge(exact, emul)
+    dev = em.deviance(exact, emul)
     trusted = em.trusted(th)
     em.templates(th[:8], gen)  # first use of the routing path (indexed copy kernel)
     torch.cuda.synchronize()
@@ -857,7 +857,7 @@ def run_ours(args):
     if not args.no_ragged:
         ragged = run_ragged(ctx)
 
-    # ---- learned template emulator (production grid), judged against exact templates
+    # ---- learned template emulator (production grid), scored against exact templates
     emulator = None
     if not args.no_emulator:
         emulator = run_emulator(ctx, w)

@@ -478,7 +478,7 @@ int sfh_fg_ragged_dev(sfh_ctx *ctx, const sfh_galaxies *galaxies, const double *
    hidden layers, FP32 master weights, BF16-rounded matmul operands with FP32
    accumulation) maps standardised (log age, [M/H], distance modulus) to scaled
    coefficients on a PCA basis of variance-stabilised templates; templates are rebuilt
-   from the coefficients, and the exact partial_cmd_smooth template judges them by Poisson
+   from the coefficients, and the exact partial_cmd_smooth template scores them by Poisson
    deviance per star and replaces any that fail.  All arrays are device FP32 and
    row-major.  Parameter block: W1 (h1 x in), b1, W2 (h2 x h1), b2, W3 (out x h2), b3. */
 int sfh_mlp_param_count(int in, int h1, int h2, int out, int64_t *n);
@@ -532,7 +532,7 @@ int sfh_emu_prepare(sfh_ctx *ctx, float *d_Y, int64_t rows, int64_t cols, int mo
 int sfh_emu_reconstruct(sfh_ctx *ctx, const float *d_coef, const float *d_basis,
                         const float *d_offset, int K, int64_t nbins, int64_t B, int mode,
                         float *d_out);
-/* Judge: d_dev[t] = 2 sum_i (e - x + x log(x / e)) / sum_i x for exact x = d_exact[t, :],
+/* Score: d_dev[t] = 2 sum_i (e - x + x log(x / e)) / sum_i x for exact x = d_exact[t, :],
    emulated e = d_emul[t, :] (floored at 1e-30), in FP64; B x nbins row-major inputs. */
 int sfh_poisson_deviance(sfh_ctx *ctx, const float *d_exact, const float *d_emul,
                          int64_t nbins, int B, double *d_dev);

@@ -941,7 +941,7 @@ double sfho_amr_fg(int kind, const double *variables, int64_t nages, double T_ma
 
 /* ======================= learned template emulator (no reference counterpart) ====== */
 /* A plain FP64 restatement of the device MLP: the forward pass, the backward pass of
-   the mean-squared-error loss, and the Poisson deviance used as the judge. */
+   the mean-squared-error loss, and the Poisson deviance used as the score. */
 
 static double bf16_round(double x) {
     float f = (float)x;

@@ -2,12 +2,12 @@
 //
 // No counterpart in the reference (new component): (log age, [M/H], distance modulus)
 // -> MLP 3 -> 256 -> 256 -> 64 (GELU) -> standardised PCA coefficients -> template
-// = mean + Σ_k c_k v_k.  The exact partial_cmd_smooth template is the judge (Poisson
+// = mean + Σ_k c_k v_k.  The exact partial_cmd_smooth template is the arbiter (Poisson
 // deviance per star) and the fallback.
 //
 // Kernels: tiled GEMMs with BF16-rounded operands and FP32 accumulation (the MLP's
 // "BF16 matmuls" over FP32 master weights), bias + GELU, GELU backward, MSE loss
-// gradient, Adam; reconstruction of templates from coefficients; the judge.  The
+// gradient, Adam; reconstruction of templates from coefficients; the deviance score.  The
 // training loop runs on the device: each step draws its minibatch indices with Philox.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -223,7 +223,7 @@ __global__ void k_finish(float *__restrict__ out, int64_t rows, int64_t cols,
     out[k] = mode == 1 ? y * y : y;
 }
 
-// Judge: Poisson deviance per star of emulated e against exact t,
+// Score: Poisson deviance per star of emulated e against exact t,
 // 2 Σ_i [e_i - t_i + t_i log(t_i / e_i)] / Σ_i t_i  (e clamped to a tiny floor).
 __global__ void k_deviance(const float *__restrict__ exact, const float *__restrict__ emul,
                            int64_t nbins, double *__restrict__ dev) {

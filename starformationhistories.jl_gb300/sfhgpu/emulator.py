@@ -1,4 +1,4 @@
-"""Learned template emulator: MLP on a PCA basis, judged by and backed by exact templates.
+"""Learned template emulator: MLP on a PCA basis, scored against and backed by exact templates.
 
 No counterpart in the reference (a new component).  Parameters theta = (log age, [M/H],
 distance modulus) are mapped by an MLP 3 -> 256 -> 256 -> 64 (GELU, FP32 master weights,
@@ -8,9 +8,9 @@ BF16-rounded matmul operands, trained with Adam by the library's own kernels,
 proportional to the squared error in sqrt space (Poisson deviance ~ 4 sum (sqrt e -
 sqrt t)^2).  Templates are rebuilt as t = max(0, offset + c V)^2.
 
-The exact template (the GPU ``partial_cmd_smooth``) is both the judge and the fallback.
-Judge: Poisson deviance per star, D = 2 sum(e - t + t log(t/e)) / sum(t).  Routing: a
-held-out validation set is scored by the judge and the worst deviance seen in each cell
+The exact template (the GPU ``partial_cmd_smooth``) is both the arbiter and the fallback.
+Score: Poisson deviance per star, D = 2 sum(e - t + t log(t/e)) / sum(t).  Routing: a
+held-out validation set is scored by that deviance and the worst deviance seen in each cell
 of a coarse grid over theta is kept (the trust map); a requested template is emulated
 only when its cell was validated and its worst deviance is within tolerance, and is
 built exactly otherwise.  ``templates(..., audit=True)`` instead builds every exact
@@ -19,7 +19,7 @@ template as well and falls back per template.
 Everything heavy runs in libsfhgpu.so: template generation, the transform and
 centring, the GEMMs of the randomized range finder (Halko, Martinsson & Tropp 2011,
 Alg. 4.4 with power iterations), projection, training, inference, reconstruction and
-the judge.  The host does only the small QR / SVD of the range finder (L x L and
+the deviance score.  The host does only the small QR / SVD of the range finder (L x L and
 n x L factors, L = K + 16) and bookkeeping.
 """
 from __future__ import annotations
@@ -95,7 +95,7 @@ class EmulatorReport:
 
 
 class TemplateEmulator:
-    """MLP + PCA template emulator with exact-template judge and fallback."""
+    """MLP + PCA template emulator with exact-template arbiter and fallback."""
 
     def __init__(self, nbins, ncomp=64, hidden=(256, 256),
                  bounds=((6.6, 10.1), (-2.5, 0.3), (24.0, 30.0)), mode=MODE_SQRT,
@@ -233,7 +233,7 @@ class TemplateEmulator:
         """Generate n_train exact templates on the device, build the PCA basis (global, or
         one per basis cell), train the MLP(s) (Adam, cosine-decayed from lr to lr_final over
         `steps` in `segments` calls; global: `batch` rows per step, local: `batch_per_cell`
-        rows per cell per step), then score n_val fresh templates with the judge to build
+        rows per cell per step), then score n_val fresh templates by deviance to build
         the trust map."""
         torch = _torch()
         L = load()
@@ -288,7 +288,7 @@ class TemplateEmulator:
         t_train = time.perf_counter() - t0
         tr = trace[:steps].cpu().numpy()
 
-        # judge on a held-out set -> trust map
+        # score on a held-out set -> trust map
         th_val = self.sample_theta(n_val, rng)
         dev = self.deviance(th_val, generator(th_val))
         self._build_trust(th_val, dev)
@@ -317,7 +317,7 @@ class TemplateEmulator:
         self._sync_ctx()
         Ah = A.cpu().numpy().astype(np.float64)
         # one common scale for all components: the MSE is then proportional to the
-        # squared error in sqrt-template space, which is what the deviance judge sees
+        # squared error in sqrt-template space, which is what the deviance score sees
         cmu = Ah.mean(0)
         s = float(np.sqrt(np.mean(Ah.var(0)))) or 1.0
         Vh = V.cpu().numpy().astype(np.float64)
@@ -421,7 +421,7 @@ class TemplateEmulator:
         self._sync_ctx()
         return out
 
-    def judge(self, exact, emul):
+    def deviance(self, exact, emul):
         """Poisson deviance per star of each emulated row against the exact row (numpy)."""
         torch = _torch()
         B = exact.shape[0]
@@ -434,7 +434,7 @@ class TemplateEmulator:
         return d.cpu().numpy()
 
     def deviance(self, theta, exact):
-        return self.judge(exact, self.predict(theta))
+        return self.deviance(exact, self.predict(theta))
 
     # ------------------------------------------------------------------ routing
     def _cell(self, theta):
@@ -458,13 +458,13 @@ class TemplateEmulator:
 
     def templates(self, theta, generator, audit=False):
         """Templates for theta (B x 3): emulated where trusted, exact elsewhere.  With
-        audit=True every exact template is built too and each emulated one that the judge
+        audit=True every exact template is built too and each emulated one that the deviance score
         rejects is replaced.  Returns (templates (device B x nbins), emulated mask)."""
         theta = np.asarray(theta, dtype=np.float64).reshape(-1, 3)
         out = self.predict(theta)
         if audit:
             exact = generator(theta)
-            dev = self.judge(exact, out)
+            dev = self.deviance(exact, out)
             use = dev <= self.tol
         else:
             use = self.trusted(theta)

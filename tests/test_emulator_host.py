@@ -1,6 +1,6 @@
 """CPU checks of the learned emulator's test infrastructure and host logic: the FP64 MLP
 restatement's analytic gradient against central finite differences, its BF16 operand
-rounding, the Poisson-deviance judge, and the emulator's routing bookkeeping."""
+rounding, the Poisson-deviance score, and the emulator's routing bookkeeping."""
 import numpy as np
 import pytest
 
