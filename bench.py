@@ -350,7 +350,7 @@ def run_emulator(ctx, w, n_train=100_000, n_val=4096, steps=4000, cells=(8, 2, 1
     emul = em.predict(th)
     torch.cuda.synchronize()
     t_emul = time.perf_counter() - t0
-    dev = em.deviance(exact, emul)
+    dev = em.score(exact, emul)
     trusted = em.trusted(th)
     em.templates(th[:8], gen)  # first use of the routing path (indexed copy kernel)
     torch.cuda.synchronize()

@@ -421,7 +421,7 @@ class TemplateEmulator:
         self._sync_ctx()
         return out
 
-    def deviance(self, exact, emul):
+    def score(self, exact, emul):
         """Poisson deviance per star of each emulated row against the exact row (numpy)."""
         torch = _torch()
         B = exact.shape[0]
@@ -434,7 +434,7 @@ class TemplateEmulator:
         return d.cpu().numpy()
 
     def deviance(self, theta, exact):
-        return self.deviance(exact, self.predict(theta))
+        return self.score(exact, self.predict(theta))
 
     # ------------------------------------------------------------------ routing
     def _cell(self, theta):
@@ -464,7 +464,7 @@ class TemplateEmulator:
         out = self.predict(theta)
         if audit:
             exact = generator(theta)
-            dev = self.deviance(exact, out)
+            dev = self.score(exact, out)
             use = dev <= self.tol
         else:
             use = self.trusted(theta)

@@ -234,9 +234,9 @@ def test_trained_network_beats_the_method_without_it(trained, torch):
     exact = gen(th)
     torch.cuda.synchronize()
     emul = em.predict(th)
-    d_net = em.deviance(exact, emul)
+    d_net = em.score(exact, emul)
     mean_tpl = em.offset.clamp_min(0) ** 2 if em.mode == 1 else em.offset.clamp_min(0)
-    d_mean = em.deviance(exact, mean_tpl.expand(th.shape[0], -1).contiguous())
+    d_mean = em.score(exact, mean_tpl.expand(th.shape[0], -1).contiguous())
     assert np.median(d_net) < 0.2 * np.median(d_mean)
     t0 = time.perf_counter()
     gen(th)
@@ -255,7 +255,7 @@ def test_routing_falls_back_to_exact_templates(trained, torch):
     th = em.sample_theta(300, rng)
     out, used = em.templates(th, gen, audit=True)
     exact = gen(th)
-    d = em.deviance(exact, em.predict(th))
+    d = em.score(exact, em.predict(th))
     assert np.array_equal(used, d <= em.tol)
     # exact templates are reproducible up to the summation order of the stamps' atomics
     def same(a, b):
@@ -266,7 +266,7 @@ def test_routing_falls_back_to_exact_templates(trained, torch):
         assert same(out[bad], exact[bad])
     good = np.nonzero(used)[0]
     if good.size:
-        assert np.all(em.deviance(exact[good].contiguous(), out[good].contiguous()) <= em.tol)
+        assert np.all(em.score(exact[good].contiguous(), out[good].contiguous()) <= em.tol)
     # trust-map routing: untrusted cells get exact templates
     out2, used2 = em.templates(th, gen)
     assert np.array_equal(used2, em.trusted(th))
@@ -389,13 +389,13 @@ def test_local_bases_beat_the_global_basis(trained, trained_local, torch):
     rng = np.random.default_rng(99)
     th = em_g.sample_theta(1024, rng)
     exact = gen(th)
-    d_g = em_g.deviance(exact, em_g.predict(th))
-    d_l = em_l.deviance(exact, em_l.predict(th))
+    d_g = em_g.score(exact, em_g.predict(th))
+    d_l = em_l.score(exact, em_l.predict(th))
     assert np.median(d_l) < 0.5 * np.median(d_g)
     # and the local networks beat the local mean templates (no network)
     grp = torch.as_tensor(em_l.group_of(th), device=exact.device)
     y = em_l.offset[grp].clamp_min(0)
-    d_mean = em_l.deviance(exact, (y * y).contiguous())
+    d_mean = em_l.score(exact, (y * y).contiguous())
     assert np.median(d_l) < 0.2 * np.median(d_mean)
 
 
@@ -405,7 +405,7 @@ def test_local_routing_falls_back_to_exact_templates(trained_local, torch):
     th = em.sample_theta(200, rng)
     out, used = em.templates(th, gen, audit=True)
     exact = gen(th)
-    d = em.deviance(exact, em.predict(th))
+    d = em.score(exact, em.predict(th))
     assert np.array_equal(used, d <= em.tol)
     bad = np.nonzero(~used)[0]
     if bad.size:
