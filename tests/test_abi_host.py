@@ -33,6 +33,25 @@ def test_library_exports_every_declared_symbol():
     del ctypes
 
 
+def test_entry_points_reject_missing_arguments_without_a_gpu():
+    """Argument validation runs before any CUDA call: a NULL context or output is
+    SFH_ERR_ARG (1) for the hard-binning, mock-observation and fit entry points."""
+    import ctypes as C
+    import sfhgpu
+    from sfhgpu._lib import FitOptions, FitResult
+    L = sfhgpu.load()
+    n = C.c_int64()
+    assert L.sfh_bin_cmd(None, None, None, None, 0, None, 1, None, 1, None) == 1
+    assert L.sfh_bin_cmd_dev(None, None, None, None, 0, None, 1, None, 1, None) == 1
+    assert L.sfh_model_cmd(None, None, None, None, None, 0, 1, 0, None, None, C.byref(n)) == 1
+    assert L.sfh_model_cmd_dev(None, None, None, None, None, 0, 1, 0, None, None, C.byref(n)) == 1
+    opt, res = FitOptions(), FitResult()
+    assert L.sfh_fit_bfgs(None, None, None, None, C.byref(opt), None, None, C.byref(res)) == 1
+    assert L.sfh_fit_bfgs_dev(None, None, None, None, C.byref(opt), None, None, C.byref(res)) == 1
+    assert L.sfh_models_set_onepass_run(None, None, 4) == 1
+    assert L.sfh_models_set_onepass_schedule(None, None, 1) == 1
+
+
 def test_host_mini_spacing_and_interpolation_match_oracle(O):
     from sfhgpu import synthetic as S
     from sfhgpu import templates as T
