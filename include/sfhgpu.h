@@ -229,14 +229,18 @@ int sfh_models_autotune(sfh_ctx *ctx, sfh_models *models, const double *d_coeffs
 /* fg! for callers that cannot allocate device memory (no counterpart in the
    reference): graph-capture regions that must not allocate, plugins inside a host
    application that owns the device memory budget, allocation-free real-time loops.
-   Same result as sfh_fg_dev on FP32 templates, but all scratch lives in one fixed
-   11 MiB device array inside the library, so the call allocates nothing: the caller
-   passes the (nbins, ntempl) column-major FP32 templates, every input and output,
-   and the stream.  Limits: nbins <= 131072 and ntempl <= 4096 (SFH_ERR_SHAPE beyond).
-   The first call on each device looks up the array's device address; make that
-   first call before any stream capture.  All calls share the one array, so calls
-   that overlap on the GPU (different streams, or different host threads) race:
-   serialise them on one stream.  d_G and d_negLogL may be NULL as in sfh_fg_dev. */
+   Same result as sfh_fg_dev on FP32 templates, computed by the two-pass FP32 plan
+   (sfh_fg_dev prefers the one-pass kernel, whose blocked template copy is an
+   allocation, so this entry is about 1.6x slower on large matrices).  All scratch
+   lives in one fixed 11 MiB device array inside the library, so the call allocates
+   nothing: the caller passes the (nbins, ntempl) column-major FP32 templates (any
+   float-aligned address), every input and output, and the stream.  Limits:
+   nbins <= 131072 and ntempl <= 4096 (SFH_ERR_SHAPE beyond).  The first call in each
+   CUDA context looks up the array's device address in that context (the address is
+   cached per context); make that first call before any stream capture.  All calls
+   share the one array, so calls that overlap on the GPU (different streams, or
+   different host threads) race: serialise them on one stream.  d_G and d_negLogL may
+   be NULL as in sfh_fg_dev. */
 int sfh_fg_dev_noalloc(void *stream, const float *d_models, int64_t nbins, int64_t ntempl,
                        const double *d_coeffs, const double *d_data, double *d_composite,
                        double *d_G, double *d_negLogL, double eps);

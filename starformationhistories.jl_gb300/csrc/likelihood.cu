@@ -1068,10 +1068,14 @@ int sfh_launch_loglikelihood(sfh_ctx *ctx, const double *composite, const double
 // Some callers cannot call cudaMalloc at all: code running inside a CUDA-graph
 // capture that must not allocate, plugins living inside a host application that
 // owns the device memory budget (and forbids side allocations), or real-time loops
-// where an allocation could stall.  sfh_fg_dev_noalloc serves them: it runs the same
-// four kernels as sfh_fg_dev, but its scratch is this fixed, file-scope device array,
-// so the call itself allocates nothing.  The array is 11 MiB and is held by every GPU
-// that loads the library until the process exits.
+// where an allocation could stall.  sfh_fg_dev_noalloc serves them with the two-pass
+// FP32 plan (m = M r with the Poisson terms and w, then G = -Mᵀ w): the same
+// arithmetic as sfh_fg_dev's two-pass path, but not the one-pass kernel that
+// sfh_fg_dev prefers for FP32 storage (that kernel keeps a blocked copy of the
+// templates, an allocation), so on the production matrix it is about 1.6x slower
+// than sfh_fg_dev.  Its scratch is this fixed, file-scope device array, so the call
+// itself allocates nothing.  The array is 11 MiB and is held by every GPU that loads
+// the library until the process exits.
 namespace {
 constexpr int64_t kNoAllocMaxBins = 131072;  // e.g. a 362 x 362 Hess grid
 constexpr int64_t kNoAllocMaxTempl = 4096;
@@ -1079,8 +1083,28 @@ constexpr int kNoAllocMaxSplit = 8;
 constexpr size_t kNoAllocBytes = 11u << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
+// The array's device address differs per CUDA context (a host application may create
+// its own driver-API contexts, and a reset device gets a new primary context), so the
+// looked-up address is cached per context, not per device ordinal.
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+CtxGetCurrentFn ctx_get_current() {
+    static CtxGetCurrentFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (CtxGetCurrentFn)p;
+    }
+    return fn;
+}
+constexpr int kNoAllocCtxSlots = 64;
 std::mutex g_noalloc_mu;
-void *g_noalloc_ptr[64] = {nullptr};
+CUcontext g_noalloc_ctx[kNoAllocCtxSlots] = {nullptr};
+void *g_noalloc_ptr[kNoAllocCtxSlots] = {nullptr};
 }  // namespace
 
 extern "C" int sfh_fg_dev_noalloc(void *stream, const float *d_models, int64_t nbins,
@@ -1092,20 +1116,36 @@ extern "C" int sfh_fg_dev_noalloc(void *stream, const float *d_models, int64_t n
     if (nbins > kNoAllocMaxBins || ntempl > kNoAllocMaxTempl)
         return SFH_ERR_SHAPE;  // beyond the fixed scratch: use sfh_fg_dev instead
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return SFH_ERR_CUDA;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return SFH_ERR_CUDA;
+    // The context current on this thread (the caller's, or the runtime's primary
+    // context, which cudaSetDevice binds to a thread that has not used it yet).
+    CtxGetCurrentFn get_ctx = ctx_get_current();
+    CUcontext cu = nullptr;
+    if (!get_ctx || get_ctx(&cu) != CUDA_SUCCESS) return SFH_ERR_CUDA;
+    if (!cu) {
+        if (cudaSetDevice(dev) != cudaSuccess) return SFH_ERR_CUDA;
+        if (get_ctx(&cu) != CUDA_SUCCESS || !cu) return SFH_ERR_CUDA;
+    }
     void *base = nullptr;
     {
-        // First call on this device: resolve the device address of the array (the
+        // First call in this context: resolve the device address of the array (the
         // host-side symbol is only a stand-in).  Make that first call outside any
         // stream capture.
         std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (!g_noalloc_ptr[dev]) {
-            if (cudaGetSymbolAddress(&g_noalloc_ptr[dev], g_noalloc_scratch) != cudaSuccess) {
-                g_noalloc_ptr[dev] = nullptr;
-                return SFH_ERR_CUDA;
-            }
+        int slot = -1, free_slot = -1;
+        for (int k = 0; k < kNoAllocCtxSlots; ++k) {
+            if (g_noalloc_ctx[k] == cu) { slot = k; break; }
+            if (!g_noalloc_ctx[k] && free_slot < 0) free_slot = k;
         }
-        base = g_noalloc_ptr[dev];
+        if (slot < 0) {
+            if (free_slot < 0) return SFH_ERR_CUDA;  // more than 64 live contexts
+            void *p = nullptr;
+            if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return SFH_ERR_CUDA;
+            g_noalloc_ctx[free_slot] = cu;
+            g_noalloc_ptr[free_slot] = p;
+            slot = free_slot;
+        }
+        base = g_noalloc_ptr[slot];
     }
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
@@ -1145,7 +1185,11 @@ extern "C" int sfh_fg_dev_noalloc(void *stream, const float *d_models, int64_t n
 
     dim3 grid(nrowblk, ksplit);
     const size_t sm_n = 2 * (size_t)kchunk * sizeof(float);
-    if (nbins % 4 == 0)
+    // The float4 loads need every column to start on a 16-byte boundary: nbins a
+    // multiple of 4 and a 16-byte-aligned base.  A caller's pointer is only known to be
+    // float-aligned (a sliced or offset view), so check it.
+    const bool vec = (nbins % 4 == 0) && (((uintptr_t)d_models & 15) == 0);
+    if (vec)
         k_gemv_n_f32<true><<<grid, kThreads, sm_n, st>>>(d_models, nbins, ntempl, d_coeffs, kchunk,
                                                          part);
     else
@@ -1174,7 +1218,7 @@ extern "C" int sfh_fg_dev_noalloc(void *stream, const float *d_models, int64_t n
     if (!want_g) return SFH_OK;
     dim3 gridt(ncolgroups, nchunks);
     const size_t sm_t = 2 * (size_t)R * sizeof(float);
-    if (nbins % 4 == 0)
+    if (vec)
         k_gemv_t_f32<true><<<gridt, kThreads, sm_t, st>>>(d_models, nbins, ntempl, w32, R, cb,
                                                           ncolgroups, partG);
     else

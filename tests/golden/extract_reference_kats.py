@@ -1,16 +1,20 @@
 """Extract the known-answer values of StarFormationHistories.jl's own tests and
 doctests into reference_kats.json.
 
-Run in the build container, where the reference checkout exists; the JSON it
-writes is committed so tests need no access to the reference at run time.
-Each value is read as text from the file:line recorded beside it.
+Usage: python extract_reference_kats.py <path of a StarFormationHistories.jl checkout>
+
+Run where a reference checkout exists; the JSON it writes is committed so tests
+need no access to the reference at run time.  Each value is read as text from the
+file:line recorded beside it.
 """
 import json
 import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    raise SystemExit("usage: python extract_reference_kats.py <reference checkout>")
+REF = sys.argv[1]
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_kats.json")
 
 

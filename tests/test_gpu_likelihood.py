@@ -92,7 +92,7 @@ def test_fg_against_oracle(sfh, O, nbins, nt, storage):
     np.testing.assert_allclose(comp, w_ref, rtol=rt, atol=rt)
     # logL: deviation per 1e4 stars
     nst = data.sum()
-    tol = (1e-9 if storage == "f64" else 1e-5) * max(1.0, nst / 1e4)
+    tol = (1e-9 if storage == "f64" else 1e-6) * max(1.0, nst / 1e4)
     assert abs(v - v_ref) <= tol, (v, v_ref)
     # gradient: relative to the natural scale sum_i |M_ij w_i|
     scale = np.abs(Mst).T @ np.abs(w_ref) + 1e-300
@@ -188,6 +188,6 @@ def test_autotuned_plan_keeps_parity(sfh, O):
     v = sfh.fg_(True, G, r, H, data, comp)
     Mst = M.astype(np.float32).astype(np.float64)
     v_ref, G_ref, w_ref = O.fg(r, Mst, data)
-    assert abs(v - v_ref) <= 1e-5 * max(1.0, data.sum() / 1e4)
+    assert abs(v - v_ref) <= 1e-6 * max(1.0, data.sum() / 1e4)
     scale = np.abs(Mst).T @ np.abs(w_ref) + 1e-300
     assert np.max(np.abs(G - G_ref) / scale) <= 2e-6
