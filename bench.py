@@ -136,7 +136,7 @@ def _bf16_peak():
         return 1900.0, "fallback"
 
 
-def run_batched(ctx, d_T, nbins, nt, r, data, M64, steps, warmup, B=4096, check=2):
+def run_batched(ctx, d_T, nbins, nt, r, data, M64, steps, warmup, B=4096, check=8):
     """Many coefficient vectors per call on the tensor cores (sfh_fg_batched_dev)."""
     import numpy as np
     import torch
@@ -168,16 +168,20 @@ def run_batched(ctx, d_T, nbins, nt, r, data, M64, steps, warmup, B=4096, check=
     # outputs for the accuracy check against the FP64 oracle, done in the CPU leg
     check_data = {"R": R[:check], "negL": negL[:check]}
     nst = float(data.sum())
-    flops = 4.0 * nbins * nt * B  # two GEMMs, algorithmic (the hi/lo split triples tensor work)
+    # algorithmic FLOPs: the two products C = R M^T and G = W M, 2 nbins nt B each; the
+    # digit-plane products of the exact composite and the hi/lo products of G are
+    # implementation work and are not counted
+    flops = 4.0 * nbins * nt * B
     peak, kind = _bf16_peak()
     Hb.free()
     return {
         "workload": f"{B} coefficient vectors x {nt} templates x {nbins} bins (one call)",
         "evals_per_s": B / (ms / 1e3), "ms_per_batch": ms, "B": B, "steps": steps,
+        "composite": "exact digit planes (logL), BF16 hi/lo products for G = W M",
         "tensor_roofline": {"bound": "tensor", "achieved": flops / (ms / 1e3) / 1e12,
-                            "achieved_with_hilo": 3 * flops / (ms / 1e3) / 1e12, "peak": peak,
-                            "unit": "TFLOP/s", "frac": 3 * flops / (ms / 1e3) / 1e12 / peak,
-                            "peak_source": kind},
+                            "peak": peak, "unit": "TFLOP/s",
+                            "frac": flops / (ms / 1e3) / 1e12 / peak, "peak_source": kind,
+                            "flops": "algorithmic: 4 nbins nt B per call"},
         "_check": check_data,
     }
 
@@ -549,18 +553,11 @@ def oracle_checks(batched, ragged, M64, r, data, neglogl):
              "negLogL_oracle": v_ref}
     if batched and "_check" in batched:
         c = batched.pop("_check")
-        Mt = torch.tensor(M64)
-        hi = Mt.float().to(torch.bfloat16).double()
-        Ms = np.asfortranarray((hi + (Mt - hi).float().to(torch.bfloat16).double()).numpy())
-        Rt = torch.tensor(c["R"])
-        rh = Rt.float().to(torch.bfloat16).double()
-        Rs = (rh + (Rt - rh).float().to(torch.bfloat16).double()).numpy()
-        ref_s, _ = O.fg_batched(Rs, Ms, data, nthreads=thr, want_g=False)
+        # FP64 oracle on the stored FP32 templates and the exact FP64 coefficient vectors
         ref_f, _ = O.fg_batched(c["R"], M64, data, nthreads=thr, want_g=False)
-        batched["dlogL_per_1e4_stars_vs_stored"] = float(
-            np.max(np.abs(c["negL"] - ref_s)) / (nst / 1e4))
-        batched["dlogL_per_1e4_stars_vs_fp32_templates"] = float(
+        batched["dlogL_per_1e4_stars_vs_oracle"] = float(
             np.max(np.abs(c["negL"] - ref_f)) / (nst / 1e4))
+        batched["vectors_checked"] = int(len(c["negL"]))
     if ragged and "_check" in ragged:
         err_l, err_g = 0.0, 0.0
         for Mg, rg, ng, negl, Gg in ragged.pop("_check"):

@@ -548,7 +548,9 @@ int sfh_batched_prepare(sfh_ctx *ctx, const sfh_models *m, int64_t B, const doub
     const size_t o_gp = o_lp + sz_lp, sz_gp = sfh_align256((size_t)P.ks2 * B_pad * nt * sizeof(float));
     const size_t o_data = o_gp + sz_gp, sz_data = sfh_align256((size_t)nbins * sizeof(float));
     const size_t o_err = o_data + sz_data;
-    P.scratch_bytes = o_err + 256;
+    P.exact = sfh_exact_supported(m);
+    const size_t o_x = o_err + 256;
+    P.scratch_bytes = o_x + (P.exact ? sfh_exact_scratch(m, B, nullptr) : 0);
     if (!scratch) {  // size query
         *pl = P;
         return SFH_OK;
@@ -563,13 +565,15 @@ int sfh_batched_prepare(sfh_ctx *ctx, const sfh_models *m, int64_t B, const doub
     P.gp = (float *)(s + o_gp);
     P.dataf = (float *)(s + o_data);
     P.err = (int *)(s + o_err);
+    P.data = d_data;
+    int rc;
+    if (P.exact && (rc = sfh_exact_prepare(ctx, m, B, s + o_x, &P.xp))) return rc;
     cudaStream_t st = ctx->stream;
     SFH_CK(ctx, cudaMemsetAsync(P.err, 0, sizeof(int), st));
     // data as FP32 (counts are exact below 2^24)
     k_f64_to_f32<<<(unsigned)((nbins + 255) / 256), 256, 0, st>>>(d_data, P.dataf, nbins);
     SFH_LAUNCHED(ctx);
     CUtensorMap *mp = P.maps;
-    int rc;
     if ((rc = make_map(ctx, &mp[0], P.Rh, B_pad, ntp, ntp, BM))) return rc;
     if ((rc = make_map(ctx, &mp[1], P.Rl, B_pad, ntp, ntp, BM))) return rc;
     if ((rc = make_map(ctx, &mp[2], m->row_hi, nbins, ntp, ntp, BN))) return rc;
@@ -588,13 +592,19 @@ int sfh_batched_launch(sfh_ctx *ctx, const sfh_models *m, const SfhBatchedPlan &
     const int64_t B = pl.B, B_pad = pl.B_pad;
     const bool want_g = d_G != nullptr, want_l = d_negLogL != nullptr;
     cudaStream_t st = ctx->stream;
-    {
+    if (!(want_l && pl.exact)) {
         const int64_t n = B_pad * ntp;
         k_split_coeffs<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_R, B, nt, B_pad, ntp, pl.Rh,
                                                                     pl.Rl);
         SFH_LAUNCHED(ctx);
     }
     int rc;
+    if (want_l && pl.exact) {
+        // composite, Poisson terms and w from the exact digit planes (GEMM 1 done)
+        if ((rc = sfh_exact_launch(ctx, m, pl.xp, d_R, pl.data, d_negLogL, pl.Wh, pl.Wl, nbp,
+                                   want_g ? 1 : 0, eps, pl.err)))
+            return rc;
+    } else {
     GemmParams P1{};
     P1.m_tiles = pl.m_tiles;
     P1.n_tiles = pl.n_tiles1;
@@ -619,6 +629,7 @@ int sfh_batched_launch(sfh_ctx *ctx, const sfh_models *m, const SfhBatchedPlan &
         k_logl_reduce<<<(unsigned)((B + 255) / 256), 256, 0, st>>>(pl.lp, 2 * pl.n_tiles1, (int)B,
                                                                    (int)B_pad, d_negLogL);
         SFH_LAUNCHED(ctx);
+    }
     }
     if (want_g) {
         GemmParams P2{};

@@ -150,6 +150,9 @@ static void free_models(sfh_models *m) {
     if (m->row_lo) cudaFree(m->row_lo);
     for (float *b : m->d_blk)
         if (b) cudaFree(b);
+    if (m->d_rowb) cudaFree(m->d_rowb);
+    if (m->digits) cudaFree(m->digits);
+    if (m->escale) cudaFree(m->escale);
     delete m;
 }
 
@@ -167,13 +170,43 @@ extern "C" int sfh_models_info(const sfh_models *m, int64_t *nbins, int64_t *nt,
     return SFH_OK;
 }
 
+namespace {
+// One thread per bin: (sum, max) of |M_ij| over j (a warp reads 32 consecutive bins of a
+// column: coalesced).  The sum is an FP32 sum of nonnegative terms (relative rounding below
+// nt 2^-24, covered by the inflation in sfh_row_bound).
+__global__ void k_row_stats(const float *__restrict__ M, int64_t nbins, int64_t nt,
+                            float2 *__restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nbins) return;
+    float s = 0.f, mx = 0.f;
+    for (int64_t j = 0; j < nt; ++j) {
+        const float v = fabsf(__ldg(M + j * nbins + i));
+        s += v;
+        mx = fmaxf(mx, v);
+    }
+    // rounding of a long FP32 sum: bound it from above by the max times the count too
+    out[i] = make_float2(fminf(s * (1.0f + 1e-3f), mx * (float)nt), mx);
+}
+}  // namespace
+
+int sfh_row_stats(sfh_ctx *ctx, const float *d_M, int64_t nbins, int64_t nt, float2 *d_out) {
+    k_row_stats<<<(unsigned)((nbins + 255) / 256), 256, 0, ctx->stream>>>(d_M, nbins, nt, d_out);
+    SFH_LAUNCHED(ctx);
+    return SFH_OK;
+}
+
 // Finishes a handle whose FP32 column-major copy is in m->d_f32.
 static int finish_models(sfh_ctx *ctx, sfh_models *m) {
+    SFH_CK(ctx, cudaMalloc(&m->d_rowb, (size_t)m->nbins * sizeof(float2)));
+    int rc0 = sfh_row_stats(ctx, m->d_f32, m->nbins, m->nt, m->d_rowb);
+    if (rc0 != SFH_OK) return rc0;
     if (m->storage == SFH_F32) {
         m->d_col = m->d_f32;
     } else if (m->storage == SFH_BF16X2) {
         int rc = sfh_build_bf16_planes(ctx, m, m->d_f32);
         if (rc != SFH_OK) return rc;
+        // digit planes of the exact logL path (batched_exact.cu)
+        if ((rc = sfh_build_digit_planes(ctx, m)) != SFH_OK) return rc;
     }
     return SFH_OK;
 }

@@ -13,9 +13,10 @@
 //               block/last-block reduction, w_i = 1 - n_i/max(m_i, eps)
 //   k_gemv_t  : G_j partials over row chunks, w staged in shared memory
 //   k_reduce_g: fixed-order sum of the G partials
-// FP32 storage multiplies by r = r_hi + r_lo (two FP32 products) and accumulates
-// short FP32 chunks into a compensated FP32 pair, so the composite carries
-// ~1e-8 relative error against FP64 arithmetic on the same stored templates.
+// FP32 storage multiplies by r = r_hi + r_lo (two FP32 products) and accumulates the
+// products error-free against a power-of-two anchor per bin (sfh_anc_acc), so the
+// composite carries ~1e-12 relative error against FP64 arithmetic on the same stored
+// templates.
 // k_gemv_t walks template columns in the reverse of k_gemv_n's launch order so
 // the tail of M that k_gemv_n streamed last is still resident in L2.
 #include <cuda_runtime.h>
@@ -46,6 +47,10 @@ __device__ __forceinline__ float4 ld_stream4(const float *p) {
 }
 
 // ---------------------------------------------------------------- k_gemv_n (FP32 storage)
+// Groups of 8 template rows are summed error-free against a power-of-two anchor taken
+// from the group's own bound sum |M_ij| |r_j| (sfh_anc_acc: no row statistics needed, so
+// this kernel also serves callers without a models handle); the groups fold into a
+// compensated FP32 pair.
 template <bool VEC>
 __global__ void __launch_bounds__(kThreads)
 k_gemv_n_f32(const float *__restrict__ M, int64_t nbins, int64_t nt,
@@ -64,73 +69,50 @@ k_gemv_n_f32(const float *__restrict__ M, int64_t nbins, int64_t nt,
     __syncthreads();
     const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * 4;
     if (i >= nbins) return;
+    const int nr = VEC ? 4 : (int)min((int64_t)4, nbins - i);
     float ah[4] = {0.f, 0.f, 0.f, 0.f}, al[4] = {0.f, 0.f, 0.f, 0.f};
     const float *colp = M + j0 * nbins + i;
-    int k = 0;
-    if (VEC) {
-        for (; k + 8 <= kn; k += 8) {
-            float4 v[8];
+    for (int k = 0; k < kn; k += 8) {
+        const int kk = min(8, kn - k);
+        float m[8][4];
+        if (VEC) {
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (u < kk) v = __ldg(reinterpret_cast<const float4 *>(colp + (int64_t)(k + u) * nbins));
+                m[u][0] = v.x;
+                m[u][1] = v.y;
+                m[u][2] = v.z;
+                m[u][3] = v.w;
+            }
+        } else {
 #pragma unroll
             for (int u = 0; u < 8; ++u)
-                v[u] = __ldg(reinterpret_cast<const float4 *>(colp + (int64_t)(k + u) * nbins));
-            float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const float h = rhi[k + u], l = rlo[k + u];
-                s0 = fmaf(v[u].x, h, fmaf(v[u].x, l, s0));
-                s1 = fmaf(v[u].y, h, fmaf(v[u].y, l, s1));
-                s2 = fmaf(v[u].z, h, fmaf(v[u].z, l, s2));
-                s3 = fmaf(v[u].w, h, fmaf(v[u].w, l, s3));
-            }
-            two_sum_acc(ah[0], al[0], s0);
-            two_sum_acc(ah[1], al[1], s1);
-            two_sum_acc(ah[2], al[2], s2);
-            two_sum_acc(ah[3], al[3], s3);
-        }
-        for (; k < kn; ++k) {
-            const float4 v = __ldg(reinterpret_cast<const float4 *>(colp + (int64_t)k * nbins));
-            const float h = rhi[k], l = rlo[k];
-            two_sum_acc(ah[0], al[0], fmaf(v.x, h, v.x * l));
-            two_sum_acc(ah[1], al[1], fmaf(v.y, h, v.y * l));
-            two_sum_acc(ah[2], al[2], fmaf(v.z, h, v.z * l));
-            two_sum_acc(ah[3], al[3], fmaf(v.w, h, v.w * l));
-        }
-        double *dst = part + (int64_t)split * nbins + i;
-        dst[0] = (double)ah[0] + (double)al[0];
-        dst[1] = (double)ah[1] + (double)al[1];
-        dst[2] = (double)ah[2] + (double)al[2];
-        dst[3] = (double)ah[3] + (double)al[3];
-    } else {
-        const int nr = (int)min((int64_t)4, nbins - i);
-        for (; k + 8 <= kn; k += 8) {
-            float s[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const float h = rhi[k + u], l = rlo[k + u];
-                const float *c = colp + (int64_t)(k + u) * nbins;
 #pragma unroll
                 for (int q = 0; q < 4; ++q)
-                    if (q < nr) {
-                        const float x = __ldg(c + q);
-                        s[q] = fmaf(x, h, fmaf(x, l, s[q]));
-                    }
-            }
-#pragma unroll
-            for (int q = 0; q < 4; ++q) two_sum_acc(ah[q], al[q], s[q]);
+                    m[u][q] = (u < kk && q < nr) ? __ldg(colp + (int64_t)(k + u) * nbins + q) : 0.f;
         }
-        for (; k < kn; ++k) {
-            const float h = rhi[k], l = rlo[k];
-            const float *c = colp + (int64_t)k * nbins;
+        float hv[8], lv[8];
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
-                if (q < nr) {
-                    const float x = __ldg(c + q);
-                    two_sum_acc(ah[q], al[q], fmaf(x, h, x * l));
-                }
+        for (int u = 0; u < 8; ++u) {
+            hv[u] = u < kk ? rhi[k + u] : 0.f;
+            lv[u] = u < kk ? rlo[k + u] : 0.f;
         }
-        double *dst = part + (int64_t)split * nbins + i;
-        for (int q = 0; q < nr; ++q) dst[q] = (double)ah[q] + (double)al[q];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            float b = 0.f;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) b = fmaf(fabsf(m[u][q]), fabsf(hv[u]), b);
+            const float sg = sfh_anchor(b * 1.0009765625f);
+            float a = sg, lo = 0.f;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) sfh_anc_acc(a, lo, m[u][q], hv[u], lv[u]);
+            two_sum_acc(ah[q], al[q], __fsub_rn(a, sg));
+            al[q] = __fadd_rn(al[q], lo);
+        }
     }
+    double *dst = part + (int64_t)split * nbins + i;
+    for (int q = 0; q < nr; ++q) dst[q] = (double)ah[q] + (double)al[q];
 }
 
 // ---------------------------------------------------------------- k_gemv_n (FP64 storage)
@@ -375,6 +357,7 @@ struct Pass1Args {
     double *negLogL;
     const sfh_df *tab;  // log table of the double-float Poisson terms
     float eps_f;        // eps(T) (a power of two) in FP32
+    const float2 *rowb; // per bin (sum, max) of |M_ij|: the accumulation anchors' bound
 };
 
 __device__ __forceinline__ void block_sum_to(double v, double *s_red, double *out_tid0) {
@@ -402,63 +385,86 @@ __global__ void __launch_bounds__(kThreads) k_fg_pass1_f32(Pass1Args a) {
     const int nsplit = gridDim.x, ntile = gridDim.y;
     const int64_t j0 = (int64_t)split * a.kchunk;
     const int kn = (int)min((int64_t)a.kchunk, a.nt - j0);
+    float rmx = 0.f, rsm = 0.f;
     for (int t = threadIdx.x; t < kn; t += blockDim.x) {
         const double v = a.r[j0 + t];
         const float h = __double2float_rn(v);
         rhi[t] = h;
         rlo[t] = __double2float_rn(v - (double)h);
+        rmx = fmaxf(rmx, fabsf(h));
+        rsm += fabsf(h);
+    }
+    // the chunk's max and sum of |r| for the anchors' bound
+    __shared__ float s_rs[2][kThreads / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        rmx = fmaxf(rmx, __shfl_xor_sync(0xffffffffu, rmx, o));
+        rsm += __shfl_xor_sync(0xffffffffu, rsm, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        s_rs[0][threadIdx.x >> 5] = rmx;
+        s_rs[1][threadIdx.x >> 5] = rsm;
     }
     __syncthreads();
+    float rmax = 0.f, rsum = 0.f;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) {
+        rmax = fmaxf(rmax, s_rs[0][w]);
+        rsum += s_rs[1][w];
+    }
     const int64_t nbins = a.nbins;
     const int64_t i = ((int64_t)tile * blockDim.x + threadIdx.x) * 4;
     if (i < nbins) {
-        float ah[4] = {0.f, 0.f, 0.f, 0.f}, al[4] = {0.f, 0.f, 0.f, 0.f};
+        // m r over the chunk, accumulated against each bin's power-of-two anchor (error-free
+        // up to ~2^-47 of the anchor per term, sfh_anc_acc)
+        const int nr = (int)min((int64_t)4, nbins - i);
+        float sg[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float2 rb = q < nr ? __ldg(a.rowb + i + q) : make_float2(0.f, 0.f);
+            sg[q] = sfh_anchor(sfh_row_bound(rb, rmax, rsum));
+        }
         const float *colp = a.M + j0 * nbins + i;
-        int k = 0;
+        float2 *dst = a.part + (int64_t)split * nbins + i;
         if (VEC) {
+            float2 a01 = make_float2(sg[0], sg[1]), a23 = make_float2(sg[2], sg[3]);
+            float2 l01 = make_float2(0.f, 0.f), l23 = l01;
+            int k = 0;
             for (; k + 8 <= kn; k += 8) {
                 float4 v[8];
 #pragma unroll
                 for (int u = 0; u < 8; ++u) v[u] = ld_stream4(colp + (int64_t)(k + u) * nbins);
-                float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
 #pragma unroll
                 for (int u = 0; u < 8; ++u) {
-                    const float h = rhi[k + u], l = rlo[k + u];
-                    s0 = fmaf(v[u].x, h, fmaf(v[u].x, l, s0));
-                    s1 = fmaf(v[u].y, h, fmaf(v[u].y, l, s1));
-                    s2 = fmaf(v[u].z, h, fmaf(v[u].z, l, s2));
-                    s3 = fmaf(v[u].w, h, fmaf(v[u].w, l, s3));
+                    const float2 h2 = make_float2(rhi[k + u], rhi[k + u]);
+                    const float2 l2 = make_float2(rlo[k + u], rlo[k + u]);
+                    sfh_anc_acc2(a01, l01, make_float2(v[u].x, v[u].y), h2, l2);
+                    sfh_anc_acc2(a23, l23, make_float2(v[u].z, v[u].w), h2, l2);
                 }
-                two_sum_acc(ah[0], al[0], s0);
-                two_sum_acc(ah[1], al[1], s1);
-                two_sum_acc(ah[2], al[2], s2);
-                two_sum_acc(ah[3], al[3], s3);
             }
             for (; k < kn; ++k) {
                 const float4 x = __ldg(reinterpret_cast<const float4 *>(colp + (int64_t)k * nbins));
-                const float h = rhi[k], l = rlo[k];
-                two_sum_acc(ah[0], al[0], fmaf(x.x, h, x.x * l));
-                two_sum_acc(ah[1], al[1], fmaf(x.y, h, x.y * l));
-                two_sum_acc(ah[2], al[2], fmaf(x.z, h, x.z * l));
-                two_sum_acc(ah[3], al[3], fmaf(x.w, h, x.w * l));
+                const float2 h2 = make_float2(rhi[k], rhi[k]), l2 = make_float2(rlo[k], rlo[k]);
+                sfh_anc_acc2(a01, l01, make_float2(x.x, x.y), h2, l2);
+                sfh_anc_acc2(a23, l23, make_float2(x.z, x.w), h2, l2);
             }
-            float2 *dst = a.part + (int64_t)split * nbins + i;
-            *reinterpret_cast<float4 *>(dst) = make_float4(ah[0], al[0], ah[1], al[1]);
-            *reinterpret_cast<float4 *>(dst + 2) = make_float4(ah[2], al[2], ah[3], al[3]);
+            const sfh_df c0 = sfh_anc_result(a01.x, l01.x, sg[0]), c1 = sfh_anc_result(a01.y, l01.y, sg[1]);
+            const sfh_df c2 = sfh_anc_result(a23.x, l23.x, sg[2]), c3 = sfh_anc_result(a23.y, l23.y, sg[3]);
+            *reinterpret_cast<float4 *>(dst) = make_float4(c0.h, c0.l, c1.h, c1.l);
+            *reinterpret_cast<float4 *>(dst + 2) = make_float4(c2.h, c2.l, c3.h, c3.l);
         } else {
-            const int nr = (int)min((int64_t)4, nbins - i);
-            for (; k < kn; ++k) {
+            float av[4] = {sg[0], sg[1], sg[2], sg[3]}, lv[4] = {0.f, 0.f, 0.f, 0.f};
+            for (int k = 0; k < kn; ++k) {
                 const float h = rhi[k], l = rlo[k];
                 const float *c = colp + (int64_t)k * nbins;
 #pragma unroll
                 for (int q = 0; q < 4; ++q)
-                    if (q < nr) {
-                        const float x = __ldg(c + q);
-                        two_sum_acc(ah[q], al[q], fmaf(x, h, x * l));
-                    }
+                    if (q < nr) sfh_anc_acc(av[q], lv[q], __ldg(c + q), h, l);
             }
-            float2 *dst = a.part + (int64_t)split * nbins + i;
-            for (int q = 0; q < nr; ++q) dst[q] = make_float2(ah[q], al[q]);
+            for (int q = 0; q < nr; ++q) {
+                const sfh_df cq = sfh_anc_result(av[q], lv[q], sg[q]);
+                dst[q] = make_float2(cq.h, cq.l);
+            }
         }
     }
     // ---- the last split block of this row tile finalises the tile's rows
@@ -773,6 +779,8 @@ int sfh_launch_fg(sfh_ctx *ctx, const sfh_models *m, const FgArgs &a, cudaEvent_
         p1.negLogL = a.negLogL;
         p1.tab = ctx->d_df_tab;
         p1.eps_f = (float)a.eps;
+        p1.rowb = m->d_rowb;
+        if (!p1.rowb) return sfh_set_error(ctx, SFH_ERR_ARG, "models handle has no row statistics");
         dim3 grid(p.ksplit, p.nrowblk);
         const size_t sm = 2 * (size_t)p.kchunk * sizeof(float);
         if (nbins % 4 == 0)

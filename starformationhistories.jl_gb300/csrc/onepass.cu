@@ -17,13 +17,14 @@
 //   warp 14             the Poisson terms.
 // Per tile, two named barriers:
 //   phase A   owners form m r for their units as the boxes land (r split hi + lo, packed
-//             FP32 pairs, compensated per unit) and sum the lanes that share bins;
+//             FP32 pairs accumulated error-free against a power-of-two anchor per bin,
+//             sfh_anc_acc2) and sum the lanes that share bins;
 //   bar 1
 //   finish    owners 0-7: each bin's 14 owner partials summed by a group of lanes (fixed
 //             shuffle tree, double-float), max(m, eps), w = 1 - n/m, the composite;
 //   bar 2
 //   phase B   owners form M w over their units, accumulated over the CTA's tiles in
-//             per-lane double-float registers, and release each unit's box (two owners
+//             per-lane packed FP32 registers, and release each unit's box (two owners
 //             per box); warp 14 forms the tile's Poisson terms (double-float,
 //             sfh_dfloat.cuh) meanwhile.
 // After the last tile the CTAs' G and logL partials are summed after a grid barrier in a
@@ -87,6 +88,7 @@ struct OnePassArgs {
     double gsign;
     double *G, *negLogL;  // results (either may be NULL)
     const int *skip;      // device flag: nonzero makes every CTA return at once (may be NULL)
+    const float2 *rowb;   // per bin: (sum, max) of |M_ij| over the templates (the anchors' bound)
 };
 
 // Dynamic shared memory: ring | r (hi, lo) | s_part | s_w | s_cn | s_tab | full | empty |
@@ -102,6 +104,20 @@ __device__ __forceinline__ bool op_wait(uint64_t *bar, uint32_t parity, volatile
                                         int *err, int code) {
     if (mbar_test(bar, parity)) return true;
     return mbar_wait_sleep(bar, parity, abort_flag, err, code);
+}
+
+// Anchors of bins i0 .. i0 + 3 (power-of-two accumulator starts, sfh_anc_acc2) from the
+// handle's row statistics and the coefficients' max and sum of |r|.
+__device__ __forceinline__ void op_anchors(const OnePassArgs &a, int64_t i0, float rmax, float rsum,
+                                           float2 &sg01, float2 &sg23) {
+    float sg[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const float2 rb = (i0 + q < a.nbins) ? __ldg(a.rowb + i0 + q) : make_float2(0.f, 0.f);
+        sg[q] = sfh_anchor(sfh_row_bound(rb, rmax, rsum));
+    }
+    sg01 = make_float2(sg[0], sg[1]);
+    sg23 = make_float2(sg[2], sg[3]);
 }
 
 template <int BINS, int OWN, bool SKEW>
@@ -148,8 +164,10 @@ k_fg_onepass(const OnePassArgs a) {
     __syncthreads();
     // the first copies are issued now; the consumers stage r and the tables meanwhile and
     // meet at a consumer-only barrier before their first tile
+    __shared__ float s_rstat[2][32];  // per consumer warp: max and sum of |r|
     if (warp < kWarps) {
         const int nk = nch * kBoxCols, ct = kWarps * 32;
+        float rmx = 0.f, rsm = 0.f;
         for (int k0 = threadIdx.x; k0 < nk; k0 += 4 * ct) {
             double v[4];
 #pragma unroll
@@ -162,7 +180,18 @@ k_fg_onepass(const OnePassArgs a) {
                 const int k = k0 + q * ct;
                 const float h = __double2float_rn(v[q]);
                 if (k < nk) rr[k] = make_float2(h, __double2float_rn(v[q] - (double)h));
+                rmx = fmaxf(rmx, fabsf(h));
+                rsm += fabsf(h);
             }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            rmx = fmaxf(rmx, __shfl_xor_sync(0xffffffffu, rmx, o));
+            rsm += __shfl_xor_sync(0xffffffffu, rsm, o);
+        }
+        if (lane == 0) {
+            s_rstat[0][warp] = rmx;
+            s_rstat[1][warp] = rsm;
         }
         if (a.want_logl)
             for (int k = threadIdx.x; k < SFH_DF_TAB_ALL; k += ct) s_tab[k] = a.tab[k];
@@ -219,12 +248,20 @@ k_fg_onepass(const OnePassArgs a) {
     // finish: warp fw < kFinishers, lanes of bin fb = fw * (32 / LB) + lane / LB
     const bool finisher = warp < kFinishers;
     const int fb = warp * (32 / LB) + lane / LB, fl = lane % LB;
-    // G of the lane's rows of unit j over its 4 bins and all of the CTA's tiles
-    float gh[kUnits][GU], gl[kUnits][GU];
+    // G of the lane's rows of unit j over its 4 bins (packed pairs: bins 0, 2 and 1, 3) and
+    // all of the CTA's tiles
+    float2 g2[kUnits][GU];
 #pragma unroll
     for (int j = 0; j < kUnits; ++j)
 #pragma unroll
-        for (int k = 0; k < GU; ++k) gh[j][k] = gl[j][k] = 0.f;
+        for (int k = 0; k < GU; ++k) g2[j][k] = make_float2(0.f, 0.f);
+    // bound of the coefficients for the anchors: max and sum of |r_hi| (FP32 sum of
+    // nt <= 1536 terms, relative rounding below 1e-4)
+    float rmax = 0.f, rsum = 0.f;
+    for (int w = 0; w < kWarps; ++w) {
+        rmax = fmaxf(rmax, s_rstat[0][w]);
+        rsum += s_rstat[1][w];
+    }
     sfh_df term{0.f, 0.f};
     int s0 = 0;        // slot of the tile's first box
     uint32_t ph0 = 0;  // its use parity
@@ -237,8 +274,11 @@ k_fg_onepass(const OnePassArgs a) {
         __syncwarp();  // lane-dependent code ends: reconverge the warp (here and below)
         if (owner) {
             // phase A: m r over the owner's units for the lane's 4 bins (r split hi + lo,
-            // packed FP32 pairs, two chains per bin pair; compensated per unit)
-            float ah[4] = {0.f, 0.f, 0.f, 0.f}, al[4] = {0.f, 0.f, 0.f, 0.f};
+            // packed FP32 pairs accumulated against the bins' anchors: error-free up to
+            // ~2^-47 of the anchor per term)
+            float2 sg01, sg23;
+            op_anchors(a, tb + 4 * quad, rmax, rsum, sg01, sg23);
+            float2 a01 = sg01, a23 = sg23, l01 = make_float2(0.f, 0.f), l23 = l01;
 #pragma unroll
             for (int j = 0; j < kUnits; ++j) {
                 const int u = warp + kOwners * j;
@@ -251,31 +291,22 @@ k_fg_onepass(const OnePassArgs a) {
                 if (!op_wait(&full[rs], ph, s_abort, err, 2)) { ok = false; break; }
                 const float *bp = ring + (size_t)s * GE::kBoxFloats + (32 * h + g) * BINS + 4 * quad;
                 const float2 *rp = rr + c * kBoxCols + 32 * h + g;
-                float2 e01 = make_float2(0.f, 0.f), e23 = e01, o01 = e01, o23 = e01;
 #pragma unroll
                 for (int k = 0; k < GU; ++k) {
                     const float4 m = *(const float4 *)(bp + k * RPL * BINS);
                     const float2 rv = rp[RPL * k];
                     const float2 h2 = make_float2(rv.x, rv.x), l2 = make_float2(rv.y, rv.y);
-                    const float2 m01 = make_float2(m.x, m.y), m23 = make_float2(m.z, m.w);
-                    if (k & 1) {
-                        o01 = __ffma2_rn(m01, h2, __ffma2_rn(m01, l2, o01));
-                        o23 = __ffma2_rn(m23, h2, __ffma2_rn(m23, l2, o23));
-                    } else {
-                        e01 = __ffma2_rn(m01, h2, __ffma2_rn(m01, l2, e01));
-                        e23 = __ffma2_rn(m23, h2, __ffma2_rn(m23, l2, e23));
-                    }
+                    sfh_anc_acc2(a01, l01, make_float2(m.x, m.y), h2, l2);
+                    sfh_anc_acc2(a23, l23, make_float2(m.z, m.w), h2, l2);
                 }
-                sfh_two_sum_acc(ah[0], al[0], e01.x + o01.x);
-                sfh_two_sum_acc(ah[1], al[1], e01.y + o01.y);
-                sfh_two_sum_acc(ah[2], al[2], e23.x + o23.x);
-                sfh_two_sum_acc(ah[3], al[3], e23.y + o23.y);
             }
             __syncwarp();
+            const sfh_df av[4] = {sfh_anc_result(a01.x, l01.x, sg01.x), sfh_anc_result(a01.y, l01.y, sg01.y),
+                                  sfh_anc_result(a23.x, l23.x, sg23.x), sfh_anc_result(a23.y, l23.y, sg23.y)};
             // sum over the lanes that hold the same bins (other rows)
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                sfh_df v = df_fast_two_sum(ah[k], al[k]);
+                sfh_df v = av[k];
 #pragma unroll
                 for (int o = LPR; o <= 16; o <<= 1) {
                     const sfh_df u{__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)};
@@ -338,9 +369,8 @@ k_fg_onepass(const OnePassArgs a) {
 #pragma unroll
                     for (int k = 0; k < GU; ++k) {
                         const float4 m = *(const float4 *)(bp + k * RPL * BINS);
-                        const float2 p = __ffma2_rn(make_float2(m.z, m.w), w23,
-                                                    __fmul2_rn(make_float2(m.x, m.y), w01));
-                        sfh_two_sum_acc(gh[j][k], gl[j][k], p.x + p.y);
+                        g2[j][k] = __ffma2_rn(make_float2(m.z, m.w), w23,
+                                              __ffma2_rn(make_float2(m.x, m.y), w01, g2[j][k]));
                     }
                 }
                 __syncwarp();
@@ -376,7 +406,9 @@ k_fg_onepass(const OnePassArgs a) {
         if (doA && finisher && fl == 0 && tb + fb < nbins) nd = a.data[tb + fb];
         __syncwarp();
         if (owner) {
-            float ah[4] = {0.f, 0.f, 0.f, 0.f}, al[4] = {0.f, 0.f, 0.f, 0.f};
+            float2 sg01 = make_float2(1.f, 1.f), sg23 = sg01;
+            if (doA) op_anchors(a, tb + 4 * quad, rmax, rsum, sg01, sg23);
+            float2 a01 = sg01, a23 = sg23, l01 = make_float2(0.f, 0.f), l23 = l01;
             float2 w01 = make_float2(0.f, 0.f), w23 = w01;
             if (doB) {
                 const float4 w4 = *(const float4 *)(s_w + 4 * quad);
@@ -398,9 +430,8 @@ k_fg_onepass(const OnePassArgs a) {
 #pragma unroll
                         for (int k = 0; k < GU; ++k) {
                             const float4 m = *(const float4 *)(bp + k * RPL * BINS);
-                            const float2 p = __ffma2_rn(make_float2(m.z, m.w), w23,
-                                                        __fmul2_rn(make_float2(m.x, m.y), w01));
-                            sfh_two_sum_acc(gh[j][k], gl[j][k], p.x + p.y);
+                            g2[j][k] = __ffma2_rn(make_float2(m.z, m.w), w23,
+                                                  __ffma2_rn(make_float2(m.x, m.y), w01, g2[j][k]));
                         }
                     }
                     __syncwarp();
@@ -420,33 +451,24 @@ k_fg_onepass(const OnePassArgs a) {
                     } else {
                         const float *bp = ring + (size_t)s * GE::kBoxFloats + rowoff;
                         const float2 *rp = rr + c * kBoxCols + 32 * h + g;
-                        float2 e01 = make_float2(0.f, 0.f), e23 = e01, o01 = e01, o23 = e01;
 #pragma unroll
                         for (int k = 0; k < GU; ++k) {
                             const float4 m = *(const float4 *)(bp + k * RPL * BINS);
                             const float2 rv = rp[RPL * k];
                             const float2 h2 = make_float2(rv.x, rv.x), l2 = make_float2(rv.y, rv.y);
-                            const float2 m01 = make_float2(m.x, m.y), m23 = make_float2(m.z, m.w);
-                            if (k & 1) {
-                                o01 = __ffma2_rn(m01, h2, __ffma2_rn(m01, l2, o01));
-                                o23 = __ffma2_rn(m23, h2, __ffma2_rn(m23, l2, o23));
-                            } else {
-                                e01 = __ffma2_rn(m01, h2, __ffma2_rn(m01, l2, e01));
-                                e23 = __ffma2_rn(m23, h2, __ffma2_rn(m23, l2, e23));
-                            }
+                            sfh_anc_acc2(a01, l01, make_float2(m.x, m.y), h2, l2);
+                            sfh_anc_acc2(a23, l23, make_float2(m.z, m.w), h2, l2);
                         }
-                        sfh_two_sum_acc(ah[0], al[0], e01.x + o01.x);
-                        sfh_two_sum_acc(ah[1], al[1], e01.y + o01.y);
-                        sfh_two_sum_acc(ah[2], al[2], e23.x + o23.x);
-                        sfh_two_sum_acc(ah[3], al[3], e23.y + o23.y);
                     }
                     __syncwarp();
                 }
             }
             if (doA) {
+                const sfh_df av[4] = {sfh_anc_result(a01.x, l01.x, sg01.x), sfh_anc_result(a01.y, l01.y, sg01.y),
+                                      sfh_anc_result(a23.x, l23.x, sg23.x), sfh_anc_result(a23.y, l23.y, sg23.y)};
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
-                    sfh_df v = df_fast_two_sum(ah[k], al[k]);
+                    sfh_df v = av[k];
 #pragma unroll
                     for (int o = LPR; o <= 16; o <<= 1) {
                         const sfh_df uu{__shfl_xor_sync(0xffffffffu, v.h, o),
@@ -512,7 +534,7 @@ k_fg_onepass(const OnePassArgs a) {
             if (u >= nunits) break;
 #pragma unroll
             for (int k = 0; k < GU; ++k) {
-                sfh_df v = df_fast_two_sum(gh[j][k], gl[j][k]);
+                sfh_df v = df_two_sum(g2[j][k].x, g2[j][k].y);
 #pragma unroll
                 for (int o = 1; o < LPR; o <<= 1) {
                     const sfh_df w{__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)};
@@ -776,6 +798,8 @@ int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
     a.G = d_G;
     a.negLogL = d_negLogL;
     a.skip = d_skip;
+    a.rowb = m->d_rowb;
+    if (!a.rowb) return sfh_set_error(ctx, SFH_ERR_ARG, "models handle has no row statistics");
     cudaStream_t st = ctx->stream;
     if (ev) SFH_CK(ctx, cudaEventRecord(ev[0], st));
     int rc = per_sm == 2 ? launch_onepass<16, 6, false>(ctx, a, grid, st)

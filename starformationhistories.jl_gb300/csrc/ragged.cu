@@ -5,7 +5,8 @@
 // (nbins_g x ntempl_g, column-major FP32, packed in one device array), coefficients,
 // data, composite and gradient.  Two launches cover the whole batch:
 //   pass 1  one CTA per (galaxy, 256-bin row tile): m = M r with the coefficient split
-//           into FP32 hi + lo and compensated FP32 accumulation, the Poisson terms
+//           into FP32 hi + lo, groups of 8 products summed error-free against a
+//           power-of-two anchor (sfh_anc_acc) and folded compensated, the Poisson terms
 //           (FP64-light form), w = 1 - n / max(m, eps) written over the composite;
 //   pass 2  one CTA per (galaxy, 8-template column group): G = Mᵀ w (fg!'s G .*= -1 of
 //           -Mᵀ w), compensated FP32 per column, FP64 block reduction;
@@ -125,19 +126,26 @@ k_ragged_pass1(const float *__restrict__ M, const GalDesc *__restrict__ gals,
         __syncthreads();
         if (!live) continue;
         const float *col = M + G.moff + j0 * G.nbins + i;
-        int k = 0;
-        for (; k + 8 <= kn; k += 8) {
-            float v[8];
+        // groups of 8 templates summed error-free against the group's own power-of-two
+        // anchor (sfh_anc_acc), folded into the compensated pair
+        for (int k = 0; k < kn; k += 8) {
+            const int kk = min(8, kn - k);
+            float v[8], hv[8], lv[8];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) v[u] = __ldg(col + (int64_t)(k + u) * G.nbins);
-            float s = 0.f;
+            for (int u = 0; u < 8; ++u) {
+                v[u] = u < kk ? __ldg(col + (int64_t)(k + u) * G.nbins) : 0.f;
+                hv[u] = u < kk ? rhi[k + u] : 0.f;
+                lv[u] = u < kk ? rlo[k + u] : 0.f;
+            }
+            float b = 0.f;
 #pragma unroll
-            for (int u = 0; u < 8; ++u) s = fmaf(v[u], rhi[k + u], fmaf(v[u], rlo[k + u], s));
-            sfh_two_sum_acc(ah, al, s);
-        }
-        for (; k < kn; ++k) {
-            const float v = __ldg(col + (int64_t)k * G.nbins);
-            sfh_two_sum_acc(ah, al, fmaf(v, rhi[k], v * rlo[k]));
+            for (int u = 0; u < 8; ++u) b = fmaf(fabsf(v[u]), fabsf(hv[u]), b);
+            const float sg = sfh_anchor(b * 1.0009765625f);
+            float a = sg, lo = 0.f;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) sfh_anc_acc(a, lo, v[u], hv[u], lv[u]);
+            sfh_two_sum_acc(ah, al, __fsub_rn(a, sg));
+            al = __fadd_rn(al, lo);
         }
     }
     sfh_df term{0.f, 0.f};
@@ -240,15 +248,25 @@ k_ragged_fused(const float *__restrict__ M, const GalDesc *__restrict__ gals,
             for (int u = 0; u < 4; ++u)
                 m[j0 + u] = (j0 < nt && live && j0 + u < nt)
                                 ? __ldg(col + (int64_t)(j0 + u) * G.nbins) : 0.f;
-        float ah = 0.f, al = 0.f;
+        // the bin's products summed error-free against a power-of-two anchor from the bin's
+        // own bound sum_j |M_ij| |r_j| (sfh_anc_acc)
+        float b = 0.f;
 #pragma unroll
         for (int j0 = 0; j0 < NT; j0 += 4) {
             if (j0 >= nt) break;
-            float s = 0.f;
 #pragma unroll
-            for (int u = 0; u < 4; ++u) s = fmaf(m[j0 + u], rhi[j0 + u], fmaf(m[j0 + u], rlo[j0 + u], s));
-            sfh_two_sum_acc(ah, al, s);
+            for (int u = 0; u < 4; ++u) b = fmaf(fabsf(m[j0 + u]), fabsf(rhi[j0 + u]), b);
         }
+        const float sg = sfh_anchor(b * 1.0009765625f);
+        float aa = sg, lo = 0.f;
+#pragma unroll
+        for (int j0 = 0; j0 < NT; j0 += 4) {
+            if (j0 >= nt) break;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) sfh_anc_acc(aa, lo, m[j0 + u], rhi[j0 + u], rlo[j0 + u]);
+        }
+        const sfh_df cm = sfh_anc_result(aa, lo, sg);
+        const float ah = cm.h, al = cm.l;
         float w = 0.f;
         if (live) bin_terms(ah, al, data, G.boff + i, eps, want_logl, want_g, s_tab, composite, term, w);
         __syncwarp();  // reconverge after the lane-dependent tail

@@ -45,7 +45,16 @@ struct sfh_models {
     __nv_bfloat16 *col_hi = nullptr, *col_lo = nullptr, *row_hi = nullptr, *row_lo = nullptr;
     // FP32 copy kept with BF16X2 storage so single-vector calls still work.
     float *d_f32 = nullptr;
+    // Per bin (sum, max) of |M_ij| over the templates (FP32 and BF16X2 storage): the bound
+    // from which the single-vector kernels pick their accumulation anchors.
+    float2 *d_rowb = nullptr;
     int64_t nbins_pad = 0, nt_pad = 0;
+    // Exact batched composite (batched_exact.cu): 5 BF16 digit planes of the templates,
+    // plane q row i column j (rows padded to nbins_pad128, columns to nt_pad), and the
+    // per-bin power-of-two scales 2^E_i (NULL when nt_pad > 2304).
+    __nv_bfloat16 *digits = nullptr;
+    float *escale = nullptr;
+    int64_t nbins_pad128 = 0;
     // Single-vector launch plan chosen by sfh_models_autotune (0 = built-in heuristics):
     // pass-1 template splits, pass-2 row chunk, pass-2 waves.
     int tune_ks = 0, tune_R = 0, tune_w2 = 0;
@@ -108,6 +117,51 @@ __device__ __forceinline__ void sfh_two_sum_acc(float &hi, float &lo, float x) {
     const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(x, bp));
     hi = s;
     lo = __fadd_rn(lo, err);
+}
+
+// ------------------------------------------------------------------ anchored sums
+// Error-free accumulation of products m*r (r = h + l, two FP32 numbers) against a
+// power-of-two anchor.  The accumulator a starts at sigma, a power of two with
+// |sum of all terms| <= sigma/2, so every intermediate a lies in [sigma/2, 2 sigma):
+//   s  = fma(m, h, a)          one rounding, at ulp(sigma)
+//   nu = a - s                 exact (Sterbenz: a and s are within a factor 2)
+//   e  = fma(m, h, nu)         = (m h + a) - s, the rounding error of s, to 2^-24 of itself
+//   lo = fma(m, l, lo + e)     the error and the low product, both ~2^-24 of the terms
+// The sum is (a - sigma) + lo, a - sigma exact; its error is ~2^-47 sigma per term
+// instead of the 2^-25 |partial| of a plain FP32 chain, so the composite carries
+// ~1e-12 relative error for sigma within a few powers of two of it.  (The anchor is the
+// "extraction against a power of two" of error-free vector transformations: Rump, Ogita,
+// Oishi, "Accurate floating-point summation", SIAM J. Sci. Comput. 31(1), 2008.)
+__device__ __forceinline__ void sfh_anc_acc(float &a, float &lo, float m, float h, float l) {
+    const float s = __fmaf_rn(m, h, a);
+    const float e = __fmaf_rn(m, h, __fsub_rn(a, s));
+    lo = __fmaf_rn(m, l, __fadd_rn(lo, e));
+    a = s;
+}
+// The same on packed pairs (two bins at once, FFMA2 / FADD2).
+__device__ __forceinline__ void sfh_anc_acc2(float2 &a, float2 &lo, float2 m, float2 h, float2 l) {
+    const float2 s = __ffma2_rn(m, h, a);
+    const float2 nu = __ffma2_rn(s, make_float2(-1.f, -1.f), a);  // a - s, exact
+    const float2 e = __ffma2_rn(m, h, nu);
+    lo = __ffma2_rn(m, l, __fadd2_rn(lo, e));
+    a = s;
+}
+// Anchor for a sum bounded by b >= 0: the power of two 2^(E+3) where b < 2^(E+1), i.e.
+// at least 4 b (so a bound a little short of the true one still leaves the factor-2
+// margin); 2^-124 for b = 0 or subnormal b (all terms then vanish or stay below it).
+__device__ __forceinline__ float sfh_anchor(float b) {
+    const int ex = (int)((__float_as_uint(b) >> 23) & 0xffu);  // b >= 0
+    return __uint_as_float((unsigned int)min(ex + 3, 254) << 23);
+}
+// Bound of |sum_j M_ij r_j| for bin i from the handle's row statistics (sum and max of
+// |M_ij| over j) and the coefficients' max and sum of |r_j|, inflated for the rounding of
+// those FP32 statistics.
+__device__ __forceinline__ float sfh_row_bound(float2 rowb, float rmax, float rsum) {
+    return fminf(rmax * rowb.x, rsum * rowb.y) * 1.0009765625f;
+}
+// (a - sigma) + lo as a normalised double-float (a - sigma is exact).
+__device__ __forceinline__ sfh_df sfh_anc_result(float a, float lo, float sigma) {
+    return df_two_sum(__fsub_rn(a, sigma), lo);
 }
 
 // log1p(d) - d for d = c/n - 1 > -1, in FP32 without cancellation (relative error
@@ -231,10 +285,31 @@ int sfh_check_onepass(sfh_ctx *ctx);
 int sfh_launch_loglikelihood(sfh_ctx *ctx, const double *composite, const double *data,
                              int64_t nbins, double eps, double *d_out);
 
+// Exact batched composite (batched_exact.cu): digit planes of the coefficients, their
+// scales and the logL partials live in the batched plan's scratch.
+#include <cuda.h>
+struct SfhExactPlan {
+    int64_t B = 0, B_pad = 0;
+    int n_mt = 0, n_vt = 0;
+    __nv_bfloat16 *Rd = nullptr;
+    float *rscale = nullptr;
+    int *nplanes = nullptr;
+    float2 *lpart = nullptr;
+    CUtensorMap maps[2];
+};
+bool sfh_exact_supported(const sfh_models *m);
+int sfh_build_digit_planes(sfh_ctx *ctx, sfh_models *m);
+size_t sfh_exact_scratch(const sfh_models *m, int64_t B, int64_t *B_pad_out);
+int sfh_exact_prepare(sfh_ctx *ctx, const sfh_models *m, int64_t B, void *scratch, SfhExactPlan *xp);
+int sfh_exact_launch(sfh_ctx *ctx, const sfh_models *m, const SfhExactPlan &xp, const double *d_R,
+                     const double *d_data, double *d_negLogL, __nv_bfloat16 *W_hi,
+                     __nv_bfloat16 *W_lo, int64_t w_ld, int want_w, double eps, int *d_err);
+
 // Batched objective (batched.cu).  prepare() sizes/lays out scratch (scratch == NULL
 // is a size query), converts the data and encodes the tensor maps; launch() only
 // enqueues kernels (capturable in a CUDA graph); check() reads the timeout flag.
-#include <cuda.h>
+// With logL requested and exact planes available, the composite and the Poisson terms
+// come from the exact digit-plane kernel; gradient-only calls keep the hi/lo form.
 struct SfhBatchedPlan {
     int64_t B = 0, B_pad = 0;
     int m_tiles = 0, n_tiles1 = 0, n_tiles2 = 0, ks2 = 1, per2 = 0, kb2 = 0;
@@ -244,6 +319,9 @@ struct SfhBatchedPlan {
     float *gp = nullptr, *dataf = nullptr;
     int *err = nullptr;
     CUtensorMap maps[8];
+    const double *data = nullptr;  // FP64 counts (the exact epilogue splits them itself)
+    bool exact = false;
+    SfhExactPlan xp;
 };
 int sfh_batched_prepare(sfh_ctx *ctx, const sfh_models *m, int64_t B, const double *d_data,
                         void *scratch, size_t scratch_bytes, SfhBatchedPlan *pl);
@@ -252,6 +330,8 @@ int sfh_batched_launch(sfh_ctx *ctx, const sfh_models *m, const SfhBatchedPlan &
 int sfh_batched_check(sfh_ctx *ctx, const SfhBatchedPlan &pl);
 int sfh_launch_fg_batched(sfh_ctx *ctx, const sfh_models *m, const double *d_R, int64_t B,
                           const double *d_data, double *d_negLogL, float *d_G, double eps);
+// Per-bin (sum, max) of |M_ij| of an FP32 (nbins, nt) column-major matrix (core.cu).
+int sfh_row_stats(sfh_ctx *ctx, const float *d_M, int64_t nbins, int64_t nt, float2 *d_out);
 // Builds the BF16 hi/lo planes from an FP32 column-major matrix (batched.cu).
 int sfh_build_bf16_planes(sfh_ctx *ctx, sfh_models *m, const float *d_f32);
 

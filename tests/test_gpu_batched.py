@@ -1,48 +1,33 @@
 """GPU parity of the batched tensor-core objective (sfh_fg_batched_dev) against the FP64
-oracle evaluated on the same stored values: templates and coefficients as their BF16
-hi + lo pairs.
+oracle on the stored FP32 templates and the exact FP64 coefficient vectors.
 
-Tolerances reflect FP32 accumulation in tensor memory: the composite carries a relative
-error of a few 1e-6 (measured ~4e-6 for 1,200 templates), which enters logL as
-~eps * (sum(m) - N); the tests bound |ΔlogL| by 1e-2 per 1e4 stars (+ 1e-7 * |sum m - N|)
-and the gradient error by 1e-4 of sum_i |M_ij| |w_i| (W stored as BF16 hi + lo)."""
+With logL requested the composite comes from the exact digit-plane kernel
+(batched_exact.cu): |ΔlogL| <= 1e-6 per 1e4 stars, the hot-path tolerance.  The gradient
+G = W M runs on BF16 hi/lo planes of W and M with FP32 accumulation: its error is bounded
+by 1e-4 of sum_i |M_ij| |w_i|.  Gradient-only calls form W from the hi/lo composite
+(three BF16 products, FP32 accumulation) under the same gradient bound."""
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
-
-def _bf16_hilo(x):
-    """x -> hi + lo with hi = bf16(x), lo = bf16(x - hi) (round to nearest even)."""
-    import torch
-    t = torch.tensor(np.asarray(x, dtype=np.float32))
-    hi = t.to(torch.bfloat16).to(torch.float32)
-    lo = (t - hi).to(torch.bfloat16).to(torch.float32)
-    return (hi.double() + lo.double()).numpy()
+EPS = 2.220446049250313e-16
 
 
-def _bf16_hilo_f64(x):
-    import torch
-    t = torch.tensor(np.asarray(x, dtype=np.float64))
-    hi = t.float().to(torch.bfloat16).double()
-    lo = (t - hi).float().to(torch.bfloat16).double()
-    return (hi + lo).numpy()
-
-
-def _problem(nbins, nt, B, seed, n_stars):
+def _problem(nbins, nt, B, seed, n_stars, spread=0.3):
     rng = np.random.default_rng(seed)
     M = rng.random((nbins, nt)) * (rng.random((nbins, nt)) > 0.3)
     r0 = np.exp(rng.standard_normal(nt))
     r0 *= n_stars / (M @ r0).sum()
     data = rng.poisson(M @ r0).astype(float)
-    R = r0[None, :] * np.exp(0.3 * rng.standard_normal((B, nt)))
+    R = r0[None, :] * np.exp(spread * rng.standard_normal((B, nt)))
     return np.asfortranarray(M.astype(np.float32)), R, data
 
 
-def _run(sfh, M32, R, data, want_l=True, want_g=True):
+def _run(sfh, M32, R, data, want_l=True, want_g=True, H=None):
     import torch
     L = sfh.load()
-    H = sfh.Models(M32, storage="bf16x2")
+    H = H or sfh.Models(M32, storage="bf16x2")
     ctx = H.ctx
     dev = torch.device("cuda", 0)
     B, nt = R.shape
@@ -53,29 +38,52 @@ def _run(sfh, M32, R, data, want_l=True, want_g=True):
     torch.cuda.synchronize()
     rc = L.sfh_fg_batched_dev(ctx.handle, H.handle, d_R.data_ptr(), B, d_n.data_ptr(),
                               d_L.data_ptr() if want_l else None,
-                              d_G.data_ptr() if want_g else None, 2.220446049250313e-16)
+                              d_G.data_ptr() if want_g else None, EPS)
     sfh._lib.check(rc, ctx.handle, "sfh_fg_batched_dev")
     ctx.synchronize()
     return (d_L.cpu().numpy() if want_l else None), (d_G.cpu().numpy() if want_g else None)
 
 
-@pytest.mark.parametrize("nbins,nt,B", [(7500, 50, 128), (20000, 300, 300), (4099, 77, 5),
-                                        (60000, 64, 256)])
-def test_batched_against_oracle(sfh, O, nbins, nt, B):
-    M32, R, data = _problem(nbins, nt, B, seed=nbins + nt + B, n_stars=1e5)
-    negL, G = _run(sfh, M32, R, data)
-    Ms = np.asfortranarray(_bf16_hilo(M32))
-    Rs = _bf16_hilo_f64(R)
-    check = np.linspace(0, B - 1, min(B, 6)).astype(int)
-    ref_L, ref_G = O.fg_batched(Rs[check], Ms, data, nthreads=4)
+def _check(O, M32, R, data, negL, G, nchk=6):
+    Ms = np.asfortranarray(M32.astype(np.float64))
+    B = R.shape[0]
+    check = np.linspace(0, B - 1, min(B, nchk)).astype(int)
+    ref_L, ref_G = O.fg_batched(R[check], Ms, data, nthreads=4)
     nst = data.sum()
     dL = np.abs(negL[check] - ref_L)
-    mism = np.array([abs((Ms @ Rs[b]).sum() - nst) for b in check])
-    assert np.all(dL <= 1e-2 * max(1.0, nst / 1e4) + 1e-7 * mism), (dL, nst, mism)
-    for k, b in enumerate(check):
-        w = 1.0 - data / np.maximum(Ms @ Rs[b], 2.220446049250313e-16)
-        scale = np.abs(Ms).T @ np.abs(w) + 1e-300
-        assert np.max(np.abs(G[b] - ref_G[k]) / scale) <= 1e-4
+    # the hot-path bar: 1e-6 per 1e4 stars against FP64 on the stored templates
+    assert np.all(dL <= 1e-6 * max(1.0, nst / 1e4)), (dL, nst)
+    if G is not None:
+        for k, b in enumerate(check):
+            w = 1.0 - data / np.maximum(Ms @ R[b], EPS)
+            scale = np.abs(Ms).T @ np.abs(w) + 1e-300
+            assert np.max(np.abs(G[b] - ref_G[k]) / scale) <= 1e-4
+    return dL.max() / max(1.0, nst / 1e4)
+
+
+@pytest.mark.parametrize("nbins,nt,B,nst", [(7500, 50, 128, 1e5), (20000, 300, 300, 1e4),
+                                            (4099, 77, 5, 1e5), (60000, 64, 256, 1e5),
+                                            (1000, 1, 33, 1e4)])
+def test_batched_against_oracle(sfh, O, nbins, nt, B, nst):
+    M32, R, data = _problem(nbins, nt, B, seed=nbins + nt + B, n_stars=nst)
+    negL, G = _run(sfh, M32, R, data)
+    _check(O, M32, R, data, negL, G)
+
+
+def test_batched_production_shape(sfh, O):
+    """60,000 bins x 1,200 templates x 256 vectors, 1e6 stars: the batched workload's
+    matrix, at the hot-path tolerance."""
+    M32, R, data = _problem(60000, 1200, 256, seed=17, n_stars=1e6)
+    negL, G = _run(sfh, M32, R, data)
+    _check(O, M32, R, data, negL, G, nchk=4)
+
+
+def test_batched_wide_coefficient_range(sfh, O):
+    """Coefficient vectors spanning ~1e5 within a vector (exp(2 N(0,1)) spread): the
+    per-vector exponent leaves the small entries fewer digits, the bar still holds."""
+    M32, R, data = _problem(20000, 200, 64, seed=23, n_stars=1e5, spread=2.0)
+    negL, G = _run(sfh, M32, R, data)
+    _check(O, M32, R, data, negL, G)
 
 
 def test_batched_logl_only_and_grad_only(sfh, O):
@@ -84,7 +92,9 @@ def test_batched_logl_only_and_grad_only(sfh, O):
     _, G = _run(sfh, M32, R, data, want_l=False, want_g=True)
     negL2, G2 = _run(sfh, M32, R, data)
     np.testing.assert_array_equal(negL, negL2)   # deterministic: fixed reduction order
-    np.testing.assert_array_equal(G, G2)
+    # gradient-only calls form W from the hi/lo composite: the same bound against the oracle
+    _check(O, M32, R, data, negL2, G)
+    _check(O, M32, R, data, negL2, G2)
 
 
 def test_batched_requires_bf16_storage(sfh):
