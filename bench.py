@@ -571,6 +571,40 @@ def oracle_checks(batched, ragged, M64, r, data, neglogl):
     return plain
 
 
+def template_checks(w, m_ini, mags, offs, lens, M32, nsample=8):
+    """FP32 GPU templates of the timed build against the FP64 oracle's partial_cmd_smooth on
+    `nsample` templates spread over the grid (a spawn process pool): the worst per-bin error
+    normalised by the tolerance 1e-5 |ref| + 1e-6 max(ref) (<= 1 passes) and the largest
+    relative error over bins above 1e-3 of the template's maximum."""
+    import numpy as np
+
+    import oracle as O
+    from sfhgpu import synthetic as S
+    nx, ny = w.grid
+    ex = (w.xedges[0], (w.xedges[-1] - w.xedges[0]) / nx, nx)
+    ey = (w.yedges[0], (w.yedges[-1] - w.yedges[0]) / ny, ny)
+    err = [(e.a, e.b, e.c, e.d, e.cap) for e in S.error_models()]
+    com = [(c.A, c.m50, c.rho) for c in S.completeness_models()]
+    idx = np.linspace(0, w.ntempl - 1, nsample).astype(int)
+    jobs = [(m_ini[offs[t]:offs[t] + lens[t]], mags[:, offs[t]:offs[t] + lens[t]], err, com, 1,
+             (0, 1), w.dmod, 1.0, ex, ey) for t in idx]
+    t0 = time.perf_counter()
+    refs = O.partial_cmd_smooth_many(jobs)
+    worst, relmax = 0.0, 0.0
+    for k, t in enumerate(idx):
+        R = refs[k]
+        G = M32[t].reshape(ny, nx).T.astype(np.float64)
+        e = np.abs(G - R)
+        worst = max(worst, float(np.max(e / np.maximum(1e-5 * np.abs(R) + 1e-6 * np.abs(R).max(),
+                                                       1e-300))))
+        big = np.abs(R) > 1e-3 * np.abs(R).max()
+        relmax = max(relmax, float(np.max(e[big] / np.abs(R[big]))))
+    return {"templates_checked": int(idx.size), "max_err_over_tolerance": worst,
+            "max_rel_err_bins_above_1e-3_of_max": relmax,
+            "tolerance": "1e-5 |ref| + 1e-6 max(ref) per bin", "oracle_seconds":
+            time.perf_counter() - t0}
+
+
 def cpu_fg_baseline(M64, r, data, budget_s=10.0, threads=None):
     """The oracle's fg! (FP64, OpenMP over bins/templates) on a bounded number of evals."""
     import numpy as np
@@ -892,6 +926,7 @@ def run_ours(args):
     plain_check = None
     if rank == 0 and world == 1 and not args.no_cpu:
         plain_check = oracle_checks(batched, ragged, M64, r, data, neglogl)
+        plain_check["templates"] = template_checks(w, m_ini, mags, offs, lens, M32)
         v, thr, n, dt = cpu_fg_baseline(M64, r, data, budget_s=args.cpu_budget_s)
         tps, nt_done, tdt = cpu_template_baseline(w, budget_s=args.cpu_budget_s)
         cpu = {"value": v, "unit": UNIT, "cores": thr, "kind": "port",

@@ -532,3 +532,28 @@ def poisson_deviance(exact, emul):
     """Poisson deviance per star of emul against exact."""
     e, t = _f64(emul).ravel(), _f64(exact).ravel()
     return lib().sfho_poisson_deviance(t, e, t.size)
+
+
+# ---------------- many templates at once (a process pool over the single-thread oracle) ----
+
+def _pcs_job(args):
+    (m_ini, mags, err, compl, y_index, color_indices, dmod, normalize_value, ex, ey) = args
+    imf = kroupa2001()
+    return partial_cmd_smooth(m_ini, mags, [ErrModel(*e) for e in err],
+                              [ComplModel(*c) for c in compl], y_index, color_indices, imf, dmod,
+                              normalize_value, imf_mean(imf), ex, ey)
+
+
+def partial_cmd_smooth_many(jobs, processes=None):
+    """partial_cmd_smooth (StarFormationHistories.jl:829-888) for many isochrones with a
+    Kroupa2001(0.08, 100) IMF, in a pool of processes started with ``spawn`` (safe after the
+    caller has used a GPU).  ``jobs``: tuples (m_ini, mags, err (a, b, c, d, cap) tuples,
+    completeness (A, m50, rho) tuples, y_index, color_indices, dmod, normalize_value,
+    (x first, step, n), (y first, step, n)).  Returns the (nx, ny) arrays in job order."""
+    import multiprocessing as mp
+    jobs = list(jobs)
+    processes = processes or min(len(jobs), os.cpu_count() or 1)
+    if processes <= 1:
+        return [_pcs_job(j) for j in jobs]
+    with mp.get_context("spawn").Pool(processes) as pool:
+        return pool.map(_pcs_job, jobs, chunksize=1)

@@ -125,3 +125,39 @@ def test_partial_cmd_smooth_host_callables(sfh, O):
                              (w.xedges[0], (w.xedges[-1] - w.xedges[0]) / nx, nx),
                              (w.yedges[0], (w.yedges[-1] - w.yedges[0]) / ny, ny))
     _close(H, R)
+
+
+@pytest.mark.parametrize("y_index,branch", [(1, "covariant"), (2, "separable")])
+def test_partial_cmd_smooth_production_grid(sfh, O, y_index, branch):
+    """The production workload: all 1,200 templates (40 log-ages x 30 [M/H]) on the 200 x 300
+    grid built in FP32 on the GPU, 24 of them spread over the age-metallicity grid checked
+    against the FP64 oracle (y = V inside the colour B - V: the covariant kernel; y = R: the
+    separable kernel)."""
+    import torch
+    from sfhgpu import synthetic as S
+    w = S.config2()
+    m_ini, mags, offs, lens = S.isochrone_batch(w)
+    dev = torch.device("cuda", 0)
+    out = sfh.partial_cmd_smooth_batch(
+        torch.tensor(m_ini, device=dev), torch.tensor(mags, device=dev), offs, lens, y_index,
+        (0, 1), S.error_models(), S.completeness_models(), S.imf(), w.dmod, w.normalize_value,
+        (w.xedges, w.yedges))
+    torch.cuda.synchronize()
+    assert out.shape[0] == 1200
+    nx, ny = w.grid
+    ex = (w.xedges[0], (w.xedges[-1] - w.xedges[0]) / nx, nx)
+    ey = (w.yedges[0], (w.yedges[-1] - w.yedges[0]) / ny, ny)
+    err = [(e.a, e.b, e.c, e.d, e.cap) for e in S.error_models()]
+    com = [(c.A, c.m50, c.rho) for c in S.completeness_models()]
+    # 6 ages x 4 metallicities, corners included
+    ia = np.linspace(0, w.logAges.size - 1, 6).astype(int)
+    im = np.linspace(0, w.MHs.size - 1, 4).astype(int)
+    idx = [a * w.MHs.size + z for a in ia for z in im]
+    jobs = [(m_ini[offs[t]:offs[t] + lens[t]], mags[:, offs[t]:offs[t] + lens[t]], err, com,
+             y_index, (0, 1), w.dmod, w.normalize_value, ex, ey) for t in idx]
+    refs = O.partial_cmd_smooth_many(jobs)
+    gpu = out[idx].cpu().numpy()
+    for k, t in enumerate(idx):
+        R = refs[k]
+        assert R.sum() > 0
+        _close(gpu[k].reshape(ny, nx).T, R)
