@@ -62,6 +62,20 @@ int sfh_ctx_synchronize(sfh_ctx *ctx);
 int sfh_ctx_stream(sfh_ctx *ctx, void **stream_out);
 /* Number of kernels this library has launched on this context (telemetry). */
 int sfh_ctx_launch_count(const sfh_ctx *ctx, int64_t *count_out);
+/* Budget of each bounded device-side wait of the single-vector fg! pipeline, in SM clock
+   cycles (0 restores the default, 4e9 cycles, about 2 s at 2 GHz; minimum 1e5).  When a
+   wait runs out the kernel stops at a tile boundary, drains its copies and the call
+   returns SFH_ERR_TIMEOUT; the context stays usable.  No counterpart in the reference
+   (Julia's fg! has no device waits). */
+int sfh_ctx_set_wait_budget(sfh_ctx *ctx, int64_t cycles);
+/* One-shot failure injection for tests of the error paths (no counterpart in the
+   reference); nothing here faults the GPU:
+     SFH_INJECT_DROP_COPY   the next one-pass fg! launch skips its first bulk copy, so the
+                            consumers' wait for that box runs out (SFH_ERR_TIMEOUT);
+     SFH_INJECT_ALLOC_FAIL  the next device or pinned allocation of this context is
+                            refused on the host (SFH_ERR_NOMEM). */
+enum sfh_inject { SFH_INJECT_NONE = 0, SFH_INJECT_DROP_COPY = 1, SFH_INJECT_ALLOC_FAIL = 2 };
+int sfh_ctx_inject_fault(sfh_ctx *ctx, int what);
 
 /* ---------------------------------------------------------------- templates matrix */
 /* Copies a host column-major (nbins, ntempl) matrix (src_dtype SFH_F64 or SFH_F32)
@@ -104,7 +118,9 @@ int sfh_grad_loglikelihood(sfh_ctx *ctx, const sfh_models *models, int dtype,
 /* fg!(F, G, coeffs, models, data, composite), solvers.jl:20-38.
    negLogL == NULL is the `F === nothing` branch, G == NULL the `G === nothing`
    branch.  composite receives what the reference leaves in it (the model when G
-   is NULL, 1 - n/c otherwise); composite may be NULL to skip that copy-out. */
+   is NULL, 1 - n/c otherwise); composite may be NULL to skip that copy-out.
+   Non-finite coefficients: *negLogL and G are set to NaN (what the reference's
+   arithmetic produces) and SFH_ERR_NUMERIC is returned without launching. */
 int sfh_fg(sfh_ctx *ctx, const sfh_models *models, int dtype, const void *coeffs,
            const void *data, void *composite, void *G, double *negLogL);
 
@@ -140,7 +156,8 @@ enum sfh_fit_status {
 typedef struct sfh_fit_options {
     int transform;    /* sfh_fit_transform */
     int max_iter;     /* accepted steps (Optim's iterations; its default is 1000) */
-    int max_evals;    /* fg! evaluations, 0 = 50 (max_iter + 1) */
+    int max_evals;    /* fg! evaluations, 0 = 50 (max_iter + 1); checked between graph
+                         replays, so a fit may run up to graph_slots - 1 more */
     int graph_slots;  /* evaluations per graph replay, 0 = 8 (at most 64) */
     double g_abstol;  /* Optim default 1e-8 */
     double f_reltol;  /* Optim default 0 (stops only on an unchanged f) */
@@ -286,6 +303,8 @@ typedef struct {
     int32_t alpha_free, beta_free, sigma_free;
     double alpha, beta, sigma;  /* values of parameters held fixed */
     double T_max;               /* the AMR models: earliest lookback time in Gyr */
+    const double *d_minv0;      /* D starting diagonal inverse mass (device; NULL = ones), e.g.
+                                   the diagonal of a MAP fit's inverse Hessian */
 } sfh_hmc_config;
 
 /* Batched HMC over all chains at once, every leapfrog step one sfh_fg_batched_dev-style
@@ -312,6 +331,22 @@ int sfh_hmc_sample_dev(sfh_ctx *ctx, const sfh_models *models, const double *d_d
 int sfh_logdensity_batched_dev(sfh_ctx *ctx, const sfh_models *models, const double *d_data,
                                const sfh_hmc_config *cfg, const double *d_theta, double *d_logd,
                                double *d_grad);
+
+/* fit_sfh's optimisations on the device (generic_fitting.jl:242-409): BFGS, as
+   sfh_fit_bfgs_dev, over the hierarchical log density of cfg's metallicity model
+   (SFH_HMC_MZR, SFH_HMC_LINEAR_AMR or SFH_HMC_LOG_AMR; the sampler fields of cfg are
+   ignored) for one vector θ = [log R_j..., free model parameters in their transforms]
+   (D = nages + free ones, the layout of sfh_hmc_sample_dev).  map = 1 minimises
+   -(logL + Jacobian terms of the log transforms) (fg_map!, :324-334), map = 0 minimises
+   -logL (fg_mle!, :335-345); opt->transform is ignored.  Each evaluation maps θ to the
+   template coefficients (calculate_coeffs), runs the single-vector fg! (any template
+   storage) and applies the chain rule, all on the device.  Device buffers: d_data
+   (nbins), d_theta0 (D) -> d_theta_out (D), d_invH (D x D, the final BFGS inverse
+   Hessian, or NULL).  Synchronous. */
+int sfh_fit_sfh_dev(sfh_ctx *ctx, sfh_models *models, const double *d_data,
+                    const sfh_hmc_config *cfg, const double *d_theta0, int map,
+                    const sfh_fit_options *opt, double *d_theta_out, double *d_invH,
+                    sfh_fit_result *res);
 
 /* ---------------------------------------------------------------- mock observation */
 /* model_cmd(mags, errfuncs, completefuncs, biasfuncs; rng, ret_idxs), src/simulate.jl:621-680:

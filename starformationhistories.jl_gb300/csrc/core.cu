@@ -95,6 +95,18 @@ extern "C" int sfh_ctx_synchronize(sfh_ctx *ctx) {
     return sfh_check_onepass(ctx);  // a timed-out one-pass fg! since the last check
 }
 
+extern "C" int sfh_ctx_set_wait_budget(sfh_ctx *ctx, int64_t cycles) {
+    if (!ctx || cycles < 0 || (cycles > 0 && cycles < 100000)) return SFH_ERR_ARG;
+    ctx->wait_budget = cycles ? (long long)cycles : 4000000000LL;
+    return SFH_OK;
+}
+
+extern "C" int sfh_ctx_inject_fault(sfh_ctx *ctx, int what) {
+    if (!ctx || what < SFH_INJECT_NONE || what > SFH_INJECT_ALLOC_FAIL) return SFH_ERR_ARG;
+    ctx->inject = what;
+    return SFH_OK;
+}
+
 extern "C" int sfh_ctx_stream(sfh_ctx *ctx, void **stream_out) {
     if (!ctx || !stream_out) return SFH_ERR_ARG;
     *stream_out = (void *)ctx->stream;
@@ -107,8 +119,16 @@ extern "C" int sfh_ctx_launch_count(const sfh_ctx *ctx, int64_t *count_out) {
     return SFH_OK;
 }
 
+// A one-shot injected allocation failure (SFH_INJECT_ALLOC_FAIL), refused on the host.
+static int injected_alloc_failure(sfh_ctx *ctx) {
+    if (ctx->inject != SFH_INJECT_ALLOC_FAIL) return SFH_OK;
+    ctx->inject = SFH_INJECT_NONE;
+    return sfh_set_error(ctx, SFH_ERR_NOMEM, "allocation refused (injected failure)");
+}
+
 static int reserve(sfh_ctx *ctx, void **buf, size_t *cur, size_t bytes) {
     if (bytes <= *cur) return SFH_OK;
+    if (int rc = injected_alloc_failure(ctx)) return rc;
     // Growth is rare: drain the stream so the old buffer is no longer in use.
     SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
     if (*buf) cudaFree(*buf);
@@ -128,12 +148,17 @@ int sfh_stage_reserve(sfh_ctx *ctx, size_t bytes) {
 }
 int sfh_host_stage_reserve(sfh_ctx *ctx, size_t bytes) {
     if (bytes <= ctx->h_stage_bytes) return SFH_OK;
+    if (int rc = injected_alloc_failure(ctx)) return rc;
     SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     ctx->h_stage = nullptr;
+    ctx->d_h_stage = nullptr;
     ctx->h_stage_bytes = 0;
     const size_t want = bytes + bytes / 4;
-    SFH_CK(ctx, cudaMallocHost(&ctx->h_stage, want));
+    // mapped pinned memory: kernels of the host-array entry points read their inputs from it
+    // and write their outputs into it through its device alias (no separate DMA steps)
+    SFH_CK(ctx, cudaHostAlloc(&ctx->h_stage, want, cudaHostAllocMapped));
+    SFH_CK(ctx, cudaHostGetDevicePointer(&ctx->d_h_stage, ctx->h_stage, 0));
     ctx->h_stage_bytes = want;
     return SFH_OK;
 }
@@ -478,15 +503,29 @@ extern "C" int sfh_fg(sfh_ctx *ctx, const sfh_models *m, int dtype, const void *
     if (!ctx || !m || !coeffs || !data || !dtype_ok(dtype)) return SFH_ERR_ARG;
     SFH_CK(ctx, cudaSetDevice(ctx->device));
     const int64_t nb = m->nbins, nt = m->nt;
-    // inputs [r | n] and outputs [composite | G | -logL] each contiguous, so one DMA each
-    // way through the pinned mirror of the staging area, and one stream sync per call
+    // Non-finite coefficients: the reference's arithmetic would return NaN; report it
+    // without a launch (the outputs carry the NaN a caller ignoring the status would see).
+    bool finite = true;
+    for (int64_t j = 0; j < nt && finite; ++j)
+        finite = std::isfinite(dtype == SFH_F64 ? ((const double *)coeffs)[j]
+                                                : (double)((const float *)coeffs)[j]);
+    if (!finite) {
+        if (negLogL) *negLogL = NAN;
+        for (int64_t j = 0; G && j < nt; ++j) {
+            if (dtype == SFH_F64) ((double *)G)[j] = NAN;
+            else ((float *)G)[j] = NAN;
+        }
+        return sfh_set_error(ctx, SFH_ERR_NUMERIC, "fg!: non-finite coefficients");
+    }
+    // inputs [r | n] and outputs [composite | G | -logL] in the mapped pinned staging area:
+    // the kernels read the inputs and write the outputs across the host link themselves, so
+    // a call is one copy in, one launch, one stream sync and one copy out
     const size_t o_r = 0, o_n = sfh_align256(nt * 8), o_c = o_n + sfh_align256(nb * 8),
                  o_g = o_c + sfh_align256(nb * 8), o_l = o_g + sfh_align256(nt * 8),
                  o_end = o_l + 8;
-    int rc = sfh_stage_reserve(ctx, o_end + 256);
-    if (rc) return rc;
+    int rc;
     if ((rc = sfh_host_stage_reserve(ctx, o_end + 256))) return rc;
-    char *base = (char *)ctx->stage, *hb = (char *)ctx->h_stage;
+    char *base = (char *)ctx->d_h_stage, *hb = (char *)ctx->h_stage;
     double *hr = (double *)(hb + o_r), *hn = (double *)(hb + o_n);
     if (dtype == SFH_F64) {
         memcpy(hr, coeffs, (size_t)nt * 8);
@@ -496,8 +535,6 @@ extern "C" int sfh_fg(sfh_ctx *ctx, const sfh_models *m, int dtype, const void *
         for (int64_t i = 0; i < nt; ++i) hr[i] = cf[i];
         for (int64_t i = 0; i < nb; ++i) hn[i] = df[i];
     }
-    SFH_CK(ctx, cudaMemcpyAsync(base, hb, o_n + (size_t)nb * 8, cudaMemcpyHostToDevice,
-                                ctx->stream));
     FgArgs a{};
     a.coeffs = (const double *)(base + o_r);
     a.data = (const double *)(base + o_n);
@@ -508,12 +545,6 @@ extern "C" int sfh_fg(sfh_ctx *ctx, const sfh_models *m, int dtype, const void *
     a.gsign = 1.0;
     a.mode = FG_MODE_FG;
     if ((rc = sfh_launch_fg(ctx, m, a))) return rc;
-    // the output span actually needed: from the first requested array to the last
-    const size_t lo = composite ? o_c : (G ? o_g : o_l);
-    const size_t hi = negLogL ? o_end : (G ? o_g + (size_t)nt * 8 : o_c + (size_t)nb * 8);
-    if (composite || G || negLogL)
-        SFH_CK(ctx, cudaMemcpyAsync(hb + lo, base + lo, hi - lo, cudaMemcpyDeviceToHost,
-                                    ctx->stream));
     SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
     if (negLogL) {
         double v;

@@ -35,6 +35,8 @@ constexpr int kMaxBacktracks = 40;
 constexpr int kMaxExpand = 10;
 constexpr double kArmijo = 1e-4;
 constexpr double kApproxEps = 1e-6, kSigma = 0.9, kDelta = 0.1;
+// transform value of a general objective: it writes f(θt) to negLogL and ∇f(θt) to Graw
+constexpr int kFitObjective = SFH_FIT_OBJECTIVE;
 
 struct FitState {
     double f, f_prev, dg0, alpha, gnorm, xchange;
@@ -138,8 +140,9 @@ __global__ void __launch_bounds__(kVecThreads) k_fit_trial(FitState *S, FitVecs 
         for (int64_t i = threadIdx.x; i < nt; i += blockDim.x)
             V.theta_t[i] = V.theta[i] + alpha * V.d[i];
     }
-    for (int64_t i = threadIdx.x; i < nt; i += blockDim.x)
-        V.r[i] = to_coeff(V.transform, V.theta_t[i]);
+    if (V.transform != kFitObjective)  // a general objective maps θ itself
+        for (int64_t i = threadIdx.x; i < nt; i += blockDim.x)
+            V.r[i] = to_coeff(V.transform, V.theta_t[i]);
     if (threadIdx.x == 0) {
         S->alpha = alpha;
         S->newdir = 0;
@@ -162,7 +165,9 @@ __global__ void __launch_bounds__(kVecThreads) k_fit_eval(FitState *S, FitVecs V
     for (int64_t i = threadIdx.x; i < nt; i += blockDim.x) {
         const double th = V.theta_t[i], G = V.Graw[i];
         double gt;
-        if (V.transform == SFH_FIT_SQRT) {
+        if (V.transform == kFitObjective) {
+            gt = G;  // the objective wrote the gradient of f in θ
+        } else if (V.transform == SFH_FIT_SQRT) {
             gt = G * 2.0 * th;
         } else {
             gt = V.transform == SFH_FIT_LOG_MAP ? G * V.r[i] - 1.0 : G * V.r[i];
@@ -343,48 +348,38 @@ __global__ void __launch_bounds__(kRowWarps * 32) k_fit_hupdate(const FitState *
 
 }  // namespace
 
-extern "C" int sfh_fit_bfgs_dev(sfh_ctx *ctx, sfh_models *m, const double *d_data,
-                                const double *d_theta0, const sfh_fit_options *opt,
-                                double *d_theta_out, double *d_invH, sfh_fit_result *res) {
-    if (!ctx || !m || !d_data || !d_theta0 || !opt || !d_theta_out || !res) return SFH_ERR_ARG;
-    if (opt->transform < SFH_FIT_LOG_MAP || opt->transform > SFH_FIT_SQRT || opt->max_iter < 0 ||
-        !(opt->g_abstol >= 0.0) || !(opt->f_reltol >= 0.0) || !(opt->x_abstol >= 0.0) ||
-        opt->max_evals < 0 || opt->graph_slots < 0 || opt->graph_slots > 64 || !(opt->eps >= 0.0))
+// The BFGS loop over an objective: `objective` enqueues the evaluation at θt (nvar) on
+// the context stream.  For the transforms of fit_templates it receives r = transform(θt)
+// and writes fg!'s -logL and raw gradient; for kFitObjective it writes f(θt) and ∇f(θt).
+// The slots are captured in a CUDA graph when the objective is capturable.
+int sfh_bfgs_run(sfh_ctx *ctx, int64_t nvar, const double *d_theta0, const sfh_fit_options *opt,
+                 int transform, const SfhFitObjective &objective, double *d_theta_out,
+                 double *d_invH, sfh_fit_result *res) {
+    if (opt->max_iter < 0 || !(opt->g_abstol >= 0.0) || !(opt->f_reltol >= 0.0) ||
+        !(opt->x_abstol >= 0.0) || opt->max_evals < 0 || opt->graph_slots < 0 ||
+        opt->graph_slots > 64 || !(opt->eps >= 0.0))
         return sfh_set_error(ctx, SFH_ERR_ARG, "invalid fit options");
     *res = sfh_fit_result{};
-    SFH_CK(ctx, cudaSetDevice(ctx->device));
-    const int64_t nt = m->nt, nbins = m->nbins;
+    const int64_t nt = nvar;
     const size_t vec = sfh_align256((size_t)nt * 8);
-    const size_t o_state = 0, o_vecs = 256, o_comp = o_vecs + 13 * vec,
-                 o_H = o_comp + sfh_align256((size_t)nbins * 8), total = o_H + (size_t)nt * nt * 8;
+    const size_t o_state = 0, o_vecs = 256, o_H = o_vecs + 13 * vec, total = o_H + (size_t)nt * nt * 8;
     char *buf = nullptr;
     SFH_CK(ctx, cudaMalloc(&buf, total));
     FitState *S = (FitState *)(buf + o_state);
     double *v[13];
     for (int k = 0; k < 13; ++k) v[k] = (double *)(buf + o_vecs + k * vec);
     FitVecs V{v[0], v[1], v[2], v[3], v[4], v[5], v[6], v[7], v[8], v[9], v[10], v[11], v[12],
-              (double *)(buf + o_H), nt, opt->transform, opt->max_iter, opt->g_abstol,
+              (double *)(buf + o_H), nt, transform, opt->max_iter, opt->g_abstol,
               opt->f_reltol, opt->x_abstol};
-    double *comp = (double *)(buf + o_comp);
     cudaStream_t st = ctx->stream;
     int rc = SFH_OK;
     const int64_t max_evals = opt->max_evals > 0 ? opt->max_evals : 50 * ((int64_t)opt->max_iter + 1);
     const int K = opt->graph_slots > 0 ? opt->graph_slots : 8;
     const int hgrid = (int)((nt + kRowWarps - 1) / kRowWarps);
-    FgArgs a{};
-    a.coeffs = V.r;
-    a.data = d_data;
-    a.composite = comp;
-    a.G = V.Graw;
-    a.negLogL = V.negLogL;
-    a.eps = opt->eps > 0.0 ? opt->eps : 2.220446049250313e-16;
-    a.gsign = 1.0;
-    a.mode = FG_MODE_FG;
-    a.skip = &S->skip;
     auto slot = [&]() -> int {
         k_fit_trial<<<1, kVecThreads, 0, st>>>(S, V);
         SFH_LAUNCHED(ctx);
-        int r = sfh_launch_fg(ctx, m, a);
+        int r = objective(V.theta_t, V.r, V.Graw, V.negLogL, &S->skip);
         if (r) return r;
         k_fit_eval<<<1, kVecThreads, 0, st>>>(S, V);
         SFH_LAUNCHED(ctx);
@@ -411,14 +406,18 @@ extern "C" int sfh_fit_bfgs_dev(sfh_ctx *ctx, sfh_models *m, const double *d_dat
             break;
         }
         ctx->launches++;
-        // the first evaluation runs eagerly (it also prepares the fg! plan and its scratch)
+        // the first evaluation runs eagerly (it also prepares the objective's plans and scratch)
         if ((rc = slot())) break;
         bool use_graph = true;
+        int64_t per_replay = 0;  // kernels in one replay of the captured slots
         if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) use_graph = false;
         if (use_graph) {
             int r = SFH_OK;
+            const int64_t l0 = ctx->launches;
             for (int k = 0; k < K && !r; ++k) r = slot();
             cudaError_t e = cudaStreamEndCapture(st, &graph);
+            per_replay = ctx->launches - l0;
+            ctx->launches = l0;  // captured, not launched: counted per replay below
             if (r || e != cudaSuccess || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
                 if (graph) cudaGraphDestroy(graph);
                 graph = nullptr;
@@ -442,7 +441,7 @@ extern "C" int sfh_fit_bfgs_dev(sfh_ctx *ctx, sfh_models *m, const double *d_dat
                     rc = sfh_cuda_error(ctx, cudaGetLastError(), "fit graph launch");
                     break;
                 }
-                ctx->launches += 4 * K;  // trial, eval, and the two H kernels (fg! counts itself)
+                ctx->launches += per_replay;
             } else {
                 for (int k = 0; k < K && !rc; ++k) rc = slot();
                 if (rc) break;
@@ -467,6 +466,37 @@ extern "C" int sfh_fit_bfgs_dev(sfh_ctx *ctx, sfh_models *m, const double *d_dat
     if (graph) cudaGraphDestroy(graph);
     cudaStreamSynchronize(st);
     cudaFree(buf);
+    return rc;
+}
+
+extern "C" int sfh_fit_bfgs_dev(sfh_ctx *ctx, sfh_models *m, const double *d_data,
+                                const double *d_theta0, const sfh_fit_options *opt,
+                                double *d_theta_out, double *d_invH, sfh_fit_result *res) {
+    if (!ctx || !m || !d_data || !d_theta0 || !opt || !d_theta_out || !res) return SFH_ERR_ARG;
+    if (opt->transform < SFH_FIT_LOG_MAP || opt->transform > SFH_FIT_SQRT)
+        return sfh_set_error(ctx, SFH_ERR_ARG, "invalid fit options");
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    double *comp = nullptr;
+    SFH_CK(ctx, cudaMalloc(&comp, (size_t)m->nbins * 8));
+    FgArgs a{};
+    a.data = d_data;
+    a.composite = comp;
+    a.eps = opt->eps > 0.0 ? opt->eps : 2.220446049250313e-16;
+    a.gsign = 1.0;
+    a.mode = FG_MODE_FG;
+    // fg! at r = transform(θt): -logL and the raw gradient G (k_fit_eval transforms them)
+    SfhFitObjective fg = [&](const double *, double *r, double *Graw, double *negLogL,
+                             const int *skip) -> int {
+        FgArgs b = a;
+        b.coeffs = r;
+        b.G = Graw;
+        b.negLogL = negLogL;
+        b.skip = skip;
+        return sfh_launch_fg(ctx, m, b);
+    };
+    const int rc = sfh_bfgs_run(ctx, m->nt, d_theta0, opt, opt->transform, fg, d_theta_out, d_invH, res);
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(comp);
     return rc;
 }
 

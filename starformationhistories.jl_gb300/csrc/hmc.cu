@@ -80,6 +80,7 @@ struct HmcConst {
     int alpha_free, beta_free, sigma_free;
     double alpha, beta, sigma, logM0;
     double T_max;  // LinearAMR / LogarithmicAMR: earliest lookback time (Gyr)
+    int jac;       // 1: log p carries the Jacobian terms of the log transforms (MAP, sampling)
 };
 
 // ---------------------------------------------------------------- trajectory kernels
@@ -313,8 +314,9 @@ __global__ void k_mzr_map(const double *__restrict__ theta, HmcConst c, MzrDev z
 // transforms and Jacobian terms of generic_fitting.jl:143-171; writes ∇ log p and log p.
 // For LinearAMR (amr.jl:122-157) μ_j depends on the age only: ∂μ/∂R = 0 removes the
 // cross-age terms and ∂μ/∂α = T_max - t_j.
+template <typename GT>  // float: the batched gradient; double: the single-vector one
 __global__ void k_mzr_grad(const double *__restrict__ theta, const double *__restrict__ r,
-                           const float *__restrict__ Gfg, const double *__restrict__ negL,
+                           const GT *__restrict__ Gfg, const double *__restrict__ negL,
                            HmcConst c, MzrDev z, double *__restrict__ g, double *__restrict__ logd,
                            int want_logd) {
     extern __shared__ double sm[];
@@ -331,7 +333,7 @@ __global__ void k_mzr_grad(const double *__restrict__ theta, const double *__res
     const double *th = theta + (int64_t)b * c.D;
     const double *cum = z.aux + (int64_t)b * 4 * na, *mu = cum + na, *Asum = mu + na;
     const double *A = z.A + (int64_t)b * z.nt;
-    const float *G = Gfg + (int64_t)b * z.nt;
+    const GT *G = Gfg + (int64_t)b * z.nt;
     double alpha = c.alpha, beta = c.beta, sigma = c.sigma;
     {
         int q = na;
@@ -392,23 +394,25 @@ __global__ void k_mzr_grad(const double *__restrict__ theta, const double *__res
             Gv[na + 1] += ps[j] * dz;
             Gv[na + 2] -= ss[j];
         }
-        // ∇ log p over the free variables; log p = logL + Σ log(positive x)
+        // ∇ log p over the free variables; log p = logL + Σ log(positive x) with the
+        // Jacobian terms (generic_fitting.jl:143-171), logL alone without them (the MLE)
         double* gb = g + (int64_t)b * c.D;
+        const double jf = c.jac ? 1.0 : 0.0;
         double jac = 0.0;
         for (int j = 0; j < na; ++j) {
             const double Rj = exp(th[j]);
-            gb[j] = -Gv[j] * Rj + 1.0;
+            gb[j] = -Gv[j] * Rj + jf;
             jac += th[j];
         }
         int q = na;
-        if (c.alpha_free) { gb[q] = -Gv[na] * alpha + 1.0; jac += th[q]; ++q; }
+        if (c.alpha_free) { gb[q] = -Gv[na] * alpha + jf; jac += th[q]; ++q; }
         if (c.beta_free) {
-            if (c.model == 3) { gb[q] = -Gv[na + 1] * beta + 1.0; jac += th[q]; }  // log β
+            if (c.model == 3) { gb[q] = -Gv[na + 1] * beta + jf; jac += th[q]; }  // log β
             else gb[q] = -Gv[na + 1];
             ++q;
         }
-        if (c.sigma_free) { gb[q] = -Gv[na + 2] * sigma + 1.0; jac += th[q]; ++q; }
-        if (want_logd) logd[b] = -negL[b] + jac;
+        if (c.sigma_free) { gb[q] = -Gv[na + 2] * sigma + jf; jac += th[q]; ++q; }
+        if (want_logd) logd[b] = -negL[b] + jf * jac;
     }
 }
 
@@ -439,8 +443,8 @@ int launch_eval(sfh_ctx *ctx, const sfh_models *m, HmcRun &h, bool want_logd) {
                                             h.s.logd, want_logd ? 1 : 0);
     } else {
         const size_t sm = (size_t)(h.z.nages * 8 + 3) * sizeof(double);
-        k_mzr_grad<<<h.c.B, 64, sm, st>>>(h.s.theta, h.d_r, h.d_G, h.d_negL, h.c, h.z, h.s.g,
-                                          h.s.logd, want_logd ? 1 : 0);
+        k_mzr_grad<float><<<h.c.B, 64, sm, st>>>(h.s.theta, h.d_r, h.d_G, h.d_negL, h.c, h.z,
+                                                 h.s.g, h.s.logd, want_logd ? 1 : 0);
     }
     SFH_LAUNCHED(ctx);
     return SFH_OK;
@@ -503,17 +507,20 @@ __global__ void k_finish(ChainState s, HmcConst c, double *mean, double *var, do
 
 // Validates the configuration, allocates the run's device buffers (recorded in `owned`)
 // and prepares the batched objective for nchains vectors.
+// batched = false: one parameter vector for the single-vector objective of the device fit
+// (any template storage; no sampler state, no batched plan).
 int setup_run(sfh_ctx *ctx, const sfh_models *m, const double *d_data, const sfh_hmc_config *cfg,
-              float *d_draws, HmcRun &h, std::vector<void *> &owned) {
+              float *d_draws, HmcRun &h, std::vector<void *> &owned, bool batched = true) {
     if (!ctx || !m || !d_data || !cfg) return SFH_ERR_ARG;
-    if (m->storage != SFH_BF16X2)
+    if (batched && m->storage != SFH_BF16X2)
         return sfh_set_error(ctx, SFH_ERR_ARG, "HMC needs models stored as SFH_BF16X2");
-    if (cfg->nchains < 1 || cfg->nleap < 1 || cfg->ntraj < 0 || cfg->nwarmup < 0 ||
-        !(cfg->step0 > 0) || !(cfg->target_accept > 0 && cfg->target_accept < 1))
+    if (batched && (cfg->nchains < 1 || cfg->nleap < 1 || cfg->ntraj < 0 || cfg->nwarmup < 0 ||
+                    !(cfg->step0 > 0) || !(cfg->target_accept > 0 && cfg->target_accept < 1)))
         return sfh_set_error(ctx, SFH_ERR_ARG, "invalid HMC configuration");
     SFH_CK(ctx, cudaSetDevice(ctx->device));
     HmcConst &c = h.c;
-    c.B = cfg->nchains;
+    c.B = batched ? cfg->nchains : 1;
+    c.jac = 1;
     c.model = cfg->model;
     c.nwarm = cfg->nwarmup;
     c.nsamp = cfg->ntraj;
@@ -620,6 +627,7 @@ int setup_run(sfh_ctx *ctx, const sfh_models *m, const double *d_data, const sfh
     }
     for (void *p : owned)
         if (!p) return sfh_set_error(ctx, SFH_ERR_NOMEM, "HMC buffers");
+    if (!batched) return SFH_OK;
     int rc;
     if ((rc = sfh_batched_prepare(ctx, m, c.B, d_data, nullptr, 0, &h.plan))) return rc;
     if ((rc = sfh_scratch_reserve(ctx, h.plan.scratch_bytes))) return rc;
@@ -676,6 +684,8 @@ extern "C" int sfh_hmc_sample_dev(sfh_ctx *ctx, const sfh_models *m, const doubl
     k_init_state<<<(unsigned)((std::max(BD, (int64_t)std::max(c.B, c.D)) + kT - 1) / kT), kT, 0, st>>>(
         s, c, cfg->step0);
     SFH_LAUNCHED(ctx);
+    if (cfg->d_minv0)  // a starting metric, e.g. the diagonal of a MAP fit's inverse Hessian
+        SFH_CK(ctx, cudaMemcpyAsync(s.minv, cfg->d_minv0, (size_t)c.D * 8, cudaMemcpyDeviceToDevice, st));
     // gradient and log density at the starting points (eager: also warms every kernel)
     if ((rc = launch_eval(ctx, m, h, true))) { cleanup(); return rc; }
     if ((rc = sfh_batched_check(ctx, h.plan))) { cleanup(); return rc; }
@@ -715,5 +725,82 @@ extern "C" int sfh_hmc_sample_dev(sfh_ctx *ctx, const sfh_models *m, const doubl
         cudaGetLastError();
     }
     cleanup();
+    return rc;
+}
+
+// ---------------------------------------------------------------- device fit_sfh objective
+namespace {
+// f = -log p and ∇f = -∇ log p for the BFGS loop, from the model's log density.
+__global__ void k_hier_out(const double *__restrict__ g, const double *__restrict__ logd, int D,
+                           double *__restrict__ grad, double *__restrict__ f) {
+    for (int k = threadIdx.x; k < D; k += blockDim.x) grad[k] = -g[k];
+    if (threadIdx.x == 0) *f = -*logd;
+}
+}  // namespace
+
+extern "C" int sfh_fit_sfh_dev(sfh_ctx *ctx, sfh_models *m, const double *d_data,
+                               const sfh_hmc_config *cfg, const double *d_theta0, int map,
+                               const sfh_fit_options *opt, double *d_theta_out, double *d_invH,
+                               sfh_fit_result *res) {
+    if (!ctx || !m || !d_data || !cfg || !d_theta0 || !opt || !d_theta_out || !res)
+        return SFH_ERR_ARG;
+    if (cfg->model != SFH_HMC_MZR && cfg->model != SFH_HMC_LINEAR_AMR &&
+        cfg->model != SFH_HMC_LOG_AMR)
+        return sfh_set_error(ctx, SFH_ERR_ARG, "fit_sfh needs a metallicity model");
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    HmcRun h{};
+    std::vector<void *> owned;
+    int rc = setup_run(ctx, m, d_data, cfg, nullptr, h, owned, false);
+    if (rc) { free_run(ctx, owned); return rc; }
+    h.c.jac = map ? 1 : 0;  // MAP: Jacobian terms of the transforms; MLE: logL only
+    const HmcConst c = h.c;
+    const MzrDev z = h.z;
+    double *comp = nullptr, *Gr = nullptr, *gth = nullptr, *logd = nullptr;
+    {
+        void *p[4] = {nullptr, nullptr, nullptr, nullptr};
+        const size_t bytes[4] = {(size_t)m->nbins * 8, (size_t)m->nt * 8, (size_t)c.D * 8, 8};
+        for (int k = 0; k < 4; ++k) {
+            if (cudaMalloc(&p[k], bytes[k]) != cudaSuccess) {
+                free_run(ctx, owned);
+                for (int q = 0; q < k; ++q) cudaFree(p[q]);
+                return sfh_set_error(ctx, SFH_ERR_NOMEM, "fit_sfh buffers");
+            }
+            owned.push_back(p[k]);
+        }
+        comp = (double *)p[0];
+        Gr = (double *)p[1];
+        gth = (double *)p[2];
+        logd = (double *)p[3];
+    }
+    double *r = h.d_r, *negL = h.d_negL;
+    const size_t sm = (size_t)(c.nages * 8 + 3) * sizeof(double);
+    cudaStream_t st = ctx->stream;
+    FgArgs a{};
+    a.data = d_data;
+    a.composite = comp;
+    a.coeffs = r;
+    a.G = Gr;
+    a.negLogL = negL;
+    a.eps = opt->eps > 0.0 ? opt->eps : 2.220446049250313e-16;
+    a.gsign = 1.0;
+    a.mode = FG_MODE_FG;
+    // θt -> r = calculate_coeffs (mzr.jl:50-79, amr.jl:50-72) -> fg!(r) -> chain rule
+    // (mzr.jl:131-209, amr.jl:122-157) -> f = -log p, ∇f (generic_fitting.jl:90-199)
+    SfhFitObjective obj = [&](const double *theta_t, double *, double *grad, double *f,
+                              const int *skip) -> int {
+        k_mzr_map<<<1, kT, 0, st>>>(theta_t, c, z, r);
+        SFH_LAUNCHED(ctx);
+        FgArgs b = a;
+        b.skip = skip;
+        int r2 = sfh_launch_fg(ctx, m, b);
+        if (r2) return r2;
+        k_mzr_grad<double><<<1, 64, sm, st>>>(theta_t, r, Gr, negL, c, z, gth, logd, 1);
+        SFH_LAUNCHED(ctx);
+        k_hier_out<<<1, 64, 0, st>>>(gth, logd, c.D, grad, f);
+        SFH_LAUNCHED(ctx);
+        return SFH_OK;
+    };
+    rc = sfh_bfgs_run(ctx, c.D, d_theta0, opt, SFH_FIT_OBJECTIVE, obj, d_theta_out, d_invH, res);
+    free_run(ctx, owned);
     return rc;
 }

@@ -89,6 +89,8 @@ struct OnePassArgs {
     double *G, *negLogL;  // results (either may be NULL)
     const int *skip;      // device flag: nonzero makes every CTA return at once (may be NULL)
     const float2 *rowb;   // per bin: (sum, max) of |M_ij| over the templates (the anchors' bound)
+    long long budget;     // SM cycles a device wait may take before the launch gives up
+    int drop_copy;        // test-only: producer lane 0 skips its first bulk copy
 };
 
 // Dynamic shared memory: ring | r (hi, lo) | s_part | s_w | s_cn | s_tab | full | empty |
@@ -101,9 +103,9 @@ __host__ __device__ inline size_t op_smem_bytes(int bins, int owners, int slots,
 
 // Bounded wait with an inline fast path (the box has usually landed already).
 __device__ __forceinline__ bool op_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag,
-                                        int *err, int code) {
+                                        int *err, int code, long long budget) {
     if (mbar_test(bar, parity)) return true;
-    return mbar_wait_sleep(bar, parity, abort_flag, err, code);
+    return mbar_wait_sleep(bar, parity, abort_flag, err, code, budget);
 }
 
 // Anchors of bins i0 .. i0 + 3 (power-of-two accumulator starts, sfh_anc_acc2) from the
@@ -213,13 +215,15 @@ k_fg_onepass(const OnePassArgs a) {
             int64_t tl = 0;
             while (k >= nr) { k -= nr; ++tl; }
             for (int64_t q = lane; q < nq; q += kProducers) {
-                if (!op_wait(&empty[s], ph ^ 1u, s_abort, err, 1)) break;
+                if (!op_wait(&empty[s], ph ^ 1u, s_abort, err, 1, a.budget)) break;
                 const int64_t t = (int64_t)blockIdx.x + tl * gridDim.x;
                 const int c0 = k << lp, nb = min(P, nch - c0);
-                mbar_expect_tx(&full[s], (uint32_t)(nb * GE::kBoxBytes));
-                bulk_load(ring + ((size_t)s << lp) * GE::kBoxFloats,
-                          a.blk + ((size_t)t * nch + c0) * GE::kBoxFloats,
-                          (uint32_t)(nb * GE::kBoxBytes), &full[s]);
+                if (!(a.drop_copy && q == 0)) {  // the injected failure: this copy never lands
+                    mbar_expect_tx(&full[s], (uint32_t)(nb * GE::kBoxBytes));
+                    bulk_load(ring + ((size_t)s << lp) * GE::kBoxFloats,
+                              a.blk + ((size_t)t * nch + c0) * GE::kBoxFloats,
+                              (uint32_t)(nb * GE::kBoxBytes), &full[s]);
+                }
                 last = q;
                 s += kProducers;
                 if (s >= runs) { s -= runs; ph ^= 1u; }
@@ -230,7 +234,9 @@ k_fg_onepass(const OnePassArgs a) {
             volatile int never = 0;
             int dummy = 0;
             for (int64_t q = last; q >= 0 && q > last - runs; q -= kProducers)
-                mbar_wait(&full[q % runs], (uint32_t)(q / runs) & 1u, &never, &dummy, 0);
+                if (!(a.drop_copy && q == 0))
+                    mbar_wait_sleep(&full[q % runs], (uint32_t)(q / runs) & 1u, &never, &dummy, 0,
+                                    a.budget);
         }
         return;
     }
@@ -288,7 +294,7 @@ k_fg_onepass(const OnePassArgs a) {
                 uint32_t ph = ph0;
                 if (rs >= runs) { rs -= runs; ph ^= 1u; }
                 const int s = (rs << lp) + (c & (P - 1));
-                if (!op_wait(&full[rs], ph, s_abort, err, 2)) { ok = false; break; }
+                if (!op_wait(&full[rs], ph, s_abort, err, 2, a.budget)) { ok = false; break; }
                 const float *bp = ring + (size_t)s * GE::kBoxFloats + (32 * h + g) * BINS + 4 * quad;
                 const float2 *rp = rr + c * kBoxCols + 32 * h + g;
 #pragma unroll
@@ -446,7 +452,7 @@ k_fg_onepass(const OnePassArgs a) {
                     uint32_t ph = ph0;
                     if (rs >= runs) { rs -= runs; ph ^= 1u; }
                     const int s = (rs << lp) + (c & (P - 1));
-                    if (!op_wait(&full[rs], ph, s_abort, err, 2)) {
+                    if (!op_wait(&full[rs], ph, s_abort, err, 2, a.budget)) {
                         ok = false;
                     } else {
                         const float *bp = ring + (size_t)s * GE::kBoxFloats + rowoff;
@@ -568,7 +574,7 @@ k_fg_onepass(const OnePassArgs a) {
         } else {
             const long long t0 = clock64();
             while (*gen == g0) {
-                if (clock64() - t0 > kSfhWaitBudget) {
+                if (clock64() - t0 > a.budget) {
                     atomicExch(err, 3);
                     break;
                 }
@@ -799,6 +805,9 @@ int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
     a.negLogL = d_negLogL;
     a.skip = d_skip;
     a.rowb = m->d_rowb;
+    a.budget = ctx->wait_budget;
+    a.drop_copy = ctx->inject == SFH_INJECT_DROP_COPY ? 1 : 0;
+    if (a.drop_copy) ctx->inject = SFH_INJECT_NONE;  // one shot
     if (!a.rowb) return sfh_set_error(ctx, SFH_ERR_ARG, "models handle has no row statistics");
     cudaStream_t st = ctx->stream;
     if (ev) SFH_CK(ctx, cudaEventRecord(ev[0], st));

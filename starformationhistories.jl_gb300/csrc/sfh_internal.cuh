@@ -5,6 +5,7 @@
 #include <cuda_bf16.h>
 #include <stdint.h>
 
+#include <functional>
 #include <mutex>
 #include <string>
 
@@ -22,8 +23,8 @@ struct sfh_ctx {
     // Device staging used by the host-array entry points.
     void *stage = nullptr;
     size_t stage_bytes = 0;
-    // Pinned host mirror of `stage` (one DMA each way per host-array call).
-    void *h_stage = nullptr;
+    // Mapped pinned host staging of the host-array entry points and its device alias.
+    void *h_stage = nullptr, *d_h_stage = nullptr;
     size_t h_stage_bytes = 0;
     // Zero-initialised counters for last-block reductions (reset by the last block).
     unsigned int *d_counters = nullptr;
@@ -31,6 +32,10 @@ struct sfh_ctx {
     // (sfh_dfloat.cuh), for the Poisson terms evaluated on the FP32 pipes.
     sfh_df *d_df_tab = nullptr;
     int64_t launches = 0;
+    // Budget of the single-vector pipeline's device waits (SM cycles) and the one-shot
+    // failure injection of the error-path tests (SFH_INJECT_*).
+    long long wait_budget = 4000000000LL;
+    int inject = 0;
 };
 
 struct sfh_models {
@@ -330,6 +335,18 @@ int sfh_batched_launch(sfh_ctx *ctx, const sfh_models *m, const SfhBatchedPlan &
 int sfh_batched_check(sfh_ctx *ctx, const SfhBatchedPlan &pl);
 int sfh_launch_fg_batched(sfh_ctx *ctx, const sfh_models *m, const double *d_R, int64_t B,
                           const double *d_data, double *d_negLogL, float *d_G, double eps);
+// Device BFGS loop (fit.cu) over an objective that enqueues its evaluation at θt on the
+// context stream: for the transforms of fit_templates it gets r = transform(θt) and writes
+// fg!'s -logL and raw gradient; with transform kFitObjective (100) it writes f(θt) to f and
+// ∇f(θt) to grad.  `skip` is a device flag set once the loop has finished (queued slots
+// may turn into no-ops).
+using SfhFitObjective = std::function<int(const double *theta_t, double *r, double *grad,
+                                          double *f, const int *skip)>;
+constexpr int SFH_FIT_OBJECTIVE = 100;
+int sfh_bfgs_run(sfh_ctx *ctx, int64_t nvar, const double *d_theta0, const sfh_fit_options *opt,
+                 int transform, const SfhFitObjective &objective, double *d_theta_out,
+                 double *d_invH, sfh_fit_result *res);
+
 // Per-bin (sum, max) of |M_ij| of an FP32 (nbins, nt) column-major matrix (core.cu).
 int sfh_row_stats(sfh_ctx *ctx, const float *d_M, int64_t nbins, int64_t nt, float2 *d_out);
 // Builds the BF16 hi/lo planes from an FP32 column-major matrix (batched.cu).

@@ -77,14 +77,15 @@ __device__ __forceinline__ bool mbar_test_sleep(uint64_t *bar, uint32_t parity, 
 }
 
 // mbar_wait with sleeping polls (for roles that often wait long: producers on a full
-// ring, consumers ahead of the memory stream).
+// ring, consumers ahead of the memory stream) and a caller-given budget in SM cycles.
 static __device__ __noinline__ bool mbar_wait_sleep(uint64_t *bar, uint32_t parity,
-                                                    volatile int *abort_flag, int *err, int code) {
+                                                    volatile int *abort_flag, int *err, int code,
+                                                    long long budget = kSfhWaitBudget) {
     const long long t0 = clock64();
     for (;;) {
         if (mbar_test_sleep(bar, parity, 1000u)) return true;
         if (*abort_flag) return false;
-        if (clock64() - t0 > kSfhWaitBudget) {
+        if (clock64() - t0 > budget) {
             *abort_flag = 1;
             atomicExch(err, code);
             return false;

@@ -12,8 +12,9 @@ from .fitting import (Galaxies, composite_, construct_x0, construct_x0_mdf, fg_,
                       fit_templates_fast, fit_templates_lbfgsb, grad_loglikelihood,
                       fit_bfgs_device, FIT_LOG_MAP, FIT_LOG_MLE, FIT_SQRT,
                       grad_loglikelihood_, loglikelihood, renormalize_x0, stack_models)
-from .sampling import (GaussianDispersion, LinearAMR, LogarithmicAMR, MH_from_Z, PowerLawMZR,
-                       calculate_coeffs, dMH_dZ, hmc_sample, logdensity_batched, sample_sfh)
+from .sampling import (BFGSResult, CompositeBFGSResult, GaussianDispersion, LinearAMR,
+                       LogarithmicAMR, MH_from_Z, PowerLawMZR, calculate_coeffs, dMH_dZ, fit_sfh,
+                       fit_sfh_x0, hmc_sample, logdensity_batched, sample_sfh)
 from .templates import (BrokenPowerLawIMF, Histogram, Kroupa2001, Martin2016_complete,
                         bin_cmd_smooth, calculate_edges, calculate_weights, compl_model, err_model,
                         exp_photerr, histogram_data, histogram_pix, interpolate_mini, midpoints,
@@ -38,5 +39,5 @@ __all__ = [
     "hmc_sample", "logdensity_batched", "sample_sfh", "Galaxies", "fg_ragged",
     "partial_cmd_smooth_ragged", "SyntheticGenerator", "TemplateEmulator", "LinearAMR",
     "construct_x0_mdf", "fixed_amr", "truncate_relweights", "LogarithmicAMR", "MH_from_Z",
-    "dMH_dZ",
+    "dMH_dZ", "fit_sfh", "fit_sfh_x0", "BFGSResult", "CompositeBFGSResult",
 ]

@@ -44,6 +44,15 @@ class Context:
         check(load().sfh_ctx_launch_count(self.handle, C.byref(n)), self.handle)
         return int(n.value)
 
+    def set_wait_budget(self, cycles: int = 0):
+        """Budget of each bounded device wait of the single-vector pipeline, in SM cycles
+        (0: the default, about 2 s)."""
+        check(load().sfh_ctx_set_wait_budget(self.handle, int(cycles)), self.handle)
+
+    def inject_fault(self, what: int):
+        """One-shot failure injection for tests of the error paths (SFH_INJECT_*)."""
+        check(load().sfh_ctx_inject_fault(self.handle, int(what)), self.handle)
+
     def torch_stream(self):
         import torch
         return torch.cuda.ExternalStream(self.stream, device=torch.device("cuda", self.device))

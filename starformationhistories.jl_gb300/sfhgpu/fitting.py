@@ -147,19 +147,31 @@ def fg_(F, G, coeffs, models, data, composite):
               "axes(models,1) == axes(data,1) == axes(composite,1)")
     T = _T(coeffs, data, composite)
     r, n = _arr(coeffs, T), _arr(data, T)
-    c = np.empty(M.nbins, dtype=T)
-    g = np.empty(M.nt, dtype=T) if G is not None else None
+    # results land in the caller's arrays directly when their memory is the flat layout
+    # (a contiguous vector, or a Fortran-ordered Hess matrix); otherwise via a temporary
+    c = _flat_out(composite, T, M.nbins)
+    g = _flat_out(G, T, M.nt) if G is not None else None
     out = C.c_double()
     ctx = M.ctx
     check(load().sfh_fg(ctx.handle, M.handle, _code(T), r.ctypes.data, n.ctypes.data,
                         c.ctypes.data, g.ctypes.data if g is not None else None,
                         C.byref(out) if F is not None else None), ctx.handle, "fg!")
-    composite[...] = c.reshape(np.shape(composite), order="F")
-    if G is not None:
+    if c is not composite:
+        composite[...] = c.reshape(np.shape(composite), order="F")
+    if G is not None and g is not G:
         G[...] = g
     if F is not None:
         return T.type(out.value)
     return None
+
+
+def _flat_out(a, T, n):
+    """`a` itself when it is a writable ndarray of dtype T whose memory is the n-element
+    flat (column-major) layout; else a new buffer."""
+    if (isinstance(a, np.ndarray) and a.dtype == T and a.size == n and a.flags.writeable and
+            (a.flags.f_contiguous or a.ndim == 1 and a.flags.c_contiguous)):
+        return a
+    return np.empty(n, dtype=T)
 
 
 # ---------------------------------------------------------------- initial guesses

@@ -43,7 +43,7 @@ class HMCConfig(C.Structure):
                 ("h_logAge", C.POINTER(C.c_double)), ("h_MH", C.POINTER(C.c_double)),
                 ("logMstar0", C.c_double), ("alpha_free", C.c_int32), ("beta_free", C.c_int32),
                 ("sigma_free", C.c_int32), ("alpha", C.c_double), ("beta", C.c_double),
-                ("sigma", C.c_double), ("T_max", C.c_double)]
+                ("sigma", C.c_double), ("T_max", C.c_double), ("d_minv0", C.c_void_p)]
 
 
 def _bind():
@@ -54,6 +54,10 @@ def _bind():
         L.sfh_hmc_sample_dev.restype = C.c_int
         L.sfh_logdensity_batched_dev.argtypes = [vp, vp, vp, C.POINTER(HMCConfig), vp, vp, vp]
         L.sfh_logdensity_batched_dev.restype = C.c_int
+        from ._lib import FitOptions, FitResult
+        L.sfh_fit_sfh_dev.argtypes = [vp, vp, vp, C.POINTER(HMCConfig), vp, C.c_int,
+                                      C.POINTER(FitOptions), vp, vp, C.POINTER(FitResult)]
+        L.sfh_fit_sfh_dev.restype = C.c_int
         L._sfh_hmc_bound = True
         del i64
     return L
@@ -266,18 +270,208 @@ def hmc_sample(models: Models, data, nsteps, nchains=1, nwarmup=200, nleap=10, s
     return _run_hmc(models, data, theta0, cfg, keep, keep_draws)
 
 
-def sample_sfh(models: Models, data, logAge, MH, mzr, disp: GaussianDispersion,
-               mstars0, nsteps, nchains=1, nwarmup=200, nleap=10, step0=0.01,
-               target_accept=0.8, seed=20261203, keep_draws=False, thin=1, jitter=0.05):
-    """Posterior sampling of (R_j, α, β, σ) under a PowerLawMZR or LinearAMR metallicity
-    model with GaussianDispersion (sample_sfh, generic_fitting.jl:458-527), all chains in
-    lock step.  Means are reported on the natural scale in the order [R_j..., α, β, σ]
-    (free parameters only)."""
-    th = mzr_theta(mstars0, mzr, disp)
+def sample_sfh(models: Models, data, logAge, MH, mzr=None, disp: GaussianDispersion = None,
+               mstars0=None, nsteps=1000, nchains=1, nwarmup=200, nleap=10, step0=0.01,
+               target_accept=0.8, seed=20261203, keep_draws=False, thin=1, jitter=0.05,
+               fit=None):
+    """Posterior sampling of (R_j, α, β, σ) under a PowerLawMZR, LinearAMR or
+    LogarithmicAMR metallicity model with GaussianDispersion (sample_sfh,
+    generic_fitting.jl:458-527), all chains in lock step.  Means are reported on the
+    natural scale in the order [R_j..., α, β, σ] (free parameters only).
+
+    With fit (the CompositeBFGSResult of fit_sfh), the chains start around the MAP point
+    (spread by `jitter` standard deviations of its inverse Hessian) with the diagonal of
+    that inverse Hessian as the starting metric, as the reference starts its sampler from
+    the MAP fit and its covariance (:458-470); mzr, disp and mstars0 then come from the
+    MAP result."""
     rng = np.random.default_rng(seed)
-    theta0 = th[None, :] + jitter * rng.standard_normal((nchains, th.size))
+    minv0 = None
+    if fit is not None:
+        mzr, disp = fit.map.MH_model, fit.map.disp_model
+        th = np.asarray(fit.map.theta, float)
+        sd = np.sqrt(np.clip(np.diag(fit.map.invH), 1e-300, None))
+        theta0 = th[None, :] + jitter * sd[None, :] * rng.standard_normal((nchains, th.size))
+        minv0 = np.ascontiguousarray(np.diag(fit.map.invH), dtype=np.float64)
+    else:
+        th = mzr_theta(mstars0, mzr, disp)
+        theta0 = th[None, :] + jitter * rng.standard_normal((nchains, th.size))
     kind = (SFH_HMC_LINEAR_AMR if isinstance(mzr, LinearAMR) else
             SFH_HMC_LOG_AMR if isinstance(mzr, LogarithmicAMR) else SFH_HMC_MZR)
     cfg, keep = _config(nchains, kind, nsteps, nwarmup, nleap, thin, step0,
                         target_accept, seed, mzr=mzr, disp=disp, logAge=logAge, MH=MH)
+    if minv0 is not None:
+        import torch
+        d_minv0 = torch.as_tensor(minv0, device=torch.device("cuda", models.ctx.device))
+        cfg.d_minv0 = d_minv0.data_ptr()
+        keep.append(d_minv0)
     return _run_hmc(models, data, theta0, cfg, keep, keep_draws)
+
+
+# ---------------------------------------------------------------- fit_sfh (device BFGS)
+
+@dataclass
+class BFGSResult:
+    """BFGSResult (generic_fitting.jl): natural-scale values `mu` and standard errors
+    `sigma` of every variable [R_j..., metallicity-model parameters..., dispersion
+    parameters...] (fixed ones included, σ = 0), the inverse Hessian `invH` and the
+    transformed optimum `theta` over the free variables, the optimiser outcome `result`,
+    and the models with the fitted parameters."""
+    mu: np.ndarray
+    sigma: np.ndarray
+    invH: np.ndarray
+    theta: np.ndarray
+    result: dict
+    MH_model: object
+    disp_model: object
+
+
+@dataclass
+class CompositeBFGSResult:
+    """The MAP and MLE results of fit_sfh (generic_fitting.jl:318-409)."""
+    map: BFGSResult
+    mle: BFGSResult
+
+
+def _model_params(mzr):
+    """(fittable parameters, transforms) of a metallicity model: PowerLawMZR (α, MH0),
+    transforms (1, 0) (mzr.jl:283-284); LinearAMR (α, β), (1, 0) (amr.jl:212-213);
+    LogarithmicAMR (α, β), (1, 1) (amr.jl:289-290)."""
+    if isinstance(mzr, LogarithmicAMR):
+        return (mzr.alpha, mzr.beta), (1, 1)
+    if isinstance(mzr, LinearAMR):
+        return (mzr.alpha, mzr.beta), (1, 0)
+    return (mzr.alpha, mzr.MH0), (1, 0)
+
+
+def _update_model(mzr, vals):
+    import dataclasses
+    if isinstance(mzr, (LinearAMR, LogarithmicAMR)):
+        return dataclasses.replace(mzr, alpha=float(vals[0]), beta=float(vals[1]))
+    return dataclasses.replace(mzr, alpha=float(vals[0]), MH0=float(vals[1]))
+
+
+def fit_sfh_x0(MH_model0, disp_model0, models, data, logAge, metallicities, x0):
+    """The renormalisation of x0 in fit_sfh (generic_fitting.jl:261-283): x0 scaled so the
+    composite holds the data's total; when calculate_coeffs gives NaN (an MZR far from the
+    stellar mass x0 implies), x0 replicated over the metallicity bins first, then up to
+    five rounds of renormalisation while the coefficients stay finite."""
+    import warnings
+    from .fitting import renormalize_x0
+    full = calculate_coeffs(MH_model0, disp_model0, x0, logAge, metallicities)
+    if np.any(np.isnan(full)):
+        if not isinstance(MH_model0, (LinearAMR, LogarithmicAMR)):
+            warnings.warn("Initial `x0` provided to `fit_sfh` produced NaN coefficients. "
+                          "Attempting to renormalize `x0` by replicating across metallicity bins.")
+        n_mh = len(dict.fromkeys(np.asarray(metallicities, float).tolist()))
+        full = np.tile(np.asarray(x0, float), n_mh)  # Julia's repeat(x0, n)
+        x0 = renormalize_x0(data, models, x0, full)
+        for i in range(1, 6):
+            full = calculate_coeffs(MH_model0, disp_model0, x0, logAge, metallicities)
+            if np.any(np.isnan(full)):
+                warnings.warn(f"Renormalization of x0 failed to produce valid coefficients "
+                              f"after {i} iterations. Returning last valid x0.")
+                break
+            x0 = renormalize_x0(data, models, x0, full)
+    else:
+        x0 = renormalize_x0(data, models, x0, full)
+    return np.asarray(x0, float)
+
+
+def fit_sfh(MH_model0, disp_model0, models: Models, data, logAge, metallicities, x0=None,
+            g_abstol=1e-8, f_reltol=0.0, x_abstol=0.0, max_iter=1000, max_evals=0,
+            graph_slots=8):
+    """fit_sfh(MH_model0, disp_model0, models, data, logAge, metallicities; x0),
+    src/fitting/hierarchical/generic_fitting.jl:242-409: the MAP and then the MLE of the
+    hierarchical model by BFGS, both run on the device (sfh_fit_sfh_dev: the coefficient
+    map, fg! and the chain rule in every evaluation, the BFGS loop replayed from CUDA
+    graphs).  Returns a CompositeBFGSResult; μ and σ follow the reference's assembly
+    (:358-401), including its indexing of the μ vector when some parameters are fixed."""
+    import torch
+    from ._lib import FitOptions, FitResult
+    L = _bind()
+    M = models
+    logAge = np.asarray(logAge, float)
+    metallicities = np.asarray(metallicities, float)
+    data = np.asarray(data, float).reshape(-1)
+    uniq = list(dict.fromkeys(logAge.tolist()))
+    if x0 is None:
+        from .fitting import construct_x0_mdf
+        x0 = construct_x0_mdf(logAge, 13.7, normalize_value=1e6)
+    x0 = np.asarray(x0, float)
+    if x0.size != len(uniq):
+        raise ValueError("length(x0) != length(unique(logAge))")
+    if M.nbins != data.size:
+        raise ValueError("size(models, 1) == length(data)")
+    if not (M.nt == logAge.size == metallicities.size):
+        raise ValueError("size(models, 2) == length(logAge) == length(metallicities)")
+    x0 = fit_sfh_x0(MH_model0, disp_model0, M, data, logAge, metallicities, x0)
+    theta0 = mzr_theta(x0, MH_model0, disp_model0)
+    kind = (SFH_HMC_LINEAR_AMR if isinstance(MH_model0, LinearAMR) else
+            SFH_HMC_LOG_AMR if isinstance(MH_model0, LogarithmicAMR) else SFH_HMC_MZR)
+    cfg, keep = _config(1, kind, mzr=MH_model0, disp=disp_model0, logAge=logAge,
+                        MH=metallicities)
+    dev = torch.device("cuda", M.ctx.device)
+    d_n = torch.as_tensor(data, device=dev)
+    D = theta0.size
+    opt = FitOptions()
+    opt.transform, opt.max_iter, opt.max_evals, opt.graph_slots = 0, int(max_iter), int(max_evals), int(graph_slots)
+    opt.g_abstol, opt.f_reltol, opt.x_abstol, opt.eps = float(g_abstol), float(f_reltol), float(x_abstol), 0.0
+
+    def run(th0, is_map):
+        d_th0 = torch.as_tensor(np.asarray(th0, float), device=dev)
+        d_out = torch.empty(D, dtype=torch.float64, device=dev)
+        d_H = torch.empty((D, D), dtype=torch.float64, device=dev)
+        res = FitResult()
+        torch.cuda.synchronize(dev)
+        check(L.sfh_fit_sfh_dev(M.ctx.handle, M.handle, d_n.data_ptr(), C.byref(cfg),
+                                d_th0.data_ptr(), 1 if is_map else 0, C.byref(opt),
+                                d_out.data_ptr(), d_H.data_ptr(), C.byref(res)),
+              M.ctx.handle, "fit_sfh")
+        H = d_H.cpu().numpy()
+        info = {"f": res.f, "g_norm": res.g_norm, "iterations": int(res.iterations),
+                "evaluations": int(res.evaluations), "status": int(res.status),
+                "converged": int(res.status) in (0, 1, 2), "graph": bool(res.graph)}
+        return d_out.cpu().numpy(), 0.5 * (H + H.T), info
+
+    th_map, H_map, info_map = run(theta0, True)
+    th_mle, H_mle, info_mle = run(th_map, False)
+    del keep
+
+    par = _model_params(MH_model0)[0] + (disp_model0.sigma,)
+    tf = _model_params(MH_model0)[1] + (1,)
+    free = tuple(bool(f) for f in MH_model0.free) + tuple(bool(f) for f in disp_model0.free)
+    nb = len(uniq)
+    ntot = nb + len(par)
+    mu_map, mu_mle = np.empty(ntot), np.empty(ntot)
+    s_map, s_mle = np.empty(ntot), np.empty(ntot)
+    st_map = np.sqrt(np.clip(np.diag(H_map), 0, None))
+    st_mle = np.sqrt(np.clip(np.diag(H_mle), 0, None))
+    for i in range(nb):
+        mu_map[i], mu_mle[i] = np.exp(th_map[i]), np.exp(th_mle[i])
+        s_map[i], s_mle[i] = mu_map[i] * st_map[i], mu_mle[i] * st_mle[i]
+    free_count = 0
+    for i in range(nb, ntot):
+        k = i - nb
+        if free[k]:
+            j = i - free_count  # as the reference indexes μ_map with j (:377-393)
+            if tf[k] == 1:
+                mu_map[i], mu_mle[i] = np.exp(th_map[j]), np.exp(th_mle[j])
+                s_map[i], s_mle[i] = mu_map[j] * st_map[j], mu_map[j] * st_mle[j]
+            elif tf[k] == 0:
+                mu_map[i], mu_mle[i] = th_map[j], th_mle[j]
+                s_map[i], s_mle[i] = st_map[j], st_mle[j]
+            else:
+                mu_map[i], mu_mle[i] = -np.exp(th_map[j]), -np.exp(th_mle[j])
+                s_map[i], s_mle[i] = -mu_map[j] * st_map[j], -mu_map[j] * st_mle[j]
+        else:
+            mu_map[i] = mu_mle[i] = par[k]
+            s_map[i] = s_mle[i] = 0.0
+            free_count += 1
+    import dataclasses
+    nmh = len(_model_params(MH_model0)[0])
+
+    def res_of(mu, sig, H, th, info):
+        return BFGSResult(mu, sig, H, th, info, _update_model(MH_model0, mu[nb:nb + nmh]),
+                          dataclasses.replace(disp_model0, sigma=float(mu[nb + nmh])))
+    return CompositeBFGSResult(res_of(mu_map, s_map, H_map, th_map, info_map),
+                               res_of(mu_mle, s_mle, H_mle, th_mle, info_mle))
