@@ -23,14 +23,23 @@
 // that small coefficients keep their precision.  The classes from P on are dropped.  The
 // composite then matches FP64 on the stored FP32 templates to ~1e-10 relative.
 //
+// The Poisson sum is split so the epilogue only forms logarithms (fitting_base.jl:84-96):
+//   logL_b = Σ_{i: n_i>0} n_i log c_bi  -  Σ_j R_bj colsum_j  +  Σ_{i: n_i>0} (n_i - n_i log n_i),
+// the middle term an FP64 dot product per vector with the templates' column sums (Σ_i c_bi
+// for nonnegative templates and coefficients, where max(c, eps) moves a bin by < eps), the
+// last a constant of the data.  With a negative template value or coefficient the
+// epilogue subtracts each max(c, eps) itself instead.
+//
 // k_tc_exact: one CTA per SM, 320 threads, persistent over (bin tile of 128, vector tile
 // of 32) units, vector tiles inner so concurrent CTAs share the template planes in L2:
 //   warp 0     TMA producer: 2-stage ring of {5 M planes 128x64, P R planes 32x64}
 //   warp 1     allocates 512 TMEM columns (two buffers of up to 8 classes x 32 columns);
 //              lane 0 issues the MMAs (M=128, N = 32 (P - q), K=16)
-//   warps 2-9  epilogue: per (bin, vector) the six class sums combined in double-float,
-//              scaled, the Poisson term in double-float (sfh_dfloat.cuh) and w = 1 - n/c
-//              (BF16 hi/lo, the A operand of G = W M); logL partials per (bin tile, vector).
+//   warps 2-9  epilogue: per (bin, vector) the class sums combined in double-float (the
+//              two leading classes by an error-free sum, the rest, below 2^-11 of the
+//              composite, in FP32), scaled, n log c in double-float (sfh_dfloat.cuh) and
+//              w = 1 - n/c (BF16 hi/lo, the A operand of G = W M); partial sums of n log c
+//              per (bin tile, lane quarter, vector).
 // Every mbarrier wait is bounded as in batched.cu.
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -57,7 +66,8 @@ constexpr int XCLS_COLS = kPMax * XBN;                     // 256 accumulator co
 constexpr int XTMEM_COLS = 512;
 constexpr int kXThreads = 320;
 constexpr int kXEpi = 256;
-constexpr size_t kXSmem = 1024 + (size_t)XSTAGES * XSTAGE_BYTES + 256;
+constexpr size_t kXSmem = 1024 + (size_t)XSTAGES * XSTAGE_BYTES + 256 +
+                          (size_t)SFH_DF_TAB_LOG * sizeof(sfh_df);  // + the log table
 
 // kind::f16 instruction descriptor: D F32, A = B = BF16, both K-major, N, M = 128.
 __host__ __device__ constexpr uint32_t xidesc(int n) {
@@ -72,6 +82,8 @@ struct ExactParams {
     const float *escale;       // nbins: 2^E_i
     const float *rscale;       // B_pad: 2^S_b
     const int *nplanes;        // P (device scalar, set by k_r_digits)
+    const int *negflag;        // nonzero: a coefficient is negative (set by k_r_digits)
+    int m_negative;            // the templates hold a negative value
     float eps;
     const sfh_df *tab;
     __nv_bfloat16 *W_hi, *W_lo;
@@ -138,7 +150,9 @@ k_tc_exact(const __grid_constant__ CUtensorMap tM, const __grid_constant__ CUten
              *tempty = bar + 2 * XSTAGES + 2, *drain = bar + 2 * XSTAGES + 4;
     uint32_t *tmem_slot = (uint32_t *)(bar + 2 * XSTAGES + 5);
     volatile int *s_abort = (volatile int *)(tmem_slot + 1);
+    sfh_df *s_tab = (sfh_df *)(smem + (size_t)XSTAGES * XSTAGE_BYTES + 256);  // log(1 + j/128)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = threadIdx.x; k < SFH_DF_TAB_LOG; k += blockDim.x) s_tab[k] = P.tab[k];
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < XSTAGES; ++s) {
@@ -252,6 +266,7 @@ k_tc_exact(const __grid_constant__ CUtensorMap tM, const __grid_constant__ CUten
         // ---------------- epilogue (warps 2-9): warp covers TMEM lanes 32 (warp & 3) ..,
         // vectors 16 h .. 16 h + 15 of the tile
         const int qd = warp & 3, h = (warp - 2) >> 2;
+        const bool per_c = P.m_negative || *P.negflag;  // Σ c from the column sums does not hold
         int lt = 0;
         for (int u = blockIdx.x; u < total; u += gridDim.x, ++lt) {
             const int mt = u / P.n_vt, vt = u - mt * P.n_vt;
@@ -262,6 +277,9 @@ k_tc_exact(const __grid_constant__ CUtensorMap tM, const __grid_constant__ CUten
             float nh = 0.f, nl = 0.f;
             if (live) sfh_split_double(__ldg(P.data + i), nh, nl);
             const float es = live ? __ldg(P.escale + i) : 0.f;
+            float rsv[16];  // the 16 vectors' scales 2^S_b, loaded while the MMAs run
+#pragma unroll
+            for (int k = 0; k < 16; ++k) rsv[k] = __ldg(P.rscale + vt * XBN + 16 * h + k);
             if (!mbar_wait(&tfull[buf], tph, s_abort, P.err, 14)) break;
             __syncwarp();  // the lanes left the wait at different polls: reconverge for tcgen05.ld
             xfence_after();
@@ -285,20 +303,29 @@ k_tc_exact(const __grid_constant__ CUtensorMap tM, const __grid_constant__ CUten
                 for (int e = 0; e < 8; ++e) {
                     const int vv = 16 * h + 8 * half + e;
                     const int b = vt * XBN + vv;
-                    // Σ_s 2^{-6s} A_s in double-float (each A_s an exact integer), then the
+                    // Σ_s 2^{-6s} A_s (each A_s an exact integer): A_0 + 2^-6 A_1 error-free,
+                    // the classes from 2 on (below 2^-11 of the sum) in FP32, then the
                     // power-of-two scale 2^{E_i + S_b - 12}
-                    sfh_df c{acc[0][e], 0.f};
+                    float tail = 0.f;
 #pragma unroll
-                    for (int s = 1; s < kPMax; ++s)
-                        if (s < NP) c = df_add_f(c, acc[s][e] * __uint_as_float((uint32_t)(127 - 6 * s) << 23));
-                    const float sc = es * __ldg(P.rscale + b) * 2.44140625e-4f;  // 2^-12
+                    for (int s = kPMax - 1; s >= 2; --s)
+                        if (s < NP) tail = fmaf(acc[s][e], __uint_as_float((uint32_t)(127 - 6 * s) << 23), tail);
+                    sfh_df c = df_two_sum(acc[0][e], acc[1][e] * 0.015625f);
+                    c = df_two_sum(c.h, c.l + tail);
+                    const float sc = es * rsv[8 * half + e] * 2.44140625e-4f;  // 2^-12
                     c = sfh_df{c.h * sc, c.l * sc};
                     if (c.h < P.eps || (c.h == P.eps && c.l < 0.f)) c = sfh_df{P.eps, 0.f};
                     sfh_df t{0.f, 0.f};
                     float w = 0.f;  // padding bins carry w = 0 into G = W M
                     if (live && b < P.B) {
-                        t = sfh_bin_term(c, nh, nl, P.tab);
-                        w = __fdiv_rn(df_add(c, sfh_df{-nh, -nl}).h, c.h);  // 1 - n/c
+                        // w = 1 - n/c to FP32 accuracy (it enters G as BF16 hi + lo)
+                        w = __fdividef(c.h - nh, c.h);
+                        if (nh != 0.f || nl != 0.f) {  // n log c, the per-bin part of logL
+                            sfh_df lc = df_log_f_fast(c.h, s_tab);  // c >= eps: a normal float
+                            lc = df_add_f(lc, __fdividef(c.l, c.h));
+                            t = df_mul(lc, sfh_df{nh, nl});
+                        }
+                        if (per_c) t = df_add(t, df_neg(c));  // -max(c, eps) per bin
                     }
                     if (P.want_w && b < P.B && i < P.w_ld) {
                         const __nv_bfloat16 wh = __float2bfloat16_rn(w);
@@ -317,7 +344,7 @@ k_tc_exact(const __grid_constant__ CUtensorMap tM, const __grid_constant__ CUten
 #pragma unroll
             for (int k = 0; k < 16; ++k) {
                 const sfh_df o{__shfl_xor_sync(0xffffffffu, tv[k].h, 16), __shfl_xor_sync(0xffffffffu, tv[k].l, 16)};
-                tv[k] = df_add(tv[k], o);
+                tv[k] = df_add_fast(tv[k], o);
             }
 #pragma unroll
             for (int o = 8; o >= 1; o >>= 1) {
@@ -327,7 +354,7 @@ k_tc_exact(const __grid_constant__ CUtensorMap tM, const __grid_constant__ CUten
                     const sfh_df send = upper ? tv[k] : tv[k + o];
                     const sfh_df keep = upper ? tv[k + o] : tv[k];
                     const sfh_df got{__shfl_xor_sync(0xffffffffu, send.h, o), __shfl_xor_sync(0xffffffffu, send.l, o)};
-                    tv[k] = df_add(keep, got);
+                    tv[k] = df_add_fast(keep, got);
                 }
             }
             // after the halving lane l holds vector (l & 15) of this warp's half: the bit
@@ -386,32 +413,43 @@ __global__ void k_m_digits(const float *__restrict__ M, const float2 *__restrict
 // batch, by atomicMax into *nplanes, which the caller zeroes first).
 __global__ void k_r_digits(const double *__restrict__ R, int64_t B, int64_t nt, int64_t B_pad,
                            int64_t nt_pad, __nv_bfloat16 *__restrict__ planes,
-                           float *__restrict__ rscale, int *__restrict__ nplanes) {
-    __shared__ double s_m[2][32];
+                           float *__restrict__ rscale, int *__restrict__ nplanes,
+                           const double *__restrict__ colsum, double *__restrict__ csum,
+                           int *__restrict__ negflag) {
+    __shared__ double s_m[3][32];
     const int64_t b = blockIdx.x;
-    double mx = 0.0, mn = INFINITY;
+    double mx = 0.0, mn = INFINITY, dot = 0.0;
+    bool neg = false;
     if (b < B)
         for (int64_t j = threadIdx.x; j < nt; j += blockDim.x) {
-            const double a = fabs(R[b * nt + j]);
+            const double v = R[b * nt + j], a = fabs(v);
             mx = fmax(mx, a);
             if (a > 0.0) mn = fmin(mn, a);
+            dot = fma(v, colsum[j], dot);  // Σ_j R_bj Σ_i M_ij = Σ_i c_bi
+            neg |= v < 0.0;
         }
+    if (neg) atomicOr(negflag, 1);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        dot += __shfl_xor_sync(0xffffffffu, dot, o);
     }
     if ((threadIdx.x & 31) == 0) {
         s_m[0][threadIdx.x >> 5] = mx;
         s_m[1][threadIdx.x >> 5] = mn;
+        s_m[2][threadIdx.x >> 5] = dot;
     }
     __syncthreads();
     mx = 0.0;
     mn = INFINITY;
+    dot = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
         mx = fmax(mx, s_m[0][w]);
         mn = fmin(mn, s_m[1][w]);
+        dot += s_m[2][w];
     }
+    if (threadIdx.x == 0) csum[b] = dot;
     int e = 0;
     if (mx > 0.0) frexp(mx, &e);
     if (e < -120) e = -120;  // the scale stays a normal float
@@ -433,8 +471,11 @@ __global__ void k_r_digits(const double *__restrict__ R, int64_t B, int64_t nt, 
     }
 }
 
-// -logL_b = -Σ_tiles (hi + lo), fixed order; zero sum -> -typemax semantics.
+// -logL_b = -(Σ_tiles (hi + lo) - Σ_i c_bi + Σ_i (n_i - n_i log n_i)), fixed order; an
+// exactly zero sum gives -typemax semantics (fitting_base.jl:95).
 __global__ void k_logl_reduce_x(const float2 *__restrict__ part, int n_mt, int B, int B_pad,
+                                const double *__restrict__ csum, const int *__restrict__ negflag,
+                                int m_negative, const double *__restrict__ kn,
                                 double *__restrict__ negLogL) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= B) return;
@@ -443,7 +484,52 @@ __global__ void k_logl_reduce_x(const float2 *__restrict__ part, int n_mt, int B
         const float2 v = part[(int64_t)t * B_pad + b];
         acc += (double)v.x + (double)v.y;
     }
+    if (!(m_negative || *negflag)) acc -= csum[b];  // else the epilogue subtracted each c
+    acc += *kn;
     negLogL[b] = (acc != 0.0) ? -acc : INFINITY;
+}
+
+// Σ_{i: n_i > 0} (n_i - n_i log n_i) in FP64, one block, fixed order.
+__global__ void k_data_const(const double *__restrict__ n, int64_t nbins, double *__restrict__ kn) {
+    __shared__ double s[32];
+    double a = 0.0;
+    for (int64_t i = threadIdx.x; i < nbins; i += blockDim.x) {
+        const double v = n[i];
+        if (v > 0.0) a += v - v * log(v);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s[w];
+        *kn = t;
+    }
+}
+
+// Column sums Σ_i M_ij in FP64 (one block per template) and whether any value is negative.
+__global__ void k_colsum(const float *__restrict__ M, int64_t nbins, double *__restrict__ colsum,
+                         int *__restrict__ negative) {
+    __shared__ double s[32];
+    const int64_t j = blockIdx.x;
+    double a = 0.0;
+    bool neg = false;
+    for (int64_t i = threadIdx.x; i < nbins; i += blockDim.x) {
+        const float v = M[j * nbins + i];
+        a += (double)v;
+        neg |= v < 0.f;
+    }
+    if (neg) atomicOr(negative, 1);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s[w];
+        colsum[j] = t;
+    }
 }
 
 int xmake_map(sfh_ctx *ctx, CUtensorMap *map, const void *base, int64_t rows, int64_t cols,
@@ -481,6 +567,17 @@ int sfh_build_digit_planes(sfh_ctx *ctx, sfh_models *m) {
     k_m_digits<<<grid, block, 0, ctx->stream>>>(m->d_f32, m->d_rowb, m->nbins, m->nt,
                                                m->nbins_pad128, m->nt_pad, m->digits, m->escale);
     SFH_LAUNCHED(ctx);
+    // column sums (FP64) and, in the slot after them, whether any template value is negative
+    const size_t o_flag = sfh_align256((size_t)m->nt * sizeof(double));
+    SFH_CK(ctx, cudaMalloc(&m->colsum, o_flag + 256));
+    int *neg = (int *)((char *)m->colsum + o_flag);
+    SFH_CK(ctx, cudaMemsetAsync(neg, 0, sizeof(int), ctx->stream));
+    k_colsum<<<(unsigned)m->nt, 256, 0, ctx->stream>>>(m->d_f32, m->nbins, m->colsum, neg);
+    SFH_LAUNCHED(ctx);
+    int hneg = 0;
+    SFH_CK(ctx, cudaMemcpyAsync(&hneg, neg, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    m->m_negative = hneg;
     return SFH_OK;
 }
 
@@ -489,7 +586,7 @@ size_t sfh_exact_scratch(const sfh_models *m, int64_t B, int64_t *B_pad_out) {
     const int64_t n_mt = m->nbins_pad128 / XBM;
     if (B_pad_out) *B_pad_out = B_pad;
     return sfh_align256((size_t)kPMax * B_pad * m->nt_pad * 2) + sfh_align256((size_t)B_pad * 4) +
-           256 +
+           256 + sfh_align256((size_t)B_pad * 8) + 256 +
            sfh_align256((size_t)n_mt * 4 * B_pad * sizeof(float2));
 }
 
@@ -507,8 +604,11 @@ int sfh_exact_prepare(sfh_ctx *ctx, const sfh_models *m, int64_t B, void *scratc
     s += sfh_align256((size_t)kPMax * B_pad * m->nt_pad * 2);
     xp->rscale = (float *)s;
     s += sfh_align256((size_t)B_pad * 4);
-    xp->nplanes = (int *)s;
+    xp->nplanes = (int *)s;        // [0] planes, [1] negative-coefficient flag
+    xp->kn = (double *)(s + 128);  // Σ (n - n log n)
     s += 256;
+    xp->csum = (double *)s;
+    s += sfh_align256((size_t)B_pad * 8);
     xp->lpart = (float2 *)s;
     int rc;
     if ((rc = xmake_map(ctx, &xp->maps[0], m->digits, (int64_t)kQ * m->nbins_pad128, m->nt_pad, XBM)))
@@ -527,10 +627,15 @@ int sfh_exact_launch(sfh_ctx *ctx, const sfh_models *m, const SfhExactPlan &xp, 
         attr = true;
     }
     cudaStream_t st = ctx->stream;
-    SFH_CK(ctx, cudaMemsetAsync(xp.nplanes, 0, sizeof(int), st));
+    SFH_CK(ctx, cudaMemsetAsync(xp.nplanes, 0, 2 * sizeof(int), st));
     k_r_digits<<<(unsigned)xp.B_pad, 256, 0, st>>>(d_R, xp.B, m->nt, xp.B_pad, m->nt_pad, xp.Rd,
-                                                    xp.rscale, xp.nplanes);
+                                                    xp.rscale, xp.nplanes, m->colsum, xp.csum,
+                                                    xp.nplanes + 1);
     SFH_LAUNCHED(ctx);
+    if (d_negLogL) {
+        k_data_const<<<1, 1024, 0, st>>>(d_data, m->nbins, xp.kn);
+        SFH_LAUNCHED(ctx);
+    }
     ExactParams P{};
     P.n_mt = xp.n_mt;
     P.n_vt = xp.n_vt;
@@ -543,6 +648,8 @@ int sfh_exact_launch(sfh_ctx *ctx, const sfh_models *m, const SfhExactPlan &xp, 
     P.escale = m->escale;
     P.rscale = xp.rscale;
     P.nplanes = xp.nplanes;
+    P.negflag = xp.nplanes + 1;
+    P.m_negative = m->m_negative;
     P.eps = (float)fmax(eps, 1.1754943508222875e-38);
     P.tab = ctx->d_df_tab;
     P.W_hi = W_hi;
@@ -556,8 +663,9 @@ int sfh_exact_launch(sfh_ctx *ctx, const sfh_models *m, const SfhExactPlan &xp, 
     k_tc_exact<<<grid, kXThreads, kXSmem, st>>>(xp.maps[0], xp.maps[1], P);
     SFH_LAUNCHED(ctx);
     if (d_negLogL) {
-        k_logl_reduce_x<<<(unsigned)((xp.B + 255) / 256), 256, 0, st>>>(xp.lpart, 4 * xp.n_mt, (int)xp.B,
-                                                                        (int)xp.B_pad, d_negLogL);
+        k_logl_reduce_x<<<(unsigned)((xp.B + 255) / 256), 256, 0, st>>>(
+            xp.lpart, 4 * xp.n_mt, (int)xp.B, (int)xp.B_pad, xp.csum, xp.nplanes + 1, m->m_negative,
+            xp.kn, d_negLogL);
         SFH_LAUNCHED(ctx);
     }
     return SFH_OK;

@@ -178,6 +178,7 @@ static void free_models(sfh_models *m) {
     if (m->d_rowb) cudaFree(m->d_rowb);
     if (m->digits) cudaFree(m->digits);
     if (m->escale) cudaFree(m->escale);
+    if (m->colsum) cudaFree(m->colsum);
     delete m;
 }
 

@@ -60,6 +60,8 @@ struct sfh_models {
     __nv_bfloat16 *digits = nullptr;
     float *escale = nullptr;
     int64_t nbins_pad128 = 0;
+    double *colsum = nullptr;  // Σ_i M_ij per template (FP64)
+    int m_negative = 0;        // a template value is negative
     // Single-vector launch plan chosen by sfh_models_autotune (0 = built-in heuristics):
     // pass-1 template splits, pass-2 row chunk, pass-2 waves.
     int tune_ks = 0, tune_R = 0, tune_w2 = 0;
@@ -298,7 +300,9 @@ struct SfhExactPlan {
     int n_mt = 0, n_vt = 0;
     __nv_bfloat16 *Rd = nullptr;
     float *rscale = nullptr;
-    int *nplanes = nullptr;
+    int *nplanes = nullptr;   // [0] R planes, [1] negative-coefficient flag
+    double *kn = nullptr;     // Σ_{n>0} (n - n log n)
+    double *csum = nullptr;   // per vector Σ_j R_bj colsum_j
     float2 *lpart = nullptr;
     CUtensorMap maps[2];
 };

@@ -14,8 +14,10 @@ def _problem(sfh, mzr, disp, nages=8, nmh=5, nbins=6000, n_stars=1e5, seed=3):
     rng = np.random.default_rng(seed)
     la = np.repeat(np.linspace(7.0, 10.0, nages), nmh)
     mh = np.tile(np.linspace(-2.5, 0.0, nmh), nages)
-    M = rng.random((nbins, nages * nmh)) * (rng.random((nbins, nages * nmh)) > 0.3)
-    R = np.exp(0.5 * rng.standard_normal(nages)) * 1e6
+    # templates per unit stellar mass (~1e-5 stars per bin and solar mass), so the stellar
+    # masses per age are ~1e6 Msun and the mass-metallicity relation sits inside the grid
+    M = 1e-5 * rng.random((nbins, nages * nmh)) * (rng.random((nbins, nages * nmh)) > 0.3)
+    R = np.exp(0.5 * rng.standard_normal(nages))
     r = sfh.calculate_coeffs(mzr, disp, R, la, mh)
     s = n_stars / (M @ r).sum()
     R *= s
