@@ -772,7 +772,8 @@ def run_ours(args):
     eps = float(np.finfo(np.float64).eps)
 
     # launch plan picked by the library's autotuner on this matrix and these inputs
-    tuned = H.autotune(r, data, iters=10)
+    tuned = ({"plan": [None, None, None], "ms": None} if args.no_autotune
+             else H.autotune(r, data, iters=10))
     if args.fg_path != "auto":
         H.set_path(args.fg_path)
     if args.onepass_variant:
@@ -814,17 +815,63 @@ def run_ours(args):
     ms = _max_over_ranks(world, ms)
     value = world * args.steps / (ms / 1e3)
     neglogl = float(d_L.item())
+    nocc, occ_sparse, occ_build_ms = H.occupied_info(d_n.data_ptr())
+    nsm = torch.cuda.get_device_properties(0).multi_processor_count
+
+    def kernel_times():
+        kms = (C.c_double * 4)()
+        sfhgpu._lib.check(L.sfh_fg_kernel_times(ctx.handle, H.handle, d_r.data_ptr(),
+                                                d_n.data_ptr(), d_c.data_ptr(), d_G.data_ptr(),
+                                                d_L.data_ptr(), eps, 50, kms),
+                          ctx.handle, "sfh_fg_kernel_times")
+        return kms
+
+    # ---- the same evaluations on the dense kernel (every bin's template row streamed)
+    occupied = None
+    if occ_sparse:
+        H.set_occupied("off")
+        for _ in range(args.warmup):
+            step()
+        nd = min(args.steps, 1000)
+        with torch.cuda.stream(tstream):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(tstream)
+            for _ in range(nd):
+                step()
+            e1.record(tstream)
+        e1.synchronize()
+        dense_ms = e0.elapsed_time(e1) / nd
+        dkms = kernel_times()
+        dense_alg = NBINS * NTW * 4 + NTW * 8 + NBINS * 8 * 2 + 2 * nsm * NTW * 8 + NTW * 8
+        dpeak, _ = _peaks()
+        H.set_occupied("auto")
+        for _ in range(args.warmup):  # a new plan for the timed data (built outside timing)
+            step()
+        ctx.synchronize()
+        occupied = {
+            "occupied_bins": nocc, "fraction": nocc / NBINS, "plan_build_ms": occ_build_ms,
+            "dense_evals_per_s": world / (dense_ms / 1e3), "dense_ms_per_eval": dense_ms,
+            "speedup_vs_dense": value / (world / (dense_ms / 1e3)),
+            "dense_kernel_ms": dkms[0],
+            "dense_roofline_frac": dense_alg / (dkms[0] * 1e-3) / 1e9 / dpeak,
+            "note": "fg! with G needs the composite only where n > 0; empty bins enter "
+                    "through FP64 template column sums (sfh_models_set_occupied)",
+        }
 
     # ---- per-kernel times (CUDA events) for the roofline of the dominant kernel
-    kms = (C.c_double * 4)()
-    sfhgpu._lib.check(L.sfh_fg_kernel_times(ctx.handle, H.handle, d_r.data_ptr(), d_n.data_ptr(),
-                                            d_c.data_ptr(), d_G.data_ptr(), d_L.data_ptr(), eps,
-                                            50, kms), ctx.handle, "sfh_fg_kernel_times")
+    kms = kernel_times()
     path = H.path
-    if path == "onepass":
+    if path == "onepass" and occ_sparse:
+        # the one-pass kernel on the occupied-bin plan: the occupied bins' template rows
+        # once, r, n and the composite of every bin (the empty ones are checked and set to
+        # w = 1), the per-SM partials, G and the column sums over the empty bins
+        names = ["k_fg_onepass_occupied", "(fused into the one-pass kernel)",
+                 "(fused: grid reduction)", "(none)"]
+        alg = [nocc * NTW * 4 + NTW * 8 + NBINS * 8 * 2 + 2 * nsm * NTW * 8 + 2 * NTW * 8, 0, 0, 0]
+        alg_eval = nocc * NTW * 4 + NTW * 8 * 3 + NBINS * 8 * 2
+    elif path == "onepass":
         # [0] the one-pass kernel (M once, r, n, composite out, G and -logL through
         # per-SM partials and an in-kernel grid reduction); slots [1]-[3] stay empty.
-        nsm = torch.cuda.get_device_properties(0).multi_processor_count
         names = ["k_fg_onepass", "(fused into the one-pass kernel)", "(fused: grid reduction)",
                  "(none)"]
         alg = [NBINS * NTW * 4 + NTW * 8 + NBINS * 8 * 2 + 2 * nsm * NTW * 8 + NTW * 8, 0, 0, 0]
@@ -846,6 +893,7 @@ def run_ours(args):
                 "peak_source": peak_kind,
                 "kernel_ms": {n: kms[i] for i, n in enumerate(names)},
                 "fg_total_gbs": alg_eval / (ms / args.steps * 1e-3) / 1e9,
+                "occupied_bin_plan": occupied,
                 "autotuned_plan": {"path": path, "onepass_ms": H.onepass_ms,
                                    "onepass_variant": list(H.onepass_variant),
                                    "pass1_template_splits": tuned["plan"][0], "pass2_rows": tuned["plan"][1],
@@ -880,8 +928,10 @@ def run_ours(args):
     # ---- batched form (tensor cores): 4,096 vectors per call on the same templates
     batched = None
     if not args.no_batched:
-        batched = run_batched(ctx, d_T, NBINS, NTW, r, data, M64, steps=5, warmup=2)
+        batched = run_batched(ctx, d_T, NBINS, NTW, r, data, M64, steps=5, warmup=2, B=args.batch)
         batched["speedup_vs_plain"] = batched["evals_per_s"] / value
+        if occupied:
+            batched["speedup_vs_plain_dense"] = batched["evals_per_s"] / occupied["dense_evals_per_s"]
 
     # ---- ragged galaxies: 256 uneven Hess grids, templates + fg! in one call each
     ragged = None
@@ -896,11 +946,12 @@ def run_ours(args):
     # ---- end-to-end hierarchical HMC (1,024 chains, MZR) on the same templates
     hmc = None
     if not args.no_hmc:
-        hmc = run_hmc(ctx, d_T, w)
+        hmc = run_hmc(ctx, d_T, w, nchains=args.hmc_chains, nwarmup=args.hmc_warmup,
+                      ntraj=args.hmc_traj)
         hmc["speedup_vs_plain_evals"] = hmc["chain_gradient_evals_per_s"] / value
         # the plain single-chain GPU path needs the same number of gradient evaluations to
         # reach the same posterior-mean error (equal effective samples per draw assumed)
-        nev = 1024 * 2000 * 10
+        nev = args.hmc_chains * (args.hmc_warmup + args.hmc_traj) * 10
         hmc["plain_single_chain_seconds_at_matched_error"] = nev / value
         hmc["speedup_vs_plain_single_chain_at_matched_error"] = nev / value / hmc["seconds"]
         em = getattr(run_emulator, "last", None)
@@ -910,7 +961,8 @@ def run_ours(args):
             th = np.stack([la, mh, np.full(la.size, w.dmod)], 1)
             d_em, used = em.templates(th, SyntheticGenerator(w.xedges, w.yedges, ctx=ctx))
             torch.cuda.synchronize()
-            he = run_hmc(ctx, d_T, w, d_model=d_em)
+            he = run_hmc(ctx, d_T, w, nchains=args.hmc_chains, nwarmup=args.hmc_warmup,
+                         ntraj=args.hmc_traj, d_model=d_em)
             hmc["emulated_templates"] = {
                 "emulated_fraction": float(np.mean(used)), "seconds": he["seconds"],
                 "posterior_mean_alpha_MH0_sigma": he["posterior_mean_alpha_MH0_sigma"],
@@ -987,6 +1039,15 @@ def main():
                          "(e.g. 32,1,phased,2)")
     ap.add_argument("--ntempl", type=int, default=NT,
                     help="templates (multiple of 30); fewer than 1200 only for profiling")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="skip the single-vector autotuner (profiling runs: fewer launches "
+                         "before the timed ones; pin the variant with --onepass-variant)")
+    ap.add_argument("--batch", type=int, default=4096,
+                    help="coefficient vectors per batched call (4096: the batched workload)")
+    ap.add_argument("--hmc-chains", type=int, default=1024)
+    ap.add_argument("--hmc-warmup", type=int, default=500)
+    ap.add_argument("--hmc-traj", type=int, default=1500,
+                    help="sampling trajectories (fewer only for profiling runs)")
     ap.add_argument("--cpu-budget-s", type=float, default=10.0)
     ap.add_argument("--reference-budget-s", type=float, default=60.0)
     args = ap.parse_args()

@@ -68,6 +68,25 @@ int sfh_ctx_launch_count(const sfh_ctx *ctx, int64_t *count_out);
    returns SFH_ERR_TIMEOUT; the context stays usable.  No counterpart in the reference
    (Julia's fg! has no device waits). */
 int sfh_ctx_set_wait_budget(sfh_ctx *ctx, int64_t cycles);
+/* How the host-array entry point sfh_fg reaches the caller's arrays:
+     SFH_HOST_ACCESS_STAGED  through the context's mapped pinned staging area (one host
+                             copy in, one out);
+     SFH_HOST_ACCESS_DIRECT  the kernels read r and n and write the composite and G in the
+                             caller's arrays themselves (double arrays, 8-byte aligned,
+                             composite given); needs a device that reads pageable host
+                             memory through the host page tables (a coherent host link),
+                             else SFH_ERR_UNSUPPORTED;
+     SFH_HOST_ACCESS_AUTO    (default) DIRECT where the device supports it, else STAGED.
+   Both give bit-identical results.  No counterpart in the reference (Julia's fg! runs on
+   the host arrays). */
+enum sfh_host_access {
+    SFH_HOST_ACCESS_AUTO = -1,
+    SFH_HOST_ACCESS_STAGED = 0,
+    SFH_HOST_ACCESS_DIRECT = 1
+};
+int sfh_ctx_set_host_access(sfh_ctx *ctx, int mode);
+/* The mode sfh_fg uses now (STAGED or DIRECT; AUTO resolved). */
+int sfh_ctx_host_access(const sfh_ctx *ctx, int *mode_out);
 /* One-shot failure injection for tests of the error paths (no counterpart in the
    reference); nothing here faults the GPU:
      SFH_INJECT_DROP_COPY   the next one-pass fg! launch skips its first bulk copy, so the
@@ -229,6 +248,32 @@ int sfh_models_onepass_variant(sfh_ctx *ctx, const sfh_models *models, int *bins
 /* The path fg! calls with G take on this handle now (ONEPASS or TWOPASS), and the
    one-pass time measured by sfh_models_autotune (0 if not measured); either may be NULL. */
 int sfh_models_path(sfh_ctx *ctx, const sfh_models *models, int *path_out, double *onepass_ms);
+
+/* Occupied-bin restriction of the single-vector fg! with G (FP32 storage, one-pass path;
+   no reference counterpart, same results as fitting_base.jl:84-96,265-285 and
+   solvers.jl:20-38).  With G requested the composite matters only where n_i > 0: an
+   empty bin has w_i = 1 exactly and adds -max(c_i, eps) to logL, so its terms reduce to
+   the template column sums over the empty bins, E_j (kept in FP64):
+     logL = Σ_{n_i > 0} (n_i - c_i - n_i log(n_i / c_i)) - Σ_j r_j E_j,
+     G_j  = Σ_{n_i > 0} M_ij (1 - n_i / c_i) + E_j,
+   and the composite output holds w, 1.0 in the empty bins, as fg! leaves it.  The only
+   difference from the dense sum is -c_i for -max(c_i, eps) in empty bins whose model is
+   below eps (at most eps per bin).  The handle keeps a plan per observed diagram (keyed by
+   its data pointer, built on first use: the occupied bins, a blocked copy of their template
+   rows, E_j; up to 4 diagrams per handle): the kernel then reads only the occupied rows.
+   Every call checks that the plan's empty bins are still empty; a bin that is not is
+   folded in exactly inside the same launch, and the next call builds a new plan.  Calls
+   made during stream capture use an existing plan only.
+     SFH_OCC_OFF    the dense kernel always;
+     SFH_OCC_AUTO   (default) the plan when at most 60 % of the bins are occupied;
+     SFH_OCC_ON     the plan whenever some bin is empty and some occupied. */
+enum sfh_occ_mode { SFH_OCC_OFF = 0, SFH_OCC_AUTO = 1, SFH_OCC_ON = 2 };
+int sfh_models_set_occupied(sfh_ctx *ctx, sfh_models *models, int mode);
+/* Telemetry of the plan for d_data: occupied bins (or -1 when no plan exists), whether
+   the restricted kernel serves it (0/1), and the host wall time of the last plan build
+   (ms); any output may be NULL. */
+int sfh_models_occupied_info(sfh_ctx *ctx, const sfh_models *models, const double *d_data,
+                             int64_t *nocc_out, int *sparse_out, double *build_ms_out);
 
 /* Autotuner (no reference counterpart): times candidate launch plans of the FP32
    single-vector fg! on this matrix with the caller's inputs (pass-1 template splits whose

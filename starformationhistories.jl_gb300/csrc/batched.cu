@@ -444,13 +444,14 @@ __global__ void k_logl_reduce(const float2 *__restrict__ part, int n_tiles, int 
 
 // G = Σ_ks Gpart[ks], fixed order.
 __global__ void k_g_reduce(const float *__restrict__ part, int ksplit, int64_t B, int64_t B_pad,
-                           int64_t nt, float *__restrict__ G) {
+                           int64_t nt, float *__restrict__ G, const double *__restrict__ colsum_e) {
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= B * nt) return;
     const int64_t b = idx / nt, j = idx - b * nt;
     float hi = 0.f, lo = 0.f;
     for (int s = 0; s < ksplit; ++s) sfh_two_sum_acc(hi, lo, part[((int64_t)s * B_pad + b) * nt + j]);
-    G[idx] = hi + lo;
+    // a derived occupied-bin handle: the parent's empty bins, w = 1, enter as E_j
+    G[idx] = colsum_e ? (float)((double)hi + (double)lo + colsum_e[j]) : hi + lo;
 }
 
 // ------------------------------------------------------------------ host side
@@ -646,7 +647,8 @@ int sfh_batched_launch(sfh_ctx *ctx, const sfh_models *m, const SfhBatchedPlan &
         P2.err = pl.err;
         if ((rc = launch_gemm(ctx, pl.maps[4], pl.maps[5], pl.maps[6], pl.maps[7], P2))) return rc;
         const int64_t n = B * nt;
-        k_g_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(pl.gp, pl.ks2, B, B_pad, nt, d_G);
+        k_g_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(pl.gp, pl.ks2, B, B_pad, nt, d_G,
+                                                                m->colsum_e);
         SFH_LAUNCHED(ctx);
     }
     (void)nbp;
@@ -661,8 +663,8 @@ int sfh_batched_check(sfh_ctx *ctx, const SfhBatchedPlan &pl) {
     return SFH_OK;
 }
 
-int sfh_launch_fg_batched(sfh_ctx *ctx, const sfh_models *m, const double *d_R, int64_t B,
-                          const double *d_data, double *d_negLogL, float *d_G, double eps) {
+static int run_batched(sfh_ctx *ctx, const sfh_models *m, const double *d_R, int64_t B,
+                       const double *d_data, double *d_negLogL, float *d_G, double eps) {
     SfhBatchedPlan pl{};
     int rc = sfh_batched_prepare(ctx, m, B, d_data, nullptr, 0, &pl);
     if (rc) return rc;
@@ -670,6 +672,23 @@ int sfh_launch_fg_batched(sfh_ctx *ctx, const sfh_models *m, const double *d_R, 
     if ((rc = sfh_batched_prepare(ctx, m, B, d_data, ctx->scratch, ctx->scratch_bytes, &pl))) return rc;
     if ((rc = sfh_batched_launch(ctx, m, pl, d_R, d_negLogL, d_G, eps))) return rc;
     return sfh_batched_check(ctx, pl);
+}
+
+int sfh_launch_fg_batched(sfh_ctx *ctx, const sfh_models *m, const double *d_R, int64_t B,
+                          const double *d_data, double *d_negLogL, float *d_G, double eps) {
+    // the occupied-bin plan's derived handle when the diagram leaves bins empty
+    const sfh_models *mb = m;
+    const double *db = d_data;
+    SfhOccPlan *occ = nullptr;
+    int rc = sfh_occ_batched(ctx, const_cast<sfh_models *>(m), d_data, d_negLogL != nullptr, &mb,
+                             &db, &occ);
+    if (rc) return rc;
+    if ((rc = run_batched(ctx, mb, d_R, B, db, d_negLogL, d_G, eps))) return rc;
+    if (occ && *occ->h_bviol) {  // a plan-empty bin holds counts now: the dense evaluation
+        sfh_occ_retire(occ);
+        rc = run_batched(ctx, m, d_R, B, d_data, d_negLogL, d_G, eps);
+    }
+    return rc;
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 sfh_tensor_map_encoder() {

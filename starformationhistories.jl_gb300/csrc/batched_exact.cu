@@ -415,10 +415,11 @@ __global__ void k_r_digits(const double *__restrict__ R, int64_t B, int64_t nt, 
                            int64_t nt_pad, __nv_bfloat16 *__restrict__ planes,
                            float *__restrict__ rscale, int *__restrict__ nplanes,
                            const double *__restrict__ colsum, double *__restrict__ csum,
-                           int *__restrict__ negflag) {
-    __shared__ double s_m[3][32];
+                           int *__restrict__ negflag, const double *__restrict__ colsum_e,
+                           double *__restrict__ csum_e) {
+    __shared__ double s_m[4][32];
     const int64_t b = blockIdx.x;
-    double mx = 0.0, mn = INFINITY, dot = 0.0;
+    double mx = 0.0, mn = INFINITY, dot = 0.0, dote = 0.0;
     bool neg = false;
     if (b < B)
         for (int64_t j = threadIdx.x; j < nt; j += blockDim.x) {
@@ -426,6 +427,7 @@ __global__ void k_r_digits(const double *__restrict__ R, int64_t B, int64_t nt, 
             mx = fmax(mx, a);
             if (a > 0.0) mn = fmin(mn, a);
             dot = fma(v, colsum[j], dot);  // Σ_j R_bj Σ_i M_ij = Σ_i c_bi
+            if (colsum_e) dote = fma(v, colsum_e[j], dote);  // Σ over a parent's empty bins
             neg |= v < 0.0;
         }
     if (neg) atomicOr(negflag, 1);
@@ -434,22 +436,29 @@ __global__ void k_r_digits(const double *__restrict__ R, int64_t B, int64_t nt, 
         mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
         dot += __shfl_xor_sync(0xffffffffu, dot, o);
+        dote += __shfl_xor_sync(0xffffffffu, dote, o);
     }
     if ((threadIdx.x & 31) == 0) {
         s_m[0][threadIdx.x >> 5] = mx;
         s_m[1][threadIdx.x >> 5] = mn;
         s_m[2][threadIdx.x >> 5] = dot;
+        s_m[3][threadIdx.x >> 5] = dote;
     }
     __syncthreads();
     mx = 0.0;
     mn = INFINITY;
     dot = 0.0;
+    dote = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
         mx = fmax(mx, s_m[0][w]);
         mn = fmin(mn, s_m[1][w]);
         dot += s_m[2][w];
+        dote += s_m[3][w];
     }
-    if (threadIdx.x == 0) csum[b] = dot;
+    if (threadIdx.x == 0) {
+        csum[b] = dot;
+        if (colsum_e) csum_e[b] = dote;
+    }
     int e = 0;
     if (mx > 0.0) frexp(mx, &e);
     if (e < -120) e = -120;  // the scale stays a normal float
@@ -476,7 +485,7 @@ __global__ void k_r_digits(const double *__restrict__ R, int64_t B, int64_t nt, 
 __global__ void k_logl_reduce_x(const float2 *__restrict__ part, int n_mt, int B, int B_pad,
                                 const double *__restrict__ csum, const int *__restrict__ negflag,
                                 int m_negative, const double *__restrict__ kn,
-                                double *__restrict__ negLogL) {
+                                double *__restrict__ negLogL, const double *__restrict__ csum_e) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= B) return;
     double acc = 0.0;
@@ -485,6 +494,7 @@ __global__ void k_logl_reduce_x(const float2 *__restrict__ part, int n_mt, int B
         acc += (double)v.x + (double)v.y;
     }
     if (!(m_negative || *negflag)) acc -= csum[b];  // else the epilogue subtracted each c
+    else if (csum_e) acc -= csum_e[b];  // and a derived handle's parent's empty bins remain
     acc += *kn;
     negLogL[b] = (acc != 0.0) ? -acc : INFINITY;
 }
@@ -586,7 +596,7 @@ size_t sfh_exact_scratch(const sfh_models *m, int64_t B, int64_t *B_pad_out) {
     const int64_t n_mt = m->nbins_pad128 / XBM;
     if (B_pad_out) *B_pad_out = B_pad;
     return sfh_align256((size_t)kPMax * B_pad * m->nt_pad * 2) + sfh_align256((size_t)B_pad * 4) +
-           256 + sfh_align256((size_t)B_pad * 8) + 256 +
+           256 + 2 * sfh_align256((size_t)B_pad * 8) + 256 +
            sfh_align256((size_t)n_mt * 4 * B_pad * sizeof(float2));
 }
 
@@ -609,6 +619,8 @@ int sfh_exact_prepare(sfh_ctx *ctx, const sfh_models *m, int64_t B, void *scratc
     s += 256;
     xp->csum = (double *)s;
     s += sfh_align256((size_t)B_pad * 8);
+    xp->csum_e = (double *)s;
+    s += sfh_align256((size_t)B_pad * 8);
     xp->lpart = (float2 *)s;
     int rc;
     if ((rc = xmake_map(ctx, &xp->maps[0], m->digits, (int64_t)kQ * m->nbins_pad128, m->nt_pad, XBM)))
@@ -630,7 +642,7 @@ int sfh_exact_launch(sfh_ctx *ctx, const sfh_models *m, const SfhExactPlan &xp, 
     SFH_CK(ctx, cudaMemsetAsync(xp.nplanes, 0, 2 * sizeof(int), st));
     k_r_digits<<<(unsigned)xp.B_pad, 256, 0, st>>>(d_R, xp.B, m->nt, xp.B_pad, m->nt_pad, xp.Rd,
                                                     xp.rscale, xp.nplanes, m->colsum, xp.csum,
-                                                    xp.nplanes + 1);
+                                                    xp.nplanes + 1, m->colsum_e, xp.csum_e);
     SFH_LAUNCHED(ctx);
     if (d_negLogL) {
         k_data_const<<<1, 1024, 0, st>>>(d_data, m->nbins, xp.kn);
@@ -665,7 +677,7 @@ int sfh_exact_launch(sfh_ctx *ctx, const sfh_models *m, const SfhExactPlan &xp, 
     if (d_negLogL) {
         k_logl_reduce_x<<<(unsigned)((xp.B + 255) / 256), 256, 0, st>>>(
             xp.lpart, 4 * xp.n_mt, (int)xp.B, (int)xp.B_pad, xp.csum, xp.nplanes + 1, m->m_negative,
-            xp.kn, d_negLogL);
+            xp.kn, d_negLogL, m->colsum_e ? xp.csum_e : nullptr);
         SFH_LAUNCHED(ctx);
     }
     return SFH_OK;

@@ -53,6 +53,11 @@ extern "C" int sfh_ctx_create(int device, sfh_ctx **out) {
     sfh_ctx *ctx = new sfh_ctx();
     ctx->device = device;
     ctx->sm_count = prop.multiProcessorCount;
+    int pma = 0, pma_host = 0;
+    if (cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, device) == cudaSuccess &&
+        cudaDeviceGetAttribute(&pma_host, cudaDevAttrPageableMemoryAccessUsesHostPageTables,
+                               device) == cudaSuccess)
+        ctx->pageable_direct = pma && pma_host;
     sfh_df tab[SFH_DF_TAB_ALL];
     sfh_df_log_table(tab);
     sfh_df_nlogn_table(tab + SFH_DF_TAB_LOG);
@@ -98,6 +103,24 @@ extern "C" int sfh_ctx_synchronize(sfh_ctx *ctx) {
 extern "C" int sfh_ctx_set_wait_budget(sfh_ctx *ctx, int64_t cycles) {
     if (!ctx || cycles < 0 || (cycles > 0 && cycles < 100000)) return SFH_ERR_ARG;
     ctx->wait_budget = cycles ? (long long)cycles : 4000000000LL;
+    return SFH_OK;
+}
+
+extern "C" int sfh_ctx_set_host_access(sfh_ctx *ctx, int mode) {
+    if (!ctx || mode < SFH_HOST_ACCESS_AUTO || mode > SFH_HOST_ACCESS_DIRECT) return SFH_ERR_ARG;
+    if (mode == SFH_HOST_ACCESS_DIRECT && !ctx->pageable_direct)
+        return sfh_set_error(ctx, SFH_ERR_UNSUPPORTED,
+                             "direct host access needs pageable memory access through the "
+                             "host page tables");
+    ctx->host_access = mode;
+    return SFH_OK;
+}
+
+extern "C" int sfh_ctx_host_access(const sfh_ctx *ctx, int *mode_out) {
+    if (!ctx || !mode_out) return SFH_ERR_ARG;
+    *mode_out = ctx->host_access == SFH_HOST_ACCESS_AUTO
+                    ? (ctx->pageable_direct ? SFH_HOST_ACCESS_DIRECT : SFH_HOST_ACCESS_STAGED)
+                    : ctx->host_access;
     return SFH_OK;
 }
 
@@ -179,6 +202,7 @@ static void free_models(sfh_models *m) {
     if (m->digits) cudaFree(m->digits);
     if (m->escale) cudaFree(m->escale);
     if (m->colsum) cudaFree(m->colsum);
+    sfh_occ_plans_free(m);
     delete m;
 }
 
@@ -285,6 +309,49 @@ extern "C" int sfh_models_upload(sfh_ctx *ctx, const void *host, int src_dtype, 
     if (e != cudaSuccess) { free_models(m); return sfh_cuda_error(ctx, e, "upload models"); }
     int rc = finish_models(ctx, m);
     if (rc != SFH_OK) { free_models(m); return rc; }
+    *out = m;
+    return SFH_OK;
+}
+
+namespace {
+// out[j nrows + p] = M[j nbins + rows[p]] (column-major gather of rows).
+__global__ void k_gather_rows(const float *__restrict__ M, int64_t nbins, int64_t nt,
+                              const int *__restrict__ rows, int64_t nrows, float *__restrict__ out) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nrows * nt) return;
+    const int64_t j = idx / nrows, p = idx - j * nrows;
+    out[idx] = M[j * nbins + rows[p]];
+}
+}  // namespace
+
+int sfh_models_derive_rows(sfh_ctx *ctx, const sfh_models *parent, const int *d_rows,
+                           int64_t nrows, const double *colsum_e, sfh_models **out) {
+    *out = nullptr;
+    if (!parent->d_f32 || nrows <= 0) return sfh_set_error(ctx, SFH_ERR_ARG, "derive_rows");
+    sfh_models *m = new sfh_models();
+    m->device = ctx->device;
+    m->nbins = nrows;
+    m->nt = parent->nt;
+    m->storage = parent->storage;
+    m->occ_mode = SFH_OCC_OFF;
+    const int64_t n = nrows * parent->nt;
+    cudaError_t e = cudaMalloc(&m->d_f32, (size_t)n * sizeof(float));
+    if (e != cudaSuccess) { free_models(m); return sfh_cuda_error(ctx, e, "derive_rows alloc"); }
+    k_gather_rows<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(parent->d_f32, parent->nbins,
+                                                                      parent->nt, d_rows, nrows, m->d_f32);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) { free_models(m); return sfh_cuda_error(ctx, e, "k_gather_rows"); }
+    ctx->launches++;
+    int rc = finish_models(ctx, m);
+    if (rc == SFH_OK && parent->colsum && m->colsum)
+        if ((e = cudaMemcpyAsync(m->colsum, parent->colsum, (size_t)m->nt * 8, cudaMemcpyDeviceToDevice,
+                                 ctx->stream)) != cudaSuccess)
+            rc = sfh_cuda_error(ctx, e, "derive_rows colsum");
+    if (rc == SFH_OK && (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess)
+        rc = sfh_cuda_error(ctx, e, "derive_rows sync");
+    if (rc != SFH_OK) { free_models(m); return rc; }
+    m->m_negative = parent->m_negative;
+    m->colsum_e = colsum_e;
     *out = m;
     return SFH_OK;
 }
@@ -518,13 +585,52 @@ extern "C" int sfh_fg(sfh_ctx *ctx, const sfh_models *m, int dtype, const void *
         }
         return sfh_set_error(ctx, SFH_ERR_NUMERIC, "fg!: non-finite coefficients");
     }
+    int rc;
+    int access = SFH_HOST_ACCESS_STAGED;
+    sfh_ctx_host_access(ctx, &access);
+    const auto al8 = [](const void *p) { return ((uintptr_t)p & 7u) == 0; };
+    if (access == SFH_HOST_ACCESS_DIRECT && dtype == SFH_F64 && composite && al8(coeffs) &&
+        al8(data) && al8(composite) && (!G || al8(G))) {
+        // the kernels read r and n and write the composite, G and -logL in the caller's own
+        // arrays through the host page tables: one launch and one stream sync, no copies
+        // (-logL goes through the staging slot, which a caller's stack variable can share
+        // a page with while the kernel runs).  The host touches both ends of every array
+        // first, so a bad pointer fails here rather than on the device.
+        volatile double sink = ((const double *)data)[0] + ((const double *)data)[nb - 1];
+        (void)sink;
+        ((double *)composite)[0] = 0.0;
+        ((double *)composite)[nb - 1] = 0.0;
+        if (G) {
+            ((double *)G)[0] = 0.0;
+            ((double *)G)[nt - 1] = 0.0;
+        }
+        if ((rc = sfh_host_stage_reserve(ctx, 256))) return rc;
+        double *hl = (double *)ctx->h_stage;
+        FgArgs a{};
+        a.coeffs = (const double *)coeffs;
+        a.data = (const double *)data;
+        a.composite = (double *)composite;
+        a.G = (double *)G;
+        a.negLogL = negLogL ? (double *)ctx->d_h_stage : nullptr;
+        a.eps = eps_of(dtype);
+        a.gsign = 1.0;
+        a.mode = FG_MODE_FG;
+        a.occ_key = m;  // one plan slot for the host-array calls on this handle
+        if ((rc = sfh_launch_fg(ctx, m, a))) return rc;
+        SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+        if (negLogL) {
+            const double v = *(volatile double *)hl;
+            if (std::isnan(v) && (rc = sfh_check_onepass(ctx))) return rc;
+            *negLogL = v;
+        }
+        return SFH_OK;
+    }
     // inputs [r | n] and outputs [composite | G | -logL] in the mapped pinned staging area:
     // the kernels read the inputs and write the outputs across the host link themselves, so
     // a call is one copy in, one launch, one stream sync and one copy out
     const size_t o_r = 0, o_n = sfh_align256(nt * 8), o_c = o_n + sfh_align256(nb * 8),
                  o_g = o_c + sfh_align256(nb * 8), o_l = o_g + sfh_align256(nt * 8),
                  o_end = o_l + 8;
-    int rc;
     if ((rc = sfh_host_stage_reserve(ctx, o_end + 256))) return rc;
     char *base = (char *)ctx->d_h_stage, *hb = (char *)ctx->h_stage;
     double *hr = (double *)(hb + o_r), *hn = (double *)(hb + o_n);
@@ -545,6 +651,7 @@ extern "C" int sfh_fg(sfh_ctx *ctx, const sfh_models *m, int dtype, const void *
     a.eps = eps_of(dtype);
     a.gsign = 1.0;
     a.mode = FG_MODE_FG;
+    a.occ_key = m;
     if ((rc = sfh_launch_fg(ctx, m, a))) return rc;
     SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
     if (negLogL) {

@@ -414,7 +414,9 @@ int sfh_bfgs_run(sfh_ctx *ctx, int64_t nvar, const double *d_theta0, const sfh_f
         if (use_graph) {
             int r = SFH_OK;
             const int64_t l0 = ctx->launches;
+            ctx->internal_capture = true;  // the graph lives only inside this call
             for (int k = 0; k < K && !r; ++k) r = slot();
+            ctx->internal_capture = false;
             cudaError_t e = cudaStreamEndCapture(st, &graph);
             per_replay = ctx->launches - l0;
             ctx->launches = l0;  // captured, not launched: counted per replay below

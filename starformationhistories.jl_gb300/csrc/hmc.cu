@@ -421,6 +421,7 @@ struct HmcRun {
     ChainState s;
     MzrDev z;
     SfhBatchedPlan plan;
+    const sfh_models *mb = nullptr;  // the handle the batched evaluations use
     double *d_r = nullptr, *d_negL = nullptr;
     float *d_G = nullptr;
     double eps_abs;
@@ -435,8 +436,8 @@ int launch_eval(sfh_ctx *ctx, const sfh_models *m, HmcRun &h, bool want_logd) {
         k_mzr_map<<<h.c.B, kT, 0, st>>>(h.s.theta, h.c, h.z, h.d_r);
     }
     SFH_LAUNCHED(ctx);
-    int rc = sfh_batched_launch(ctx, m, h.plan, h.d_r, want_logd ? h.d_negL : nullptr, h.d_G,
-                                h.eps_abs);
+    int rc = sfh_batched_launch(ctx, h.mb ? h.mb : m, h.plan, h.d_r, want_logd ? h.d_negL : nullptr,
+                                h.d_G, h.eps_abs);
     if (rc) return rc;
     if (h.c.model == 0) {
         k_direct_grad<<<h.c.B, kT, 0, st>>>(h.s.theta, h.d_r, h.d_G, h.d_negL, h.c.D, h.s.g,
@@ -629,9 +630,25 @@ int setup_run(sfh_ctx *ctx, const sfh_models *m, const double *d_data, const sfh
         if (!p) return sfh_set_error(ctx, SFH_ERR_NOMEM, "HMC buffers");
     if (!batched) return SFH_OK;
     int rc;
-    if ((rc = sfh_batched_prepare(ctx, m, c.B, d_data, nullptr, 0, &h.plan))) return rc;
+    // the occupied-bin plan's derived handle (the diagram is fixed for the whole run: its
+    // counts are gathered and checked once here)
+    const sfh_models *mb = m;
+    const double *db = d_data;
+    SfhOccPlan *occ = nullptr;
+    if ((rc = sfh_occ_batched(ctx, const_cast<sfh_models *>(m), d_data, true, &mb, &db, &occ)))
+        return rc;
+    if (occ) {
+        SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+        if (*occ->h_bviol) {
+            sfh_occ_retire(occ);
+            mb = m;
+            db = d_data;
+        }
+    }
+    h.mb = mb;
+    if ((rc = sfh_batched_prepare(ctx, mb, c.B, db, nullptr, 0, &h.plan))) return rc;
     if ((rc = sfh_scratch_reserve(ctx, h.plan.scratch_bytes))) return rc;
-    return sfh_batched_prepare(ctx, m, c.B, d_data, ctx->scratch, ctx->scratch_bytes, &h.plan);
+    return sfh_batched_prepare(ctx, mb, c.B, db, ctx->scratch, ctx->scratch_bytes, &h.plan);
 }
 
 void free_run(sfh_ctx *ctx, std::vector<void *> &owned) {
@@ -698,7 +715,9 @@ extern "C" int sfh_hmc_sample_dev(sfh_ctx *ctx, const sfh_models *m, const doubl
         if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) use_graph = false;
     }
     if (use_graph) {
+        ctx->internal_capture = true;  // the graph lives only inside this call
         rc = launch_trajectory(ctx, m, h);
+        ctx->internal_capture = false;
         cudaError_t e = cudaStreamEndCapture(st, &graph);
         if (rc || e != cudaSuccess || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
             if (graph) cudaGraphDestroy(graph);

@@ -739,7 +739,7 @@ int sfh_launch_fg(sfh_ctx *ctx, const sfh_models *m, const FgArgs &a, cudaEvent_
         if (rc) return rc;
         return sfh_launch_fg_onepass(ctx, const_cast<sfh_models *>(m), a.coeffs, a.data,
                                      a.composite, a.G, a.negLogL, a.eps, a.gsign, ctx->scratch, ev,
-                                     a.skip);
+                                     a.skip, a.occ_key);
     }
     const bool fused_path = !f64 && (a.mode == FG_MODE_FG || a.mode == FG_MODE_COMPOSITE);
     const Plan p = make_plan(ctx, nbins, nt, f64, fused_path, m);

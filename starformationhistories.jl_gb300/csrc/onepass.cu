@@ -36,7 +36,10 @@
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <vector>
 
 #include "sfh_internal.cuh"
 #include "sfh_ptx.cuh"
@@ -91,7 +94,42 @@ struct OnePassArgs {
     const float2 *rowb;   // per bin: (sum, max) of |M_ij| over the templates (the anchors' bound)
     long long budget;     // SM cycles a device wait may take before the launch gives up
     int drop_copy;        // test-only: producer lane 0 skips its first bulk copy
+    // Occupied-bin plan (all NULL for the dense kernel).  Tile bin p is bin occ[p] (nbins
+    // above counts the tile bins); empty[0 .. nempty) are the plan's empty bins; colsum_e
+    // their per-template column sums E_j; viol counts empty bins found occupied in this
+    // launch (reset by the launch), flag is set for the host when one was; mcol is the
+    // (nbins_all, nt) column-major FP32 matrix the in-launch correction reads.
+    const int *occ;
+    const int *empty;
+    int64_t nempty, nbins_all;
+    const double *colsum_e;
+    unsigned int *viol;
+    unsigned int *flag;
+    const float *mcol;
 };
+
+// Grid barrier over the launch's resident CTAs (arrivals a.bar[0], generation a.bar[1]),
+// called by one thread per CTA; bounded like the pipeline's waits.
+__device__ __forceinline__ void op_grid_barrier(const OnePassArgs &a) {
+    __threadfence();
+    volatile unsigned int *gen = a.bar + 1;
+    const unsigned int g0 = *gen;
+    if (atomicAdd(a.bar, 1u) == gridDim.x - 1) {
+        *a.bar = 0u;  // re-armed for the next use
+        __threadfence();
+        atomicAdd(a.bar + 1, 1u);
+    } else {
+        const long long t0 = clock64();
+        while (*gen == g0) {
+            if (clock64() - t0 > a.budget) {
+                atomicExch(a.err, 3u);
+                break;
+            }
+            __nanosleep(64);
+        }
+    }
+    __threadfence();
+}
 
 // Dynamic shared memory: ring | r (hi, lo) | s_part | s_w | s_cn | s_tab | full | empty |
 // flags.
@@ -120,6 +158,57 @@ __device__ __forceinline__ void op_anchors(const OnePassArgs &a, int64_t i0, flo
     }
     sg01 = make_float2(sg[0], sg[1]);
     sg23 = make_float2(sg[2], sg[3]);
+}
+
+// Empty bins of the plan that this call's data occupies (the CTA's share of a.empty, as
+// checked in the prologue): each becomes a tile bin after the fact.  Per bin the consumer
+// threads form c = Σ_j M_ij r_j in FP64 (a fixed reduction tree), thread 0 applies the
+// finish's arithmetic (clamp, w in FP32, the Poisson term) and adds t_i + c_i to the
+// CTA's logL partial (the plan subtracted c_i through E_j), and G's partial gets
+// M_ij (w_i - 1) (E_j counted the bin with w = 1).  Slow, exact, and rare: the next call
+// builds a plan for the new data.  `red` holds at least 32 doubles of shared memory.
+__device__ __noinline__ void op_fold_occupied(const OnePassArgs &a, const sfh_df *s_tab, double *red) {
+    const int nthr = (int)(blockDim.x - 32);  // the consumer threads
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5, nwarps = nthr >> 5;
+    __shared__ float s_wfold;
+    double lcorr = 0.0;
+    for (int64_t k0 = (int64_t)blockIdx.x * nthr; k0 < a.nempty; k0 += (int64_t)gridDim.x * nthr) {
+        for (int q = 0; q < nthr && k0 + q < a.nempty; ++q) {  // the share's bins in order
+            const int i = __ldg(a.empty + k0 + q);
+            const double n = a.data[i];
+            if (n == 0.0) continue;  // the same value in every thread
+            double c = 0.0;
+            for (int64_t j = t; j < a.nt; j += nthr) c = fma((double)a.mcol[j * a.nbins_all + i], a.r[j], c);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+            if (lane == 0) red[warp] = c;
+            named_bar_sync(1, nthr);
+            if (t == 0) {
+                double tot = 0.0;
+                for (int w = 0; w < nwarps; ++w) tot += red[w];
+                const float ch = __double2float_rn(tot);
+                sfh_df cm{ch, __double2float_rn(tot - (double)ch)};
+                if (cm.h < a.eps_f || (cm.h == a.eps_f && cm.l < 0.f)) cm = sfh_df{a.eps_f, 0.f};
+                float nh, nl;
+                sfh_split_double(n, nh, nl);
+                const float wv = __fdiv_rn(df_add(cm, sfh_df{-nh, -nl}).h, cm.h);
+                a.composite[i] = sfh_f2d(wv);
+                s_wfold = wv;
+                if (a.want_logl) {
+                    const sfh_df tt = sfh_bin_term(cm, nh, nl, s_tab);
+                    lcorr += (sfh_f2d(tt.h) + sfh_f2d(tt.l)) + tot;
+                }
+            }
+            named_bar_sync(1, nthr);
+            if (a.gpart) {
+                const double wm1 = (double)s_wfold - 1.0;
+                for (int64_t j = t; j < a.nt; j += nthr)
+                    a.gpart[(int64_t)blockIdx.x * a.nt + j] += (double)a.mcol[j * a.nbins_all + i] * wm1;
+            }
+            named_bar_sync(1, nthr);
+        }
+    }
+    if (t == 0 && a.want_logl) a.lpart[blockIdx.x] += lcorr;
 }
 
 template <int BINS, int OWN, bool SKEW>
@@ -167,6 +256,7 @@ k_fg_onepass(const OnePassArgs a) {
     // the first copies are issued now; the consumers stage r and the tables meanwhile and
     // meet at a consumer-only barrier before their first tile
     __shared__ float s_rstat[2][32];  // per consumer warp: max and sum of |r|
+    __shared__ unsigned int s_nviol;  // the CTA's empty bins found occupied
     if (warp < kWarps) {
         const int nk = nch * kBoxCols, ct = kWarps * 32;
         float rmx = 0.f, rsm = 0.f;
@@ -197,7 +287,24 @@ k_fg_onepass(const OnePassArgs a) {
         }
         if (a.want_logl)
             for (int k = threadIdx.x; k < SFH_DF_TAB_ALL; k += ct) s_tab[k] = a.tab[k];
+        if (a.empty) {
+            // the plan's empty bins: w = 1 in the output, and a check that n is still <= 0
+            // (each thread one bin of the CTA's share per pass, loads issued together)
+            if (threadIdx.x == 0) s_nviol = 0;
+            named_bar_sync(1, kWarps * 32);
+            unsigned int nv = 0;
+            for (int64_t k0 = (int64_t)blockIdx.x * ct; k0 < a.nempty; k0 += (int64_t)gridDim.x * ct) {
+                const int64_t k = k0 + threadIdx.x;
+                if (k < a.nempty) {
+                    const int i = __ldg(a.empty + k);
+                    a.composite[i] = 1.0;
+                    nv += a.data[i] != 0.0 ? 1u : 0u;  // w = 1 needs n = 0 exactly
+                }
+            }
+            if (nv) atomicAdd(&s_nviol, nv);
+        }
         named_bar_sync(1, kWarps * 32);
+        if (a.empty && threadIdx.x == 0 && s_nviol) atomicAdd(a.viol, s_nviol);
     }
 
     // ------------------------------------------------------------ producers
@@ -276,7 +383,11 @@ k_fg_onepass(const OnePassArgs a) {
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
         const int64_t tb = (int64_t)t * BINS;
         double nd = 0.0;
-        if (finisher && fl == 0 && tb + fb < nbins) nd = a.data[tb + fb];  // loads while boxes land
+        int64_t ib = tb + fb;  // the finisher lane's bin (through the plan's map)
+        if (finisher && fl == 0 && tb + fb < nbins) {  // loads while boxes land
+            if (a.occ) ib = __ldg(a.occ + tb + fb);
+            nd = a.data[ib];
+        }
         __syncwarp();  // lane-dependent code ends: reconverge the warp (here and below)
         if (owner) {
             // phase A: m r over the owner's units for the lane's 4 bins (r split hi + lo,
@@ -339,14 +450,14 @@ k_fg_onepass(const OnePassArgs a) {
             if (fl == 0) {
                 float wv = 0.f;
                 if (i < nbins) {
-                    if (!want_g) a.composite[i] = sfh_f2d(cm.h) + sfh_f2d(cm.l);  // the model, unclamped
+                    if (!want_g) a.composite[ib] = sfh_f2d(cm.h) + sfh_f2d(cm.l);  // the model, unclamped
                     // max(composite, eps(T)); eps(T) is a power of two, exact in FP32
                     if (cm.h < a.eps_f || (cm.h == a.eps_f && cm.l < 0.f)) cm = sfh_df{a.eps_f, 0.f};
                     float nh, nl;
                     sfh_split_double(nd, nh, nl);
                     if (want_g) {
                         wv = __fdiv_rn(df_add(cm, sfh_df{-nh, -nl}).h, cm.h);  // 1 - n/c
-                        a.composite[i] = sfh_f2d(wv);
+                        a.composite[ib] = sfh_f2d(wv);
                     }
                     s_cn[fb] = make_float4(cm.h, cm.l, nh, nl);
                 }
@@ -409,7 +520,11 @@ k_fg_onepass(const OnePassArgs a) {
         const bool doA = it < nloc, doB = it > 0;  // the same in every warp
         const int64_t tb = ((int64_t)blockIdx.x + (int64_t)it * gridDim.x) * BINS;  // tile it
         double nd = 0.0;
-        if (doA && finisher && fl == 0 && tb + fb < nbins) nd = a.data[tb + fb];
+        int64_t ib = tb + fb;
+        if (doA && finisher && fl == 0 && tb + fb < nbins) {
+            if (a.occ) ib = __ldg(a.occ + tb + fb);
+            nd = a.data[ib];
+        }
         __syncwarp();
         if (owner) {
             float2 sg01 = make_float2(1.f, 1.f), sg23 = sg01;
@@ -510,13 +625,13 @@ k_fg_onepass(const OnePassArgs a) {
             if (fl == 0) {
                 float wv = 0.f;
                 if (i < nbins) {
-                    if (!want_g) a.composite[i] = sfh_f2d(cm.h) + sfh_f2d(cm.l);
+                    if (!want_g) a.composite[ib] = sfh_f2d(cm.h) + sfh_f2d(cm.l);
                     if (cm.h < a.eps_f || (cm.h == a.eps_f && cm.l < 0.f)) cm = sfh_df{a.eps_f, 0.f};
                     float nh, nl;
                     sfh_split_double(nd, nh, nl);
                     if (want_g) {
                         wv = __fdiv_rn(df_add(cm, sfh_df{-nh, -nl}).h, cm.h);
-                        a.composite[i] = sfh_f2d(wv);
+                        a.composite[ib] = sfh_f2d(wv);
                     }
                     s_cn[fb] = make_float4(cm.h, cm.l, nh, nl);
                 }
@@ -563,27 +678,20 @@ k_fg_onepass(const OnePassArgs a) {
     // over CTAs, a fixed shuffle tree) and CTA 0 sums -logL: a fixed order, so results are
     // reproducible.  The barrier's wait is bounded like the pipeline's.
     named_bar_sync(1, kWarps * 32);  // this CTA's partials are written
-    if (threadIdx.x == 0) {
-        __threadfence();
-        volatile unsigned int *gen = a.bar + 1;
-        const unsigned int g0 = *gen;
-        if (atomicAdd(a.bar, 1u) == gridDim.x - 1) {
-            *a.bar = 0u;  // re-armed for the next launch
-            __threadfence();
-            atomicAdd(a.bar + 1, 1u);
-        } else {
-            const long long t0 = clock64();
-            while (*gen == g0) {
-                if (clock64() - t0 > a.budget) {
-                    atomicExch(err, 3);
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-    }
+    if (threadIdx.x == 0) op_grid_barrier(a);
     named_bar_sync(1, kWarps * 32);
+    if (a.empty && *(volatile unsigned int *)a.viol != 0u) {
+        // some plan-empty bin is occupied in this call's data: every CTA folds in the ones
+        // of its share exactly (the same arithmetic as a tile bin), then a second barrier
+        op_fold_occupied(a, s_tab, (double *)s_part);
+        named_bar_sync(1, kWarps * 32);
+        if (threadIdx.x == 0) op_grid_barrier(a);
+        named_bar_sync(1, kWarps * 32);
+        if (blockIdx.x == 0 && threadIdx.x == 0) {  // every CTA read the count before
+            *(volatile unsigned int *)a.viol = 0u;  // the second barrier
+            *(volatile unsigned int *)a.flag = 1u;  // the host builds a new plan
+        }
+    }
     const bool bad = *(volatile unsigned int *)a.err != 0u;
     if (a.G) {  // warp w sums columns j0 + w, j0 + w + kWarps, ...: lane l takes CTAs
                 // l, l + 32, ..., then a fixed shuffle tree
@@ -603,6 +711,7 @@ k_fg_onepass(const OnePassArgs a) {
             for (int q = 0; q < 12; ++q) acc += v[q];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+            if (a.colsum_e) acc += a.colsum_e[j];  // the empty bins, w = 1
             if (lane == 0) a.G[j] = bad ? NAN : a.gsign * acc;
         }
     }
@@ -616,6 +725,8 @@ k_fg_onepass(const OnePassArgs a) {
         double acc = 0.0;
 #pragma unroll
         for (int q = 0; q < 12; ++q) acc += v[q];
+        if (a.colsum_e)  // the empty bins: -Σ_j r_j E_j
+            for (int64_t j = lane; j < a.nt; j += 32) acc = fma(-a.r[j], a.colsum_e[j], acc);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
         // loglikelihood returns -typemax(T) = -Inf when the sum is exactly zero (fitting_base.jl:95)
@@ -635,6 +746,63 @@ __global__ void k_onepass_block(const float *__restrict__ M, int64_t nbins, int6
     const int64_t c = tc % nch, t = tc / nch;
     const int64_t bin = t * bins + b, col = c * kBoxCols + j;
     blk[idx] = (bin < nbins && col < nt) ? M[col * nbins + bin] : 0.f;
+}
+
+// Blocked copy of a plan's occupied rows for BINS-bin tiles: as k_onepass_block with tile
+// bin p standing for bin occ[p] (occ[p] < 0: padding, zero).
+__global__ void k_occ_block(const float *__restrict__ M, int64_t nbins, int64_t nt, int bins,
+                            int nch, int64_t total, const int *__restrict__ occ,
+                            float *__restrict__ blk) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const int64_t b = idx % bins, rest = idx / bins;
+    const int64_t j = rest % kBoxCols, tc = rest / kBoxCols;
+    const int64_t c = tc % nch, t = tc / nch;
+    const int bin = occ[t * bins + b];
+    const int64_t col = c * kBoxCols + j;
+    blk[idx] = (bin >= 0 && col < nt) ? M[col * nbins + bin] : 0.f;
+}
+
+// Row statistics of the tile bins (zero for padding).
+__global__ void k_occ_rowb(const float2 *__restrict__ rowb, const int *__restrict__ occ, int64_t n,
+                           float2 *__restrict__ out) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int bin = occ[p];
+    out[p] = bin >= 0 ? rowb[bin] : make_float2(0.f, 0.f);
+}
+
+// E_j = Σ over the empty bins of M_ij in FP64, one block per template (fixed tree).
+__global__ void k_occ_colsum(const float *__restrict__ M, int64_t nbins,
+                             const int *__restrict__ empty, int64_t nempty,
+                             double *__restrict__ out) {
+    __shared__ double s_red[32];
+    const int64_t j = blockIdx.x;
+    double acc = 0.0;
+    for (int64_t k = threadIdx.x; k < nempty; k += blockDim.x) acc += (double)M[j * nbins + empty[k]];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tot = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += s_red[w];
+        out[j] = tot;
+    }
+}
+
+// Counts of the occupied bins for the derived handle (out[p] = data[rows[p]]) and the check
+// that the plan's empty bins are still empty (their count into *viol).
+__global__ void k_occ_gather(const double *__restrict__ data, const int *__restrict__ rows,
+                             int64_t nocc, const int *__restrict__ empty, int64_t nempty,
+                             double *__restrict__ out, unsigned int *viol) {
+    unsigned int nv = 0;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nocc || k < nempty;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        if (k < nocc) out[k] = data[rows[k]];
+        if (k < nempty) nv += data[empty[k]] != 0.0 ? 1u : 0u;
+    }
+    if (nv) atomicAdd(viol, nv);
 }
 
 // Shared memory a CTA may use when `per_sm` CTAs share an SM.
@@ -753,6 +921,260 @@ bool sfh_onepass_choose(sfh_ctx *ctx, const sfh_models *m, OnePassChoice *c) {
     return runs > 0;
 }
 
+// ------------------------------------------------------------------ occupied-bin plans
+static void occ_plan_free(SfhOccPlan &p) {
+    for (int k = 0; k < 2; ++k) {
+        if (p.d_occ[k]) cudaFree(p.d_occ[k]);
+        if (p.d_blk[k]) cudaFree(p.d_blk[k]);
+        if (p.d_rowb[k]) cudaFree(p.d_rowb[k]);
+    }
+    if (p.d_empty) cudaFree(p.d_empty);
+    if (p.d_colsum_e) cudaFree(p.d_colsum_e);
+    if (p.d_viol) cudaFree(p.d_viol);
+    if (p.h_flag) cudaFreeHost((void *)p.h_flag);
+    if (p.sub) sfh_models_free(p.sub);
+    if (p.d_rows) cudaFree(p.d_rows);
+    if (p.d_nocc) cudaFree(p.d_nocc);
+    if (p.h_bviol) cudaFreeHost((void *)p.h_bviol);
+    p = SfhOccPlan{};
+}
+
+void sfh_occ_plans_free(sfh_models *m) {
+    for (int k = 0; k < m->nocc_plans; ++k) occ_plan_free(m->occ[k]);
+    m->nocc_plans = 0;
+}
+
+// A new plan for the diagram at d_data (device, mapped or host-page-table memory): one
+// synchronous copy of the counts to the host, the bin lists, E_j.  The per-width parts
+// come from occ_plan_width, from the same snapshot.
+static int occ_plan_build(sfh_ctx *ctx, sfh_models *m, const void *key, const double *d_data,
+                          int streak, SfhOccPlan &p) {
+    const auto t0 = std::chrono::steady_clock::now();
+    const int64_t nbins = m->nbins, nt = m->nt;
+    std::vector<double> h((size_t)nbins);
+    SFH_CK(ctx, cudaMemcpyAsync(h.data(), d_data, (size_t)nbins * 8, cudaMemcpyDefault, ctx->stream));
+    SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    std::vector<int> empty, occ;
+    for (int64_t i = 0; i < nbins; ++i) {
+        if (h[i] != 0.0) occ.push_back((int)i);  // NaN and negative counts stay tile bins
+        else empty.push_back((int)i);
+    }
+    p = SfhOccPlan{};
+    p.key = key;
+    p.streak = streak;
+    p.nocc = (int64_t)occ.size();
+    p.nempty = (int64_t)empty.size();
+    const bool some = p.nocc > 0 && p.nempty > 0;
+    p.sparse = some && streak < 3 &&
+               (m->occ_mode == SFH_OCC_ON || (double)p.nocc <= 0.6 * (double)nbins);
+    if (p.sparse) {
+        p.occ_host = std::move(occ);
+        SFH_CK(ctx, cudaMalloc(&p.d_empty, (size_t)p.nempty * sizeof(int)));
+        SFH_CK(ctx, cudaMalloc(&p.d_colsum_e, (size_t)nt * sizeof(double)));
+        SFH_CK(ctx, cudaMalloc(&p.d_viol, sizeof(unsigned int)));
+        void *hf = nullptr;
+        SFH_CK(ctx, cudaHostAlloc(&hf, sizeof(unsigned int), cudaHostAllocMapped));
+        p.h_flag = (volatile unsigned int *)hf;
+        *p.h_flag = 0u;
+        SFH_CK(ctx, cudaHostGetDevicePointer((void **)&p.d_flag, hf, 0));
+        SFH_CK(ctx, cudaMemcpyAsync(p.d_empty, empty.data(), (size_t)p.nempty * sizeof(int),
+                                    cudaMemcpyHostToDevice, ctx->stream));
+        SFH_CK(ctx, cudaMemsetAsync(p.d_viol, 0, sizeof(unsigned int), ctx->stream));
+        k_occ_colsum<<<(unsigned)nt, 256, 0, ctx->stream>>>(m->d_f32, nbins, p.d_empty, p.nempty,
+                                                          p.d_colsum_e);
+        SFH_LAUNCHED(ctx);
+        SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));  // `empty` leaves scope
+    }
+    m->occ_build_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return SFH_OK;
+}
+
+// The tile-width parts of a sparse plan (occupied bins padded to whole tiles, their
+// blocked rows and row statistics), built on first use of the width.
+static int occ_plan_width(sfh_ctx *ctx, sfh_models *m, SfhOccPlan &p, int bins, int mi, int nch) {
+    if (p.d_blk[mi]) return SFH_OK;
+    const int64_t nbins = m->nbins, nt = m->nt;
+    const int64_t ntiles = (p.nocc + bins - 1) / bins;
+    std::vector<int> occ((size_t)(ntiles * bins), -1);
+    std::copy(p.occ_host.begin(), p.occ_host.end(), occ.begin());
+    const int64_t total = ntiles * nch * kBoxCols * bins;
+    SFH_CK(ctx, cudaMalloc(&p.d_occ[mi], occ.size() * sizeof(int)));
+    SFH_CK(ctx, cudaMalloc(&p.d_rowb[mi], occ.size() * sizeof(float2)));
+    SFH_CK(ctx, cudaMalloc(&p.d_blk[mi], (size_t)total * sizeof(float)));
+    SFH_CK(ctx, cudaMemcpyAsync(p.d_occ[mi], occ.data(), occ.size() * sizeof(int),
+                                cudaMemcpyHostToDevice, ctx->stream));
+    k_occ_rowb<<<(unsigned)((occ.size() + 255) / 256), 256, 0, ctx->stream>>>(
+        m->d_rowb, p.d_occ[mi], (int64_t)occ.size(), p.d_rowb[mi]);
+    SFH_LAUNCHED(ctx);
+    k_occ_block<<<(unsigned)((total + 255) / 256), 256, 0, ctx->stream>>>(
+        m->d_f32, nbins, nt, bins, nch, total, p.d_occ[mi], p.d_blk[mi]);
+    SFH_LAUNCHED(ctx);
+    SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));  // `occ` leaves scope
+    return SFH_OK;
+}
+
+// The sparse plan serving `key` (the data pointer, or the handle's host-array slot) at
+// this tile width, or NULL for the dense kernel.  A plan whose launches saw an occupied
+// empty bin is retired and replaced; with every slot taken the least recently used plan
+// that no capture holds is freed.  During stream capture only an existing, complete plan
+// is used (and is then kept for the handle's lifetime).
+static SfhOccPlan *occ_plan_get(sfh_ctx *ctx, sfh_models *m, const void *key,
+                                const double *d_data, int bins, int mi, int nch, int *rc) {
+    *rc = SFH_OK;
+    if (m->occ_mode == SFH_OCC_OFF || !m->d_rowb || !key) return nullptr;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(ctx->stream, &cs) != cudaSuccess) return nullptr;
+    const bool capturing = cs != cudaStreamCaptureStatusNone;
+    SfhOccPlan *p = nullptr;
+    for (int k = 0; k < m->nocc_plans; ++k)
+        if (!m->occ[k].retired && m->occ[k].key == key) p = &m->occ[k];
+    int streak = 0;
+    if (p && p->sparse && !capturing && *p->h_flag) {
+        p->retired = true;
+        streak = p->streak + 1;
+        p = nullptr;
+    }
+    if (!p) {
+        if (capturing) return nullptr;
+        int slot = -1;
+        if (m->nocc_plans < kSfhOccPlans) {
+            slot = m->nocc_plans++;
+        } else {  // evict: retired first, then the least recently used
+            uint64_t best = UINT64_MAX;
+            for (int k = 0; k < kSfhOccPlans; ++k) {
+                const SfhOccPlan &q = m->occ[k];
+                if (q.captured) continue;
+                const uint64_t age = q.retired ? 0 : q.last_use + 1;
+                if (age < best) { best = age; slot = k; }
+            }
+            if (slot < 0) return nullptr;  // every plan is held by a capture
+            cudaError_t e = cudaStreamSynchronize(ctx->stream);
+            if (e != cudaSuccess) {
+                *rc = sfh_cuda_error(ctx, e, "occupied-bin plan eviction");
+                return nullptr;
+            }
+            occ_plan_free(m->occ[slot]);
+        }
+        if ((*rc = occ_plan_build(ctx, m, key, d_data, streak, m->occ[slot]))) {
+            occ_plan_free(m->occ[slot]);
+            m->occ[slot].retired = true;
+            return nullptr;
+        }
+        p = &m->occ[slot];
+    }
+    p->last_use = ++m->occ_clock;
+    if (!p->sparse) return nullptr;
+    if (!p->d_blk[mi]) {
+        if (capturing) return nullptr;
+        if ((*rc = occ_plan_width(ctx, m, *p, bins, mi, nch))) return nullptr;
+    }
+    if (capturing && !ctx->internal_capture) p->captured = true;
+    return p;
+}
+
+// The batched path's part of a plan: the occupied bins, the derived handle of their rows,
+// the gathered counts and the mapped check count (built on first use).
+static int occ_plan_batched_parts(sfh_ctx *ctx, sfh_models *m, SfhOccPlan &p) {
+    if (p.sub) return SFH_OK;
+    SFH_CK(ctx, cudaMalloc(&p.d_rows, (size_t)p.nocc * sizeof(int)));
+    SFH_CK(ctx, cudaMalloc(&p.d_nocc, (size_t)p.nocc * sizeof(double)));
+    void *hv = nullptr;
+    SFH_CK(ctx, cudaHostAlloc(&hv, sizeof(unsigned int), cudaHostAllocMapped));
+    p.h_bviol = (volatile unsigned int *)hv;
+    *p.h_bviol = 0u;
+    SFH_CK(ctx, cudaHostGetDevicePointer((void **)&p.d_bviol, hv, 0));
+    SFH_CK(ctx, cudaMemcpyAsync(p.d_rows, p.occ_host.data(), (size_t)p.nocc * sizeof(int),
+                                cudaMemcpyHostToDevice, ctx->stream));
+    return sfh_models_derive_rows(ctx, m, p.d_rows, p.nocc, p.d_colsum_e, &p.sub);  // syncs
+}
+
+void sfh_occ_retire(SfhOccPlan *p) {
+    if (p) p->retired = true;
+}
+
+int sfh_occ_batched(sfh_ctx *ctx, sfh_models *m, const double *d_data, bool want_l,
+                    const sfh_models **mb, const double **db, SfhOccPlan **plan) {
+    *mb = m;
+    *db = d_data;
+    *plan = nullptr;
+    if (m->occ_mode == SFH_OCC_OFF || m->storage != SFH_BF16X2 || !m->colsum || !m->d_f32)
+        return SFH_OK;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(ctx->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)
+        return SFH_OK;
+    SfhOccPlan *p = nullptr;
+    for (int k = 0; k < m->nocc_plans; ++k)
+        if (!m->occ[k].retired && m->occ[k].key == d_data) p = &m->occ[k];
+    int streak = 0;
+    if (p && p->sparse && (*p->h_flag || (p->h_bviol && *p->h_bviol))) {
+        p->retired = true;
+        streak = p->streak + 1;
+        p = nullptr;
+    }
+    if (!p) {
+        int slot = -1;
+        if (m->nocc_plans < kSfhOccPlans) {
+            slot = m->nocc_plans++;
+        } else {
+            uint64_t best = UINT64_MAX;
+            for (int k = 0; k < kSfhOccPlans; ++k) {
+                const SfhOccPlan &q = m->occ[k];
+                if (q.captured) continue;
+                const uint64_t age = q.retired ? 0 : q.last_use + 1;
+                if (age < best) { best = age; slot = k; }
+            }
+            if (slot < 0) return SFH_OK;
+            SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+            occ_plan_free(m->occ[slot]);
+        }
+        int rc = occ_plan_build(ctx, m, d_data, d_data, streak, m->occ[slot]);
+        if (rc) {
+            occ_plan_free(m->occ[slot]);
+            m->occ[slot].retired = true;
+            return rc;
+        }
+        p = &m->occ[slot];
+    }
+    p->last_use = ++m->occ_clock;
+    if (!p->sparse) return SFH_OK;
+    int rc = occ_plan_batched_parts(ctx, m, *p);
+    if (rc) {
+        p->retired = true;
+        return rc;
+    }
+    if (want_l && !sfh_exact_supported(p->sub)) return SFH_OK;  // the split logL needs it
+    *p->h_bviol = 0u;  // the previous batched call on this plan has completed (it synced)
+    const int64_t n = p->nocc > p->nempty ? p->nocc : p->nempty;
+    k_occ_gather<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, ctx->stream>>>(
+        d_data, p->d_rows, p->nocc, p->d_empty, p->nempty, p->d_nocc, p->d_bviol);
+    SFH_LAUNCHED(ctx);
+    *mb = p->sub;
+    *db = p->d_nocc;
+    *plan = p;
+    return SFH_OK;
+}
+
+extern "C" int sfh_models_set_occupied(sfh_ctx *ctx, sfh_models *m, int mode) {
+    if (!ctx || !m || mode < SFH_OCC_OFF || mode > SFH_OCC_ON) return SFH_ERR_ARG;
+    if (mode != m->occ_mode)  // plans were chosen under the old mode
+        for (int k = 0; k < m->nocc_plans; ++k) m->occ[k].retired = true;
+    m->occ_mode = mode;
+    return SFH_OK;
+}
+
+extern "C" int sfh_models_occupied_info(sfh_ctx *ctx, const sfh_models *m, const double *d_data,
+                                        int64_t *nocc_out, int *sparse_out, double *build_ms_out) {
+    if (!ctx || !m) return SFH_ERR_ARG;
+    const SfhOccPlan *p = nullptr;
+    for (int k = 0; k < m->nocc_plans; ++k)
+        if (!m->occ[k].retired && m->occ[k].key == d_data) p = &m->occ[k];
+    if (nocc_out) *nocc_out = p ? p->nocc : -1;
+    if (sparse_out) *sparse_out = p && p->sparse ? 1 : 0;
+    if (build_ms_out) *build_ms_out = m->occ_build_ms;
+    return SFH_OK;
+}
+
 size_t sfh_onepass_scratch(const sfh_ctx *ctx, const sfh_models *m) {  // up to 2 CTAs per SM
     return sfh_align256((size_t)2 * ctx->sm_count * (size_t)m->nt * 8) +
            sfh_align256((size_t)2 * ctx->sm_count * 8);
@@ -761,7 +1183,7 @@ size_t sfh_onepass_scratch(const sfh_ctx *ctx, const sfh_models *m) {  // up to 
 int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
                           const double *d_data, double *d_composite, double *d_G,
                           double *d_negLogL, double eps, double gsign, void *scratch,
-                          cudaEvent_t *ev, const int *d_skip) {
+                          cudaEvent_t *ev, const int *d_skip, const void *occ_key) {
     const int64_t nbins = m->nbins, nt = m->nt;
     const int nch = (int)((nt + kBoxCols - 1) / kBoxCols);
     OnePassChoice ch{};
@@ -770,8 +1192,12 @@ int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
     const int bins = ch.bins, per_sm = ch.per_sm;
     const bool skew = ch.skew != 0;  // 16-bin tiles, one CTA per SM, two tiles resident
     const int mi = bins == 16 ? 0 : 1;
-    const int ntiles = (int)((nbins + bins - 1) / bins);
-    if (!m->d_blk[mi]) {  // the blocked copy, once per handle and tile width
+    int prc = SFH_OK;
+    SfhOccPlan *pl =
+        d_G ? occ_plan_get(ctx, m, occ_key ? occ_key : d_data, d_data, bins, mi, nch, &prc) : nullptr;
+    if (prc) return prc;
+    const int ntiles = (int)(((pl ? pl->nocc : nbins) + bins - 1) / bins);
+    if (!pl && !m->d_blk[mi]) {  // the blocked copy, once per handle and tile width
         const int64_t total = (int64_t)ntiles * nch * kBoxCols * bins;
         SFH_CK(ctx, cudaMalloc(&m->d_blk[mi], (size_t)total * sizeof(float)));
         k_onepass_block<<<(unsigned)((total + 255) / 256), 256, 0, ctx->stream>>>(
@@ -782,8 +1208,18 @@ int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
     const int cap = ctx->sm_count * per_sm < 384 ? ctx->sm_count * per_sm : 384;
     const int grid = ntiles < cap ? ntiles : cap;
     OnePassArgs a{};
-    a.blk = m->d_blk[mi];
-    a.nbins = nbins;
+    a.blk = pl ? pl->d_blk[mi] : m->d_blk[mi];
+    a.nbins = pl ? pl->nocc : nbins;
+    a.nbins_all = nbins;
+    if (pl) {
+        a.occ = pl->d_occ[mi];
+        a.empty = pl->d_empty;
+        a.nempty = pl->nempty;
+        a.colsum_e = pl->d_colsum_e;
+        a.viol = pl->d_viol;
+        a.flag = pl->d_flag;
+        a.mcol = m->d_f32;
+    }
     a.nt = nt;
     a.ntiles = ntiles;
     a.nch = nch;
@@ -804,7 +1240,7 @@ int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
     a.G = d_G;
     a.negLogL = d_negLogL;
     a.skip = d_skip;
-    a.rowb = m->d_rowb;
+    a.rowb = pl ? pl->d_rowb[mi] : m->d_rowb;
     a.budget = ctx->wait_budget;
     a.drop_copy = ctx->inject == SFH_INJECT_DROP_COPY ? 1 : 0;
     if (a.drop_copy) ctx->inject = SFH_INJECT_NONE;  // one shot

@@ -8,6 +8,7 @@
 #include <functional>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "../../include/sfhgpu.h"
 #include "sfh_dfloat.cuh"
@@ -36,7 +37,51 @@ struct sfh_ctx {
     // failure injection of the error-path tests (SFH_INJECT_*).
     long long wait_budget = 4000000000LL;
     int inject = 0;
+    // The device reads pageable host memory through the host's page tables (a coherent
+    // host link): the host-array fg! then hands the caller's own arrays to the kernels.
+    bool pageable_direct = false;
+    // Set while the library captures a graph that it destroys before returning (resources
+    // such a graph uses need no pin beyond the call).
+    bool internal_capture = false;
+    int host_access = SFH_HOST_ACCESS_AUTO;  // sfh_ctx_set_host_access
 };
+
+// Occupied-bin plan of the single-vector fg! (onepass.cu).  With G requested, fg! needs the
+// composite only where n_i > 0: an empty bin (n_i <= 0) has w_i = 1 - 0/max(c_i, eps) = 1
+// exactly and contributes -max(c_i, eps) to logL, so its terms are sums over the template
+// column: Σ_{i empty} M_ij w_i = E_j and Σ_{i empty} c_i = Σ_j r_j E_j (to eps per bin).
+// The plan keeps, for one observed Hess diagram, the occupied bins, a blocked copy of their
+// template rows and E_j; the kernel streams only those rows and checks every call that the
+// empty bins are still empty (a bin that is not is corrected inside the same launch, and
+// the next call builds a new plan).
+struct SfhOccPlan {
+    const void *key = nullptr;    // the data pointer the plan was built for
+    bool retired = false;         // superseded by a newer plan for the same key
+    bool captured = false;        // launched under stream capture: a graph may hold it, so
+                                  // it is never freed before the handle
+    bool sparse = false;          // false: the dense kernel serves this data
+    int streak = 0;               // plans retired in a row for this key (3: stay dense)
+    uint64_t last_use = 0;
+    int64_t nocc = 0, nempty = 0;
+    std::vector<int> occ_host;    // the occupied bins of the snapshot the plan was built from
+    // batched path (BF16X2 storage): a derived handle of the occupied rows, the occupied
+    // bins, the counts gathered for it, and a mapped pinned count of plan-empty bins found
+    // occupied by the last gather
+    sfh_models *sub = nullptr;
+    int *d_rows = nullptr;
+    double *d_nocc = nullptr;
+    volatile unsigned int *h_bviol = nullptr;
+    unsigned int *d_bviol = nullptr;
+    int *d_occ[2] = {nullptr, nullptr};   // per tile width: occupied bins, -1 padded to tiles
+    float *d_blk[2] = {nullptr, nullptr};  // per tile width: blocked copy of the occupied rows
+    float2 *d_rowb[2] = {nullptr, nullptr};  // per tile width: their row statistics
+    int *d_empty = nullptr;       // empty bins (ascending)
+    double *d_colsum_e = nullptr;  // E_j = Σ_{i empty} M_ij (FP64)
+    unsigned int *d_viol = nullptr;  // violations seen in the current launch (reset in-kernel)
+    volatile unsigned int *h_flag = nullptr;  // mapped pinned: set when a launch saw one
+    unsigned int *d_flag = nullptr;           // its device alias
+};
+constexpr int kSfhOccPlans = 4;
 
 struct sfh_models {
     int device = 0;
@@ -62,6 +107,10 @@ struct sfh_models {
     int64_t nbins_pad128 = 0;
     double *colsum = nullptr;  // Σ_i M_ij per template (FP64)
     int m_negative = 0;        // a template value is negative
+    // A handle derived from a parent's occupied rows (batched occupied-bin path): E_j, the
+    // parent's column sums over its empty bins (borrowed from the parent's plan), added to
+    // G; colsum above is the parent's full column sum.
+    const double *colsum_e = nullptr;
     // Single-vector launch plan chosen by sfh_models_autotune (0 = built-in heuristics):
     // pass-1 template splits, pass-2 row chunk, pass-2 waves.
     int tune_ks = 0, tune_R = 0, tune_w2 = 0;
@@ -77,6 +126,13 @@ struct sfh_models {
     int onepass_skew = 0;  // 1: skewed schedule (phase B of one tile beside phase A of the next)
     int onepass_lp = -1;   // log2 boxes per bulk copy (-1: 2 for 16-bin tiles, 1 for 32-bin)  // one-pass CTAs per SM: 1 (14 owner warps) or 2 (6 each); 0: 1
     float *d_blk[2] = {nullptr, nullptr};
+    // Occupied-bin plans (SFH_OCC_*): up to kSfhOccPlans observed diagrams, kept until the
+    // handle is freed.
+    int occ_mode = SFH_OCC_AUTO;
+    SfhOccPlan occ[kSfhOccPlans];
+    int nocc_plans = 0;
+    uint64_t occ_clock = 0;
+    double occ_build_ms = 0.0;  // host wall time of the last plan build
 };
 
 // Counter slots in sfh_ctx::d_counters (zeroed at context creation; every kernel that
@@ -269,6 +325,9 @@ struct FgArgs {
     double gsign;           // +1: gradient of -logL (fg!), -1: ∇loglikelihood!
     int mode;               // see FG_MODE_*
     const int *skip;        // device flag that turns the one-pass kernel into a no-op (or NULL)
+    // key of the occupied-bin plan (NULL: the data pointer; the host-array entry passes
+    // its handle slot, since its staging pointer is shared by every diagram)
+    const void *occ_key;
 };
 enum {
     FG_MODE_FG = 0,          // composite from coeffs, then logL/G as requested
@@ -282,7 +341,21 @@ size_t sfh_onepass_scratch(const sfh_ctx *ctx, const sfh_models *m);
 int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
                           const double *d_data, double *d_composite, double *d_G,
                           double *d_negLogL, double eps, double gsign, void *scratch,
-                          cudaEvent_t *ev, const int *d_skip = nullptr);
+                          cudaEvent_t *ev, const int *d_skip = nullptr,
+                          const void *occ_key = nullptr);
+void sfh_occ_plans_free(sfh_models *m);
+// Batched occupied-bin path: the handle and counts the batched kernels take for the
+// diagram at d_data (the parent's derived handle and the gathered counts, or m and d_data
+// themselves), and the plan whose gather check the caller reads after its sync (NULL when
+// dense).  Not during stream capture.
+int sfh_occ_batched(sfh_ctx *ctx, sfh_models *m, const double *d_data, bool want_l,
+                    const sfh_models **mb, const double **db, SfhOccPlan **plan);
+// Retires a plan whose gather found a plan-empty bin occupied.
+void sfh_occ_retire(SfhOccPlan *p);
+// A BF16X2 handle of rows d_rows[0 .. nrows) of parent's FP32 matrix, with the parent's
+// full column sums, its negative flag, and colsum_e as E_j.
+int sfh_models_derive_rows(sfh_ctx *ctx, const sfh_models *parent, const int *d_rows,
+                           int64_t nrows, const double *colsum_e, sfh_models **out);
 struct OnePassChoice {
     int bins, per_sm, skew, runs, lp;
 };
@@ -303,6 +376,7 @@ struct SfhExactPlan {
     int *nplanes = nullptr;   // [0] R planes, [1] negative-coefficient flag
     double *kn = nullptr;     // Σ_{n>0} (n - n log n)
     double *csum = nullptr;   // per vector Σ_j R_bj colsum_j
+    double *csum_e = nullptr; // per vector Σ_j R_bj E_j (derived occupied-bin handles)
     float2 *lpart = nullptr;
     CUtensorMap maps[2];
 };

@@ -18,17 +18,21 @@ SFH_OK, SFH_ERR_ARG, SFH_ERR_SHAPE, SFH_ERR_CUDA, SFH_ERR_TIMEOUT, SFH_ERR_NOMEM
     SFH_ERR_UNSUPPORTED, SFH_ERR_NUMERIC = range(8)
 SFH_F64, SFH_F32, SFH_BF16X2 = 0, 1, 2
 SFH_INJECT_NONE, SFH_INJECT_DROP_COPY, SFH_INJECT_ALLOC_FAIL = 0, 1, 2
+SFH_HOST_ACCESS_AUTO, SFH_HOST_ACCESS_STAGED, SFH_HOST_ACCESS_DIRECT = -1, 0, 1
+SFH_OCC_OFF, SFH_OCC_AUTO, SFH_OCC_ON = 0, 1, 2
 
 # Every symbol declared in include/sfhgpu.h.
 EXPORTED = [
     "sfh_abi_version", "sfh_status_string", "sfh_ctx_create", "sfh_ctx_destroy",
     "sfh_ctx_last_error", "sfh_ctx_synchronize", "sfh_ctx_stream", "sfh_ctx_launch_count",
-    "sfh_ctx_set_wait_budget", "sfh_ctx_inject_fault",
+    "sfh_ctx_set_wait_budget", "sfh_ctx_inject_fault", "sfh_ctx_set_host_access",
+    "sfh_ctx_host_access",
     "sfh_models_upload", "sfh_models_from_device", "sfh_models_free", "sfh_models_info",
     "sfh_models_combine",
     "sfh_composite", "sfh_loglikelihood", "sfh_grad_loglikelihood", "sfh_fg", "sfh_fg_dev",
     "sfh_fg_batched_dev", "sfh_fg_kernel_times", "sfh_models_autotune", "sfh_models_set_path", "sfh_models_set_onepass_tile",
     "sfh_models_set_onepass_ctas", "sfh_models_set_onepass_schedule", "sfh_models_onepass_variant", "sfh_models_set_onepass_run",
+    "sfh_models_set_occupied", "sfh_models_occupied_info",
     "sfh_models_path", "sfh_fg_dev_noalloc", "sfh_hmc_sample_dev",
     "sfh_logdensity_batched_dev", "sfh_fit_sfh_dev", "sfh_model_cmd", "sfh_model_cmd_dev", "sfh_fit_bfgs", "sfh_fit_bfgs_dev", "sfh_bin_cmd", "sfh_bin_cmd_dev", "sfh_bin_cmd_smooth", "sfh_bin_cmd_smooth_batch_dev",
     "sfh_partial_cmd_smooth_batch_dev", "sfh_partial_cmd_smooth_ragged_dev",
@@ -117,6 +121,8 @@ def load(path: str | None = None):
             "sfh_ctx_launch_count": ([_vp, C.POINTER(_i64)], C.c_int),
             "sfh_ctx_set_wait_budget": ([_vp, _i64], C.c_int),
             "sfh_ctx_inject_fault": ([_vp, C.c_int], C.c_int),
+            "sfh_ctx_set_host_access": ([_vp, C.c_int], C.c_int),
+            "sfh_ctx_host_access": ([_vp, C.POINTER(C.c_int)], C.c_int),
             "sfh_models_upload": ([_vp, _vp, C.c_int, _i64, _i64, C.c_int, C.POINTER(_vp)], C.c_int),
             "sfh_models_from_device": ([_vp, _vp, _i64, _i64, C.c_int, C.POINTER(_vp)], C.c_int),
             "sfh_models_free": ([_vp], C.c_int),
@@ -138,6 +144,9 @@ def load(path: str | None = None):
             "sfh_models_onepass_variant": ([_vp, _vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                             C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
             "sfh_models_set_onepass_run": ([_vp, _vp, C.c_int], C.c_int),
+            "sfh_models_set_occupied": ([_vp, _vp, C.c_int], C.c_int),
+            "sfh_models_occupied_info": ([_vp, _vp, _vp, C.POINTER(_i64), C.POINTER(C.c_int),
+                                          C.POINTER(_d)], C.c_int),
             "sfh_models_path": ([_vp, _vp, C.POINTER(C.c_int), C.POINTER(_d)], C.c_int),
             "sfh_fg_dev_noalloc": ([_vp, _vp, _i64, _i64, _vp, _vp, _vp, _vp, _vp, _d], C.c_int),
             "sfh_fg_kernel_times": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, C.c_int,

@@ -53,6 +53,18 @@ class Context:
         """One-shot failure injection for tests of the error paths (SFH_INJECT_*)."""
         check(load().sfh_ctx_inject_fault(self.handle, int(what)), self.handle)
 
+    @property
+    def host_access(self) -> int:
+        """How sfh_fg reaches host arrays: SFH_HOST_ACCESS_STAGED (mapped pinned staging)
+        or SFH_HOST_ACCESS_DIRECT (the kernels use the caller's arrays)."""
+        m = C.c_int()
+        check(load().sfh_ctx_host_access(self.handle, C.byref(m)), self.handle)
+        return int(m.value)
+
+    @host_access.setter
+    def host_access(self, mode: int):
+        check(load().sfh_ctx_set_host_access(self.handle, int(mode)), self.handle)
+
     def torch_stream(self):
         import torch
         return torch.cuda.ExternalStream(self.stream, device=torch.device("cuda", self.device))
@@ -170,6 +182,25 @@ class Models:
         (sfh_models_set_onepass_run)."""
         check(load().sfh_models_set_onepass_run(self.ctx.handle, self._h, int(boxes)),
               self.ctx.handle, "models_set_onepass_run")
+
+    OCC = {"off": 0, "auto": 1, "on": 2}
+
+    def set_occupied(self, mode):
+        """Occupied-bin restriction of fg! with G (sfh_models_set_occupied): "off" (the
+        dense kernel), "auto" (default: a plan per observed diagram when at most 60 % of
+        its bins hold counts) or "on"."""
+        check(load().sfh_models_set_occupied(self.ctx.handle, self._h, self.OCC[mode]),
+              self.ctx.handle, "models_set_occupied")
+
+    def occupied_info(self, data_ptr=None):
+        """(occupied bins or -1, restricted kernel in use, last plan build ms) of the plan
+        for the device data pointer (None: the host-array calls' slot)."""
+        n, sp, ms = C.c_int64(), C.c_int(), C.c_double()
+        key = data_ptr if data_ptr is not None else self._h
+        check(load().sfh_models_occupied_info(self.ctx.handle, self._h, key, C.byref(n),
+                                              C.byref(sp), C.byref(ms)),
+              self.ctx.handle, "models_occupied_info")
+        return int(n.value), bool(sp.value), float(ms.value)
 
     @property
     def onepass_variant(self):

@@ -108,3 +108,85 @@ def test_batched_requires_bf16_storage(sfh):
     torch.cuda.synchronize()
     assert L.sfh_fg_batched_dev(H.ctx.handle, H.handle, d_R.data_ptr(), 4, d_n.data_ptr(),
                                 None, None, 2.2e-16) == 1
+
+
+def _band(nbins, nt, B, seed, n_stars, occupied=0.25, spread=0.3):
+    """A populated band (a fraction `occupied` of the bins) and faint tails, so that most
+    bins of the Poisson draw stay empty, as in Hess diagrams."""
+    rng = np.random.default_rng(seed)
+    M = rng.random((nbins, nt))
+    M[rng.random(nbins) >= occupied] *= 1e-9
+    r0 = np.exp(rng.standard_normal(nt))
+    r0 *= n_stars / (M @ r0).sum()
+    data = rng.poisson(M @ r0).astype(float)
+    R = r0[None, :] * np.exp(spread * rng.standard_normal((B, nt)))
+    return np.asfortranarray(M.astype(np.float32)), R, data
+
+
+@pytest.mark.parametrize("nbins,nt,B,nst", [(20000, 300, 128, 1e5), (60000, 1200, 256, 1e6),
+                                            (7503, 65, 37, 1e4)])
+def test_batched_occupied_plan_matches_oracle_and_dense(sfh, O, nbins, nt, B, nst):
+    """The occupied-bin plan (a derived handle of the occupied rows; the empty bins through
+    FP64 column sums) against the oracle and the dense call."""
+    M32, R, data = _band(nbins, nt, B, seed=nbins + B, n_stars=nst)
+    H = sfh.Models(M32, storage="bf16x2")
+    out = {}
+    for mode in ("off", "on"):
+        H.set_occupied(mode)
+        out[mode] = _run(sfh, M32, R, data, H=H)
+        _check(O, M32, R, data, *out[mode], nchk=4)
+    (L0, G0), (L1, G1) = out["off"], out["on"]
+    assert np.max(np.abs(L1 - L0)) <= 1e-6 * max(1.0, data.sum() / 1e4)
+    Ms = M32.astype(np.float64)
+    for b in (0, B - 1):
+        w = 1.0 - data / np.maximum(Ms @ R[b], EPS)
+        scale = np.abs(Ms).T @ np.abs(w) + 1e-300
+        assert np.max(np.abs(G1[b] - G0[b]) / scale) <= 1e-4
+
+
+def test_batched_occupied_plan_negative_coefficient(sfh, O):
+    """A negative coefficient turns the split logL off (each c subtracted per bin); the
+    parent's empty bins then enter through Σ_j R_bj E_j."""
+    M32, R, data = _band(8000, 40, 16, seed=5, n_stars=1e4)
+    R[3, 7] = -0.5 * abs(R[3, 7])
+    H = sfh.Models(M32, storage="bf16x2")
+    H.set_occupied("on")
+    negL, G = _run(sfh, M32, R, data, H=H)
+    Ms = np.asfortranarray(M32.astype(np.float64))
+    ref_L, _ = O.fg_batched(R[[0, 3]], Ms, data, nthreads=4)
+    assert np.all(np.abs(negL[[0, 3]] - ref_L) <= 1e-6 * max(1.0, data.sum() / 1e4))
+
+
+def test_batched_occupied_plan_follows_new_counts(sfh, O):
+    """Counts written into plan-empty bins: the call finds them, evaluates densely, and the
+    next call builds a plan for the new diagram."""
+    import torch
+    L = sfh.load()
+    M32, R, data = _band(20000, 100, 64, seed=29, n_stars=1e5)
+    H = sfh.Models(M32, storage="bf16x2")
+    H.set_occupied("on")
+    dev = torch.device("cuda", 0)
+    d_R = torch.tensor(R, device=dev)
+    d_n = torch.tensor(data, device=dev)
+    d_L = torch.empty(R.shape[0], dtype=torch.float64, device=dev)
+    d_G = torch.empty(R.shape, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+
+    def call():
+        rc = L.sfh_fg_batched_dev(H.ctx.handle, H.handle, d_R.data_ptr(), R.shape[0],
+                                  d_n.data_ptr(), d_L.data_ptr(), d_G.data_ptr(), EPS)
+        sfh._lib.check(rc, H.ctx.handle, "sfh_fg_batched_dev")
+        H.ctx.synchronize()
+        return d_L.cpu().numpy(), d_G.cpu().numpy()
+
+    _check(O, M32, R, data, *call())
+    nocc0 = H.occupied_info(d_n.data_ptr())[0]
+    assert nocc0 == np.count_nonzero(data)
+    rng = np.random.default_rng(3)
+    new = data.copy()
+    new[rng.choice(np.flatnonzero(data == 0), 23, replace=False)] = 4.0
+    d_n.copy_(torch.tensor(new, device=dev))
+    torch.cuda.synchronize()
+    _check(O, M32, R, new, *call())
+    _check(O, M32, R, new, *call())
+    assert H.occupied_info(d_n.data_ptr())[0] == np.count_nonzero(new)

@@ -125,6 +125,34 @@ def test_fg_device_arrays_and_determinism(sfh, O):
     assert abs(outs[0][0] - v_ref) <= 1e-6 * data.sum() / 1e4
 
 
+@pytest.mark.parametrize("storage", ["f32", "f64"])
+def test_fg_host_access_modes_are_bit_identical(sfh, O, storage):
+    """sfh_fg through the mapped pinned staging and with the kernels on the caller's own
+    arrays (where the device reads pageable host memory) give the same bits."""
+    from sfhgpu._lib import SFH_HOST_ACCESS_DIRECT, SFH_HOST_ACCESS_STAGED
+    M, r, data = _problem(20000, 200, seed=11, n_stars=1e6)
+    H = sfh.Models(M, storage=storage)
+    ctx = H.ctx
+    res = {}
+    for mode in (SFH_HOST_ACCESS_STAGED, SFH_HOST_ACCESS_DIRECT):
+        try:
+            ctx.host_access = mode
+        except sfh.SFHError:
+            pytest.skip("the device does not read pageable host memory directly")
+        assert ctx.host_access == mode
+        comp, G = np.empty(M.shape[0]), np.empty(M.shape[1])
+        v = sfh.fg_(True, G, r, H, data, comp)
+        v2 = sfh.fg_(True, G.copy(), r, H, data, comp.copy())  # repeatable
+        res[mode] = (v, G, comp)
+        assert v2 == v
+    ctx.host_access = -1
+    (v0, G0, c0), (v1, G1, c1) = res[SFH_HOST_ACCESS_STAGED], res[SFH_HOST_ACCESS_DIRECT]
+    assert v0 == v1 and np.array_equal(G0, G1) and np.array_equal(c0, c1)
+    Mst = M.astype(np.float32).astype(np.float64) if storage == "f32" else M
+    v_ref, G_ref, _ = O.fg(r, Mst, data)
+    assert abs(v1 - v_ref) <= 1e-6 * data.sum() / 1e4
+
+
 def test_shape_errors_raise_argument_error(sfh):
     M = np.random.default_rng(0).random((10, 3))
     with pytest.raises(ValueError):

@@ -47,6 +47,7 @@ VARIANTS = [(16, 1, "phased", 0), (32, 1, "phased", 0), (16, 2, "phased", 0),
 def test_onepass_matches_oracle(sfh, O, nbins, nt, bins, ctas, schedule, run):
     M, r, data = _problem(nbins, nt, seed=7 * nbins + nt)
     H = sfh.Models(M, storage="f32")
+    H.set_occupied("off")  # the dense kernel (test_gpu_occupied.py covers the plan)
     H.set_path("onepass")
     H.set_onepass_tile(bins)
     H.set_onepass_ctas(ctas)
