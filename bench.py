@@ -49,6 +49,19 @@ def _peaks():
         return 6800.0, "fallback"
 
 
+def _profile_value(key: str):
+    """A figure `key: value` from the committed ncu summaries, else None."""
+    pdir = os.path.join(ROOT, "profiles")
+    for name in sorted(os.listdir(pdir)) if os.path.isdir(pdir) else []:
+        if not name.endswith(".md"):
+            continue
+        with open(os.path.join(pdir, name)) as f:
+            for line in f:
+                if line.startswith(key + ":"):
+                    return float(line.split(":", 1)[1].strip().split()[0])
+    return None
+
+
 def _profile_traffic(kernel: str):
     """dram bytes per launch of `kernel` from the committed ncu summaries, else None."""
     pdir = os.path.join(ROOT, "profiles")
@@ -168,10 +181,13 @@ def run_batched(ctx, d_T, nbins, nt, r, data, M64, steps, warmup, B=4096, check=
     # outputs for the accuracy check against the FP64 oracle, done in the CPU leg
     check_data = {"R": R[:check], "negL": negL[:check]}
     nst = float(data.sum())
-    # algorithmic FLOPs: the two products C = R M^T and G = W M, 2 nbins nt B each; the
+    # algorithmic FLOPs: the two products C = R M^T and G = W M, 2 nbins nt B each, over
+    # the bins the call needs (the occupied ones under an occupied-bin plan); the
     # digit-plane products of the exact composite and the hi/lo products of G are
     # implementation work and are not counted
-    flops = 4.0 * nbins * nt * B
+    nocc, sparse, _ = Hb.occupied_info(d_n.data_ptr())
+    nb_alg = nocc if sparse else nbins
+    flops = 4.0 * nb_alg * nt * B
     peak, kind = _bf16_peak()
     Hb.free()
     return {
@@ -181,7 +197,10 @@ def run_batched(ctx, d_T, nbins, nt, r, data, M64, steps, warmup, B=4096, check=
         "tensor_roofline": {"bound": "tensor", "achieved": flops / (ms / 1e3) / 1e12,
                             "peak": peak, "unit": "TFLOP/s",
                             "frac": flops / (ms / 1e3) / 1e12 / peak, "peak_source": kind,
-                            "flops": "algorithmic: 4 nbins nt B per call"},
+                            "flops": "algorithmic: 4 bins nt B per call over the "
+                                     f"{'occupied' if sparse else 'all'} bins ({nb_alg})",
+                            "dense_equivalent_tflops": 4.0 * nbins * nt * B / (ms / 1e3) / 1e12},
+        "occupied_bins": nocc if sparse else None,
         "_check": check_data,
     }
 
@@ -1002,6 +1021,11 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}"},
             "templates_per_s": templates_per_s, "template_build_ms": build_ms,
             "template_bin_updates_per_s": bin_updates / (build_ms / 1e3),
+            "template_build_roofline": {
+                "kernel": "k_stamps", "bound": "fp32 pipes (instruction issue)",
+                "frac": _profile_value("fma_pipe_fraction k_stamps"),
+                "issue_frac": _profile_value("issue_fraction k_stamps"),
+                "unit": "FMA pipe share of its peak (ncu, profiles/k_stamps_production.md)"},
             "template_bin_updates_per_build": bin_updates,
             "negLogL": neglogl, "precision": plain_check, "gpu_launches": launches,
             "roofline": roofline,

@@ -68,6 +68,12 @@ int sfh_ctx_launch_count(const sfh_ctx *ctx, int64_t *count_out);
    returns SFH_ERR_TIMEOUT; the context stays usable.  No counterpart in the reference
    (Julia's fg! has no device waits). */
 int sfh_ctx_set_wait_budget(sfh_ctx *ctx, int64_t cycles);
+/* Back-to-back single-vector fg! launches on this context overlap: each one-pass launch is a
+   programmatic dependent of the previous kernel in the stream, so its start-up and first
+   template copies run while the previous launch finishes (its inputs and outputs are
+   touched only after the previous kernel completes).  On by default; 0 turns it off.  No
+   counterpart in the reference. */
+int sfh_ctx_set_overlap(sfh_ctx *ctx, int on);
 /* How the host-array entry point sfh_fg reaches the caller's arrays:
      SFH_HOST_ACCESS_STAGED  through the context's mapped pinned staging area (one host
                              copy in, one out);

@@ -407,7 +407,8 @@ __global__ void k_m_digits(const float *__restrict__ M, const float2 *__restrict
 }
 
 // R digit planes: one block per vector b (B_pad blocks): S_b from max_j |R_bj|, then
-// plane p row b column j = d_p,bj for p < 8 (FP64, 49 bits: exact); padding rows and
+// plane p row b column j = d_p,bj for p < 8 (balanced base-64 digits of R_bj / S_b to
+// 2^-43, from integer arithmetic on the mantissa); padding rows and
 // columns zero.  The planes a launch needs: P = 6 while the ratio of the largest to the
 // smallest nonzero |R_bj| stays below 2^19, 7 below 2^25, else 8 (the maximum over the
 // batch, by atomicMax into *nplanes, which the caller zeroes first).
@@ -417,65 +418,89 @@ __global__ void k_r_digits(const double *__restrict__ R, int64_t B, int64_t nt, 
                            const double *__restrict__ colsum, double *__restrict__ csum,
                            int *__restrict__ negflag, const double *__restrict__ colsum_e,
                            double *__restrict__ csum_e) {
-    __shared__ double s_m[4][32];
+    // integer operations wherever the result is exact (max / min of |R| on the bit patterns,
+    // the digits from the mantissa): FP64 is the slow pipe; the two dot products stay FP64
+    __shared__ double s_d[2][32];
+    __shared__ unsigned long long s_m[2][32];
     const int64_t b = blockIdx.x;
-    double mx = 0.0, mn = INFINITY, dot = 0.0, dote = 0.0;
+    unsigned long long mxb = 0ull, mnb = ~0ull;  // |R| bit patterns: monotone in the value
+    double dot = 0.0, dote = 0.0;
     bool neg = false;
     if (b < B)
         for (int64_t j = threadIdx.x; j < nt; j += blockDim.x) {
-            const double v = R[b * nt + j], a = fabs(v);
-            mx = fmax(mx, a);
-            if (a > 0.0) mn = fmin(mn, a);
+            const double v = R[b * nt + j];
+            const unsigned long long ab = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+            mxb = ab > mxb ? ab : mxb;
+            if (ab) mnb = ab < mnb ? ab : mnb;
             dot = fma(v, colsum[j], dot);  // Σ_j R_bj Σ_i M_ij = Σ_i c_bi
             if (colsum_e) dote = fma(v, colsum_e[j], dote);  // Σ over a parent's empty bins
-            neg |= v < 0.0;
+            neg |= __double_as_longlong(v) < 0 && ab;
         }
     if (neg) atomicOr(negflag, 1);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        const unsigned long long a1 = __shfl_xor_sync(0xffffffffu, mxb, o);
+        const unsigned long long a2 = __shfl_xor_sync(0xffffffffu, mnb, o);
+        mxb = a1 > mxb ? a1 : mxb;
+        mnb = a2 < mnb ? a2 : mnb;
         dot += __shfl_xor_sync(0xffffffffu, dot, o);
         dote += __shfl_xor_sync(0xffffffffu, dote, o);
     }
     if ((threadIdx.x & 31) == 0) {
-        s_m[0][threadIdx.x >> 5] = mx;
-        s_m[1][threadIdx.x >> 5] = mn;
-        s_m[2][threadIdx.x >> 5] = dot;
-        s_m[3][threadIdx.x >> 5] = dote;
+        s_m[0][threadIdx.x >> 5] = mxb;
+        s_m[1][threadIdx.x >> 5] = mnb;
+        s_d[0][threadIdx.x >> 5] = dot;
+        s_d[1][threadIdx.x >> 5] = dote;
     }
     __syncthreads();
-    mx = 0.0;
-    mn = INFINITY;
+    mxb = 0ull;
+    mnb = ~0ull;
     dot = 0.0;
     dote = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-        mx = fmax(mx, s_m[0][w]);
-        mn = fmin(mn, s_m[1][w]);
-        dot += s_m[2][w];
-        dote += s_m[3][w];
+        mxb = s_m[0][w] > mxb ? s_m[0][w] : mxb;
+        mnb = s_m[1][w] < mnb ? s_m[1][w] : mnb;
+        dot += s_d[0][w];
+        dote += s_d[1][w];
     }
     if (threadIdx.x == 0) {
         csum[b] = dot;
         if (colsum_e) csum_e[b] = dote;
     }
+    const double mx = __longlong_as_double((long long)mxb);
     int e = 0;
-    if (mx > 0.0) frexp(mx, &e);
+    if (mx > 0.0) frexp(mx, &e);  // mx = f 2^e, f in [0.5, 1): |R_bj| < 2^e
     if (e < -120) e = -120;  // the scale stays a normal float
     if (e > 120) e = 120;
     if (threadIdx.x == 0) {
         rscale[b] = ldexpf(1.f, e);
         if (b < B && mx > 0.0) {
-            const double bits = log2(mx / mn);
+            const double bits = log2(mx / __longlong_as_double((long long)mnb));
             atomicMax(nplanes, bits <= 19.0 ? 6 : bits <= 25.0 ? 7 : 8);
         }
     }
+    // X = round(R_bj 2^(48 - e)) (|X| < 2^48: x = R 2^(6 - e) in units of 2^-42), then its
+    // balanced base-64 digits from the top: d_p = round(X_p / 2^(42 - 6p)), X_{p+1} = X_p -
+    // d_p 2^(42 - 6p); |d_0| <= 64, |d_p| <= 32, Σ_p d_p 64^-p = x to 2^-43
     for (int64_t j = threadIdx.x; j < nt_pad; j += blockDim.x) {
-        double x = (b < B && j < nt) ? ldexp(R[b * nt + j], -e) * 64.0 : 0.0;
+        long long X = 0;
+        if (b < B && j < nt) {
+            const unsigned long long vb = (unsigned long long)__double_as_longlong(R[b * nt + j]);
+            const int E = (int)((vb >> 52) & 0x7ffu);
+            if (E) {  // subnormals are far below 2^(e - 48) unless every entry is: zero
+                const long long m = (long long)((vb & 0xfffffffffffffull) | (1ull << 52));
+                // m 2^(E - 1075 + 48 - e) = m / 2^sh, sh >= 5 for |R| < 2^e (sh is held at 5
+                // for coefficients beyond the clamped scale, 2^120)
+                const int sh = max(5, 1075 - 48 + e - E);
+                X = sh < 63 ? (m + (1ll << (sh - 1))) >> sh : 0;
+                if (vb >> 63) X = -X;
+            }
+        }
         for (int p = 0; p < kPMax; ++p) {
-            const double d = rint(x);
+            const int sh = 42 - 6 * p;
+            const long long d = sh ? (X + (1ll << (sh - 1))) >> sh : X;
+            X -= d << sh;
             planes[((int64_t)p * B_pad + b) * nt_pad + j] = __float2bfloat16_rn((float)d);
-            x = (x - d) * 64.0;
         }
     }
 }
@@ -486,24 +511,41 @@ __global__ void k_logl_reduce_x(const float2 *__restrict__ part, int n_mt, int B
                                 const double *__restrict__ csum, const int *__restrict__ negflag,
                                 int m_negative, const double *__restrict__ kn,
                                 double *__restrict__ negLogL, const double *__restrict__ csum_e) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= B) return;
-    double acc = 0.0;
-    for (int t = 0; t < n_mt; ++t) {
+    // one warp per vector: lane l sums partials l, l + 32, ... in double-float (FP32 pipes),
+    // then a fixed shuffle tree
+    const int b = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (b >= B) return;  // whole warps leave together
+    sfh_df acc{0.f, 0.f};
+    for (int t = lane; t < n_mt; t += 32) {
         const float2 v = part[(int64_t)t * B_pad + b];
-        acc += (double)v.x + (double)v.y;
+        acc = df_add(acc, df_two_sum(v.x, v.y));
     }
-    if (!(m_negative || *negflag)) acc -= csum[b];  // else the epilogue subtracted each c
-    else if (csum_e) acc -= csum_e[b];  // and a derived handle's parent's empty bins remain
-    acc += *kn;
-    negLogL[b] = (acc != 0.0) ? -acc : INFINITY;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const sfh_df u{__shfl_down_sync(0xffffffffu, acc.h, o), __shfl_down_sync(0xffffffffu, acc.l, o)};
+        acc = df_add(acc, u);
+    }
+    if (lane) return;
+    double a = sfh_f2d(acc.h) + sfh_f2d(acc.l);
+    if (!(m_negative || *negflag)) a -= csum[b];  // else the epilogue subtracted each c
+    else if (csum_e) a -= csum_e[b];  // and a derived handle's parent's empty bins remain
+    a += *kn;
+    negLogL[b] = (a != 0.0) ? -a : INFINITY;
 }
 
-// Σ_{i: n_i > 0} (n_i - n_i log n_i) in FP64, one block, fixed order.
-__global__ void k_data_const(const double *__restrict__ n, int64_t nbins, double *__restrict__ kn) {
+// Σ_{i: n_i > 0} (n_i - n_i log n_i) in FP64: each block a contiguous chunk (the log runs on
+// the FP64 pipe, so the work is spread over the SMs), the last block sums the block partials
+// in block order (fixed order, reproducible) and re-arms the ticket.
+constexpr int kDcBlocks = 64;
+__global__ void k_data_const(const double *__restrict__ n, int64_t nbins, double *__restrict__ part,
+                             unsigned int *ticket, double *__restrict__ kn) {
     __shared__ double s[32];
+    __shared__ bool last;
+    const int64_t per = (nbins + gridDim.x - 1) / gridDim.x;
+    const int64_t i0 = (int64_t)blockIdx.x * per, i1 = min(nbins, i0 + per);
     double a = 0.0;
-    for (int64_t i = threadIdx.x; i < nbins; i += blockDim.x) {
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
         const double v = n[i];
         if (v > 0.0) a += v - v * log(v);
     }
@@ -514,7 +556,17 @@ __global__ void k_data_const(const double *__restrict__ n, int64_t nbins, double
     if (threadIdx.x == 0) {
         double t = 0.0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s[w];
+        part[blockIdx.x] = t;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        double t = 0.0;
+        for (int b = 0; b < (int)gridDim.x; ++b) t += ((volatile double *)part)[b];
         *kn = t;
+        *ticket = 0u;
     }
 }
 
@@ -596,7 +648,7 @@ size_t sfh_exact_scratch(const sfh_models *m, int64_t B, int64_t *B_pad_out) {
     const int64_t n_mt = m->nbins_pad128 / XBM;
     if (B_pad_out) *B_pad_out = B_pad;
     return sfh_align256((size_t)kPMax * B_pad * m->nt_pad * 2) + sfh_align256((size_t)B_pad * 4) +
-           256 + 2 * sfh_align256((size_t)B_pad * 8) + 256 +
+           256 + 2 * sfh_align256((size_t)B_pad * 8) + 256 + sfh_align256(kDcBlocks * 8) +
            sfh_align256((size_t)n_mt * 4 * B_pad * sizeof(float2));
 }
 
@@ -621,6 +673,8 @@ int sfh_exact_prepare(sfh_ctx *ctx, const sfh_models *m, int64_t B, void *scratc
     s += sfh_align256((size_t)B_pad * 8);
     xp->csum_e = (double *)s;
     s += sfh_align256((size_t)B_pad * 8);
+    xp->kpart = (double *)s;
+    s += sfh_align256(kDcBlocks * 8);
     xp->lpart = (float2 *)s;
     int rc;
     if ((rc = xmake_map(ctx, &xp->maps[0], m->digits, (int64_t)kQ * m->nbins_pad128, m->nt_pad, XBM)))
@@ -639,13 +693,14 @@ int sfh_exact_launch(sfh_ctx *ctx, const sfh_models *m, const SfhExactPlan &xp, 
         attr = true;
     }
     cudaStream_t st = ctx->stream;
-    SFH_CK(ctx, cudaMemsetAsync(xp.nplanes, 0, 2 * sizeof(int), st));
+    SFH_CK(ctx, cudaMemsetAsync(xp.nplanes, 0, 3 * sizeof(int), st));  // planes, flag, ticket
     k_r_digits<<<(unsigned)xp.B_pad, 256, 0, st>>>(d_R, xp.B, m->nt, xp.B_pad, m->nt_pad, xp.Rd,
                                                     xp.rscale, xp.nplanes, m->colsum, xp.csum,
                                                     xp.nplanes + 1, m->colsum_e, xp.csum_e);
     SFH_LAUNCHED(ctx);
     if (d_negLogL) {
-        k_data_const<<<1, 1024, 0, st>>>(d_data, m->nbins, xp.kn);
+        k_data_const<<<kDcBlocks, 256, 0, st>>>(d_data, m->nbins, xp.kpart,
+                                                (unsigned int *)(xp.nplanes + 2), xp.kn);
         SFH_LAUNCHED(ctx);
     }
     ExactParams P{};
@@ -675,7 +730,7 @@ int sfh_exact_launch(sfh_ctx *ctx, const sfh_models *m, const SfhExactPlan &xp, 
     k_tc_exact<<<grid, kXThreads, kXSmem, st>>>(xp.maps[0], xp.maps[1], P);
     SFH_LAUNCHED(ctx);
     if (d_negLogL) {
-        k_logl_reduce_x<<<(unsigned)((xp.B + 255) / 256), 256, 0, st>>>(
+        k_logl_reduce_x<<<(unsigned)((xp.B * 32 + 255) / 256), 256, 0, st>>>(
             xp.lpart, 4 * xp.n_mt, (int)xp.B, (int)xp.B_pad, xp.csum, xp.nplanes + 1, m->m_negative,
             xp.kn, d_negLogL, m->colsum_e ? xp.csum_e : nullptr);
         SFH_LAUNCHED(ctx);

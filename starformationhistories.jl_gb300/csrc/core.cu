@@ -106,6 +106,12 @@ extern "C" int sfh_ctx_set_wait_budget(sfh_ctx *ctx, int64_t cycles) {
     return SFH_OK;
 }
 
+extern "C" int sfh_ctx_set_overlap(sfh_ctx *ctx, int on) {
+    if (!ctx) return SFH_ERR_ARG;
+    ctx->pdl = on != 0;
+    return SFH_OK;
+}
+
 extern "C" int sfh_ctx_set_host_access(sfh_ctx *ctx, int mode) {
     if (!ctx || mode < SFH_HOST_ACCESS_AUTO || mode > SFH_HOST_ACCESS_DIRECT) return SFH_ERR_ARG;
     if (mode == SFH_HOST_ACCESS_DIRECT && !ctx->pageable_direct)

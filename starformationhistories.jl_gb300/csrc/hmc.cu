@@ -247,7 +247,7 @@ struct MzrDev {
     const int *age_tmpl;
     const int *sorted;       // ages by decreasing logAge (sortperm(unique_logAge; rev=true))
     const double *tage;      // LinearAMR: lookback time of each age in Gyr, 10^(logAge - 9)
-    double *aux;             // B x (4 nages): cum, mu, Asum, (spare)
+    double *aux;             // B x (4 nages): cum, mu, Asum, R_j / Asum_j
     double *A;               // B x nt Gaussian weights A_jk
 };
 
@@ -266,48 +266,56 @@ __device__ __forceinline__ double dmh_dz(double Z) {
 // calculate_coeffs (mzr.jl:50-79, amr.jl:50-72) per chain: one block per chain.
 __global__ void k_mzr_map(const double *__restrict__ theta, HmcConst c, MzrDev z,
                           double *__restrict__ r) {
+    // per-age work (exp R_j, μ_j, the normalisation) is done once per age, in parallel; per
+    // template one FP64 exp (the Gaussian weight) and one multiply: FP64 is the slow pipe
     const int b = blockIdx.x;
     const double *th = theta + (int64_t)b * c.D;
     double *cum = z.aux + (int64_t)b * 4 * z.nages, *mu = cum + z.nages, *Asum = mu + z.nages;
+    double *f = Asum + z.nages;  // R_j, then R_j / Σ_k A_jk
     double alpha = c.alpha, beta = c.beta, sigma = c.sigma;
     int q = z.nages;
     if (c.alpha_free) alpha = exp(th[q++]);
     if (c.beta_free) beta = (c.model == 3) ? exp(th[q++]) : th[q++];  // LogarithmicAMR: β > 0
     if (c.sigma_free) sigma = exp(th[q++]);
-    if (threadIdx.x == 0) {
-        if (c.model == 2) {
-            // LinearAMR: μ_j = β + α (T_max - t_j), amr.jl:205
-            for (int j = 0; j < z.nages; ++j) mu[j] = beta + alpha * (c.T_max - z.tage[j]);
-        } else if (c.model == 3) {
-            // LogarithmicAMR: μ_j = MH_from_Z(β + α (T_max - t_j)), amr.jl:278
-            for (int j = 0; j < z.nages; ++j) mu[j] = mh_from_z(beta + alpha * (c.T_max - z.tage[j]));
-        } else {
+    for (int j = threadIdx.x; j < z.nages; j += blockDim.x) f[j] = exp(th[j]);
+    __syncthreads();
+    if (c.model == 2 || c.model == 3) {
+        // LinearAMR: μ_j = β + α (T_max - t_j), amr.jl:205; LogarithmicAMR: μ_j =
+        // MH_from_Z(β + α (T_max - t_j)), amr.jl:278
+        for (int j = threadIdx.x; j < z.nages; j += blockDim.x) {
+            const double x = beta + alpha * (c.T_max - z.tage[j]);
+            mu[j] = c.model == 2 ? x : mh_from_z(x);
+        }
+    } else {
+        if (threadIdx.x == 0) {
             double acc = 0.0;  // cumsum in decreasing-age order
             for (int p = 0; p < z.nages; ++p) {
                 const int j = z.sorted[p];
-                acc += exp(th[j]);
+                acc += f[j];
                 cum[j] = acc;
             }
-            for (int j = 0; j < z.nages; ++j) mu[j] = beta + alpha * (log10(cum[j]) - c.logM0);
         }
+        __syncthreads();
+        for (int j = threadIdx.x; j < z.nages; j += blockDim.x)
+            mu[j] = beta + alpha * (log10(cum[j]) - c.logM0);
     }
     __syncthreads();
     double *A = z.A + (int64_t)b * z.nt;
+    const double hinv = 0.5 / (sigma * sigma);
     for (int k = threadIdx.x; k < z.nt; k += blockDim.x) {
-        const double dd = (z.MH[k] - mu[z.jidx[k]]) / sigma;
-        A[k] = exp(-dd * dd / 2.0);  // dispersion_models.jl:92
+        const double dd = z.MH[k] - mu[z.jidx[k]];
+        A[k] = exp(-dd * dd * hinv);  // dispersion_models.jl:92
     }
     __syncthreads();
     for (int j = threadIdx.x; j < z.nages; j += blockDim.x) {
-        double s = 0.0;
-        for (int q2 = z.age_off[j]; q2 < z.age_off[j + 1]; ++q2) s += A[z.age_tmpl[q2]];
-        Asum[j] = s;
+        double sA = 0.0;
+        for (int q2 = z.age_off[j]; q2 < z.age_off[j + 1]; ++q2) sA += A[z.age_tmpl[q2]];
+        Asum[j] = sA;
+        f[j] = f[j] / sA;
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < z.nt; k += blockDim.x) {
-        const int j = z.jidx[k];
-        r[(int64_t)b * z.nt + k] = A[k] * exp(th[j]) / Asum[j];
-    }
+    for (int k = threadIdx.x; k < z.nt; k += blockDim.x)
+        r[(int64_t)b * z.nt + k] = A[k] * f[z.jidx[k]];
 }
 
 // Chain rule of mzr.jl:131-209 (gradient of -logL w.r.t. R_j, α, β, σ) followed by the
@@ -330,8 +338,11 @@ __global__ void k_mzr_grad(const double *__restrict__ theta, const double *__res
     double *t1 = ksDr + na;          // Σ fullG (r/R + ...)
     double *ps = t1 + na;            // psum per age
     double *ss = ps + na;            // ssum per age
+    double *Rv = ss + na;            // R_j
+    double *lc = Rv + na;            // log10(cum_j) - logM0 (MZR)
     const double *th = theta + (int64_t)b * c.D;
     const double *cum = z.aux + (int64_t)b * 4 * na, *mu = cum + na, *Asum = mu + na;
+    const double *fR = Asum + na;    // R_j / Asum_j (k_mzr_map)
     const double *A = z.A + (int64_t)b * z.nt;
     const GT *G = Gfg + (int64_t)b * z.nt;
     double alpha = c.alpha, beta = c.beta, sigma = c.sigma;
@@ -341,36 +352,45 @@ __global__ void k_mzr_grad(const double *__restrict__ theta, const double *__res
         if (c.beta_free) beta = (c.model == 3) ? exp(th[q++]) : th[q++];
         if (c.sigma_free) sigma = exp(th[q++]);
     }
+    (void)r;
     const double ln10 = 2.302585092994046;
-    // per-age sums in fixed template order (deterministic)
+    const double is2 = 1.0 / (sigma * sigma), is3 = is2 / sigma;
+    // per-age sums in fixed template order (deterministic); the divisions are hoisted out of
+    // the template loops (FP64 division is slow on this part)
     for (int j = threadIdx.x; j < na; j += blockDim.x) {
         const double Rj = exp(th[j]);
-        const double dmu_dR = (c.model >= 2) ? 0.0 : alpha / cum[j] / ln10;
+        Rv[j] = Rj;
+        if (c.model < 2) lc[j] = log10(cum[j]) - c.logM0;
+        const double dmu_dR = (c.model >= 2) ? 0.0 : alpha / (cum[j] * ln10);
         double sR = 0.0, sM = 0.0, sS = 0.0;
+        const double mj = mu[j];
         for (int q2 = z.age_off[j]; q2 < z.age_off[j + 1]; ++q2) {
             const int k = z.age_tmpl[q2];
-            const double d = z.MH[k] - mu[j];
-            const double dAmu = A[k] * d / (sigma * sigma);
+            const double d = z.MH[k] - mj;
+            const double Ad = A[k] * d;
+            const double dAmu = Ad * is2;
             sR += dAmu * dmu_dR;
             sM += dAmu;
-            sS += A[k] * d * d / (sigma * sigma * sigma);
+            sS += Ad * d * is3;
         }
         ksR[j] = sR;
         ksMu[j] = sM;
         ksS[j] = sS;
         double dr = 0.0, tt = 0.0, psum = 0.0, ssum = 0.0;
-        const double Av = Asum[j];
+        const double iAv = 1.0 / Asum[j], f = fR[j];  // f = R_j / Asum_j
         for (int q2 = z.age_off[j]; q2 < z.age_off[j + 1]; ++q2) {
             const int k = z.age_tmpl[q2];
             const double fullG = -(double)G[k];  // ∂logL/∂r_k
-            const double d = z.MH[k] - mu[j];
-            const double dAmu = A[k] * d / (sigma * sigma);
+            const double d = z.MH[k] - mj;
+            const double Ad = A[k] * d;
+            const double dAmu = Ad * is2;
             const double dAR = dAmu * dmu_dR;
-            const double dAs = A[k] * d * d / (sigma * sigma * sigma);
-            dr += fullG * (Rj / Av * (dAR - A[k] * sR / Av));
-            tt += fullG * (r[(int64_t)b * z.nt + k] / Rj + (dAR - sR * A[k] / Av) * Rj / Av);
-            psum -= fullG * Rj / Av * (dAmu - A[k] / Av * sM);
-            ssum += fullG * Rj / Av * (dAs - A[k] / Av * sS);
+            const double dAs = Ad * d * is3;
+            const double a = A[k] * iAv;  // A_jk / Asum_j = r_k / R_j
+            dr += fullG * (f * (dAR - a * sR));
+            tt += fullG * (a + (dAR - sR * a) * f);
+            psum -= fullG * f * (dAmu - a * sM);
+            ssum += fullG * f * (dAs - a * sS);
         }
         ksDr[j] = dr;
         t1[j] = tt;
@@ -390,7 +410,7 @@ __global__ void k_mzr_grad(const double *__restrict__ theta, const double *__res
             // ∂μ/∂α and ∂μ/∂β: mzr.jl:279-281, amr.jl:207-209, amr.jl:280-288
             const double dt = c.T_max - z.tage[j];
             const double dz = (c.model == 3) ? dmh_dz(beta + alpha * dt) : 1.0;
-            Gv[na] += ps[j] * ((c.model >= 2) ? dz * dt : log10(cum[j]) - c.logM0);
+            Gv[na] += ps[j] * ((c.model >= 2) ? dz * dt : lc[j]);
             Gv[na + 1] += ps[j] * dz;
             Gv[na + 2] -= ss[j];
         }
@@ -400,7 +420,7 @@ __global__ void k_mzr_grad(const double *__restrict__ theta, const double *__res
         const double jf = c.jac ? 1.0 : 0.0;
         double jac = 0.0;
         for (int j = 0; j < na; ++j) {
-            const double Rj = exp(th[j]);
+            const double Rj = Rv[j];
             gb[j] = -Gv[j] * Rj + jf;
             jac += th[j];
         }
@@ -443,7 +463,10 @@ int launch_eval(sfh_ctx *ctx, const sfh_models *m, HmcRun &h, bool want_logd) {
         k_direct_grad<<<h.c.B, kT, 0, st>>>(h.s.theta, h.d_r, h.d_G, h.d_negL, h.c.D, h.s.g,
                                             h.s.logd, want_logd ? 1 : 0);
     } else {
-        const size_t sm = (size_t)(h.z.nages * 8 + 3) * sizeof(double);
+        const size_t sm = (size_t)(h.z.nages * 10 + 3) * sizeof(double);
+        if (sm > 48 * 1024)
+            SFH_CK(ctx, cudaFuncSetAttribute(k_mzr_grad<float>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         k_mzr_grad<float><<<h.c.B, 64, sm, st>>>(h.s.theta, h.d_r, h.d_G, h.d_negL, h.c, h.z,
                                                  h.s.g, h.s.logd, want_logd ? 1 : 0);
     }
@@ -792,7 +815,10 @@ extern "C" int sfh_fit_sfh_dev(sfh_ctx *ctx, sfh_models *m, const double *d_data
         logd = (double *)p[3];
     }
     double *r = h.d_r, *negL = h.d_negL;
-    const size_t sm = (size_t)(c.nages * 8 + 3) * sizeof(double);
+    const size_t sm = (size_t)(c.nages * 10 + 3) * sizeof(double);
+    if (sm > 48 * 1024)
+        SFH_CK(ctx, cudaFuncSetAttribute(k_mzr_grad<double>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     cudaStream_t st = ctx->stream;
     FgArgs a{};
     a.data = d_data;

@@ -81,7 +81,7 @@ struct OnePassArgs {
     int runs, lp;      // run-slots of the ring (slots = runs << lp), log2 boxes per run
     const double *r, *data;
     double *composite;
-    double *gpart;  // [gridDim.x][nt]
+    float2 *gpart;  // [gridDim.x][nt] double-float partials of G
     double *lpart;  // [gridDim.x]
     unsigned int *err;
     unsigned int *bar;  // grid barrier: arrivals, generation
@@ -94,6 +94,12 @@ struct OnePassArgs {
     const float2 *rowb;   // per bin: (sum, max) of |M_ij| over the templates (the anchors' bound)
     long long budget;     // SM cycles a device wait may take before the launch gives up
     int drop_copy;        // test-only: producer lane 0 skips its first bulk copy
+    // Launched as a programmatic dependent of the previous kernel in the stream: the
+    // consumers wait for it to complete (griddepcontrol.wait) before they touch inputs or
+    // outputs; the producers stream the blocked matrix, which no kernel writes, at once.
+    // Every CTA lets the next such launch start after the last grid barrier (all CTAs are
+    // resident then, so a dependent cannot take an SM a CTA of this launch still needs).
+    int pdl;
     // Occupied-bin plan (all NULL for the dense kernel).  Tile bin p is bin occ[p] (nbins
     // above counts the tile bins); empty[0 .. nempty) are the plan's empty bins; colsum_e
     // their per-template column sums E_j; viol counts empty bins found occupied in this
@@ -109,26 +115,30 @@ struct OnePassArgs {
 };
 
 // Grid barrier over the launch's resident CTAs (arrivals a.bar[0], generation a.bar[1]),
-// called by one thread per CTA; bounded like the pipeline's waits.
+// called by one thread per CTA after a CTA barrier; bounded like the pipeline's waits.  The
+// arrival is an acquire-release atomic, so the last CTA to arrive sees every CTA's writes;
+// it re-arms the count and publishes the next generation with a release, which the others
+// poll with acquire loads.
 __device__ __forceinline__ void op_grid_barrier(const OnePassArgs &a) {
-    __threadfence();
-    volatile unsigned int *gen = a.bar + 1;
-    const unsigned int g0 = *gen;
-    if (atomicAdd(a.bar, 1u) == gridDim.x - 1) {
-        *a.bar = 0u;  // re-armed for the next use
-        __threadfence();
-        atomicAdd(a.bar + 1, 1u);
-    } else {
-        const long long t0 = clock64();
-        while (*gen == g0) {
-            if (clock64() - t0 > a.budget) {
-                atomicExch(a.err, 3u);
-                break;
-            }
-            __nanosleep(64);
+    unsigned int *arr = a.bar, *gen = a.bar + 1;
+    unsigned int g0, old;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(g0) : "l"(gen) : "memory");
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(arr) : "memory");
+    if (old == gridDim.x - 1) {
+        asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(arr) : "memory");  // re-armed
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(gen) : "memory");
+        return;
+    }
+    const long long t0 = clock64();
+    for (;;) {
+        unsigned int g;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(g) : "l"(gen) : "memory");
+        if (g != g0) break;
+        if (clock64() - t0 > a.budget) {
+            atomicExch(a.err, 3u);
+            break;
         }
     }
-    __threadfence();
 }
 
 // Dynamic shared memory: ring | r (hi, lo) | s_part | s_w | s_cn | s_tab | full | empty |
@@ -202,8 +212,14 @@ __device__ __noinline__ void op_fold_occupied(const OnePassArgs &a, const sfh_df
             named_bar_sync(1, nthr);
             if (a.gpart) {
                 const double wm1 = (double)s_wfold - 1.0;
-                for (int64_t j = t; j < a.nt; j += nthr)
-                    a.gpart[(int64_t)blockIdx.x * a.nt + j] += (double)a.mcol[j * a.nbins_all + i] * wm1;
+                for (int64_t j = t; j < a.nt; j += nthr) {
+                    float2 &gp = a.gpart[(int64_t)blockIdx.x * a.nt + j];
+                    const double gv = sfh_f2d(gp.x) + sfh_f2d(gp.y) +
+                                      (double)a.mcol[j * a.nbins_all + i] * wm1;
+                    float gh, gl;
+                    sfh_split_double(gv, gh, gl);
+                    gp = make_float2(gh, gl);
+                }
             }
             named_bar_sync(1, nthr);
         }
@@ -258,6 +274,7 @@ k_fg_onepass(const OnePassArgs a) {
     __shared__ float s_rstat[2][32];  // per consumer warp: max and sum of |r|
     __shared__ unsigned int s_nviol;  // the CTA's empty bins found occupied
     if (warp < kWarps) {
+        if (a.pdl) asm volatile("griddepcontrol.wait;" ::: "memory");
         const int nk = nch * kBoxCols, ct = kWarps * 32;
         float rmx = 0.f, rsm = 0.f;
         for (int k0 = threadIdx.x; k0 < nk; k0 += 4 * ct) {
@@ -270,8 +287,9 @@ k_fg_onepass(const OnePassArgs a) {
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int k = k0 + q * ct;
-                const float h = __double2float_rn(v[q]);
-                if (k < nk) rr[k] = make_float2(h, __double2float_rn(v[q] - (double)h));
+                float h, l;
+                sfh_split_any(v[q], h, l);  // integer operations: FP64 is the slow pipe
+                if (k < nk) rr[k] = make_float2(h, l);
                 rmx = fmaxf(rmx, fabsf(h));
                 rsm += fabsf(h);
             }
@@ -298,7 +316,8 @@ k_fg_onepass(const OnePassArgs a) {
                 if (k < a.nempty) {
                     const int i = __ldg(a.empty + k);
                     a.composite[i] = 1.0;
-                    nv += a.data[i] != 0.0 ? 1u : 0u;  // w = 1 needs n = 0 exactly
+                    // w = 1 needs n = 0 exactly (+-0; an integer test of the bits)
+                    nv += (__double_as_longlong(a.data[i]) << 1) != 0ll ? 1u : 0u;
                 }
             }
             if (nv) atomicAdd(&s_nviol, nv);
@@ -655,21 +674,32 @@ k_fg_onepass(const OnePassArgs a) {
             if (u >= nunits) break;
 #pragma unroll
             for (int k = 0; k < GU; ++k) {
-                sfh_df v = df_two_sum(g2[j][k].x, g2[j][k].y);
+                // FP32 sums of the lanes' packed partials (2 LPR terms, 2^-24 relative each,
+                // below the FP32 accumulation over the tiles); double-float across the CTAs
+                float v = g2[j][k].x + g2[j][k].y;
 #pragma unroll
-                for (int o = 1; o < LPR; o <<= 1) {
-                    const sfh_df w{__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)};
-                    v = df_add(v, w);
-                }
+                for (int o = 1; o < LPR; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
                 const int64_t col = (int64_t)(u >> 1) * kBoxCols + 32 * (u & 1) + g + RPL * k;
                 if (quad == 0 && col < a.nt)
-                    a.gpart[(int64_t)blockIdx.x * a.nt + col] = sfh_f2d(v.h) + sfh_f2d(v.l);
+                    a.gpart[(int64_t)blockIdx.x * a.nt + col] = make_float2(v, 0.f);
             }
         }
     }
     if (a.want_logl && warp == kPoissonWarp) {
         const sfh_df tot = sfh_df_warp_sum(term);
-        if (lane == 0) a.lpart[blockIdx.x] = sfh_f2d(tot.h) + sfh_f2d(tot.l);
+        // the plan's empty bins: -Σ_j r_j E_j over this CTA's share of the columns (the
+        // share it reduces below)
+        double te = 0.0;
+        if (a.colsum_e) {
+            const int per = (int)((a.nt + gridDim.x - 1) / gridDim.x);
+            for (int c = lane; c < per; c += 32) {
+                const int64_t j = (int64_t)blockIdx.x * per + c;
+                if (j < a.nt) te = fma(a.r[j], a.colsum_e[j], te);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) te += __shfl_down_sync(0xffffffffu, te, o);
+        }
+        if (lane == 0) a.lpart[blockIdx.x] = (sfh_f2d(tot.h) + sfh_f2d(tot.l)) - te;
     }
 
     // ------------------------------------------------------------ grid reduction
@@ -692,6 +722,8 @@ k_fg_onepass(const OnePassArgs a) {
             *(volatile unsigned int *)a.flag = 1u;  // the host builds a new plan
         }
     }
+    // every CTA is past the last grid barrier: the next dependent launch may start
+    if (a.pdl) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const bool bad = *(volatile unsigned int *)a.err != 0u;
     if (a.G) {  // warp w sums columns j0 + w, j0 + w + kWarps, ...: lane l takes CTAs
                 // l, l + 32, ..., then a fixed shuffle tree
@@ -699,20 +731,29 @@ k_fg_onepass(const OnePassArgs a) {
         for (int cw = warp; cw < per; cw += kWarps) {
             const int64_t j = (int64_t)blockIdx.x * per + cw;
             if (j >= a.nt) break;
-            // up to 12 CTAs' partials per lane (grid <= 2 x SMs <= 384), loads issued together
-            double v[12];
+            // up to 12 CTAs' partials per lane (grid <= 2 x SMs <= 384), loads issued together;
+            // double-float sums on the FP32 pipes, one FP64 add per column at the end
+            float2 v[12];
 #pragma unroll
             for (int q = 0; q < 12; ++q) {
                 const int p = lane + 32 * q;
-                v[q] = p < (int)gridDim.x ? __ldcg(a.gpart + (int64_t)p * a.nt + j) : 0.0;
+                v[q] = p < (int)gridDim.x ? __ldcg(a.gpart + (int64_t)p * a.nt + j)
+                                          : make_float2(0.f, 0.f);
             }
-            double acc = 0.0;
+            sfh_df acc{0.f, 0.f};
 #pragma unroll
-            for (int q = 0; q < 12; ++q) acc += v[q];
+            for (int q = 0; q < 12; ++q) acc = df_add(acc, sfh_df{v[q].x, v[q].y});
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-            if (a.colsum_e) acc += a.colsum_e[j];  // the empty bins, w = 1
-            if (lane == 0) a.G[j] = bad ? NAN : a.gsign * acc;
+            for (int o = 16; o > 0; o >>= 1) {
+                const sfh_df u{__shfl_down_sync(0xffffffffu, acc.h, o),
+                               __shfl_down_sync(0xffffffffu, acc.l, o)};
+                acc = df_add(acc, u);
+            }
+            if (lane == 0) {
+                double gj = sfh_f2d(acc.h) + sfh_f2d(acc.l);
+                if (a.colsum_e) gj += a.colsum_e[j];  // the empty bins, w = 1
+                a.G[j] = bad ? NAN : a.gsign * gj;
+            }
         }
     }
     if (a.negLogL && blockIdx.x == 0 && warp == 0) {
@@ -725,8 +766,6 @@ k_fg_onepass(const OnePassArgs a) {
         double acc = 0.0;
 #pragma unroll
         for (int q = 0; q < 12; ++q) acc += v[q];
-        if (a.colsum_e)  // the empty bins: -Σ_j r_j E_j
-            for (int64_t j = lane; j < a.nt; j += 32) acc = fma(-a.r[j], a.colsum_e[j], acc);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
         // loglikelihood returns -typemax(T) = -Inf when the sum is exactly zero (fitting_base.jl:95)
@@ -849,7 +888,21 @@ int launch_onepass(sfh_ctx *ctx, const OnePassArgs &a0, int grid, cudaStream_t s
     // grid <= SMs x kMinBlocks and that many CTAs fit an SM (checked by the caller): the
     // CTAs are resident together, as the in-kernel grid reduction needs; its barrier wait
     // is bounded all the same
-    k_fg_onepass<BINS, OWN, SKEW><<<grid, GE::kThreads, smem, st>>>(a0);
+    if (a0.pdl) {
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3((unsigned)grid);
+        cfg.blockDim = dim3(GE::kThreads);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = st;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        SFH_CK(ctx, cudaLaunchKernelEx(&cfg, k_fg_onepass<BINS, OWN, SKEW>, a0));
+    } else {
+        k_fg_onepass<BINS, OWN, SKEW><<<grid, GE::kThreads, smem, st>>>(a0);
+    }
     SFH_LAUNCHED(ctx);
     return SFH_OK;
 }
@@ -1197,7 +1250,9 @@ int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
         d_G ? occ_plan_get(ctx, m, occ_key ? occ_key : d_data, d_data, bins, mi, nch, &prc) : nullptr;
     if (prc) return prc;
     const int ntiles = (int)(((pl ? pl->nocc : nbins) + bins - 1) / bins);
+    bool built = false;  // a kernel of this call writes the blocked copy
     if (!pl && !m->d_blk[mi]) {  // the blocked copy, once per handle and tile width
+        built = true;
         const int64_t total = (int64_t)ntiles * nch * kBoxCols * bins;
         SFH_CK(ctx, cudaMalloc(&m->d_blk[mi], (size_t)total * sizeof(float)));
         k_onepass_block<<<(unsigned)((total + 255) / 256), 256, 0, ctx->stream>>>(
@@ -1229,7 +1284,7 @@ int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
     a.r = d_coeffs;
     a.data = d_data;
     a.composite = d_composite;
-    a.gpart = d_G ? (double *)scratch : nullptr;
+    a.gpart = d_G ? (float2 *)scratch : nullptr;
     a.lpart = (double *)((char *)scratch + sfh_align256((size_t)2 * ctx->sm_count * (size_t)nt * 8));
     a.err = ctx->d_counters + SFH_CNT_ONEPASS_ERR;
     a.bar = ctx->d_counters + SFH_CNT_ONEPASS_BAR;
@@ -1243,6 +1298,12 @@ int sfh_launch_fg_onepass(sfh_ctx *ctx, sfh_models *m, const double *d_coeffs,
     a.rowb = pl ? pl->d_rowb[mi] : m->d_rowb;
     a.budget = ctx->wait_budget;
     a.drop_copy = ctx->inject == SFH_INJECT_DROP_COPY ? 1 : 0;
+    {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        const bool capturing = cudaStreamIsCapturing(ctx->stream, &cs) != cudaSuccess ||
+                               cs != cudaStreamCaptureStatusNone;
+        a.pdl = (ctx->pdl && !built && !d_skip && !capturing && !ev) ? 1 : 0;
+    }
     if (a.drop_copy) ctx->inject = SFH_INJECT_NONE;  // one shot
     if (!a.rowb) return sfh_set_error(ctx, SFH_ERR_ARG, "models handle has no row statistics");
     cudaStream_t st = ctx->stream;

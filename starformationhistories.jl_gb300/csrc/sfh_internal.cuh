@@ -43,6 +43,9 @@ struct sfh_ctx {
     // Set while the library captures a graph that it destroys before returning (resources
     // such a graph uses need no pin beyond the call).
     bool internal_capture = false;
+    // Single-vector one-pass launches overlap the previous one's tail (programmatic
+    // dependent launch); sfh_ctx_set_overlap turns it off.
+    bool pdl = true;
     int host_access = SFH_HOST_ACCESS_AUTO;  // sfh_ctx_set_host_access
 };
 
@@ -272,6 +275,22 @@ __device__ __forceinline__ void sfh_split_double(double x, float &h, float &l) {
         sfh_split_double_slow(x, h, l);
     }
 }
+// x = h + l for any double in the normal float range, with integer operations only: h
+// keeps the top 24 significant bits (truncated), l is the remaining 29 bits rounded to a
+// float (|h + l - x| <= 2^-47 |x|, |l| < 2^-23 |h|); the FP64 conversions otherwise.
+__device__ __forceinline__ void sfh_split_any(double x, float &h, float &l) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned int e = (unsigned int)(b >> 52) & 0x7ffu;
+    if (e >= 960u && e <= 1150u) {  // 2^-63 <= |x| < 2^128
+        const unsigned int sg = (unsigned int)(b >> 32) & 0x80000000u;
+        h = __uint_as_float(sg | ((e - 896u) << 23) | (unsigned int)((b >> 29) & 0x7fffffull));
+        const float lm = __fmul_rn(__uint2float_rn((unsigned int)(b & 0x1fffffffull)),
+                                   __uint_as_float((e - 948u) << 23));  // rem 2^(e - 1075)
+        l = __uint_as_float(__float_as_uint(lm) | sg);
+    } else {
+        sfh_split_double(x, h, l);
+    }
+}
 __device__ __forceinline__ double sfh_f2d(float f) {
     const unsigned int u = __float_as_uint(f);
     const unsigned int e = (u >> 23) & 0xffu;
@@ -373,10 +392,11 @@ struct SfhExactPlan {
     int n_mt = 0, n_vt = 0;
     __nv_bfloat16 *Rd = nullptr;
     float *rscale = nullptr;
-    int *nplanes = nullptr;   // [0] R planes, [1] negative-coefficient flag
+    int *nplanes = nullptr;   // [0] R planes, [1] negative-coefficient flag, [2] ticket
     double *kn = nullptr;     // Σ_{n>0} (n - n log n)
     double *csum = nullptr;   // per vector Σ_j R_bj colsum_j
     double *csum_e = nullptr; // per vector Σ_j R_bj E_j (derived occupied-bin handles)
+    double *kpart = nullptr;  // block partials of Σ (n - n log n)
     float2 *lpart = nullptr;
     CUtensorMap maps[2];
 };

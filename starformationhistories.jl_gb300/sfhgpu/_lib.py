@@ -25,7 +25,7 @@ SFH_OCC_OFF, SFH_OCC_AUTO, SFH_OCC_ON = 0, 1, 2
 EXPORTED = [
     "sfh_abi_version", "sfh_status_string", "sfh_ctx_create", "sfh_ctx_destroy",
     "sfh_ctx_last_error", "sfh_ctx_synchronize", "sfh_ctx_stream", "sfh_ctx_launch_count",
-    "sfh_ctx_set_wait_budget", "sfh_ctx_inject_fault", "sfh_ctx_set_host_access",
+    "sfh_ctx_set_wait_budget", "sfh_ctx_inject_fault", "sfh_ctx_set_host_access", "sfh_ctx_set_overlap",
     "sfh_ctx_host_access",
     "sfh_models_upload", "sfh_models_from_device", "sfh_models_free", "sfh_models_info",
     "sfh_models_combine",
@@ -122,6 +122,7 @@ def load(path: str | None = None):
             "sfh_ctx_set_wait_budget": ([_vp, _i64], C.c_int),
             "sfh_ctx_inject_fault": ([_vp, C.c_int], C.c_int),
             "sfh_ctx_set_host_access": ([_vp, C.c_int], C.c_int),
+            "sfh_ctx_set_overlap": ([_vp, C.c_int], C.c_int),
             "sfh_ctx_host_access": ([_vp, C.POINTER(C.c_int)], C.c_int),
             "sfh_models_upload": ([_vp, _vp, C.c_int, _i64, _i64, C.c_int, C.POINTER(_vp)], C.c_int),
             "sfh_models_from_device": ([_vp, _vp, _i64, _i64, C.c_int, C.POINTER(_vp)], C.c_int),

@@ -53,6 +53,10 @@ class Context:
         """One-shot failure injection for tests of the error paths (SFH_INJECT_*)."""
         check(load().sfh_ctx_inject_fault(self.handle, int(what)), self.handle)
 
+    def set_overlap(self, on: bool = True):
+        """Overlap back-to-back single-vector fg! launches (sfh_ctx_set_overlap)."""
+        check(load().sfh_ctx_set_overlap(self.handle, 1 if on else 0), self.handle)
+
     @property
     def host_access(self) -> int:
         """How sfh_fg reaches host arrays: SFH_HOST_ACCESS_STAGED (mapped pinned staging)
