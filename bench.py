@@ -259,6 +259,78 @@ def run_hmc(ctx, d_T, w, nchains=1024, nwarmup=500, ntraj=1500, nleap=10, seed=2
     }
 
 
+def run_hmc_matched(ctx, d_T, w, nchains=1024, nwarmup=100, ndraw=20, nref=200,
+                    seed=20261207):
+    """The batched No-U-Turn sampler against the plain single-chain path at matched
+    posterior-mean error, measured on the config-5 model (PowerLawMZR + GaussianDispersion,
+    1,200 templates): a reference posterior mean from a long batched run; then the batched
+    run (nchains x ndraw draws after nwarmup) and one chain on the single-vector fg! with
+    the same total number of draws.  Error: RMS over all variables of (mean - reference) /
+    posterior sd.  Since the error of a mean falls as 1/sqrt(draws), the single chain's
+    time at the batched run's error is its time x (e_single / e_batched)^2."""
+    import numpy as np
+    import torch
+
+    import sfhgpu
+    from sfhgpu.sampling import GaussianDispersion, PowerLawMZR, calculate_coeffs
+    la, mh = w.template_params
+    Hb = sfhgpu.Models.from_device(d_T.data_ptr(), w.nbins, w.ntempl, storage="bf16x2", ctx=ctx)
+    rng = np.random.default_rng(seed)
+    mzr, disp = PowerLawMZR(0.5, -1.0, 6.0), GaussianDispersion(0.2)
+    R = np.exp(0.5 * rng.standard_normal(w.logAges.size))
+    M = d_T.double()
+    c = calculate_coeffs(mzr, disp, R, la, mh)
+    R = R * (1e6 / float((M.T @ torch.as_tensor(c, device=M.device)).sum()))
+    c = calculate_coeffs(mzr, disp, R, la, mh)
+    data = rng.poisson((M.T @ torch.as_tensor(c, device=M.device)).cpu().numpy()).astype(float)
+    del M
+
+    # every run starts from the MAP fit with its inverse-Hessian diagonal as the metric, as
+    # the reference starts its sampler (generic_fitting.jl:458-470)
+    Hf = sfhgpu.Models.from_device(d_T.data_ptr(), w.nbins, w.ntempl, storage="f32", ctx=ctx)
+    t0 = time.perf_counter()
+    fit = sfhgpu.fit_sfh(PowerLawMZR(0.45, -0.9, 6.0), GaussianDispersion(0.25), Hf, data, la, mh,
+                         x0=R * 1.1, g_abstol=1e-3)
+    t_fit = time.perf_counter() - t0
+    Hf.free()
+
+    def run(nch, nsteps, sd):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = sfhgpu.sample_sfh(Hb, data, la, mh, nsteps=nsteps, nchains=nch, nwarmup=nwarmup,
+                                step0=0.05, seed=sd, sampler="nuts", fit=fit)
+        torch.cuda.synchronize()
+        return out, time.perf_counter() - t0
+
+    ref, t_ref = run(nchains, nref, seed + 1)
+    mref = ref["mean"].mean(0)
+    sdref = np.sqrt(ref["var"].mean(0) + ref["mean"].var(0))
+    bat, t_bat = run(nchains, ndraw, seed + 2)
+    one, t_one = run(1, nchains * ndraw, seed + 3)
+    Hb.free()
+    err = lambda mu: float(np.sqrt(np.mean(((mu - mref) / sdref) ** 2)))
+    e_b, e_1 = err(bat["mean"].mean(0)), err(one["mean"][0])
+    t_match = t_one * (e_1 / e_b) ** 2
+    return {
+        "workload": f"NUTS (max depth 10), PowerLawMZR + GaussianDispersion over {w.ntempl} "
+                    f"templates x {w.nbins} bins, as the reference's sample_sfh runs it: from "
+                    "the device fit_sfh MLE point, the MAP inverse Hessian as a dense metric, "
+                    f"step 0.05 then {nwarmup} warmup trees of step adaptation per chain",
+        "map_fit_seconds": t_fit,
+        "reference": {"chains": nchains, "draws_per_chain": nref, "seconds": t_ref},
+        "batched": {"chains": nchains, "draws_per_chain": ndraw, "seconds": t_bat,
+                    "error": e_b, "mean_depth": float(bat["depth"].mean()),
+                    "accept": float(bat["accept"].mean()),
+                    "divergent": int(bat["divergent"].sum())},
+        "single_chain_plain": {"draws": nchains * ndraw, "seconds": t_one, "error": e_1,
+                               "mean_depth": float(one["depth"].mean()),
+                               "accept": float(one["accept"].mean())},
+        "single_chain_seconds_at_batched_error": t_match,
+        "speedup_at_matched_error": t_match / t_bat,
+        "error": "RMS over the 43 variables of (posterior mean - reference) / posterior sd",
+    }
+
+
 def run_ragged(ctx, steps=50, warmup=5, check=2):
     """256 independent galaxies with uneven Hess grids (50-300 bins per axis) and
     isochrone lengths (100-2,000 points): one ragged template build, then fg! over all
@@ -347,7 +419,7 @@ def run_ragged(ctx, steps=50, warmup=5, check=2):
     }
 
 
-def run_emulator(ctx, w, n_train=100_000, n_val=4096, steps=4000, cells=(8, 2, 16), nreq=1200):
+def run_emulator(ctx, w, n_train=100_000, n_val=4096, steps=20000, cells=(8, 2, 16), nreq=1200):
     """Learned template emulator on the production grid: per-cell PCA bases (64
     components of sqrt templates) and per-cell MLPs 3-256-256-64 trained on templates the
     GPU partial_cmd_smooth generates at random (log age, [M/H], distance modulus); scored
@@ -791,6 +863,7 @@ def run_ours(args):
     eps = float(np.finfo(np.float64).eps)
 
     # launch plan picked by the library's autotuner on this matrix and these inputs
+    H.set_occupied(args.occupied)
     tuned = ({"plan": [None, None, None], "ms": None} if args.no_autotune
              else H.autotune(r, data, iters=10))
     if args.fg_path != "auto":
@@ -847,7 +920,7 @@ def run_ours(args):
 
     # ---- the same evaluations on the dense kernel (every bin's template row streamed)
     occupied = None
-    if occ_sparse:
+    if occ_sparse and args.occupied == "auto":
         H.set_occupied("off")
         for _ in range(args.warmup):
             step()
@@ -968,11 +1041,8 @@ def run_ours(args):
         hmc = run_hmc(ctx, d_T, w, nchains=args.hmc_chains, nwarmup=args.hmc_warmup,
                       ntraj=args.hmc_traj)
         hmc["speedup_vs_plain_evals"] = hmc["chain_gradient_evals_per_s"] / value
-        # the plain single-chain GPU path needs the same number of gradient evaluations to
-        # reach the same posterior-mean error (equal effective samples per draw assumed)
-        nev = args.hmc_chains * (args.hmc_warmup + args.hmc_traj) * 10
-        hmc["plain_single_chain_seconds_at_matched_error"] = nev / value
-        hmc["speedup_vs_plain_single_chain_at_matched_error"] = nev / value / hmc["seconds"]
+        if args.hmc_traj >= 100:  # not in short profiling runs
+            hmc["nuts_matched_error"] = run_hmc_matched(ctx, d_T, w, nchains=args.hmc_chains)
         em = getattr(run_emulator, "last", None)
         if em is not None:
             # the same fit on emulated templates (exact where the trust map says so)
@@ -1063,6 +1133,9 @@ def main():
                          "(e.g. 32,1,phased,2)")
     ap.add_argument("--ntempl", type=int, default=NT,
                     help="templates (multiple of 30); fewer than 1200 only for profiling")
+    ap.add_argument("--occupied", choices=("auto", "off", "on"), default="auto",
+                    help="occupied-bin plan of the single-vector leg (off: the dense kernel "
+                         "throughout, for profiling it)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="skip the single-vector autotuner (profiling runs: fewer launches "
                          "before the timed ones; pin the variant with --onepass-variant)")

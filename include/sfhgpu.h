@@ -375,6 +375,28 @@ int sfh_hmc_sample_dev(sfh_ctx *ctx, const sfh_models *models, const double *d_d
                        const sfh_hmc_config *cfg, const double *d_theta0, double *d_mean,
                        double *d_var, double *d_accept, double *d_step, float *d_draws);
 
+/* The No-U-Turn sampler of DynamicHMC (the sampler of hmc_sample.jl:105-141 and
+   sample_sfh, generic_fitting.jl:458-527) for all chains at once: multinomial sampling
+   over each trajectory, trees doubled in a random direction until the generalized
+   no-U-turn criterion holds for the tree or any subtree, an energy error above 1000
+   (divergence) or max_depth doublings (1..12; DynamicHMC's default is 10).  Every chain
+   runs its own tree and advances one leapfrog step per batched evaluation, so no
+   evaluation waits for other chains' trees.  Warmup (nwarmup trees per chain): per-chain
+   dual averaging of the step on each tree's mean acceptance statistic, and a per-chain
+   diagonal metric from the chain's own draws over the middle 70 % of warmup (starting
+   from cfg->d_minv0 or ones).  d_minv_dense (D x D, device, or NULL): a dense metric M⁻¹
+   for all chains instead, kept through warmup; the reference's sample_sfh passes the
+   MAP inverse Hessian and a fixed step with no warmup (generic_fitting.jl:458-490:
+   GaussianKineticEnergy(MAP.invH), ϵ = 0.05), which nwarmup = 0 and step0 = 0.05
+   reproduce (D <= 256).  cfg as sfh_hmc_sample_dev (nleap is ignored); outputs as there,
+   plus d_depth (nchains) the mean tree depth and d_ndiv (nchains) the divergent
+   trajectories after warmup; any output may be NULL.  Synchronous. */
+int sfh_nuts_sample_dev(sfh_ctx *ctx, const sfh_models *models, const double *d_data,
+                        const sfh_hmc_config *cfg, int max_depth,
+                        const double *d_minv_dense, const double *d_theta0, double *d_mean,
+                        double *d_var, double *d_accept, double *d_step, double *d_depth,
+                        int64_t *d_ndiv, float *d_draws);
+
 /* Log density and its gradient for B parameter vectors of the same model as
    sfh_hmc_sample_dev (logdensity_and_gradient of hmc_sample.jl:24-37 and
    generic_fitting.jl:90-199 with Jacobian terms), batched on the tensor cores:

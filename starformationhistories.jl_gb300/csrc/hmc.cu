@@ -222,8 +222,9 @@ __global__ void k_direct_map(const double *__restrict__ theta, int64_t n, double
 }
 
 // log p = -negLogL + Σ θ;  ∇ = -G ⊙ r + 1   (hmc_sample.jl:34-36)
+template <typename GT>  // float: the batched gradient; double: the single-vector one
 __global__ void k_direct_grad(const double *__restrict__ theta, const double *__restrict__ r,
-                              const float *__restrict__ G, const double *__restrict__ negL, int D,
+                              const GT *__restrict__ G, const double *__restrict__ negL, int D,
                               double *__restrict__ g, double *__restrict__ logd, int want_logd) {
     __shared__ double s_red[kT / 32];
     const int b = blockIdx.x;
@@ -248,6 +249,8 @@ struct MzrDev {
     const int *sorted;       // ages by decreasing logAge (sortperm(unique_logAge; rev=true))
     const double *tage;      // LinearAMR: lookback time of each age in Gyr, 10^(logAge - 9)
     double *aux;             // B x (4 nages): cum, mu, Asum, R_j / Asum_j
+    const int *uni;          // per age: its templates (CSR order = ascending [M/H]) are
+                             // evenly spaced in [M/H], so A follows a product recurrence
     double *A;               // B x nt Gaussian weights A_jk
 };
 
@@ -303,8 +306,37 @@ __global__ void k_mzr_map(const double *__restrict__ theta, HmcConst c, MzrDev z
     double *A = z.A + (int64_t)b * z.nt;
     const double hinv = 0.5 / (sigma * sigma);
     for (int k = threadIdx.x; k < z.nt; k += blockDim.x) {
+        if (z.uni[z.jidx[k]]) continue;
         const double dd = z.MH[k] - mu[z.jidx[k]];
         A[k] = exp(-dd * dd * hinv);  // dispersion_models.jl:92
+    }
+    // evenly spaced [M/H] (step Δ): A_{k±1} / A_k = exp(-h (±2 x_k Δ + Δ²)), x_k = MH_k - μ,
+    // and successive ratios differ by the factor exp(-2 h Δ²): three exps and two products
+    // per template instead of one exp each (FP64 is the slow pipe), from the template
+    // nearest μ outwards, where every ratio is at most 1
+    for (int j = threadIdx.x; j < z.nages; j += blockDim.x) {
+        if (!z.uni[j]) continue;
+        const int a0 = z.age_off[j], n = z.age_off[j + 1] - a0;
+        const double m = mu[j];
+        const double mh0 = z.MH[z.age_tmpl[a0]];
+        const double dl = (z.MH[z.age_tmpl[a0 + n - 1]] - mh0) / (double)(n - 1);
+        int ks = (int)rint((m - mh0) / dl);
+        ks = ks < 0 ? 0 : (ks > n - 1 ? n - 1 : ks);
+        const double x = z.MH[z.age_tmpl[a0 + ks]] - m;
+        const double Ak = exp(-x * x * hinv), c2 = exp(-2.0 * dl * dl * hinv);
+        A[z.age_tmpl[a0 + ks]] = Ak;
+        double q = exp(-(2.0 * x * dl + dl * dl) * hinv), Au = Ak;
+        for (int k = ks + 1; k < n; ++k) {
+            Au *= q;
+            q *= c2;
+            A[z.age_tmpl[a0 + k]] = Au;
+        }
+        double qd = exp(-(dl * dl - 2.0 * x * dl) * hinv), Ad = Ak;
+        for (int k = ks - 1; k >= 0; --k) {
+            Ad *= qd;
+            qd *= c2;
+            A[z.age_tmpl[a0 + k]] = Ad;
+        }
     }
     __syncthreads();
     for (int j = threadIdx.x; j < z.nages; j += blockDim.x) {
@@ -354,21 +386,25 @@ __global__ void k_mzr_grad(const double *__restrict__ theta, const double *__res
     }
     (void)r;
     const double ln10 = 2.302585092994046;
-    const double is2 = 1.0 / (sigma * sigma), is3 = is2 / sigma;
+    // The per-template products run in GT: FP32 for the batched sampler, whose gradient
+    // only steers the leapfrog (the log density that accepts or weights a state is
+    // computed separately, in full precision), FP64 for the single-vector fit.
+    using CT = GT;
+    const CT is2 = (CT)(1.0 / (sigma * sigma)), is3 = (CT)(1.0 / (sigma * sigma * sigma));
     // per-age sums in fixed template order (deterministic); the divisions are hoisted out of
     // the template loops (FP64 division is slow on this part)
     for (int j = threadIdx.x; j < na; j += blockDim.x) {
         const double Rj = exp(th[j]);
         Rv[j] = Rj;
         if (c.model < 2) lc[j] = log10(cum[j]) - c.logM0;
-        const double dmu_dR = (c.model >= 2) ? 0.0 : alpha / (cum[j] * ln10);
-        double sR = 0.0, sM = 0.0, sS = 0.0;
-        const double mj = mu[j];
+        const CT dmu_dR = (CT)((c.model >= 2) ? 0.0 : alpha / (cum[j] * ln10));
+        CT sR = 0, sM = 0, sS = 0;
+        const CT mj = (CT)mu[j];
         for (int q2 = z.age_off[j]; q2 < z.age_off[j + 1]; ++q2) {
             const int k = z.age_tmpl[q2];
-            const double d = z.MH[k] - mj;
-            const double Ad = A[k] * d;
-            const double dAmu = Ad * is2;
+            const CT d = (CT)z.MH[k] - mj;
+            const CT Ad = (CT)A[k] * d;
+            const CT dAmu = Ad * is2;
             sR += dAmu * dmu_dR;
             sM += dAmu;
             sS += Ad * d * is3;
@@ -376,17 +412,18 @@ __global__ void k_mzr_grad(const double *__restrict__ theta, const double *__res
         ksR[j] = sR;
         ksMu[j] = sM;
         ksS[j] = sS;
-        double dr = 0.0, tt = 0.0, psum = 0.0, ssum = 0.0;
-        const double iAv = 1.0 / Asum[j], f = fR[j];  // f = R_j / Asum_j
+        CT dr = 0, tt = 0, psum = 0, ssum = 0;
+        const CT iAv = (CT)(1.0 / Asum[j]), f = (CT)fR[j];  // f = R_j / Asum_j
         for (int q2 = z.age_off[j]; q2 < z.age_off[j + 1]; ++q2) {
             const int k = z.age_tmpl[q2];
-            const double fullG = -(double)G[k];  // ∂logL/∂r_k
-            const double d = z.MH[k] - mj;
-            const double Ad = A[k] * d;
-            const double dAmu = Ad * is2;
-            const double dAR = dAmu * dmu_dR;
-            const double dAs = Ad * d * is3;
-            const double a = A[k] * iAv;  // A_jk / Asum_j = r_k / R_j
+            const CT fullG = -(CT)G[k];  // ∂logL/∂r_k
+            const CT d = (CT)z.MH[k] - mj;
+            const CT Ak = (CT)A[k];
+            const CT Ad = Ak * d;
+            const CT dAmu = Ad * is2;
+            const CT dAR = dAmu * dmu_dR;
+            const CT dAs = Ad * d * is3;
+            const CT a = Ak * iAv;  // A_jk / Asum_j = r_k / R_j
             dr += fullG * (f * (dAR - a * sR));
             tt += fullG * (a + (dAR - sR * a) * f);
             psum -= fullG * f * (dAmu - a * sM);
@@ -445,7 +482,18 @@ struct HmcRun {
     double *d_r = nullptr, *d_negL = nullptr;
     float *d_G = nullptr;
     double eps_abs;
+    // one chain: the single-vector fg! (the plain path) instead of the batched GEMMs
+    bool single = false;
+    const double *d_data = nullptr;
+    double *d_Gd = nullptr, *d_comp = nullptr;
 };
+
+// The run's pending device errors: the batched pipeline's flag, or the single-vector one.
+int run_check(sfh_ctx *ctx, const HmcRun &h) {
+    if (!h.single) return sfh_batched_check(ctx, h.plan);
+    SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return sfh_check_onepass(ctx);
+}
 
 int launch_eval(sfh_ctx *ctx, const sfh_models *m, HmcRun &h, bool want_logd) {
     cudaStream_t st = ctx->stream;
@@ -456,12 +504,38 @@ int launch_eval(sfh_ctx *ctx, const sfh_models *m, HmcRun &h, bool want_logd) {
         k_mzr_map<<<h.c.B, kT, 0, st>>>(h.s.theta, h.c, h.z, h.d_r);
     }
     SFH_LAUNCHED(ctx);
+    if (h.single) {  // one chain: the single-vector fg! on the FP32 templates
+        FgArgs a{};
+        a.coeffs = h.d_r;
+        a.data = h.d_data;
+        a.composite = h.d_comp;
+        a.G = h.d_Gd;
+        a.negLogL = h.d_negL;
+        a.eps = h.eps_abs;
+        a.gsign = 1.0;
+        a.mode = FG_MODE_FG;
+        int rc = sfh_launch_fg(ctx, m, a);
+        if (rc) return rc;
+        if (h.c.model == 0) {
+            k_direct_grad<double><<<1, kT, 0, st>>>(h.s.theta, h.d_r, h.d_Gd, h.d_negL, h.c.D,
+                                                    h.s.g, h.s.logd, want_logd ? 1 : 0);
+        } else {
+            const size_t sm = (size_t)(h.z.nages * 10 + 3) * sizeof(double);
+            if (sm > 48 * 1024)
+                SFH_CK(ctx, cudaFuncSetAttribute(k_mzr_grad<double>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            k_mzr_grad<double><<<1, 64, sm, st>>>(h.s.theta, h.d_r, h.d_Gd, h.d_negL, h.c, h.z,
+                                                  h.s.g, h.s.logd, want_logd ? 1 : 0);
+        }
+        SFH_LAUNCHED(ctx);
+        return SFH_OK;
+    }
     int rc = sfh_batched_launch(ctx, h.mb ? h.mb : m, h.plan, h.d_r, want_logd ? h.d_negL : nullptr,
                                 h.d_G, h.eps_abs);
     if (rc) return rc;
     if (h.c.model == 0) {
-        k_direct_grad<<<h.c.B, kT, 0, st>>>(h.s.theta, h.d_r, h.d_G, h.d_negL, h.c.D, h.s.g,
-                                            h.s.logd, want_logd ? 1 : 0);
+        k_direct_grad<float><<<h.c.B, kT, 0, st>>>(h.s.theta, h.d_r, h.d_G, h.d_negL, h.c.D, h.s.g,
+                                                   h.s.logd, want_logd ? 1 : 0);
     } else {
         const size_t sm = (size_t)(h.z.nages * 10 + 3) * sizeof(double);
         if (sm > 48 * 1024)
@@ -555,7 +629,7 @@ int setup_run(sfh_ctx *ctx, const sfh_models *m, const double *d_data, const sfh
     c.ndraws = d_draws ? (cfg->ntraj + c.thin - 1) / c.thin : 0;
     h.eps_abs = 2.220446049250313e-16;
     const int nt = (int)m->nt;
-    std::vector<int> jidx, age_off, age_tmpl, sorted;
+    std::vector<int> jidx, age_off, age_tmpl, sorted, uni;
     if (c.model == SFH_HMC_DIRECT) {
         c.D = nt;
     } else if (c.model == SFH_HMC_MZR || c.model == SFH_HMC_LINEAR_AMR ||
@@ -588,6 +662,20 @@ int setup_run(sfh_ctx *ctx, const sfh_models *m, const double *d_data, const sfh
         age_tmpl.assign(nt, 0);
         std::vector<int> fill(age_off.begin(), age_off.end() - 1);
         for (int k = 0; k < nt; ++k) age_tmpl[fill[jidx[k]]++] = k;
+        // each age's templates in ascending [M/H]; an age whose [M/H] are evenly spaced
+        // (to 1e-9 of the step) takes the product recurrence in k_mzr_map
+        uni.assign(c.nages, 0);
+        for (int j = 0; j < c.nages; ++j) {
+            int *b0 = age_tmpl.data() + age_off[j], *b1 = age_tmpl.data() + age_off[j + 1];
+            std::stable_sort(b0, b1, [&](int a, int b) { return cfg->h_MH[a] < cfg->h_MH[b]; });
+            const int n = (int)(b1 - b0);
+            if (n < 3) continue;
+            const double dl = (cfg->h_MH[b0[n - 1]] - cfg->h_MH[b0[0]]) / (n - 1);
+            bool even = dl > 0.0;
+            for (int k = 1; k < n && even; ++k)
+                even = std::fabs(cfg->h_MH[b0[k]] - cfg->h_MH[b0[0]] - k * dl) <= 1e-9 * dl;
+            uni[j] = even ? 1 : 0;
+        }
         sorted.resize(c.nages);
         for (int j = 0; j < c.nages; ++j) sorted[j] = j;
         std::stable_sort(sorted.begin(), sorted.end(),
@@ -630,6 +718,7 @@ int setup_run(sfh_ctx *ctx, const sfh_models *m, const double *d_data, const sfh
         int *dj = (int *)alloc(nt * 4), *dao = (int *)alloc((c.nages + 1) * 4);
         int *dat = (int *)alloc(nt * 4), *dso = (int *)alloc(c.nages * 4);
         double *dmh = (double *)alloc(nt * 8);
+        int *duni = (int *)alloc(c.nages * 4);
         h.z.aux = (double *)alloc((size_t)c.B * 4 * c.nages * 8);
         h.z.A = (double *)alloc((size_t)c.B * nt * 8);
         for (void *p : owned)
@@ -640,6 +729,8 @@ int setup_run(sfh_ctx *ctx, const sfh_models *m, const double *d_data, const sfh
         cudaMemcpy(dso, sorted.data(), c.nages * 4, cudaMemcpyHostToDevice);
         cudaMemcpy(dmh, cfg->h_MH, nt * 8, cudaMemcpyHostToDevice);
         cudaMemcpy(dta, tage.data(), c.nages * 8, cudaMemcpyHostToDevice);
+        cudaMemcpy(duni, uni.data(), c.nages * 4, cudaMemcpyHostToDevice);
+        h.z.uni = duni;
         h.z.tage = dta;
         h.z.nt = nt;
         h.z.nages = c.nages;
@@ -653,6 +744,15 @@ int setup_run(sfh_ctx *ctx, const sfh_models *m, const double *d_data, const sfh
         if (!p) return sfh_set_error(ctx, SFH_ERR_NOMEM, "HMC buffers");
     if (!batched) return SFH_OK;
     int rc;
+    if (c.B == 1 && sfh_onepass_eligible(ctx, m)) {
+        // one chain: the plain single-vector path (no batch to fill the tensor cores)
+        h.single = true;
+        h.d_data = d_data;
+        h.d_Gd = (double *)alloc((size_t)nt * 8);
+        h.d_comp = (double *)alloc((size_t)m->nbins * 8);
+        if (!h.d_Gd || !h.d_comp) return sfh_set_error(ctx, SFH_ERR_NOMEM, "HMC buffers");
+        return sfh_scratch_reserve(ctx, sfh_onepass_scratch(ctx, m));
+    }
     // the occupied-bin plan's derived handle (the diagram is fixed for the whole run: its
     // counts are gathered and checked once here)
     const sfh_models *mb = m;
@@ -680,6 +780,377 @@ void free_run(sfh_ctx *ctx, std::vector<void *> &owned) {
     owned.clear();
 }
 
+
+// ---------------------------------------------------------------- NUTS
+// No-U-Turn sampler with multinomial sampling (DynamicHMC's NUTS, the sampler of
+// hmc_sample.jl:105-141 and sample_sfh): every chain runs its own trajectory state machine
+// and advances by one leapfrog step per batched evaluation, so chains whose trees stop
+// early start their next trajectory at once and no evaluation is wasted on a finished
+// tree.  Per trajectory: momentum p0 ~ N(0, M), trees doubled in a random direction until
+// the generalized no-U-turn criterion (p♯ = M⁻¹ p at either end against the momentum sum
+// ρ: turning when p♯₋·ρ < 0 or p♯₊·ρ < 0) holds for the whole tree or for any subtree,
+// the energy error exceeds 1000 (divergence), or the depth reaches max_depth.  States
+// are weighted by exp(H0 - H): uniform progressive sampling inside a new subtree, biased
+// progressive sampling when it joins the tree (Betancourt 2017).  Subtree checks run
+// iteratively from O(max_depth) checkpoints of momenta and cumulative sums (the leaf
+// index's bits name the subtrees a leaf closes).  Warmup: per-chain dual averaging of
+// the step on the mean acceptance statistic of each tree (Hoffman & Gelman 2014), and a
+// per-chain diagonal metric from the variance of the chain's own draws over the middle
+// 70 % of warmup.
+constexpr int kNutsMaxDepth = 12;
+constexpr int kNutsMaxDense = 256;  // largest D for a dense metric
+enum { NUTS_FRESH = 0, NUTS_RUN = 1 };
+
+struct NutsState {
+    double *thL, *pL, *gL, *sL, *thR, *pR, *gR, *sR;  // B x D trajectory ends (s: p♯ = M⁻¹ p)
+    double *ths, *gs, *thu, *gu;            // B x D proposals: tree, subtree
+    double *rho, *rhos;                     // B x D momentum sums: tree, subtree
+    double *ckp, *ckr, *cks;                // B x maxdepth x D checkpoints: p, Σ p, p♯
+    double *minv, *wm, *wm2;                // B x D diagonal metric and its Welford window
+    double *q;                              // B x D scratch: M⁻¹ x, or the momentum draws
+    const double *Md;                       // D x D dense M⁻¹ (row-major) or NULL: diagonal
+    const double *Lt;                       // D x D: M⁻¹ = L Lᵀ, Lt = L⁻ᵀ (p = Lt z)
+    double *logds, *logdu, *H0, *logW, *logWs, *accsum, *depth_sum;  // B
+    int *depth, *dir, *leaf, *status, *nleaf, *ndiv, *div_now;       // B
+    int64_t *tb, *tick, *nwin;              // B
+    unsigned int *done;                     // chains that have all their draws
+    int maxdepth;
+};
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double logaddexp(double a, double b) {
+    const double m = fmax(a, b);
+    return m == -INFINITY ? -INFINITY : m + log(exp(a - m) + exp(b - m));
+}
+__device__ __forceinline__ double nuts_u01(const HmcConst &c, int b, int64_t tick, uint32_t stream) {
+    const u4 r = philox(u4{0xFFFFFF00u + stream, (uint32_t)b, (uint32_t)tick, (uint32_t)(tick >> 32)},
+                        (uint32_t)c.seed, (uint32_t)(c.seed >> 32));
+    return u01(r.x, r.y);
+}
+
+// out = M⁻¹ x for chain b (a warp: lane l owns entries l, l + 32, ...; x is complete in
+// memory before the call, out is complete after it).
+__device__ __forceinline__ void nuts_sharp(const NutsState &n, int b, int D, const double *x,
+                                           double *out, int lane) {
+    __syncwarp();
+    if (n.Md) {
+        for (int d = lane; d < D; d += 32) {
+            const double *row = n.Md + (int64_t)d * D;
+            double a = 0.0;
+            for (int j = 0; j < D; ++j) a = fma(row[j], x[j], a);
+            out[d] = a;
+        }
+    } else {
+        const double *mi = n.minv + (int64_t)b * D;
+        for (int d = lane; d < D; d += 32) out[d] = mi[d] * x[d];
+    }
+    __syncwarp();
+}
+
+// One leapfrog step of chain b (warp) from the state in (th, p, g) in direction v: half
+// kick, drift by M⁻¹ p; the evaluation supplies g at the new θ and the next tick the
+// second kick.
+__device__ __forceinline__ void nuts_leap(const NutsState &n, int b, double *th, double *p,
+                                          const double *g, int D, double e, int v, int lane) {
+    double *q = n.q + (int64_t)b * D;
+    for (int d = lane; d < D; d += 32) p[d] += v * 0.5 * e * g[d];
+    nuts_sharp(n, b, D, p, q, lane);
+    for (int d = lane; d < D; d += 32) th[d] += v * e * q[d];
+}
+
+__device__ void nuts_start(ChainState &s, NutsState &n, const HmcConst &c, int b, int lane) {
+    const int D = c.D;
+    double *th = s.theta + (int64_t)b * D, *p = s.p + (int64_t)b * D, *g = s.g + (int64_t)b * D;
+    double *q = n.q + (int64_t)b * D;
+    const int64_t t = n.tb[b];
+    // p ~ N(0, M): p = L⁻ᵀ z for a dense M⁻¹ = L Lᵀ, z / sqrt(minv) for a diagonal one;
+    // either way ½ pᵀ M⁻¹ p = ½ |z|²
+    double kin = 0.0;
+    for (int d = lane; d < D; d += 32) {
+        const double z = normal(c.seed, (uint32_t)d, (uint32_t)b, (uint32_t)t, 3u);
+        q[d] = z;
+        kin += 0.5 * z * z;
+    }
+    kin = warp_sum_d(kin);
+    __syncwarp();
+    if (n.Lt) {
+        for (int d = lane; d < D; d += 32) {
+            const double *row = n.Lt + (int64_t)d * D;
+            double a = 0.0;
+            for (int j = 0; j < D; ++j) a = fma(row[j], q[j], a);
+            p[d] = a;
+        }
+    } else {
+        const double *mi = n.minv + (int64_t)b * D;
+        for (int d = lane; d < D; d += 32) p[d] = q[d] / sqrt(mi[d]);
+    }
+    nuts_sharp(n, b, D, p, q, lane);  // p♯ of the starting state
+    for (int d = lane; d < D; d += 32) {
+        const int64_t k = (int64_t)b * D + d;
+        n.thL[k] = n.thR[k] = n.ths[k] = th[d];
+        n.gL[k] = n.gR[k] = n.gs[k] = g[d];
+        n.pL[k] = n.pR[k] = n.rho[k] = p[d];
+        n.sL[k] = n.sR[k] = q[d];
+    }
+    const int64_t tk = n.tick[b];
+    const int v = nuts_u01(c, b, tk, 0) < 0.5 ? -1 : 1;
+    if (lane == 0) {
+        n.H0[b] = -s.logd[b] + kin;
+        n.logds[b] = s.logd[b];
+        n.logW[b] = 0.0;
+        n.depth[b] = 0;
+        n.dir[b] = v;
+        n.leaf[b] = 0;
+        n.accsum[b] = 0.0;
+        n.nleaf[b] = 0;
+        n.div_now[b] = 0;
+        n.status[b] = NUTS_RUN;
+    }
+    nuts_leap(n, b, th, p, g, D, s.eps[b], v, lane);
+}
+
+// The tree is finished: record its proposal, adapt during warmup, start the next tree.
+__device__ void nuts_finish(ChainState &s, NutsState &n, const HmcConst &c, int b, int lane) {
+    const int D = c.D;
+    const int64_t t = n.tb[b];
+    const double a = n.nleaf[b] > 0 ? n.accsum[b] / n.nleaf[b] : 0.0;
+    double *th = s.theta + (int64_t)b * D, *g = s.g + (int64_t)b * D;
+    for (int d = lane; d < D; d += 32) {  // the proposal becomes the chain's state
+        const int64_t k = (int64_t)b * D + d;
+        th[d] = n.ths[k];
+        g[d] = n.gs[k];
+    }
+    const int64_t w0 = (int64_t)(0.15 * c.nwarm), w1 = (int64_t)(0.85 * c.nwarm);
+    if (t < c.nwarm) {
+        if (lane == 0) {
+            dual_average(s.da + 4 * b, s.eps + b, a, c.target);
+            if (t == c.nwarm - 1) s.eps[b] = exp(s.da[4 * b + 2]);
+        }
+        // the metric window (a diagonal metric only; a dense one is given and kept)
+        if (!n.Md && t >= w0 && t < w1 && c.nwarm >= 20) {
+            const double m1 = (double)(n.nwin[b] + 1);
+            for (int d = lane; d < D; d += 32) {
+                const int64_t k = (int64_t)b * D + d;
+                const double x = th[d], dl = x - n.wm[k];
+                n.wm[k] += dl / m1;
+                n.wm2[k] += dl * (x - n.wm[k]);
+            }
+            __syncwarp();
+            if (lane == 0) n.nwin[b] += 1;
+            if (t == w1 - 1) {  // the diagonal metric from the window, regularised
+                const double nw = m1;
+                for (int d = lane; d < D; d += 32) {
+                    const int64_t k = (int64_t)b * D + d;
+                    const double var = nw > 1.0 ? n.wm2[k] / (nw - 1.0) : 1.0;
+                    n.minv[k] = (nw / (nw + 5.0)) * var + 1e-3 * (5.0 / (nw + 5.0));
+                }
+                if (lane == 0) {  // restart the step adaptation around the current step
+                    double *da = s.da + 4 * b;
+                    da[0] = log(10.0 * s.eps[b]);
+                    da[1] = da[2] = da[3] = 0.0;
+                }
+            }
+        }
+    } else if (t < c.nwarm + c.nsamp) {
+        const int64_t ts = t - c.nwarm;
+        for (int d = lane; d < D; d += 32) {
+            const int64_t k = (int64_t)b * D + d;
+            const double x = nat_param(c, th, d);
+            const double n1 = (double)(ts + 1);
+            const double delta = x - s.mean[k];
+            s.mean[k] += delta / n1;
+            s.m2[k] += delta * (x - s.mean[k]);
+            if (s.draws && c.thin > 0 && ts % c.thin == 0 && ts / c.thin < c.ndraws)
+                s.draws[((int64_t)b * c.ndraws + ts / c.thin) * D + d] = (float)x;
+        }
+        if (lane == 0) {
+            s.acc_sum[b] += a;
+            n.depth_sum[b] += n.depth[b];
+            n.ndiv[b] += n.div_now[b];
+        }
+    }
+    if (lane == 0) {
+        s.logd[b] = n.logds[b];
+        n.tb[b] = t + 1;
+        if (t + 1 == c.nwarm + c.nsamp) atomicAdd(n.done, 1u);
+    }
+    __syncwarp();
+    nuts_start(s, n, c, b, lane);
+}
+
+// One tick per chain (a warp each): the second half kick of the step just evaluated, the
+// tree bookkeeping, and the next leapfrog step (whose position the next evaluation takes).
+__global__ void k_nuts_tick(ChainState s, NutsState n, HmcConst c) {
+    const int b = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (b >= c.B) return;
+    const int D = c.D;
+    if (n.status[b] == NUTS_FRESH) {  // the starting point was evaluated
+        nuts_start(s, n, c, b, lane);
+        if (lane == 0) n.tick[b] += 1;
+        return;
+    }
+    double *th = s.theta + (int64_t)b * D, *p = s.p + (int64_t)b * D, *g = s.g + (int64_t)b * D;
+    double *q = n.q + (int64_t)b * D;
+    const double e = s.eps[b];
+    const int v = n.dir[b], j = n.depth[b], leaf = n.leaf[b];
+    const int64_t tk = n.tick[b];
+    for (int d = lane; d < D; d += 32) p[d] += v * 0.5 * e * g[d];
+    nuts_sharp(n, b, D, p, q, lane);  // p♯ of the new state
+    double kin = 0.0;
+    for (int d = lane; d < D; d += 32) kin += 0.5 * p[d] * q[d];
+    kin = warp_sum_d(kin);
+    const double logd = s.logd[b];
+    const double delta = n.H0[b] - (-logd + kin);  // log weight of the new state
+    const bool divergent = !(delta >= -1000.0);     // NaN counts as divergent
+    if (lane == 0) {
+        n.accsum[b] += divergent ? 0.0 : exp(fmin(0.0, delta));
+        n.nleaf[b] += 1;
+        n.tick[b] = tk + 1;
+    }
+    if (divergent) {
+        if (lane == 0) n.div_now[b] = 1;
+        __syncwarp();
+        nuts_finish(s, n, c, b, lane);
+        return;
+    }
+    // the subtree: progressive (uniform) sampling and the momentum sum
+    const int64_t base = (int64_t)b * D;
+    bool take;
+    double lws;
+    if (leaf == 0) {
+        lws = delta;
+        take = true;
+    } else {
+        lws = logaddexp(n.logWs[b], delta);
+        take = nuts_u01(c, b, tk, 1) < exp(delta - lws);
+    }
+    for (int d = lane; d < D; d += 32) {
+        const int64_t k = base + d;
+        n.rhos[k] = (leaf == 0 ? 0.0 : n.rhos[k]) + p[d];
+        if (take) {
+            n.thu[k] = th[d];
+            n.gu[k] = g[d];
+        }
+    }
+    if (lane == 0) {
+        n.logWs[b] = lws;
+        if (take) n.logdu[b] = logd;
+    }
+    // checkpoints and the subtrees this leaf closes
+    const int64_t ck = (int64_t)b * n.maxdepth * D;
+    const int imax = __popc((unsigned)leaf >> 1);
+    bool turning = false;
+    if ((leaf & 1) == 0) {
+        for (int d = lane; d < D; d += 32) {
+            n.ckp[ck + (int64_t)imax * D + d] = p[d];
+            n.ckr[ck + (int64_t)imax * D + d] = n.rhos[base + d];
+            n.cks[ck + (int64_t)imax * D + d] = q[d];
+        }
+    } else {
+        const int imin = imax - (__ffs(~(unsigned)leaf) - 1) + 1;  // trailing ones
+        for (int i = imax; i >= imin && !turning; --i) {
+            double a1 = 0.0, a2 = 0.0;
+            for (int d = lane; d < D; d += 32) {
+                const int64_t kc = ck + (int64_t)i * D + d;
+                const double sr = n.rhos[base + d] - n.ckr[kc] + n.ckp[kc];
+                a1 += n.cks[kc] * sr;
+                a2 += q[d] * sr;
+            }
+            a1 = warp_sum_d(a1);
+            a2 = warp_sum_d(a2);
+            turning = a1 < 0.0 || a2 < 0.0;
+        }
+    }
+    if (turning) {  // the subtree is dropped; the tree's proposal stands
+        __syncwarp();
+        nuts_finish(s, n, c, b, lane);
+        return;
+    }
+    if (leaf + 1 < (1 << j)) {  // the subtree continues from this state
+        if (lane == 0) n.leaf[b] = leaf + 1;
+        nuts_leap(n, b, th, p, g, D, e, v, lane);
+        return;
+    }
+    // the subtree is complete: join it (biased progressive sampling), check the whole tree
+    const bool jump = nuts_u01(c, b, tk, 2) < exp(lws - n.logW[b]);
+    double *eth = v > 0 ? n.thR : n.thL, *ep = v > 0 ? n.pR : n.pL, *eg = v > 0 ? n.gR : n.gL;
+    double *es = v > 0 ? n.sR : n.sL;
+    double t1 = 0.0, t2 = 0.0;
+    for (int d = lane; d < D; d += 32) {
+        const int64_t k = base + d;
+        if (jump) {
+            n.ths[k] = n.thu[k];
+            n.gs[k] = n.gu[k];
+        }
+        eth[k] = th[d];
+        ep[k] = p[d];
+        eg[k] = g[d];
+        es[k] = q[d];
+        const double r = n.rho[k] + n.rhos[k];
+        n.rho[k] = r;
+        t1 += n.sL[k] * r;
+        t2 += n.sR[k] * r;
+    }
+    t1 = warp_sum_d(t1);
+    t2 = warp_sum_d(t2);
+    if (lane == 0) {
+        if (jump) n.logds[b] = n.logdu[b];
+        n.logW[b] = logaddexp(n.logW[b], lws);
+    }
+    const int jn = j + 1;
+    if (t1 < 0.0 || t2 < 0.0 || jn >= n.maxdepth) {
+        if (lane == 0) n.depth[b] = jn;
+        __syncwarp();
+        nuts_finish(s, n, c, b, lane);
+        return;
+    }
+    // double again from the end in a fresh direction
+    const int vn = nuts_u01(c, b, tk, 3) < 0.5 ? -1 : 1;
+    const double *sth = vn > 0 ? n.thR : n.thL, *sp = vn > 0 ? n.pR : n.pL, *sg = vn > 0 ? n.gR : n.gL;
+    __syncwarp();
+    for (int d = lane; d < D; d += 32) {
+        th[d] = sth[base + d];
+        p[d] = sp[base + d];
+        g[d] = sg[base + d];
+    }
+    if (lane == 0) {
+        n.depth[b] = jn;
+        n.dir[b] = vn;
+        n.leaf[b] = 0;
+    }
+    nuts_leap(n, b, th, p, g, D, e, vn, lane);
+}
+
+__global__ void k_nuts_init(NutsState n, HmcConst c, const double *minv0) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < (int64_t)c.B * c.D) {
+        n.minv[k] = minv0 ? minv0[k % c.D] : 1.0;
+        n.wm[k] = 0.0;
+        n.wm2[k] = 0.0;
+    }
+    if (k < c.B) {
+        n.status[k] = NUTS_FRESH;
+        n.tb[k] = 0;
+        n.tick[k] = 0;
+        n.nwin[k] = 0;
+        n.depth_sum[k] = 0.0;
+        n.ndiv[k] = 0;
+    }
+}
+
+__global__ void k_nuts_out(ChainState s, NutsState n, HmcConst c, double *depth, int64_t *ndiv) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < c.B) {
+        if (depth) depth[k] = c.nsamp > 0 ? n.depth_sum[k] / (double)c.nsamp : 0.0;
+        if (ndiv) ndiv[k] = n.ndiv[k];
+    }
+}
+
 }  // namespace
 
 extern "C" int sfh_logdensity_batched_dev(sfh_ctx *ctx, const sfh_models *m, const double *d_data,
@@ -695,7 +1166,7 @@ extern "C" int sfh_logdensity_batched_dev(sfh_ctx *ctx, const sfh_models *m, con
         // evaluate into the run's state arrays, then copy out
         cudaMemcpyAsync(h.s.theta, d_theta, BD * 8, cudaMemcpyDeviceToDevice, ctx->stream);
         rc = launch_eval(ctx, m, h, true);
-        if (!rc) rc = sfh_batched_check(ctx, h.plan);
+        if (!rc) rc = run_check(ctx, h);
         if (!rc) {
             cudaMemcpyAsync(d_logd, h.s.logd, (size_t)h.c.B * 8, cudaMemcpyDeviceToDevice, ctx->stream);
             cudaMemcpyAsync(d_grad, h.s.g, BD * 8, cudaMemcpyDeviceToDevice, ctx->stream);
@@ -728,7 +1199,7 @@ extern "C" int sfh_hmc_sample_dev(sfh_ctx *ctx, const sfh_models *m, const doubl
         SFH_CK(ctx, cudaMemcpyAsync(s.minv, cfg->d_minv0, (size_t)c.D * 8, cudaMemcpyDeviceToDevice, st));
     // gradient and log density at the starting points (eager: also warms every kernel)
     if ((rc = launch_eval(ctx, m, h, true))) { cleanup(); return rc; }
-    if ((rc = sfh_batched_check(ctx, h.plan))) { cleanup(); return rc; }
+    if ((rc = run_check(ctx, h))) { cleanup(); return rc; }
     // capture one trajectory and replay it
     const int64_t ntot = c.nwarm + c.nsamp;
     cudaGraph_t graph = nullptr;
@@ -737,10 +1208,14 @@ extern "C" int sfh_hmc_sample_dev(sfh_ctx *ctx, const sfh_models *m, const doubl
     if (use_graph) {
         if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) use_graph = false;
     }
+    int64_t per_replay = 0;  // kernels in one replay (counted while capturing)
     if (use_graph) {
+        const int64_t l0 = ctx->launches;
         ctx->internal_capture = true;  // the graph lives only inside this call
         rc = launch_trajectory(ctx, m, h);
         ctx->internal_capture = false;
+        per_replay = ctx->launches - l0;
+        ctx->launches = l0;
         cudaError_t e = cudaStreamEndCapture(st, &graph);
         if (rc || e != cudaSuccess || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
             if (graph) cudaGraphDestroy(graph);
@@ -752,15 +1227,15 @@ extern "C" int sfh_hmc_sample_dev(sfh_ctx *ctx, const sfh_models *m, const doubl
     for (int64_t t = 0; t < ntot; ++t) {
         if (use_graph) {
             if (cudaGraphLaunch(exec, st) != cudaSuccess) { rc = sfh_cuda_error(ctx, cudaGetLastError(), "graph launch"); break; }
-            ctx->launches += 7 * c.nleap + 6;
+            ctx->launches += per_replay;
         } else if ((rc = launch_trajectory(ctx, m, h))) {
             break;
         }
-        if ((t & 63) == 63 && (rc = sfh_batched_check(ctx, h.plan))) break;
+        if ((t & 63) == 63 && (rc = run_check(ctx, h))) break;
     }
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
-    if (!rc) rc = sfh_batched_check(ctx, h.plan);
+    if (!rc) rc = run_check(ctx, h);
     if (!rc) {
         k_finish<<<(unsigned)((std::max(BD, (int64_t)c.B) + kT - 1) / kT), kT, 0, st>>>(
             s, c, d_mean, d_var, d_accept, d_step);
@@ -768,6 +1243,196 @@ extern "C" int sfh_hmc_sample_dev(sfh_ctx *ctx, const sfh_models *m, const doubl
     }
     cleanup();
     return rc;
+}
+
+extern "C" int sfh_nuts_sample_dev(sfh_ctx *ctx, const sfh_models *m, const double *d_data,
+                                   const sfh_hmc_config *cfg, int max_depth,
+                                   const double *d_minv_dense, const double *d_theta0,
+                                   double *d_mean, double *d_var, double *d_accept,
+                                   double *d_step, double *d_depth, int64_t *d_ndiv,
+                                   float *d_draws) {
+    if (!ctx || !m || !d_data || !cfg || !d_theta0) return SFH_ERR_ARG;
+    if (max_depth < 1 || max_depth > kNutsMaxDepth)
+        return sfh_set_error(ctx, SFH_ERR_ARG, "max_depth must be in 1..12");
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    HmcRun h{};
+    std::vector<void *> owned;
+    auto cleanup = [&]() { free_run(ctx, owned); };
+    int rc = setup_run(ctx, m, d_data, cfg, d_draws, h, owned);
+    if (rc) { cleanup(); return rc; }
+    HmcConst &c = h.c;
+    ChainState &s = h.s;
+    const int64_t BD = (int64_t)c.B * c.D;
+    cudaStream_t st = ctx->stream;
+    NutsState n{};
+    n.maxdepth = max_depth;
+    if (d_minv_dense) {
+        // a dense metric M⁻¹ (the reference's sample_sfh passes the MAP inverse Hessian,
+        // generic_fitting.jl:484-490): its Cholesky factor L and Lt = L⁻ᵀ for the momenta
+        const int D = c.D;
+        if (D > kNutsMaxDense) {
+            cleanup();
+            return sfh_set_error(ctx, SFH_ERR_ARG, "a dense metric needs D <= 256");
+        }
+        std::vector<double> Mi((size_t)D * D), L((size_t)D * D, 0.0), Lt((size_t)D * D, 0.0);
+        if (cudaMemcpy(Mi.data(), d_minv_dense, Mi.size() * 8, cudaMemcpyDeviceToHost) != cudaSuccess) {
+            cleanup();
+            return sfh_cuda_error(ctx, cudaGetLastError(), "dense metric copy");
+        }
+        for (int i = 0; i < D; ++i)
+            for (int k = 0; k <= i; ++k) {
+                double a = 0.5 * (Mi[(size_t)i * D + k] + Mi[(size_t)k * D + i]);
+                for (int q = 0; q < k; ++q) a -= L[(size_t)i * D + q] * L[(size_t)k * D + q];
+                if (i == k) {
+                    if (!(a > 0.0)) {
+                        cleanup();
+                        return sfh_set_error(ctx, SFH_ERR_ARG, "the dense metric is not positive definite");
+                    }
+                    L[(size_t)i * D + i] = std::sqrt(a);
+                } else {
+                    L[(size_t)i * D + k] = a / L[(size_t)k * D + k];
+                }
+            }
+        // X = L⁻¹ by forward substitution, then Lt = Xᵀ
+        std::vector<double> X((size_t)D * D, 0.0);
+        for (int col = 0; col < D; ++col)
+            for (int i = col; i < D; ++i) {
+                double a = i == col ? 1.0 : 0.0;
+                for (int q = col; q < i; ++q) a -= L[(size_t)i * D + q] * X[(size_t)q * D + col];
+                X[(size_t)i * D + col] = a / L[(size_t)i * D + i];
+            }
+        for (int i = 0; i < D; ++i)
+            for (int k = 0; k < D; ++k) Lt[(size_t)i * D + k] = X[(size_t)k * D + i];
+        // the symmetrised metric and Lt in one allocation
+        double *dm = nullptr;
+        if (cudaMalloc(&dm, Mi.size() * 16) != cudaSuccess) {
+            cleanup();
+            return sfh_set_error(ctx, SFH_ERR_NOMEM, "dense metric");
+        }
+        owned.push_back(dm);
+        for (int i = 0; i < D; ++i)
+            for (int k = 0; k < i; ++k)
+                Mi[(size_t)i * D + k] = Mi[(size_t)k * D + i] =
+                    0.5 * (Mi[(size_t)i * D + k] + Mi[(size_t)k * D + i]);
+        if (cudaMemcpy(dm, Mi.data(), Mi.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(dm + Mi.size(), Lt.data(), Lt.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess) {
+            cleanup();
+            return sfh_cuda_error(ctx, cudaGetLastError(), "dense metric upload");
+        }
+        n.Md = dm;
+        n.Lt = dm + Mi.size();
+    }
+    {
+        double **vec[] = {&n.thL, &n.pL, &n.gL, &n.sL, &n.thR, &n.pR, &n.gR, &n.sR, &n.ths, &n.gs,
+                          &n.thu, &n.gu, &n.rho, &n.rhos, &n.minv, &n.wm, &n.wm2, &n.q};
+        double **sca[] = {&n.logds, &n.logdu, &n.H0, &n.logW, &n.logWs, &n.accsum, &n.depth_sum};
+        int **isc[] = {&n.depth, &n.dir, &n.leaf, &n.status, &n.nleaf, &n.ndiv, &n.div_now};
+        int64_t **lsc[] = {&n.tb, &n.tick, &n.nwin};
+        auto get = [&](size_t bytes) -> void * {
+            void *q = nullptr;
+            if (cudaMalloc(&q, bytes) != cudaSuccess) return nullptr;
+            owned.push_back(q);
+            return q;
+        };
+        bool ok = true;
+        for (auto v : vec) ok = ok && (*v = (double *)get((size_t)BD * 8));
+        for (auto v : sca) ok = ok && (*v = (double *)get((size_t)c.B * 8));
+        for (auto v : isc) ok = ok && (*v = (int *)get((size_t)c.B * 4));
+        for (auto v : lsc) ok = ok && (*v = (int64_t *)get((size_t)c.B * 8));
+        ok = ok && (n.ckp = (double *)get((size_t)BD * max_depth * 8));
+        ok = ok && (n.ckr = (double *)get((size_t)BD * max_depth * 8));
+        ok = ok && (n.cks = (double *)get((size_t)BD * max_depth * 8));
+        if (!ok) {
+            cleanup();
+            return sfh_set_error(ctx, SFH_ERR_NOMEM, "NUTS state");
+        }
+    }
+    unsigned int *h_done = nullptr, *d_done = nullptr;
+    if (cudaHostAlloc((void **)&h_done, sizeof(unsigned int), cudaHostAllocMapped) != cudaSuccess ||
+        cudaHostGetDevicePointer((void **)&d_done, h_done, 0) != cudaSuccess) {
+        if (h_done) cudaFreeHost(h_done);
+        cleanup();
+        return sfh_set_error(ctx, SFH_ERR_NOMEM, "NUTS completion flag");
+    }
+    *(volatile unsigned int *)h_done = 0u;
+    n.done = d_done;
+    auto done_call = [&](int r) {
+        cudaStreamSynchronize(st);
+        cudaFreeHost(h_done);
+        cleanup();
+        return r;
+    };
+    if (cudaMemcpyAsync(s.theta, d_theta0, BD * 8, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+        return done_call(sfh_cuda_error(ctx, cudaGetLastError(), "theta0 copy"));
+    k_init_state<<<(unsigned)((std::max(BD, (int64_t)std::max(c.B, c.D)) + kT - 1) / kT), kT, 0, st>>>(
+        s, c, cfg->step0);
+    ctx->launches++;
+    k_nuts_init<<<(unsigned)((std::max(BD, (int64_t)c.B) + kT - 1) / kT), kT, 0, st>>>(n, c, cfg->d_minv0);
+    ctx->launches++;
+    if ((rc = launch_eval(ctx, m, h, true))) return done_call(rc);
+    if ((rc = run_check(ctx, h))) return done_call(rc);
+    // K ticks per replay of a captured graph: a tick is the tree bookkeeping of every chain
+    // and one batched evaluation at the positions it produced
+    const int K = 16;
+    const unsigned tb_grid = (unsigned)(((int64_t)c.B * 32 + kT - 1) / kT);
+    auto tick = [&]() -> int {
+        k_nuts_tick<<<tb_grid, kT, 0, st>>>(s, n, c);
+        SFH_LAUNCHED(ctx);
+        return launch_eval(ctx, m, h, true);
+    };
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int64_t per_replay = 0;
+    bool use_graph = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (use_graph) {
+        const int64_t l0 = ctx->launches;
+        ctx->internal_capture = true;
+        for (int k = 0; k < K && !rc; ++k) rc = tick();
+        ctx->internal_capture = false;
+        cudaError_t e = cudaStreamEndCapture(st, &graph);
+        per_replay = ctx->launches - l0;
+        ctx->launches = l0;
+        if (rc || e != cudaSuccess || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            graph = nullptr;
+            exec = nullptr;
+            cudaGetLastError();
+            use_graph = false;
+            rc = SFH_OK;
+        }
+    }
+    // every chain needs nwarm + nsamp trees of at most 2^max_depth states each
+    const int64_t ntot = c.nwarm + c.nsamp;
+    const int64_t max_ticks = (ntot + 1) * ((int64_t)1 << max_depth) + 2 * K;
+    for (int64_t t = 0; t < max_ticks && rc == SFH_OK; t += K) {
+        if (use_graph) {
+            if (cudaGraphLaunch(exec, st) != cudaSuccess) {
+                rc = sfh_cuda_error(ctx, cudaGetLastError(), "graph launch");
+                break;
+            }
+            ctx->launches += per_replay;
+        } else {
+            for (int k = 0; k < K && !rc; ++k) rc = tick();
+            if (rc) break;
+        }
+        if ((t / K) % 8 == 7) {  // completion is read from mapped memory after a sync
+            if ((rc = run_check(ctx, h))) break;
+            if (*(volatile unsigned int *)h_done >= (unsigned)c.B) break;
+        }
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (!rc) rc = run_check(ctx, h);
+    if (!rc && *(volatile unsigned int *)h_done < (unsigned)c.B)
+        rc = sfh_set_error(ctx, SFH_ERR_TIMEOUT, "NUTS: chains did not finish within the tick bound");
+    if (!rc) {
+        k_finish<<<(unsigned)((std::max(BD, (int64_t)c.B) + kT - 1) / kT), kT, 0, st>>>(
+            s, c, d_mean, d_var, d_accept, d_step);
+        k_nuts_out<<<(unsigned)((c.B + kT - 1) / kT), kT, 0, st>>>(s, n, c, d_depth, d_ndiv);
+        ctx->launches += 2;
+        cudaGetLastError();
+    }
+    return done_call(rc);
 }
 
 // ---------------------------------------------------------------- device fit_sfh objective

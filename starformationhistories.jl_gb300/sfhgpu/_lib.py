@@ -33,7 +33,7 @@ EXPORTED = [
     "sfh_fg_batched_dev", "sfh_fg_kernel_times", "sfh_models_autotune", "sfh_models_set_path", "sfh_models_set_onepass_tile",
     "sfh_models_set_onepass_ctas", "sfh_models_set_onepass_schedule", "sfh_models_onepass_variant", "sfh_models_set_onepass_run",
     "sfh_models_set_occupied", "sfh_models_occupied_info",
-    "sfh_models_path", "sfh_fg_dev_noalloc", "sfh_hmc_sample_dev",
+    "sfh_models_path", "sfh_fg_dev_noalloc", "sfh_hmc_sample_dev", "sfh_nuts_sample_dev",
     "sfh_logdensity_batched_dev", "sfh_fit_sfh_dev", "sfh_model_cmd", "sfh_model_cmd_dev", "sfh_fit_bfgs", "sfh_fit_bfgs_dev", "sfh_bin_cmd", "sfh_bin_cmd_dev", "sfh_bin_cmd_smooth", "sfh_bin_cmd_smooth_batch_dev",
     "sfh_partial_cmd_smooth_batch_dev", "sfh_partial_cmd_smooth_ragged_dev",
     "sfh_binary_hess_batch_dev", "sfh_mix_binary_templates_dev",

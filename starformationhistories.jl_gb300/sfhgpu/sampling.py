@@ -52,6 +52,9 @@ def _bind():
         vp, i64 = C.c_void_p, C.c_int64
         L.sfh_hmc_sample_dev.argtypes = [vp, vp, vp, C.POINTER(HMCConfig), vp, vp, vp, vp, vp, vp]
         L.sfh_hmc_sample_dev.restype = C.c_int
+        L.sfh_nuts_sample_dev.argtypes = [vp, vp, vp, C.POINTER(HMCConfig), C.c_int, vp, vp, vp,
+                                          vp, vp, vp, vp, vp, vp]
+        L.sfh_nuts_sample_dev.restype = C.c_int
         L.sfh_logdensity_batched_dev.argtypes = [vp, vp, vp, C.POINTER(HMCConfig), vp, vp, vp]
         L.sfh_logdensity_batched_dev.restype = C.c_int
         from ._lib import FitOptions, FitResult
@@ -228,7 +231,8 @@ def logdensity_batched(models: Models, data, theta, model=SFH_HMC_DIRECT, mzr=No
     return logd.cpu().numpy(), grad.cpu().numpy()
 
 
-def _run_hmc(models, data, theta0, cfg, keep, keep_draws):
+def _run_hmc(models, data, theta0, cfg, keep, keep_draws, sampler="hmc", max_depth=10,
+             minv_dense=None):
     import torch
     L = _bind()
     dev = torch.device("cuda", models.ctx.device)
@@ -242,24 +246,50 @@ def _run_hmc(models, data, theta0, cfg, keep, keep_draws):
     ndraw = (cfg.ntraj + cfg.thin - 1) // cfg.thin
     draws = torch.empty((B, ndraw, D), dtype=torch.float32, device=dev) if keep_draws else None
     torch.cuda.synchronize(dev)
-    check(L.sfh_hmc_sample_dev(models.ctx.handle, models.handle, n.data_ptr(), C.byref(cfg),
-                               th0.data_ptr(), mean.data_ptr(), var.data_ptr(), acc.data_ptr(),
-                               step.data_ptr(), draws.data_ptr() if keep_draws else None),
-          models.ctx.handle, "hmc")
+    if sampler == "nuts":
+        depth = torch.empty(B, dtype=torch.float64, device=dev)
+        ndiv = torch.empty(B, dtype=torch.int64, device=dev)
+        md = None
+        if minv_dense is not None:
+            md = torch.as_tensor(np.ascontiguousarray(minv_dense, dtype=np.float64), device=dev)
+            torch.cuda.synchronize(dev)
+        check(L.sfh_nuts_sample_dev(models.ctx.handle, models.handle, n.data_ptr(), C.byref(cfg),
+                                    int(max_depth), md.data_ptr() if md is not None else None,
+                                    th0.data_ptr(), mean.data_ptr(),
+                                    var.data_ptr(), acc.data_ptr(), step.data_ptr(),
+                                    depth.data_ptr(), ndiv.data_ptr(),
+                                    draws.data_ptr() if keep_draws else None),
+              models.ctx.handle, "nuts")
+    else:
+        if sampler != "hmc":
+            raise ValueError("sampler is 'hmc' or 'nuts'")
+        check(L.sfh_hmc_sample_dev(models.ctx.handle, models.handle, n.data_ptr(), C.byref(cfg),
+                                   th0.data_ptr(), mean.data_ptr(), var.data_ptr(),
+                                   acc.data_ptr(), step.data_ptr(),
+                                   draws.data_ptr() if keep_draws else None),
+              models.ctx.handle, "hmc")
     del keep
     out = {"mean": mean.cpu().numpy(), "var": var.cpu().numpy(), "accept": acc.cpu().numpy(),
            "step": step.cpu().numpy()}
+    if sampler == "nuts":
+        out["depth"] = depth.cpu().numpy()
+        out["divergent"] = ndiv.cpu().numpy()
     if keep_draws:
         out["draws"] = draws.cpu().numpy()
     return out
 
 
 def hmc_sample(models: Models, data, nsteps, nchains=1, nwarmup=200, nleap=10, step0=0.01,
-               target_accept=0.8, seed=20261203, theta0=None, keep_draws=False, thin=1):
+               target_accept=0.8, seed=20261203, theta0=None, keep_draws=False, thin=1,
+               sampler="hmc", max_depth=10, minv_dense=None):
     """hmc_sample(models, data, nsteps, nchains), hmc_sample.jl:105-141: posterior of the
     log coefficients, all chains in lock step.  Returns a dict with per-chain posterior
     mean / variance of the coefficients (natural scale), acceptance and step size, and
-    optionally the draws (nchains x ceil(nsteps/thin) x ntemplates)."""
+    optionally the draws (nchains x ceil(nsteps/thin) x ntemplates).  sampler "hmc":
+    fixed-length trajectories of nleap steps; "nuts": DynamicHMC's No-U-Turn sampler
+    (sfh_nuts_sample_dev, trees up to max_depth doublings; adds "depth" and "divergent");
+    minv_dense (D x D) is a dense inverse metric for "nuts" (DynamicHMC's
+    GaussianKineticEnergy(M⁻¹)), kept through warmup."""
     if theta0 is None:
         from .fitting import renormalize_x0
         x0 = renormalize_x0(np.asarray(data, float).reshape(-1), models, np.ones(models.nt))
@@ -267,26 +297,36 @@ def hmc_sample(models: Models, data, nsteps, nchains=1, nwarmup=200, nleap=10, s
         theta0 = np.log(x0)[None, :] + 0.1 * rng.standard_normal((nchains, models.nt))
     cfg, keep = _config(nchains, SFH_HMC_DIRECT, nsteps, nwarmup, nleap, thin, step0,
                         target_accept, seed)
-    return _run_hmc(models, data, theta0, cfg, keep, keep_draws)
+    return _run_hmc(models, data, theta0, cfg, keep, keep_draws, sampler, max_depth, minv_dense)
 
 
 def sample_sfh(models: Models, data, logAge, MH, mzr=None, disp: GaussianDispersion = None,
                mstars0=None, nsteps=1000, nchains=1, nwarmup=200, nleap=10, step0=0.01,
                target_accept=0.8, seed=20261203, keep_draws=False, thin=1, jitter=0.05,
-               fit=None):
+               fit=None, sampler="hmc", max_depth=10):
     """Posterior sampling of (R_j, α, β, σ) under a PowerLawMZR, LinearAMR or
     LogarithmicAMR metallicity model with GaussianDispersion (sample_sfh,
     generic_fitting.jl:458-527), all chains in lock step.  Means are reported on the
     natural scale in the order [R_j..., α, β, σ] (free parameters only).
 
-    With fit (the CompositeBFGSResult of fit_sfh), the chains start around the MAP point
-    (spread by `jitter` standard deviations of its inverse Hessian) with the diagonal of
-    that inverse Hessian as the starting metric, as the reference starts its sampler from
-    the MAP fit and its covariance (:458-470); mzr, disp and mstars0 then come from the
-    MAP result."""
+    With fit (the CompositeBFGSResult of fit_sfh) and sampler "nuts", the run is the
+    reference's: every chain starts at the MLE point and the MAP inverse Hessian is the
+    dense metric (:470-490; the reference also keeps its step ϵ = 0.05 with no warmup, i.e.
+    step0=0.05, nwarmup=0).  With fit and sampler "hmc", the chains start around the MAP
+    point (spread by `jitter` standard deviations of its inverse Hessian) with the diagonal
+    of that inverse Hessian as the starting metric.  mzr, disp and mstars0 then come from
+    the fit.  sampler "nuts" adds "depth" and "divergent" to the result."""
     rng = np.random.default_rng(seed)
     minv0 = None
-    if fit is not None:
+    minv_dense = None
+    if fit is not None and sampler == "nuts":
+        # the reference's sample_sfh: NUTS from the MLE point with the MAP inverse Hessian as
+        # a dense metric (generic_fitting.jl:470-490)
+        mzr, disp = fit.mle.MH_model, fit.mle.disp_model
+        th = np.asarray(fit.mle.theta, float)
+        theta0 = np.repeat(th[None, :], nchains, axis=0)
+        minv_dense = np.asarray(fit.map.invH, float)
+    elif fit is not None:
         mzr, disp = fit.map.MH_model, fit.map.disp_model
         th = np.asarray(fit.map.theta, float)
         sd = np.sqrt(np.clip(np.diag(fit.map.invH), 1e-300, None))
@@ -304,7 +344,7 @@ def sample_sfh(models: Models, data, logAge, MH, mzr=None, disp: GaussianDispers
         d_minv0 = torch.as_tensor(minv0, device=torch.device("cuda", models.ctx.device))
         cfg.d_minv0 = d_minv0.data_ptr()
         keep.append(d_minv0)
-    return _run_hmc(models, data, theta0, cfg, keep, keep_draws)
+    return _run_hmc(models, data, theta0, cfg, keep, keep_draws, sampler, max_depth, minv_dense)
 
 
 # ---------------------------------------------------------------- fit_sfh (device BFGS)

@@ -111,3 +111,28 @@ def test_sample_sfh_starts_from_the_map_fit(sfh):
     assert np.all(np.abs(pm[:nages] - res.map.mu[:nages]) < 4 * res.map.sigma[:nages] + 1e-9)
     assert abs(pm[nages] - res.map.mu[nages]) < 4 * res.map.sigma[nages]
     assert np.mean(out["accept"]) > 0.3
+
+
+def test_sample_sfh_nuts_as_the_reference_runs_it(sfh):
+    """sample_sfh with a fit and sampler "nuts" is the reference's run: every chain starts
+    at the MLE point with the MAP inverse Hessian as a dense metric and a fixed step of
+    0.05 without warmup (generic_fitting.jl:470-490); with step adaptation the same run
+    recovers the fit."""
+    truth = sfh.PowerLawMZR(0.5, -1.0, 6.0)
+    disp = sfh.GaussianDispersion(0.2)
+    M, R, la, mh, data = _problem(sfh, truth, disp, n_stars=1e6)
+    res = sfh.fit_sfh(sfh.PowerLawMZR(0.45, -0.9, 6.0), sfh.GaussianDispersion(0.25),
+                      sfh.Models(M, storage="f64"), data, la, mh, x0=R * 1.2)
+    Hb = sfh.Models(M.astype(np.float32), storage="bf16x2")
+    fixed = sfh.sample_sfh(Hb, data, la, mh, nsteps=20, nchains=16, nwarmup=0, step0=0.05,
+                           fit=res, sampler="nuts")
+    assert np.all(fixed["step"] == 0.05)        # no warmup: the reference's fixed step
+    # with step adaptation around the same dense metric
+    out = sfh.sample_sfh(Hb, data, la, mh, nsteps=200, nchains=64, nwarmup=150, step0=0.05,
+                         fit=res, sampler="nuts")
+    pm = out["mean"].mean(0)
+    nages = R.size
+    assert np.all(np.abs(pm[:nages] - res.mle.mu[:nages]) < 4 * res.map.sigma[:nages] + 1e-9)
+    assert abs(pm[nages] - res.mle.mu[nages]) < 4 * res.map.sigma[nages]
+    assert np.mean(out["accept"]) > 0.6, np.mean(out["accept"])
+    assert np.mean(out["divergent"]) < 1.0

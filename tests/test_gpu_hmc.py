@@ -208,3 +208,114 @@ def test_log_amr_logdensity_matches_oracle(sfh, O):
         ref_g = np.concatenate([-Gv[:na] * v[:na] + 1.0, -Gv[na:] * v[na:] + 1.0])
         assert abs(logd[k] - ref_logd) <= 1e-2 * max(1.0, data.sum() / 1e4), (logd[k], ref_logd)
         np.testing.assert_allclose(grad[k], ref_g, rtol=2e-3, atol=2e-3 * np.abs(ref_g).max())
+
+
+def test_nuts_direct_matches_laplace_posterior(sfh):
+    """The No-U-Turn sampler on hmc_sample's log density: the same Laplace check as the
+    fixed-length sampler, trees that stop by turning (no divergences, depth below the
+    limit) and per-chain trees that end at different times."""
+    rng = np.random.default_rng(21)
+    nbins, nt = 4000, 4
+    M32 = np.asfortranarray((rng.random((nbins, nt)) ** 3).astype(np.float32))
+    x_true = np.array([2000.0, 1000.0, 3000.0, 500.0]) / 100
+    data = rng.poisson(M32.astype(np.float64) @ x_true).astype(np.float64)
+    Ms = np.asfortranarray(_bf16_hilo(M32))
+    _, mle = sfh.fit_templates_lbfgsb(sfh.Models(Ms, storage="f64"), data, x0=x_true,
+                                      factr=10.0, pgtol=1e-10)
+    m = Ms @ mle
+    Hobs = (Ms * (data / m ** 2)[:, None]).T @ Ms
+    sd_lap = np.sqrt(np.diag(np.linalg.inv(Hobs)))
+    H = sfh.Models(M32, storage="bf16x2")
+    out = sfh.hmc_sample(H, data, nsteps=400, nchains=64, nwarmup=300, seed=5, sampler="nuts",
+                         max_depth=10)
+    pm = out["mean"].mean(axis=0)
+    pv = out["var"].mean(axis=0) + out["mean"].var(axis=0)
+    assert 0.6 < out["accept"].mean() < 0.99, out["accept"].mean()
+    assert np.all(out["divergent"] == 0)
+    assert 0.5 < out["depth"].mean() < 9.0, out["depth"].mean()
+    assert np.all(np.abs(pm - mle) < 0.25 * sd_lap + 3 * np.sqrt(pv / (64 * 100))), (pm, mle, sd_lap)
+    ratio = np.sqrt(pv) / sd_lap
+    assert np.all((ratio > 0.8) & (ratio < 1.25)), ratio
+
+
+def test_nuts_mzr_recovers_parameters_and_draws_are_kept(sfh):
+    la, mh, M32, R, mzr, disp, data = _mzr_problem(seed=8, nbins=6000, scale=5.0)
+    H = sfh.Models(M32, storage="bf16x2")
+    from sfhgpu.sampling import GaussianDispersion, PowerLawMZR
+    out = sfh.sample_sfh(H, data, la, mh, PowerLawMZR(0.4, -0.8, 6.0), GaussianDispersion(0.3),
+                         R * 1.1, nsteps=300, nchains=32, nwarmup=300, seed=9, sampler="nuts",
+                         keep_draws=True, thin=3)
+    na = R.size
+    pm = out["mean"].mean(axis=0)
+    psd = np.sqrt(out["var"].mean(axis=0) + out["mean"].var(axis=0))
+    truth = np.concatenate([R, [0.5, -1.0, 0.2]])
+    assert 0.5 < out["accept"].mean() < 0.995, out["accept"].mean()
+    z = np.abs(pm - truth) / psd
+    assert np.all(z[na:] < 4.0), (pm[na:], psd[na:])
+    assert np.median(z[:na]) < 3.0, z[:na]
+    dr = out["draws"]
+    assert dr.shape == (32, 100, na + 3) and np.all(np.isfinite(dr))
+    # the kept draws' means agree with the running means up to the thinning
+    assert np.all(np.abs(dr.mean(axis=1).mean(0) - pm) < 0.5 * psd)
+
+
+def test_nuts_is_reproducible(sfh):
+    rng = np.random.default_rng(4)
+    M32 = np.asfortranarray((rng.random((2000, 3)) ** 2).astype(np.float32))
+    data = rng.poisson(M32.astype(np.float64) @ np.array([30.0, 20.0, 10.0])).astype(float)
+    H = sfh.Models(M32, storage="bf16x2")
+    a = sfh.hmc_sample(H, data, nsteps=50, nchains=8, nwarmup=50, seed=7, sampler="nuts")
+    b = sfh.hmc_sample(H, data, nsteps=50, nchains=8, nwarmup=50, seed=7, sampler="nuts")
+    assert np.array_equal(a["mean"], b["mean"]) and np.array_equal(a["depth"], b["depth"])
+
+
+@pytest.mark.parametrize("sampler", ["hmc", "nuts"])
+def test_single_chain_runs_on_the_plain_path(sfh, sampler):
+    """One chain evaluates the single-vector fg! (no batch for the tensor cores): its
+    posterior agrees with the 16-chain run on the batched path."""
+    la, mh, M32, R, mzr, disp, data = _mzr_problem(seed=8, nbins=6000, scale=5.0)
+    from sfhgpu.sampling import GaussianDispersion, PowerLawMZR
+    res = {}
+    for nch, steps in ((1, 1500), (16, 200)):
+        H = sfh.Models(M32, storage="bf16x2")
+        res[nch] = sfh.sample_sfh(H, data, la, mh, PowerLawMZR(0.4, -0.8, 6.0),
+                                  GaussianDispersion(0.3), R * 1.1, nsteps=steps, nchains=nch,
+                                  nwarmup=300, nleap=10, seed=9, sampler=sampler)
+    one, many = res[1], res[16]
+    na = R.size
+    pm1 = one["mean"][0]
+    pm = many["mean"].mean(axis=0)
+    psd = np.sqrt(many["var"].mean(axis=0) + many["mean"].var(axis=0))
+    assert 0.4 < one["accept"][0] < 0.999
+    # hyperparameters within 4 posterior sd of the many-chain mean
+    assert np.all(np.abs(pm1[na:] - pm[na:]) < 4 * psd[na:]), (pm1[na:], pm[na:], psd[na:])
+
+
+def test_nuts_dense_metric_on_the_laplace_covariance(sfh):
+    """A dense metric equal to the Laplace covariance of θ = log x whitens the posterior:
+    a fixed step of 0.3 without warmup gives high acceptance, short trees and the Laplace
+    moments."""
+    rng = np.random.default_rng(21)
+    nbins, nt = 4000, 4
+    M32 = np.asfortranarray((rng.random((nbins, nt)) ** 3).astype(np.float32))
+    x_true = np.array([2000.0, 1000.0, 3000.0, 500.0]) / 100
+    data = rng.poisson(M32.astype(np.float64) @ x_true).astype(np.float64)
+    Ms = np.asfortranarray(_bf16_hilo(M32))
+    _, mle = sfh.fit_templates_lbfgsb(sfh.Models(Ms, storage="f64"), data, x0=x_true,
+                                      factr=10.0, pgtol=1e-10)
+    m = Ms @ mle
+    Hobs = (Ms * (data / m ** 2)[:, None]).T @ Ms
+    cov_x = np.linalg.inv(Hobs)
+    cov_th = cov_x / np.outer(mle, mle)  # θ = log x
+    H = sfh.Models(M32, storage="bf16x2")
+    theta0 = np.repeat(np.log(mle)[None, :], 64, axis=0)
+    out = sfh.hmc_sample(H, data, nsteps=400, nchains=64, nwarmup=0, step0=0.3, seed=8,
+                         sampler="nuts", theta0=theta0, minv_dense=cov_th)
+    assert out["accept"].mean() > 0.85, out["accept"].mean()
+    assert np.all(out["divergent"] == 0) and out["depth"].mean() < 4.0, out["depth"].mean()
+    pm = out["mean"].mean(axis=0)
+    pv = out["var"].mean(axis=0) + out["mean"].var(axis=0)
+    sd_lap = np.sqrt(np.diag(cov_x))
+    assert np.all(np.abs(pm - mle) < 0.25 * sd_lap + 3 * np.sqrt(pv / (64 * 100))), (pm, mle)
+    ratio = np.sqrt(pv) / sd_lap
+    assert np.all((ratio > 0.8) & (ratio < 1.25)), ratio
