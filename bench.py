@@ -259,15 +259,20 @@ def run_hmc(ctx, d_T, w, nchains=1024, nwarmup=500, ntraj=1500, nleap=10, seed=2
     }
 
 
-def run_hmc_matched(ctx, d_T, w, nchains=1024, nwarmup=100, ndraw=20, nref=200,
+def run_hmc_matched(ctx, d_T, w, nchains=1024, nwarmup=200, ndraw=10, nref=200,
                     seed=20261207):
-    """The batched No-U-Turn sampler against the plain single-chain path at matched
-    posterior-mean error, measured on the config-5 model (PowerLawMZR + GaussianDispersion,
-    1,200 templates): a reference posterior mean from a long batched run; then the batched
-    run (nchains x ndraw draws after nwarmup) and one chain on the single-vector fg! with
-    the same total number of draws.  Error: RMS over all variables of (mean - reference) /
-    posterior sd.  Since the error of a mean falls as 1/sqrt(draws), the single chain's
-    time at the batched run's error is its time x (e_single / e_batched)^2."""
+    """The batched sampler against the plain single-chain path at matched posterior-mean
+    error, measured on the config-5 model (PowerLawMZR + GaussianDispersion, 1,200
+    templates, trajectories of 10 leapfrog steps).  Every run starts from the device
+    fit_sfh MAP point with its inverse-Hessian diagonal as the starting metric, as
+    sample_sfh(fit=...) does.  A reference posterior mean comes from a long batched run;
+    then the batched run (nchains x ndraw draws after nwarmup) and one chain on the
+    single-vector fg! with the same total number of draws.  Error: RMS over all variables
+    of (mean - reference) / posterior sd.  Since the error of a mean falls as
+    1/sqrt(draws), the single chain's time at the batched run's error is its time x
+    (e_single / e_batched)^2.  Then the No-U-Turn sampler as the reference's sample_sfh
+    runs it (the MLE point, the MAP inverse Hessian as a dense metric), timed on the
+    same chains."""
     import numpy as np
     import torch
 
@@ -284,50 +289,61 @@ def run_hmc_matched(ctx, d_T, w, nchains=1024, nwarmup=100, ndraw=20, nref=200,
     c = calculate_coeffs(mzr, disp, R, la, mh)
     data = rng.poisson((M.T @ torch.as_tensor(c, device=M.device)).cpu().numpy()).astype(float)
     del M
-
-    # every run starts from the MAP fit with its inverse-Hessian diagonal as the metric, as
-    # the reference starts its sampler (generic_fitting.jl:458-470)
     Hf = sfhgpu.Models.from_device(d_T.data_ptr(), w.nbins, w.ntempl, storage="f32", ctx=ctx)
     t0 = time.perf_counter()
     fit = sfhgpu.fit_sfh(PowerLawMZR(0.45, -0.9, 6.0), GaussianDispersion(0.25), Hf, data, la, mh,
-                         x0=R * 1.1, g_abstol=1e-3)
+                         x0=R * 1.1)
     t_fit = time.perf_counter() - t0
+    print(f"[hmc] fit {t_fit:.2f} s, MAP status {fit.map.result['status']}, "
+          f"{fit.map.result['iterations']} iterations, |g| {fit.map.result['g_norm']:.2e}",
+          file=sys.stderr, flush=True)
     Hf.free()
 
-    def run(nch, nsteps, sd):
+    def run(nch, nsteps, sd, sampler="hmc", nw=nwarmup, **kw):
         torch.cuda.synchronize()
+        l0 = ctx.launches
         t0 = time.perf_counter()
-        out = sfhgpu.sample_sfh(Hb, data, la, mh, nsteps=nsteps, nchains=nch, nwarmup=nwarmup,
-                                step0=0.05, seed=sd, sampler="nuts", fit=fit)
+        out = sfhgpu.sample_sfh(Hb, data, la, mh, nsteps=nsteps, nchains=nch, nwarmup=nw,
+                                nleap=10, step0=0.05, seed=sd, fit=fit, sampler=sampler, **kw)
         torch.cuda.synchronize()
-        return out, time.perf_counter() - t0
+        dt = time.perf_counter() - t0
+        out["launches"] = ctx.launches - l0
+        print(f"[hmc] {sampler} {nch} chains x {nsteps} draws: {dt:.2f} s, accept "
+              f"{out['accept'].mean():.3f}", file=sys.stderr, flush=True)
+        return out, dt
 
     ref, t_ref = run(nchains, nref, seed + 1)
     mref = ref["mean"].mean(0)
     sdref = np.sqrt(ref["var"].mean(0) + ref["mean"].var(0))
     bat, t_bat = run(nchains, ndraw, seed + 2)
     one, t_one = run(1, nchains * ndraw, seed + 3)
+    nuts, t_nuts = run(nchains, 50, seed + 4, sampler="nuts", nw=50, max_depth=8)
     Hb.free()
     err = lambda mu: float(np.sqrt(np.mean(((mu - mref) / sdref) ** 2)))
     e_b, e_1 = err(bat["mean"].mean(0)), err(one["mean"][0])
     t_match = t_one * (e_1 / e_b) ** 2
     return {
-        "workload": f"NUTS (max depth 10), PowerLawMZR + GaussianDispersion over {w.ntempl} "
-                    f"templates x {w.nbins} bins, as the reference's sample_sfh runs it: from "
-                    "the device fit_sfh MLE point, the MAP inverse Hessian as a dense metric, "
-                    f"step 0.05 then {nwarmup} warmup trees of step adaptation per chain",
+        "workload": f"PowerLawMZR + GaussianDispersion over {w.ntempl} templates x {w.nbins} "
+                    f"bins; trajectories of 10 leapfrog steps, {nwarmup} warmup trajectories "
+                    "per chain; every run starts from the device fit_sfh MAP point",
         "map_fit_seconds": t_fit,
+        "map_fit": {k: fit.map.result[k] for k in ("status", "iterations", "g_norm")},
         "reference": {"chains": nchains, "draws_per_chain": nref, "seconds": t_ref},
         "batched": {"chains": nchains, "draws_per_chain": ndraw, "seconds": t_bat,
-                    "error": e_b, "mean_depth": float(bat["depth"].mean()),
-                    "accept": float(bat["accept"].mean()),
-                    "divergent": int(bat["divergent"].sum())},
+                    "error": e_b, "accept": float(bat["accept"].mean())},
         "single_chain_plain": {"draws": nchains * ndraw, "seconds": t_one, "error": e_1,
-                               "mean_depth": float(one["depth"].mean()),
                                "accept": float(one["accept"].mean())},
         "single_chain_seconds_at_batched_error": t_match,
         "speedup_at_matched_error": t_match / t_bat,
         "error": "RMS over the 43 variables of (posterior mean - reference) / posterior sd",
+        "nuts": {"chains": nchains, "warmup_trees": 50, "draws_per_chain": 50,
+                 "max_depth": 8, "seconds": t_nuts,
+                 "trees_per_s": nchains * 100 / t_nuts,
+                 "mean_depth": float(nuts["depth"].mean()),
+                 "accept": float(nuts["accept"].mean()),
+                 "divergent": int(nuts["divergent"].sum()),
+                 "metric": "dense: the MAP inverse Hessian, from the MLE point (the "
+                           "reference's sample_sfh); the step adapted over the warmup trees"},
     }
 
 
@@ -1042,7 +1058,7 @@ def run_ours(args):
                       ntraj=args.hmc_traj)
         hmc["speedup_vs_plain_evals"] = hmc["chain_gradient_evals_per_s"] / value
         if args.hmc_traj >= 100:  # not in short profiling runs
-            hmc["nuts_matched_error"] = run_hmc_matched(ctx, d_T, w, nchains=args.hmc_chains)
+            hmc["matched_error"] = run_hmc_matched(ctx, d_T, w, nchains=args.hmc_chains)
         em = getattr(run_emulator, "last", None)
         if em is not None:
             # the same fit on emulated templates (exact where the trust map says so)

@@ -190,7 +190,9 @@ __global__ void k_accept(ChainState s, HmcConst c) {
 // averaging around the current step sizes.
 __global__ void k_adapt_mass(ChainState s, HmcConst c) {
     const int64_t t = *s.t;
-    if (c.nwarm < 20 || t != c.nwarm / 2) return;
+    // the pooled variance needs chains to pool over: with fewer than 16 the starting
+    // metric (ones, or cfg->d_minv0) is kept and only the step adapts
+    if (c.nwarm < 20 || t != c.nwarm / 2 || c.B < 16) return;
     const int d = blockIdx.x * blockDim.x + threadIdx.x;
     if (d < c.D) {
         double m = 0.0, q = 0.0;

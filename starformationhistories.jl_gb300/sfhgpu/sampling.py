@@ -303,7 +303,7 @@ def hmc_sample(models: Models, data, nsteps, nchains=1, nwarmup=200, nleap=10, s
 def sample_sfh(models: Models, data, logAge, MH, mzr=None, disp: GaussianDispersion = None,
                mstars0=None, nsteps=1000, nchains=1, nwarmup=200, nleap=10, step0=0.01,
                target_accept=0.8, seed=20261203, keep_draws=False, thin=1, jitter=0.05,
-               fit=None, sampler="hmc", max_depth=10):
+               fit=None, sampler="hmc", max_depth=10, minv_dense=None):
     """Posterior sampling of (R_j, α, β, σ) under a PowerLawMZR, LinearAMR or
     LogarithmicAMR metallicity model with GaussianDispersion (sample_sfh,
     generic_fitting.jl:458-527), all chains in lock step.  Means are reported on the
@@ -315,17 +315,18 @@ def sample_sfh(models: Models, data, logAge, MH, mzr=None, disp: GaussianDispers
     step0=0.05, nwarmup=0).  With fit and sampler "hmc", the chains start around the MAP
     point (spread by `jitter` standard deviations of its inverse Hessian) with the diagonal
     of that inverse Hessian as the starting metric.  mzr, disp and mstars0 then come from
-    the fit.  sampler "nuts" adds "depth" and "divergent" to the result."""
+    the fit.  sampler "nuts" adds "depth" and "divergent" to the result; minv_dense (D x D)
+    replaces the MAP inverse Hessian as its dense metric."""
     rng = np.random.default_rng(seed)
     minv0 = None
-    minv_dense = None
     if fit is not None and sampler == "nuts":
         # the reference's sample_sfh: NUTS from the MLE point with the MAP inverse Hessian as
         # a dense metric (generic_fitting.jl:470-490)
         mzr, disp = fit.mle.MH_model, fit.mle.disp_model
         th = np.asarray(fit.mle.theta, float)
         theta0 = np.repeat(th[None, :], nchains, axis=0)
-        minv_dense = np.asarray(fit.map.invH, float)
+        if minv_dense is None:
+            minv_dense = np.asarray(fit.map.invH, float)
     elif fit is not None:
         mzr, disp = fit.map.MH_model, fit.map.disp_model
         th = np.asarray(fit.map.theta, float)
