@@ -435,59 +435,115 @@ def run_ragged(ctx, steps=50, warmup=5, check=2):
     }
 
 
-def run_emulator(ctx, w, n_train=100_000, n_val=4096, steps=20000, cells=(8, 2, 16), nreq=1200):
-    """Learned template emulator on the production grid: per-cell PCA bases (64
-    components of sqrt templates) and per-cell MLPs 3-256-256-64 trained on templates the
-    GPU partial_cmd_smooth generates at random (log age, [M/H], distance modulus); scored
-    by Poisson deviance per star against exact templates (tolerance 1e-3)."""
+def run_emulator(ctx, w, n_train=150_000, n_val=8192, steps=60000, cells=(32, 4, 1),
+                 trust_cells=None, nreq=1200):
+    """Learned template emulator for one galaxy at a known distance: theta = (log age,
+    [M/H]) over the whole production grid's box with the distance modulus within 0.05 mag
+    of the galaxy's.  Per-cell PCA bases (64 components of sqrt templates) and per-cell MLPs
+    3-256-256-64 trained on templates the GPU partial_cmd_smooth generates at random; a
+    trust map (on the basis cells unless trust_cells is given) keeps each cell's worst
+    validation deviance.  Scored
+    by Poisson deviance per star against exact templates (tolerance 1e-3) on the 1,200
+    templates of the production grid (the requests a fit of that galaxy makes) and on
+    random requests; routed = emulated where trusted, exact elsewhere."""
     import numpy as np
     import torch
 
-    from sfhgpu.emulator import SyntheticGenerator, TemplateEmulator
+    from sfhgpu.emulator import SyntheticGenerator, TemplateEmulator, group_segments
     gen = SyntheticGenerator(w.xedges, w.yedges, ctx=ctx)
-    em = TemplateEmulator(gen.nbins, ncomp=64, hidden=(256, 256), tol=1e-3, basis_cells=cells,
-                          ctx=ctx)
+    bounds = ((6.6, 10.1), (-2.5, 0.3), (w.dmod - 0.05, w.dmod + 0.05))
+    em = TemplateEmulator(gen.nbins, ncomp=64, hidden=(256, 256), tol=1e-3, bounds=bounds,
+                          basis_cells=cells, trust_cells=trust_cells, ctx=ctx)
     t0 = time.perf_counter()
     rep = em.fit(gen, n_train=n_train, n_val=n_val, steps=steps, lr=1e-3, batch_per_cell=32)
     fit_s = time.perf_counter() - t0
-    th = em.sample_theta(nreq, np.random.default_rng(5))
-    em.predict(th)
+    la, mh = w.template_params
+    th_grid = np.stack([la, mh, np.full(la.size, w.dmod)], 1)
+    th_rand = em.sample_theta(nreq, np.random.default_rng(5))
+
+    def timed(f, reps=5):
+        f()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            r = f()
+        torch.cuda.synchronize()
+        return r, (time.perf_counter() - t0) / reps
+
+    out = {}
+    for name, th in (("grid", th_grid), ("random", th_rand)):
+        exact, t_exact = timed(lambda: gen(th), reps=2)
+        emul, t_emul = timed(lambda: em.predict(th))
+        dev = em.score(exact, emul)
+        trusted = em.trusted(th)
+        (routed, used), t_routed = timed(lambda: em.templates(th, gen), reps=2)
+        assert np.array_equal(used, trusted)
+        dr = em.score(exact, routed)
+        out[name] = {
+            "requests": int(th.shape[0]),
+            "frac_within_1e-3": float(np.mean(dev <= 1e-3)),
+            "frac_within_1e-2": float(np.mean(dev <= 1e-2)),
+            "deviance_median": float(np.median(dev)),
+            "trusted_frac": float(np.mean(trusted)),
+            "trusted_within_1e-3": float(np.mean(dev[trusted] <= 1e-3)) if trusted.any() else None,
+            "routed_deviance_max": float(dr.max()),
+            "emulated_templates_per_s": th.shape[0] / t_emul,
+            "exact_templates_per_s": th.shape[0] / t_exact,
+            "routed_templates_per_s": th.shape[0] / t_routed,
+            "routed_speedup_vs_exact": t_exact / t_routed,
+        }
+        del exact, emul, routed
+
+    # the reconstruction kernel alone (cell segments; each segment reads its cell's basis once)
+    coef = em.coefficients(th_grid)
+    rows, seg = group_segments(em.group_of(th_grid))
+    d_rows = torch.as_tensor(rows, device=coef.device)
+    d_seg = torch.as_tensor(seg, device=coef.device)
+    B = th_grid.shape[0]
+    buf = torch.empty((B, em.nbins), dtype=torch.float32, device=coef.device)
+    import sfhgpu
+    L = sfhgpu.load()
+    peak, peak_src = _peaks()
+    s = ctx.torch_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def recon():
+        L.sfh_emu_reconstruct_groups(ctx.handle, coef.data_ptr(), d_rows.data_ptr(),
+                                     d_seg.data_ptr(), seg.shape[0], em.ngroups,
+                                     em.basis.data_ptr(), em.offset.data_ptr(), em.K, em.nbins,
+                                     B, em.mode, buf.data_ptr())
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    exact = gen(th)
+    for _ in range(3):
+        recon()
+    e0.record(s)
+    for _ in range(20):
+        recon()
+    e1.record(s)
     torch.cuda.synchronize()
-    t_exact = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    emul = em.predict(th)
-    torch.cuda.synchronize()
-    t_emul = time.perf_counter() - t0
-    dev = em.score(exact, emul)
-    trusted = em.trusted(th)
-    em.templates(th[:8], gen)  # first use of the routing path (indexed copy kernel)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    em.templates(th, gen)  # trust-map routing: emulated where validated, exact elsewhere
-    torch.cuda.synchronize()
-    t_routed = time.perf_counter() - t0
+    t_rec = e0.elapsed_time(e1) / 20 * 1e-3
+    rec_bytes = 4.0 * em.nbins * (seg.shape[0] * (em.K + 1) + B)
     run_emulator.last = em
     return {
-        "workload": f"{n_train} training templates on the 200x300 grid, theta = (log age "
-                    f"U[6.6,10.1], [M/H] U[-2.5,0.3], dmod U[24,30]); {int(np.prod(cells))} "
-                    f"cells {cells}, PCA 64 of sqrt templates, MLP 3-256-256-64 per cell; "
-                    f"{nreq} fresh requests",
+        "workload": f"one galaxy at distance modulus {w.dmod} (+-0.05): {n_train} training "
+                    f"templates on the 200x300 grid, theta = (log age U[6.6,10.1], [M/H] "
+                    f"U[-2.5,0.3], dmod); {int(np.prod(cells))} basis cells {cells}, PCA 64 of "
+                    f"sqrt templates, MLP 3-256-256-64 per cell trained for {steps} steps; "
+                    f"trust map on {trust_cells or cells} cells from {n_val} validation "
+                    f"templates; requests: the {B} templates of "
+                    f"the production grid and {nreq} random theta",
         "fit_seconds": fit_s, "generate_seconds": rep.generate_seconds,
         "pca_seconds": rep.pca_seconds, "train_seconds": rep.train_seconds,
         "final_loss": rep.final_loss, "val_deviance_quantiles": rep.val_deviance_quantiles,
         "val_frac_within_1e-3": rep.val_frac_within_tol,
-        "requests_frac_within_1e-3": float(np.mean(dev <= 1e-3)),
-        "requests_deviance_median": float(np.median(dev)),
-        "trusted_frac": float(np.mean(trusted)),
-        # the trust map keeps each cell's worst validation deviance, so the fraction that
-        # would be routed to the emulator at a looser tolerance follows directly
-        "trusted_frac_at_tol_1e-2": float(np.mean(em.trust[em._cell(th)[0]] <= 1e-2)),
-        "emulated_templates_per_s": nreq / t_emul, "exact_templates_per_s": nreq / t_exact,
-        "routed_templates_per_s": nreq / t_routed,
-        "routed_speedup_vs_exact": t_exact / t_routed,
+        "trusted_cell_fraction": rep.trusted_cell_fraction,
+        "grid_requests": out["grid"], "random_requests": out["random"],
+        "reconstruct_roofline": {
+            "kernel": "k_recon_groups", "bound": "hbm", "segments": int(seg.shape[0]),
+            "ms": t_rec * 1e3, "achieved": rec_bytes / t_rec / 1e9,
+            "peak": peak, "peak_source": peak_src, "unit": "GB/s",
+            "frac": rec_bytes / t_rec / 1e9 / peak,
+            "bytes": "4 nbins (segments (K + 1) + B): each segment's basis and offset read "
+                     "once, every template written once"},
     }
 
 
@@ -1049,7 +1105,7 @@ def run_ours(args):
     # ---- learned template emulator (production grid), scored against exact templates
     emulator = None
     if not args.no_emulator:
-        emulator = run_emulator(ctx, w)
+        emulator = run_emulator(ctx, w, n_train=args.emu_train, steps=args.emu_steps)
 
     # ---- end-to-end hierarchical HMC (1,024 chains, MZR) on the same templates
     hmc = None
@@ -1142,6 +1198,9 @@ def main():
                          "(for profiling runs, where profiler overhead can change the choice)")
     ap.add_argument("--no-emulator", action="store_true", help="skip the emulator leg")
     ap.add_argument("--no-fit", action="store_true", help="skip the whole-fit leg")
+    ap.add_argument("--emu-train", type=int, default=150_000,
+                    help="emulator training templates (smaller for a profiling case)")
+    ap.add_argument("--emu-steps", type=int, default=60_000, help="emulator training steps")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the binary_hess / bin_cmd / model_cmd leg")
     ap.add_argument("--onepass-variant", default="",

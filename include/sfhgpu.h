@@ -633,6 +633,16 @@ int sfh_mlp_forward_rows(sfh_ctx *ctx, int in, int h1, int h2, int out, const fl
 int sfh_emu_reconstruct_rows(sfh_ctx *ctx, const float *d_coef, const int32_t *d_group,
                              int64_t ngroups, const float *d_basis, const float *d_offset, int K,
                              int64_t nbins, int64_t B, int mode, float *d_out);
+/* As sfh_emu_reconstruct_rows, one group's rows at a time: segment s (d_seg[3s..3s+2] =
+   group, start, count; 1 <= count <= 16) builds rows d_rows[start .. start + count) from
+   group `group`'s basis, read once for the whole segment.  d_rows holds row indices of d_out
+   (0 <= row < B), normally sorted by group.  nseg <= 65535, K <= 1024.  A segment with an
+   out-of-range group or rows writes NaN to the rows it can address.  Enqueued, not
+   synchronised. */
+int sfh_emu_reconstruct_groups(sfh_ctx *ctx, const float *d_coef, const int32_t *d_rows,
+                               const int32_t *d_seg, int64_t nseg, int64_t ngroups,
+                               const float *d_basis, const float *d_offset, int K,
+                               int64_t nbins, int64_t B, int mode, float *d_out);
 /* d_C (M x N) = alpha op(A) op(B) (+ d_C when accum), FP32 accumulation, ta / tb select
    row-major A (M x K) / (K x M) and B (K x N) / (N x K); bf16 != 0 rounds the operands to
    BF16 first.  Used for the PCA basis (randomized range finder) and projections. */

@@ -330,6 +330,123 @@ __global__ void k_recon_rows(const float *__restrict__ coef, const int32_t *__re
     out[b * nbins + i] = mode == 1 ? y * y : y;
 }
 
+// Templates of one group's rows at a time: a segment (group g, rows d_rows[start .. start +
+// count), count <= kRecRows) reads its group's basis once for all of its rows, so a batch
+// costs (segments x K x nbins + B x nbins) x 4 bytes instead of B x K x nbins x 4.  Each
+// thread owns V consecutive bins and R row accumulators; R is the segment's row count
+// rounded up to 4, 8 or 16 (block-uniform).  Coefficients of the segment sit in shared
+// memory, zero past count.
+constexpr int kRecRows = 16;
+constexpr int kRecThreads = 256;
+
+template <int R, int V>
+__device__ __forceinline__ void recon_segment(const float *__restrict__ sc, int K,
+                                              const float *__restrict__ vb,
+                                              const float *__restrict__ off, int64_t nbins,
+                                              int64_t i0, const int32_t *__restrict__ srow,
+                                              int cnt, int mode, float *__restrict__ out) {
+    float acc[R][V];
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc[r][v] = 0.f;
+    if (V == 4) {
+        for (int k = 0; k < K; ++k) {
+            const float4 b = __ldg(reinterpret_cast<const float4 *>(vb + (int64_t)k * nbins + i0));
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const float c = sc[r * K + k];
+                acc[r][0] = fmaf(c, b.x, acc[r][0]);
+                acc[r][1] = fmaf(c, b.y, acc[r][1]);
+                acc[r][2] = fmaf(c, b.z, acc[r][2]);
+                acc[r][3] = fmaf(c, b.w, acc[r][3]);
+            }
+        }
+    } else {
+        for (int k = 0; k < K; ++k) {
+            float b[V];
+#pragma unroll
+            for (int v = 0; v < V; ++v)
+                b[v] = i0 + v < nbins ? __ldg(vb + (int64_t)k * nbins + i0 + v) : 0.f;
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const float c = sc[r * K + k];
+#pragma unroll
+                for (int v = 0; v < V; ++v) acc[r][v] = fmaf(c, b[v], acc[r][v]);
+            }
+        }
+    }
+    float o[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) o[v] = i0 + v < nbins ? __ldg(off + i0 + v) : 0.f;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        if (r >= cnt) break;
+        float *dst = out + (int64_t)srow[r] * nbins + i0;
+        float y[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const float t = fmaxf(acc[r][v] + o[v], 0.f);
+            y[v] = mode == 1 ? t * t : t;
+        }
+        if (V == 4) {
+            *reinterpret_cast<float4 *>(dst) = make_float4(y[0], y[1], y[2], y[3]);
+        } else {
+#pragma unroll
+            for (int v = 0; v < V; ++v)
+                if (i0 + v < nbins) dst[v] = y[v];
+        }
+    }
+}
+
+// seg: nseg x 3 int32 (group, start, count).  A segment whose group is out of range or whose
+// rows fall outside [0, B) writes NaN to the rows it can address and nothing else.
+template <int V>
+__global__ void __launch_bounds__(kRecThreads)
+k_recon_groups(const float *__restrict__ coef, const int32_t *__restrict__ rows,
+               const int32_t *__restrict__ seg, int64_t B, int64_t ngroups,
+               const float *__restrict__ basis, const float *__restrict__ offset, int K,
+               int64_t nbins, int mode, float *__restrict__ out) {
+    extern __shared__ float sc[];  // kRecRows x K
+    __shared__ int32_t srow[kRecRows];
+    const int s = blockIdx.y;
+    const int g = seg[3 * s], start = seg[3 * s + 1];
+    int cnt = seg[3 * s + 2];
+    const bool bad = g < 0 || g >= ngroups || start < 0 || cnt < 1 || cnt > kRecRows ||
+                     (int64_t)start + cnt > B;
+    if (threadIdx.x < kRecRows) {
+        int32_t r = -1;
+        if (start >= 0 && (int64_t)start + threadIdx.x < B && (int)threadIdx.x < cnt)
+            r = rows[start + threadIdx.x];
+        srow[threadIdx.x] = (r >= 0 && r < B) ? r : -1;
+    }
+    __syncthreads();
+    const int64_t i0 = ((int64_t)blockIdx.x * kRecThreads + threadIdx.x) * V;
+    if (bad) {
+        for (int r = 0; r < kRecRows; ++r)
+            if (srow[r] >= 0 && i0 < nbins)
+                for (int v = 0; v < V && i0 + v < nbins; ++v)
+                    out[(int64_t)srow[r] * nbins + i0 + v] = __int_as_float(0x7fc00000);
+        return;
+    }
+    for (int r = 0; r < kRecRows; ++r)
+        if (srow[r] < 0 && r < cnt) cnt = r;  // a row index out of range ends the segment
+    for (int t = threadIdx.x; t < kRecRows * K; t += kRecThreads) {
+        const int r = t / K;
+        sc[t] = r < cnt ? coef[(int64_t)srow[r] * K + (t - r * K)] : 0.f;
+    }
+    __syncthreads();
+    if (i0 >= nbins) return;
+    const float *vb = basis + (int64_t)g * K * nbins;
+    const float *off = offset + (int64_t)g * nbins;
+    if (cnt <= 4)
+        recon_segment<4, V>(sc, K, vb, off, nbins, i0, srow, cnt, mode, out);
+    else if (cnt <= 8)
+        recon_segment<8, V>(sc, K, vb, off, nbins, i0, srow, cnt, mode, out);
+    else
+        recon_segment<16, V>(sc, K, vb, off, nbins, i0, srow, cnt, mode, out);
+}
+
 struct Acts {  // activations of one batch (G groups x B rows)
     float *Z1, *A1, *Z2, *A2, *Y;
 };
@@ -642,6 +759,41 @@ extern "C" int sfh_emu_reconstruct_rows(sfh_ctx *ctx, const float *d_coef, const
     dim3 grid((unsigned)((nbins + 255) / 256), (unsigned)B);
     k_recon_rows<<<grid, 256, (size_t)K * sizeof(float), ctx->stream>>>(
         d_coef, d_group, ngroups, d_basis, d_offset, K, nbins, mode, d_out);
+    SFH_LAUNCHED(ctx);
+    return SFH_OK;
+}
+
+extern "C" int sfh_emu_reconstruct_groups(sfh_ctx *ctx, const float *d_coef,
+                                          const int32_t *d_rows, const int32_t *d_seg,
+                                          int64_t nseg, int64_t ngroups, const float *d_basis,
+                                          const float *d_offset, int K, int64_t nbins, int64_t B,
+                                          int mode, float *d_out) {
+    if (!ctx || !d_coef || !d_rows || !d_seg || !d_basis || !d_offset || !d_out || K < 1 ||
+        K > 1024 || nbins < 1 || B < 1 || B > INT32_MAX || nseg < 1 || nseg > 65535 ||
+        ngroups < 1 || (mode != 0 && mode != 1))
+        return SFH_ERR_ARG;
+    SFH_CK(ctx, cudaSetDevice(ctx->device));
+    const size_t shm = (size_t)kRecRows * K * sizeof(float);
+    // float4 rows need every basis, offset and output row on a 16-byte boundary
+    const bool vec = nbins % 4 == 0 && ((uintptr_t)d_basis | (uintptr_t)d_offset |
+                                        (uintptr_t)d_out) % 16 == 0;
+    if (vec) {
+        if (shm > 48 * 1024)
+            SFH_CK(ctx, cudaFuncSetAttribute(k_recon_groups<4>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)shm));
+        dim3 grid((unsigned)((nbins + 4 * kRecThreads - 1) / (4 * kRecThreads)), (unsigned)nseg);
+        k_recon_groups<4><<<grid, kRecThreads, shm, ctx->stream>>>(
+            d_coef, d_rows, d_seg, B, ngroups, d_basis, d_offset, K, nbins, mode, d_out);
+    } else {
+        if (shm > 48 * 1024)
+            SFH_CK(ctx, cudaFuncSetAttribute(k_recon_groups<1>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)shm));
+        dim3 grid((unsigned)((nbins + kRecThreads - 1) / kRecThreads), (unsigned)nseg);
+        k_recon_groups<1><<<grid, kRecThreads, shm, ctx->stream>>>(
+            d_coef, d_rows, d_seg, B, ngroups, d_basis, d_offset, K, nbins, mode, d_out);
+    }
     SFH_LAUNCHED(ctx);
     return SFH_OK;
 }

@@ -41,6 +41,7 @@ EXPORTED = [
     "sfh_mlp_param_count", "sfh_mlp_forward",
     "sfh_mlp_loss_grad", "sfh_mlp_train", "sfh_mlp_train_grouped", "sfh_mlp_forward_rows",
     "sfh_gemm_f32", "sfh_emu_prepare", "sfh_emu_reconstruct", "sfh_emu_reconstruct_rows",
+    "sfh_emu_reconstruct_groups",
     "sfh_poisson_deviance",
 ]
 
@@ -198,6 +199,8 @@ def load(path: str | None = None):
                                      C.c_int),
             "sfh_emu_reconstruct_rows": ([_vp, _vp, _vp, _i64, _vp, _vp, C.c_int, _i64, _i64,
                                           C.c_int, _vp], C.c_int),
+            "sfh_emu_reconstruct_groups": ([_vp, _vp, _vp, _vp, _i64, _i64, _vp, _vp, C.c_int,
+                                            _i64, _i64, C.c_int, _vp], C.c_int),
             "sfh_gemm_f32": ([_vp, _vp, _vp, _vp, _i64, _i64, _i64, C.c_int, C.c_int, C.c_int,
                               C.c_float, C.c_int], C.c_int),
             "sfh_emu_prepare": ([_vp, _vp, _i64, _i64, C.c_int, _vp], C.c_int),

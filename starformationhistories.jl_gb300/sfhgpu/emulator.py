@@ -79,6 +79,22 @@ class SyntheticGenerator:
         return out
 
 
+def group_segments(group, max_rows=16):
+    """(rows, seg) for sfh_emu_reconstruct_groups: row indices stably sorted by group, and
+    one (group, start, count) triple per run of at most max_rows rows of one group."""
+    group = np.asarray(group, dtype=np.int64).reshape(-1)
+    rows = np.argsort(group, kind="stable").astype(np.int32)
+    g = group[rows]
+    n = g.size
+    idx = np.arange(n)
+    first = np.ones(n, dtype=bool)
+    first[1:] = g[1:] != g[:-1]
+    run0 = np.maximum.accumulate(np.where(first, idx, 0))   # start of each row's group run
+    starts = np.nonzero(first | ((idx - run0) % max_rows == 0))[0]
+    counts = np.diff(np.append(starts, n))
+    return rows, np.stack([g[starts], starts, counts], 1).astype(np.int32).reshape(-1, 3)
+
+
 @dataclass
 class EmulatorReport:
     n_train: int
@@ -99,13 +115,17 @@ class TemplateEmulator:
 
     def __init__(self, nbins, ncomp=64, hidden=(256, 256),
                  bounds=((6.6, 10.1), (-2.5, 0.3), (24.0, 30.0)), mode=MODE_SQRT,
-                 tol=1e-3, cells=(12, 12, 12), basis_cells=None, ctx=None):
+                 tol=1e-3, cells=(12, 12, 12), basis_cells=None, trust_cells=None, ctx=None):
         """basis_cells=None: one global PCA basis and one MLP.  basis_cells=(na, nm, nd):
         one basis and one MLP per cell of that grid over theta (local form); the trust
-        map then uses the same cells."""
+        map then uses the same cells unless trust_cells gives a grid of its own (a finer
+        one confines each failing validation template to a smaller cell; every cell needs
+        validation templates of its own, so n_val grows with it)."""
         self.ctx = ctx or default_context()
         self.basis_cells = tuple(int(c) for c in basis_cells) if basis_cells else None
-        if self.basis_cells:
+        if trust_cells:
+            cells = trust_cells
+        elif self.basis_cells:
             cells = self.basis_cells
         self.ngroups = int(np.prod(self.basis_cells)) if self.basis_cells else 1
         self.nbins = int(nbins)
@@ -406,14 +426,19 @@ class TemplateEmulator:
             out = torch.empty((B, self.nbins), dtype=torch.float32, device=self._dev)
         L = load()
         if self.basis_cells:
-            grp = torch.as_tensor(self.group_of(theta).astype(np.int32), device=self._dev)
+            # rows sorted by cell, in segments of at most 16: each cell's basis is read once
+            # per segment rather than once per row
+            rows, seg = group_segments(self.group_of(theta))
+            d_rows = torch.as_tensor(rows, device=self._dev)
+            d_seg = torch.as_tensor(seg, device=self._dev)
             self._sync_torch()
-            for s0 in range(0, B, 65535):
-                e = min(B, s0 + 65535)
-                check(L.sfh_emu_reconstruct_rows(
-                    self.ctx.handle, coef[s0:e].data_ptr(), grp[s0:e].data_ptr(), self.ngroups,
-                    self.basis.data_ptr(), self.offset.data_ptr(), self.K, self.nbins, e - s0,
-                    self.mode, out[s0:e].data_ptr()), self.ctx.handle, "emu_reconstruct_rows")
+            for s0 in range(0, seg.shape[0], 65535):
+                e = min(seg.shape[0], s0 + 65535)
+                check(L.sfh_emu_reconstruct_groups(
+                    self.ctx.handle, coef.data_ptr(), d_rows.data_ptr(), d_seg[s0:e].data_ptr(),
+                    e - s0, self.ngroups, self.basis.data_ptr(), self.offset.data_ptr(), self.K,
+                    self.nbins, B, self.mode, out.data_ptr()), self.ctx.handle,
+                    "emu_reconstruct_groups")
         else:
             check(L.sfh_emu_reconstruct(self.ctx.handle, coef.data_ptr(), self.basis.data_ptr(),
                                         self.offset.data_ptr(), self.K, self.nbins, B, self.mode,

@@ -89,3 +89,25 @@ def test_emulator_trust_map_routing():
     assert not em.trusted(np.array([[9.5, -2.0, 25.0]]))[0]
     assert np.allclose(em.standardize([[6.6, -2.5, 24.0], [10.1, 0.3, 30.0]]),
                        [[-1, -1, -1], [1, 1, 1]])
+
+
+@pytest.mark.parametrize("n,ngroups,max_rows", [(1, 1, 16), (37, 3, 16), (500, 11, 16),
+                                                 (64, 1, 16), (90, 5, 4)])
+def test_group_segments_cover_every_row_once(n, ngroups, max_rows):
+    """Row segments for the cell-grouped reconstruction: every row in exactly one segment,
+    each segment one group, 1..max_rows rows, rows sorted by group (stable)."""
+    from sfhgpu.emulator import group_segments
+    g = np.random.default_rng(n).integers(0, ngroups, n)
+    rows, seg = group_segments(g, max_rows=max_rows)
+    assert rows.dtype == np.int32 and seg.dtype == np.int32 and seg.shape[1] == 3
+    assert np.array_equal(rows, np.argsort(g, kind="stable"))
+    seen = np.zeros(n, int)
+    for grp, start, count in seg:
+        assert 1 <= count <= max_rows
+        assert np.all(g[rows[start:start + count]] == grp)
+        seen[rows[start:start + count]] += 1
+    assert np.all(seen == 1)
+    # segments are as long as they may be: one short segment per group at most
+    for grp in np.unique(g):
+        c = seg[seg[:, 0] == grp, 2]
+        assert np.sum(c < max_rows) <= 1 and c.sum() == np.sum(g == grp)

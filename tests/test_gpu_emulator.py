@@ -369,6 +369,54 @@ def test_reconstruct_rows_matches_numpy(torch, L, ctx):
         assert np.allclose(out.cpu().numpy(), ref, rtol=2e-5, atol=1e-6)
 
 
+@pytest.mark.parametrize("K,nb", [(5, 777), (64, 1024), (130, 2048)])
+def test_reconstruct_groups_matches_rows(torch, L, ctx, K, nb):
+    """The segment kernel (one basis read per cell segment; float4 rows when nbins % 4 == 0,
+    scalar otherwise; 4-, 8- and 16-row accumulators) gives the per-row kernel's bits."""
+    from sfhgpu.emulator import group_segments
+    rng = np.random.default_rng(K)
+    G = 6
+    grp = np.concatenate([np.full(n, g) for g, n in enumerate([1, 3, 7, 16, 21, 40])])
+    grp = rng.permutation(grp).astype(np.int32)
+    B = grp.size
+    coef = rng.standard_normal((B, K)).astype(np.float32)
+    basis = (rng.standard_normal((G, K, nb)) * 0.1).astype(np.float32)
+    off = (rng.standard_normal((G, nb)) * 0.3).astype(np.float32)
+    d = [_dev(torch, a) for a in (coef, basis, off)]
+    dg = _dev(torch, grp, np.int32)
+    rows, seg = group_segments(grp)
+    assert seg[:, 2].max() == 16 and seg[:, 2].min() == 1
+    dr, ds = _dev(torch, rows, np.int32), _dev(torch, seg, np.int32)
+    ref = torch.empty((B, nb), dtype=torch.float32, device="cuda:0")
+    out = torch.full((B, nb), -1.0, dtype=torch.float32, device="cuda:0")
+    torch.cuda.synchronize()
+    for mode in (0, 1):
+        assert L.sfh_emu_reconstruct_rows(ctx.handle, d[0].data_ptr(), dg.data_ptr(), G,
+                                          d[1].data_ptr(), d[2].data_ptr(), K, nb, B, mode,
+                                          ref.data_ptr()) == 0
+        assert L.sfh_emu_reconstruct_groups(ctx.handle, d[0].data_ptr(), dr.data_ptr(),
+                                            ds.data_ptr(), seg.shape[0], G, d[1].data_ptr(),
+                                            d[2].data_ptr(), K, nb, B, mode,
+                                            out.data_ptr()) == 0
+        _sync(L, ctx)
+        assert torch.equal(out, ref)
+    # a segment naming a group out of range writes NaN to its rows and nothing else
+    bad = seg.copy()
+    bad[0, 0] = G
+    ds = _dev(torch, bad, np.int32)
+    out.fill_(-1.0)
+    torch.cuda.synchronize()
+    assert L.sfh_emu_reconstruct_groups(ctx.handle, d[0].data_ptr(), dr.data_ptr(),
+                                        ds.data_ptr(), bad.shape[0], G, d[1].data_ptr(),
+                                        d[2].data_ptr(), K, nb, B, 1, out.data_ptr()) == 0
+    _sync(L, ctx)
+    nanrows = rows[bad[0, 1]:bad[0, 1] + bad[0, 2]]
+    assert bool(torch.isnan(out[torch.as_tensor(nanrows, device="cuda:0")]).all())
+    keep = np.setdiff1d(np.arange(B), nanrows)
+    assert torch.equal(out[torch.as_tensor(keep, device="cuda:0")],
+                       ref[torch.as_tensor(keep, device="cuda:0")])
+
+
 @pytest.fixture(scope="module")
 def trained_local(torch, sfh, ctx):
     from sfhgpu import emulator as E
@@ -397,6 +445,58 @@ def test_local_bases_beat_the_global_basis(trained, trained_local, torch):
     y = em_l.offset[grp].clamp_min(0)
     d_mean = em_l.score(exact, (y * y).contiguous())
     assert np.median(d_l) < 0.2 * np.median(d_mean)
+
+
+@pytest.fixture(scope="module")
+def trained_fixed(torch, sfh, ctx):
+    """An emulator for one distance (modulus 27 +- 0.05), the way a fit of one galaxy uses
+    it: per-cell bases over (log age, [M/H]) only."""
+    from sfhgpu import emulator as E
+    xe, ye = np.linspace(-0.6, 2.4, 41), np.linspace(19.0, 30.0, 51)
+    gen = E.SyntheticGenerator(xe, ye, n_iso=200)
+    em = E.TemplateEmulator(gen.nbins, ncomp=64, hidden=(256, 256), tol=1e-2,
+                            bounds=((6.6, 10.1), (-2.5, 0.3), (26.95, 27.05)),
+                            basis_cells=(4, 2, 1), trust_cells=(8, 4, 1), ctx=ctx)
+    rep = em.fit(gen, n_train=8192, n_val=2048, steps=3000, lr=1e-3, seed=5, batch_per_cell=64)
+    return em, gen, rep
+
+
+def test_routed_templates_fit_like_exact_templates(trained_fixed, torch, sfh):
+    """The gain against the exact-template path at the tolerance: a fit on routed templates
+    (emulated where the trust map allows, exact elsewhere) builds fewer exact templates, and
+    its optimum, scored on the exact templates, is within tol x stars of the exact-template
+    fit's optimum (the Poisson deviance of the composite of templates that each sit within
+    tol per star of the exact ones is at most tol per star, by joint convexity)."""
+    from sfhgpu.fitting import fit_templates_fast
+    em, gen, _ = trained_fixed
+    assert em.cells == (8, 4, 1) and em.trust.size == 32   # the trust map's own grid
+    rng = np.random.default_rng(41)
+    th = em.sample_theta(4096, rng)
+    tr = em.trusted(th)
+    assert tr.any(), "no trusted cell at tol 1e-2"
+    th = np.concatenate([th[tr][:24], th[~tr][:24]])
+    B = th.shape[0]
+    exact = gen(th)
+    routed, used = em.templates(th, gen)
+    torch.cuda.synchronize()
+    assert used.any() and (~used).sum() < B      # exact templates built: fewer than requested
+    X = exact.double().cpu().numpy().T            # (nbins, B)
+    Xr = routed.cpu().numpy().T.astype(np.float64)
+    c = np.exp(rng.standard_normal(B))
+    c *= 1e5 / (X @ c).sum()
+    data = rng.poisson(X @ c).astype(np.float64)
+    nstars = data.sum()
+
+    def nll(M, x):
+        m = np.maximum(M @ x, 1e-300)
+        pos = data > 0
+        return float(np.sum(m - data) + np.sum(data[pos] * np.log(data[pos] / m[pos])))
+
+    c_x, _ = fit_templates_fast(sfh.Models(np.asfortranarray(X)), data, g_abstol=1e-6)
+    c_r, _ = fit_templates_fast(sfh.Models(np.asfortranarray(Xr)), data, g_abstol=1e-6)
+    gap = nll(X, c_r) - nll(X, c_x)
+    assert -1e-6 * nstars <= gap <= em.tol * nstars
+    assert abs(c_r.sum() / c_x.sum() - 1.0) < 0.05
 
 
 def test_local_routing_falls_back_to_exact_templates(trained_local, torch):
