@@ -351,6 +351,9 @@ __device__ __forceinline__ void recon_segment(const float *__restrict__ sc, int 
 #pragma unroll
         for (int v = 0; v < V; ++v) acc[r][v] = 0.f;
     if (V == 4) {
+        // four basis rows in flight per thread: one 16-byte load at a time leaves the
+        // kernel latency-bound at the two blocks per SM its registers allow
+#pragma unroll 4
         for (int k = 0; k < K; ++k) {
             const float4 b = __ldg(reinterpret_cast<const float4 *>(vb + (int64_t)k * nbins + i0));
 #pragma unroll
