@@ -361,8 +361,9 @@ typedef struct {
 /* Batched HMC over all chains at once, every leapfrog step one sfh_fg_batched_dev-style
    evaluation on the tensor cores; replaces the per-chain DynamicHMC loop of hmc_sample
    (hmc_sample.jl:105-141) and sample_sfh (generic_fitting.jl:458-527).  Fixed-length
-   trajectories, per-chain dual-averaging step size and a pooled diagonal mass during
-   warmup, Metropolis accept.  Device arrays: d_theta0 (nchains x D) starting points in
+   trajectories, per-chain dual-averaging step size and a diagonal mass during warmup
+   (pooled over chains with 16 or more; with fewer, each chain's own variance over the
+   second quarter of warmup), Metropolis accept.  Device arrays: d_theta0 (nchains x D) starting points in
    the transformed space (D = ntempl for SFH_HMC_DIRECT; nages + free parameters, order
    [log R_j..., log α, β, log σ], for SFH_HMC_MZR).  Outputs (each may be NULL):
    d_mean / d_var (nchains x D) posterior mean and variance of the natural parameters

@@ -30,6 +30,9 @@
 namespace {
 
 constexpr int kT = 256;
+// fewer chains than this adapt the diagonal metric from their own warmup windows rather
+// than from the spread of positions across chains
+constexpr int kPoolMin = 16;
 
 using sfh_rng::philox;
 using sfh_rng::u01;
@@ -174,6 +177,17 @@ __global__ void k_accept(ChainState s, HmcConst c) {
             s.theta[k] = s.theta0[k];
             s.g[k] = s.g0[k];
         }
+        if (ts < 0 && c.B < kPoolMin && c.nwarm >= 20 && t >= c.nwarm / 4 &&
+            t < c.nwarm / 2) {
+            // too few chains to pool over: each chain's own window of warmup positions
+            // (the second quarter of warmup) gives its variance; the sums are cleared when
+            // the metric is set
+            const double x = s.theta[k];
+            const double n1 = (double)(t - c.nwarm / 4 + 1);
+            const double delta = x - s.mean[k];
+            s.mean[k] += delta / n1;
+            s.m2[k] += delta * (x - s.mean[k]);
+        }
         if (ts >= 0) {
             const double x = nat_param(c, s.theta + (int64_t)b * c.D, d);
             const double n1 = (double)(ts + 1);
@@ -186,15 +200,27 @@ __global__ void k_accept(ChainState s, HmcConst c) {
     }
 }
 
-// At half of warmup: inverse mass = variance of θ pooled over chains; restart dual
-// averaging around the current step sizes.
+// At half of warmup: inverse mass = variance of θ pooled over chains (at least kPoolMin of
+// them), else the chains' own variances over the second quarter of warmup (DynamicHMC
+// adapts each chain from its own draws); restart dual averaging around the current steps.
 __global__ void k_adapt_mass(ChainState s, HmcConst c) {
     const int64_t t = *s.t;
-    // the pooled variance needs chains to pool over: with fewer than 16 the starting
-    // metric (ones, or cfg->d_minv0) is kept and only the step adapts
-    if (c.nwarm < 20 || t != c.nwarm / 2 || c.B < 16) return;
+    if (c.nwarm < 20 || t != c.nwarm / 2) return;
     const int d = blockIdx.x * blockDim.x + threadIdx.x;
-    if (d < c.D) {
+    if (d < c.D && c.B < kPoolMin) {
+        // the chains' own window variances (second quarter of warmup), averaged over the
+        // chains and regularised by the window length; then the sums are cleared for the
+        // sampling statistics
+        const double nw = (double)(c.nwarm / 2 - c.nwarm / 4);
+        double v = 0.0;
+        for (int b = 0; b < c.B; ++b) {
+            const int64_t k = (int64_t)b * c.D + d;
+            v += nw > 1.0 ? s.m2[k] / (nw - 1.0) : 1.0;
+            s.mean[k] = 0.0;
+            s.m2[k] = 0.0;
+        }
+        s.minv[d] = (nw / (nw + 5.0)) * (v / c.B) + 1e-3 * (5.0 / (nw + 5.0));
+    } else if (d < c.D) {
         double m = 0.0, q = 0.0;
         for (int b = 0; b < c.B; ++b) {
             const double x = s.theta[(int64_t)b * c.D + d];
