@@ -2,6 +2,7 @@
 // entry points of the C ABI (include/sfhgpu.h).
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <cmath>
@@ -38,6 +39,45 @@ extern "C" const char *sfh_status_string(int status) {
 }
 
 // ------------------------------------------------------------------ context
+// The completion word (sfh_ctx::h_done): best effort, the context works without it.
+static void sfh_done_init(sfh_ctx *ctx) {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuStreamWriteValue32", &fn, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+        return;
+    void *h = nullptr, *d = nullptr;
+    if (cudaHostAlloc(&h, 64, cudaHostAllocMapped) != cudaSuccess) return;
+    if (cudaHostGetDevicePointer(&d, h, 0) != cudaSuccess || !d) {
+        cudaFreeHost(h);
+        return;
+    }
+    *(volatile unsigned int *)h = 0u;
+    ctx->h_done = (volatile unsigned int *)h;
+    ctx->d_done = d;
+    ctx->write_value32 = fn;
+}
+
+cudaError_t sfh_host_call_wait(sfh_ctx *ctx) {
+    typedef CUresult (*WriteValue32)(CUstream, CUdeviceptr, cuuint32_t, unsigned int);
+    if (!ctx->write_value32) return cudaStreamSynchronize(ctx->stream);
+    const unsigned int seq = ++ctx->done_seq;
+    if (((WriteValue32)ctx->write_value32)((CUstream)ctx->stream, (CUdeviceptr)ctx->d_done, seq,
+                                           0u) != CUDA_SUCCESS) {
+        ctx->write_value32 = nullptr;  // not available here: synchronise from now on
+        return cudaStreamSynchronize(ctx->stream);
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    for (unsigned int it = 1;; ++it) {
+        if (__atomic_load_n((const unsigned int *)ctx->h_done, __ATOMIC_ACQUIRE) == seq)
+            return cudaSuccess;
+        if ((it & 255u) == 0u &&
+            std::chrono::steady_clock::now() - t0 > std::chrono::microseconds(2000))
+            return cudaStreamSynchronize(ctx->stream);
+    }
+}
+
 extern "C" int sfh_ctx_create(int device, sfh_ctx **out) {
     if (!out) return SFH_ERR_ARG;
     *out = nullptr;
@@ -72,6 +112,7 @@ extern "C" int sfh_ctx_create(int device, sfh_ctx **out) {
         delete ctx;
         return SFH_ERR_CUDA;
     }
+    sfh_done_init(ctx);
     *out = ctx;
     return SFH_OK;
 }
@@ -83,6 +124,7 @@ extern "C" int sfh_ctx_destroy(sfh_ctx *ctx) {
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->stage) cudaFree(ctx->stage);
     if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+    if (ctx->h_done) cudaFreeHost((void *)ctx->h_done);
     if (ctx->d_counters) cudaFree(ctx->d_counters);
     if (ctx->d_df_tab) cudaFree(ctx->d_df_tab);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -623,7 +665,7 @@ extern "C" int sfh_fg(sfh_ctx *ctx, const sfh_models *m, int dtype, const void *
         a.mode = FG_MODE_FG;
         a.occ_key = m;  // one plan slot for the host-array calls on this handle
         if ((rc = sfh_launch_fg(ctx, m, a))) return rc;
-        SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+        SFH_CK(ctx, sfh_host_call_wait(ctx));
         if (negLogL) {
             const double v = *(volatile double *)hl;
             if (std::isnan(v) && (rc = sfh_check_onepass(ctx))) return rc;
@@ -659,7 +701,7 @@ extern "C" int sfh_fg(sfh_ctx *ctx, const sfh_models *m, int dtype, const void *
     a.mode = FG_MODE_FG;
     a.occ_key = m;
     if ((rc = sfh_launch_fg(ctx, m, a))) return rc;
-    SFH_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    SFH_CK(ctx, sfh_host_call_wait(ctx));
     if (negLogL) {
         double v;
         memcpy(&v, hb + o_l, 8);

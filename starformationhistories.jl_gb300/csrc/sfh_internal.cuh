@@ -47,7 +47,20 @@ struct sfh_ctx {
     // dependent launch); sfh_ctx_set_overlap turns it off.
     bool pdl = true;
     int host_access = SFH_HOST_ACCESS_AUTO;  // sfh_ctx_set_host_access
+    // Completion word of the host-array calls (sfh_host_call_wait): after a call's kernels
+    // the stream writes a sequence number into mapped pinned memory with a stream memory
+    // operation, which fences the kernels' writes first, and the host polls the word
+    // instead of synchronising the stream.  write_value32 NULL: plain synchronisation.
+    volatile unsigned int *h_done = nullptr;
+    void *d_done = nullptr;
+    unsigned int done_seq = 0;
+    void *write_value32 = nullptr;  // cuStreamWriteValue32 (driver entry point)
 };
+
+// Waits for the work queued on ctx->stream by a host-array call (see sfh_ctx::h_done):
+// polls the completion word for up to 2 ms, then falls back to cudaStreamSynchronize,
+// which also reports any error the stream met.
+cudaError_t sfh_host_call_wait(sfh_ctx *ctx);
 
 // Occupied-bin plan of the single-vector fg! (onepass.cu).  With G requested, fg! needs the
 // composite only where n_i > 0: an empty bin (n_i <= 0) has w_i = 1 - 0/max(c_i, eps) = 1

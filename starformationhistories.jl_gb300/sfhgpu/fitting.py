@@ -138,10 +138,37 @@ def grad_loglikelihood(*args):
     return T.type(G[0])
 
 
+_F64 = np.dtype(np.float64)
+
+
+def _addr(a):
+    """Data address of an ndarray (the buffer protocol for writable arrays, a fraction of
+    the cost of `.ctypes.data`)."""
+    try:
+        return C.addressof(C.c_char.from_buffer(a))
+    except (TypeError, ValueError, BufferError):
+        return a.ctypes.data
+
+
+def _flat64(a, n, writable=False):
+    """True when `a` is a float64 ndarray of n elements laid out flat (column-major)."""
+    return (type(a) is np.ndarray and a.dtype == _F64 and a.size == n and a.flags.f_contiguous
+            and (not writable or a.flags.writeable))
+
+
 def fg_(F, G, coeffs, models, data, composite):
     """fg!(F, G, coeffs, models, data, composite), src/fitting/solvers.jl:20-38.
     Returns -logL when F is not None; fills G with -∇logL when G is not None."""
-    M = as_models(models)
+    M = models if isinstance(models, Models) else as_models(models)
+    if (_flat64(coeffs, M.nt) and _flat64(data, M.nbins) and _flat64(composite, M.nbins, True)
+            and (G is None or _flat64(G, M.nt, True))):
+        # Float64 arrays already in the flat layout: straight to the C call
+        out = C.c_double()
+        ctx = M.ctx
+        check(load().sfh_fg(ctx.handle, M.handle, SFH_F64, _addr(coeffs), _addr(data),
+                            _addr(composite), _addr(G) if G is not None else None,
+                            C.byref(out) if F is not None else None), ctx.handle, "fg!")
+        return _F64.type(out.value) if F is not None else None
     _argcheck(np.size(coeffs) == M.nt, "axes(coeffs,1) == axes(models,2)")
     _argcheck(M.nbins == np.size(data) == np.size(composite),
               "axes(models,1) == axes(data,1) == axes(composite,1)")

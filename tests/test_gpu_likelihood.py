@@ -153,6 +153,34 @@ def test_fg_host_access_modes_are_bit_identical(sfh, O, storage):
     assert abs(v1 - v_ref) <= 1e-6 * data.sum() / 1e4
 
 
+def test_fg_array_layouts_and_repeated_calls_agree(sfh):
+    """fg! on float64 flat arrays (the direct C call), on a C-ordered Hess matrix and a
+    float32 composite (converted copies), and 300 calls in a row (each waiting on the
+    context's completion word) all give the same bits."""
+    M, r, data = _problem(20000, 200, seed=12, n_stars=1e6)
+    H = sfh.Models(M, storage="f32")
+    nb, nt = M.shape
+    comp, G = np.empty(nb), np.empty(nt)
+    v = sfh.fg_(True, G, r, H, data, comp)
+    # the same diagram as a (100, 200) matrix: Fortran order is the flat layout, C order
+    # is converted
+    dF = np.asfortranarray(data.reshape(100, 200, order="F"))
+    dC = np.ascontiguousarray(dF)
+    for d in (dF, dC):
+        c2, G2 = np.empty(nb), np.empty(nt)
+        assert sfh.fg_(True, G2, r, H, d, c2) == v
+        assert np.array_equal(G2, G) and np.array_equal(c2, comp)
+    c32 = np.empty(nb, dtype=np.float32)
+    G32 = np.empty(nt, dtype=np.float32)
+    v32 = sfh.fg_(True, G32, r.astype(np.float32), H, data.astype(np.float32), c32)
+    assert np.isfinite(v32) and abs(v32 - v) <= 1e-3 * abs(v)
+    c3, G3 = np.empty(nb), np.empty(nt)
+    for _ in range(300):
+        assert sfh.fg_(True, G3, r, H, data, c3) == v
+    assert np.array_equal(G3, G) and np.array_equal(c3, comp)
+    assert sfh.fg_(None, G3, r, H, data, c3) is None and np.array_equal(G3, G)
+
+
 def test_shape_errors_raise_argument_error(sfh):
     M = np.random.default_rng(0).random((10, 3))
     with pytest.raises(ValueError):
