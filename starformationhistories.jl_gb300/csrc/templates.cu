@@ -525,9 +525,21 @@ int sfh_launch_stamps(sfh_ctx *ctx, const double *d_x, const double *d_y, const 
                       double xs, int64_t nx, double yf, double ys, int64_t ny, float *d_out) {
     if (nx < 1 || ny < 1 || nx > (1 << 20) || ny > (1 << 20) || ntempl < 1 || ntempl > 65535)
         return sfh_set_error(ctx, SFH_ERR_ARG, "stamp grid or template count out of range");
-    const int TY = band_rows(nx, ny);
+    int TY = band_rows(nx, ny);
     if (TY < 1)
         return sfh_set_error(ctx, SFH_ERR_UNSUPPORTED, "Hess grid too wide for a shared-memory band");
+    {
+        // few templates: shorter bands, so that the grid holds about four CTAs per SM
+        // (each band scans its template's stars and skips those that miss it, so the
+        // extra bands cost little next to an idle SM)
+        const int64_t want = 4 * (int64_t)ctx->sm_count;
+        const int64_t have = ntempl * ((ny + TY - 1) / TY);
+        if (have < want) {
+            const int64_t tiles = std::min<int64_t>((want + ntempl - 1) / ntempl,
+                                                    std::max<int64_t>(1, ny / 8));
+            TY = (int)std::min<int64_t>(TY, (ny + tiles - 1) / tiles);
+        }
+    }
     Grid2 g{xf, xs, yf, ys, (int)nx, (int)ny};
     const int ntiles = (int)((ny + TY - 1) / TY);
     const size_t smem = stamp_smem(nx, TY);
