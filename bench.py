@@ -318,6 +318,14 @@ def run_hmc_matched(ctx, d_T, w, nchains=1024, nwarmup=200, ndraw=10, nref=200,
     bat, t_bat = run(nchains, ndraw, seed + 2)
     one, t_one = run(1, nchains * ndraw, seed + 3)
     nuts, t_nuts = run(nchains, 50, seed + 4, sampler="nuts", nw=50, max_depth=8)
+    # the same with the Laplace covariance at the MLE as the dense metric (curvature of
+    # log p by central differences of one batched gradient evaluation)
+    t0 = time.perf_counter()
+    cov = sfhgpu.laplace_metric(Hb, data, fit.mle.theta, mzr=fit.mle.MH_model,
+                                disp=fit.mle.disp_model, logAge=la, MH=mh)
+    t_lap = time.perf_counter() - t0
+    nuts_l, t_nuts_l = run(nchains, 50, seed + 4, sampler="nuts", nw=50, max_depth=8,
+                           minv_dense=cov)
     Hb.free()
     err = lambda mu: float(np.sqrt(np.mean(((mu - mref) / sdref) ** 2)))
     e_b, e_1 = err(bat["mean"].mean(0)), err(one["mean"][0])
@@ -344,6 +352,16 @@ def run_hmc_matched(ctx, d_T, w, nchains=1024, nwarmup=200, ndraw=10, nref=200,
                  "divergent": int(nuts["divergent"].sum()),
                  "metric": "dense: the MAP inverse Hessian, from the MLE point (the "
                            "reference's sample_sfh); the step adapted over the warmup trees"},
+        "nuts_laplace_metric": {
+            "chains": nchains, "warmup_trees": 50, "draws_per_chain": 50, "max_depth": 8,
+            "metric_seconds": t_lap, "seconds": t_nuts_l,
+            "trees_per_s": nchains * 100 / t_nuts_l,
+            "mean_depth": float(nuts_l["depth"].mean()),
+            "accept": float(nuts_l["accept"].mean()),
+            "divergent": int(nuts_l["divergent"].sum()),
+            "error_vs_reference": err(nuts_l["mean"].mean(0)),
+            "metric": "dense: the Laplace covariance at the MLE (laplace_metric), from the "
+                      "MLE point; the step adapted over the warmup trees"},
     }
 
 

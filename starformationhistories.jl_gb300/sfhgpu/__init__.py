@@ -14,7 +14,7 @@ from .fitting import (Galaxies, composite_, construct_x0, construct_x0_mdf, fg_,
                       grad_loglikelihood_, loglikelihood, renormalize_x0, stack_models)
 from .sampling import (BFGSResult, CompositeBFGSResult, GaussianDispersion, LinearAMR,
                        LogarithmicAMR, MH_from_Z, PowerLawMZR, calculate_coeffs, dMH_dZ, fit_sfh,
-                       fit_sfh_x0, hmc_sample, logdensity_batched, sample_sfh)
+                       fit_sfh_x0, hmc_sample, laplace_metric, logdensity_batched, sample_sfh)
 from .templates import (BrokenPowerLawIMF, Histogram, Kroupa2001, Martin2016_complete,
                         bin_cmd_smooth, calculate_edges, calculate_weights, compl_model, err_model,
                         exp_photerr, histogram_data, histogram_pix, interpolate_mini, midpoints,
@@ -36,7 +36,7 @@ __all__ = [
     "histogram_pix", "interpolate_mini", "midpoints", "mini_spacing", "partial_cmd_smooth",
     "partial_cmd_smooth_batch", "NoBinaries", "RandomBinaryPairs", "trapz", "binary_points",
     "binary_hess_batch", "partial_cmd_smooth_binary_batch", "GaussianDispersion", "PowerLawMZR", "calculate_coeffs",
-    "hmc_sample", "logdensity_batched", "sample_sfh", "Galaxies", "fg_ragged",
+    "hmc_sample", "laplace_metric", "logdensity_batched", "sample_sfh", "Galaxies", "fg_ragged",
     "partial_cmd_smooth_ragged", "SyntheticGenerator", "TemplateEmulator", "LinearAMR",
     "construct_x0_mdf", "fixed_amr", "truncate_relweights", "LogarithmicAMR", "MH_from_Z",
     "dMH_dZ", "fit_sfh", "fit_sfh_x0", "BFGSResult", "CompositeBFGSResult",

@@ -231,6 +231,41 @@ def logdensity_batched(models: Models, data, theta, model=SFH_HMC_DIRECT, mzr=No
     return logd.cpu().numpy(), grad.cpu().numpy()
 
 
+def model_kind(mzr):
+    """The sampler's model code for a metallicity model (None: the direct coefficients)."""
+    if mzr is None:
+        return SFH_HMC_DIRECT
+    return (SFH_HMC_LINEAR_AMR if isinstance(mzr, LinearAMR) else
+            SFH_HMC_LOG_AMR if isinstance(mzr, LogarithmicAMR) else SFH_HMC_MZR)
+
+
+def laplace_metric(models: Models, data, theta, mzr=None, disp=None, logAge=None, MH=None,
+                   step=1e-2, floor=1e-10):
+    """Dense inverse metric for the No-U-Turn sampler from the curvature of log p at theta
+    (the Laplace covariance), in the sampler's transformed space: H = -d²log p / dθ² by
+    central differences of the batched gradient (2D rows in one evaluation, step `step`
+    per coordinate), symmetrised.  Eigenvalues enter by magnitude and no smaller than
+    floor x the largest, so the result is positive definite away from the mode as well.
+    No reference counterpart: the reference's sample_sfh takes the BFGS inverse Hessian."""
+    th = np.asarray(theta, float).reshape(-1)
+    D = th.size
+    h = np.broadcast_to(np.asarray(step, float), (D,)).copy()
+    if np.any(~(h > 0)):
+        raise ValueError("step must be positive")
+    rows = np.repeat(th[None, :], 2 * D, axis=0)
+    k = np.arange(D)
+    rows[k, k] += h
+    rows[D + k, k] -= h
+    _, g = logdensity_batched(models, data, rows, model=model_kind(mzr), mzr=mzr, disp=disp,
+                              logAge=logAge, MH=MH)
+    H = -(g[:D] - g[D:]) / (2.0 * h[:, None])
+    H = 0.5 * (H + H.T)
+    w, V = np.linalg.eigh(H)
+    w = np.abs(w)
+    w = np.maximum(w, floor * max(float(w.max()), 1e-300))
+    return (V / w) @ V.T
+
+
 def _run_hmc(models, data, theta0, cfg, keep, keep_draws, sampler="hmc", max_depth=10,
              minv_dense=None):
     import torch
@@ -336,8 +371,7 @@ def sample_sfh(models: Models, data, logAge, MH, mzr=None, disp: GaussianDispers
     else:
         th = mzr_theta(mstars0, mzr, disp)
         theta0 = th[None, :] + jitter * rng.standard_normal((nchains, th.size))
-    kind = (SFH_HMC_LINEAR_AMR if isinstance(mzr, LinearAMR) else
-            SFH_HMC_LOG_AMR if isinstance(mzr, LogarithmicAMR) else SFH_HMC_MZR)
+    kind = model_kind(mzr)
     cfg, keep = _config(nchains, kind, nsteps, nwarmup, nleap, thin, step0,
                         target_accept, seed, mzr=mzr, disp=disp, logAge=logAge, MH=MH)
     if minv0 is not None:

@@ -319,3 +319,31 @@ def test_nuts_dense_metric_on_the_laplace_covariance(sfh):
     assert np.all(np.abs(pm - mle) < 0.25 * sd_lap + 3 * np.sqrt(pv / (64 * 100))), (pm, mle)
     ratio = np.sqrt(pv) / sd_lap
     assert np.all((ratio > 0.8) & (ratio < 1.25)), ratio
+
+
+def test_laplace_metric_matches_the_exact_covariance(sfh):
+    """laplace_metric (central differences of the batched gradient in θ = log x) gives the
+    Laplace covariance of the direct model at its MLE, whose exact form is known."""
+    rng = np.random.default_rng(22)
+    nbins, nt = 4000, 5
+    M32 = np.asfortranarray((rng.random((nbins, nt)) ** 3).astype(np.float32))
+    x_true = np.array([2000.0, 1000.0, 3000.0, 500.0, 1500.0]) / 100
+    data = rng.poisson(M32.astype(np.float64) @ x_true).astype(np.float64)
+    Ms = np.asfortranarray(_bf16_hilo(M32))
+    _, mle = sfh.fit_templates_lbfgsb(sfh.Models(Ms, storage="f64"), data, x0=x_true,
+                                      factr=10.0, pgtol=1e-10)
+    m = Ms @ mle
+    Hobs = (Ms * (data / m ** 2)[:, None]).T @ Ms
+    cov_th = np.linalg.inv(Hobs) / np.outer(mle, mle)
+    H = sfh.Models(M32, storage="bf16x2")
+    cov = sfh.laplace_metric(H, data, np.log(mle))
+    assert np.allclose(cov, cov.T)
+    assert np.all(np.linalg.eigvalsh(cov) > 0)
+    sd, sd_ref = np.sqrt(np.diag(cov)), np.sqrt(np.diag(cov_th))
+    assert np.all(np.abs(sd / sd_ref - 1) < 0.02), sd / sd_ref
+    corr = cov / np.outer(sd, sd)
+    corr_ref = cov_th / np.outer(sd_ref, sd_ref)
+    assert np.max(np.abs(corr - corr_ref)) < 0.02
+    with pytest.raises(ValueError):
+        sfh.laplace_metric(H, data, np.log(mle), step=0.0)
+
