@@ -637,9 +637,10 @@ int sfh_emu_reconstruct_rows(sfh_ctx *ctx, const float *d_coef, const int32_t *d
 /* As sfh_emu_reconstruct_rows, one group's rows at a time: segment s (d_seg[3s..3s+2] =
    group, start, count; 1 <= count <= 16) builds rows d_rows[start .. start + count) from
    group `group`'s basis, read once for the whole segment.  d_rows holds row indices of d_out
-   (0 <= row < B), normally sorted by group.  nseg <= 65535, K <= 1024.  A segment with an
-   out-of-range group or rows writes NaN to the rows it can address.  Enqueued, not
-   synchronised. */
+   (0 <= row < B), normally sorted by group.  nseg <= 65535, K <= 1024.  A segment whose
+   group, start or count is out of range writes NaN to the rows it can address; a row index
+   outside [0, B) ends its segment there (the segment's later rows are not written).
+   Enqueued, not synchronised. */
 int sfh_emu_reconstruct_groups(sfh_ctx *ctx, const float *d_coef, const int32_t *d_rows,
                                const int32_t *d_seg, int64_t nseg, int64_t ngroups,
                                const float *d_basis, const float *d_offset, int K,

@@ -402,8 +402,9 @@ __device__ __forceinline__ void recon_segment(const float *__restrict__ sc, int 
     }
 }
 
-// seg: nseg x 3 int32 (group, start, count).  A segment whose group is out of range or whose
-// rows fall outside [0, B) writes NaN to the rows it can address and nothing else.
+// seg: nseg x 3 int32 (group, start, count).  A segment whose group, start or count is out
+// of range writes NaN to the rows it can address and nothing else; a row index outside
+// [0, B) ends its segment at that row.
 template <int V>
 __global__ void __launch_bounds__(kRecThreads)
 k_recon_groups(const float *__restrict__ coef, const int32_t *__restrict__ rows,
