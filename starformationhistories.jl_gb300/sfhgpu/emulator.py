@@ -399,6 +399,8 @@ class TemplateEmulator:
         """Scaled PCA coefficients predicted by the MLP(s) (device, B x K)."""
         torch = _torch()
         theta = np.asarray(theta, dtype=np.float64).reshape(-1, 3)
+        if theta.shape[0] == 0:
+            return torch.empty((0, self.K), dtype=torch.float32, device=self._dev)
         X = torch.as_tensor(self.local_inputs(theta).astype(np.float32), device=self._dev)
         B = X.shape[0]
         Yc = torch.empty((B, self.K), dtype=torch.float32, device=self._dev)
@@ -424,6 +426,8 @@ class TemplateEmulator:
         B = coef.shape[0]
         if out is None:
             out = torch.empty((B, self.nbins), dtype=torch.float32, device=self._dev)
+        if B == 0:
+            return out
         L = load()
         if self.basis_cells:
             # rows sorted by cell, in segments of at most 16: each cell's basis is read once

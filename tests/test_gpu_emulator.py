@@ -369,7 +369,7 @@ def test_reconstruct_rows_matches_numpy(torch, L, ctx):
         assert np.allclose(out.cpu().numpy(), ref, rtol=2e-5, atol=1e-6)
 
 
-@pytest.mark.parametrize("K,nb", [(5, 777), (64, 1024), (130, 2048)])
+@pytest.mark.parametrize("K,nb", [(5, 777), (64, 1024), (130, 2048), (1, 3), (1, 4)])
 def test_reconstruct_groups_matches_rows(torch, L, ctx, K, nb):
     """The segment kernel (one basis read per cell segment; float4 rows when nbins % 4 == 0,
     scalar otherwise; 4-, 8- and 16-row accumulators) gives the per-row kernel's bits."""
@@ -459,6 +459,15 @@ def trained_fixed(torch, sfh, ctx):
                             basis_cells=(4, 2, 1), trust_cells=(8, 4, 1), ctx=ctx)
     rep = em.fit(gen, n_train=8192, n_val=2048, steps=3000, lr=1e-3, seed=5, batch_per_cell=64)
     return em, gen, rep
+
+
+def test_no_requests_give_empty_templates(trained_fixed, torch):
+    em, gen, _ = trained_fixed
+    none = np.empty((0, 3))
+    assert tuple(em.coefficients(none).shape) == (0, em.K)
+    assert tuple(em.predict(none).shape) == (0, em.nbins)
+    out, used = em.templates(none, gen)
+    assert tuple(out.shape) == (0, em.nbins) and used.size == 0
 
 
 def test_routed_templates_fit_like_exact_templates(trained_fixed, torch, sfh):
